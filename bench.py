@@ -1,0 +1,356 @@
+"""Benchmark: ms per Q_r field at 1 % RMS error on the 128^3 correlated-k
+channel (synthetic k(band, g, T, x_H2O) table of 64 bands x 16 g x 50 T x 8 x,
+8 band groups), plus rays/s.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+A step is one full solve of one Q_r field with the inputs resident in HBM:
+sampling-table upload, the march kernel, the finalize kernel and the copy of
+Q and sigma into pinned host memory, timed with CUDA events on the solver's
+stream.  The ray budget is the smallest one whose estimated RMS error
+sqrt(mean var(Q)) / rms(Q) is <= 1 % (pilot solve, 1/N scaling, then checked
+on the timed solves).  Inputs (16.8 MB) fit in L2, so L2 is flushed (a
+256 MB device write) before every timed step.  `e2e` repeats the step through
+the public API from host arrays: dnsmc_set_fields (host->device) + solve +
+dnsmc_get_results (device->host), wall clock.
+
+With --gpus N (torchrun), every rank solves its own snapshots (seed = rank):
+cells are independent, no collective is needed; the whole-job value is the
+max-over-ranks time divided by the fields all ranks produced (weak scaling).
+
+--impl reference times the reference's estimator as restated in the oracle
+(one thread per cell, code/mc_gpu.cu:44-438; the reference's CUDA file does
+not build with CUDA 13) on all host cores, FP32 like the reference build, on
+a bounded sample of cells, and extrapolates ms per field at 1 % RMS.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "ms per Q_r field at 1% RMS error: plain vs NN-control-variate MC; rays/s"
+N_CELL = 128
+GROUPS = 8
+BYTES_PER_STEP = 32  # T 4 + x_H2O 4 + k bilinear 4x4 + Ib linear 2x4
+TARGET_ERR = 0.01
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.samples = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thr = threading.Thread(target=self._read, daemon=True)
+            self.thr.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if len(s) > 8 and s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if len(s) > 8 and s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples if len(s) > 8 for i in range(4) if s[5 + i] == "Active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def make_inputs(seed):
+    from dnsmc_gb300 import synth
+    d = synth.ck_channel(N_CELL, seed)
+    return d["T"], d["x"], d["T_wall"]
+
+
+def make_solver(table, T_wall, seed, threads=0):
+    import dnsmc_gb300 as D
+    cfg = D.default_config(model=D.MODEL_TABLE, imax=N_CELL, jmax=N_CELL, kmax=N_CELL, Lx=2.0, Ly=2 * math.pi,
+                           Lz=math.pi, stretched_x=0, T_west=T_wall, T_east=T_wall, n_groups=GROUPS, seed=seed,
+                           block_threads=threads)
+    s = D.Solver(cfg)
+    s.set_table(table["k"], table["wvc"], table["T0"], table["dT"], dnu=table["dnu"], wq=table["wq"],
+                X0=table["X0"], dX=table["dX"])
+    return s
+
+
+def rms_error(Q, S):
+    return float(math.sqrt(float((S ** 2).mean())) / math.sqrt(float((Q ** 2).mean())))
+
+
+def ray_budget(s, pilot=32):
+    s.set_rays(pilot)
+    Q, S = s.solve(timeout_s=600)
+    e = rms_error(Q, S)
+    r = int(math.ceil(pilot * (e / TARGET_ERR) ** 2 * 1.02))
+    r = max(4, min(65536, r))
+    return r, e
+
+
+def flush_l2(buf):
+    if buf is not None:
+        buf.fill_(1.0)
+        import torch
+        torch.cuda.synchronize()
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if args.impl != "reference" else "gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+def barrier_max(pg, value):
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_reference(table, T, x, T_wall, rays_per_cell, sample_cells=96, budget_s=20.0):
+    """Reference estimator (oracle port, FP32 as the reference build) on all
+    host cores over a sample of cells; returns rays/s and ms per field at 1 %."""
+    from oracle import oracle as O
+    from dnsmc_gb300 import synth  # noqa: F401
+    n = N_CELL
+    xbar = float(x.mean())
+    # x-uniform slice of the table in the reference layout (the reference has
+    # no x_H2O axis): k(band, T, g) at xbar, CDFs and Planck mean from it.
+    X = table["X0"] + table["dX"] * np.arange(table["k"].shape[3])
+    kx = np.empty(table["k"].shape[:3], np.float64)
+    for b in range(kx.shape[0]):
+        for g in range(kx.shape[1]):
+            kx[b, g] = [np.interp(xbar, X, table["k"][b, g, t]) for t in range(kx.shape[2])]
+    nT = kx.shape[2]
+    Tnb = (table["T0"] + table["dT"] * np.arange(nT)).astype(np.float32)
+    C1, C2 = 3.741771790075259e-16, 0.014387741858429
+    nu = table["wvc"].astype(np.float64)
+    Ib = C1 * (nu[None, :] * 100) ** 3 / (np.pi * (np.exp(C2 * nu[None, :] * 100 / Tnb[:, None]) - 1))  # [nT][nB]
+    e = kx.transpose(2, 0, 1) * Ib[:, :, None] * table["dnu"][None, :, None] * 100 * table["wq"][None, None, :]
+    eb = e.sum(2)
+    prob = np.cumsum(eb, 1) / eb.sum(1, keepdims=True)
+    probg = np.cumsum(e, 2) / np.maximum(e.sum(2, keepdims=True), 1e-300)
+    kP = np.pi * eb.sum(1) / (5.670373e-08 * Tnb.astype(np.float64) ** 4)
+    tables = dict(Tnb=Tnb, kq=kx.transpose(0, 2, 1).astype(np.float32), wvc=table["wvc"],
+                  prob=prob.astype(np.float32), probg=probg.astype(np.float32), kP=kP.astype(np.float32))
+    Tf = np.zeros((n + 2, n + 2, n + 2), np.float32)
+    Tf[1:-1, 1:-1, 1:-1] = T
+    rng = np.random.default_rng(0)
+    cells = np.stack([rng.integers(1, n + 1, sample_cells) for _ in range(3)], 1)
+    cores = os.cpu_count() or 1
+    photmax = 64
+    kw = dict(imax=n, jmax=n, kmax=n, Lx=2.0, Ly=2 * math.pi, Lz=math.pi, T_west=T_wall, T_east=T_wall, model=0,
+              tables=tables, nvar=2, grid_num=1, stretched=0, use_double=0, seed=5, threads=cores)
+    while True:
+        t0 = time.perf_counter()
+        r = O.ref_mc(Tf.ravel(), cells, photmax=photmax, **kw)
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 4 or photmax >= 1 << 16:
+            break
+        photmax = int(photmax * max(2.0, min(8.0, budget_s / 4 / max(dt, 1e-3))))
+    rays = sample_cells * 2 * photmax
+    rays_s = rays / dt
+    nr = 2 * photmax
+    var_ray = (r["se"] ** 2 * nr)  # per-ray variance of each sampled cell
+    qrms = math.sqrt(float((r["Q"] ** 2).mean()))
+    n_needed = float(var_ray.mean()) / (TARGET_ERR * qrms) ** 2
+    ms_field = n_needed * n ** 3 / rays_s * 1e3
+    return dict(rays_s=rays_s, steps_s=float(r["steps"].sum()) / dt, ms_field=ms_field, rays_per_cell_1pct=n_needed,
+                cores=cores, sample=f"{sample_cells} random cells x {nr} rays of the 128^3 field (x-uniform table "
+                                     f"slice at mean x_H2O), {dt:.1f} s, FP32 oracle port")
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_setup(args)
+    if rank != 0:
+        return 0
+    from dnsmc_gb300 import synth
+    T, x, Tw = make_inputs(0)
+    table = synth.ck_table()
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        info = cpu_reference(table, T, x, Tw, None, budget_s=max(4.0, 60.0 / (args.warmup + args.steps)))
+        if i >= args.warmup:
+            vals.append(info["ms_field"])
+    v = float(np.mean(vals))
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic",
+           "config": {"workload": "ck channel 128^3, 64 bands x 16 g x 50 T x 8 x_H2O, extrapolated from a sample",
+                      "parallelism": "host threads"},
+           "cpu_baseline": {"value": v, "unit": "ms", "cores": info["cores"], "kind": "port", "sample": info["sample"]},
+           "rays_per_s": info["rays_s"],
+           "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--threads", type=int, default=0)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    world, rank, local, pg = dist_setup(args)
+    import torch
+    torch.cuda.set_device(local)
+    from dnsmc_gb300 import synth
+    table = synth.ck_table()
+    T, x, Tw = make_inputs(rank)
+    s = make_solver(table, Tw, seed=1000 + rank, threads=args.threads)
+    s.set_fields(T, x)
+    rays, e_pilot = ray_budget(s)
+    rays = int(barrier_max(pg, rays))
+    s.set_rays(rays)
+    flushbuf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    for _ in range(max(3, args.warmup)):
+        s.solve(timeout_s=600)
+    # ---- device-resident timed region --------------------------------------
+    solve_ms, march_ms, errs, steps_tot, rays_tot = [], [], [], 0.0, 0.0
+    if pg is not None:
+        pg.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush_l2(flushbuf)
+            Q, S = s.solve(timeout_s=600)
+            a, b = s.timing()
+            c = s.counters()
+            solve_ms.append(a)
+            march_ms.append(b)
+            steps_tot += c.steps
+            rays_tot += c.rays
+            errs.append(rms_error(Q, S))
+    torch.cuda.synchronize()
+    t_rank = float(np.sum(solve_ms))
+    t_max = barrier_max(pg, t_rank)
+    fields = args.steps * world
+    ms_field = t_max / fields
+    rays_s = rays_tot * world / (t_max / 1e3)
+    march_avg = float(np.mean(march_ms))
+    steps_per_launch = steps_tot / args.steps
+    achieved = BYTES_PER_STEP * steps_per_launch / (march_avg / 1e3) / 1e9
+    peak, peak_kind = peaks()
+    # ---- end to end through the public API from host arrays ------------------
+    e2e_ms = []
+    Qh = None
+    for i in range(args.steps + 1):
+        t0 = time.perf_counter()
+        s.set_fields(T, x)
+        s.solve_async()
+        Qh, Sh = s.results()
+        dt = (time.perf_counter() - t0) * 1e3
+        if i > 0:
+            e2e_ms.append(dt)
+    e2e_rank = float(np.sum(e2e_ms))
+    e2e_max = barrier_max(pg, e2e_rank) / fields
+    h2d = T.nbytes + x.nbytes
+    d2h = Qh.nbytes + Sh.nbytes
+    if rank != 0:
+        s.close()
+        if pg is not None:
+            pg.destroy_process_group()
+        return 0
+    cpu = None
+    if not args.no_cpu:
+        try:
+            info = cpu_reference(table, T, x, Tw, rays)
+            cpu = {"value": info["ms_field"], "unit": "ms", "cores": info["cores"], "kind": "port",
+                   "sample": info["sample"], "rays_per_s": info["rays_s"]}
+        except Exception as ex:  # the baseline must not take the GPU number down
+            cpu = {"value": None, "unit": "ms", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {ex}"}
+    out = {
+        "metric": METRIC, "value": ms_field, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_field, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "ck channel 128^3 (x,z periodic 2pi x pi, y walls black 400 K), T 400-1800 K + 5% "
+                               "Fourier, x_H2O 0.1+0.05f, k table 64 bands x 16 g x 50 T x 8 x, 8 band groups, "
+                               "plain MC (no control variate)",
+                   "rays_per_cell_per_group": rays, "rays_per_cell": rays * GROUPS, "target_rms_error": TARGET_ERR,
+                   "rms_error_pilot": e_pilot, "rms_error_timed": float(np.mean(errs)),
+                   "l2": "flushed before every timed step (256 MB device write)", "parallelism": f"cells x{world}"},
+        "rays_per_s": rays_s, "ray_steps_per_s": steps_tot * world / (t_max / 1e3),
+        "march_ms": march_avg, "solve_ms": float(np.mean(solve_ms)),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": None, "peak_kind": peak_kind,
+                     "note": f"algorithmic gather bytes {BYTES_PER_STEP} B per ray-voxel step x lane-steps per "
+                             f"launch / march kernel time (CUDA events)"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_max, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "timing": "wall clock around set_fields + solve + get_results"},
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+    s.close()
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,298 @@
+"""Python host mirror of the solver's C ABI.
+
+Two surfaces, as in include/dnsmc.h:
+
+* ``mc_gpu(T, ystart)`` / ``get_results(Qr, Vr)`` -- the reference's
+  Fortran-facing pair (code/mc_gpu.cu:440, :640) with the same array layouts:
+  T is real(4) TMC(0:imax+1,0:jmax+1,0:kmax+1) in Fortran order (numpy
+  shape (kmax+2, jmax+2, imax+2), i fastest) and the outputs are
+  (kmax+2, jmax/p_row+2, imax+2); only interior cells are written.
+* ``Solver`` -- the handle-based API (tables, resident snapshots, band groups,
+  adaptive rays, error codes, status, counters).
+
+Arrays are numpy; the C library owns all device memory.  There is no
+CPU fallback: every call goes through libdnsmc.so.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import Config, TableDesc, check
+
+
+def _fp(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_lib.c_float_p)
+
+
+def _dp(a: np.ndarray | None):
+    if a is None:
+        return None
+    return a.ctypes.data_as(_lib.c_double_p)
+
+
+def default_config(**overrides) -> Config:
+    """The reference's shipped code/param.h values, with keyword overrides."""
+    lib = _lib.load()
+    c = Config()
+    lib.dnsmc_set_default_config(ctypes.byref(c))
+    for k, v in overrides.items():
+        if not hasattr(c, k):
+            raise KeyError(f"unknown config field {k!r}")
+        setattr(c, k, v)
+    return c
+
+
+@dataclass
+class Counters:
+    rays: float
+    steps: float
+    march_ms: float
+
+
+class Solver:
+    """One solver instance (its own CUDA stream, tables, fields and buffers)."""
+
+    def __init__(self, config: Config | None = None, **overrides):
+        self._lib = _lib.load()
+        cfg = config if config is not None else default_config()
+        for k, v in overrides.items():
+            setattr(cfg, k, v)
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        check(self._lib.dnsmc_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._region = (0, cfg.imax, 0, cfg.jmax, 0, cfg.kmax)
+        self._nfields = 0
+        self._keep = []
+        self._rays = cfg.nvar * cfg.photmax
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.dnsmc_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- tables -------------------------------------------------------------
+    def load_reference_tables(self, directory: str, model: int, nT: int = 52, nB: int = 119,
+                              nQ: int | None = None) -> None:
+        if nQ is None:
+            nQ = 16 if model == _lib.MODEL_CK else 1
+        check(self._lib.dnsmc_load_tables_ref(self._h, directory.encode(), model, nT, nB, nQ))
+
+    def use_grey_band_tables(self, nB: int = 1000, nT: int = 55, wvmax: float = 15000.0,
+                             Tmin: float = 500.0) -> None:
+        check(self._lib.dnsmc_use_grey_band_tables(self._h, nB, nT, wvmax, Tmin))
+
+    def set_table(self, k, wvc, T0, dT, dnu=None, wq=None, X0=0.0, dX=1.0, Ib=None,
+                  prob=None, probg=None, kP=None) -> None:
+        """k: array [nbands, nq, nT, nX] (or [nbands, nq, nT]) in 1/m."""
+        k = np.ascontiguousarray(k, dtype=np.float32)
+        if k.ndim == 3:
+            k = k[..., None]
+        nb, nq, nT, nX = k.shape
+        arrs = dict(k=k, wvc=wvc, dnu=dnu, wq=wq, Ib=Ib, prob=prob, probg=probg, kP=kP)
+        conv = {n: (None if a is None else np.ascontiguousarray(a, dtype=np.float32)) for n, a in arrs.items()}
+        d = TableDesc()
+        d.nbands, d.nq, d.nT, d.nX = nb, nq, nT, nX
+        d.T0, d.dT, d.X0, d.dX = T0, dT, X0, dX
+        for n, a in conv.items():
+            setattr(d, n, _fp(a))
+        check(self._lib.dnsmc_set_table(self._h, ctypes.byref(d)))
+
+    def table_info(self) -> dict:
+        vals = [ctypes.c_int() for _ in range(4)] + [ctypes.c_float() for _ in range(4)]
+        check(self._lib.dnsmc_get_table_info(self._h, *[ctypes.byref(v) for v in vals]))
+        keys = ["nbands", "nq", "nT", "nX", "T0", "dT", "X0", "dX"]
+        return {k: v.value for k, v in zip(keys, vals)}
+
+    def table(self) -> dict:
+        i = self.table_info()
+        nb, nq, nT, nX = i["nbands"], i["nq"], i["nT"], i["nX"]
+        k = np.zeros((nb, nq, nT, nX), np.float32)
+        wvc = np.zeros(nb, np.float32)
+        Ib = np.zeros((nb, nT), np.float32)
+        prob = np.zeros((nT, nb), np.float32)
+        probg = np.zeros((nT, nb, nq), np.float32)
+        kP = np.zeros(nT, np.float32)
+        check(self._lib.dnsmc_get_table(self._h, _fp(k), _fp(wvc), _fp(Ib), _fp(prob), _fp(probg), _fp(kP)))
+        return dict(k=k, wvc=wvc, Ib=Ib, prob=prob, probg=probg, kP=kP, **i)
+
+    # -- fields -------------------------------------------------------------
+    def set_fields(self, T, x=None, layout: int = _lib.LAYOUT_DENSE) -> None:
+        """T: (nfields, kmax, jmax, imax) or (kmax, jmax, imax) float32, i fastest
+        (Fortran order); FORTRAN layout adds the ghost layer on every axis."""
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        c = self.cfg
+        per = (c.kmax, c.jmax, c.imax) if layout == _lib.LAYOUT_DENSE else (c.kmax + 2, c.jmax + 2, c.imax + 2)
+        if T.shape == per:
+            T = T[None]
+        if T.shape[1:] != per:
+            raise ValueError(f"field shape {T.shape} does not match {per}")
+        X = None
+        if x is not None:
+            X = np.ascontiguousarray(x, dtype=np.float32).reshape(T.shape)
+        check(self._lib.dnsmc_set_fields(self._h, T.shape[0], _fp(T), _fp(X), layout))
+        self._nfields = T.shape[0]
+
+    def set_region(self, i0, i1, j0, j1, k0, k1) -> None:
+        check(self._lib.dnsmc_set_region(self._h, i0, i1, j0, j1, k0, k1))
+        self._region = (i0, i1, j0, j1, k0, k1)
+
+    def packet_count(self) -> int:
+        n = ctypes.c_int()
+        check(self._lib.dnsmc_packet_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def set_rays(self, rays_per_group: int, rays_per_packet=None) -> None:
+        rp = None
+        if rays_per_packet is not None:
+            rp = np.ascontiguousarray(rays_per_packet, dtype=np.int32)
+            if rp.size != self.packet_count():
+                raise ValueError("rays_per_packet needs one entry per packet")
+            self._keep = [rp]
+        else:
+            self._keep = []
+        check(self._lib.dnsmc_set_rays(self._h, int(rays_per_group),
+                                       None if rp is None else rp.ctypes.data_as(_lib.c_int_p)))
+        self._rays = int(rays_per_group)
+
+    # -- solve --------------------------------------------------------------
+    def solve_async(self) -> None:
+        check(self._lib.dnsmc_solve_async(self._h))
+
+    def wait(self, timeout_s: float = 0.0) -> None:
+        check(self._lib.dnsmc_wait(self._h, timeout_s))
+
+    def _region_shape(self):
+        i0, i1, j0, j1, k0, k1 = self._region
+        return (self._nfields, k1 - k0, j1 - j0, i1 - i0)
+
+    def results(self):
+        """(Q, sigma): float64 arrays (nfields, nk, nj, ni) over the region."""
+        shp = self._region_shape()
+        Q = np.zeros(shp, np.float64)
+        S = np.zeros(shp, np.float64)
+        check(self._lib.dnsmc_get_results(self._h, _dp(Q), _dp(S)))
+        return Q, S
+
+    def solve(self, timeout_s: float = 0.0):
+        self.solve_async()
+        self.wait(timeout_s)
+        return self.results()
+
+    def group_results(self):
+        """(Qg, varg): (nfields, n_groups, nk, nj, ni) group means and variances."""
+        ng = self.sampling()["n_groups"]
+        shp = self._region_shape()
+        shp = (shp[0], ng) + shp[1:]
+        Q = np.zeros(shp, np.float64)
+        V = np.zeros(shp, np.float64)
+        check(self._lib.dnsmc_get_group_results(self._h, _dp(Q), _dp(V)))
+        return Q, V
+
+    def status(self) -> int:
+        s = ctypes.c_uint32()
+        check(self._lib.dnsmc_status(self._h, ctypes.byref(s)))
+        return s.value
+
+    def counters(self) -> Counters:
+        r, s, m = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(self._lib.dnsmc_get_counters(self._h, ctypes.byref(r), ctypes.byref(s), ctypes.byref(m)))
+        return Counters(r.value, s.value, m.value)
+
+    def timing(self):
+        """(solve_ms, march_ms) of the last solve, CUDA events on its stream."""
+        a, b = ctypes.c_double(), ctypes.c_double()
+        check(self._lib.dnsmc_get_timing(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def tmax(self) -> float:
+        t = ctypes.c_float()
+        check(self._lib.dnsmc_get_tmax(self._h, ctypes.byref(t)))
+        return t.value
+
+    def sampling(self) -> dict:
+        ng, ne = ctypes.c_int(), ctypes.c_int()
+        check(self._lib.dnsmc_get_sampling(self._h, ctypes.byref(ng), None, ctypes.byref(ne),
+                                           None, None, None, None, None, None))
+        n, e = ng.value, ne.value
+        gs = np.zeros(n + 1, np.int32)
+        prob = np.zeros(max(e, 1), np.float32)
+        alias = np.zeros(max(e, 1), np.int32)
+        band = np.zeros(max(e, 1), np.int32)
+        gq = np.zeros(max(e, 1), np.int32)
+        W = np.zeros(max(e, 1), np.float32)
+        nb = max(self.table_info()["nbands"], 1)
+        ibw = np.zeros(2 * nb, np.float32)
+        ip = lambda a: a.ctypes.data_as(_lib.c_int_p)
+        check(self._lib.dnsmc_get_sampling(self._h, None, ip(gs), None, _fp(prob), ip(alias), ip(band), ip(gq),
+                                           _fp(W), _fp(ibw)))
+        return dict(n_groups=n, group_start=gs, prob=prob[:e], alias=alias[:e], band=band[:e], gq=gq[:e],
+                    W=W[:e], ibw=ibw)
+
+    def prepare_sampling(self, Tmax: float, xmean: float = 0.0) -> dict:
+        """Build the sampling tables on the host for Tmax (no GPU needed)."""
+        check(self._lib.dnsmc_prepare_sampling(self._h, float(Tmax), float(xmean)))
+        return self.sampling()
+
+    def geometry(self):
+        xu = np.zeros(self.cfg.imax + 1, np.float32)
+        dy, dz = ctypes.c_float(), ctypes.c_float()
+        check(self._lib.dnsmc_get_geometry(self._h, _fp(xu), ctypes.byref(dy), ctypes.byref(dz)))
+        return xu, dy.value, dz.value
+
+    def trace(self, f: int, g: int, p: int, r: int, max_steps: int = 4096):
+        rec = np.zeros((max_steps, 6), np.int32)
+        n = ctypes.c_int()
+        rng = np.zeros(4, np.uint32)
+        check(self._lib.dnsmc_trace_ray(self._h, f, g, p, r, max_steps, rec.ctypes.data_as(_lib.c_int32_p),
+                                        ctypes.byref(n), rng.ctypes.data_as(_lib.c_uint32_p)))
+        return rec[: min(n.value, max_steps)], n.value, rng
+
+
+# -- reference drop-in pair -----------------------------------------------------
+def dropin_configure(config: Config | None = None, table_dir: str | None = None) -> None:
+    lib = _lib.load()
+    check(lib.dnsmc_dropin_configure(None if config is None else ctypes.byref(config),
+                                     None if table_dir is None else table_dir.encode()))
+
+
+def dropin_release() -> None:
+    _lib.load().dnsmc_dropin_release()
+
+
+def mc_gpu(T: np.ndarray, ystart: int) -> None:
+    """code/mc_gpu.cu:440 -- enqueue the MC for the slab starting at global j
+    = ystart (1-based); returns immediately."""
+    lib = _lib.load()
+    if T.dtype != np.float32 or not T.flags.c_contiguous:
+        raise TypeError("T must be a C-contiguous float32 array in Fortran (i-fastest) order")
+    ys = ctypes.c_int(int(ystart))
+    lib.mc_gpu_(_fp(T), ctypes.byref(ys))
+
+
+def get_results(Qr: np.ndarray, Vr: np.ndarray) -> None:
+    """code/mc_gpu.cu:640 -- block, then write Q and sigma into interior cells."""
+    lib = _lib.load()
+    for a in (Qr, Vr):
+        if a.dtype != np.float32 or not a.flags.c_contiguous:
+            raise TypeError("outputs must be C-contiguous float32 arrays")
+    lib.get_results_(_fp(Qr), _fp(Vr))

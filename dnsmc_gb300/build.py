@@ -1,0 +1,71 @@
+"""Build recipe for libdnsmc.so (the C-ABI library) -- in-tree, sm_103a only.
+
+    python -m dnsmc_gb300.build        # or dnsmc_gb300.build.build()
+
+Compiles the CUDA translation unit with nvcc for sm_103a (-fmad=false: the
+march is written with explicit fmaf so the host replay can reproduce it bit
+for bit) and the host runtime with the same nvcc driver, in parallel, then
+links one shared library with the static CUDA runtime.
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+LIBDIR = os.path.join(HERE, "lib")
+LIBNAME = "libdnsmc.so"
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc() -> str:
+    cand = [os.environ.get("NVCC", ""), shutil.which("nvcc") or "", "/usr/local/cuda/bin/nvcc"]
+    for c in cand:
+        if c and os.path.exists(c):
+            return c
+    raise RuntimeError("nvcc not found (set NVCC or put CUDA on PATH)")
+
+
+def lib_path() -> str:
+    return os.path.join(LIBDIR, LIBNAME)
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+
+
+def build(verbose: bool = False) -> str:
+    nvcc = _nvcc()
+    bdir = os.path.join(HERE, "_build")
+    os.makedirs(bdir, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo"] + inc
+    jobs = [
+        [nvcc, *ARCH, *common, "-fmad=false", "-c", os.path.join(CSRC, "mc_kernels.cu"),
+         "-o", os.path.join(bdir, "mc_kernels.o")],
+        [nvcc, *common, "-x", "c++", "-c", os.path.join(CSRC, "mc_host.cpp"),
+         "-o", os.path.join(bdir, "mc_host.o")],
+    ]
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        list(ex.map(_run, jobs))
+    out = lib_path()
+    tmp = out + ".tmp"
+    _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-Xcompiler", "-fPIC",
+          os.path.join(bdir, "mc_kernels.o"), os.path.join(bdir, "mc_host.o"), "-o", tmp])
+    os.replace(tmp, out)
+    if verbose:
+        print("built", out)
+    return out
+
+
+if __name__ == "__main__":
+    build(verbose=True)
+    sys.exit(0)

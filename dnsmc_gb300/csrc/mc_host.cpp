@@ -1,0 +1,1317 @@
+// mc_host.cpp -- host runtime behind the C ABI of include/dnsmc.h.
+//
+// Replaces the reference host path (code/mc_gpu.cu:440-784, code/memory_copy.cu,
+// code/read_tables.cpp, code/grey_tables.cpp): the reference rebuilds every
+// device object per call and ends with cudaDeviceReset; here tables, fields
+// and buffers are persistent per solver, the solve is one stream-ordered
+// sequence (sampling upload, march, finalize, device-to-host copy), and every
+// failure is an error code instead of exit(1).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/dnsmc.h"
+#include "mc_internal.h"
+
+using namespace dnsmc;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CUDA_TRY(x)                                                                       \
+    do {                                                                                  \
+        cudaError_t e_ = (x);                                                             \
+        if (e_ != cudaSuccess)                                                            \
+            return fail(DNSMC_ERR_CUDA, "%s failed: %s", #x, cudaGetErrorString(e_));     \
+    } while (0)
+
+#define TRY(x)                   \
+    do {                         \
+        int rc_ = (x);           \
+        if (rc_ != DNSMC_OK) return rc_; \
+    } while (0)
+
+constexpr double kSigma = 5.670373e-08;  // code/param.h:70
+constexpr double kPi = 3.14159265358979323846;
+
+// Band-centre Planck intensity per unit wavenumber [W/(m^2 sr m^-1)], nu in
+// 1/cm: the reference I_blackC (code/memory_copy.cu:291-300), same FP32 steps.
+float planck_band(float T, float nu) {
+    if (!(T > 0.0f)) return 0.0f;
+    const float C1 = 3.741771790075259e-16f;
+    const float C2 = 0.014387741858429f;
+    const float n100 = nu * 100.0f;
+    const float n3 = n100 * n100 * n100;
+    const float den = expf(C2 * nu * 100.0f / T) - 1.0f;
+    return (float)(1.0 / kPi * (double)C1 * (double)n3 / (double)den);
+}
+
+// 16 positive nodes and weights of 32-point Gauss-Legendre on [-1, 1]: the
+// g-quadrature of code/NarrowBand.h:201-207 (computed, not tabulated).
+void gauss_half(int nq, std::vector<float> &gq, std::vector<float> &wq) {
+    const int n = 2 * nq;
+    std::vector<double> x(n), w(n);
+    for (int i = 0; i < n; ++i) {
+        double z = cos(kPi * (i + 0.75) / (n + 0.5));
+        for (int it = 0; it < 100; ++it) {
+            double p1 = 1.0, p2 = 0.0;
+            for (int j = 1; j <= n; ++j) {
+                const double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+            }
+            const double pp = n * (z * p1 - p2) / (z * z - 1.0);
+            const double z1 = z;
+            z = z1 - p1 / pp;
+            if (fabs(z - z1) < 1e-15) {
+                x[i] = z;
+                w[i] = 2.0 / ((1.0 - z * z) * pp * pp);
+                break;
+            }
+        }
+    }
+    gq.clear();
+    wq.clear();
+    for (int i = n - 1; i >= 0; --i)
+        if (x[i] > 0) { gq.push_back((float)x[i]); wq.push_back((float)w[i]); }
+}
+
+struct HostTable {
+    int nbands = 0, nq = 0, nT = 0, nX = 1;
+    float T0 = 0.f, dT = 1.f, X0 = 0.f, dX = 1.f;
+    std::vector<float> k, wvc, dnu, wq, Ib, prob, probg, kP;
+    bool ref_sampling = false;
+    bool valid = false;
+    // reference grey bands (rebuilt from Tmax at every solve)
+    bool grey_bands = false;
+    int gb_nB = 0, gb_nT = 0;
+    float gb_wvmax = 0.f, gb_Tmin = 0.f, gb_kappa = 1.f;
+};
+
+// Reference wall-normal grid (code/definitions.h:108-134), FP32 like the
+// reference; uniform when stretched == 0.
+void make_faces(int im, float L, int stretched, std::vector<float> &xu) {
+    xu.assign(im + 1, 0.0f);
+    if (!stretched) {
+        for (int i = 0; i <= im; ++i) xu[i] = (float)i * (L / (float)im);
+        xu[im] = L;
+        return;
+    }
+    const int im0 = im;
+    std::vector<float> xu0(im0 + 1, 0.0f);
+    for (int i = 1; i < im0 / 2 + 1; ++i) {
+        const float r = (1.f * i) / im0;
+        const float dx = (float)(0.5 - 1.45 * (r - 0.5) * (r - 0.5));
+        xu0[i] = xu0[i - 1] + dx;
+    }
+    const float xnorm = xu0[im0 / 2];
+    for (int i = 1; i < im0 / 2 + 1; ++i) xu0[i] = (float)(L / 2. * xu0[i] / xnorm);
+    for (int i = im0; i > im0 / 2; --i) xu0[i] = L - xu0[im0 - i];
+    for (int i = 1; i < im + 1; ++i) xu[i] = xu0[i * im0 / im];
+}
+
+template <class T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    int ensure(size_t want) {
+        if (want <= n) return DNSMC_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        if (want == 0) return DNSMC_OK;
+        cudaError_t e = cudaMalloc((void **)&p, want * sizeof(T));
+        if (e != cudaSuccess) return fail(DNSMC_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", want * sizeof(T), cudaGetErrorString(e));
+        n = want;
+        return DNSMC_OK;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; n = 0; }
+};
+
+template <class T>
+struct PinBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    int ensure(size_t want) {
+        if (want <= n) return DNSMC_OK;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        if (want == 0) return DNSMC_OK;
+        cudaError_t e = cudaMallocHost((void **)&p, want * sizeof(T));
+        if (e != cudaSuccess) return fail(DNSMC_ERR_NOMEM, "cudaMallocHost(%zu bytes): %s", want * sizeof(T), cudaGetErrorString(e));
+        n = want;
+        return DNSMC_OK;
+    }
+    void release() { if (p) cudaFreeHost(p); p = nullptr; n = 0; }
+};
+
+}  // namespace
+
+struct dnsmc_solver {
+    dnsmc_config cfg{};
+    int device = 0;
+    bool dev_ready = false;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_march0 = nullptr, ev_march1 = nullptr, ev_done = nullptr, ev_solve0 = nullptr;
+    bool solved = false, in_flight = false;
+
+    // geometry
+    std::vector<float> fw;
+    float da = 0.f, db = 0.f;
+    DevBuf<float> d_fw;
+
+    // tables
+    HostTable tab;
+    DevBuf<float> d_k, d_ib, d_ibw;
+    bool tables_dirty = true;
+
+    // fields
+    int nfields = 0;
+    bool have_x = false;
+    float tmax_fields = 0.f, tmin_fields = 0.f;
+    double xsum = 0.0;
+    DevBuf<float> d_fieldT;
+    DevBuf<float2> d_fieldTX;
+    DevBuf<float> d_raw;
+    PinBuf<float> h_stage;
+    DevBuf<double> d_stat_part;
+    DevBuf<float> d_stat_out;
+
+    // region and rays
+    int r_i0 = 0, r_i1 = 0, r_j0 = 0, r_j1 = 0, r_k0 = 0, r_k1 = 0;
+    int rays = 0;
+    std::vector<int> rays_pp;
+    DevBuf<int> d_rays_pp;
+
+    // sampling of the last solve
+    float tmax_used = 0.f;
+    std::vector<SpecEntry> entries;
+    std::vector<int> group_start, group_empty;
+    std::vector<float> ibw;
+    DevBuf<SpecEntry> d_entries;
+    DevBuf<int> d_group_start, d_group_empty;
+    int mode = MODE_GREY;
+    int n_groups_used = 1;
+
+    // outputs
+    DevBuf<double2> d_tally;
+    DevBuf<double> d_Q, d_var, d_Qg, d_varg;
+    PinBuf<double> h_Q, h_var;
+    DevBuf<unsigned int> d_misc;  // [0] queue, [1] status
+    DevBuf<unsigned long long> d_counters;
+    unsigned long long h_counters[2] = {0, 0};
+    unsigned int h_status = 0;
+    float march_ms = 0.f, solve_ms = 0.f;
+    MarchParams last{};
+    FinalizeParams lastF{};
+};
+
+namespace {
+
+// The device side of a solver (stream, events, faces) is created on first
+// use, so table parsing and sampling construction work without a GPU.
+int ensure_device(dnsmc_solver *s) {
+    if (s->dev_ready) {
+        CUDA_TRY(cudaSetDevice(s->device));
+        return DNSMC_OK;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev < 1) return fail(DNSMC_ERR_NODEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+    CUDA_TRY(cudaGetDevice(&s->device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreate(&s->ev_march0));
+    CUDA_TRY(cudaEventCreate(&s->ev_march1));
+    CUDA_TRY(cudaEventCreate(&s->ev_done));
+    CUDA_TRY(cudaEventCreate(&s->ev_solve0));
+    s->dev_ready = true;
+    if (int rc = s->d_fw.ensure(s->fw.size())) return rc;
+    CUDA_TRY(cudaMemcpy(s->d_fw.p, s->fw.data(), s->fw.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return DNSMC_OK;
+}
+
+int set_device(dnsmc_solver *s) { return ensure_device(s); }
+
+int check_config(const dnsmc_config &c) {
+    if (c.imax < 1 || c.jmax < 1 || c.kmax < 1) return fail(DNSMC_ERR_ARG, "imax, jmax, kmax must be >= 1");
+    if (c.p_row < 1 || c.jmax % c.p_row) return fail(DNSMC_ERR_ARG, "jmax (%d) must be a multiple of p_row (%d)", c.jmax, c.p_row);
+    if (!(c.Lx > 0) || !(c.Ly > 0) || !(c.Lz > 0)) return fail(DNSMC_ERR_ARG, "Lx, Ly, Lz must be > 0");
+    if (c.nvar < 1 || c.photmax < 1) return fail(DNSMC_ERR_ARG, "nvar and photmax must be >= 1");
+    if (!(c.toll > 0) || c.toll >= 1) return fail(DNSMC_ERR_ARG, "toll must be in (0,1)");
+    if (c.max_steps < 1) return fail(DNSMC_ERR_ARG, "max_steps must be >= 1");
+    if (c.grid_num != 1) return fail(DNSMC_ERR_ARG, "grid_num %d: only the fine grid (grid_num = 1) is marched", c.grid_num);
+    if (c.model < 0 || c.model > 4) return fail(DNSMC_ERR_ARG, "unknown model %d", c.model);
+    if (c.n_groups < 1) return fail(DNSMC_ERR_ARG, "n_groups must be >= 1");
+    if (c.block_threads && c.block_threads != 128 && c.block_threads != 256 && c.block_threads != 512)
+        return fail(DNSMC_ERR_ARG, "block_threads must be 0, 128, 256 or 512");
+    if (c.tile_a && c.tile_a != 8 && c.tile_a != 16 && c.tile_a != 32)
+        return fail(DNSMC_ERR_ARG, "tile_a must be 0, 8, 16 or 32");
+    if (!(c.eps_west == 1.0f) || !(c.eps_east == 1.0f))
+        return fail(DNSMC_ERR_ARG, "grey walls (eps < 1) are not supported by this solver build");
+    if (!(c.T_west >= 0) || !(c.T_east >= 0)) return fail(DNSMC_ERR_ARG, "wall temperatures must be >= 0");
+    return DNSMC_OK;
+}
+
+// ---- reference text-format readers ---------------------------------------
+FILE *open_table(const std::string &path) { return fopen(path.c_str(), "r"); }
+
+int read_ck_tables(const std::string &dir, int nT, int nB, int nQ, HostTable &t) {
+    // planck-mean.txt: "T kP kPr kM" (code/read_tables.cpp:25-30)
+    std::vector<float> Tnb(nT), kP(nT);
+    FILE *fp = open_table(dir + "/planck-mean.txt");
+    if (!fp) return fail(DNSMC_ERR_IO, "cannot open %s/planck-mean.txt", dir.c_str());
+    for (int i = 0; i < nT; ++i) {
+        float d1, d2;
+        if (fscanf(fp, "%f %e %e %e", &Tnb[i], &kP[i], &d1, &d2) != 4) { fclose(fp); return fail(DNSMC_ERR_IO, "planck-mean.txt: bad row %d", i); }
+    }
+    fclose(fp);
+    t.nbands = nB; t.nq = nQ; t.nT = nT; t.nX = 1;
+    t.T0 = Tnb[0]; t.dT = Tnb[1] - Tnb[0]; t.X0 = 0.f; t.dX = 1.f;
+    t.k.assign((size_t)nB * nQ * nT, 0.f);
+    t.wvc.assign(nB, 0.f); t.dnu.assign(nB, 0.f);
+    // NarrBand%d.txt: "wl wr wvc" then nT rows "T cuprob kavg kq[nQ]" (:339-359)
+    for (int b = 0; b < nB; ++b) {
+        char name[64];
+        snprintf(name, sizeof name, "/NarrBand%d.txt", b);
+        fp = open_table(dir + name);
+        if (!fp) return fail(DNSMC_ERR_IO, "cannot open %s%s", dir.c_str(), name);
+        float wl, wr;
+        if (fscanf(fp, "%e %e %e", &wl, &wr, &t.wvc[b]) != 3) { fclose(fp); return fail(DNSMC_ERR_IO, "%s: bad header", name); }
+        t.dnu[b] = wr - wl;
+        for (int i = 0; i < nT; ++i) {
+            float T, cp, kavg;
+            if (fscanf(fp, "%f %f %f", &T, &cp, &kavg) != 3) { fclose(fp); return fail(DNSMC_ERR_IO, "%s: bad row %d", name, i); }
+            for (int g = 0; g < nQ; ++g) {
+                float v;
+                if (fscanf(fp, "%e", &v) != 1) { fclose(fp); return fail(DNSMC_ERR_IO, "%s: bad row %d", name, i); }
+                t.k[((size_t)b * nQ + g) * nT + i] = v;
+            }
+        }
+        fclose(fp);
+    }
+    // prob_new2.txt: nT*nB rows "T nb cuprob probg[nQ]" (:364-386)
+    t.prob.assign((size_t)nT * nB, 0.f);
+    t.probg.assign((size_t)nT * nB * nQ, 0.f);
+    fp = open_table(dir + "/prob_new2.txt");
+    if (!fp) return fail(DNSMC_ERR_IO, "cannot open %s/prob_new2.txt", dir.c_str());
+    for (int i = 0; i < nT; ++i)
+        for (int b = 0; b < nB; ++b) {
+            float T;
+            int nb;
+            if (fscanf(fp, "%f %d %e", &T, &nb, &t.prob[(size_t)i * nB + b]) != 3) { fclose(fp); return fail(DNSMC_ERR_IO, "prob_new2.txt: bad row"); }
+            for (int g = 0; g < nQ; ++g)
+                if (fscanf(fp, "%e", &t.probg[((size_t)i * nB + b) * nQ + g]) != 1) { fclose(fp); return fail(DNSMC_ERR_IO, "prob_new2.txt: bad row"); }
+        }
+    fclose(fp);
+    t.kP = kP;
+    std::vector<float> gq;
+    if (nQ == 16) gauss_half(16, gq, t.wq); else t.wq.assign(nQ, 1.0f / nQ);
+    t.ref_sampling = true;
+    return DNSMC_OK;
+}
+
+int read_particle_tables(const std::string &dir0, int nT, int nB, HostTable &t) {
+    const std::string dir = dir0 + "/particles";
+    std::vector<float> Tnb(nT), kP(nT);
+    FILE *fp = open_table(dir + "/planck-mean.txt");  // "T kP" (code/read_tables.cpp:491-496)
+    if (!fp) return fail(DNSMC_ERR_IO, "cannot open %s/planck-mean.txt", dir.c_str());
+    for (int i = 0; i < nT; ++i)
+        if (fscanf(fp, "%f %e", &Tnb[i], &kP[i]) != 2) { fclose(fp); return fail(DNSMC_ERR_IO, "particles/planck-mean.txt: bad row %d", i); }
+    fclose(fp);
+    t.nbands = nB; t.nq = 1; t.nT = nT; t.nX = 1;
+    t.T0 = Tnb[0]; t.dT = Tnb[1] - Tnb[0]; t.X0 = 0.f; t.dX = 1.f;
+    t.k.assign((size_t)nB * nT, 0.f);
+    t.wvc.assign(nB, 0.f); t.dnu.assign(nB, 0.f);
+    for (int b = 0; b < nB; ++b) {  // "wl wr wvc kq ..." (:505-518), kq constant in T
+        char name[64];
+        snprintf(name, sizeof name, "/NarrBand%d.txt", b);
+        fp = open_table(dir + name);
+        if (!fp) return fail(DNSMC_ERR_IO, "cannot open %s%s", dir.c_str(), name);
+        float wl, wr, kq;
+        if (fscanf(fp, "%e %e %e %e", &wl, &wr, &t.wvc[b], &kq) != 4) { fclose(fp); return fail(DNSMC_ERR_IO, "particles%s: bad header", name); }
+        fclose(fp);
+        t.dnu[b] = wr - wl;
+        for (int i = 0; i < nT; ++i) t.k[(size_t)b * nT + i] = kq;
+    }
+    t.prob.assign((size_t)nT * nB, 0.f);  // prob.txt: "T nb cuprob" (:520-540)
+    fp = open_table(dir + "/prob.txt");
+    if (!fp) return fail(DNSMC_ERR_IO, "cannot open %s/prob.txt", dir.c_str());
+    for (int i = 0; i < nT; ++i)
+        for (int b = 0; b < nB; ++b) {
+            float T;
+            int nb;
+            if (fscanf(fp, "%f %d %e", &T, &nb, &t.prob[(size_t)i * nB + b]) != 3) { fclose(fp); return fail(DNSMC_ERR_IO, "particles/prob.txt: bad row"); }
+        }
+    fclose(fp);
+    t.probg.clear();
+    t.kP = kP;
+    t.wq.assign(1, 1.0f);
+    t.ref_sampling = true;
+    return DNSMC_OK;
+}
+
+// Reference grey tables (code/grey_tables.cpp:19-109 / code/read_tables.cpp:404-483)
+void build_grey_band_tables(HostTable &t, float Tmax) {
+    const int nB = t.gb_nB, nT = t.gb_nT;
+    std::vector<float> Tnb(nT);
+    for (int i = 0; i < nT; ++i)
+        Tnb[i] = t.gb_Tmin * 0.9f + (Tmax * 1.1f - t.gb_Tmin * 0.9f) * ((float)i) / ((float)nT);
+    t.nbands = nB; t.nq = 1; t.nT = nT; t.nX = 1;
+    t.T0 = Tnb[0]; t.dT = Tnb[1] - Tnb[0];
+    t.X0 = 0.f; t.dX = 1.f;
+    std::vector<float> wvl(nB), wvr(nB);
+    wvl[0] = 0;
+    for (int i = 1; i < nB; ++i) wvl[i] = wvl[i - 1] + t.gb_wvmax / nB;
+    wvr[0] = t.gb_wvmax / nB;
+    for (int i = 1; i < nB; ++i) wvr[i] = wvr[i - 1] + t.gb_wvmax / nB;
+    t.wvc.resize(nB); t.dnu.resize(nB);
+    for (int i = 0; i < nB; ++i) { t.wvc[i] = (float)((wvl[i] + wvr[i]) / 2.); t.dnu[i] = wvr[i] - wvl[i]; }
+    t.k.assign((size_t)nB * nT, t.gb_kappa);
+    t.kP.assign(nT, t.gb_kappa);
+    t.Ib.assign((size_t)nB * nT, 0.f);
+    for (int b = 0; b < nB; ++b)
+        for (int i = 0; i < nT; ++i) t.Ib[(size_t)b * nT + i] = planck_band(Tnb[i], t.wvc[b]);
+    t.prob.assign((size_t)nT * nB, 0.f);
+    for (int i = 0; i < nT; ++i) {
+        float acc = t.Ib[(size_t)0 * nT + i] * (wvr[0] - wvl[0]) * 100;
+        t.prob[(size_t)i * nB] = acc;
+        for (int b = 1; b < nB; ++b) {
+            acc = acc + t.Ib[(size_t)b * nT + i] * (wvr[b] - wvl[b]) * 100;
+            t.prob[(size_t)i * nB + b] = acc;
+        }
+        const float last = t.prob[(size_t)i * nB + nB - 1];
+        for (int b = 0; b < nB; ++b) t.prob[(size_t)i * nB + b] = t.prob[(size_t)i * nB + b] / last;
+    }
+    t.probg.clear();
+    t.wq.assign(1, 1.0f);
+    t.ref_sampling = true;
+    t.valid = true;
+}
+
+void fill_ib(HostTable &t) {
+    if (!t.Ib.empty()) return;
+    t.Ib.assign((size_t)t.nbands * t.nT, 0.f);
+    for (int b = 0; b < t.nbands; ++b)
+        for (int i = 0; i < t.nT; ++i) t.Ib[(size_t)b * t.nT + i] = planck_band(t.T0 + i * t.dT, t.wvc[b]);
+}
+
+// Clamped linear position (same as the kernel's grid_pos, in double).
+void gpos(double v, double v0, double d, int n, int *i, double *f) {
+    double p = (v - v0) / d;
+    p = std::min(std::max(p, 0.0), (double)(n - 1));
+    int ii = std::min((int)p, n - 2);
+    if (n < 2) ii = 0;
+    *i = ii;
+    *f = p - ii;
+}
+
+double k_at(const HostTable &t, int b, int g, double T, double x) {
+    int ti, xi = 0;
+    double ft, fx = 0.0;
+    gpos(T, t.T0, t.dT, t.nT, &ti, &ft);
+    const float *s = t.k.data() + ((size_t)b * t.nq + g) * t.nT * t.nX;
+    if (t.nX > 1) {
+        gpos(x, t.X0, t.dX, t.nX, &xi, &fx);
+        const double k0 = s[ti * t.nX + xi] + fx * (s[ti * t.nX + xi + 1] - s[ti * t.nX + xi]);
+        const double k1 = s[(ti + 1) * t.nX + xi] + fx * (s[(ti + 1) * t.nX + xi + 1] - s[(ti + 1) * t.nX + xi]);
+        return k0 + ft * (k1 - k0);
+    }
+    return s[ti] + ft * (s[ti + 1] - s[ti]);
+}
+
+double ib_at(const HostTable &t, int b, double T) {
+    int ti;
+    double ft;
+    gpos(T, t.T0, t.dT, t.nT, &ti, &ft);
+    const float *s = t.Ib.data() + (size_t)b * t.nT;
+    return s[ti] + ft * (s[ti + 1] - s[ti]);
+}
+
+// Vose alias table over K probabilities, thresholds quantised to 2^-24, then
+// the exact sampling probability of every entry as the kernel draws it:
+// slot j = floor(x*K / 2^32) for a 32-bit x, accept slot j when
+// (y>>8)*2^-24 < thr_j, else take alias_j.
+void build_alias(const std::vector<double> &q, std::vector<float> &thr, std::vector<int> &alias,
+                 std::vector<double> &peff) {
+    const int K = (int)q.size();
+    thr.assign(K, 1.0f);
+    alias.resize(K);
+    for (int j = 0; j < K; ++j) alias[j] = j;
+    std::vector<double> sc(K);
+    double tot = 0.0;
+    for (double v : q) tot += v;
+    std::vector<int> small, large;
+    for (int j = 0; j < K; ++j) {
+        sc[j] = q[j] / tot * K;
+        (sc[j] < 1.0 ? small : large).push_back(j);
+    }
+    std::vector<double> pr(K, 1.0);
+    while (!small.empty() && !large.empty()) {
+        const int s = small.back(); small.pop_back();
+        const int l = large.back(); large.pop_back();
+        pr[s] = sc[s];
+        alias[s] = l;
+        sc[l] = (sc[l] + sc[s]) - 1.0;
+        (sc[l] < 1.0 ? small : large).push_back(l);
+    }
+    for (int j : large) pr[j] = 1.0;
+    for (int j : small) pr[j] = 1.0;
+    peff.assign(K, 0.0);
+    const double two32 = 4294967296.0, two24 = 16777216.0;
+    for (int j = 0; j < K; ++j) {
+        double m = ceil(pr[j] * two24);
+        if (m > two24) m = two24;
+        if (m < 0) m = 0;
+        thr[j] = (float)(m / two24);
+        const double pacc = m / two24;
+        // number of 32-bit x with floor(x*K/2^32) == j
+        const double lo = ceil(j * two32 / K), hi = ceil((j + 1) * two32 / K);
+        const double pslot = (hi - lo) / two32;
+        peff[j] += pslot * pacc;
+        peff[alias[j]] += pslot * (1.0 - pacc);
+    }
+}
+
+int build_sampling(dnsmc_solver *s, float Tmax, float xm) {
+    HostTable &t = s->tab;
+    const dnsmc_config &c = s->cfg;
+    s->entries.clear();
+    s->group_start.clear();
+    s->group_empty.clear();
+    if (c.model == DNSMC_MODEL_GREY) {
+        s->n_groups_used = 1;
+        s->group_start = {0, 0};
+        s->group_empty = {0};
+        return DNSMC_OK;
+    }
+    fill_ib(t);
+    const int nB = t.nbands, nQ = t.nq;
+    const int nG = std::min(c.n_groups, nB);
+    s->n_groups_used = nG;
+    const double Tm = Tmax;
+    std::vector<double> C((size_t)nB * nQ, 0.0), q((size_t)nB * nQ, 0.0);
+    if (t.ref_sampling) {
+        // nearest table temperature to Tmax (code/mc_gpu.cu:142, :837)
+        int tm = (int)((Tmax - t.T0) / t.dT);
+        tm = std::max(0, std::min(tm, t.nT - 2));
+        const float Tt0 = t.T0 + tm * t.dT, Tt1 = t.T0 + (tm + 1) * t.dT;
+        const int ts = ((Tmax - Tt0) < (Tt1 - Tmax)) ? tm : tm + 1;
+        // kappamax: Planck mean at Tmax (code/read_tables.cpp:334-336)
+        int tk = (int)((Tmax - t.T0) / t.dT);
+        tk = std::max(0, std::min(tk, t.nT - 2));
+        const double kmax = (double)(t.kP[tk + 1] - t.kP[tk]) / t.dT * (Tmax - (t.T0 + tk * t.dT)) + t.kP[tk];
+        const double E = 4.0 * kmax * kSigma * Tm * Tm * Tm * Tm;
+        double tot = 0.0;
+        for (int b = 0; b < nB; ++b) {
+            const double pb = (double)t.prob[(size_t)ts * nB + b] - (b ? (double)t.prob[(size_t)ts * nB + b - 1] : 0.0);
+            for (int g = 0; g < nQ; ++g) {
+                double pg = (g == 0) ? 1.0 : 0.0;
+                if (!t.probg.empty()) {
+                    const float *cg = t.probg.data() + ((size_t)ts * nB + b) * nQ;
+                    pg = (double)cg[g] - (g ? (double)cg[g - 1] : 0.0);
+                }
+                const double p = std::max(0.0, pb) * std::max(0.0, pg);
+                q[(size_t)b * nQ + g] = p;
+                tot += p;
+            }
+        }
+        if (!(tot > 0)) return fail(DNSMC_ERR_TABLE, "band CDF at T=%g is empty", (double)(t.T0 + ts * t.dT));
+        for (int b = 0; b < nB; ++b)
+            for (int g = 0; g < nQ; ++g) {
+                const size_t s_ = (size_t)b * nQ + g;
+                if (q[s_] <= 0) continue;
+                q[s_] /= tot;
+                const double den = ib_at(t, b, Tm) * k_at(t, b, g, Tm, xm);
+                // ray weight of the reference: Ibmax*ratioI = E * k_i Ib_i / (k_m Ib_m)
+                C[s_] = den > 0 ? q[s_] * E / den : 0.0;
+                if (!(den > 0)) q[s_] = 0.0;
+            }
+    } else {
+        double mean = 0.0;
+        for (int b = 0; b < nB; ++b)
+            for (int g = 0; g < nQ; ++g) {
+                const size_t s_ = (size_t)b * nQ + g;
+                C[s_] = 4.0 * kPi * 100.0 * t.dnu[b] * t.wq[g];
+                q[s_] = C[s_] * k_at(t, b, g, Tm, xm) * ib_at(t, b, Tm);
+                mean += q[s_];
+            }
+        mean /= (double)(nB * nQ);
+        // floor keeps every sample with a non-zero weight reachable
+        for (size_t s_ = 0; s_ < q.size(); ++s_)
+            if (C[s_] > 0) q[s_] = std::max(q[s_], 1e-6 * mean);
+    }
+    s->group_start.push_back(0);
+    for (int G = 0; G < nG; ++G) {
+        const int b0 = (int)((long long)G * nB / nG), b1 = (int)((long long)(G + 1) * nB / nG);
+        std::vector<double> qg;
+        std::vector<int> ids;
+        for (int b = b0; b < b1; ++b)
+            for (int g = 0; g < nQ; ++g)
+                if (q[(size_t)b * nQ + g] > 0) { qg.push_back(q[(size_t)b * nQ + g]); ids.push_back(b * nQ + g); }
+        if (qg.empty()) {
+            s->group_empty.push_back(1);
+            s->group_start.push_back((int)s->entries.size());
+            continue;
+        }
+        if (qg.size() > 65535) return fail(DNSMC_ERR_TABLE, "band group has more than 65535 samples");
+        std::vector<float> thr;
+        std::vector<int> al;
+        std::vector<double> peff;
+        build_alias(qg, thr, al, peff);
+        for (size_t j = 0; j < qg.size(); ++j) {
+            const int sid = ids[j];
+            const int b = sid / nQ, g = sid % nQ;
+            SpecEntry e;
+            e.prob = thr[j];
+            e.alias_nb = (uint32_t)al[j] | ((uint32_t)b << 16);
+            e.koff = (int32_t)(((size_t)b * nQ + g) * t.nT * t.nX);
+            e.W = peff[j] > 0 ? (float)(C[sid] / peff[j]) : 0.0f;
+            s->entries.push_back(e);
+        }
+        s->group_empty.push_back(0);
+        s->group_start.push_back((int)s->entries.size());
+    }
+    s->ibw.assign((size_t)2 * nB, 0.f);
+    for (int b = 0; b < nB; ++b) {
+        s->ibw[b] = planck_band(c.T_west, t.wvc[b]);
+        s->ibw[nB + b] = planck_band(c.T_east, t.wvc[b]);
+    }
+    return DNSMC_OK;
+}
+
+int upload_tables(dnsmc_solver *s) {
+    HostTable &t = s->tab;
+    fill_ib(t);
+    TRY(s->d_k.ensure(t.k.size()));
+    TRY(s->d_ib.ensure(t.Ib.size()));
+    CUDA_TRY(cudaMemcpyAsync(s->d_k.p, t.k.data(), t.k.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->d_ib.p, t.Ib.data(), t.Ib.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->tables_dirty = false;
+    return DNSMC_OK;
+}
+
+int region_dims(const dnsmc_solver *s, int *ni, int *nj, int *nk) {
+    *ni = s->r_i1 - s->r_i0;
+    *nj = s->r_j1 - s->r_j0;
+    *nk = s->r_k1 - s->r_k0;
+    return DNSMC_OK;
+}
+
+void tiling(const dnsmc_solver *s, int *ta, int *tb, int *npa, int *npb, int *npw) {
+    int ni, nj, nk;
+    region_dims(s, &ni, &nj, &nk);
+    int a = s->cfg.tile_a;
+    if (!a) a = nj >= 32 ? 32 : (nj >= 16 ? 16 : 8);
+    *ta = a;
+    *tb = 32 / a;
+    *npa = (nj + a - 1) / a;
+    *npb = (nk + *tb - 1) / *tb;
+    *npw = ni;
+}
+
+int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, int tmax_steps,
+                  int *d_trace_rec, int *d_trace_n, unsigned int *d_trace_rng) {
+    dnsmc_config &c = s->cfg;
+    if (s->nfields < 1) return fail(DNSMC_ERR_STATE, "no fields: call dnsmc_set_fields first");
+    if (c.model != DNSMC_MODEL_GREY && !s->tab.valid && !s->tab.grey_bands)
+        return fail(DNSMC_ERR_STATE, "no tables: load or set tables first");
+    TRY(set_device(s));
+    const float Tmax = std::max(s->tmax_fields, std::max(c.T_west, c.T_east));
+    const float xm = s->have_x ? (float)(s->xsum / ((double)s->nfields * c.imax * c.jmax * c.kmax)) : 0.f;
+    if (!trace) {
+        CUDA_TRY(cudaEventRecord(s->ev_solve0, s->stream));
+        if (s->tab.grey_bands) { build_grey_band_tables(s->tab, Tmax); s->tables_dirty = true; }
+        s->tmax_used = Tmax;
+        TRY(build_sampling(s, Tmax, xm));
+        if (c.model != DNSMC_MODEL_GREY && s->tables_dirty) TRY(upload_tables(s));
+        if (c.model != DNSMC_MODEL_GREY) {
+            TRY(s->d_entries.ensure(std::max<size_t>(1, s->entries.size())));
+            TRY(s->d_ibw.ensure(s->ibw.size()));
+            CUDA_TRY(cudaMemcpyAsync(s->d_entries.p, s->entries.data(), s->entries.size() * sizeof(SpecEntry), cudaMemcpyHostToDevice, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(s->d_ibw.p, s->ibw.data(), s->ibw.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        }
+        TRY(s->d_group_start.ensure(s->group_start.size()));
+        TRY(s->d_group_empty.ensure(s->group_empty.size()));
+        CUDA_TRY(cudaMemcpyAsync(s->d_group_start.p, s->group_start.data(), s->group_start.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(s->d_group_empty.p, s->group_empty.data(), s->group_empty.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    }
+    const HostTable &t = s->tab;
+    int ni, nj, nk, ta, tb, npa, npb, npw;
+    region_dims(s, &ni, &nj, &nk);
+    tiling(s, &ta, &tb, &npa, &npb, &npw);
+    MarchParams P{};
+    P.nw = c.imax; P.na = c.jmax; P.nb = c.kmax;
+    P.da = s->da; P.db = s->db; P.fw = s->d_fw.p;
+    P.ew0 = s->r_i0; P.ew1 = s->r_i1; P.ea0 = s->r_j0; P.ea1 = s->r_j1; P.eb0 = s->r_k0; P.eb1 = s->r_k1;
+    P.tile_a = ta; P.tile_b = tb; P.npa = npa; P.npb = npb; P.npw = npw;
+    P.n_packets = npa * npb * npw;
+    P.nfields = s->nfields;
+    P.field_stride = (long long)c.imax * c.jmax * c.kmax;
+    int mode = MODE_GREY;
+    if (c.model != DNSMC_MODEL_GREY) mode = (t.nX > 1) ? MODE_TX : MODE_T;
+    s->mode = mode;
+    P.fieldT = (mode == MODE_TX) ? nullptr : s->d_fieldT.p;
+    P.fieldTX = (mode == MODE_TX) ? s->d_fieldTX.p : nullptr;
+    if (mode == MODE_TX && !s->have_x) return fail(DNSMC_ERR_STATE, "table has an x_H2O axis but fields were set without x");
+    if (mode != MODE_TX && s->have_x)
+        return fail(DNSMC_ERR_STATE, "fields carry x_H2O but the spectral model has no x axis: set fields without x");
+    P.nbands = t.nbands; P.nT = t.nT; P.nX = t.nX;
+    P.T0 = t.T0; P.invdT = 1.0f / t.dT; P.X0 = t.X0; P.invdX = 1.0f / t.dX;
+    P.ktab = s->d_k.p; P.ibtab = s->d_ib.p; P.ibw = s->d_ibw.p;
+    P.entries = s->d_entries.p; P.group_start = s->d_group_start.p;
+    P.n_groups = s->n_groups_used;
+    P.kappa = c.kappa;
+    P.Wgrey = (float)(4.0 * c.kappa * kSigma);
+    P.Tw4[0] = c.T_west * c.T_west * c.T_west * c.T_west;
+    P.Tw4[1] = c.T_east * c.T_east * c.T_east * c.T_east;
+    P.rays = s->rays;
+    P.rays_per_packet = s->rays_pp.empty() ? nullptr : s->d_rays_pp.p;
+    P.key0 = (uint32_t)(c.seed & 0xffffffffu);
+    P.key1 = (uint32_t)(c.seed >> 32);
+    P.field_base = 0;
+    P.toll = c.toll;
+    P.max_steps = c.max_steps;
+    P.region_cells = (long long)ni * nj * nk;
+    P.n_items = (long long)s->nfields * P.n_groups * P.n_packets;
+    TRY(s->d_misc.ensure(4));
+    TRY(s->d_counters.ensure(2));
+    P.queue = s->d_misc.p;
+    P.status = s->d_misc.p + 1;
+    P.counters = s->d_counters.p;
+    const int threads = c.block_threads ? c.block_threads : 256;
+    if (trace) {
+        P.trace_f = tf; P.trace_g = tg; P.trace_p = tp; P.trace_r = tr; P.trace_max = tmax_steps;
+        P.trace_rec = d_trace_rec; P.trace_n = d_trace_n; P.trace_rng = d_trace_rng;
+        P.tally = nullptr;
+        const int rc = launch_march(mode, P, 1, 32, s->stream, true);
+        if (rc) return fail(DNSMC_ERR_CUDA, "trace launch: %s", cudaGetErrorString((cudaError_t)rc));
+        return DNSMC_OK;
+    }
+    TRY(s->d_tally.ensure((size_t)s->nfields * P.n_groups * P.region_cells));
+    P.tally = s->d_tally.p;
+    CUDA_TRY(cudaMemsetAsync(s->d_misc.p, 0, 4 * sizeof(unsigned int), s->stream));
+    CUDA_TRY(cudaMemsetAsync(s->d_counters.p, 0, 2 * sizeof(unsigned long long), s->stream));
+    const int sms = device_sm_count();
+    const int occ = march_occupancy(mode, threads);
+    const int blocks = std::max(1, sms * occ);
+    CUDA_TRY(cudaEventRecord(s->ev_march0, s->stream));
+    int rc = launch_march(mode, P, blocks, threads, s->stream, false);
+    if (rc) return fail(DNSMC_ERR_CUDA, "march launch: %s", cudaGetErrorString((cudaError_t)rc));
+    CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
+    s->last = P;
+
+    FinalizeParams F{};
+    F.nfields = s->nfields; F.n_groups = P.n_groups; F.region_cells = P.region_cells;
+    F.niR = ni; F.njR = nj; F.nkR = nk;
+    F.tile_a = ta; F.tile_b = tb; F.npa = npa; F.npb = npb;
+    F.rays = s->rays; F.rays_per_packet = P.rays_per_packet;
+    F.group_empty = s->d_group_empty.p;
+    F.tally = s->d_tally.p;
+    const size_t nout = (size_t)s->nfields * P.region_cells;
+    TRY(s->d_Q.ensure(nout));
+    TRY(s->d_var.ensure(nout));
+    TRY(s->d_Qg.ensure(nout * P.n_groups));
+    TRY(s->d_varg.ensure(nout * P.n_groups));
+    F.Q = s->d_Q.p; F.var = s->d_var.p; F.Qg = s->d_Qg.p; F.varg = s->d_varg.p;
+    F.status = P.status;
+    rc = launch_finalize(F, s->stream);
+    if (rc) return fail(DNSMC_ERR_CUDA, "finalize launch: %s", cudaGetErrorString((cudaError_t)rc));
+    s->lastF = F;
+    TRY(s->h_Q.ensure(nout));
+    TRY(s->h_var.ensure(nout));
+    CUDA_TRY(cudaMemcpyAsync(s->h_Q.p, s->d_Q.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->h_var.p, s->d_var.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaEventRecord(s->ev_done, s->stream));
+    s->in_flight = true;
+    s->solved = true;
+    return DNSMC_OK;
+}
+
+int wait_done(dnsmc_solver *s, double timeout_s) {
+    if (!s->in_flight) return DNSMC_OK;
+    TRY(set_device(s));
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaEventQuery(s->ev_done);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) return fail(DNSMC_ERR_CUDA, "solve failed: %s", cudaGetErrorString(e));
+        if (timeout_s > 0) {
+            const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (el > timeout_s) return fail(DNSMC_ERR_TIMEOUT, "solve still running after %.3f s", timeout_s);
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    s->in_flight = false;
+    CUDA_TRY(cudaEventElapsedTime(&s->march_ms, s->ev_march0, s->ev_march1));
+    CUDA_TRY(cudaEventElapsedTime(&s->solve_ms, s->ev_solve0, s->ev_done));
+    unsigned int misc[4];
+    CUDA_TRY(cudaMemcpy(misc, s->d_misc.p, sizeof misc, cudaMemcpyDeviceToHost));
+    CUDA_TRY(cudaMemcpy(s->h_counters, s->d_counters.p, sizeof s->h_counters, cudaMemcpyDeviceToHost));
+    s->h_status = misc[1];
+    return DNSMC_OK;
+}
+
+int upload_fields_host(dnsmc_solver *s, int nfields, const float *T, const float *x, int layout) {
+    const dnsmc_config &c = s->cfg;
+    const long long ncell = (long long)c.imax * c.jmax * c.kmax;
+    long long si = 1, sj, sk, base, nsrc;
+    if (layout == DNSMC_LAYOUT_DENSE) {
+        sj = c.imax; sk = (long long)c.imax * c.jmax; base = 0; nsrc = ncell;
+    } else if (layout == DNSMC_LAYOUT_FORTRAN) {
+        sj = c.imax + 2; sk = (long long)(c.imax + 2) * (c.jmax + 2);
+        base = 1 + sj + sk;
+        nsrc = (long long)(c.imax + 2) * (c.jmax + 2) * (c.kmax + 2);
+    } else {
+        return fail(DNSMC_ERR_ARG, "unknown layout %d", layout);
+    }
+    // Tmax / Tmin / sum x over interior cells (code/mc_gpu.cu:470-486)
+    float tmax = -1e30f, tmin = 1e30f;
+    double xs = 0.0;
+    bool bad = false;
+    for (int f = 0; f < nfields; ++f)
+        for (int k = 0; k < c.kmax; ++k)
+            for (int j = 0; j < c.jmax; ++j) {
+                const long long o = f * nsrc + base + j * sj + k * sk;
+                for (int i = 0; i < c.imax; ++i) {
+                    const float v = T[o + i];
+                    if (!(v > 0.0f) || !std::isfinite(v)) bad = true;
+                    tmax = std::max(tmax, v);
+                    tmin = std::min(tmin, v);
+                    if (x) xs += x[o + i];
+                }
+            }
+    if (bad) return fail(DNSMC_ERR_ARG, "temperature field has non-positive or non-finite values");
+    TRY(set_device(s));
+    TRY(wait_done(s, 0));
+    const bool want_x = (x != nullptr);
+    TRY(s->h_stage.ensure((size_t)nsrc * (want_x ? 2 : 1)));
+    TRY(s->d_raw.ensure((size_t)nsrc * (want_x ? 2 : 1)));
+    if (want_x) TRY(s->d_fieldTX.ensure((size_t)nfields * ncell));
+    else TRY(s->d_fieldT.ensure((size_t)nfields * ncell));
+    for (int f = 0; f < nfields; ++f) {
+        CUDA_TRY(cudaStreamSynchronize(s->stream));  // staging reuse
+        memcpy(s->h_stage.p, T + f * nsrc, nsrc * sizeof(float));
+        if (want_x) memcpy(s->h_stage.p + nsrc, x + f * nsrc, nsrc * sizeof(float));
+        CUDA_TRY(cudaMemcpyAsync(s->d_raw.p, s->h_stage.p, nsrc * (want_x ? 2 : 1) * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        int rc;
+        if (want_x)
+            rc = launch_pack_TX(s->d_raw.p, s->d_raw.p + nsrc, s->d_fieldTX.p + f * ncell, c.imax, c.jmax, c.kmax, si, sj, sk, base, s->stream);
+        else
+            rc = launch_pack_T(s->d_raw.p, s->d_fieldT.p + f * ncell, c.imax, c.jmax, c.kmax, si, sj, sk, base, s->stream);
+        if (rc) return fail(DNSMC_ERR_CUDA, "pack launch: %s", cudaGetErrorString((cudaError_t)rc));
+    }
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->nfields = nfields;
+    s->have_x = want_x;
+    s->tmax_fields = tmax;
+    s->tmin_fields = tmin;
+    s->xsum = xs;
+    return DNSMC_OK;
+}
+
+std::mutex g_dropin_mu;
+dnsmc_solver *g_dropin = nullptr;
+std::string g_dropin_tables;
+dnsmc_config g_dropin_cfg;
+bool g_dropin_cfg_set = false;
+
+[[noreturn]] void dropin_die(const char *where) {
+    fprintf(stderr, "Fatal error: %s (%s)\n*** FAILED - ABORTING\n", where, dnsmc_last_error());
+    exit(1);
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *dnsmc_last_error(void) { return g_err.c_str(); }
+const char *dnsmc_version(void) { return "dnsmc-gb300 0.1 (sm_103a)"; }
+
+void dnsmc_set_default_config(dnsmc_config *c) {
+    if (!c) return;
+    memset(c, 0, sizeof *c);
+    c->imax = 64; c->jmax = 64; c->kmax = 64; c->p_row = 1;
+    c->Lx = 1.f; c->Ly = 1.f; c->Lz = 1.f;
+    c->stretched_x = 1;
+    c->nvar = 3; c->photmax = 20000;
+    c->T_west = 500.f; c->T_east = 500.f;
+    c->eps_west = 1.f; c->eps_east = 1.f;
+    c->toll = 1.0e-3f;
+    c->max_steps = 100000;
+    c->grid_num = 1;
+    c->model = DNSMC_MODEL_PARTICLE;
+    c->kappa = 1.0f;
+    c->n_groups = 1;
+    c->seed = 1234;
+    c->block_threads = 0;
+    c->tile_a = 0;
+}
+
+int dnsmc_config_from_env(dnsmc_config *c) {
+    if (!c) return fail(DNSMC_ERR_ARG, "null config");
+    struct { const char *name; int *iv; float *fv; } items[] = {
+        {"DNSMC_IMAX", &c->imax, nullptr}, {"DNSMC_JMAX", &c->jmax, nullptr}, {"DNSMC_KMAX", &c->kmax, nullptr},
+        {"DNSMC_PROW", &c->p_row, nullptr}, {"DNSMC_NVAR", &c->nvar, nullptr}, {"DNSMC_PHOTMAX", &c->photmax, nullptr},
+        {"DNSMC_MODEL", &c->model, nullptr}, {"DNSMC_GRID_NUM", &c->grid_num, nullptr},
+        {"DNSMC_STRETCHED", &c->stretched_x, nullptr}, {"DNSMC_GROUPS", &c->n_groups, nullptr},
+        {"DNSMC_LX", nullptr, &c->Lx}, {"DNSMC_LY", nullptr, &c->Ly}, {"DNSMC_LZ", nullptr, &c->Lz},
+        {"DNSMC_TWEST", nullptr, &c->T_west}, {"DNSMC_TEAST", nullptr, &c->T_east},
+        {"DNSMC_KAPPA", nullptr, &c->kappa},
+    };
+    for (auto &it : items) {
+        const char *v = getenv(it.name);
+        if (!v || !*v) continue;
+        char *end = nullptr;
+        if (it.iv) {
+            long x = strtol(v, &end, 10);
+            if (*end) return fail(DNSMC_ERR_ARG, "%s=%s is not an integer", it.name, v);
+            *it.iv = (int)x;
+        } else {
+            float x = strtof(v, &end);
+            if (*end) return fail(DNSMC_ERR_ARG, "%s=%s is not a number", it.name, v);
+            *it.fv = x;
+        }
+    }
+    const char *sd = getenv("DNSMC_SEED");
+    if (sd && *sd) {
+        char *end = nullptr;
+        unsigned long long x = strtoull(sd, &end, 10);
+        if (*end) return fail(DNSMC_ERR_ARG, "DNSMC_SEED=%s is not an integer", sd);
+        c->seed = x;
+    }
+    return DNSMC_OK;
+}
+
+int dnsmc_create(const dnsmc_config *cfg, dnsmc_solver **out) {
+    if (!cfg || !out) return fail(DNSMC_ERR_ARG, "null argument");
+    *out = nullptr;
+    TRY(check_config(*cfg));
+    dnsmc_solver *s = new dnsmc_solver();
+    s->cfg = *cfg;
+    make_faces(cfg->imax, cfg->Lx, cfg->stretched_x, s->fw);
+    s->da = cfg->Ly / (float)cfg->jmax;
+    s->db = cfg->Lz / (float)cfg->kmax;
+    s->r_i0 = 0; s->r_i1 = cfg->imax; s->r_j0 = 0; s->r_j1 = cfg->jmax; s->r_k0 = 0; s->r_k1 = cfg->kmax;
+    s->rays = cfg->nvar * cfg->photmax;
+    if (cfg->model == DNSMC_MODEL_GREY) s->tab.valid = true;
+    *out = s;
+    return DNSMC_OK;
+}
+
+int dnsmc_destroy(dnsmc_solver *s) {
+    if (!s) return DNSMC_OK;
+    if (!s->dev_ready) { delete s; return DNSMC_OK; }
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    s->d_fw.release(); s->d_k.release(); s->d_ib.release(); s->d_ibw.release();
+    s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();
+    s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release();
+    s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
+    s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_Qg.release(); s->d_varg.release();
+    s->h_Q.release(); s->h_var.release(); s->d_misc.release(); s->d_counters.release();
+    if (s->ev_march0) cudaEventDestroy(s->ev_march0);
+    if (s->ev_march1) cudaEventDestroy(s->ev_march1);
+    if (s->ev_done) cudaEventDestroy(s->ev_done);
+    if (s->ev_solve0) cudaEventDestroy(s->ev_solve0);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+    return DNSMC_OK;
+}
+
+int dnsmc_load_tables_ref(dnsmc_solver *s, const char *dir, int model, int nT, int nB, int nQ) {
+    if (!s || !dir) return fail(DNSMC_ERR_ARG, "null argument");
+    if (nT < 2 || nB < 1 || nQ < 1) return fail(DNSMC_ERR_ARG, "bad table sizes");
+    HostTable t;
+    if (model == DNSMC_MODEL_CK) {
+        TRY(read_ck_tables(dir, nT, nB, nQ, t));
+    } else if (model == DNSMC_MODEL_PARTICLE) {
+        TRY(read_particle_tables(dir, nT, nB, t));
+    } else {
+        return fail(DNSMC_ERR_ARG, "dnsmc_load_tables_ref: model must be CK (0) or PARTICLE (2)");
+    }
+    if (!(t.dT > 0)) return fail(DNSMC_ERR_TABLE, "table temperatures are not increasing");
+    t.valid = true;
+    s->tab = std::move(t);
+    s->tables_dirty = true;
+    return DNSMC_OK;
+}
+
+int dnsmc_use_grey_band_tables(dnsmc_solver *s, int nB, int nT, float wvmax, float Tmin) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (nB < 1 || nT < 2 || !(wvmax > 0) || !(Tmin > 0)) return fail(DNSMC_ERR_ARG, "bad grey-band parameters");
+    HostTable t;
+    t.grey_bands = true;
+    t.gb_nB = nB; t.gb_nT = nT; t.gb_wvmax = wvmax; t.gb_Tmin = Tmin; t.gb_kappa = s->cfg.kappa;
+    s->tab = std::move(t);
+    s->tables_dirty = true;
+    return DNSMC_OK;
+}
+
+int dnsmc_set_table(dnsmc_solver *s, const dnsmc_table_desc *d) {
+    if (!s || !d) return fail(DNSMC_ERR_ARG, "null argument");
+    if (d->nbands < 1 || d->nq < 1 || d->nT < 2 || d->nX < 1 || !d->k || !d->wvc)
+        return fail(DNSMC_ERR_ARG, "bad table description");
+    if (d->nbands > 65535) return fail(DNSMC_ERR_ARG, "at most 65535 bands");
+    if (!(d->dT > 0) || (d->nX > 1 && !(d->dX > 0))) return fail(DNSMC_ERR_ARG, "table grid steps must be > 0");
+    if (!d->prob && (!d->dnu || !d->wq)) return fail(DNSMC_ERR_ARG, "dnu and wq are needed without reference CDFs");
+    if (d->prob && !d->kP) return fail(DNSMC_ERR_ARG, "reference sampling needs kP");
+    HostTable t;
+    t.nbands = d->nbands; t.nq = d->nq; t.nT = d->nT; t.nX = d->nX;
+    t.T0 = d->T0; t.dT = d->dT; t.X0 = d->X0; t.dX = d->nX > 1 ? d->dX : 1.0f;
+    const size_t nk = (size_t)t.nbands * t.nq * t.nT * t.nX;
+    t.k.assign(d->k, d->k + nk);
+    for (float v : t.k)
+        if (!(v >= 0) || !std::isfinite(v)) return fail(DNSMC_ERR_TABLE, "absorption coefficients must be finite and >= 0");
+    t.wvc.assign(d->wvc, d->wvc + t.nbands);
+    if (d->dnu) t.dnu.assign(d->dnu, d->dnu + t.nbands); else t.dnu.assign(t.nbands, 0.f);
+    if (d->wq) t.wq.assign(d->wq, d->wq + t.nq); else t.wq.assign(t.nq, 1.0f / t.nq);
+    if (d->Ib) t.Ib.assign(d->Ib, d->Ib + (size_t)t.nbands * t.nT);
+    if (d->prob) {
+        t.prob.assign(d->prob, d->prob + (size_t)t.nT * t.nbands);
+        if (d->probg) t.probg.assign(d->probg, d->probg + (size_t)t.nT * t.nbands * t.nq);
+        t.kP.assign(d->kP, d->kP + t.nT);
+        t.ref_sampling = true;
+    }
+    t.valid = true;
+    s->tab = std::move(t);
+    s->tables_dirty = true;
+    return DNSMC_OK;
+}
+
+int dnsmc_get_table_info(const dnsmc_solver *s, int *nbands, int *nq, int *nT, int *nX, float *T0, float *dT,
+                         float *X0, float *dX) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    const HostTable &t = s->tab;
+    if (nbands) *nbands = t.nbands;
+    if (nq) *nq = t.nq;
+    if (nT) *nT = t.nT;
+    if (nX) *nX = t.nX;
+    if (T0) *T0 = t.T0;
+    if (dT) *dT = t.dT;
+    if (X0) *X0 = t.X0;
+    if (dX) *dX = t.dX;
+    return DNSMC_OK;
+}
+
+int dnsmc_get_table(const dnsmc_solver *s, float *k, float *wvc, float *Ib, float *prob, float *probg, float *kP) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    HostTable t = s->tab;
+    fill_ib(t);
+    if (k) std::copy(t.k.begin(), t.k.end(), k);
+    if (wvc) std::copy(t.wvc.begin(), t.wvc.end(), wvc);
+    if (Ib) std::copy(t.Ib.begin(), t.Ib.end(), Ib);
+    if (prob) std::copy(t.prob.begin(), t.prob.end(), prob);
+    if (probg) std::copy(t.probg.begin(), t.probg.end(), probg);
+    if (kP) std::copy(t.kP.begin(), t.kP.end(), kP);
+    return DNSMC_OK;
+}
+
+int dnsmc_prepare_sampling(dnsmc_solver *s, float Tmax, float xmean) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (!(Tmax > 0)) return fail(DNSMC_ERR_ARG, "Tmax must be > 0");
+    if (s->cfg.model != DNSMC_MODEL_GREY && !s->tab.valid && !s->tab.grey_bands)
+        return fail(DNSMC_ERR_STATE, "no tables: load or set tables first");
+    if (s->tab.grey_bands) { build_grey_band_tables(s->tab, Tmax); s->tables_dirty = true; }
+    s->tmax_used = Tmax;
+    return build_sampling(s, Tmax, xmean);
+}
+
+int dnsmc_set_fields(dnsmc_solver *s, int nfields, const float *T, const float *x, int layout) {
+    if (!s || !T || nfields < 1) return fail(DNSMC_ERR_ARG, "bad arguments");
+    if (nfields > 65535) return fail(DNSMC_ERR_ARG, "at most 65535 fields per solve");
+    return upload_fields_host(s, nfields, T, x, layout);
+}
+
+int dnsmc_set_fields_device(dnsmc_solver *s, int nfields, const float *dT, const float *dx) {
+    if (!s || !dT || nfields < 1) return fail(DNSMC_ERR_ARG, "bad arguments");
+    if (nfields > 65535) return fail(DNSMC_ERR_ARG, "at most 65535 fields per solve");
+    const dnsmc_config &c = s->cfg;
+    const long long ncell = (long long)c.imax * c.jmax * c.kmax;
+    TRY(set_device(s));
+    TRY(wait_done(s, 0));
+    if (dx) TRY(s->d_fieldTX.ensure((size_t)nfields * ncell));
+    else TRY(s->d_fieldT.ensure((size_t)nfields * ncell));
+    for (int f = 0; f < nfields; ++f) {
+        int rc;
+        if (dx)
+            rc = launch_pack_TX(dT + f * ncell, dx + f * ncell, s->d_fieldTX.p + f * ncell, c.imax, c.jmax, c.kmax, 1, c.imax, (long long)c.imax * c.jmax, 0, s->stream);
+        else
+            rc = launch_pack_T(dT + f * ncell, s->d_fieldT.p + f * ncell, c.imax, c.jmax, c.kmax, 1, c.imax, (long long)c.imax * c.jmax, 0, s->stream);
+        if (rc) return fail(DNSMC_ERR_CUDA, "pack launch: %s", cudaGetErrorString((cudaError_t)rc));
+    }
+    TRY(s->d_stat_part.ensure(field_stats_partials()));
+    TRY(s->d_stat_out.ensure(4));
+    int rc = launch_field_stats(dx ? nullptr : s->d_fieldT.p, dx ? s->d_fieldTX.p : nullptr, nfields * ncell, s->d_stat_part.p, s->d_stat_out.p, s->stream);
+    if (rc) return fail(DNSMC_ERR_CUDA, "stats launch: %s", cudaGetErrorString((cudaError_t)rc));
+    float st[3];
+    CUDA_TRY(cudaMemcpyAsync(st, s->d_stat_out.p, sizeof st, cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (!(st[1] > 0) || !std::isfinite(st[0])) return fail(DNSMC_ERR_ARG, "temperature field has non-positive or non-finite values");
+    s->nfields = nfields;
+    s->have_x = dx != nullptr;
+    s->tmax_fields = st[0];
+    s->tmin_fields = st[1];
+    s->xsum = st[2];
+    return DNSMC_OK;
+}
+
+int dnsmc_set_region(dnsmc_solver *s, int i0, int i1, int j0, int j1, int k0, int k1) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    const dnsmc_config &c = s->cfg;
+    if (i0 < 0 || i1 > c.imax || i0 >= i1 || j0 < 0 || j1 > c.jmax || j0 >= j1 || k0 < 0 || k1 > c.kmax || k0 >= k1)
+        return fail(DNSMC_ERR_ARG, "region out of range");
+    TRY(wait_done(s, 0));
+    s->r_i0 = i0; s->r_i1 = i1; s->r_j0 = j0; s->r_j1 = j1; s->r_k0 = k0; s->r_k1 = k1;
+    s->rays_pp.clear();
+    return DNSMC_OK;
+}
+
+int dnsmc_packet_count(const dnsmc_solver *s, int *npackets) {
+    if (!s || !npackets) return fail(DNSMC_ERR_ARG, "null argument");
+    int ta, tb, npa, npb, npw;
+    tiling(s, &ta, &tb, &npa, &npb, &npw);
+    *npackets = npa * npb * npw;
+    return DNSMC_OK;
+}
+
+int dnsmc_set_rays(dnsmc_solver *s, int rays_per_group, const int *rays_per_packet) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (rays_per_group < 1 && !rays_per_packet) return fail(DNSMC_ERR_ARG, "rays must be >= 1");
+    TRY(set_device(s));
+    TRY(wait_done(s, 0));
+    s->rays = rays_per_group;
+    if (rays_per_packet) {
+        int np;
+        TRY(dnsmc_packet_count(s, &np));
+        for (int i = 0; i < np; ++i)
+            if (rays_per_packet[i] < 0) return fail(DNSMC_ERR_ARG, "negative ray count");
+        s->rays_pp.assign(rays_per_packet, rays_per_packet + np);
+        TRY(s->d_rays_pp.ensure(np));
+        CUDA_TRY(cudaMemcpy(s->d_rays_pp.p, s->rays_pp.data(), np * sizeof(int), cudaMemcpyHostToDevice));
+    } else {
+        s->rays_pp.clear();
+    }
+    return DNSMC_OK;
+}
+
+int dnsmc_solve_async(dnsmc_solver *s) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    TRY(wait_done(s, 0));
+    return solve_enqueue(s, false, 0, 0, 0, 0, 0, nullptr, nullptr, nullptr);
+}
+
+int dnsmc_wait(dnsmc_solver *s, double timeout_s) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    return wait_done(s, timeout_s);
+}
+
+int dnsmc_get_results(dnsmc_solver *s, double *Q, double *sigma) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (!s->solved) return fail(DNSMC_ERR_STATE, "no solve has been run");
+    TRY(wait_done(s, 0));
+    const size_t n = (size_t)s->nfields * s->last.region_cells;
+    if (Q) memcpy(Q, s->h_Q.p, n * sizeof(double));
+    if (sigma)
+        for (size_t i = 0; i < n; ++i) sigma[i] = sqrt(s->h_var.p[i]);
+    return DNSMC_OK;
+}
+
+int dnsmc_get_group_results(dnsmc_solver *s, double *Qg, double *varg) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (!s->solved) return fail(DNSMC_ERR_STATE, "no solve has been run");
+    TRY(wait_done(s, 0));
+    TRY(set_device(s));
+    const size_t n = (size_t)s->nfields * s->last.region_cells * s->last.n_groups;
+    if (Qg) CUDA_TRY(cudaMemcpy(Qg, s->d_Qg.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (varg) CUDA_TRY(cudaMemcpy(varg, s->d_varg.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return DNSMC_OK;
+}
+
+int dnsmc_status(dnsmc_solver *s, uint32_t *status) {
+    if (!s || !status) return fail(DNSMC_ERR_ARG, "null argument");
+    TRY(wait_done(s, 0));
+    *status = s->h_status;
+    return DNSMC_OK;
+}
+
+int dnsmc_get_counters(dnsmc_solver *s, double *rays, double *steps, double *march_ms) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    TRY(wait_done(s, 0));
+    if (rays) *rays = (double)s->h_counters[0];
+    if (steps) *steps = (double)s->h_counters[1];
+    if (march_ms) *march_ms = s->march_ms;
+    return DNSMC_OK;
+}
+
+int dnsmc_get_timing(dnsmc_solver *s, double *solve_ms, double *march_ms) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    TRY(wait_done(s, 0));
+    if (solve_ms) *solve_ms = s->solve_ms;
+    if (march_ms) *march_ms = s->march_ms;
+    return DNSMC_OK;
+}
+
+int dnsmc_get_tmax(const dnsmc_solver *s, float *tmax) {
+    if (!s || !tmax) return fail(DNSMC_ERR_ARG, "null argument");
+    *tmax = s->tmax_used;
+    return DNSMC_OK;
+}
+
+int dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *group_start, int *n_entries, float *prob,
+                       int *alias, int *band, int *gq, float *W, float *ibw) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (n_groups) *n_groups = s->n_groups_used;
+    if (group_start) std::copy(s->group_start.begin(), s->group_start.end(), group_start);
+    if (n_entries) *n_entries = (int)s->entries.size();
+    const int nq = std::max(1, s->tab.nq);
+    for (size_t i = 0; i < s->entries.size(); ++i) {
+        const SpecEntry &e = s->entries[i];
+        if (prob) prob[i] = e.prob;
+        if (alias) alias[i] = (int)(e.alias_nb & 0xFFFFu);
+        if (band) band[i] = (int)(e.alias_nb >> 16);
+        if (gq) gq[i] = (int)((e.koff / (s->tab.nT * s->tab.nX)) % nq);
+        if (W) W[i] = e.W;
+    }
+    if (ibw) std::copy(s->ibw.begin(), s->ibw.end(), ibw);
+    return DNSMC_OK;
+}
+
+int dnsmc_get_geometry(const dnsmc_solver *s, float *xu, float *dy, float *dz) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (xu) std::copy(s->fw.begin(), s->fw.end(), xu);
+    if (dy) *dy = s->da;
+    if (dz) *dz = s->db;
+    return DNSMC_OK;
+}
+
+int dnsmc_trace_ray(dnsmc_solver *s, int f, int g, int p, int r, int max_steps, int32_t *rec, int *n_steps,
+                    uint32_t *rng4) {
+    if (!s || !rec || !n_steps || max_steps < 1) return fail(DNSMC_ERR_ARG, "bad arguments");
+    if (!s->solved) return fail(DNSMC_ERR_STATE, "trace needs a prior solve (sampling tables)");
+    TRY(wait_done(s, 0));
+    if (f < 0 || f >= s->nfields || g < 0 || g >= s->n_groups_used || r < 0) return fail(DNSMC_ERR_ARG, "trace index out of range");
+    int np;
+    TRY(dnsmc_packet_count(s, &np));
+    if (p < 0 || p >= np) return fail(DNSMC_ERR_ARG, "packet out of range");
+    if (s->mode != MODE_GREY && s->group_empty[g]) return fail(DNSMC_ERR_ARG, "band group is empty");
+    TRY(set_device(s));
+    int *d_rec = nullptr, *d_n = nullptr;
+    unsigned int *d_rng = nullptr;
+    CUDA_TRY(cudaMalloc((void **)&d_rec, (size_t)max_steps * 6 * sizeof(int)));
+    cudaMalloc((void **)&d_n, sizeof(int));
+    cudaMalloc((void **)&d_rng, 4 * sizeof(unsigned int));
+    int rc = solve_enqueue(s, true, f, g, p, r, max_steps, d_rec, d_n, d_rng);
+    if (rc == DNSMC_OK) {
+        cudaError_t e = cudaStreamSynchronize(s->stream);
+        if (e != cudaSuccess) rc = fail(DNSMC_ERR_CUDA, "trace: %s", cudaGetErrorString(e));
+    }
+    if (rc == DNSMC_OK) {
+        cudaMemcpy(n_steps, d_n, sizeof(int), cudaMemcpyDeviceToHost);
+        const int nrec = std::min(*n_steps, max_steps);
+        cudaMemcpy(rec, d_rec, (size_t)nrec * 6 * sizeof(int), cudaMemcpyDeviceToHost);
+        if (rng4) cudaMemcpy(rng4, d_rng, 4 * sizeof(unsigned int), cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d_rec);
+    cudaFree(d_n);
+    cudaFree(d_rng);
+    return rc;
+}
+
+// ---- reference drop-in ------------------------------------------------------
+int dnsmc_dropin_configure(const dnsmc_config *cfg, const char *table_dir) {
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (g_dropin) { dnsmc_destroy(g_dropin); g_dropin = nullptr; }
+    if (cfg) {
+        TRY(check_config(*cfg));
+        g_dropin_cfg = *cfg;
+        g_dropin_cfg_set = true;
+    } else {
+        g_dropin_cfg_set = false;
+    }
+    g_dropin_tables = table_dir ? table_dir : "";
+    return DNSMC_OK;
+}
+
+int dnsmc_dropin_release(void) {
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (g_dropin) dnsmc_destroy(g_dropin);
+    g_dropin = nullptr;
+    return DNSMC_OK;
+}
+
+void mc_gpu_(float *Tfort, int *ystart) {
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!Tfort || !ystart) { fail(DNSMC_ERR_ARG, "null argument"); dropin_die("mc_gpu_"); }
+    if (!g_dropin) {
+        dnsmc_config c;
+        if (g_dropin_cfg_set) {
+            c = g_dropin_cfg;
+        } else {
+            dnsmc_set_default_config(&c);
+            if (dnsmc_config_from_env(&c)) dropin_die("mc_gpu_ configuration");
+        }
+        if (dnsmc_create(&c, &g_dropin)) dropin_die("mc_gpu_ set-up");
+        std::string dir = g_dropin_tables;
+        if (dir.empty()) { const char *e = getenv("DNSMC_TABLES"); dir = e && *e ? e : "../distr/tables"; }
+        int rc = DNSMC_OK;
+        if (c.model == DNSMC_MODEL_CK) rc = dnsmc_load_tables_ref(g_dropin, dir.c_str(), DNSMC_MODEL_CK, 52, 119, 16);
+        else if (c.model == DNSMC_MODEL_PARTICLE) rc = dnsmc_load_tables_ref(g_dropin, dir.c_str(), DNSMC_MODEL_PARTICLE, 52, 119, 1);
+        else if (c.model == DNSMC_MODEL_GREY_BANDS) rc = dnsmc_use_grey_band_tables(g_dropin, 1000, 55, 15000.f, 500.f);
+        else if (c.model == DNSMC_MODEL_TABLE) rc = fail(DNSMC_ERR_STATE, "the drop-in pair cannot use a raw table");
+        if (rc) dropin_die("mc_gpu_ tables");
+    }
+    const dnsmc_config &c = g_dropin->cfg;
+    const int jl = c.jmax / c.p_row;
+    const int j0 = *ystart - 1;
+    if (j0 < 0 || j0 + jl > c.jmax) { fail(DNSMC_ERR_ARG, "ystart %d out of range", *ystart); dropin_die("mc_gpu_"); }
+    if (dnsmc_set_fields(g_dropin, 1, Tfort, nullptr, DNSMC_LAYOUT_FORTRAN)) dropin_die("mc_gpu_ fields");
+    if (g_dropin->r_j0 != j0 || g_dropin->r_j1 != j0 + jl)
+        if (dnsmc_set_region(g_dropin, 0, c.imax, j0, j0 + jl, 0, c.kmax)) dropin_die("mc_gpu_ region");
+    if (dnsmc_solve_async(g_dropin)) dropin_die("mc_gpu_ launch");
+}
+
+void get_results_(float *resfort, float *varfort) {
+    std::lock_guard<std::mutex> lk(g_dropin_mu);
+    if (!g_dropin || !g_dropin->solved) { fail(DNSMC_ERR_STATE, "get_results_ before mc_gpu_"); dropin_die("get_results_"); }
+    if (wait_done(g_dropin, 0)) dropin_die("get_results_");
+    const dnsmc_config &c = g_dropin->cfg;
+    const int jl = c.jmax / c.p_row;
+    const double vscale = c.nvar > 1 ? (double)c.nvar / (c.nvar - 0.5) : 1.0;
+    const double *Q = g_dropin->h_Q.p, *V = g_dropin->h_var.p;
+    for (int k = 1; k <= c.kmax; ++k)
+        for (int j = 1; j <= jl; ++j)
+            for (int i = 1; i <= c.imax; ++i) {
+                const size_t src = (size_t)(i - 1) + (size_t)c.imax * ((j - 1) + (size_t)jl * (k - 1));
+                const size_t dst = (size_t)i + (size_t)(c.imax + 2) * (j + (size_t)(jl + 2) * k);
+                if (resfort) resfort[dst] = (float)Q[src];
+                if (varfort) varfort[dst] = (float)sqrt(V[src] * vscale);
+            }
+}
+
+}  // extern "C"

@@ -1,0 +1,110 @@
+// mc_internal.h -- data layout and kernel interface shared by the host runtime
+// (mc_host.cpp) and the device code (mc_kernels.cu).
+//
+// Device layout (HBM):
+//   field  : [f][i][k][j] with j fastest (the periodic axis the 32 lanes of a
+//            packet tile), float T or float2 (T, x_H2O);
+//   k table: [band][g][t][x] float, one contiguous nT*nX slice per spectral
+//            sample (band, g) so a warp-uniform sample reads one slice;
+//   Ib     : [band][t] float;  Ib_wall: [2][band] float (west, east);
+//   tally  : [f][group][iR][kR][jR] double2 (sum X, sum X^2) over the rays of
+//            one (cell, group) work item, j fastest so a packet stores 512
+//            contiguous bytes.
+#pragma once
+#include <cstdint>
+
+namespace dnsmc {
+
+enum MarchMode { MODE_GREY = 0, MODE_T = 1, MODE_TX = 2 };
+
+// One alias-table entry of a spectral sample (band, g) inside a band group.
+struct SpecEntry {
+    float    prob;      // alias threshold (quantised to multiples of 2^-24)
+    uint32_t alias_nb;  // alias index (low 16 bits) | band (high 16 bits)
+    int32_t  koff;      // offset of the (band, g) slice in the k table
+    float    W;         // ray weight factor: w = W * k(T_i) * Ib(T_i)
+};
+
+struct MarchParams {
+    // geometry: nw wall-normal cells (reference i), na (j) and nb (k) periodic
+    int nw, na, nb;
+    float da, db;             // periodic cell sizes
+    const float *fw;          // nw+1 wall-normal faces
+    // emission region (cells computed) and packet tiling
+    int ew0, ew1, ea0, ea1, eb0, eb1;
+    int tile_a, tile_b;       // tile_a * tile_b == 32
+    int npa, npb, npw;        // packets along j, k, i
+    int n_packets;            // npa * npb * npw
+    int nfields;
+    long long field_stride;   // cells per field (nw*na*nb)
+    const float  *fieldT;     // MODE_GREY / MODE_T
+    const float2 *fieldTX;    // MODE_TX
+    // spectral tables
+    int nbands, nT, nX;
+    float T0, invdT, X0, invdX;
+    const float *ktab;        // [band][g][t][x]
+    const float *ibtab;       // [band][t]
+    const float *ibw;         // [2][band]
+    const SpecEntry *entries;
+    const int *group_start;   // n_groups + 1
+    int n_groups;
+    // grey model
+    float kappa;              // absorption coefficient
+    float Wgrey;              // 4 * kappa * sigma
+    float Tw4[2];             // wall T^4 (west, east), grey model
+    // rays
+    int rays;                 // rays per (cell, group) when rays_per_packet == 0
+    const int *rays_per_packet;
+    uint32_t key0, key1;      // Philox key (seed)
+    uint32_t field_base;      // field index offset for the RNG counter
+    float toll;
+    int max_steps;
+    // work queue and outputs
+    unsigned int *queue;      // atomic item counter (zeroed per launch)
+    long long n_items;
+    double2 *tally;           // see layout above
+    long long region_cells;   // (ew1-ew0)*(ea1-ea0)*(eb1-eb0)
+    unsigned int *status;     // DNSMC_STATUS_* bits
+    unsigned long long *counters;  // [0] rays (lane-rays), [1] lane-steps
+    // trace (trace launches only)
+    int trace_f, trace_g, trace_p, trace_r, trace_max;
+    int *trace_rec;           // 6 words per step
+    int *trace_n;
+    unsigned int *trace_rng;
+};
+
+struct FinalizeParams {
+    int nfields, n_groups;
+    long long region_cells;
+    int niR, njR, nkR;        // region extents (i, j, k)
+    int tile_a, tile_b, npa, npb;
+    int rays;
+    const int *rays_per_packet;
+    const int *group_empty;   // 1 when the group has no emission
+    const double2 *tally;
+    double *Q;                // [f][cell] dense region, i fastest
+    double *var;              // [f][cell]
+    double *Qg;               // [f][group][cell] or nullptr
+    double *varg;             // [f][group][cell] or nullptr
+    unsigned int *status;
+};
+
+// launchers (mc_kernels.cu); all stream-ordered
+int launch_march(int mode, const MarchParams &p, int blocks, int threads,
+                 void *stream, bool trace);
+int launch_finalize(const FinalizeParams &p, void *stream);
+// src element (i, j, k) at src[base + i*si + j*sj + k*sk]; writes dst[f] layout
+int launch_pack_T(const float *src, float *dst, int nw, int na, int nb,
+                  long long si, long long sj, long long sk, long long base,
+                  void *stream);
+int launch_pack_TX(const float *srcT, const float *srcX, float2 *dst, int nw,
+                   int na, int nb, long long si, long long sj, long long sk,
+                   long long base, void *stream);
+// max T, min T, sum x over n cells into out[0..2] (device), deterministic
+int launch_field_stats(const float *fT, const float2 *fTX, long long n,
+                       double *partials, float *out, void *stream);
+int field_stats_partials();   // doubles needed in `partials`
+int march_occupancy(int mode, int threads);  // resident blocks per SM
+int device_sm_count();
+
+}  // namespace dnsmc

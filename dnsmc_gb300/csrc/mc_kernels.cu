@@ -1,0 +1,557 @@
+// mc_kernels.cu -- sm_103a device code of the reverse (emission-based, OERM)
+// Monte Carlo radiative-source solver.
+//
+// Replaces kernel_fluid / march_ray / find_band / emiss_ang / kernel_results
+// of the reference (code/mc_gpu.cu:44-438, :813-896, :959-970) with one
+// persistent work-queue kernel built around "packets":
+//
+//   * a packet is 32 cells that share the wall-normal index i and tile the
+//     periodic (j, k) plane (tile_a x tile_b, j fastest in memory);
+//   * one warp owns a packet; lane l owns cell l and keeps that cell's FP64
+//     tallies in registers, so no reduction is needed;
+//   * every ray of the packet shares one Philox draw: the isotropic direction
+//     (reference emiss_ang, code/mc_gpu.cu:813-820) and the spectral sample
+//     (band, g) drawn from an alias table (reference find_band, :830-896).
+//     The reference already shares its Sobol direction sequence across all
+//     cells (code/mc_gpu.cu:80-81).  Because the origins differ by whole
+//     periodic cells, the voxel walk (which face is crossed next, and the
+//     segment length) is identical in all 32 lanes: the DDA is warp-uniform,
+//     lanes only offset their (j, k) indices.  Field gathers of the 32 lanes
+//     are contiguous (256 B per step for float2 fields) and the spectral
+//     table slice is the same for the whole warp.
+//   * per segment each lane does the OERM update of march_ray
+//     (code/mc_gpu.cu:264-276): alpha = 1 - exp(-k ds),
+//     D += tau*alpha*(Ib_i - Ib_j)/Ib_i, tau *= 1 - alpha, the remainder is
+//     dumped when tau < toll, black walls add tau*(Ib_i - Ib_w)/Ib_i
+//     (code/mc_gpu.cu:297,314).  The ray contribution is X = W*k_i*Ib_i*D.
+//
+// Arithmetic is FP32 with explicit fmaf and the file is compiled with
+// -fmad=false, so the host replay reproduces every ray bit for bit; exp and
+// sin/cos are the project's own polynomial kernels (mc_expm1 / mc_sincos) for
+// the same reason.  Tallies (sum X, sum X^2) are FP64.
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "mc_internal.h"
+#include "../../include/dnsmc.h"
+
+namespace dnsmc {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC'11).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    }
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// expm1 for x <= 0: Cody-Waite reduction x = n*ln2 + r, |r| <= ln2/2, Taylor
+// series of expm1(r) to r^8/8!, then 2^n*expm1(r) + (2^n - 1).  Only +, *,
+// fmaf and rintf: bit-identical on any IEEE-754 machine.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float mc_expm1(float x) {
+    x = fmaxf(x, -87.0f);
+    const float n = rintf(x * 1.44269504088896341f);
+    float r = fmaf(-n, 0.693145751953125f, x);
+    r = fmaf(-n, 1.42860682030941723212e-6f, r);
+    float p = 2.48015873015873016e-5f;             // 1/8!
+    p = fmaf(p, r, 1.98412698412698413e-4f);       // 1/7!
+    p = fmaf(p, r, 1.38888888888888889e-3f);       // 1/6!
+    p = fmaf(p, r, 8.33333333333333333e-3f);       // 1/5!
+    p = fmaf(p, r, 4.16666666666666667e-2f);       // 1/4!
+    p = fmaf(p, r, 1.66666666666666667e-1f);       // 1/3!
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = p * r;                                     // expm1(r)
+    const int ni = (int)n;                         // in [-126, 0]
+    const float two_n = __int_as_float((ni + 127) << 23);
+    return fmaf(two_n, p, two_n - 1.0f);
+}
+
+// sin and cos of x in [0, pi/4]: Taylor series to x^11 / x^12.
+__device__ __forceinline__ void mc_sincos_oct(float x, float *s, float *c) {
+    const float z = x * x;
+    float ps = -2.50521083854417188e-8f;           // -1/11!
+    ps = fmaf(ps, z, 2.75573192239858907e-6f);     //  1/9!
+    ps = fmaf(ps, z, -1.98412698412698413e-4f);    // -1/7!
+    ps = fmaf(ps, z, 8.33333333333333333e-3f);     //  1/5!
+    ps = fmaf(ps, z, -1.66666666666666667e-1f);    // -1/3!
+    *s = fmaf(ps * z, x, x);
+    float pc = 2.08767569878680990e-9f;            //  1/12!
+    pc = fmaf(pc, z, -2.75573192239858907e-7f);    // -1/10!
+    pc = fmaf(pc, z, 2.48015873015873016e-5f);     //  1/8!
+    pc = fmaf(pc, z, -1.38888888888888889e-3f);    // -1/6!
+    pc = fmaf(pc, z, 4.16666666666666667e-2f);     //  1/4!
+    pc = fmaf(pc, z, -0.5f);
+    *c = fmaf(pc, z, 1.0f);
+}
+
+// cos and sin of 2*pi*m/2^24 for a 24-bit integer m: exact quadrant and
+// octant reduction on the integer, polynomial on [0, pi/4].
+__device__ __forceinline__ void mc_sincos_turn(uint32_t m, float *cs, float *sn) {
+    const uint32_t q = m >> 22;
+    const uint32_t r = m & 0x3FFFFFu;
+    const bool hi = r > 0x200000u;
+    const float th = (float)(hi ? (0x400000u - r) : r) * 3.74507028e-7f;  // pi*2^-23
+    float s, c;
+    mc_sincos_oct(th, &s, &c);
+    const float cq = hi ? s : c, sq = hi ? c : s;
+    float co, si;
+    switch (q) {
+        case 0: co = cq;  si = sq;  break;
+        case 1: co = -sq; si = cq;  break;
+        case 2: co = -cq; si = -sq; break;
+        default: co = sq; si = -cq; break;
+    }
+    *cs = co; *sn = si;
+}
+
+__device__ __forceinline__ float u24(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
+
+// Linear position in a uniform grid of n points, clamped as the reference's
+// clamp-addressed linear-filter textures (code/memory_copy.cu:245-247).
+__device__ __forceinline__ void grid_pos(float v, float v0, float inv, int n, int *i, float *f) {
+    float p = (v - v0) * inv;
+    p = fminf(fmaxf(p, 0.0f), (float)(n - 1));
+    int ii = (int)p;
+    ii = min(ii, n - 2);
+    *i = ii;
+    *f = p - (float)ii;
+}
+
+template <int MODE>
+__device__ __forceinline__ float lookup_k(const MarchParams &P, int koff, int ti, float ft, int xi, float fx) {
+    if (MODE == MODE_TX) {
+        const float *s = P.ktab + koff + ti * P.nX + xi;
+        const float k00 = __ldg(s), k01 = __ldg(s + 1);
+        const float k10 = __ldg(s + P.nX), k11 = __ldg(s + P.nX + 1);
+        const float k0 = fmaf(fx, k01 - k00, k00);
+        const float k1 = fmaf(fx, k11 - k10, k10);
+        return fmaf(ft, k1 - k0, k0);
+    } else {
+        const float *s = P.ktab + koff + ti;
+        const float k0 = __ldg(s), k1 = __ldg(s + 1);
+        return fmaf(ft, k1 - k0, k0);
+    }
+}
+
+__device__ __forceinline__ float lookup_ib(const MarchParams &P, int nb, int ti, float ft) {
+    const float *s = P.ibtab + nb * P.nT + ti;
+    const float i0 = __ldg(s), i1 = __ldg(s + 1);
+    return fmaf(ft, i1 - i0, i0);
+}
+
+// ---------------------------------------------------------------------------
+// The march kernel.  Persistent: every warp pulls work items (field, band
+// group, packet) from an atomic counter until the queue is empty.
+// ---------------------------------------------------------------------------
+template <int MODE, bool TRACE>
+__global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int la = lane % P.tile_a, lb = lane / P.tile_a;
+    const int njR = P.ea1 - P.ea0, nkR = P.eb1 - P.eb0;
+    const long long plane = (long long)P.na * P.nb;
+    unsigned long long my_rays = 0, my_steps = 0;
+    unsigned int flags = 0;
+
+    for (;;) {
+        long long item;
+        if (TRACE) {
+            if (threadIdx.x >= 32) return;
+            item = ((long long)P.trace_f * P.n_groups + P.trace_g) * P.n_packets + P.trace_p;
+        } else {
+            unsigned int it = 0;
+            if (lane == 0) it = atomicAdd(P.queue, 1u);
+            it = __shfl_sync(FULL, it, 0);
+            if ((long long)it >= P.n_items) break;
+            item = it;
+        }
+        const int p = (int)(item % P.n_packets);
+        const long long fg = item / P.n_packets;
+        const int G = (int)(fg % P.n_groups);
+        const int f = (int)(fg / P.n_groups);
+        const int pa = p % P.npa;
+        const int rest = p / P.npa;
+        const int pb = rest % P.npb;
+        const int pw = rest / P.npb;
+        const int w0 = P.ew0 + pw;
+        const int a0 = P.ea0 + pa * P.tile_a + la;
+        const int b0 = P.eb0 + pb * P.tile_b + lb;
+        const bool active = (a0 < P.ea1) && (b0 < P.eb1);
+        const int acl = active ? a0 : P.ea0, bcl = active ? b0 : P.eb0;
+        const int N = P.rays_per_packet ? P.rays_per_packet[p] : P.rays;
+        int gs = 0, K = 1;
+        if (MODE != MODE_GREY) { gs = P.group_start[G]; K = P.group_start[G + 1] - gs; }
+
+        const long long fbase = (long long)f * P.field_stride;
+        const long long own = fbase + (long long)w0 * plane + (long long)bcl * P.na + acl;
+        // own-cell quantities
+        float Ti, Ti4 = 0.f, invTi4 = 0.f;
+        int ti_i = 0, xi_i = 0;
+        float ft_i = 0.f, fx_i = 0.f;
+        if (MODE == MODE_TX) {
+            const float2 v = __ldg(P.fieldTX + own);
+            Ti = v.x;
+            grid_pos(v.y, P.X0, P.invdX, P.nX, &xi_i, &fx_i);
+        } else {
+            Ti = __ldg(P.fieldT + own);
+        }
+        if (!(Ti > 0.0f) && active) flags |= DNSMC_STATUS_BAD_FIELD;
+        if (MODE == MODE_GREY) {
+            const float t2 = Ti * Ti;
+            Ti4 = t2 * t2;
+            invTi4 = Ti4 > 0.f ? 1.0f / Ti4 : 0.f;
+        } else {
+            grid_pos(Ti, P.T0, P.invdT, P.nT, &ti_i, &ft_i);
+        }
+        const float oW = (__ldg(P.fw + w0) + __ldg(P.fw + w0 + 1)) * 0.5f;
+
+        double S = 0.0, S2 = 0.0;
+        const int rbeg = TRACE ? P.trace_r : 0;
+        const int rend = TRACE ? P.trace_r + 1 : ((K > 0) ? N : 0);
+        for (int r = rbeg; r < rend; ++r) {
+            const uint4 x = philox4x32_10(
+                make_uint4((uint32_t)r, (uint32_t)p,
+                           (uint32_t)G | ((uint32_t)(f + P.field_base) << 16), 0u),
+                P.key0, P.key1);
+            if (TRACE && lane == 0) {
+                P.trace_rng[0] = x.x; P.trace_rng[1] = x.y; P.trace_rng[2] = x.z; P.trace_rng[3] = x.w;
+            }
+            // isotropic direction: cos(theta) = 1 - 2u, phi = 2*pi*u'
+            const float mu = fmaf((float)(x.y >> 8), -1.1920928955078125e-7f, 1.0f);
+            const float st = sqrtf(fmaxf(0.0f, fmaf(-mu, mu, 1.0f)));
+            float cph, sph;
+            mc_sincos_turn(x.x >> 8, &cph, &sph);
+            const float sW = mu, sA = st * cph, sB = st * sph;
+
+            // spectral sample and ray weight
+            float w, Ii, invI;
+            int nbnd = 0, koff = 0;
+            if (MODE == MODE_GREY) {
+                Ii = Ti4;
+                invI = invTi4;
+                w = P.Wgrey * Ti4;
+            } else {
+                const int j = (int)__umulhi(x.z, (uint32_t)K);
+                SpecEntry e = P.entries[gs + j];
+                if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
+                nbnd = (int)(e.alias_nb >> 16);
+                koff = e.koff;
+                const float ki = lookup_k<MODE>(P, koff, ti_i, ft_i, xi_i, fx_i);
+                Ii = lookup_ib(P, nbnd, ti_i, ft_i);
+                invI = Ii > 0.f ? 1.0f / Ii : 0.f;
+                w = e.W * ki * Ii;
+            }
+
+            // warp-uniform DDA set-up (origin at the cell centre)
+            const float invW = 1.0f / fabsf(sW), invA = 1.0f / fabsf(sA), invB = 1.0f / fabsf(sB);
+            const int dW = sW > 0.f ? 1 : -1, dA = sA > 0.f ? 1 : -1, dB = sB > 0.f ? 1 : -1;
+            float tW = (dW > 0 ? (__ldg(P.fw + w0 + 1) - oW) : (oW - __ldg(P.fw + w0))) * invW;
+            const float dtA = P.da * invA, dtB = P.db * invB;
+            float tA = 0.5f * dtA, tB = 0.5f * dtB;
+            int nA = 0, nB = 0;
+            float t = 0.0f;
+            int cw = w0, ca = acl, cb = bcl;
+            long long rowW = fbase + (long long)w0 * plane;
+            long long rowB = (long long)cb * P.na;
+            float tau = active ? 1.0f : 0.0f;
+            float D = 0.0f;
+            int steps = 0;
+            for (;;) {
+                int axis;
+                float tn;
+                if (tW <= tA && tW <= tB) { axis = 0; tn = tW; }
+                else if (tA <= tB)         { axis = 1; tn = tA; }
+                else                       { axis = 2; tn = tB; }
+                const float ds = tn - t;
+                if (tau > 0.0f) {
+                    ++my_steps;
+                    const long long cell = rowW + rowB + ca;
+                    float kj, gj;
+                    if (MODE == MODE_GREY) {
+                        const float Tj = __ldg(P.fieldT + cell);
+                        const float t2 = Tj * Tj;
+                        gj = (Ti4 - t2 * t2) * invI;
+                        kj = P.kappa;
+                    } else {
+                        int tj, xj = 0;
+                        float ftj, fxj = 0.f, Tj;
+                        if (MODE == MODE_TX) {
+                            const float2 v = __ldg(P.fieldTX + cell);
+                            Tj = v.x;
+                            grid_pos(v.y, P.X0, P.invdX, P.nX, &xj, &fxj);
+                        } else {
+                            Tj = __ldg(P.fieldT + cell);
+                        }
+                        grid_pos(Tj, P.T0, P.invdT, P.nT, &tj, &ftj);
+                        kj = lookup_k<MODE>(P, koff, tj, ftj, xj, fxj);
+                        const float Ibj = lookup_ib(P, nbnd, tj, ftj);
+                        gj = (Ii - Ibj) * invI;
+                    }
+                    const float alpha = -mc_expm1(-(kj * ds));
+                    const float ta = tau * alpha;
+                    D = fmaf(ta, gj, D);
+                    tau = tau - ta;
+                    if (tau < P.toll) { D = fmaf(tau, gj, D); tau = 0.0f; }
+                }
+                if (TRACE && lane == 0 && steps < P.trace_max) {
+                    int *rec = P.trace_rec + 6 * steps;
+                    rec[0] = cw; rec[1] = dA * nA; rec[2] = dB * nB; rec[3] = axis;
+                    rec[4] = __float_as_int(ds); rec[5] = __float_as_int(tau);
+                }
+                t = tn;
+                ++steps;
+                if (axis == 0) {
+                    cw += dW;
+                    if (cw < 0 || cw >= P.nw) {
+                        if (tau > 0.0f) {
+                            const int side = cw < 0 ? 0 : 1;
+                            const float Iw = (MODE == MODE_GREY) ? P.Tw4[side]
+                                                                 : __ldg(P.ibw + side * P.nbands + nbnd);
+                            D = fmaf(tau, (Ii - Iw) * invI, D);
+                            tau = 0.0f;
+                        }
+                        break;
+                    }
+                    tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - oW) : (oW - __ldg(P.fw + cw))) * invW;
+                    rowW = fbase + (long long)cw * plane;
+                } else if (axis == 1) {
+                    ++nA;
+                    tA = ((float)nA + 0.5f) * dtA;
+                    ca += dA;
+                    if (ca == P.na) ca = 0; else if (ca < 0) ca = P.na - 1;
+                } else {
+                    ++nB;
+                    tB = ((float)nB + 0.5f) * dtB;
+                    cb += dB;
+                    if (cb == P.nb) cb = 0; else if (cb < 0) cb = P.nb - 1;
+                    rowB = (long long)cb * P.na;
+                }
+                if (!__any_sync(FULL, tau > 0.0f)) break;
+                if (steps >= P.max_steps) {
+                    if (tau > 0.0f) flags |= DNSMC_STATUS_STEP_CAP;
+                    break;
+                }
+            }
+            if (TRACE && lane == 0) *P.trace_n = steps;
+            const float X = w * D;
+            if (active) {
+                ++my_rays;
+                if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
+                const double Xd = (double)X;
+                S += Xd;
+                S2 = fma(Xd, Xd, S2);
+            }
+        }
+        if (TRACE) return;
+        if (active) {
+            const long long tc = ((long long)(w0 - P.ew0) * nkR + (b0 - P.eb0)) * njR + (a0 - P.ea0);
+            P.tally[fg * P.region_cells + tc] = make_double2(S, S2);
+        }
+    }
+    // per-warp counters and status
+    for (int o = 16; o > 0; o >>= 1) {
+        my_rays += __shfl_xor_sync(FULL, my_rays, o);
+        my_steps += __shfl_xor_sync(FULL, my_steps, o);
+        flags |= __shfl_xor_sync(FULL, flags, o);
+    }
+    if (lane == 0) {
+        if (my_rays) atomicAdd(P.counters + 0, my_rays);
+        if (my_steps) atomicAdd(P.counters + 1, my_steps);
+        if (flags) atomicOr(P.status, flags);
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Finalize: per cell of the region, Q = sum over groups of the group means,
+// var(Q) = sum of the variances of the group means (groups are independent
+// strata).  Replaces kernel_results + the host scatter (code/mc_gpu.cu:959-970,
+// :762-776); the output is dense, i fastest.
+// ---------------------------------------------------------------------------
+__global__ void finalize_kernel(const FinalizeParams F) {
+    const long long n = (long long)F.nfields * F.region_cells;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int f = (int)(idx / F.region_cells);
+        const long long c = idx - (long long)f * F.region_cells;
+        const int iR = (int)(c % F.niR);
+        const long long jk = c / F.niR;
+        const int jR = (int)(jk % F.njR);
+        const int kR = (int)(jk / F.njR);
+        const long long tc = ((long long)iR * F.nkR + kR) * F.njR + jR;
+        const int p = (iR * F.npb + kR / F.tile_b) * F.npa + jR / F.tile_a;
+        const int N = F.rays_per_packet ? F.rays_per_packet[p] : F.rays;
+        double Q = 0.0, V = 0.0;
+        for (int g = 0; g < F.n_groups; ++g) {
+            double m = 0.0, v = 0.0;
+            if (!F.group_empty[g] && N > 0) {
+                const double2 t = F.tally[((long long)f * F.n_groups + g) * F.region_cells + tc];
+                m = t.x / N;
+                if (N > 1) v = fmax(0.0, t.y / N - m * m) / (N - 1);
+            }
+            Q += m;
+            V += v;
+            if (F.Qg) {
+                const long long o = ((long long)f * F.n_groups + g) * F.region_cells + c;
+                F.Qg[o] = m;
+                F.varg[o] = v;
+            }
+        }
+        F.Q[idx] = Q;
+        F.var[idx] = V;
+    }
+}
+
+// Transpose a host-order field (i fastest, optional ghost layer) into the
+// device order [i][k][j].  One thread per destination cell.
+__global__ void pack_T_kernel(const float *src, float *dst, int nw, int na, int nb,
+                              long long si, long long sj, long long sk, long long base) {
+    const long long n = (long long)nw * na * nb;
+    for (long long d = blockIdx.x * (long long)blockDim.x + threadIdx.x; d < n;
+         d += (long long)gridDim.x * blockDim.x) {
+        const int a = (int)(d % na);
+        const long long r = d / na;
+        const int b = (int)(r % nb);
+        const int w = (int)(r / nb);
+        dst[d] = src[base + w * si + a * sj + b * sk];
+    }
+}
+
+__global__ void pack_TX_kernel(const float *srcT, const float *srcX, float2 *dst, int nw, int na,
+                               int nb, long long si, long long sj, long long sk, long long base) {
+    const long long n = (long long)nw * na * nb;
+    for (long long d = blockIdx.x * (long long)blockDim.x + threadIdx.x; d < n;
+         d += (long long)gridDim.x * blockDim.x) {
+        const int a = (int)(d % na);
+        const long long r = d / na;
+        const int b = (int)(r % nb);
+        const int w = (int)(r / nb);
+        const long long s = base + w * si + a * sj + b * sk;
+        dst[d] = make_float2(srcT[s], srcX ? srcX[s] : 0.0f);
+    }
+}
+
+// Deterministic two-pass reduction: max T, min T, sum x (fixed block count,
+// fixed order), used when fields arrive as device pointers.
+constexpr int kStatBlocks = 256, kStatThreads = 256;
+__global__ void field_stats_pass1(const float *fT, const float2 *fTX, long long n, double *part) {
+    __shared__ double smax[kStatThreads], smin[kStatThreads], ssum[kStatThreads];
+    double mx = -1e300, mn = 1e300, sm = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        float T, x = 0.f;
+        if (fTX) { const float2 v = fTX[i]; T = v.x; x = v.y; } else { T = fT[i]; }
+        mx = fmax(mx, (double)T); mn = fmin(mn, (double)T); sm += x;
+    }
+    smax[threadIdx.x] = mx; smin[threadIdx.x] = mn; ssum[threadIdx.x] = sm;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+            ssum[threadIdx.x] += ssum[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = smax[0]; part[3 * blockIdx.x + 1] = smin[0]; part[3 * blockIdx.x + 2] = ssum[0];
+    }
+}
+__global__ void field_stats_pass2(const double *part, int nparts, float *out) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double mx = -1e300, mn = 1e300, sm = 0.0;
+    for (int i = 0; i < nparts; ++i) {
+        mx = fmax(mx, part[3 * i]); mn = fmin(mn, part[3 * i + 1]); sm += part[3 * i + 2];
+    }
+    out[0] = (float)mx; out[1] = (float)mn; out[2] = (float)sm;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline int grid_for(long long n, int threads) {
+    long long b = (n + threads - 1) / threads;
+    if (b > 4096) b = 4096;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+int launch_march(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (trace) { blocks = 1; threads = 32; }
+    switch (mode) {
+        case MODE_GREY:
+            if (trace) march_kernel<MODE_GREY, true><<<blocks, threads, 0, st>>>(p);
+            else march_kernel<MODE_GREY, false><<<blocks, threads, 0, st>>>(p);
+            break;
+        case MODE_T:
+            if (trace) march_kernel<MODE_T, true><<<blocks, threads, 0, st>>>(p);
+            else march_kernel<MODE_T, false><<<blocks, threads, 0, st>>>(p);
+            break;
+        case MODE_TX:
+            if (trace) march_kernel<MODE_TX, true><<<blocks, threads, 0, st>>>(p);
+            else march_kernel<MODE_TX, false><<<blocks, threads, 0, st>>>(p);
+            break;
+        default:
+            return (int)cudaErrorInvalidValue;
+    }
+    return (int)cudaGetLastError();
+}
+
+int march_occupancy(int mode, int threads) {
+    int nb = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    if (mode == MODE_GREY) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false>, threads, 0);
+    if (mode == MODE_T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false>, threads, 0);
+    if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false>, threads, 0);
+    if (e != cudaSuccess) return 1;
+    return nb > 0 ? nb : 1;
+}
+
+int launch_finalize(const FinalizeParams &p, void *stream) {
+    const long long n = (long long)p.nfields * p.region_cells;
+    finalize_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(p);
+    return (int)cudaGetLastError();
+}
+
+int launch_pack_T(const float *src, float *dst, int nw, int na, int nb, long long si, long long sj,
+                  long long sk, long long base, void *stream) {
+    const long long n = (long long)nw * na * nb;
+    pack_T_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(src, dst, nw, na, nb, si, sj, sk, base);
+    return (int)cudaGetLastError();
+}
+
+int launch_pack_TX(const float *srcT, const float *srcX, float2 *dst, int nw, int na, int nb, long long si,
+                   long long sj, long long sk, long long base, void *stream) {
+    const long long n = (long long)nw * na * nb;
+    pack_TX_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(srcT, srcX, dst, nw, na, nb, si, sj, sk, base);
+    return (int)cudaGetLastError();
+}
+
+int launch_field_stats(const float *fT, const float2 *fTX, long long n, double *partials, float *out,
+                       void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    field_stats_pass1<<<kStatBlocks, kStatThreads, 0, st>>>(fT, fTX, n, partials);
+    field_stats_pass2<<<1, 32, 0, st>>>(partials, kStatBlocks, out);
+    return (int)cudaGetLastError();
+}
+
+int field_stats_partials() { return 3 * kStatBlocks; }
+
+int device_sm_count() {
+    int dev = 0, n = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return n;
+}
+
+}  // namespace dnsmc

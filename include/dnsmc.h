@@ -1,0 +1,241 @@
+/*
+ * dnsmc.h -- C ABI of the GB300 reverse Monte Carlo radiative-source solver.
+ *
+ * Two layers:
+ *
+ *  1. The reference drop-in pair  mc_gpu_ / get_results_.  Same names, same
+ *     by-reference Fortran calling convention, same array layouts and the same
+ *     asynchronous-launch / blocking-collect split as the reference routine
+ *     (code/mc_gpu.cu:440 and code/mc_gpu.cu:640, called from
+ *     code/main_comp.f:156,193,202 and code/rad_main.f:100,102).  The reference
+ *     fixes its configuration at compile time in code/param.h; here the same
+ *     values are a runtime dnsmc_config, taken from dnsmc_set_default_config()
+ *     or from the environment (see dnsmc_config_from_env), so a Fortran caller
+ *     links this library instead of mc_gpu.o without source changes.
+ *
+ *  2. The handle-based dnsmc_* API: explicit configuration, table loading in
+ *     the reference text formats or from raw arrays, resident fields, several
+ *     snapshots per solve, band-group stratification, adaptive ray counts,
+ *     integer error codes (the reference exits the process on any error,
+ *     code/param.h:85-95), a status word and a bounded wait.
+ *
+ * Plain C types only: pointers, sizes, ints and floats.  Every function that
+ * can fail returns an int error code (DNSMC_OK == 0); dnsmc_last_error()
+ * gives a one-line description of the most recent failure on the calling
+ * thread.
+ *
+ * Axis convention (the reference's): i is wall-normal (the two walls sit at
+ * x = 0 and x = Lx), j and k are periodic.  Field arrays are dense, i fastest
+ * (index i + imax*(j + jmax*k)) unless a function states otherwise.
+ */
+#ifndef DNSMC_H
+#define DNSMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes --------------------------------------------------------- */
+#define DNSMC_OK            0
+#define DNSMC_ERR_ARG       1   /* invalid argument or inconsistent sizes      */
+#define DNSMC_ERR_STATE     2   /* call out of order (e.g. solve before tables) */
+#define DNSMC_ERR_CUDA      3   /* CUDA runtime failure                         */
+#define DNSMC_ERR_IO        4   /* table file missing or malformed              */
+#define DNSMC_ERR_TIMEOUT   5   /* bounded wait expired; work still in flight   */
+#define DNSMC_ERR_NOMEM     6   /* host or device allocation failed             */
+#define DNSMC_ERR_TABLE     7   /* table values unusable (non-positive, NaN)    */
+#define DNSMC_ERR_NODEVICE  8   /* no CUDA device visible                       */
+
+/* ---- status bits (dnsmc_status) ------------------------------------------ */
+#define DNSMC_STATUS_STEP_CAP   0x1u  /* a ray stopped at the per-ray step cap   */
+#define DNSMC_STATUS_NONFINITE  0x2u  /* a non-finite ray contribution was seen  */
+#define DNSMC_STATUS_BAD_FIELD  0x4u  /* a temperature <= 0 or NaN was supplied  */
+
+/* ---- spectral models (reference code/param.h:48-49, `grey`) -------------- */
+#define DNSMC_MODEL_CK         0  /* narrow-band correlated-k gas tables        */
+#define DNSMC_MODEL_GREY_BANDS 1  /* reference grey tables: 1000 equal bands     */
+#define DNSMC_MODEL_PARTICLE   2  /* reference particle-absorption tables        */
+#define DNSMC_MODEL_GREY       3  /* grey medium, constant kappa, sigma*T^4      */
+#define DNSMC_MODEL_TABLE      4  /* raw k(band, g, T, x_H2O) table (set_table)  */
+
+/* ---- field layouts -------------------------------------------------------- */
+#define DNSMC_LAYOUT_DENSE     0  /* imax*jmax*kmax, i fastest, no ghosts        */
+#define DNSMC_LAYOUT_FORTRAN   1  /* (imax+2)(jmax+2)(kmax+2), i fastest, ghost  */
+                                  /* layer included: the reference TMC array     */
+
+typedef struct dnsmc_config {
+    /* geometry (code/param.h:4-11) */
+    int   imax, jmax, kmax;      /* cells; i wall-normal, j and k periodic      */
+    int   p_row;                 /* number of j-slabs (decomp_2d p_row)         */
+    float Lx, Ly, Lz;            /* domain lengths [m]                           */
+    int   stretched_x;           /* 1: the reference wall-normal stretching     */
+                                 /* (code/definitions.h:108-134), 0: uniform    */
+    /* rays (code/param.h:13-14) */
+    int   nvar;                  /* batches per cell (sigma normaliser, :221)    */
+    int   photmax;               /* rays per batch; rays/cell = nvar*photmax    */
+    /* walls (code/param.h:56-83): west = x 0, east = x Lx; j,k periodic */
+    float T_west, T_east;        /* wall temperatures [K]                        */
+    float eps_west, eps_east;    /* wall emissivity, 1 = black (bdw=bde=2)      */
+    /* march (code/param.h:72, :25-37) */
+    float toll;                  /* transmissivity cut-off                      */
+    int   max_steps;             /* per-ray step cap                             */
+    int   grid_num;              /* multigrid levels; 1 = fine grid only        */
+    /* spectral model */
+    int   model;                 /* DNSMC_MODEL_*                                */
+    float kappa;                 /* grey absorption coefficient [1/m] (GREY)     */
+    int   n_groups;              /* band groups for stratified sampling (>=1)    */
+    /* randomness */
+    uint64_t seed;
+    /* kernel shape (0 = automatic) */
+    int   block_threads;         /* 128, 256 or 512                              */
+    int   tile_a;                /* cells of a packet along j: 8, 16 or 32       */
+} dnsmc_config;
+
+/* Raw spectral table for DNSMC_MODEL_TABLE (and the internal representation of
+ * every tabulated model).  k is an absorption coefficient in 1/m on a uniform
+ * T grid and a uniform x_H2O grid; it is interpolated linearly in T and x.     */
+typedef struct dnsmc_table_desc {
+    int   nbands, nq, nT, nX;    /* nX == 1: no x_H2O dependence                */
+    float T0, dT;                /* T grid: T0 + t*dT, t = 0..nT-1              */
+    float X0, dX;                /* x grid: X0 + u*dX, u = 0..nX-1              */
+    const float *k;              /* [nbands][nq][nT][nX]                        */
+    const float *wvc;            /* [nbands] band-centre wavenumber [1/cm]      */
+    const float *dnu;            /* [nbands] band width [1/cm]                  */
+    const float *wq;             /* [nq] quadrature weights (sum 1)             */
+    const float *Ib;             /* [nbands][nT] band Planck intensity, or NULL */
+                                 /* (then computed at wvc, code/memory_copy.cu:291) */
+    /* Reference sampling data (optional).  When prob != NULL the band and
+     * g-point are drawn from these CDFs at the table temperature nearest to
+     * Tmax and weighted with the Planck-mean kP, as code/mc_gpu.cu:142-169 and
+     * :830-896 do; otherwise the sampling density is built from k, Ib, dnu, wq
+     * at Tmax (and the field-mean x_H2O).                                      */
+    const float *prob;           /* [nT][nbands] band CDF                       */
+    const float *probg;          /* [nT][nbands][nq] g-point CDF, or NULL       */
+    const float *kP;             /* [nT] Planck-mean absorption coefficient     */
+} dnsmc_table_desc;
+
+typedef struct dnsmc_solver dnsmc_solver;
+
+/* ---- configuration -------------------------------------------------------- */
+/* The reference's shipped code/param.h values (64^3, particle tables, black
+ * x-walls at 500 K, Lx=Ly=Lz=1, nVar=3, photmax=20000), except grid_num = 1:
+ * rays march on the fine grid only.                                          */
+void dnsmc_set_default_config(dnsmc_config *cfg);
+/* Overlay DNSMC_* environment variables (DNSMC_IMAX, DNSMC_JMAX, DNSMC_KMAX,
+ * DNSMC_PROW, DNSMC_LX, DNSMC_LY, DNSMC_LZ, DNSMC_NVAR, DNSMC_PHOTMAX,
+ * DNSMC_TWEST, DNSMC_TEAST, DNSMC_MODEL, DNSMC_GRID_NUM, DNSMC_SEED,
+ * DNSMC_STRETCHED) on cfg.  Returns DNSMC_ERR_ARG on an unparsable value.     */
+int  dnsmc_config_from_env(dnsmc_config *cfg);
+const char *dnsmc_last_error(void);
+const char *dnsmc_version(void);
+
+/* ---- solver lifetime ------------------------------------------------------ */
+int  dnsmc_create(const dnsmc_config *cfg, dnsmc_solver **out);
+int  dnsmc_destroy(dnsmc_solver *s);
+
+/* ---- tables (host-side parse; no GPU needed) ------------------------------ */
+/* Read the reference text tables from dir (the reference hard-codes
+ * ../distr/tables/, code/read_tables.cpp:25,43,65) for model CK (planck-mean.txt,
+ * NarrBand%d.txt, prob_new2.txt; code/read_tables.cpp:20-92) or PARTICLE
+ * (particles/{planck-mean,NarrBand%d,prob}.txt; code/read_tables.cpp:185-241).
+ * nT, nB, nQ as in code/NarrowBand.h (52,119,16 for CK; 52,119,1 for PARTICLE).*/
+int  dnsmc_load_tables_ref(dnsmc_solver *s, const char *dir, int model,
+                           int nT, int nB, int nQ);
+/* Reference grey tables (code/grey_tables.cpp:19-109): nB equal bands up to
+ * wvmax [1/cm], kappa everywhere, T grid from 0.9*Tmin to 1.1*Tmax.  The T grid
+ * depends on Tmax, so the table is rebuilt at every solve.                     */
+int  dnsmc_use_grey_band_tables(dnsmc_solver *s, int nB, int nT, float wvmax,
+                                float Tmin);
+int  dnsmc_set_table(dnsmc_solver *s, const dnsmc_table_desc *t);
+/* Copy of the parsed table (host arrays of the sizes in the desc); any pointer
+ * may be NULL.  For tests of the parsers.                                      */
+int  dnsmc_get_table_info(const dnsmc_solver *s, int *nbands, int *nq, int *nT,
+                          int *nX, float *T0, float *dT, float *X0, float *dX);
+int  dnsmc_get_table(const dnsmc_solver *s, float *k, float *wvc, float *Ib,
+                     float *prob, float *probg, float *kP);
+
+/* ---- fields and solve ------------------------------------------------------ */
+/* Upload nfields snapshots of temperature [K] and optional H2O mole fraction
+ * (x may be NULL: taken as 0) to device-resident storage, in the given layout.
+ * Host arrays may be reused as soon as the call returns.                       */
+int  dnsmc_set_fields(dnsmc_solver *s, int nfields, const float *T,
+                      const float *x, int layout);
+/* Same, from device pointers (dense layout), stream-ordered on the solver's
+ * stream; no host copy.                                                        */
+int  dnsmc_set_fields_device(dnsmc_solver *s, int nfields, const float *dT,
+                             const float *dx);
+/* Cells to compute: i in [i0,i1), j in [j0,j1), k in [k0,k1) (0-based); the
+ * march always sees the whole field.  Default: all cells.                      */
+int  dnsmc_set_region(dnsmc_solver *s, int i0, int i1, int j0, int j1, int k0,
+                      int k1);
+/* Rays per cell per band group.  rays_per_packet (length = number of packets,
+ * see dnsmc_packet_count) overrides it per packet of 32 cells when non-NULL.  */
+int  dnsmc_set_rays(dnsmc_solver *s, int rays_per_group,
+                    const int *rays_per_packet);
+int  dnsmc_packet_count(const dnsmc_solver *s, int *npackets);
+/* Enqueue a solve of every resident snapshot on the solver's stream and return.*/
+int  dnsmc_solve_async(dnsmc_solver *s);
+/* Wait for the last solve, at most timeout_s seconds (<=0: no limit).          */
+int  dnsmc_wait(dnsmc_solver *s, double timeout_s);
+/* Results of the last solve, blocking: per cell of the region (dense, i fastest,
+ * snapshot slowest) the radiative source Q [W/m^3] (emission minus absorption)
+ * and the standard error of Q.  Either pointer may be NULL.                    */
+int  dnsmc_get_results(dnsmc_solver *s, double *Q, double *sigma);
+/* Per band group: mean and variance of the mean, [field][group][cell].         */
+int  dnsmc_get_group_results(dnsmc_solver *s, double *Qg, double *varg);
+/* Bits DNSMC_STATUS_* accumulated by the last solve.                           */
+int  dnsmc_status(dnsmc_solver *s, uint32_t *status);
+/* Counters of the last solve: emitted rays and ray-voxel steps (all lanes),
+ * device time of the march kernel in milliseconds.                             */
+int  dnsmc_get_counters(dnsmc_solver *s, double *rays, double *steps,
+                        double *march_ms);
+/* Device time of the last solve measured with CUDA events on the solver's
+ * stream: from the first enqueued operation (sampling upload) to the end of
+ * the result copy into pinned host memory, and of the march kernel alone.    */
+int  dnsmc_get_timing(dnsmc_solver *s, double *solve_ms, double *march_ms);
+/* Tmax used for sampling (max over fields and wall temperatures).              */
+int  dnsmc_get_tmax(const dnsmc_solver *s, float *tmax);
+
+/* ---- spectral sampling tables (for the host replay in the tests) ----------- */
+/* Entries of every band group: alias threshold, alias index, band, g-point,
+ * weight factor W (ray weight = W * k(T_i) * Ib(T_i)), k-table offset.  Valid
+ * after a solve.  n_entries / group_start have n_groups+1 / n_groups entries.  */
+int  dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *group_start,
+                        int *n_entries, float *prob, int *alias, int *band,
+                        int *gq, float *W, float *ibw);
+/* Build the sampling tables for a given Tmax and mean x_H2O on the host
+ * without solving (no GPU needed); dnsmc_get_sampling then returns them.     */
+int  dnsmc_prepare_sampling(dnsmc_solver *s, float Tmax, float xmean);
+/* Wall-normal faces (imax+1) and periodic cell sizes used by the march.       */
+int  dnsmc_get_geometry(const dnsmc_solver *s, float *xu, float *dy, float *dz);
+
+/* ---- trace of one packet-ray (bit-exact replay tests) ---------------------- */
+/* Record the voxel walk of ray r of packet p in band group g of field f: per
+ * step the wall-normal index, the j/k offsets, the crossed axis, the segment
+ * length and lane 0's transmissivity.  Up to max_steps records of 6 words.    */
+int  dnsmc_trace_ray(dnsmc_solver *s, int f, int g, int p, int r, int max_steps,
+                     int32_t *rec, int *n_steps, uint32_t *rng4);
+
+/* ---- reference drop-in (code/mc_gpu.cu:440, :640) -------------------------- */
+/* Tfort: real(4) TMC(0:imax+1,0:jmax+1,0:kmax+1), i fastest, whole domain with
+ * ghost layers.  *ystart: 1-based global j of this rank's slab (xstart(2)).
+ * Enqueues the solve of the slab's cells and returns (the caller runs DNS
+ * steps meanwhile).  On error prints to stderr and exits, as the reference.   */
+void mc_gpu_(float *Tfort, int *ystart);
+/* resfort, varfort: real(4) (0:imax+1, 0:jmax/p_row+1, 0:kmax+1), i fastest.
+ * Blocks, then writes Q [W/m^3] and its standard deviation with the
+ * reference's 1/((nVar-0.5)(nVar-1)) normaliser into interior cells only.     */
+void get_results_(float *resfort, float *varfort);
+/* Configure the instance the drop-in pair uses (optional; otherwise the
+ * defaults overlaid with the environment are used on the first mc_gpu_ call).
+ * table_dir NULL means "../distr/tables" as the reference.                    */
+int  dnsmc_dropin_configure(const dnsmc_config *cfg, const char *table_dir);
+int  dnsmc_dropin_release(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DNSMC_H */

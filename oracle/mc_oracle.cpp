@@ -1,0 +1,867 @@
+// mc_oracle.cpp -- TEST INFRASTRUCTURE ONLY.  CPU restatement of the
+// reference reverse Monte Carlo of simone-silvestri/dnsMC, used by tests/,
+// __graft_entry__.smoke() and bench.py's CPU-baseline leg as the checker.
+// Nothing in the product (dnsmc_gb300/) links or calls it.
+//
+// Three parts:
+//  (1) orc_ref_mc: the reference estimator in the reference's own structure
+//      -- one thread per cell, nVar batches of photmax rays
+//      (code/mc_gpu.cu:44-226), emission direction (:813-820), band and
+//      g-point bisection on the CDF at the table temperature nearest Tmax
+//      (:830-896), the OERM weights (:59-63, :162-169), the position-update
+//      voxel march with periodic and black-wall boundaries (:228-438), the
+//      multigrid switch (:193-207) on spline-coarsened temperature
+//      (code/spline.cpp:35-170), linear-filter table lookups with clamp
+//      addressing (code/memory_copy.cu:131-289) optionally with the 8-bit
+//      fixed-point filter weights of the texture unit.  Templated on the
+//      arithmetic type: FP32 reproduces the reference build (the timed CPU
+//      baseline), FP64 is the oracle.  curand is replaced by Philox4x32-10
+//      streams keyed per (cell, batch, ray): the reference's stream is not
+//      reproducible (colliding seeds, code/mc_gpu.cu:99), so comparisons with
+//      it are statistical.
+//  (2) orc_packet_mc / orc_packet_trace: an independent restatement of the
+//      GB300 packet scheme (32 cells of one wall-normal plane share each
+//      ray's direction and spectral sample) that reproduces the device march
+//      bit for bit in FP32 (same Philox counters, same alias draw, same
+//      fmaf-based polynomial exp/sin/cos), or runs it in FP64.
+//  (3) helpers: Philox4x32-10, the reference grids, the spline.
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11): 10 rounds of the 4x32
+// Philox S-box with multipliers D2511F53, CD9E8D57 and Weyl key increments
+// 9E3779B9, BB67AE85.
+// ---------------------------------------------------------------------------
+static inline void philox(const uint32_t in[4], uint32_t k0, uint32_t k1, uint32_t out[4]) {
+    uint32_t c0 = in[0], c1 = in[1], c2 = in[2], c3 = in[3];
+    for (int r = 0; r < 10; ++r) {
+        if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        const uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+        const uint32_t n1 = (uint32_t)p1;
+        const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+        const uint32_t n3 = (uint32_t)p0;
+        c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox(ctr, key[0], key[1], out); }
+
+// ---------------------------------------------------------------------------
+// Reference grids (code/definitions.h:68-136): stretched wall-normal faces
+// for im cells taken from the im0 fine grid, uniform periodic faces.
+// ---------------------------------------------------------------------------
+void orc_ref_faces(int im, int im0, float L, int stretched, float *xu) {
+    if (!stretched) {
+        for (int i = 0; i <= im; ++i) xu[i] = (float)i * (L / (float)im);
+        xu[im] = L;
+        return;
+    }
+    std::vector<float> xu0(im0 + 1, 0.0f);
+    for (int i = 1; i < im0 / 2 + 1; ++i) {
+        const float r = (1.f * i) / im0;
+        const float dx = (float)(0.5 - 1.45 * (r - 0.5) * (r - 0.5));
+        xu0[i] = xu0[i - 1] + dx;
+    }
+    const float xnorm = xu0[im0 / 2];
+    for (int i = 1; i < im0 / 2 + 1; ++i) xu0[i] = (float)(L / 2. * xu0[i] / xnorm);
+    for (int i = im0; i > im0 / 2; --i) xu0[i] = L - xu0[im0 - i];
+    xu[0] = 0;
+    for (int i = 1; i < im + 1; ++i) xu[i] = xu0[i * im0 / im];
+}
+
+}  // extern "C"
+
+namespace {
+
+struct Grid {  // one level, reference Gridn + Var_CPU (1-based cells, ghosts at 0, n+1)
+    int im, jm, km, sm;
+    std::vector<float> x, xu, y, yu, z, zu, T;
+};
+
+void mk_grid(Grid &g, int im, int jm, int km, int im0, int sm, float Lx, float Ly, float Lz, int stretched) {
+    g.im = im; g.jm = jm; g.km = km; g.sm = sm;
+    g.x.assign(im + 2, 0.f); g.xu.assign(im + 1, 0.f);
+    g.y.assign(jm + 2, 0.f); g.yu.assign(jm + 1, 0.f);
+    g.z.assign(km + 2, 0.f); g.zu.assign(km + 1, 0.f);
+    const float dy = Ly / jm, dz = Lz / km;
+    for (int i = 0; i < jm + 1; ++i) g.yu[i] = i * dy;
+    for (int i = 0; i < km + 1; ++i) g.zu[i] = i * dz;
+    g.y[0] = -dy / 2; g.z[0] = -dz / 2;
+    for (int i = 1; i < jm + 1; ++i) g.y[i] = (g.yu[i - 1] + g.yu[i]) / 2;
+    for (int i = 1; i < km + 1; ++i) g.z[i] = (g.zu[i - 1] + g.zu[i]) / 2;
+    g.y[jm + 1] = g.y[jm] + dy; g.z[km + 1] = g.z[km] + dz;
+    orc_ref_faces(im, im0, Lx, stretched, g.xu.data());
+    for (int i = 1; i < im + 1; ++i) g.x[i] = (float)(0.5 * (g.xu[i] + g.xu[i - 1]));
+    g.x[0] = -g.x[1];
+    g.x[im + 1] = g.xu[im] + (g.xu[im] - g.x[im]);
+    g.T.assign((size_t)(im + 2) * (jm + 2) * (km + 2), 0.f);
+}
+
+inline size_t idxT(int i, int j, int k, int im, int jm) { return i + (size_t)(im + 2) * (j + (size_t)k * (jm + 2)); }
+
+// Natural cubic spline on 1-based arrays (Numerical Recipes, as code/spline.cpp:119-170).
+void spline(const float *x, const float *y, int n, float *y2) {
+    std::vector<float> u(n + 1);
+    y2[1] = u[1] = 0.0f;
+    for (int i = 2; i <= n - 1; ++i) {
+        const float sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+        const float p = sig * y2[i - 1] + 2.0f;
+        y2[i] = (sig - 1.0f) / p;
+        float ui = (y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]);
+        u[i] = (float)((6.0 * ui / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p);
+    }
+    y2[n] = 0.0f;
+    for (int k = n - 1; k >= 1; --k) y2[k] = y2[k] * y2[k + 1] + u[k];
+}
+
+float splint(const float *xa, const float *ya, const float *y2a, int n, float x) {
+    int klo = 1, khi = n;
+    while (khi - klo > 1) {
+        const int k = (khi + klo) >> 1;
+        if (xa[k] > x) khi = k; else klo = k;
+    }
+    const float h = xa[khi] - xa[klo];
+    const float a = (xa[khi] - x) / h, b = (x - xa[klo]) / h;
+    return (float)(a * ya[klo] + b * ya[khi] + ((a * a * a - a) * y2a[klo] + (b * b * b - b) * y2a[khi]) * (h * h) / 6.0);
+}
+
+// Separable spline coarsening of the fine temperature (code/spline.cpp:35-116).
+void interp3d(std::vector<Grid> &g) {
+    const Grid &f = g[0];
+    const int I = f.im, J = f.jm, K = f.km;
+    const int ng = (int)g.size();
+    std::vector<std::vector<float>> tx(ng), txy(ng);
+    for (int l = 1; l < ng; ++l) {
+        tx[l].assign((size_t)(g[l].im + 2) * (J + 2) * (K + 2), 0.f);
+        txy[l].assign((size_t)(g[l].im + 2) * (g[l].jm + 2) * (K + 2), 0.f);
+    }
+    std::vector<float> a(std::max({I, J, K}) + 2), a2(std::max({I, J, K}) + 2);
+    for (int j = 1; j <= J; ++j)
+        for (int k = 1; k <= K; ++k) {
+            for (int i = 1; i <= I; ++i) a[i] = f.T[idxT(i, j, k, I, J)];
+            spline(f.x.data(), a.data(), I, a2.data());
+            for (int l = 1; l < ng; ++l)
+                for (int i = 1; i <= g[l].im; ++i)
+                    tx[l][idxT(i, j, k, g[l].im, J)] = splint(f.x.data(), a.data(), a2.data(), I, g[l].x[i]);
+        }
+    for (int l = 1; l < ng; ++l)
+        for (int i = 1; i <= g[l].im; ++i)
+            for (int k = 1; k <= K; ++k) {
+                for (int j = 1; j <= J; ++j) a[j] = tx[l][idxT(i, j, k, g[l].im, J)];
+                spline(f.y.data(), a.data(), J, a2.data());
+                for (int j = 1; j <= g[l].jm; ++j)
+                    txy[l][idxT(i, j, k, g[l].im, g[l].jm)] = splint(f.y.data(), a.data(), a2.data(), J, g[l].y[j]);
+            }
+    for (int l = 1; l < ng; ++l)
+        for (int i = 1; i <= g[l].im; ++i)
+            for (int j = 1; j <= g[l].jm; ++j) {
+                for (int k = 1; k <= K; ++k) a[k] = txy[l][idxT(i, j, k, g[l].im, g[l].jm)];
+                spline(f.z.data(), a.data(), K, a2.data());
+                for (int k = 1; k <= g[l].km; ++k)
+                    g[l].T[idxT(i, j, k, g[l].im, g[l].jm)] = splint(f.z.data(), a.data(), a2.data(), K, g[l].z[k]);
+            }
+}
+
+float I_blackC(float T, float nu) {
+    if (!(T > 0)) return 0.0f;
+    const float C1 = 3.741771790075259e-16f, C2 = 0.014387741858429f;
+    const float n = nu * 100.0f;
+    return (float)(1.0 / 3.14159265358979323846 * (double)C1 * (double)(n * n * n) /
+                   (double)(expf(C2 * nu * 100.0f / T) - 1.0f));
+}
+
+}  // namespace
+
+extern "C" {
+
+// ===========================================================================
+// (1) reference-structured estimator
+// ===========================================================================
+typedef struct {
+    int imax, jmax, kmax;
+    float Lx, Ly, Lz;
+    int stretched;
+    int grid_num;
+    int maxs[6];
+    float T_west, T_east;
+    float toll;
+    int nvar, photmax;
+    int hwfilter;
+    int use_double;
+    uint64_t seed;
+    int model;          // 0 ck, 1 grey bands (built here), 2 particle
+    float kappa;        // grey-band absorption coefficient
+    int nT, nB, nQ;
+    const float *Tnb;   // [nT]
+    const float *kq;    // [nB][nT][nQ]
+    const float *wvc;   // [nB]
+    const float *prob;  // [nT][nB]
+    const float *probg; // [nT][nB][nQ] or NULL
+    const float *kP;    // [nT]
+} OrcRefConfig;
+
+}  // extern "C"
+
+namespace {
+
+struct RefTables {
+    int nT, nB, nQ;
+    std::vector<float> Tnb, kq, wvc, prob, probg, kP, Ib, ibw_w, ibw_e;
+    float Tmax, kappamax;
+    int tm;
+};
+
+// Linear-filter fetch along one axis of a clamp-addressed texture at
+// coordinate pos+0.5 (texel centres at integers), as the texture unit does;
+// hw: quantise the fraction to 1/256 (8-bit fixed point weights).
+template <class R>
+inline R tex_lerp(const float *row, int stride, int n, R pos, int hw) {
+    R xb = pos;  // = (pos + 0.5) - 0.5
+    R fl = std::floor(xb);
+    int i0 = (int)fl;
+    R a = xb - fl;
+    if (hw) a = std::round(a * (R)256) / (R)256;
+    const int c0 = std::min(std::max(i0, 0), n - 1), c1 = std::min(std::max(i0 + 1, 0), n - 1);
+    return ((R)1 - a) * (R)row[(size_t)c0 * stride] + a * (R)row[(size_t)c1 * stride];
+}
+
+template <class R>
+struct RefMC {
+    const OrcRefConfig &c;
+    const RefTables &t;
+    const std::vector<Grid> &g;
+    RefMC(const OrcRefConfig &c_, const RefTables &t_, const std::vector<Grid> &g_) : c(c_), t(t_), g(g_) {}
+
+    R kfetch(int nb, R pos, int gq) const {  // tex3D(tex, nb+.5, pos+.5, g+.5), extent (nB, nT, nQ)
+        const int gg = std::min(std::max(gq, 0), t.nQ - 1);
+        // kq layout [nB][nT][nQ]: along T the stride is nQ
+        return tex_lerp<R>(t.kq.data() + (size_t)nb * t.nT * t.nQ + gg, t.nQ, t.nT, pos, c.hwfilter);
+    }
+    R ibfetch(int nb, R pos) const {  // tex2D(tex_Ib, nb+.5, pos+.5), Ib[nT][nB]
+        return tex_lerp<R>(t.Ib.data() + nb, t.nB, t.nT, pos, c.hwfilter);
+    }
+
+    // find_band (code/mc_gpu.cu:830-896)
+    void find_band(R u1, R u2, int *nb, int *gq) const {
+        const int tm = t.tm;
+        const R T0 = t.Tnb[tm], T1 = t.Tnb[tm + 1];
+        const int ts = ((R)t.Tmax - T0) < (T1 - (R)t.Tmax) ? tm : tm + 1;
+        const float *pd = t.prob.data() + (size_t)ts * t.nB;
+        int lo = 0, w = t.nB;
+        while (w > lo + 1) {
+            const int d = (lo + w) / 2;
+            if (u1 < (R)pd[d]) w = d; else lo = d;
+        }
+        lo = lo + 1;
+        if (u1 < (R)pd[0]) lo = 0;
+        if (u1 == (R)1) lo = t.nB - 1;
+        *nb = lo;
+        if (c.model == 1) { *gq = 0; return; }
+        int gg = 0;
+        w = t.nQ;
+        const float *pg = t.probg.empty() ? nullptr : t.probg.data() + ((size_t)ts * t.nB + lo) * t.nQ;
+        while (w > gg + 1) {
+            const int d = (gg + w) / 2;
+            const R pr = pg ? (R)pg[d] : (R)0;
+            if (u2 < pr) w = d; else gg = d;
+        }
+        gg = gg + 1;
+        const R p0 = pg ? (R)pg[0] : (R)0;
+        if (u2 < p0) gg = 0;
+        if (u2 == (R)1) gg = t.nQ - 1;
+        *gq = gg;  // may equal nQ (reference behaviour for nQ == 1); fetches clamp
+    }
+
+    void cell(int ci, int cj, int ck, uint64_t cell_id, double *sol, double *var, double *se, double *nsteps) const {
+        const R pi = (R)3.14159265358979323846;
+        const R stefan = (R)5.670373e-08;
+        const Grid &g0 = g[0];
+        const R dT = (R)t.Tnb[1] - (R)t.Tnb[0];
+        const R Tnb0 = (R)t.Tnb[0];
+        const R Tn0 = dT, Tn1 = Tnb0 / dT;  // code/mc_gpu.cu:59
+        const R Ibmax = (R)4 * (R)t.kappamax * (R)t.Tmax * (R)t.Tmax * (R)t.Tmax * (R)t.Tmax * stefan / (R)c.photmax;
+        const R Ti = (R)g0.T[idxT(ci, cj, ck, g0.im, g0.jm)];
+        std::vector<R> Dv(c.nvar, (R)0);
+        double sum = 0, sum2 = 0, steps = 0;
+        const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
+        for (int v = 0; v < c.nvar; ++v) {
+            R De = 0;
+            for (int h = 0; h < c.photmax; ++h) {
+                const uint32_t ctr[4] = {(uint32_t)h, (uint32_t)v, (uint32_t)cell_id, (uint32_t)(cell_id >> 32) ^ 0x5EF0u};
+                uint32_t rn[4];
+                philox(ctr, k0, k1, rn);
+                // curand_uniform is in (0, 1]
+                auto U = [](uint32_t x) { return (R)((x >> 8) + 1) * (R)5.9604644775390625e-8; };
+                R xp = g0.x[ci], yp = g0.y[cj], zp = g0.z[ck];
+                int ic = ci, jc = cj, kc = ck;
+                const R phi = U(rn[0]) * (R)2 * pi;
+                const R theta = std::acos((R)1 - (R)2 * U(rn[1]));
+                R sx = std::cos(theta), sy = std::sin(theta) * std::cos(phi), sz = std::sin(theta) * std::sin(phi);
+                if (sx == 0) sx = (R)1e-10;
+                if (sy == 0) sy = (R)1e-10;
+                if (sz == 0) sz = (R)1e-10;
+                const int fl[3] = {sx < 0, sy < 0, sz < 0};
+                int nb, gq;
+                find_band(U(rn[2]), U(rn[3]), &nb, &gq);
+                R tra = 1;
+                R pos = (Ti - Tnb0) / dT;
+                const R a2 = kfetch(nb, pos, gq);
+                const R invTi4 = (R)1 / ibfetch(nb, pos);
+                pos = ((R)t.Tmax - Tnb0) / dT;
+                const R a1 = kfetch(nb, pos, gq);
+                const R ratioI = ((R)1 / invTi4) / ibfetch(nb, pos) * a2 / a1;
+                // start-cell fix-ups (code/mc_gpu.cu:174-186)
+                if (fl[0] && xp == (R)g0.xu[ic - 1]) ic--;
+                if (fl[1] && yp == (R)g0.yu[jc - 1]) jc--;
+                if (fl[2] && zp == (R)g0.zu[kc - 1]) kc--;
+                if (!fl[0] && xp == (R)g0.xu[ic]) ic++;
+                if (!fl[1] && yp == (R)g0.yu[jc]) jc++;
+                if (!fl[2] && zp == (R)g0.zu[kc]) kc++;
+                const R before = De;
+                for (int grd = 0; grd < (int)g.size(); ++grd) {
+                    const Grid &G = g[grd];
+                    int counter = 0;
+                    while (tra > (R)c.toll && counter < G.sm) {
+                        const R dsx = ((R)G.xu[ic - fl[0]] - xp) / sx;
+                        const R dsy = ((R)G.yu[jc - fl[1]] - yp) / sy;
+                        const R dsz = ((R)G.zu[kc - fl[2]] - zp) / sz;
+                        const R tf = (R)G.T[idxT(ic, jc, kc, G.im, G.jm)];
+                        const R p2 = tf / Tn0 - Tn1;
+                        const R absco = kfetch(nb, p2, gq);
+                        const R bp = ibfetch(nb, p2);
+                        R ds = dsx;
+                        if (ds > dsy) ds = dsy;
+                        if (ds > dsz) ds = dsz;
+                        if (ds == dsx) xp = G.xu[ic - fl[0]]; else xp = xp + ds * sx;
+                        if (ds == dsy) yp = G.yu[jc - fl[1]]; else yp = yp + ds * sy;
+                        if (ds == dsz) zp = G.zu[kc - fl[2]]; else zp = zp + ds * sz;
+                        const R alpha = (R)1 - std::exp(-ds * absco);
+                        De -= Ibmax * tra * alpha * ratioI * (invTi4 * bp - (R)1);
+                        tra = tra * ((R)1 - alpha);
+                        if (tra < (R)c.toll) {
+                            De -= Ibmax * tra * ratioI * (invTi4 * bp - (R)1);
+                            tra = 0;
+                        }
+                        if (dsx < dsy) {
+                            if (dsx < dsz) {
+                                if (fl[0]) {
+                                    ic--;
+                                    if (ic == 0) { De -= Ibmax * tra * (invTi4 * (R)t.ibw_w[nb] - (R)1) * ratioI; tra = 0; }
+                                } else {
+                                    ic++;
+                                    if (ic == G.im + 1) { De -= Ibmax * tra * (invTi4 * (R)t.ibw_e[nb] - (R)1) * ratioI; tra = 0; }
+                                }
+                            } else {
+                                if (fl[2]) { kc--; if (kc == 0) { kc = G.km; zp = c.Lz; } }
+                                else { kc++; if (kc == G.km + 1) { kc = 1; zp = 0; } }
+                            }
+                        } else {
+                            if (dsy < dsz) {
+                                if (fl[1]) { jc--; if (jc == 0) { jc = G.jm; yp = c.Ly; } }
+                                else { jc++; if (jc == G.jm + 1) { jc = 1; yp = 0; } }
+                            } else {
+                                if (fl[2]) { kc--; if (kc == 0) { kc = G.km; zp = c.Lz; } }
+                                else { kc++; if (kc == G.km + 1) { kc = 1; zp = 0; } }
+                            }
+                        }
+                        ++counter;
+                        steps += 1;
+                    }
+                    if (grd < (int)g.size() - 1) {
+                        const int ri = G.im / g[grd + 1].im, rj = G.jm / g[grd + 1].jm, rk = G.km / g[grd + 1].km;
+                        ic = (ic + ri - 1) / ri; jc = (jc + rj - 1) / rj; kc = (kc + rk - 1) / rk;
+                    }
+                }
+                const double xr = (double)(De - before) * c.photmax;
+                sum += xr;
+                sum2 += xr * xr;
+            }
+            Dv[v] = De;
+        }
+        R sol_ = 0;
+        for (int v = 0; v < c.nvar; ++v) sol_ += Dv[v];
+        sol_ /= (R)c.nvar;
+        double var_ = 0;
+        for (int v = 0; v < c.nvar; ++v)
+            var_ += 1. / (c.nvar - 0.5) * 1. / (c.nvar - 1) * (double)(Dv[v] - sol_) * (double)(Dv[v] - sol_);
+        const double n = (double)c.nvar * c.photmax;
+        const double m = sum / n;
+        *sol = (double)sol_;
+        *var = c.nvar > 1 ? var_ : 0.0;
+        *se = n > 1 ? std::sqrt(std::max(0.0, sum2 / n - m * m) / (n - 1)) : 0.0;
+        *nsteps = steps;
+    }
+};
+
+int build_ref_tables(const OrcRefConfig &c, const std::vector<Grid> &g, RefTables &t) {
+    // Tmax over interior cells and walls (code/mc_gpu.cu:470-486)
+    const Grid &f = g[0];
+    float Tmax = 0;
+    for (int k = 1; k <= f.km; ++k)
+        for (int j = 1; j <= f.jm; ++j)
+            for (int i = 1; i <= f.im; ++i) Tmax = std::max(Tmax, f.T[idxT(i, j, k, f.im, f.jm)]);
+    Tmax = std::max(Tmax, std::max(c.T_west, c.T_east));
+    t.Tmax = Tmax;
+    if (c.model == 1) {  // code/grey_tables.cpp:19-109
+        const int nB = 1000, nT = 55;
+        const float wvmax = 15000.f, Tmins = 500.f;
+        t.nB = nB; t.nT = nT; t.nQ = 1;
+        t.Tnb.resize(nT);
+        for (int i = 0; i < nT; ++i) t.Tnb[i] = Tmins * 0.9f + (Tmax * 1.1f - Tmins * 0.9f) * ((float)i) / ((float)nT);
+        std::vector<float> wvl(nB), wvr(nB);
+        wvl[0] = 0;
+        for (int i = 1; i < nB; ++i) wvl[i] = wvl[i - 1] + wvmax / nB;
+        wvr[0] = wvmax / nB;
+        for (int i = 1; i < nB; ++i) wvr[i] = wvr[i - 1] + wvmax / nB;
+        t.wvc.resize(nB);
+        for (int i = 0; i < nB; ++i) t.wvc[i] = (float)((wvl[i] + wvr[i]) / 2.);
+        t.kq.assign((size_t)nB * nT, c.kappa);
+        t.kP.assign(nT, c.kappa);
+        t.prob.assign((size_t)nT * nB, 0.f);
+        for (int i = 0; i < nT; ++i) {
+            float acc = I_blackC(t.Tnb[i], t.wvc[0]) * (wvr[0] - wvl[0]) * 100;
+            t.prob[(size_t)i * nB] = acc;
+            for (int b = 1; b < nB; ++b) {
+                acc = acc + I_blackC(t.Tnb[i], t.wvc[b]) * (wvr[b] - wvl[b]) * 100;
+                t.prob[(size_t)i * nB + b] = acc;
+            }
+            const float last = t.prob[(size_t)i * nB + nB - 1];
+            for (int b = 0; b < nB; ++b) t.prob[(size_t)i * nB + b] /= last;
+        }
+        t.kappamax = c.kappa;
+    } else {
+        t.nB = c.nB; t.nT = c.nT; t.nQ = c.nQ;
+        t.Tnb.assign(c.Tnb, c.Tnb + c.nT);
+        t.kq.assign(c.kq, c.kq + (size_t)c.nB * c.nT * c.nQ);
+        t.wvc.assign(c.wvc, c.wvc + c.nB);
+        t.prob.assign(c.prob, c.prob + (size_t)c.nT * c.nB);
+        if (c.probg) t.probg.assign(c.probg, c.probg + (size_t)c.nT * c.nB * c.nQ);
+        t.kP.assign(c.kP, c.kP + c.nT);
+        int tk = (int)((Tmax - t.Tnb[0]) / (t.Tnb[1] - t.Tnb[0]));
+        tk = std::max(0, std::min(tk, t.nT - 2));
+        t.kappamax = (t.kP[tk + 1] - t.kP[tk]) / (t.Tnb[tk + 1] - t.Tnb[tk]) * (Tmax - t.Tnb[tk]) + t.kP[tk];
+    }
+    t.tm = (int)((Tmax - t.Tnb[0]) / (t.Tnb[1] - t.Tnb[0]));
+    t.tm = std::max(0, std::min(t.tm, t.nT - 2));
+    t.Ib.assign((size_t)t.nT * t.nB, 0.f);
+    for (int i = 0; i < t.nT; ++i)
+        for (int b = 0; b < t.nB; ++b) t.Ib[(size_t)i * t.nB + b] = I_blackC(t.Tnb[i], t.wvc[b]);
+    t.ibw_w.resize(t.nB); t.ibw_e.resize(t.nB);
+    for (int b = 0; b < t.nB; ++b) { t.ibw_w[b] = I_blackC(c.T_west, t.wvc[b]); t.ibw_e[b] = I_blackC(c.T_east, t.wvc[b]); }
+    return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Tfort: (imax+2)(jmax+2)(kmax+2), i fastest, with ghosts.  cells: 3*ncells
+// 1-based (i, j, k).  Outputs per cell: reference batch mean, reference
+// variance (normaliser 1/((nVar-0.5)(nVar-1))), per-ray standard error, steps.
+int orc_ref_mc(const OrcRefConfig *c, const float *Tfort, int ncells, const int *cells, int nthreads,
+               double *sol, double *var, double *se, double *steps) {
+    if (!c || !Tfort || !cells || c->grid_num < 1 || c->grid_num > 6) return 1;
+    std::vector<Grid> g(c->grid_num);
+    for (int l = 0; l < c->grid_num; ++l) {
+        const int sh = 1 << l;
+        mk_grid(g[l], c->imax / sh, c->jmax / sh, c->kmax / sh, c->imax, c->maxs[l], c->Lx, c->Ly, c->Lz, c->stretched);
+    }
+    memcpy(g[0].T.data(), Tfort, g[0].T.size() * sizeof(float));
+    if (c->grid_num > 1) interp3d(g);
+    RefTables t;
+    build_ref_tables(*c, g, t);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int n = 0; n < ncells; ++n) {
+        const int i = cells[3 * n], j = cells[3 * n + 1], k = cells[3 * n + 2];
+        const uint64_t id = (uint64_t)i + (uint64_t)(c->imax + 2) * ((uint64_t)j + (uint64_t)(c->jmax + 2) * k);
+        if (c->use_double) RefMC<double>(*c, t, g).cell(i, j, k, id, sol + n, var + n, se + n, steps + n);
+        else RefMC<float>(*c, t, g).cell(i, j, k, id, sol + n, var + n, se + n, steps + n);
+    }
+    return 0;
+}
+
+// Spline-coarsened temperature of level `level` (for tests of interp3D).
+int orc_coarsen(int imax, int jmax, int kmax, float Lx, float Ly, float Lz, int stretched, int grid_num,
+                const float *Tfort, int level, float *Tout) {
+    if (level < 0 || level >= grid_num) return 1;
+    std::vector<Grid> g(grid_num);
+    for (int l = 0; l < grid_num; ++l) {
+        const int sh = 1 << l;
+        mk_grid(g[l], imax / sh, jmax / sh, kmax / sh, imax, 1, Lx, Ly, Lz, stretched);
+    }
+    memcpy(g[0].T.data(), Tfort, g[0].T.size() * sizeof(float));
+    interp3d(g);
+    memcpy(Tout, g[level].T.data(), g[level].T.size() * sizeof(float));
+    return 0;
+}
+
+// ===========================================================================
+// (2) packet scheme replay
+// ===========================================================================
+typedef struct {
+    int nw, na, nb;
+    float da, db;
+    const float *fw;          // nw+1
+    int ew0, ew1, ea0, ea1, eb0, eb1;
+    int tile_a;
+    int mode;                 // 0 grey, 1 table(T), 2 table(T, x)
+    int nfields;
+    const float *fieldT;      // [f][k][j][i] dense, i fastest
+    const float *fieldX;      // same, or NULL
+    int nbands, nq, nT, nX;
+    float T0, dT, X0, dX;
+    const float *ktab;        // [band][g][t][x]
+    const float *ibtab;       // [band][t]
+    const float *ibw;         // [2][band]
+    int n_groups;
+    const int *group_start;   // n_groups+1
+    const float *prob;        // alias thresholds
+    const int *alias;
+    const int *band;
+    const int *gq;
+    const float *W;
+    float kappa;
+    float T_west, T_east;
+    int rays;
+    const int *rays_per_packet;
+    uint64_t seed;
+    float toll;
+    int max_steps;
+    int use_double;
+} OrcPacketConfig;
+
+}  // extern "C"
+
+namespace {
+
+// Own polynomial exp/sin/cos of the packet specification (FP32, fmaf only).
+inline float p_expm1(float x) {
+    x = std::fmax(x, -87.0f);
+    const float n = rintf(x * 1.44269504088896341f);
+    float r = fmaf(-n, 0.693145751953125f, x);
+    r = fmaf(-n, 1.42860682030941723212e-6f, r);
+    const float cf[8] = {2.48015873015873016e-5f, 1.98412698412698413e-4f, 1.38888888888888889e-3f,
+                         8.33333333333333333e-3f, 4.16666666666666667e-2f, 1.66666666666666667e-1f, 0.5f, 1.0f};
+    float p = cf[0];
+    for (int i = 1; i < 8; ++i) p = fmaf(p, r, cf[i]);
+    p = p * r;
+    const int ni = (int)n;
+    uint32_t bits = (uint32_t)(ni + 127) << 23;
+    float two_n;
+    memcpy(&two_n, &bits, 4);
+    return fmaf(two_n, p, two_n - 1.0f);
+}
+
+inline void p_sincos_turn(uint32_t m, float *cs, float *sn) {
+    const uint32_t q = m >> 22, r = m & 0x3FFFFFu;
+    const bool hi = r > 0x200000u;
+    const float x = (float)(hi ? (0x400000u - r) : r) * 3.74507028e-7f;
+    const float z = x * x;
+    float ps = -2.50521083854417188e-8f;
+    ps = fmaf(ps, z, 2.75573192239858907e-6f);
+    ps = fmaf(ps, z, -1.98412698412698413e-4f);
+    ps = fmaf(ps, z, 8.33333333333333333e-3f);
+    ps = fmaf(ps, z, -1.66666666666666667e-1f);
+    const float s = fmaf(ps * z, x, x);
+    float pc = 2.08767569878680990e-9f;
+    pc = fmaf(pc, z, -2.75573192239858907e-7f);
+    pc = fmaf(pc, z, 2.48015873015873016e-5f);
+    pc = fmaf(pc, z, -1.38888888888888889e-3f);
+    pc = fmaf(pc, z, 4.16666666666666667e-2f);
+    pc = fmaf(pc, z, -0.5f);
+    const float c = fmaf(pc, z, 1.0f);
+    const float cq = hi ? s : c, sq = hi ? c : s;
+    switch (q) {
+        case 0: *cs = cq; *sn = sq; break;
+        case 1: *cs = -sq; *sn = cq; break;
+        case 2: *cs = -cq; *sn = -sq; break;
+        default: *cs = sq; *sn = -cq; break;
+    }
+}
+
+template <class R>
+inline void p_gpos(R v, R v0, R inv, int n, int *i, R *f) {
+    R p = (v - v0) * inv;
+    p = std::fmin(std::fmax(p, (R)0), (R)(n - 1));
+    int ii = (int)p;
+    ii = std::min(ii, n - 2);
+    *i = ii;
+    *f = p - (R)ii;
+}
+
+template <class R> inline R FMA(R a, R b, R c) { return std::fma(a, b, c); }
+template <> inline float FMA<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+template <class R>
+struct Packet {
+    const OrcPacketConfig &c;
+    R invdT, invdX;
+    long long plane, fstride;
+    Packet(const OrcPacketConfig &c_) : c(c_) {
+        invdT = (R)(1.0f / c.dT);
+        invdX = (R)(c.nX > 1 ? 1.0f / c.dX : 1.0f);
+        plane = (long long)c.na * c.nb;
+        fstride = plane * c.nw;
+    }
+    // dense host layout: cell (w, a, b) of field f at f*fstride + w + nw*(a + na*b)
+    inline long long cidx(int f, int w, int a, int b) const { return (long long)f * fstride + w + (long long)c.nw * (a + (long long)c.na * b); }
+    R kfun(int koff, int ti, R ft, int xi, R fx) const {
+        if (c.mode == 2) {
+            const float *s = c.ktab + koff + ti * c.nX + xi;
+            const R k00 = s[0], k01 = s[1], k10 = s[c.nX], k11 = s[c.nX + 1];
+            const R k0 = FMA<R>(fx, k01 - k00, k00), k1 = FMA<R>(fx, k11 - k10, k10);
+            return FMA<R>(ft, k1 - k0, k0);
+        }
+        const float *s = c.ktab + koff + ti;
+        const R k0 = s[0], k1 = s[1];
+        return FMA<R>(ft, k1 - k0, k0);
+    }
+    R ibfun(int nb, int ti, R ft) const {
+        const float *s = c.ibtab + (size_t)nb * c.nT + ti;
+        const R i0 = s[0], i1 = s[1];
+        return FMA<R>(ft, i1 - i0, i0);
+    }
+    R expm1n(R x) const;  // expm1 of x <= 0
+    void dirs(uint32_t x0, uint32_t x1, R *sW, R *sA, R *sB) const;
+
+    // One work item: returns per-lane S, S2; optional trace of ray tr.
+    void item(int f, int G, int p, double S[32], double S2[32], double *steps, int tr, int tmax, int32_t *rec,
+              int *nrec, uint32_t *rng) const {
+        const int ta = c.tile_a, tb = 32 / ta;
+        const int njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0;
+        const int npa = (njR + ta - 1) / ta, npb = (nkR + tb - 1) / tb;
+        const int pa = p % npa, rest = p / npa, pb = rest % npb, pw = rest / npb;
+        const int w0 = c.ew0 + pw;
+        int a0[32], b0[32];
+        bool act[32];
+        for (int l = 0; l < 32; ++l) {
+            a0[l] = c.ea0 + pa * ta + l % ta;
+            b0[l] = c.eb0 + pb * tb + l / ta;
+            act[l] = a0[l] < c.ea1 && b0[l] < c.eb1;
+            if (!act[l]) { a0[l] = c.ea0; b0[l] = c.eb0; }
+            S[l] = 0; S2[l] = 0;
+        }
+        const int N = c.rays_per_packet ? c.rays_per_packet[p] : c.rays;
+        int gs = 0, K = 1;
+        if (c.mode != 0) { gs = c.group_start[G]; K = c.group_start[G + 1] - gs; }
+        R Ti4[32], invTi4[32], ft_i[32], fx_i[32];
+        int ti_i[32], xi_i[32];
+        for (int l = 0; l < 32; ++l) {
+            const long long o = cidx(f, w0, a0[l], b0[l]);
+            const R Ti = (R)c.fieldT[o];
+            ti_i[l] = xi_i[l] = 0; ft_i[l] = fx_i[l] = 0; Ti4[l] = invTi4[l] = 0;
+            if (c.mode == 2) p_gpos<R>((R)c.fieldX[o], (R)c.X0, invdX, c.nX, &xi_i[l], &fx_i[l]);
+            if (c.mode == 0) {
+                const R t2 = Ti * Ti;
+                Ti4[l] = t2 * t2;
+                invTi4[l] = Ti4[l] > 0 ? (R)1 / Ti4[l] : (R)0;
+            } else {
+                p_gpos<R>(Ti, (R)c.T0, invdT, c.nT, &ti_i[l], &ft_i[l]);
+            }
+        }
+        const R oW = ((R)c.fw[w0] + (R)c.fw[w0 + 1]) * (R)0.5;
+        const R Wgrey = (R)(float)(4.0 * c.kappa * 5.670373e-08);
+        const float tw = c.T_west, te = c.T_east;
+        const R Tw4[2] = {(R)(tw * tw * tw * tw), (R)(te * te * te * te)};
+        const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
+        const int rb = tr >= 0 ? tr : 0, re = tr >= 0 ? tr + 1 : (K > 0 ? N : 0);
+        for (int r = rb; r < re; ++r) {
+            const uint32_t ctr[4] = {(uint32_t)r, (uint32_t)p, (uint32_t)G | ((uint32_t)f << 16), 0u};
+            uint32_t x[4];
+            philox(ctr, k0, k1, x);
+            if (rng) memcpy(rng, x, sizeof x);
+            R sW, sA, sB;
+            dirs(x[0], x[1], &sW, &sA, &sB);
+            int nbnd = 0, koff = 0;
+            R We = 0;
+            if (c.mode != 0) {
+                const int j = (int)(((uint64_t)x[2] * (uint64_t)K) >> 32);
+                int e = gs + j;
+                const float u = (float)(x[3] >> 8) * 5.9604644775390625e-8f;
+                if (!(u < c.prob[e])) e = gs + c.alias[e];
+                nbnd = c.band[e];
+                koff = (nbnd * c.nq + c.gq[e]) * c.nT * c.nX;
+                We = (R)c.W[e];
+            }
+            R w[32], Ii[32], invI[32], tau[32], D[32];
+            for (int l = 0; l < 32; ++l) {
+                if (c.mode == 0) {
+                    Ii[l] = Ti4[l]; invI[l] = invTi4[l]; w[l] = Wgrey * Ti4[l];
+                } else {
+                    const R ki = kfun(koff, ti_i[l], ft_i[l], xi_i[l], fx_i[l]);
+                    Ii[l] = ibfun(nbnd, ti_i[l], ft_i[l]);
+                    invI[l] = Ii[l] > 0 ? (R)1 / Ii[l] : (R)0;
+                    w[l] = We * ki * Ii[l];
+                }
+                tau[l] = act[l] ? (R)1 : (R)0;
+                D[l] = 0;
+            }
+            const R invW = (R)1 / std::fabs(sW), invA = (R)1 / std::fabs(sA), invB = (R)1 / std::fabs(sB);
+            const int dW = sW > 0 ? 1 : -1, dA = sA > 0 ? 1 : -1, dB = sB > 0 ? 1 : -1;
+            R tW = (dW > 0 ? ((R)c.fw[w0 + 1] - oW) : (oW - (R)c.fw[w0])) * invW;
+            const R dtA = (R)c.da * invA, dtB = (R)c.db * invB;
+            R tA = (R)0.5 * dtA, tB = (R)0.5 * dtB;
+            int nA = 0, nB = 0, cw = w0, stepn = 0;
+            int ca[32], cb[32];
+            for (int l = 0; l < 32; ++l) { ca[l] = a0[l]; cb[l] = b0[l]; }
+            R t = 0;
+            for (;;) {
+                int axis;
+                R tn;
+                if (tW <= tA && tW <= tB) { axis = 0; tn = tW; }
+                else if (tA <= tB) { axis = 1; tn = tA; }
+                else { axis = 2; tn = tB; }
+                const R ds = tn - t;
+                for (int l = 0; l < 32; ++l) {
+                    if (!(tau[l] > 0)) continue;
+                    *steps += 1;
+                    const long long o = cidx(f, cw, ca[l], cb[l]);
+                    R kj, gj;
+                    if (c.mode == 0) {
+                        const R Tj = (R)c.fieldT[o];
+                        const R t2 = Tj * Tj;
+                        gj = (Ti4[l] - t2 * t2) * invI[l];
+                        kj = (R)c.kappa;
+                    } else {
+                        int tj, xj = 0;
+                        R ftj, fxj = 0;
+                        if (c.mode == 2) p_gpos<R>((R)c.fieldX[o], (R)c.X0, invdX, c.nX, &xj, &fxj);
+                        p_gpos<R>((R)c.fieldT[o], (R)c.T0, invdT, c.nT, &tj, &ftj);
+                        kj = kfun(koff, tj, ftj, xj, fxj);
+                        gj = (Ii[l] - ibfun(nbnd, tj, ftj)) * invI[l];
+                    }
+                    const R alpha = -expm1n(-(kj * ds));
+                    const R tal = tau[l] * alpha;
+                    D[l] = FMA<R>(tal, gj, D[l]);
+                    tau[l] = tau[l] - tal;
+                    if (tau[l] < (R)c.toll) { D[l] = FMA<R>(tau[l], gj, D[l]); tau[l] = 0; }
+                }
+                if (rec && stepn < tmax) {
+                    int32_t *q = rec + 6 * stepn;
+                    q[0] = cw; q[1] = dA * nA; q[2] = dB * nB; q[3] = axis;
+                    const float dsf = (float)ds, tf = (float)tau[0];
+                    memcpy(&q[4], &dsf, 4);
+                    memcpy(&q[5], &tf, 4);
+                }
+                t = tn;
+                ++stepn;
+                if (axis == 0) {
+                    cw += dW;
+                    if (cw < 0 || cw >= c.nw) {
+                        const int side = cw < 0 ? 0 : 1;
+                        for (int l = 0; l < 32; ++l) {
+                            if (!(tau[l] > 0)) continue;
+                            const R Iw = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
+                            D[l] = FMA<R>(tau[l], (Ii[l] - Iw) * invI[l], D[l]);
+                            tau[l] = 0;
+                        }
+                        break;
+                    }
+                    tW = (dW > 0 ? ((R)c.fw[cw + 1] - oW) : (oW - (R)c.fw[cw])) * invW;
+                } else if (axis == 1) {
+                    ++nA;
+                    tA = ((R)nA + (R)0.5) * dtA;
+                    for (int l = 0; l < 32; ++l) { ca[l] += dA; if (ca[l] == c.na) ca[l] = 0; else if (ca[l] < 0) ca[l] = c.na - 1; }
+                } else {
+                    ++nB;
+                    tB = ((R)nB + (R)0.5) * dtB;
+                    for (int l = 0; l < 32; ++l) { cb[l] += dB; if (cb[l] == c.nb) cb[l] = 0; else if (cb[l] < 0) cb[l] = c.nb - 1; }
+                }
+                bool any = false;
+                for (int l = 0; l < 32; ++l) any = any || (tau[l] > 0);
+                if (!any) break;
+                if (stepn >= c.max_steps) break;
+            }
+            if (nrec) *nrec = stepn;
+            for (int l = 0; l < 32; ++l) {
+                if (!act[l]) continue;
+                const R X = w[l] * D[l];
+                const double Xd = (double)X;
+                S[l] += Xd;
+                S2[l] = std::fma(Xd, Xd, S2[l]);
+            }
+        }
+    }
+};
+
+template <> float Packet<float>::expm1n(float x) const { return p_expm1(x); }
+template <> double Packet<double>::expm1n(double x) const { return std::expm1(x); }
+template <> void Packet<float>::dirs(uint32_t x0, uint32_t x1, float *sW, float *sA, float *sB) const {
+    const float mu = fmaf((float)(x1 >> 8), -1.1920928955078125e-7f, 1.0f);
+    const float st = sqrtf(std::fmax(0.0f, fmaf(-mu, mu, 1.0f)));
+    float cph, sph;
+    p_sincos_turn(x0 >> 8, &cph, &sph);
+    *sW = mu; *sA = st * cph; *sB = st * sph;
+}
+template <> void Packet<double>::dirs(uint32_t x0, uint32_t x1, double *sW, double *sA, double *sB) const {
+    const double mu = 1.0 - (double)(x1 >> 8) * 1.1920928955078125e-7;
+    const double st = std::sqrt(std::max(0.0, 1.0 - mu * mu));
+    const double ph = 2.0 * 3.14159265358979323846 * (double)(x0 >> 8) * 5.9604644775390625e-8;
+    *sW = mu; *sA = st * std::cos(ph); *sB = st * std::sin(ph);
+}
+
+}  // namespace
+
+extern "C" {
+
+// Tally [f][G][iR][kR][jR][2] (sum X, sum X^2) exactly as the device stores it.
+int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double *steps_out) {
+    if (!c || c->tile_a < 1 || 32 % c->tile_a) return 1;
+    const int ta = c->tile_a, tb = 32 / ta;
+    const int niR = c->ew1 - c->ew0, njR = c->ea1 - c->ea0, nkR = c->eb1 - c->eb0;
+    const int npa = (njR + ta - 1) / ta, npb = (nkR + tb - 1) / tb;
+    const int np = npa * npb * niR;
+    const int nG = c->mode == 0 ? 1 : c->n_groups;
+    const long long items = (long long)c->nfields * nG * np;
+    const long long rc = (long long)niR * njR * nkR;
+    double steps = 0;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : steps)
+    for (long long it = 0; it < items; ++it) {
+        const int p = (int)(it % np);
+        const long long fg = it / np;
+        const int G = (int)(fg % nG), f = (int)(fg / nG);
+        double S[32], S2[32], st = 0;
+        if (c->use_double) Packet<double>(*c).item(f, G, p, S, S2, &st, -1, 0, nullptr, nullptr, nullptr);
+        else Packet<float>(*c).item(f, G, p, S, S2, &st, -1, 0, nullptr, nullptr, nullptr);
+        steps += st;
+        const int pa = p % npa, rest = p / npa, pb = rest % npb, pw = rest / npb;
+        for (int l = 0; l < 32; ++l) {
+            const int a = c->ea0 + pa * ta + l % ta, b = c->eb0 + pb * tb + l / ta;
+            if (a >= c->ea1 || b >= c->eb1) continue;
+            const long long tc = ((long long)pw * nkR + (b - c->eb0)) * njR + (a - c->ea0);
+            tally[2 * (fg * rc + tc)] = S[l];
+            tally[2 * (fg * rc + tc) + 1] = S2[l];
+        }
+    }
+    if (steps_out) *steps_out = steps;
+    return 0;
+}
+
+int orc_packet_trace(const OrcPacketConfig *c, int f, int G, int p, int r, int max_steps, int32_t *rec, int *n,
+                     uint32_t rng[4]) {
+    double S[32], S2[32], st = 0;
+    Packet<float>(*c).item(f, G, p, S, S2, &st, r, max_steps, rec, n, rng);
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,320 @@
+"""TEST INFRASTRUCTURE ONLY -- Python side of the oracle.
+
+* ctypes wrappers of oracle/liboracle.so (mc_oracle.cpp): the reference-
+  structured MC (code/mc_gpu.cu:44-438, 813-896) in FP32 or FP64, the packet
+  replay, Philox, the reference grids and the spline coarsening;
+* the analytic isothermal grey slab: div q(tau) = 2 kappa sigma
+  [(T^4 - Tw1^4) E2(tau) + (T^4 - Tw2^4) E2(tau_L - tau)] (exact solution of
+  the radiative transfer equation for a non-scattering isothermal slab between
+  black walls; E_n by series / continued fraction, written from their
+  definitions);
+* the optically thin limit 4 sigma (kappa_P(T) T^4 - kappa_P(T_w) T_w^4) per
+  cell for black walls (used to pin the oracle to code/resfortm.txt);
+* readers of the reference's own table reader built in oracle/_ref.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+
+import numpy as np
+
+from . import build as _build
+
+SIGMA = 5.670373e-08  # code/param.h:70
+
+_f = ctypes.POINTER(ctypes.c_float)
+_d = ctypes.POINTER(ctypes.c_double)
+_i = ctypes.POINTER(ctypes.c_int)
+_u32 = ctypes.POINTER(ctypes.c_uint32)
+_i32 = ctypes.POINTER(ctypes.c_int32)
+
+
+class RefConfig(ctypes.Structure):
+    _fields_ = [
+        ("imax", ctypes.c_int), ("jmax", ctypes.c_int), ("kmax", ctypes.c_int),
+        ("Lx", ctypes.c_float), ("Ly", ctypes.c_float), ("Lz", ctypes.c_float),
+        ("stretched", ctypes.c_int), ("grid_num", ctypes.c_int), ("maxs", ctypes.c_int * 6),
+        ("T_west", ctypes.c_float), ("T_east", ctypes.c_float), ("toll", ctypes.c_float),
+        ("nvar", ctypes.c_int), ("photmax", ctypes.c_int), ("hwfilter", ctypes.c_int),
+        ("use_double", ctypes.c_int), ("seed", ctypes.c_uint64), ("model", ctypes.c_int),
+        ("kappa", ctypes.c_float), ("nT", ctypes.c_int), ("nB", ctypes.c_int), ("nQ", ctypes.c_int),
+        ("Tnb", _f), ("kq", _f), ("wvc", _f), ("prob", _f), ("probg", _f), ("kP", _f),
+    ]
+
+
+class PacketConfig(ctypes.Structure):
+    _fields_ = [
+        ("nw", ctypes.c_int), ("na", ctypes.c_int), ("nb", ctypes.c_int),
+        ("da", ctypes.c_float), ("db", ctypes.c_float), ("fw", _f),
+        ("ew0", ctypes.c_int), ("ew1", ctypes.c_int), ("ea0", ctypes.c_int), ("ea1", ctypes.c_int),
+        ("eb0", ctypes.c_int), ("eb1", ctypes.c_int), ("tile_a", ctypes.c_int), ("mode", ctypes.c_int),
+        ("nfields", ctypes.c_int), ("fieldT", _f), ("fieldX", _f),
+        ("nbands", ctypes.c_int), ("nq", ctypes.c_int), ("nT", ctypes.c_int), ("nX", ctypes.c_int),
+        ("T0", ctypes.c_float), ("dT", ctypes.c_float), ("X0", ctypes.c_float), ("dX", ctypes.c_float),
+        ("ktab", _f), ("ibtab", _f), ("ibw", _f), ("n_groups", ctypes.c_int), ("group_start", _i),
+        ("prob", _f), ("alias", _i), ("band", _i), ("gq", _i), ("W", _f),
+        ("kappa", ctypes.c_float), ("T_west", ctypes.c_float), ("T_east", ctypes.c_float),
+        ("rays", ctypes.c_int), ("rays_per_packet", _i), ("seed", ctypes.c_uint64),
+        ("toll", ctypes.c_float), ("max_steps", ctypes.c_int), ("use_double", ctypes.c_int),
+    ]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_build.lib_path()):
+            _build.build(with_ref=False)
+        lib = ctypes.CDLL(_build.lib_path())
+        lib.orc_philox.argtypes = [_u32, _u32, _u32]
+        lib.orc_ref_faces.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_int, _f]
+        lib.orc_ref_mc.argtypes = [ctypes.POINTER(RefConfig), _f, ctypes.c_int, _i, ctypes.c_int, _d, _d, _d, _d]
+        lib.orc_ref_mc.restype = ctypes.c_int
+        lib.orc_coarsen.argtypes = [ctypes.c_int] * 3 + [ctypes.c_float] * 3 + [ctypes.c_int, ctypes.c_int, _f,
+                                                                                 ctypes.c_int, _f]
+        lib.orc_packet_mc.argtypes = [ctypes.POINTER(PacketConfig), ctypes.c_int, _d, _d]
+        lib.orc_packet_mc.restype = ctypes.c_int
+        lib.orc_packet_trace.argtypes = [ctypes.POINTER(PacketConfig)] + [ctypes.c_int] * 5 + [_i32, _i, _u32]
+        _lib = lib
+    return _lib
+
+
+def _fp(a):
+    return None if a is None else a.ctypes.data_as(_f)
+
+
+def philox(ctr, key):
+    c = (ctypes.c_uint32 * 4)(*[int(v) & 0xFFFFFFFF for v in ctr])
+    k = (ctypes.c_uint32 * 2)(*[int(v) & 0xFFFFFFFF for v in key])
+    o = (ctypes.c_uint32 * 4)()
+    load().orc_philox(c, k, o)
+    return list(o)
+
+
+def ref_faces(im: int, L: float, stretched: int = 1, im0: int | None = None) -> np.ndarray:
+    xu = np.zeros(im + 1, np.float32)
+    load().orc_ref_faces(im, im0 or im, L, stretched, _fp(xu))
+    return xu
+
+
+# ---------------------------------------------------------------------------
+# reference-structured MC
+# ---------------------------------------------------------------------------
+def ref_mc(T_fort: np.ndarray, cells: np.ndarray, *, imax, jmax, kmax, Lx, Ly, Lz, T_west, T_east,
+           model: int, tables: dict | None = None, kappa: float = 1.0, nvar: int = 3, photmax: int = 1000,
+           grid_num: int = 1, maxs=None, stretched: int = 1, toll: float = 1e-3, hwfilter: int = 0,
+           use_double: int = 1, seed: int = 1234, threads: int = 0) -> dict:
+    """Run the reference estimator on `cells` ((n, 3) 1-based i, j, k).
+
+    tables (model 0 ck / 2 particle): Tnb [nT], kq [nB][nT][nQ], wvc [nB],
+    prob [nT][nB], probg [nT][nB][nQ] or None, kP [nT].  model 1 builds the
+    reference grey-band tables from Tmax itself.
+    """
+    lib = load()
+    c = RefConfig()
+    c.imax, c.jmax, c.kmax = imax, jmax, kmax
+    c.Lx, c.Ly, c.Lz = Lx, Ly, Lz
+    c.stretched, c.grid_num = stretched, grid_num
+    if maxs is None:
+        maxs = [5] * (grid_num - 1) + [100000]
+    for i, v in enumerate(maxs):
+        c.maxs[i] = v
+    c.T_west, c.T_east, c.toll = T_west, T_east, toll
+    c.nvar, c.photmax, c.hwfilter, c.use_double, c.seed = nvar, photmax, hwfilter, use_double, seed
+    c.model, c.kappa = model, kappa
+    keep = []
+    if model != 1:
+        t = {k: (None if v is None else np.ascontiguousarray(v, np.float32)) for k, v in tables.items()}
+        keep.append(t)
+        c.nT, c.nB = t["Tnb"].size, t["wvc"].size
+        c.nQ = t["kq"].shape[-1] if t["kq"].ndim == 3 else 1
+        c.Tnb, c.kq, c.wvc, c.prob, c.kP = (_fp(t["Tnb"]), _fp(t["kq"]), _fp(t["wvc"]), _fp(t["prob"]),
+                                            _fp(t["kP"]))
+        c.probg = _fp(t.get("probg"))
+    T = np.ascontiguousarray(T_fort, np.float32)
+    assert T.size == (imax + 2) * (jmax + 2) * (kmax + 2)
+    cl = np.ascontiguousarray(cells, np.int32).reshape(-1, 3)
+    n = cl.shape[0]
+    sol, var, se, steps = (np.zeros(n) for _ in range(4))
+    rc = lib.orc_ref_mc(ctypes.byref(c), _fp(T), n, cl.ctypes.data_as(_i), threads,
+                        sol.ctypes.data_as(_d), var.ctypes.data_as(_d), se.ctypes.data_as(_d),
+                        steps.ctypes.data_as(_d))
+    assert rc == 0
+    return dict(Q=sol, var_ref=var, se=se, steps=steps)
+
+
+def coarsen(T_fort, imax, jmax, kmax, Lx, Ly, Lz, stretched, grid_num, level):
+    im, jm, km = imax >> level, jmax >> level, kmax >> level
+    out = np.zeros((km + 2) * (jm + 2) * (im + 2), np.float32)
+    load().orc_coarsen(imax, jmax, kmax, Lx, Ly, Lz, stretched, grid_num,
+                       _fp(np.ascontiguousarray(T_fort, np.float32)), level, _fp(out))
+    return out.reshape(km + 2, jm + 2, im + 2)
+
+
+# ---------------------------------------------------------------------------
+# packet replay: takes the solver's own geometry, tables and sampling
+# ---------------------------------------------------------------------------
+def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: int = 0, mode: int | None = None):
+    """Build a PacketConfig mirroring `solver`'s last solve (tables, sampling,
+    geometry, region, rays).  T, x: (nfields, kmax, jmax, imax) dense."""
+    cfg = solver.cfg
+    xu, dy, dz = solver.geometry()
+    T = np.ascontiguousarray(T, np.float32).reshape(-1, cfg.kmax, cfg.jmax, cfg.imax)
+    keep = dict(T=T, xu=xu)
+    c = PacketConfig()
+    c.nw, c.na, c.nb, c.da, c.db = cfg.imax, cfg.jmax, cfg.kmax, dy, dz
+    c.fw = _fp(xu)
+    i0, i1, j0, j1, k0, k1 = solver._region
+    c.ew0, c.ew1, c.ea0, c.ea1, c.eb0, c.eb1 = i0, i1, j0, j1, k0, k1
+    nj = j1 - j0
+    c.tile_a = cfg.tile_a or (32 if nj >= 32 else (16 if nj >= 16 else 8))
+    c.nfields = T.shape[0]
+    c.fieldT = _fp(T)
+    if x is not None:
+        X = np.ascontiguousarray(x, np.float32).reshape(T.shape)
+        keep["X"] = X
+        c.fieldX = _fp(X)
+    c.kappa, c.T_west, c.T_east = cfg.kappa, cfg.T_west, cfg.T_east
+    c.seed, c.toll, c.max_steps, c.use_double = cfg.seed, cfg.toll, cfg.max_steps, use_double
+    c.rays = solver_rays(solver)
+    if getattr(solver, "_keep", None):
+        rp = np.ascontiguousarray(solver._keep[0], np.int32)
+        keep["rp"] = rp
+        c.rays_per_packet = rp.ctypes.data_as(_i)
+    if cfg.model == 3:
+        c.mode = 0
+        c.n_groups = 1
+    else:
+        tb = solver.table()
+        s = solver.sampling()
+        c.mode = 2 if tb["nX"] > 1 else 1
+        c.nbands, c.nq, c.nT, c.nX = tb["nbands"], tb["nq"], tb["nT"], tb["nX"]
+        c.T0, c.dT, c.X0, c.dX = tb["T0"], tb["dT"], tb["X0"], tb["dX"]
+        k = np.ascontiguousarray(tb["k"], np.float32)
+        Ib = np.ascontiguousarray(tb["Ib"], np.float32)
+        keep.update(k=k, Ib=Ib, s=s)
+        c.ktab, c.ibtab, c.ibw = _fp(k), _fp(Ib), _fp(s["ibw"])
+        c.n_groups = s["n_groups"]
+        c.group_start = s["group_start"].ctypes.data_as(_i)
+        c.prob, c.W = _fp(s["prob"]), _fp(s["W"])
+        c.alias = s["alias"].ctypes.data_as(_i)
+        c.band = s["band"].ctypes.data_as(_i)
+        c.gq = s["gq"].ctypes.data_as(_i)
+    if mode is not None:
+        c.mode = mode
+    return c, keep
+
+
+def solver_rays(solver) -> int:
+    return int(getattr(solver, "_rays", solver.cfg.nvar * solver.cfg.photmax))
+
+
+def packet_mc(c: PacketConfig, n_groups: int, region_cells: int, threads: int = 0):
+    """Tally (nfields, n_groups, region_cells, 2) in the device's order."""
+    t = np.zeros((c.nfields, n_groups, region_cells, 2), np.float64)
+    steps = ctypes.c_double()
+    rc = load().orc_packet_mc(ctypes.byref(c), threads, t.ctypes.data_as(_d), ctypes.byref(steps))
+    assert rc == 0
+    return t, steps.value
+
+
+def packet_trace(c: PacketConfig, f: int, g: int, p: int, r: int, max_steps: int = 4096):
+    rec = np.zeros((max_steps, 6), np.int32)
+    n = ctypes.c_int()
+    rng = np.zeros(4, np.uint32)
+    load().orc_packet_trace(ctypes.byref(c), f, g, p, r, max_steps, rec.ctypes.data_as(_i32), ctypes.byref(n),
+                            rng.ctypes.data_as(_u32))
+    return rec[: min(n.value, max_steps)], n.value, rng
+
+
+# ---------------------------------------------------------------------------
+# analytic references
+# ---------------------------------------------------------------------------
+def expn(n: int, x: float) -> float:
+    """Exponential integral E_n(x) = int_1^inf exp(-x t) / t^n dt, x > 0
+    (continued fraction for x > 1, power series otherwise)."""
+    if x <= 0:
+        return math.inf if n <= 1 else 1.0 / (n - 1)
+    euler = 0.5772156649015329
+    if x > 1.0:
+        b = x + n
+        c = 1e300
+        d = 1.0 / b
+        h = d
+        for i in range(1, 500):
+            a = -i * (n - 1 + i)
+            b += 2.0
+            d = 1.0 / (a * d + b)
+            c = b + a / c
+            de = c * d
+            h *= de
+            if abs(de - 1.0) < 1e-15:
+                break
+        return h * math.exp(-x)
+    ans = (1.0 / (n - 1)) if n != 1 else (-math.log(x) - euler)
+    fact = 1.0
+    for i in range(1, 500):
+        fact *= -x / i
+        if i != n - 1:
+            de = -fact / (i - n + 1)
+        else:
+            psi = -euler + sum(1.0 / k for k in range(1, n))
+            de = fact * (-math.log(x) + psi)
+        ans += de
+        if abs(de) < abs(ans) * 1e-16:
+            break
+    return ans
+
+
+def slab_divq(y: np.ndarray, L: float, kappa: float, T: float, Tw1: float, Tw2: float) -> np.ndarray:
+    """Exact div q [W/m^3] at wall distances y (from wall 1) of an isothermal
+    grey slab of thickness L between black walls at Tw1, Tw2."""
+    tau = kappa * np.asarray(y, np.float64)
+    tl = kappa * L
+    e1 = np.array([expn(2, t) for t in tau])
+    e2 = np.array([expn(2, tl - t) for t in tau])
+    return 2.0 * kappa * SIGMA * ((T ** 4 - Tw1 ** 4) * e1 + (T ** 4 - Tw2 ** 4) * e2)
+
+
+def thin_limit(T: np.ndarray, Tw: float, Tnb: np.ndarray, kP: np.ndarray) -> np.ndarray:
+    """Optically thin limit 4 sigma (kP(T) T^4 - kP(Tw) Tw^4)."""
+    k = np.interp(T, Tnb, kP)
+    kw = np.interp(Tw, Tnb, kP)
+    return 4.0 * SIGMA * (k * T ** 4 - kw * Tw ** 4)
+
+
+# ---------------------------------------------------------------------------
+# the reference's own table reader (oracle/_ref), where it was built
+# ---------------------------------------------------------------------------
+def ref_tables_available(kind: str) -> bool:
+    return os.path.exists(_build.ref_lib_path(kind))
+
+
+def ref_readT(kind: str, table_root: str, Tmax: float) -> dict:
+    """Call the reference's readT (compiled from code/read_tables.cpp); it
+    opens ../distr/tables/... relative to the working directory, so this
+    switches to <table_root>/code for the call."""
+    lib = ctypes.CDLL(_build.ref_lib_path(kind))
+    nt, nb, nq = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    lib.ref_table_sizes(ctypes.byref(nt), ctypes.byref(nb), ctypes.byref(nq))
+    nT, nB, nQ = nt.value, nb.value, nq.value
+    out = dict(Tnb=np.zeros(nT, np.float32), kP=np.zeros(nT, np.float32), wvc=np.zeros(nB, np.float32),
+               kavg=np.zeros(nB, np.float32), kq=np.zeros((nB, nT, nQ), np.float32),
+               prob=np.zeros((nT, nB), np.float32), probg=np.zeros((nT, nB, nQ), np.float32))
+    km = ctypes.c_float()
+    lib.ref_readT.argtypes = [ctypes.c_float] + [_f] * 7 + [_f]
+    cwd = os.getcwd()
+    os.chdir(os.path.join(table_root, "code"))
+    try:
+        lib.ref_readT(Tmax, *[_fp(out[k]) for k in ("Tnb", "kP", "wvc", "kavg", "kq", "prob", "probg")],
+                      ctypes.byref(km))
+    finally:
+        os.chdir(cwd)
+    out["kappamax"] = km.value
+    return out

@@ -1,0 +1,388 @@
+"""GPU parity tests: the CUDA march (through the C ABI) against the oracle.
+
+* bit-exact: every (cell, band group) tally of a solve equals the oracle's
+  FP32 replay of the packet scheme -- same Philox counters, same alias draw,
+  same voxel walk, same rounding -- for the grey model, the reference particle
+  and correlated-k tables, a synthetic k(T, x_H2O) table with band groups,
+  several snapshots, adaptive ray counts and a sub-region;
+* trace: the voxel-index walk and the RNG words of single rays;
+* Philox pinned to curand's Philox4x32_10;
+* statistical: per-cell agreement (combined 3 sigma) with the oracle's
+  reference-structured estimator (code/mc_gpu.cu:44-438) on the same field
+  and tables;
+* analytic: the isothermal grey slab (E_2 solution);
+* golden: code/resfortm.txt plane means;
+* the drop-in pair mc_gpu_ / get_results_ and the error paths.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+import pytest
+
+import dnsmc_gb300 as D
+from dnsmc_gb300 import _lib, synth
+from oracle import oracle as O
+from tables_io import write_ck_tables, write_particle_tables
+
+pytestmark = pytest.mark.gpu
+
+
+def smooth_field(ni, nj, nk, lo, hi, seed):
+    rng = np.random.default_rng(seed)
+    i = (np.arange(ni) + 0.5) / ni
+    j = np.arange(nj) / nj
+    k = np.arange(nk) / nk
+    base = lo + (hi - lo) * 4 * i * (1 - i)
+    f = (np.sin(2 * np.pi * j)[None, :, None] * np.cos(2 * np.pi * k)[:, None, None] * 0.04
+         + rng.normal(0, 0.01, (nk, nj, ni)))
+    return (base[None, None, :] * (1 + f)).astype(np.float32)
+
+
+def region_tally_to_dense(tal, solver, ng):
+    i0, i1, j0, j1, k0, k1 = solver._region
+    ni, nj, nk = i1 - i0, j1 - j0, k1 - k0
+    nf = tal.shape[0]
+    return tal.reshape(nf, ng, ni, nk, nj, 2).transpose(0, 1, 3, 4, 2, 5)
+
+
+def rays_per_cell(solver):
+    i0, i1, j0, j1, k0, k1 = solver._region
+    ni, nj, nk = i1 - i0, j1 - j0, k1 - k0
+    if not solver._keep:
+        return np.full((nk, nj, ni), solver._rays, np.float64)
+    rp = solver._keep[0]
+    ta = solver.cfg.tile_a or (32 if nj >= 32 else (16 if nj >= 16 else 8))
+    tb = 32 // ta
+    npa, npb = -(-nj // ta), -(-nk // tb)
+    kk, jj, ii = np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni), indexing="ij")
+    p = (ii * npb + kk // tb) * npa + jj // ta
+    return rp[p].astype(np.float64)
+
+
+def assert_bitexact(solver, T, x=None):
+    Q, S = solver.solve(timeout_s=120)
+    Qg, Vg = solver.group_results()
+    ng = Qg.shape[1]
+    c, keep = O.packet_config(solver, T, x)
+    i0, i1, j0, j1, k0, k1 = solver._region
+    tal, steps = O.packet_mc(c, ng, (i1 - i0) * (j1 - j0) * (k1 - k0))
+    tal = region_tally_to_dense(tal, solver, ng)
+    N = rays_per_cell(solver)
+    empty = np.zeros(ng, bool)
+    if solver.cfg.model != D.MODEL_GREY:
+        gs = solver.sampling()["group_start"]
+        empty = gs[1:] == gs[:-1]
+    Qexp = np.zeros_like(Q)
+    Vexp = np.zeros_like(Q)
+    for g in range(ng):
+        with np.errstate(invalid="ignore", divide="ignore"):
+            m = np.where(N > 0, tal[:, g, ..., 0] / N, 0.0)
+            v = np.where(N > 1, np.maximum(0.0, tal[:, g, ..., 1] / N - m * m) / (N - 1), 0.0)
+        if empty[g]:
+            m, v = np.zeros_like(m), np.zeros_like(v)
+        np.testing.assert_array_equal(Qg[:, g], m)
+        np.testing.assert_array_equal(Vg[:, g], v)
+        Qexp = Qexp + m
+        Vexp = Vexp + v
+    np.testing.assert_array_equal(Q, Qexp)
+    np.testing.assert_array_equal(S, np.sqrt(Vexp))
+    cnt = solver.counters()
+    assert cnt.steps == steps
+    assert solver.status() == 0
+    assert np.isfinite(Q).all() and np.abs(Q).max() > 0
+    return Q, S
+
+
+def test_bitexact_grey():
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=16, jmax=32, kmax=8, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=300, T_east=500, kappa=1.5, seed=11))
+    T = smooth_field(16, 32, 8, 400, 1200, 1)
+    s.set_fields(T)
+    s.set_rays(96)
+    assert_bitexact(s, T)
+    s.close()
+
+
+def test_bitexact_particle_tables_stretched(tmp_path, particle_tables):
+    write_particle_tables(str(tmp_path), particle_tables)
+    s = D.Solver(D.default_config(model=D.MODEL_PARTICLE, imax=16, jmax=16, kmax=8, stretched_x=1, seed=5))
+    s.load_reference_tables(str(tmp_path), D.MODEL_PARTICLE)
+    T = smooth_field(16, 16, 8, 520, 990, 2)
+    s.set_fields(T)
+    s.set_rays(48)
+    assert_bitexact(s, T)
+    s.close()
+
+
+def test_bitexact_ck_tables(tmp_path, ck_tables):
+    write_ck_tables(str(tmp_path), ck_tables)
+    s = D.Solver(D.default_config(model=D.MODEL_CK, imax=12, jmax=32, kmax=4, Lx=0.5, Ly=1.0, Lz=0.25,
+                                  stretched_x=0, T_west=600, T_east=800, seed=3, n_groups=3))
+    s.load_reference_tables(str(tmp_path), D.MODEL_CK)
+    T = smooth_field(12, 32, 4, 550, 1000, 3)
+    s.set_fields(T)
+    s.set_rays(64)
+    assert_bitexact(s, T)
+    s.close()
+
+
+def test_bitexact_table_x_groups_fields_region():
+    tb = synth.ck_table(nbands=16, nq=8, nT=24, nX=5, seed=4)
+    s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=10, jmax=40, kmax=6, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=400, T_east=400, seed=21, n_groups=4, tile_a=16))
+    s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+    T = np.stack([smooth_field(10, 40, 6, 450, 1700, 5 + f) for f in range(2)])
+    x = np.stack([(0.1 + 0.05 * np.random.default_rng(9 + f).uniform(-1, 1, (6, 40, 10))).astype(np.float32)
+                  for f in range(2)])
+    s.set_fields(T, x)
+    s.set_region(1, 9, 3, 37, 0, 5)
+    npk = s.packet_count()
+    s.set_rays(0, np.random.default_rng(0).integers(0, 40, npk))
+    assert_bitexact(s, T, x)
+    s.close()
+
+
+def test_trace_matches_replay(tmp_path, ck_tables):
+    write_ck_tables(str(tmp_path), ck_tables)
+    s = D.Solver(D.default_config(model=D.MODEL_CK, imax=12, jmax=32, kmax=4, Lx=0.5, Ly=1.0, Lz=0.25,
+                                  stretched_x=1, T_west=600, T_east=800, seed=77))
+    s.load_reference_tables(str(tmp_path), D.MODEL_CK)
+    T = smooth_field(12, 32, 4, 550, 1000, 8)
+    s.set_fields(T)
+    s.set_rays(8)
+    s.solve(timeout_s=60)
+    c, keep = O.packet_config(s, T, None)
+    npk = s.packet_count()
+    for p, r in [(0, 0), (npk - 1, 3), (npk // 2, 7), (5, 1)]:
+        rec, n, rng = s.trace(0, 0, p, r)
+        rec2, n2, rng2 = O.packet_trace(c, 0, 0, p, r)
+        assert n == n2
+        np.testing.assert_array_equal(rng, rng2)
+        np.testing.assert_array_equal(rec, rec2)
+        assert rng[0] == O.philox((r, p, 0, 0), (77, 0))[0]
+    s.close()
+
+
+def test_philox_matches_curand(tmp_path):
+    nvcc = "/usr/local/cuda/bin/nvcc"
+    so = str(tmp_path / "libpin.so")
+    src = os.path.join(os.path.dirname(__file__), "philox_pin.cu")
+    subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-shared", "-Xcompiler", "-fPIC", src,
+                    "-o", so], check=True, capture_output=True)
+    lib = ctypes.CDLL(so)
+    rng = np.random.default_rng(1)
+    n = 512
+    ctr = rng.integers(0, 2 ** 32, (n, 4), dtype=np.uint64).astype(np.uint32)
+    key = rng.integers(0, 2 ** 32, (n, 2), dtype=np.uint64).astype(np.uint32)
+    out = np.zeros((n, 4), np.uint32)
+    p = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+    assert lib.curand_philox_batch(p(ctr), p(key), p(out), n) == 0
+    mine = np.array([O.philox(ctr[i], key[i]) for i in range(n)], np.uint32)
+    np.testing.assert_array_equal(out, mine)
+
+
+def _zstats(qa, sa, qb, sb):
+    z = (qa - qb) / np.sqrt(sa ** 2 + sb ** 2)
+    return z, math.sqrt(float((z ** 2).mean())), int((np.abs(z) > 3).sum())
+
+
+def _parity_vs_reference(s, T, model, tables, Lx, Ly, Lz, Tw, Te, stretched, ncells=64, photmax=1500):
+    ni, nj, nk = s.cfg.imax, s.cfg.jmax, s.cfg.kmax
+    s.set_fields(T)
+    s.set_rays(3 * photmax * 2)
+    Q, S = s.solve(timeout_s=300)
+    rng = np.random.default_rng(42)
+    cells = []
+    used = set()
+    while len(cells) < ncells:
+        i, j, k = int(rng.integers(0, ni)), int(rng.integers(0, nj)), int(rng.integers(0, nk))
+        pk = (i, k, j // 32)
+        if pk in used:
+            continue
+        used.add(pk)
+        cells.append((i, j, k))
+    cells = np.array(cells)
+    Tf = np.zeros((nk + 2, nj + 2, ni + 2), np.float32)
+    Tf[1:-1, 1:-1, 1:-1] = T
+    r = O.ref_mc(Tf.ravel(), cells + 1, imax=ni, jmax=nj, kmax=nk, Lx=Lx, Ly=Ly, Lz=Lz, T_west=Tw, T_east=Te,
+                 model=model, tables=tables, kappa=s.cfg.kappa, nvar=3, photmax=photmax, grid_num=1,
+                 stretched=stretched, use_double=1, seed=9)
+    qg = Q[0][cells[:, 2], cells[:, 1], cells[:, 0]]
+    sg = S[0][cells[:, 2], cells[:, 1], cells[:, 0]]
+    z, rms, n3 = _zstats(qg, sg, r["Q"], r["se"])
+    # 64 independent cells: P(n3 > 3) < 1e-3 under the null
+    assert n3 <= 3, (z, rms)
+    assert 0.6 < rms < 1.45, (z, rms)
+
+
+def test_statistical_parity_reference_ck(tmp_path, ck_tables):
+    write_ck_tables(str(tmp_path), ck_tables)
+    s = D.Solver(D.default_config(model=D.MODEL_CK, imax=16, jmax=32, kmax=8, Lx=0.3, Ly=0.6, Lz=0.3,
+                                  stretched_x=1, T_west=520, T_east=700, seed=13))
+    s.load_reference_tables(str(tmp_path), D.MODEL_CK)
+    T = smooth_field(16, 32, 8, 560, 1000, 13)
+    tables = dict(Tnb=ck_tables["Tnb"], kq=ck_tables["kq"], wvc=ck_tables["wvc"], prob=ck_tables["prob"],
+                  probg=ck_tables["probg"], kP=ck_tables["kP"])
+    _parity_vs_reference(s, T, 0, tables, 0.3, 0.6, 0.3, 520, 700, 1)
+    s.close()
+
+
+def test_statistical_parity_reference_grey_bands():
+    s = D.Solver(D.default_config(model=D.MODEL_GREY_BANDS, imax=16, jmax=32, kmax=8, Lx=1.0, Ly=2.0, Lz=1.0,
+                                  stretched_x=1, T_west=500, T_east=500, kappa=1.0, seed=17))
+    s.use_grey_band_tables()
+    T = smooth_field(16, 32, 8, 600, 1100, 17)
+    _parity_vs_reference(s, T, 1, None, 1.0, 2.0, 1.0, 500, 500, 1, photmax=800)
+    s.close()
+
+
+def test_grey_slab_matches_analytic_solution():
+    """Isothermal slab T = 1000 K, kappa = 1, tau_L = 2, walls 0 K and 300 K."""
+    ni, nj, nk = 64, 32, 16
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.2831853,
+                                  Lz=3.1415927, stretched_x=0, T_west=0.0, T_east=300.0, kappa=1.0, seed=3))
+    s.set_fields(np.full((nk, nj, ni), 1000.0, np.float32))
+    s.set_rays(8192)
+    Q, S = s.solve(timeout_s=120)
+    yc = (np.arange(ni) + 0.5) * 2.0 / ni
+    exact = O.slab_divq(yc, 2.0, 1.0, 1000.0, 0.0, 300.0)
+    # one cell per packet is independent (lanes of a packet share rays)
+    q = Q[0][:, 0, :].mean(0)
+    se = np.sqrt((S[0][:, 0, :] ** 2).sum(0)) / nk
+    z = (q - exact) / se
+    assert np.abs(z).max() < 4.0, z
+    assert math.sqrt((z ** 2).mean()) < 1.5
+    assert np.abs(q / exact - 1).max() < 0.01
+    s.close()
+
+
+def test_golden_resfortm_on_gpu(tmp_path, particle_tables, resfortm):
+    """code/resfortm.txt (particle tables, 64^3, black x-walls 500 K,
+    T = 500 + 2000 x(1-x), stretched x): plane means over a 32x32 (j,k)
+    patch of every x-row agree with the golden rows."""
+    write_particle_tables(str(tmp_path), particle_tables)
+    s = D.Solver(D.default_config(seed=7))
+    s.load_reference_tables(str(tmp_path), D.MODEL_PARTICLE)
+    xu, _, _ = s.geometry()
+    x = 0.5 * (xu[1:] + xu[:-1])
+    T = np.broadcast_to((500 - 2000 * x ** 2 + 2000 * x).astype(np.float32), (64, 64, 64)).copy()
+    s.set_fields(T)
+    s.set_region(0, 64, 0, 32, 0, 32)
+    s.set_rays(3000)
+    Q, S = s.solve(timeout_s=300)
+    q = Q[0][:, 0, :].mean(0)  # one lane per packet: 32 independent packets per row
+    se = np.sqrt((S[0][:, 0, :] ** 2).sum(0)) / 32
+    gse = resfortm["plane_std"] / 64
+    z = (q - resfortm["Q"]) / np.sqrt(se ** 2 + gse ** 2)
+    assert math.sqrt((z ** 2).mean()) < 1.6, z
+    assert np.abs(z).max() < 4.2, z
+    s.close()
+
+
+def test_dropin_pair_layouts_and_ghosts():
+    ni, nj, nk, prow = 16, 16, 8, 2
+    cfg = D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, p_row=prow, Lx=2.0, Ly=6.28, Lz=3.14,
+                           stretched_x=1, T_west=300, T_east=300, kappa=1.0, nvar=3, photmax=40, seed=5)
+    D.dropin_configure(cfg)
+    T = smooth_field(ni, nj, nk, 400, 1200, 21)
+    Tf = np.zeros((nk + 2, nj + 2, ni + 2), np.float32)
+    Tf[1:-1, 1:-1, 1:-1] = T
+    Tf[0] = Tf[-1] = -5.0  # ghost garbage must be ignored
+    jl = nj // prow
+    Qr = np.full((nk + 2, jl + 2, ni + 2), -7.0, np.float32)
+    Vr = np.full_like(Qr, -7.0)
+    D.mc_gpu(Tf, 9)
+    D.get_results(Qr, Vr)
+    D.dropin_release()
+    inner = (slice(1, -1), slice(1, -1), slice(1, -1))
+    ghost = np.ones(Qr.shape, bool)
+    ghost[inner] = False
+    assert (Qr[ghost] == -7.0).all() and (Vr[ghost] == -7.0).all()
+    s = D.Solver(cfg)
+    s.set_fields(T)
+    s.set_region(0, ni, 8, 16, 0, nk)
+    s.set_rays(120)
+    Q, S = s.solve(timeout_s=60)
+    np.testing.assert_array_equal(Qr[inner], Q[0].astype(np.float32))
+    np.testing.assert_array_equal(Vr[inner], np.sqrt(S[0] ** 2 * 3 / 2.5).astype(np.float32))
+    s.close()
+
+
+def test_dropin_reads_reference_tables_by_default(tmp_path, particle_tables, monkeypatch):
+    write_particle_tables(str(tmp_path), particle_tables)
+    monkeypatch.setenv("DNSMC_IMAX", "16")
+    monkeypatch.setenv("DNSMC_JMAX", "32")
+    monkeypatch.setenv("DNSMC_KMAX", "8")
+    monkeypatch.setenv("DNSMC_PHOTMAX", "20")
+    monkeypatch.setenv("DNSMC_TABLES", str(tmp_path))
+    D.dropin_configure(None)
+    Tf = np.zeros((10, 34, 18), np.float32)
+    Tf[1:-1, 1:-1, 1:-1] = smooth_field(16, 32, 8, 520, 990, 4)
+    Qr = np.zeros((10, 34, 18), np.float32)
+    Vr = np.zeros_like(Qr)
+    D.mc_gpu(Tf, 1)
+    D.get_results(Qr, Vr)
+    D.dropin_release()
+    assert np.isfinite(Qr).all() and (Vr[1:-1, 1:-1, 1:-1] > 0).all()
+
+
+def test_status_and_errors():
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=16, jmax=32, kmax=8, max_steps=3, seed=1))
+    with pytest.raises(D.DnsmcError) as e:
+        s.solve()
+    assert e.value.code == _lib.ERR_STATE
+    bad = smooth_field(16, 32, 8, 400, 900, 1)
+    bad[2, 3, 4] = -1.0
+    with pytest.raises(D.DnsmcError) as e:
+        s.set_fields(bad)
+    assert e.value.code == _lib.ERR_ARG
+    s.set_fields(smooth_field(16, 32, 8, 400, 900, 1))
+    s.set_rays(16)
+    s.solve(timeout_s=60)
+    assert s.status() & D.STATUS_STEP_CAP
+    s.close()
+
+
+def test_bounded_wait_times_out_then_completes():
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=64, jmax=64, kmax=64, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=300, T_east=300, kappa=0.2, seed=2))
+    s.set_fields(synth.grey_channel(64)["T"])
+    s.set_rays(2048)
+    s.solve_async()
+    with pytest.raises(D.DnsmcError) as e:
+        s.wait(1e-6)
+    assert e.value.code == _lib.ERR_TIMEOUT
+    s.wait(120)
+    Q, S = s.results()
+    assert np.isfinite(Q).all()
+    s.close()
+
+
+def test_device_field_input_matches_host_input():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("torch without CUDA")
+    T = synth.grey_channel(32)["T"]
+    cfg = D.default_config(model=D.MODEL_GREY, imax=32, jmax=32, kmax=32, Lx=2.0, Ly=6.28, Lz=3.14,
+                           stretched_x=0, T_west=300, T_east=300, kappa=1.0, seed=4)
+    a = D.Solver(cfg)
+    a.set_fields(T)
+    a.set_rays(64)
+    Qa, _ = a.solve(timeout_s=60)
+    b = D.Solver(cfg)
+    dT = torch.from_numpy(T).cuda()
+    torch.cuda.synchronize()
+    _lib.check(b._lib.dnsmc_set_fields_device(b._h, 1, ctypes.c_void_p(dT.data_ptr()), None))
+    b._nfields = 1
+    b.set_rays(64)
+    Qb, _ = b.solve(timeout_s=60)
+    np.testing.assert_array_equal(Qa, Qb)
+    assert a.tmax() == b.tmax()
+    a.close()
+    b.close()
