@@ -58,7 +58,7 @@ def fourier_fluct(ni: int, nj: int, nk: int, seed: int, nmodes: int = 8) -> np.n
     Y = np.sin(m[:, None] * math.pi * (y[None, :] + 1.0) / 2.0)            # (n, ni)
     Z = np.cos(2 * math.pi * m[:, None] * z[None, :] / LZ + qz[:, None])   # (l, nk)
     f = np.einsum("mnl,mj,ni,lk->kji", a, X, Y, Z, optimize=True)
-    return (f / np.abs(f).max()).astype(np.float64)
+    return np.ascontiguousarray(f / np.abs(f).max(), dtype=np.float64)
 
 
 def channel_temperature(n: int, T_wall: float, T_rise: float, seed: int, amp: float = 0.05) -> np.ndarray:
@@ -66,7 +66,7 @@ def channel_temperature(n: int, T_wall: float, T_rise: float, seed: int, amp: fl
     y = cell_centres(n, LY) - 1.0
     base = T_wall + T_rise * (1.0 - y * y)
     f = fourier_fluct(n, n, n, seed)
-    return (base[None, None, :] * (1.0 + amp * f)).astype(np.float32)
+    return np.ascontiguousarray(base[None, None, :] * (1.0 + amp * f), dtype=np.float32)
 
 
 def grey_channel(n: int = 64, seed: int = 0) -> dict:
@@ -83,7 +83,7 @@ def slab(n: int = 64, T: float = 1000.0) -> dict:
 
 def h2o_fraction(n: int, seed: int) -> np.ndarray:
     """x_H2O = 0.1 + 0.05 f with an independent fluctuation (seed + 1000)."""
-    return (0.1 + 0.05 * fourier_fluct(n, n, n, seed + 1000)).astype(np.float32)
+    return np.ascontiguousarray(0.1 + 0.05 * fourier_fluct(n, n, n, seed + 1000), dtype=np.float32)
 
 
 def ck_channel(n: int = 128, seed: int = 0) -> dict:

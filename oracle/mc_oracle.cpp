@@ -545,6 +545,9 @@ typedef struct {
     float toll;
     int max_steps;
     int use_double;
+    int sampler;              // 0: Philox iid, 1: digitally shifted Sobol' net (RQMC)
+    int nbatch;               // RQMC replicates per (packet, group)
+    int n_tbins;              // >0: sampling tables per temperature bin
 } OrcPacketConfig;
 
 }  // extern "C"
@@ -594,6 +597,41 @@ inline void p_sincos_turn(uint32_t m, float *cs, float *sn) {
         case 2: *cs = -cq; *sn = -sq; break;
         default: *cs = sq; *sn = -cq; break;
     }
+}
+
+// Sobol' direction numbers (Bratley-Fox recurrence) for the first four
+// dimensions: primitive polynomials 1 (van der Corput), x+1, x^2+x+1,
+// x^3+x+1 with initial m = (1), (1), (1,3), (1,3,1).
+struct SobolDirs {
+    uint32_t v[4][32];
+    SobolDirs() {
+        const int s_[4] = {0, 1, 2, 3};
+        const int a_[4] = {0, 0, 1, 1};
+        const uint32_t m0[4][3] = {{1, 0, 0}, {1, 0, 0}, {1, 3, 0}, {1, 3, 1}};
+        for (int d = 0; d < 4; ++d) {
+            uint32_t m[33] = {0};
+            if (d == 0) {
+                for (int k = 1; k <= 32; ++k) m[k] = 1;
+            } else {
+                const int sd = s_[d];
+                for (int k = 1; k <= sd; ++k) m[k] = m0[d][k - 1];
+                for (int k = sd + 1; k <= 32; ++k) {
+                    uint32_t x = m[k - sd] ^ (m[k - sd] << sd);
+                    for (int i = 1; i < sd; ++i)
+                        if ((a_[d] >> (sd - 1 - i)) & 1) x ^= m[k - i] << i;
+                    m[k] = x;
+                }
+            }
+            for (int k = 1; k <= 32; ++k) v[d][k - 1] = m[k] << (32 - k);
+        }
+    }
+};
+static const SobolDirs g_sobol;
+inline void sobol4(uint32_t idx, uint32_t out[4]) {
+    uint32_t a = 0, b = 0, c = 0, d = 0;
+    for (int k = 0; idx; ++k, idx >>= 1)
+        if (idx & 1) { a ^= g_sobol.v[0][k]; b ^= g_sobol.v[1][k]; c ^= g_sobol.v[2][k]; d ^= g_sobol.v[3][k]; }
+    out[0] = a; out[1] = b; out[2] = c; out[3] = d;
 }
 
 template <class R>
@@ -660,7 +698,17 @@ struct Packet {
         }
         const int N = c.rays_per_packet ? c.rays_per_packet[p] : c.rays;
         int gs = 0, K = 1;
-        if (c.mode != 0) { gs = c.group_start[G]; K = c.group_start[G + 1] - gs; }
+        if (c.mode != 0) {
+            int binoff = 0;
+            if (c.n_tbins > 0) {
+                const float T0v = c.fieldT[cidx(f, w0, a0[0], b0[0])];
+                int bin = (int)rintf((T0v - c.T0) / c.dT);
+                bin = std::min(std::max(bin, 0), c.n_tbins - 1);
+                binoff = bin * c.n_groups;
+            }
+            gs = c.group_start[binoff + G];
+            K = c.group_start[binoff + G + 1] - gs;
+        }
         R Ti4[32], invTi4[32], ft_i[32], fx_i[32];
         int ti_i[32], xi_i[32];
         for (int l = 0; l < 32; ++l) {
@@ -683,9 +731,18 @@ struct Packet {
         const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
         const int rb = tr >= 0 ? tr : 0, re = tr >= 0 ? tr + 1 : (K > 0 ? N : 0);
         for (int r = rb; r < re; ++r) {
-            const uint32_t ctr[4] = {(uint32_t)r, (uint32_t)p, (uint32_t)G | ((uint32_t)f << 16), 0u};
             uint32_t x[4];
-            philox(ctr, k0, k1, x);
+            if (c.sampler == 1) {
+                const int B = std::max(1, c.nbatch), M = std::max(1, N / B);
+                const uint32_t ctr[4] = {(uint32_t)(r / M), (uint32_t)p, (uint32_t)G | ((uint32_t)f << 16), 0x50B01u};
+                uint32_t sh[4], sb[4];
+                philox(ctr, k0, k1, sh);
+                sobol4((uint32_t)(r % M), sb);
+                for (int d = 0; d < 4; ++d) x[d] = sb[d] ^ sh[d];
+            } else {
+                const uint32_t ctr[4] = {(uint32_t)r, (uint32_t)p, (uint32_t)G | ((uint32_t)f << 16), 0u};
+                philox(ctr, k0, k1, x);
+            }
             if (rng) memcpy(rng, x, sizeof x);
             R sW, sA, sB;
             dirs(x[0], x[1], &sW, &sA, &sB);

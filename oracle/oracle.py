@@ -60,6 +60,7 @@ class PacketConfig(ctypes.Structure):
         ("kappa", ctypes.c_float), ("T_west", ctypes.c_float), ("T_east", ctypes.c_float),
         ("rays", ctypes.c_int), ("rays_per_packet", _i), ("seed", ctypes.c_uint64),
         ("toll", ctypes.c_float), ("max_steps", ctypes.c_int), ("use_double", ctypes.c_int),
+        ("sampler", ctypes.c_int), ("nbatch", ctypes.c_int), ("n_tbins", ctypes.c_int),
     ]
 
 

@@ -376,7 +376,7 @@ def test_device_field_input_matches_host_input():
     a.set_rays(64)
     Qa, _ = a.solve(timeout_s=60)
     b = D.Solver(cfg)
-    dT = torch.from_numpy(T).cuda()
+    dT = torch.from_numpy(np.ascontiguousarray(T)).cuda()  # the device API takes dense i-fastest memory
     torch.cuda.synchronize()
     _lib.check(b._lib.dnsmc_set_fields_device(b._h, 1, ctypes.c_void_p(dT.data_ptr()), None))
     b._nfields = 1
