@@ -22,6 +22,7 @@ ERR_ARG, ERR_STATE, ERR_CUDA, ERR_IO, ERR_TIMEOUT, ERR_NOMEM, ERR_TABLE, ERR_NOD
 STATUS_STEP_CAP, STATUS_NONFINITE, STATUS_BAD_FIELD = 0x1, 0x2, 0x4
 MODEL_CK, MODEL_GREY_BANDS, MODEL_PARTICLE, MODEL_GREY, MODEL_TABLE = 0, 1, 2, 3, 4
 LAYOUT_DENSE, LAYOUT_FORTRAN = 0, 1
+SAMPLER_IID, SAMPLER_RQMC = 0, 1
 
 
 class Config(ctypes.Structure):
@@ -36,7 +37,7 @@ class Config(ctypes.Structure):
         ("eps_west", ctypes.c_float), ("eps_east", ctypes.c_float),
         ("toll", ctypes.c_float), ("max_steps", ctypes.c_int), ("grid_num", ctypes.c_int),
         ("model", ctypes.c_int), ("kappa", ctypes.c_float), ("n_groups", ctypes.c_int),
-        ("seed", ctypes.c_uint64),
+        ("seed", ctypes.c_uint64), ("sampler", ctypes.c_int), ("local_sampling", ctypes.c_int),
         ("block_threads", ctypes.c_int), ("tile_a", ctypes.c_int),
     ]
 
@@ -81,8 +82,8 @@ SIGNATURES = {
     "dnsmc_get_counters": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
     "dnsmc_get_timing": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
     "dnsmc_get_tmax": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
-    "dnsmc_get_sampling": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_float_p, c_int_p, c_int_p,
-                                          c_int_p, c_float_p, c_float_p]),
+    "dnsmc_get_sampling": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, c_int_p, c_int_p, c_float_p, c_int_p,
+                                          c_int_p, c_int_p, c_float_p, c_float_p]),
     "dnsmc_prepare_sampling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_float]),
     "dnsmc_get_geometry": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p, c_float_p]),
     "dnsmc_trace_ray": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,

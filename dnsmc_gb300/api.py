@@ -230,11 +230,11 @@ class Solver:
         return t.value
 
     def sampling(self) -> dict:
-        ng, ne = ctypes.c_int(), ctypes.c_int()
-        check(self._lib.dnsmc_get_sampling(self._h, ctypes.byref(ng), None, ctypes.byref(ne),
+        ng, nt, ne = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        check(self._lib.dnsmc_get_sampling(self._h, ctypes.byref(ng), ctypes.byref(nt), None, ctypes.byref(ne),
                                            None, None, None, None, None, None))
-        n, e = ng.value, ne.value
-        gs = np.zeros(n + 1, np.int32)
+        n, t, e = ng.value, nt.value, ne.value
+        gs = np.zeros(n * t + 1, np.int32)
         prob = np.zeros(max(e, 1), np.float32)
         alias = np.zeros(max(e, 1), np.int32)
         band = np.zeros(max(e, 1), np.int32)
@@ -243,9 +243,9 @@ class Solver:
         nb = max(self.table_info()["nbands"], 1)
         ibw = np.zeros(2 * nb, np.float32)
         ip = lambda a: a.ctypes.data_as(_lib.c_int_p)
-        check(self._lib.dnsmc_get_sampling(self._h, None, ip(gs), None, _fp(prob), ip(alias), ip(band), ip(gq),
+        check(self._lib.dnsmc_get_sampling(self._h, None, None, ip(gs), None, _fp(prob), ip(alias), ip(band), ip(gq),
                                            _fp(W), _fp(ibw)))
-        return dict(n_groups=n, group_start=gs, prob=prob[:e], alias=alias[:e], band=band[:e], gq=gq[:e],
+        return dict(n_groups=n, n_tbins=t, group_start=gs, prob=prob[:e], alias=alias[:e], band=band[:e], gq=gq[:e],
                     W=W[:e], ibw=ibw)
 
     def prepare_sampling(self, Tmax: float, xmean: float = 0.0) -> dict:

@@ -131,6 +131,31 @@ void make_faces(int im, float L, int stretched, std::vector<float> &xu) {
     for (int i = 1; i < im + 1; ++i) xu[i] = xu0[i * im0 / im];
 }
 
+// Sobol' direction numbers of four dimensions (Bratley-Fox recurrence on the
+// primitive polynomials 1, x+1, x^2+x+1, x^3+x+1 with initial m = 1 | 1 |
+// 1,3 | 1,3,1), 32 bits.
+void sobol_directions(uint32_t v[4][32]) {
+    const int deg[4] = {0, 1, 2, 3};
+    const int poly[4] = {0, 0, 1, 1};  // interior coefficients a_1..a_{s-1}
+    const uint32_t init[4][3] = {{1, 0, 0}, {1, 0, 0}, {1, 3, 0}, {1, 3, 1}};
+    for (int d = 0; d < 4; ++d) {
+        uint32_t m[33] = {0};
+        if (deg[d] == 0) {
+            for (int k = 1; k <= 32; ++k) m[k] = 1;
+        } else {
+            const int sd = deg[d];
+            for (int k = 1; k <= sd; ++k) m[k] = init[d][k - 1];
+            for (int k = sd + 1; k <= 32; ++k) {
+                uint32_t x = m[k - sd] ^ (m[k - sd] << sd);
+                for (int i = 1; i < sd; ++i)
+                    if ((poly[d] >> (sd - 1 - i)) & 1) x ^= m[k - i] << i;
+                m[k] = x;
+            }
+        }
+        for (int k = 1; k <= 32; ++k) v[d][k - 1] = m[k] << (32 - k);
+    }
+}
+
 template <class T>
 struct DevBuf {
     T *p = nullptr;
@@ -213,7 +238,7 @@ struct dnsmc_solver {
     DevBuf<SpecEntry> d_entries;
     DevBuf<int> d_group_start, d_group_empty;
     int mode = MODE_GREY;
-    int n_groups_used = 1;
+    int n_groups_used = 1, n_tbins_used = 1;
 
     // outputs
     DevBuf<double2> d_tally;
@@ -247,6 +272,12 @@ int ensure_device(dnsmc_solver *s) {
     CUDA_TRY(cudaEventCreate(&s->ev_done));
     CUDA_TRY(cudaEventCreate(&s->ev_solve0));
     s->dev_ready = true;
+    {
+        uint32_t dirs[4][32];
+        sobol_directions(dirs);
+        const int rc = upload_sobol_dirs(dirs);
+        if (rc) return fail(DNSMC_ERR_CUDA, "Sobol' table upload: %s", cudaGetErrorString((cudaError_t)rc));
+    }
     if (int rc = s->d_fw.ensure(s->fw.size())) return rc;
     CUDA_TRY(cudaMemcpy(s->d_fw.p, s->fw.data(), s->fw.size() * sizeof(float), cudaMemcpyHostToDevice));
     return DNSMC_OK;
@@ -264,6 +295,9 @@ int check_config(const dnsmc_config &c) {
     if (c.grid_num != 1) return fail(DNSMC_ERR_ARG, "grid_num %d: only the fine grid (grid_num = 1) is marched", c.grid_num);
     if (c.model < 0 || c.model > 4) return fail(DNSMC_ERR_ARG, "unknown model %d", c.model);
     if (c.n_groups < 1) return fail(DNSMC_ERR_ARG, "n_groups must be >= 1");
+    if (c.sampler != DNSMC_SAMPLER_IID && c.sampler != DNSMC_SAMPLER_RQMC) return fail(DNSMC_ERR_ARG, "unknown sampler %d", c.sampler);
+    if (c.sampler == DNSMC_SAMPLER_RQMC && c.nvar < 2) return fail(DNSMC_ERR_ARG, "the RQMC sampler needs nvar >= 2 replicates");
+    if (c.local_sampling != 0 && c.local_sampling != 1) return fail(DNSMC_ERR_ARG, "local_sampling must be 0 or 1");
     if (c.block_threads && c.block_threads != 128 && c.block_threads != 256 && c.block_threads != 512)
         return fail(DNSMC_ERR_ARG, "block_threads must be 0, 128, 256 or 512");
     if (c.tile_a && c.tile_a != 8 && c.tile_a != 16 && c.tile_a != 32)
@@ -502,6 +536,7 @@ int build_sampling(dnsmc_solver *s, float Tmax, float xm) {
     s->group_empty.clear();
     if (c.model == DNSMC_MODEL_GREY) {
         s->n_groups_used = 1;
+        s->n_tbins_used = 1;
         s->group_start = {0, 0};
         s->group_empty = {0};
         return DNSMC_OK;
@@ -511,7 +546,10 @@ int build_sampling(dnsmc_solver *s, float Tmax, float xm) {
     const int nG = std::min(c.n_groups, nB);
     s->n_groups_used = nG;
     const double Tm = Tmax;
-    std::vector<double> C((size_t)nB * nQ, 0.0), q((size_t)nB * nQ, 0.0);
+    // Target coefficient C_s of every spectral sample s = (band, g): the group
+    // estimate is sum_s C_s k(T_i) Ib(T_i) E[D | s], drawn with density q and
+    // weighted W_s = C_s / q_eff(s).
+    std::vector<double> C((size_t)nB * nQ, 0.0);
     if (t.ref_sampling) {
         // nearest table temperature to Tmax (code/mc_gpu.cu:142, :837)
         int tm = (int)((Tmax - t.T0) / t.dT);
@@ -523,6 +561,7 @@ int build_sampling(dnsmc_solver *s, float Tmax, float xm) {
         tk = std::max(0, std::min(tk, t.nT - 2));
         const double kmax = (double)(t.kP[tk + 1] - t.kP[tk]) / t.dT * (Tmax - (t.T0 + tk * t.dT)) + t.kP[tk];
         const double E = 4.0 * kmax * kSigma * Tm * Tm * Tm * Tm;
+        std::vector<double> pr((size_t)nB * nQ, 0.0);
         double tot = 0.0;
         for (int b = 0; b < nB; ++b) {
             const double pb = (double)t.prob[(size_t)ts * nB + b] - (b ? (double)t.prob[(size_t)ts * nB + b - 1] : 0.0);
@@ -532,66 +571,70 @@ int build_sampling(dnsmc_solver *s, float Tmax, float xm) {
                     const float *cg = t.probg.data() + ((size_t)ts * nB + b) * nQ;
                     pg = (double)cg[g] - (g ? (double)cg[g - 1] : 0.0);
                 }
-                const double p = std::max(0.0, pb) * std::max(0.0, pg);
-                q[(size_t)b * nQ + g] = p;
-                tot += p;
+                pr[(size_t)b * nQ + g] = std::max(0.0, pb) * std::max(0.0, pg);
+                tot += pr[(size_t)b * nQ + g];
             }
         }
         if (!(tot > 0)) return fail(DNSMC_ERR_TABLE, "band CDF at T=%g is empty", (double)(t.T0 + ts * t.dT));
         for (int b = 0; b < nB; ++b)
             for (int g = 0; g < nQ; ++g) {
                 const size_t s_ = (size_t)b * nQ + g;
-                if (q[s_] <= 0) continue;
-                q[s_] /= tot;
+                if (pr[s_] <= 0) continue;
                 const double den = ib_at(t, b, Tm) * k_at(t, b, g, Tm, xm);
                 // ray weight of the reference: Ibmax*ratioI = E * k_i Ib_i / (k_m Ib_m)
-                C[s_] = den > 0 ? q[s_] * E / den : 0.0;
-                if (!(den > 0)) q[s_] = 0.0;
+                C[s_] = den > 0 ? pr[s_] / tot * E / den : 0.0;
             }
     } else {
+        for (int b = 0; b < nB; ++b)
+            for (int g = 0; g < nQ; ++g) C[(size_t)b * nQ + g] = 4.0 * kPi * 100.0 * t.dnu[b] * t.wq[g];
+    }
+    // sampling temperatures: Tmax only, or every table temperature
+    std::vector<double> Tbins;
+    if (c.local_sampling) for (int i = 0; i < t.nT; ++i) Tbins.push_back(t.T0 + (double)i * t.dT);
+    else Tbins.push_back(Tm);
+    s->n_tbins_used = (int)Tbins.size();
+    s->group_start.push_back(0);
+    std::vector<double> q((size_t)nB * nQ);
+    for (size_t ib = 0; ib < Tbins.size(); ++ib) {
         double mean = 0.0;
+        int npos = 0;
         for (int b = 0; b < nB; ++b)
             for (int g = 0; g < nQ; ++g) {
                 const size_t s_ = (size_t)b * nQ + g;
-                C[s_] = 4.0 * kPi * 100.0 * t.dnu[b] * t.wq[g];
-                q[s_] = C[s_] * k_at(t, b, g, Tm, xm) * ib_at(t, b, Tm);
-                mean += q[s_];
+                q[s_] = C[s_] > 0 ? C[s_] * k_at(t, b, g, Tbins[ib], xm) * ib_at(t, b, Tbins[ib]) : 0.0;
+                if (C[s_] > 0) { mean += q[s_]; ++npos; }
             }
-        mean /= (double)(nB * nQ);
-        // floor keeps every sample with a non-zero weight reachable
+        mean /= std::max(1, npos);
+        // floor keeps every sample with a non-zero coefficient reachable
         for (size_t s_ = 0; s_ < q.size(); ++s_)
             if (C[s_] > 0) q[s_] = std::max(q[s_], 1e-6 * mean);
-    }
-    s->group_start.push_back(0);
-    for (int G = 0; G < nG; ++G) {
-        const int b0 = (int)((long long)G * nB / nG), b1 = (int)((long long)(G + 1) * nB / nG);
-        std::vector<double> qg;
-        std::vector<int> ids;
-        for (int b = b0; b < b1; ++b)
-            for (int g = 0; g < nQ; ++g)
-                if (q[(size_t)b * nQ + g] > 0) { qg.push_back(q[(size_t)b * nQ + g]); ids.push_back(b * nQ + g); }
-        if (qg.empty()) {
-            s->group_empty.push_back(1);
+        for (int G = 0; G < nG; ++G) {
+            const int b0 = (int)((long long)G * nB / nG), b1 = (int)((long long)(G + 1) * nB / nG);
+            std::vector<double> qg;
+            std::vector<int> ids;
+            for (int b = b0; b < b1; ++b)
+                for (int g = 0; g < nQ; ++g)
+                    if (q[(size_t)b * nQ + g] > 0) { qg.push_back(q[(size_t)b * nQ + g]); ids.push_back(b * nQ + g); }
+            if (ib == 0) s->group_empty.push_back(qg.empty() ? 1 : 0);
+            if (qg.size() > 65535) return fail(DNSMC_ERR_TABLE, "band group has more than 65535 samples");
+            if (!qg.empty()) {
+                std::vector<float> thr;
+                std::vector<int> al;
+                std::vector<double> peff;
+                build_alias(qg, thr, al, peff);
+                for (size_t j = 0; j < qg.size(); ++j) {
+                    const int sid = ids[j];
+                    const int b = sid / nQ, g = sid % nQ;
+                    SpecEntry e;
+                    e.prob = thr[j];
+                    e.alias_nb = (uint32_t)al[j] | ((uint32_t)b << 16);
+                    e.koff = (int32_t)(((size_t)b * nQ + g) * t.nT * t.nX);
+                    e.W = peff[j] > 0 ? (float)(C[sid] / peff[j]) : 0.0f;
+                    s->entries.push_back(e);
+                }
+            }
             s->group_start.push_back((int)s->entries.size());
-            continue;
         }
-        if (qg.size() > 65535) return fail(DNSMC_ERR_TABLE, "band group has more than 65535 samples");
-        std::vector<float> thr;
-        std::vector<int> al;
-        std::vector<double> peff;
-        build_alias(qg, thr, al, peff);
-        for (size_t j = 0; j < qg.size(); ++j) {
-            const int sid = ids[j];
-            const int b = sid / nQ, g = sid % nQ;
-            SpecEntry e;
-            e.prob = thr[j];
-            e.alias_nb = (uint32_t)al[j] | ((uint32_t)b << 16);
-            e.koff = (int32_t)(((size_t)b * nQ + g) * t.nT * t.nX);
-            e.W = peff[j] > 0 ? (float)(C[sid] / peff[j]) : 0.0f;
-            s->entries.push_back(e);
-        }
-        s->group_empty.push_back(0);
-        s->group_start.push_back((int)s->entries.size());
     }
     s->ibw.assign((size_t)2 * nB, 0.f);
     for (int b = 0; b < nB; ++b) {
@@ -683,6 +726,9 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.ktab = s->d_k.p; P.ibtab = s->d_ib.p; P.ibw = s->d_ibw.p;
     P.entries = s->d_entries.p; P.group_start = s->d_group_start.p;
     P.n_groups = s->n_groups_used;
+    P.n_tbins = s->n_tbins_used;
+    P.sampler = c.sampler;
+    P.nbatch = c.nvar;
     P.kappa = c.kappa;
     P.Wgrey = (float)(4.0 * c.kappa * kSigma);
     P.Tw4[0] = c.T_west * c.T_west * c.T_west * c.T_west;
@@ -728,6 +774,8 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     F.niR = ni; F.njR = nj; F.nkR = nk;
     F.tile_a = ta; F.tile_b = tb; F.npa = npa; F.npb = npb;
     F.rays = s->rays; F.rays_per_packet = P.rays_per_packet;
+    F.batched = c.sampler == DNSMC_SAMPLER_RQMC;
+    F.nbatch = c.nvar;
     F.group_empty = s->d_group_empty.p;
     F.tally = s->d_tally.p;
     const size_t nout = (size_t)s->nfields * P.region_cells;
@@ -869,6 +917,8 @@ void dnsmc_set_default_config(dnsmc_config *c) {
     c->kappa = 1.0f;
     c->n_groups = 1;
     c->seed = 1234;
+    c->sampler = DNSMC_SAMPLER_IID;
+    c->local_sampling = 0;
     c->block_threads = 0;
     c->tile_a = 0;
 }
@@ -918,7 +968,7 @@ int dnsmc_create(const dnsmc_config *cfg, dnsmc_solver **out) {
     s->da = cfg->Ly / (float)cfg->jmax;
     s->db = cfg->Lz / (float)cfg->kmax;
     s->r_i0 = 0; s->r_i1 = cfg->imax; s->r_j0 = 0; s->r_j1 = cfg->jmax; s->r_k0 = 0; s->r_k1 = cfg->kmax;
-    s->rays = cfg->nvar * cfg->photmax;
+    s->rays = cfg->nvar * cfg->photmax;  // a multiple of nvar
     if (cfg->model == DNSMC_MODEL_GREY) s->tab.valid = true;
     *out = s;
     return DNSMC_OK;
@@ -1103,14 +1153,19 @@ int dnsmc_packet_count(const dnsmc_solver *s, int *npackets) {
 int dnsmc_set_rays(dnsmc_solver *s, int rays_per_group, const int *rays_per_packet) {
     if (!s) return fail(DNSMC_ERR_ARG, "null solver");
     if (rays_per_group < 1 && !rays_per_packet) return fail(DNSMC_ERR_ARG, "rays must be >= 1");
+    const int B = s->cfg.sampler == DNSMC_SAMPLER_RQMC ? s->cfg.nvar : 1;
+    if (!rays_per_packet && rays_per_group % B)
+        return fail(DNSMC_ERR_ARG, "RQMC: rays per group (%d) must be a multiple of nvar (%d)", rays_per_group, B);
     TRY(set_device(s));
     TRY(wait_done(s, 0));
     s->rays = rays_per_group;
     if (rays_per_packet) {
         int np;
         TRY(dnsmc_packet_count(s, &np));
-        for (int i = 0; i < np; ++i)
+        for (int i = 0; i < np; ++i) {
             if (rays_per_packet[i] < 0) return fail(DNSMC_ERR_ARG, "negative ray count");
+            if (rays_per_packet[i] % B) return fail(DNSMC_ERR_ARG, "RQMC: per-packet rays must be multiples of nvar");
+        }
         s->rays_pp.assign(rays_per_packet, rays_per_packet + np);
         TRY(s->d_rays_pp.ensure(np));
         CUDA_TRY(cudaMemcpy(s->d_rays_pp.p, s->rays_pp.data(), np * sizeof(int), cudaMemcpyHostToDevice));
@@ -1183,10 +1238,11 @@ int dnsmc_get_tmax(const dnsmc_solver *s, float *tmax) {
     return DNSMC_OK;
 }
 
-int dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *group_start, int *n_entries, float *prob,
-                       int *alias, int *band, int *gq, float *W, float *ibw) {
+int dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *n_tbins, int *group_start, int *n_entries,
+                       float *prob, int *alias, int *band, int *gq, float *W, float *ibw) {
     if (!s) return fail(DNSMC_ERR_ARG, "null solver");
     if (n_groups) *n_groups = s->n_groups_used;
+    if (n_tbins) *n_tbins = s->n_tbins_used;
     if (group_start) std::copy(s->group_start.begin(), s->group_start.end(), group_start);
     if (n_entries) *n_entries = (int)s->entries.size();
     const int nq = std::max(1, s->tab.nq);

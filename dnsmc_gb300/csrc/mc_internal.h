@@ -46,8 +46,9 @@ struct MarchParams {
     const float *ibtab;       // [band][t]
     const float *ibw;         // [2][band]
     const SpecEntry *entries;
-    const int *group_start;   // n_groups + 1
+    const int *group_start;   // n_tbins * n_groups + 1, temperature-bin major
     int n_groups;
+    int n_tbins;              // 1: one table (at Tmax); nT: per table temperature
     // grey model
     float kappa;              // absorption coefficient
     float Wgrey;              // 4 * kappa * sigma
@@ -56,6 +57,8 @@ struct MarchParams {
     int rays;                 // rays per (cell, group) when rays_per_packet == 0
     const int *rays_per_packet;
     uint32_t key0, key1;      // Philox key (seed)
+    int sampler;              // 0 iid Philox, 1 RQMC (shifted Sobol' net)
+    int nbatch;               // RQMC replicates per item (rays divisible by it)
     uint32_t field_base;      // field index offset for the RNG counter
     float toll;
     int max_steps;
@@ -80,6 +83,7 @@ struct FinalizeParams {
     int tile_a, tile_b, npa, npb;
     int rays;
     const int *rays_per_packet;
+    int batched, nbatch;      // RQMC: variance from nbatch replicate means
     const int *group_empty;   // 1 when the group has no emission
     const double2 *tally;
     double *Q;                // [f][cell] dense region, i fastest
@@ -105,6 +109,7 @@ int launch_field_stats(const float *fT, const float2 *fTX, long long n,
                        double *partials, float *out, void *stream);
 int field_stats_partials();   // doubles needed in `partials`
 int march_occupancy(int mode, int threads);  // resident blocks per SM
+int upload_sobol_dirs(const uint32_t dirs[4][32]);  // once per device
 int device_sm_count();
 
 }  // namespace dnsmc

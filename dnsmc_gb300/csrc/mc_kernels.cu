@@ -25,6 +25,13 @@
 //     dumped when tau < toll, black walls add tau*(Ib_i - Ib_w)/Ib_i
 //     (code/mc_gpu.cu:297,314).  The ray contribution is X = W*k_i*Ib_i*D.
 //
+// Rays are drawn either iid (one Philox4x32-10 call per packet-ray) or as
+// randomised quasi-Monte Carlo: the N rays of a (packet, band group) are
+// nbatch replicates of the first N/nbatch points of a 4-dimensional Sobol' net
+// (phi, cos theta, spectral index, alias threshold), each replicate XOR-shifted
+// by a Philox word; the spectral sample comes from the alias table of the
+// packet's own temperature bin when local sampling is on.
+//
 // Arithmetic is FP32 with explicit fmaf and the file is compiled with
 // -fmad=false, so the host replay reproduces every ray bit for bit; exp and
 // sin/cos are the project's own polynomial kernels (mc_expm1 / mc_sincos) for
@@ -113,6 +120,16 @@ __device__ __forceinline__ void mc_sincos_turn(uint32_t m, float *cs, float *sn)
     *cs = co; *sn = si;
 }
 
+// Sobol' direction numbers of the four sampled dimensions (host-computed).
+__constant__ uint32_t c_sobol[4][32];
+
+__device__ __forceinline__ uint4 sobol4(uint32_t m) {
+    uint32_t a = 0, b = 0, c = 0, d = 0;
+    for (int k = 0; m; ++k, m >>= 1)
+        if (m & 1u) { a ^= c_sobol[0][k]; b ^= c_sobol[1][k]; c ^= c_sobol[2][k]; d ^= c_sobol[3][k]; }
+    return make_uint4(a, b, c, d);
+}
+
 __device__ __forceinline__ float u24(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
 
 // Linear position in a uniform grid of n points, clamped as the reference's
@@ -188,9 +205,6 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
         const bool active = (a0 < P.ea1) && (b0 < P.eb1);
         const int acl = active ? a0 : P.ea0, bcl = active ? b0 : P.eb0;
         const int N = P.rays_per_packet ? P.rays_per_packet[p] : P.rays;
-        int gs = 0, K = 1;
-        if (MODE != MODE_GREY) { gs = P.group_start[G]; K = P.group_start[G + 1] - gs; }
-
         const long long fbase = (long long)f * P.field_stride;
         const long long own = fbase + (long long)w0 * plane + (long long)bcl * P.na + acl;
         // own-cell quantities
@@ -213,15 +227,43 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
             grid_pos(Ti, P.T0, P.invdT, P.nT, &ti_i, &ft_i);
         }
         const float oW = (__ldg(P.fw + w0) + __ldg(P.fw + w0 + 1)) * 0.5f;
+        // alias table of this packet: band group G of the temperature bin
+        // nearest to lane 0's temperature (one bin when sampling at Tmax)
+        int gs = 0, K = 1;
+        if (MODE != MODE_GREY) {
+            int boff = 0;
+            if (P.n_tbins > 1) {
+                const float T0v = __shfl_sync(FULL, Ti, 0);
+                int bin = __float2int_rn((T0v - P.T0) * P.invdT);
+                bin = min(max(bin, 0), P.n_tbins - 1);
+                boff = bin * P.n_groups;
+            }
+            gs = P.group_start[boff + G];
+            K = P.group_start[boff + G + 1] - gs;
+        }
+        const uint32_t ctr2 = (uint32_t)G | ((uint32_t)(f + P.field_base) << 16);
+        const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
 
-        double S = 0.0, S2 = 0.0;
+        double S = 0.0, S2 = 0.0, Sb = 0.0;
+        uint4 shift = make_uint4(0u, 0u, 0u, 0u);
+        int bcur = -1;
         const int rbeg = TRACE ? P.trace_r : 0;
         const int rend = TRACE ? P.trace_r + 1 : ((K > 0) ? N : 0);
         for (int r = rbeg; r < rend; ++r) {
-            const uint4 x = philox4x32_10(
-                make_uint4((uint32_t)r, (uint32_t)p,
-                           (uint32_t)G | ((uint32_t)(f + P.field_base) << 16), 0u),
-                P.key0, P.key1);
+            uint4 x;
+            int m = 0;
+            if (P.sampler) {
+                const int b = r / M;
+                m = r - b * M;
+                if (b != bcur) {
+                    shift = philox4x32_10(make_uint4((uint32_t)b, (uint32_t)p, ctr2, 0x50B01u), P.key0, P.key1);
+                    bcur = b;
+                }
+                const uint4 sb = sobol4((uint32_t)m);
+                x = make_uint4(sb.x ^ shift.x, sb.y ^ shift.y, sb.z ^ shift.z, sb.w ^ shift.w);
+            } else {
+                x = philox4x32_10(make_uint4((uint32_t)r, (uint32_t)p, ctr2, 0u), P.key0, P.key1);
+            }
             if (TRACE && lane == 0) {
                 P.trace_rng[0] = x.x; P.trace_rng[1] = x.y; P.trace_rng[2] = x.z; P.trace_rng[3] = x.w;
             }
@@ -348,7 +390,16 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                 if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
                 const double Xd = (double)X;
                 S += Xd;
-                S2 = fma(Xd, Xd, S2);
+                if (P.sampler) {
+                    Sb += Xd;
+                    if (m == M - 1) {  // end of a replicate: accumulate its mean squared
+                        const double mb = Sb / M;
+                        S2 = fma(mb, mb, S2);
+                        Sb = 0.0;
+                    }
+                } else {
+                    S2 = fma(Xd, Xd, S2);
+                }
             }
         }
         if (TRACE) return;
@@ -396,7 +447,12 @@ __global__ void finalize_kernel(const FinalizeParams F) {
             if (!F.group_empty[g] && N > 0) {
                 const double2 t = F.tally[((long long)f * F.n_groups + g) * F.region_cells + tc];
                 m = t.x / N;
-                if (N > 1) v = fmax(0.0, t.y / N - m * m) / (N - 1);
+                if (F.batched) {
+                    const int B = F.nbatch;
+                    if (B > 1) v = fmax(0.0, t.y / B - m * m) / (B - 1);
+                } else if (N > 1) {
+                    v = fmax(0.0, t.y / N - m * m) / (N - 1);
+                }
             }
             Q += m;
             V += v;
@@ -546,6 +602,10 @@ int launch_field_stats(const float *fT, const float2 *fTX, long long n, double *
 }
 
 int field_stats_partials() { return 3 * kStatBlocks; }
+
+int upload_sobol_dirs(const uint32_t dirs[4][32]) {
+    return (int)cudaMemcpyToSymbol(c_sobol, dirs, sizeof(uint32_t) * 4 * 32);
+}
 
 int device_sm_count() {
     int dev = 0, n = 0;

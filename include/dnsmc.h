@@ -61,6 +61,17 @@ extern "C" {
 #define DNSMC_MODEL_GREY       3  /* grey medium, constant kappa, sigma*T^4      */
 #define DNSMC_MODEL_TABLE      4  /* raw k(band, g, T, x_H2O) table (set_table)  */
 
+/* ---- ray samplers ----------------------------------------------------------
+ * IID: every ray draws (phi, cos theta, spectral index, alias threshold) from
+ *   its own Philox4x32-10 counter; sigma from the per-ray sample variance.
+ * RQMC: the rays of one (packet, band group) are nvar replicates of a Sobol'
+ *   net in those four dimensions, each replicate digitally shifted by a Philox
+ *   word (unbiased; the reference itself draws directions from Sobol',
+ *   code/mc_gpu.cu:80-81,121); sigma from the nvar replicate means, like the
+ *   reference's nVar batches (code/mc_gpu.cu:217-222).                       */
+#define DNSMC_SAMPLER_IID      0
+#define DNSMC_SAMPLER_RQMC     1
+
 /* ---- field layouts -------------------------------------------------------- */
 #define DNSMC_LAYOUT_DENSE     0  /* imax*jmax*kmax, i fastest, no ghosts        */
 #define DNSMC_LAYOUT_FORTRAN   1  /* (imax+2)(jmax+2)(kmax+2), i fastest, ghost  */
@@ -89,6 +100,11 @@ typedef struct dnsmc_config {
     int   n_groups;              /* band groups for stratified sampling (>=1)    */
     /* randomness */
     uint64_t seed;
+    int   sampler;               /* DNSMC_SAMPLER_*                              */
+    int   local_sampling;        /* 1: draw the spectral sample from the emission */
+                                 /* spectrum at the packet's own temperature     */
+                                 /* (per-temperature-bin alias tables); 0: at    */
+                                 /* Tmax for every cell, as code/mc_gpu.cu:142   */
     /* kernel shape (0 = automatic) */
     int   block_threads;         /* 128, 256 or 512                              */
     int   tile_a;                /* cells of a packet along j: 8, 16 or 32       */
@@ -200,12 +216,13 @@ int  dnsmc_get_timing(dnsmc_solver *s, double *solve_ms, double *march_ms);
 int  dnsmc_get_tmax(const dnsmc_solver *s, float *tmax);
 
 /* ---- spectral sampling tables (for the host replay in the tests) ----------- */
-/* Entries of every band group: alias threshold, alias index, band, g-point,
- * weight factor W (ray weight = W * k(T_i) * Ib(T_i)), k-table offset.  Valid
- * after a solve.  n_entries / group_start have n_groups+1 / n_groups entries.  */
-int  dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *group_start,
-                        int *n_entries, float *prob, int *alias, int *band,
-                        int *gq, float *W, float *ibw);
+/* Entries of every (temperature bin, band group): alias threshold, alias
+ * index, band, g-point, weight factor W (ray weight = W * k(T_i) * Ib(T_i)).
+ * Valid after a solve or dnsmc_prepare_sampling.  group_start has
+ * n_tbins*n_groups+1 entries (bin major); n_tbins is 1 without local sampling.*/
+int  dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *n_tbins,
+                        int *group_start, int *n_entries, float *prob,
+                        int *alias, int *band, int *gq, float *W, float *ibw);
 /* Build the sampling tables for a given Tmax and mean x_H2O on the host
  * without solving (no GPU needed); dnsmc_get_sampling then returns them.     */
 int  dnsmc_prepare_sampling(dnsmc_solver *s, float Tmax, float xmean);

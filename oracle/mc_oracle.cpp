@@ -702,7 +702,7 @@ struct Packet {
             int binoff = 0;
             if (c.n_tbins > 0) {
                 const float T0v = c.fieldT[cidx(f, w0, a0[0], b0[0])];
-                int bin = (int)rintf((T0v - c.T0) / c.dT);
+                int bin = (int)rintf((T0v - c.T0) * (1.0f / c.dT));
                 bin = std::min(std::max(bin, 0), c.n_tbins - 1);
                 binoff = bin * c.n_groups;
             }
@@ -730,14 +730,16 @@ struct Packet {
         const R Tw4[2] = {(R)(tw * tw * tw * tw), (R)(te * te * te * te)};
         const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
         const int rb = tr >= 0 ? tr : 0, re = tr >= 0 ? tr + 1 : (K > 0 ? N : 0);
+        const int Mb = c.sampler == 1 ? std::max(1, N / std::max(1, c.nbatch)) : 1;
+        double Sb[32];
+        for (int l = 0; l < 32; ++l) Sb[l] = 0.0;
         for (int r = rb; r < re; ++r) {
             uint32_t x[4];
             if (c.sampler == 1) {
-                const int B = std::max(1, c.nbatch), M = std::max(1, N / B);
-                const uint32_t ctr[4] = {(uint32_t)(r / M), (uint32_t)p, (uint32_t)G | ((uint32_t)f << 16), 0x50B01u};
+                const uint32_t ctr[4] = {(uint32_t)(r / Mb), (uint32_t)p, (uint32_t)G | ((uint32_t)f << 16), 0x50B01u};
                 uint32_t sh[4], sb[4];
                 philox(ctr, k0, k1, sh);
-                sobol4((uint32_t)(r % M), sb);
+                sobol4((uint32_t)(r % Mb), sb);
                 for (int d = 0; d < 4; ++d) x[d] = sb[d] ^ sh[d];
             } else {
                 const uint32_t ctr[4] = {(uint32_t)r, (uint32_t)p, (uint32_t)G | ((uint32_t)f << 16), 0u};
@@ -852,7 +854,16 @@ struct Packet {
                 const R X = w[l] * D[l];
                 const double Xd = (double)X;
                 S[l] += Xd;
-                S2[l] = std::fma(Xd, Xd, S2[l]);
+                if (c.sampler == 1) {
+                    Sb[l] += Xd;
+                    if (r % Mb == Mb - 1) {
+                        const double mb = Sb[l] / Mb;
+                        S2[l] = std::fma(mb, mb, S2[l]);
+                        Sb[l] = 0.0;
+                    }
+                } else {
+                    S2[l] = std::fma(Xd, Xd, S2[l]);
+                }
             }
         }
     }

@@ -183,6 +183,7 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
         c.fieldX = _fp(X)
     c.kappa, c.T_west, c.T_east = cfg.kappa, cfg.T_west, cfg.T_east
     c.seed, c.toll, c.max_steps, c.use_double = cfg.seed, cfg.toll, cfg.max_steps, use_double
+    c.sampler, c.nbatch = cfg.sampler, cfg.nvar
     c.rays = solver_rays(solver)
     if getattr(solver, "_keep", None):
         rp = np.ascontiguousarray(solver._keep[0], np.int32)
@@ -202,6 +203,7 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
         keep.update(k=k, Ib=Ib, s=s)
         c.ktab, c.ibtab, c.ibw = _fp(k), _fp(Ib), _fp(s["ibw"])
         c.n_groups = s["n_groups"]
+        c.n_tbins = s["n_tbins"] if s["n_tbins"] > 1 else 0
         c.group_start = s["group_start"].ctypes.data_as(_i)
         c.prob, c.W = _fp(s["prob"]), _fp(s["W"])
         c.alias = s["alias"].ctypes.data_as(_i)

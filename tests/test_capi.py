@@ -208,3 +208,49 @@ def test_consistent_sampling_emission_identity():
             assert abs(est / exact - 1) < 1e-5
             tot += est
         sv.close()
+
+
+def test_local_temperature_bins_emission_identity():
+    """Local sampling: one alias table per table temperature; every bin is an
+    unbiased sampler of the same emission sum, and bins differ in density."""
+    from dnsmc_gb300 import synth
+    tb = synth.ck_table(nbands=8, nq=4, nT=12, nX=3, seed=5)
+    sv = D.Solver(D.default_config(model=D.MODEL_TABLE, n_groups=2, local_sampling=1))
+    sv.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+    s = sv.prepare_sampling(2000.0, 0.1)
+    t = sv.table()
+    assert s["n_tbins"] == 12 and s["group_start"].size == 12 * 2 + 1
+    T, x = 900.0, 0.08
+    Tg = tb["T0"] + tb["dT"] * np.arange(12)
+    Xg = tb["X0"] + tb["dX"] * np.arange(3)
+    dens = []
+    for b in (0, 5, 11):
+        for g in range(2):
+            sub = dict(s)
+            sub["group_start"] = s["group_start"][b * 2:]
+            p = alias_distribution(sub, g)
+            a, e_ = int(s["group_start"][b * 2 + g]), int(s["group_start"][b * 2 + g + 1])
+            est = exact = 0.0
+            for e in range(a, e_):
+                bb, gg = s["band"][e], s["gq"][e]
+                kv = np.array([np.interp(x, Xg, t["k"][bb, gg, it]) for it in range(12)])
+                k = np.interp(T, Tg, kv)
+                ib = ib_interp(t["Ib"], tb["T0"], tb["dT"], bb, T)
+                est += p[e - a] * s["W"][e] * k * ib
+                exact += 4 * np.pi * 100 * tb["dnu"][bb] * tb["wq"][gg] * k * ib
+            assert abs(est / exact - 1) < 1e-5
+            if g == 0:
+                dens.append(p)
+    assert np.abs(dens[0] - dens[2]).max() > 1e-3  # cold and hot bins sample differently
+    sv.close()
+
+
+def test_rqmc_requires_replicates_and_divisible_rays():
+    with pytest.raises(D.DnsmcError):
+        D.Solver(D.default_config(sampler=D.SAMPLER_RQMC, nvar=1))
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, sampler=D.SAMPLER_RQMC, nvar=4, imax=8, jmax=8, kmax=8))
+    assert s.packet_count() == 8 * 2  # 8x4 tiles: 2 packets per wall-normal plane
+    with pytest.raises(D.DnsmcError) as e:
+        s.set_rays(10)
+    assert e.value.code == _lib.ERR_ARG
+    s.close()

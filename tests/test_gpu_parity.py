@@ -80,10 +80,14 @@ def assert_bitexact(solver, T, x=None):
         empty = gs[1:] == gs[:-1]
     Qexp = np.zeros_like(Q)
     Vexp = np.zeros_like(Q)
+    B = solver.cfg.nvar
     for g in range(ng):
         with np.errstate(invalid="ignore", divide="ignore"):
             m = np.where(N > 0, tal[:, g, ..., 0] / N, 0.0)
-            v = np.where(N > 1, np.maximum(0.0, tal[:, g, ..., 1] / N - m * m) / (N - 1), 0.0)
+            if solver.cfg.sampler == D.SAMPLER_RQMC:
+                v = np.where(N > 0, np.maximum(0.0, tal[:, g, ..., 1] / B - m * m) / (B - 1), 0.0)
+            else:
+                v = np.where(N > 1, np.maximum(0.0, tal[:, g, ..., 1] / N - m * m) / (N - 1), 0.0)
         if empty[g]:
             m, v = np.zeros_like(m), np.zeros_like(v)
         np.testing.assert_array_equal(Qg[:, g], m)
@@ -386,3 +390,25 @@ def test_device_field_input_matches_host_input():
     assert a.tmax() == b.tmax()
     a.close()
     b.close()
+
+
+def test_bitexact_rqmc_local_bins_and_trace():
+    tb = synth.ck_table(nbands=12, nq=8, nT=20, nX=4, seed=6)
+    s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=8, jmax=32, kmax=4, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=400, T_east=450, seed=31, n_groups=2,
+                                  sampler=D.SAMPLER_RQMC, nvar=4, local_sampling=1))
+    s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+    T = smooth_field(8, 32, 4, 450, 1700, 41)
+    x = (0.1 + 0.05 * np.random.default_rng(3).uniform(-1, 1, (4, 32, 8))).astype(np.float32)
+    s.set_fields(T, x)
+    s.set_rays(48)
+    assert_bitexact(s, T, x)
+    assert s.sampling()["n_tbins"] == 20
+    c, keep = O.packet_config(s, T, x)
+    for p, r in [(0, 0), (3, 13), (31, 47)]:
+        rec, n, rng = s.trace(0, 1, p, r)
+        rec2, n2, rng2 = O.packet_trace(c, 0, 1, p, r)
+        assert n == n2
+        np.testing.assert_array_equal(rng, rng2)
+        np.testing.assert_array_equal(rec, rec2)
+    s.close()
