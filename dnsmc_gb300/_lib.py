@@ -88,6 +88,8 @@ SIGNATURES = {
     "dnsmc_get_geometry": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p, c_float_p]),
     "dnsmc_trace_ray": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, c_int32_p, c_int_p, c_uint32_p]),
+    "dnsmc_solve_grey_noalloc": (ctypes.c_int, [ctypes.POINTER(Config), c_float_p, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_void_p, ctypes.c_void_p]),
     "mc_gpu_": (None, [c_float_p, c_int_p]),
     "get_results_": (None, [c_float_p, c_float_p]),
     "dnsmc_dropin_configure": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_char_p]),

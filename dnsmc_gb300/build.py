@@ -53,13 +53,16 @@ def build(verbose: bool = False) -> str:
          "-o", os.path.join(bdir, "mc_kernels.o")],
         [nvcc, *common, "-x", "c++", "-c", os.path.join(CSRC, "mc_host.cpp"),
          "-o", os.path.join(bdir, "mc_host.o")],
+        [nvcc, *ARCH, *common, "-c", os.path.join(CSRC, "mc_noalloc.cu"),
+         "-o", os.path.join(bdir, "mc_noalloc.o")],
     ]
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(_run, jobs))
     out = lib_path()
     tmp = out + ".tmp"
     _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-Xcompiler", "-fPIC",
-          os.path.join(bdir, "mc_kernels.o"), os.path.join(bdir, "mc_host.o"), "-o", tmp])
+          os.path.join(bdir, "mc_kernels.o"), os.path.join(bdir, "mc_host.o"),
+          os.path.join(bdir, "mc_noalloc.o"), "-o", tmp])
     os.replace(tmp, out)
     if verbose:
         print("built", out)

@@ -893,6 +893,11 @@ bool g_dropin_cfg_set = false;
 
 }  // namespace
 
+namespace dnsmc {
+// Error reporting for the other translation units of the library.
+int report_error(int code, const char *msg) { return fail(code, "%s", msg); }
+}  // namespace dnsmc
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

@@ -236,6 +236,34 @@ int  dnsmc_get_geometry(const dnsmc_solver *s, float *xu, float *dy, float *dz);
 int  dnsmc_trace_ray(dnsmc_solver *s, int f, int g, int p, int r, int max_steps,
                      int32_t *rec, int *n_steps, uint32_t *rng4);
 
+/* ---- allocation-free grey solve -------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they run: host codes whose pool allocator owns all free device
+ * memory from start-up, or runs that must keep a fixed memory footprint after
+ * initialisation.  It solves a grey medium (cfg->model == DNSMC_MODEL_GREY,
+ * IID sampler, nvar*photmax rays per cell, the whole grid) and calls no
+ * cudaMalloc/cudaFree or allocating library routine: its intermediate buffers
+ * live in one fixed file-scope device array of about 5.3 MB that every GPU
+ * loading the library holds until the process exits.
+ *   xu   : host, imax+1 wall-normal face coordinates [m] (e.g. from
+ *          dnsmc_get_geometry or the caller's own grid)
+ *   dT   : device, imax*jmax*kmax temperatures [K], dense, i fastest
+ *   dQ   : device, imax*jmax*kmax doubles out: Q [W/m^3], dense, i fastest
+ *   dvar : device, imax*jmax*kmax doubles out: variance of Q
+ *   stream: CUDA stream (NULL: default stream); the call only enqueues.
+ * Limits: at most DNSMC_NOALLOC_MAX_CELLS cells and imax <= DNSMC_NOALLOC_MAX_IMAX;
+ * larger grids return DNSMC_ERR_ARG.  The first call on a device looks up the
+ * device address of the array (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the one array and it keeps the previous call's contents (each call clears
+ * what must start at zero); calls whose work overlaps on the GPU (different
+ * streams, or host threads, without ordering between them) race on it.     */
+#define DNSMC_NOALLOC_MAX_CELLS 262144   /* 64^3 */
+#define DNSMC_NOALLOC_MAX_IMAX  1024
+int  dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu,
+                              const float *dT, double *dQ, double *dvar,
+                              void *stream);
+
 /* ---- reference drop-in (code/mc_gpu.cu:440, :640) -------------------------- */
 /* Tfort: real(4) TMC(0:imax+1,0:jmax+1,0:kmax+1), i fastest, whole domain with
  * ghost layers.  *ystart: 1-based global j of this rank's slab (xstart(2)).
