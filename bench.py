@@ -247,6 +247,7 @@ def run_reference(args):
 
 
 def main():
+    global N_CELL
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=2)
@@ -254,7 +255,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--threads", type=int, default=0)
+    ap.add_argument("--n", type=int, default=128, help="cells per axis (profiling cases)")
+    ap.add_argument("--rays", type=int, default=0, help="fixed rays per cell per group (skips the 1%% budget)")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    N_CELL = args.n
     if args.impl == "reference":
         return run_reference(args)
 
@@ -266,7 +271,10 @@ def main():
     T, x, Tw = make_inputs(rank)
     s = make_solver(table, Tw, seed=1000 + rank, threads=args.threads)
     s.set_fields(T, x)
-    rays, e_pilot = ray_budget(s)
+    if args.rays:
+        rays, e_pilot = -(-args.rays // REPLICATES) * REPLICATES, None
+    else:
+        rays, e_pilot = ray_budget(s)
     rays = int(barrier_max(pg, rays))
     s.set_rays(rays)
     flushbuf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -300,14 +308,14 @@ def main():
     peak, peak_kind = peaks()
     # ---- end to end through the public API from host arrays ------------------
     e2e_ms = []
-    Qh = None
-    for i in range(args.steps):
+    Qh, Sh = Q, S
+    for i in range(0 if args.no_e2e else args.steps):
         t0 = time.perf_counter()
         s.set_fields(T, x)
         s.solve_async()
         Qh, Sh = s.results()
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
-    e2e_rank = float(np.sum(e2e_ms))
+    e2e_rank = float(np.sum(e2e_ms)) if e2e_ms else float("nan")
     e2e_max = barrier_max(pg, e2e_rank) / fields
     h2d = T.nbytes + x.nbytes
     d2h = Qh.nbytes + Sh.nbytes
