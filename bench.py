@@ -111,11 +111,12 @@ def make_inputs(seed):
     return d["T"], d["x"], d["T_wall"]
 
 
-def make_solver(table, T_wall, seed, threads=0):
+def make_solver(table, T_wall, seed, threads=0, cv=1):
     import dnsmc_gb300 as D
     cfg = D.default_config(model=D.MODEL_TABLE, imax=N_CELL, jmax=N_CELL, kmax=N_CELL, Lx=2.0, Ly=2 * math.pi,
                            Lz=math.pi, stretched_x=0, T_west=T_wall, T_east=T_wall, n_groups=GROUPS, seed=seed,
-                           block_threads=threads or 128, sampler=D.SAMPLER_RQMC, local_sampling=1, nvar=REPLICATES)
+                           block_threads=threads or 128, sampler=D.SAMPLER_RQMC, local_sampling=1, nvar=REPLICATES,
+                           control_variate=cv)
     s = D.Solver(cfg)
     s.set_table(table["k"], table["wvc"], table["T0"], table["dT"], dnu=table["dnu"], wq=table["wq"],
                 X0=table["X0"], dX=table["dX"])
@@ -124,6 +125,21 @@ def make_solver(table, T_wall, seed, threads=0):
 
 def rms_error(Q, S):
     return float(math.sqrt(float((S ** 2).mean())) / math.sqrt(float((Q ** 2).mean())))
+
+
+def plain_extrapolated(table, T, x, T_wall, seed, pilot=128):
+    """Plain MC (no control variate) at 1 % RMS: ray budget from a pilot solve,
+    time = measured solve time per ray x that budget (solve time is linear in
+    rays; reported as extrapolated)."""
+    s = make_solver(table, T_wall, seed, cv=0)
+    s.set_fields(T, x)
+    r, e = ray_budget(s, pilot)
+    s.set_rays(pilot)
+    s.solve(timeout_s=600)
+    a, b = s.timing()
+    s.close()
+    return dict(rays_per_cell_per_group=r, rms_error_at_pilot=e, pilot_rays=pilot, pilot_solve_ms=a,
+                ms_at_1pct_extrapolated=a * r / pilot)
 
 
 def ray_budget(s, pilot=256):
@@ -258,6 +274,8 @@ def main():
     ap.add_argument("--n", type=int, default=128, help="cells per axis (profiling cases)")
     ap.add_argument("--rays", type=int, default=0, help="fixed rays per cell per group (skips the 1%% budget)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--plain", action="store_true", help="time plain MC instead of the control variate")
+    ap.add_argument("--no-plain", action="store_true", help="skip the extrapolated plain-MC comparison")
     args = ap.parse_args()
     N_CELL = args.n
     if args.impl == "reference":
@@ -269,12 +287,12 @@ def main():
     from dnsmc_gb300 import synth
     table = synth.ck_table()
     T, x, Tw = make_inputs(rank)
-    s = make_solver(table, Tw, seed=1000 + rank, threads=args.threads)
+    s = make_solver(table, Tw, seed=1000 + rank, threads=args.threads, cv=0 if args.plain else 1)
     s.set_fields(T, x)
     if args.rays:
         rays, e_pilot = -(-args.rays // REPLICATES) * REPLICATES, None
     else:
-        rays, e_pilot = ray_budget(s)
+        rays, e_pilot = ray_budget(s, 64)
     rays = int(barrier_max(pg, rays))
     s.set_rays(rays)
     flushbuf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -324,6 +342,9 @@ def main():
         if pg is not None:
             pg.destroy_process_group()
         return 0
+    plain = None
+    if not args.plain and not args.no_plain and not args.rays:
+        plain = plain_extrapolated(table, T, x, Tw, seed=2000 + rank)
     cpu = None
     if not args.no_cpu:
         try:
@@ -338,11 +359,16 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "ck channel 128^3 (x,z periodic 2pi x pi, y walls black 400 K), T 400-1800 K + 5% "
                                "Fourier, x_H2O 0.1+0.05f, k table 64 bands x 16 g x 50 T x 8 x, 8 band groups, "
-                               "plain MC (no control variate), RQMC rays (4 shifted Sobol' replicates), "
-                               "spectral sampling at the packet temperature",
+                               + ("plain MC" if args.plain else
+                                  "control variate: the same ray through the plane-averaged profile, exact 1-D "
+                                  "mean added back (beta = 1, no network)")
+                               + ", RQMC rays (4 shifted Sobol' replicates), spectral sampling at the packet "
+                                 "temperature",
+                   "method": "plain" if args.plain else "cv-profile",
                    "rays_per_cell_per_group": rays, "rays_per_cell": rays * GROUPS, "target_rms_error": TARGET_ERR,
                    "rms_error_pilot": e_pilot, "rms_error_timed": float(np.mean(errs)),
                    "l2": "flushed before every timed step (256 MB device write)", "parallelism": f"cells x{world}"},
+        "plain_mc": plain,
         "rays_per_s": rays_s, "ray_steps_per_s": steps_tot * world / (t_max / 1e3),
         "march_ms": march_avg, "solve_ms": float(np.mean(solve_ms)),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,

@@ -71,6 +71,7 @@ class Solver:
         self._nfields = 0
         self._keep = []
         self._rays = cfg.nvar * cfg.photmax
+        self._beta = None
 
     # -- lifetime -----------------------------------------------------------
     def close(self) -> None:
@@ -252,6 +253,32 @@ class Solver:
         """Build the sampling tables on the host for Tmax (no GPU needed)."""
         check(self._lib.dnsmc_prepare_sampling(self._h, float(Tmax), float(xmean)))
         return self.sampling()
+
+    def set_cv_beta(self, beta) -> None:
+        """Control-variate coefficients (nfields, n_groups, nk, nj, ni) or None (1)."""
+        if beta is None:
+            check(self._lib.dnsmc_set_cv_beta(self._h, None))
+            self._beta = None
+            return
+        b = np.ascontiguousarray(beta, dtype=np.float32)
+        check(self._lib.dnsmc_set_cv_beta(self._h, _fp(b)))
+        self._beta = b
+
+    def cv_data(self) -> dict:
+        """Layer means, surrogate table, Jhat and E[Y] of the last CV solve."""
+        ns = ctypes.c_int()
+        check(self._lib.dnsmc_get_cv_data(self._h, ctypes.byref(ns), None, None, None, None))
+        c = self.cfg
+        S = ns.value
+        nf = self._nfields
+        ng = self.sampling()["n_groups"] if c.model != _lib.MODEL_GREY else 1
+        layer = np.zeros((nf, c.imax, 2), np.float32)
+        sur = np.zeros((nf, S, c.imax, 2), np.float32)
+        Jhat = np.zeros((nf, S, c.imax), np.float64)
+        shp = self._region_shape()
+        muY = np.zeros((nf, ng) + shp[1:], np.float64)
+        check(self._lib.dnsmc_get_cv_data(self._h, None, _fp(layer), _fp(sur), _dp(Jhat), _dp(muY)))
+        return dict(layer=layer, sur=sur, Jhat=Jhat, muY=muY, n_samples=S)
 
     def geometry(self):
         xu = np.zeros(self.cfg.imax + 1, np.float32)

@@ -97,6 +97,45 @@ void gauss_half(int nq, std::vector<float> &gq, std::vector<float> &wq) {
         if (x[i] > 0) { gq.push_back((float)x[i]); wq.push_back((float)w[i]); }
 }
 
+// n-point Gauss-Legendre nodes and weights on [a, b].
+void gauss_legendre(int n, double a, double b, std::vector<double> &x, std::vector<double> &w) {
+    x.assign(n, 0.0);
+    w.assign(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        double z = cos(kPi * (i + 0.75) / (n + 0.5));
+        double pp = 1.0;
+        for (int it = 0; it < 100; ++it) {
+            double p1 = 1.0, p2 = 0.0;
+            for (int j = 1; j <= n; ++j) {
+                const double p3 = p2;
+                p2 = p1;
+                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
+            }
+            pp = n * (z * p1 - p2) / (z * z - 1.0);
+            const double z1 = z;
+            z = z1 - p1 / pp;
+            if (fabs(z - z1) < 1e-15) break;
+        }
+        x[i] = 0.5 * (b - a) * (-z) + 0.5 * (b + a);
+        w[i] = (b - a) / ((1.0 - z * z) * pp * pp);
+    }
+}
+
+// Quadrature in the wall-normal cosine mu on (0, 1] for the control-variate
+// mean: 16-point Gauss-Legendre on the panels [0, 1e-3], [1e-3, 1e-2],
+// [1e-2, 0.1], [0.1, 1] (the integrand exp(-tau/mu) varies fastest near 0).
+void cv_quadrature(std::vector<double> &mu, std::vector<double> &w) {
+    const double edges[5] = {0.0, 1e-3, 1e-2, 1e-1, 1.0};
+    mu.clear();
+    w.clear();
+    for (int p = 0; p < 4; ++p) {
+        std::vector<double> x, ww;
+        gauss_legendre(16, edges[p], edges[p + 1], x, ww);
+        mu.insert(mu.end(), x.begin(), x.end());
+        w.insert(w.end(), ww.begin(), ww.end());
+    }
+}
+
 struct HostTable {
     int nbands = 0, nq = 0, nT = 0, nX = 1;
     float T0 = 0.f, dT = 1.f, X0 = 0.f, dX = 1.f;
@@ -240,6 +279,18 @@ struct dnsmc_solver {
     int mode = MODE_GREY;
     int n_groups_used = 1, n_tbins_used = 1;
 
+    // control variate
+    std::vector<double> Ccoef;               // [band*nq+g] target coefficients
+    std::vector<int> cv_grp, cv_sid;
+    std::vector<double> cv_C;
+    DevBuf<int> d_cv_grp, d_cv_sid;
+    DevBuf<double> d_cv_C;
+    DevBuf<float2> d_layer, d_sur;
+    DevBuf<double> d_Jhat, d_muY;
+    DevBuf<float> d_beta;
+    bool beta_set = false;
+    int cv_samples = 0;
+
     // outputs
     DevBuf<double2> d_tally;
     DevBuf<double> d_Q, d_var, d_Qg, d_varg;
@@ -278,6 +329,12 @@ int ensure_device(dnsmc_solver *s) {
         const int rc = upload_sobol_dirs(dirs);
         if (rc) return fail(DNSMC_ERR_CUDA, "Sobol' table upload: %s", cudaGetErrorString((cudaError_t)rc));
     }
+    {
+        std::vector<double> mu, w;
+        cv_quadrature(mu, w);
+        const int rc = upload_quadrature(mu.data(), w.data(), (int)mu.size());
+        if (rc) return fail(DNSMC_ERR_CUDA, "quadrature upload: %s", cudaGetErrorString((cudaError_t)rc));
+    }
     if (int rc = s->d_fw.ensure(s->fw.size())) return rc;
     CUDA_TRY(cudaMemcpy(s->d_fw.p, s->fw.data(), s->fw.size() * sizeof(float), cudaMemcpyHostToDevice));
     return DNSMC_OK;
@@ -298,6 +355,7 @@ int check_config(const dnsmc_config &c) {
     if (c.sampler != DNSMC_SAMPLER_IID && c.sampler != DNSMC_SAMPLER_RQMC) return fail(DNSMC_ERR_ARG, "unknown sampler %d", c.sampler);
     if (c.sampler == DNSMC_SAMPLER_RQMC && c.nvar < 2) return fail(DNSMC_ERR_ARG, "the RQMC sampler needs nvar >= 2 replicates");
     if (c.local_sampling != 0 && c.local_sampling != 1) return fail(DNSMC_ERR_ARG, "local_sampling must be 0 or 1");
+    if (c.control_variate != 0 && c.control_variate != 1) return fail(DNSMC_ERR_ARG, "control_variate must be 0 or 1");
     if (c.block_threads && c.block_threads != 128 && c.block_threads != 256 && c.block_threads != 512)
         return fail(DNSMC_ERR_ARG, "block_threads must be 0, 128, 256 or 512");
     if (c.tile_a && c.tile_a != 8 && c.tile_a != 16 && c.tile_a != 32)
@@ -588,6 +646,17 @@ int build_sampling(dnsmc_solver *s, float Tmax, float xm) {
         for (int b = 0; b < nB; ++b)
             for (int g = 0; g < nQ; ++g) C[(size_t)b * nQ + g] = 4.0 * kPi * 100.0 * t.dnu[b] * t.wq[g];
     }
+    s->Ccoef = C;
+    s->cv_grp.assign(1, 0);
+    s->cv_sid.clear();
+    s->cv_C.clear();
+    for (int G = 0; G < nG; ++G) {
+        const int b0 = (int)((long long)G * nB / nG), b1 = (int)((long long)(G + 1) * nB / nG);
+        for (int b = b0; b < b1; ++b)
+            for (int g = 0; g < nQ; ++g)
+                if (C[(size_t)b * nQ + g] > 0) { s->cv_sid.push_back(b * nQ + g); s->cv_C.push_back(C[(size_t)b * nQ + g]); }
+        s->cv_grp.push_back((int)s->cv_sid.size());
+    }
     // sampling temperatures: Tmax only, or every table temperature
     std::vector<double> Tbins;
     if (c.local_sampling) for (int i = 0; i < t.nT; ++i) Tbins.push_back(t.T0 + (double)i * t.dT);
@@ -748,23 +817,70 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.status = s->d_misc.p + 1;
     P.counters = s->d_counters.p;
     const int threads = c.block_threads ? c.block_threads : 256;
+    const bool cv = c.control_variate != 0;
+    const int S = (mode == MODE_GREY) ? 1 : t.nbands * t.nq;
+    if (cv) {
+        P.n_samples = S;
+        P.sample_stride = t.nT * t.nX;
+        P.sur = s->d_sur.p;
+        P.beta = s->beta_set ? s->d_beta.p : nullptr;
+    }
     if (trace) {
         P.trace_f = tf; P.trace_g = tg; P.trace_p = tp; P.trace_r = tr; P.trace_max = tmax_steps;
         P.trace_rec = d_trace_rec; P.trace_n = d_trace_n; P.trace_rng = d_trace_rng;
         P.tally = nullptr;
-        const int rc = launch_march(mode, P, 1, 32, s->stream, true);
+        const int rc = cv ? launch_march_cv(mode, P, 1, 32, s->stream, true) : launch_march(mode, P, 1, 32, s->stream, true);
         if (rc) return fail(DNSMC_ERR_CUDA, "trace launch: %s", cudaGetErrorString((cudaError_t)rc));
         return DNSMC_OK;
+    }
+    if (cv) {
+        // E[Y] per (field, group, cell): layer means -> surrogate table ->
+        // 1-D quadrature Jhat -> sum over the group's samples
+        const size_t nsur = (size_t)s->nfields * S * c.imax;
+        TRY(s->d_layer.ensure((size_t)s->nfields * c.imax));
+        TRY(s->d_sur.ensure(nsur));
+        TRY(s->d_Jhat.ensure(nsur));
+        TRY(s->d_muY.ensure((size_t)s->nfields * P.n_groups * P.region_cells));
+        if (mode != MODE_GREY) {
+            TRY(s->d_cv_grp.ensure(s->cv_grp.size()));
+            TRY(s->d_cv_sid.ensure(std::max<size_t>(1, s->cv_sid.size())));
+            TRY(s->d_cv_C.ensure(std::max<size_t>(1, s->cv_C.size())));
+            CUDA_TRY(cudaMemcpyAsync(s->d_cv_grp.p, s->cv_grp.data(), s->cv_grp.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(s->d_cv_sid.p, s->cv_sid.data(), s->cv_sid.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(s->d_cv_C.p, s->cv_C.data(), s->cv_C.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+        }
+        CvParams cp{};
+        cp.nfields = s->nfields; cp.nw = c.imax; cp.na = c.jmax; cp.nb = c.kmax;
+        cp.fieldT = P.fieldT; cp.fieldTX = P.fieldTX; cp.mode = mode;
+        cp.layer = s->d_layer.p;
+        cp.nbands = t.nbands; cp.nq = std::max(1, t.nq); cp.nT = t.nT; cp.nX = t.nX;
+        cp.T0 = P.T0; cp.invdT = P.invdT; cp.X0 = P.X0; cp.invdX = P.invdX;
+        cp.ktab = P.ktab; cp.ibtab = P.ibtab; cp.ibw = P.ibw;
+        cp.kappa = c.kappa; cp.Tw4[0] = P.Tw4[0]; cp.Tw4[1] = P.Tw4[1];
+        cp.n_samples = S; cp.sur = s->d_sur.p; cp.fw = s->d_fw.p; cp.toll = c.toll;
+        cp.Jhat = s->d_Jhat.p;
+        cp.n_groups = P.n_groups;
+        cp.grp_start = s->d_cv_grp.p; cp.samp_id = s->d_cv_sid.p; cp.samp_C = s->d_cv_C.p;
+        cp.Wgrey = 4.0 * c.kappa * kSigma;
+        cp.ew0 = P.ew0; cp.ew1 = P.ew1; cp.ea0 = P.ea0; cp.ea1 = P.ea1; cp.eb0 = P.eb0; cp.eb1 = P.eb1;
+        cp.region_cells = P.region_cells;
+        cp.muY = s->d_muY.p;
+        int rc = launch_cv_prepare(cp, s->stream);
+        if (rc == 0) rc = launch_cv_mean(cp, s->stream);
+        if (rc) return fail(DNSMC_ERR_CUDA, "control-variate launch: %s", cudaGetErrorString((cudaError_t)rc));
+        s->cv_samples = S;
+        P.sur = s->d_sur.p;
     }
     TRY(s->d_tally.ensure((size_t)s->nfields * P.n_groups * P.region_cells));
     P.tally = s->d_tally.p;
     CUDA_TRY(cudaMemsetAsync(s->d_misc.p, 0, 4 * sizeof(unsigned int), s->stream));
     CUDA_TRY(cudaMemsetAsync(s->d_counters.p, 0, 2 * sizeof(unsigned long long), s->stream));
     const int sms = device_sm_count();
-    const int occ = march_occupancy(mode, threads);
+    const int occ = cv ? march_cv_occupancy(mode, threads) : march_occupancy(mode, threads);
     const int blocks = std::max(1, sms * occ);
     CUDA_TRY(cudaEventRecord(s->ev_march0, s->stream));
-    int rc = launch_march(mode, P, blocks, threads, s->stream, false);
+    int rc = cv ? launch_march_cv(mode, P, blocks, threads, s->stream, false)
+                : launch_march(mode, P, blocks, threads, s->stream, false);
     if (rc) return fail(DNSMC_ERR_CUDA, "march launch: %s", cudaGetErrorString((cudaError_t)rc));
     CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
     s->last = P;
@@ -778,6 +894,8 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     F.nbatch = c.nvar;
     F.group_empty = s->d_group_empty.p;
     F.tally = s->d_tally.p;
+    F.muY = cv ? s->d_muY.p : nullptr;
+    F.beta = cv ? P.beta : nullptr;
     const size_t nout = (size_t)s->nfields * P.region_cells;
     TRY(s->d_Q.ensure(nout));
     TRY(s->d_var.ensure(nout));
@@ -924,6 +1042,7 @@ void dnsmc_set_default_config(dnsmc_config *c) {
     c->seed = 1234;
     c->sampler = DNSMC_SAMPLER_IID;
     c->local_sampling = 0;
+    c->control_variate = 0;
     c->block_threads = 0;
     c->tile_a = 0;
 }
@@ -1260,6 +1379,59 @@ int dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *n_tbins, int *
         if (W) W[i] = e.W;
     }
     if (ibw) std::copy(s->ibw.begin(), s->ibw.end(), ibw);
+    return DNSMC_OK;
+}
+
+int dnsmc_set_cv_beta(dnsmc_solver *s, const float *beta) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    TRY(wait_done(s, 0));
+    if (!beta) { s->beta_set = false; return DNSMC_OK; }
+    if (s->nfields < 1) return fail(DNSMC_ERR_STATE, "set fields before the control-variate coefficients");
+    int ni, nj, nk;
+    region_dims(s, &ni, &nj, &nk);
+    const long long rc_ = (long long)ni * nj * nk;
+    const int nG = s->cfg.model == DNSMC_MODEL_GREY ? 1 : std::min(s->cfg.n_groups, std::max(1, s->tab.nbands));
+    // dense [f][g][k][j][i] -> tally layout [f][g][i][k][j]
+    std::vector<float> tl((size_t)s->nfields * nG * rc_);
+    for (long long fg = 0; fg < (long long)s->nfields * nG; ++fg)
+        for (int k = 0; k < nk; ++k)
+            for (int j = 0; j < nj; ++j)
+                for (int i = 0; i < ni; ++i) {
+                    const float b = beta[fg * rc_ + i + (long long)ni * (j + (long long)nj * k)];
+                    if (!std::isfinite(b)) return fail(DNSMC_ERR_ARG, "control-variate coefficients must be finite");
+                    tl[fg * rc_ + ((long long)i * nk + k) * nj + j] = b;
+                }
+    TRY(set_device(s));
+    TRY(s->d_beta.ensure(tl.size()));
+    CUDA_TRY(cudaMemcpy(s->d_beta.p, tl.data(), tl.size() * sizeof(float), cudaMemcpyHostToDevice));
+    s->beta_set = true;
+    return DNSMC_OK;
+}
+
+int dnsmc_get_cv_data(dnsmc_solver *s, int *n_samples, float *layer, float *sur, double *Jhat, double *muY) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (!s->solved || !s->cfg.control_variate) return fail(DNSMC_ERR_STATE, "no control-variate solve has been run");
+    TRY(wait_done(s, 0));
+    TRY(set_device(s));
+    const int S = s->cv_samples;
+    if (n_samples) *n_samples = S;
+    const size_t nl = (size_t)s->nfields * s->cfg.imax, ns = nl * S;
+    if (layer) CUDA_TRY(cudaMemcpy(layer, s->d_layer.p, nl * sizeof(float2), cudaMemcpyDeviceToHost));
+    if (sur) CUDA_TRY(cudaMemcpy(sur, s->d_sur.p, ns * sizeof(float2), cudaMemcpyDeviceToHost));
+    if (Jhat) CUDA_TRY(cudaMemcpy(Jhat, s->d_Jhat.p, ns * sizeof(double), cudaMemcpyDeviceToHost));
+    if (muY) {
+        int ni, nj, nk;
+        region_dims(s, &ni, &nj, &nk);
+        const long long rc_ = (long long)ni * nj * nk;
+        const long long nfg = (long long)s->nfields * s->last.n_groups;
+        std::vector<double> tl((size_t)(nfg * rc_));
+        CUDA_TRY(cudaMemcpy(tl.data(), s->d_muY.p, tl.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (long long fg = 0; fg < nfg; ++fg)
+            for (int i = 0; i < ni; ++i)
+                for (int k = 0; k < nk; ++k)
+                    for (int j = 0; j < nj; ++j)
+                        muY[fg * rc_ + i + (long long)ni * (j + (long long)nj * k)] = tl[fg * rc_ + ((long long)i * nk + k) * nj + j];
+    }
     return DNSMC_OK;
 }
 

@@ -69,6 +69,11 @@ struct MarchParams {
     long long region_cells;   // (ew1-ew0)*(ea1-ea0)*(eb1-eb0)
     unsigned int *status;     // DNSMC_STATUS_* bits
     unsigned long long *counters;  // [0] rays (lane-rays), [1] lane-steps
+    // control variate: Y = the same ray through the layer-mean medium
+    const float2 *sur;        // [f][sample][nw] (k_bar, Ib_bar) per layer
+    int n_samples;            // bands * nq (1 for the grey model)
+    int sample_stride;        // nT * nX: k-table offset -> sample index
+    const float *beta;        // [f][group][iR][kR][jR] CV coefficient, or null (1)
     // trace (trace launches only)
     int trace_f, trace_g, trace_p, trace_r, trace_max;
     int *trace_rec;           // 6 words per step
@@ -86,6 +91,8 @@ struct FinalizeParams {
     int batched, nbatch;      // RQMC: variance from nbatch replicate means
     const int *group_empty;   // 1 when the group has no emission
     const double2 *tally;
+    const double *muY;        // control variate mean, tally layout, or null
+    const float *beta;        // CV coefficient, tally layout, or null (1)
     double *Q;                // [f][cell] dense region, i fastest
     double *var;              // [f][cell]
     double *Qg;               // [f][group][cell] or nullptr
@@ -109,6 +116,40 @@ int launch_field_stats(const float *fT, const float2 *fTX, long long n,
                        double *partials, float *out, void *stream);
 int field_stats_partials();   // doubles needed in `partials`
 int march_occupancy(int mode, int threads);  // resident blocks per SM
+int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace);
+int march_cv_occupancy(int mode, int threads);
+
+// Control-variate preparation (all stream-ordered).
+struct CvParams {
+    int nfields, nw, na, nb;
+    const float *fieldT;      // packed [f][i][k][j] (grey / T modes)
+    const float2 *fieldTX;    // packed (T, x) (TX mode)
+    int mode;                 // MODE_GREY / MODE_T / MODE_TX
+    float2 *layer;            // [f][nw] (T_bar, x_bar)
+    // tables (as MarchParams)
+    int nbands, nq, nT, nX;
+    float T0, invdT, X0, invdX;
+    const float *ktab, *ibtab, *ibw;
+    float kappa, Tw4[2];
+    int n_samples;
+    float2 *sur;              // [f][sample][nw]
+    const float *fw;          // nw+1 faces
+    float toll;
+    int nquad;                // nodes per hemisphere
+    double *Jhat;             // [f][sample][nw] direction-averaged surrogate intensity
+    // mean of Y per (field, group, cell) in tally layout
+    int n_groups;
+    const int *grp_start;     // n_groups+1 into samp_id / samp_C
+    const int *samp_id;
+    const double *samp_C;
+    double Wgrey;
+    int ew0, ew1, ea0, ea1, eb0, eb1;
+    long long region_cells;
+    double *muY;
+};
+int launch_cv_prepare(const CvParams &c, void *stream);
+int launch_cv_mean(const CvParams &c, void *stream);
+int upload_quadrature(const double *mu, const double *w, int n);  // once per device
 int upload_sobol_dirs(const uint32_t dirs[4][32]);  // once per device
 int device_sm_count();
 

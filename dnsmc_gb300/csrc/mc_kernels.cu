@@ -169,7 +169,7 @@ __device__ __forceinline__ float lookup_ib(const MarchParams &P, int nb, int ti,
 // The march kernel.  Persistent: every warp pulls work items (field, band
 // group, packet) from an atomic counter until the queue is empty.
 // ---------------------------------------------------------------------------
-template <int MODE, bool TRACE>
+template <int MODE, bool TRACE, bool CV>
 __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -242,6 +242,9 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
             K = P.group_start[boff + G + 1] - gs;
         }
         const uint32_t ctr2 = (uint32_t)G | ((uint32_t)(f + P.field_base) << 16);
+        const long long tc = ((long long)(w0 - P.ew0) * nkR + (bcl - P.eb0)) * njR + (acl - P.ea0);
+        float beta = 1.0f;
+        if (CV && P.beta) beta = P.beta[fg * P.region_cells + tc];
         const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
 
         double S = 0.0, S2 = 0.0, Sb = 0.0;
@@ -275,11 +278,12 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
             const float sW = mu, sA = st * cph, sB = st * sph;
 
             // spectral sample and ray weight
-            float w, Ii, invI;
+            float w, wk, Ii, invI;
             int nbnd = 0, koff = 0;
             if (MODE == MODE_GREY) {
                 Ii = Ti4;
                 invI = invTi4;
+                wk = P.Wgrey;
                 w = P.Wgrey * Ti4;
             } else {
                 const int j = (int)__umulhi(x.z, (uint32_t)K);
@@ -290,7 +294,16 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                 const float ki = lookup_k<MODE>(P, koff, ti_i, ft_i, xi_i, fx_i);
                 Ii = lookup_ib(P, nbnd, ti_i, ft_i);
                 invI = Ii > 0.f ? 1.0f / Ii : 0.f;
-                w = e.W * ki * Ii;
+                wk = e.W * ki;
+                w = wk * Ii;
+            }
+            // surrogate walk (warp-uniform): same segments, layer-mean medium
+            const float2 *surp = nullptr;
+            float taus = 0.0f, Jbar = 0.0f;
+            if (CV) {
+                const int sid = (MODE == MODE_GREY) ? 0 : koff / P.sample_stride;
+                surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
+                taus = 1.0f;
             }
 
             // warp-uniform DDA set-up (origin at the cell centre)
@@ -344,6 +357,14 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                     tau = tau - ta;
                     if (tau < P.toll) { D = fmaf(tau, gj, D); tau = 0.0f; }
                 }
+                if (CV && taus > 0.0f) {
+                    const float2 kv = __ldg(surp + cw);
+                    const float as = -mc_expm1(-(kv.x * ds));
+                    const float tas = taus * as;
+                    Jbar = fmaf(tas, kv.y, Jbar);
+                    taus = taus - tas;
+                    if (taus < P.toll) { Jbar = fmaf(taus, kv.y, Jbar); taus = 0.0f; }
+                }
                 if (TRACE && lane == 0 && steps < P.trace_max) {
                     int *rec = P.trace_rec + 6 * steps;
                     rec[0] = cw; rec[1] = dA * nA; rec[2] = dB * nB; rec[3] = axis;
@@ -354,12 +375,15 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                 if (axis == 0) {
                     cw += dW;
                     if (cw < 0 || cw >= P.nw) {
+                        const int side = cw < 0 ? 0 : 1;
+                        const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
                         if (tau > 0.0f) {
-                            const int side = cw < 0 ? 0 : 1;
-                            const float Iw = (MODE == MODE_GREY) ? P.Tw4[side]
-                                                                 : __ldg(P.ibw + side * P.nbands + nbnd);
                             D = fmaf(tau, (Ii - Iw) * invI, D);
                             tau = 0.0f;
+                        }
+                        if (CV && taus > 0.0f) {
+                            Jbar = fmaf(taus, Iw, Jbar);
+                            taus = 0.0f;
                         }
                         break;
                     }
@@ -377,14 +401,18 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                     if (cb == P.nb) cb = 0; else if (cb < 0) cb = P.nb - 1;
                     rowB = (long long)cb * P.na;
                 }
-                if (!__any_sync(FULL, tau > 0.0f)) break;
+                if (!__any_sync(FULL, tau > 0.0f || (CV && taus > 0.0f))) break;
                 if (steps >= P.max_steps) {
-                    if (tau > 0.0f) flags |= DNSMC_STATUS_STEP_CAP;
+                    if (tau > 0.0f || (CV && taus > 0.0f)) flags |= DNSMC_STATUS_STEP_CAP;
                     break;
                 }
             }
             if (TRACE && lane == 0) *P.trace_n = steps;
-            const float X = w * D;
+            float X = w * D;
+            if (CV) {
+                const float Y = wk * (Ii - Jbar);
+                X = X - beta * Y;  // tallied: X - beta*Y, its mean is added back at finalize
+            }
             if (active) {
                 ++my_rays;
                 if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
@@ -403,10 +431,7 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
             }
         }
         if (TRACE) return;
-        if (active) {
-            const long long tc = ((long long)(w0 - P.ew0) * nkR + (b0 - P.eb0)) * njR + (a0 - P.ea0);
-            P.tally[fg * P.region_cells + tc] = make_double2(S, S2);
-        }
+        if (active) P.tally[fg * P.region_cells + tc] = make_double2(S, S2);
     }
     // per-warp counters and status
     for (int o = 16; o > 0; o >>= 1) {
@@ -445,7 +470,8 @@ __global__ void finalize_kernel(const FinalizeParams F) {
         for (int g = 0; g < F.n_groups; ++g) {
             double m = 0.0, v = 0.0;
             if (!F.group_empty[g] && N > 0) {
-                const double2 t = F.tally[((long long)f * F.n_groups + g) * F.region_cells + tc];
+                const long long ti = ((long long)f * F.n_groups + g) * F.region_cells + tc;
+                const double2 t = F.tally[ti];
                 m = t.x / N;
                 if (F.batched) {
                     const int B = F.nbatch;
@@ -453,6 +479,11 @@ __global__ void finalize_kernel(const FinalizeParams F) {
                 } else if (N > 1) {
                     v = fmax(0.0, t.y / N - m * m) / (N - 1);
                 }
+            }
+            if (F.muY && !F.group_empty[g]) {
+                const long long ti = ((long long)f * F.n_groups + g) * F.region_cells + tc;
+                const double b = F.beta ? (double)F.beta[ti] : 1.0;
+                m += b * F.muY[ti];  // Q_g = beta * E[Y] + mean(X - beta * Y)
             }
             Q += m;
             V += v;
@@ -546,16 +577,16 @@ int launch_march(int mode, const MarchParams &p, int blocks, int threads, void *
     if (trace) { blocks = 1; threads = 32; }
     switch (mode) {
         case MODE_GREY:
-            if (trace) march_kernel<MODE_GREY, true><<<blocks, threads, 0, st>>>(p);
-            else march_kernel<MODE_GREY, false><<<blocks, threads, 0, st>>>(p);
+            if (trace) march_kernel<MODE_GREY, true, false><<<blocks, threads, 0, st>>>(p);
+            else march_kernel<MODE_GREY, false, false><<<blocks, threads, 0, st>>>(p);
             break;
         case MODE_T:
-            if (trace) march_kernel<MODE_T, true><<<blocks, threads, 0, st>>>(p);
-            else march_kernel<MODE_T, false><<<blocks, threads, 0, st>>>(p);
+            if (trace) march_kernel<MODE_T, true, false><<<blocks, threads, 0, st>>>(p);
+            else march_kernel<MODE_T, false, false><<<blocks, threads, 0, st>>>(p);
             break;
         case MODE_TX:
-            if (trace) march_kernel<MODE_TX, true><<<blocks, threads, 0, st>>>(p);
-            else march_kernel<MODE_TX, false><<<blocks, threads, 0, st>>>(p);
+            if (trace) march_kernel<MODE_TX, true, false><<<blocks, threads, 0, st>>>(p);
+            else march_kernel<MODE_TX, false, false><<<blocks, threads, 0, st>>>(p);
             break;
         default:
             return (int)cudaErrorInvalidValue;
@@ -563,12 +594,230 @@ int launch_march(int mode, const MarchParams &p, int blocks, int threads, void *
     return (int)cudaGetLastError();
 }
 
+int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (trace) { blocks = 1; threads = 32; }
+    switch (mode) {
+        case MODE_GREY:
+            if (trace) march_kernel<MODE_GREY, true, true><<<blocks, threads, 0, st>>>(p);
+            else march_kernel<MODE_GREY, false, true><<<blocks, threads, 0, st>>>(p);
+            break;
+        case MODE_T:
+            if (trace) march_kernel<MODE_T, true, true><<<blocks, threads, 0, st>>>(p);
+            else march_kernel<MODE_T, false, true><<<blocks, threads, 0, st>>>(p);
+            break;
+        case MODE_TX:
+            if (trace) march_kernel<MODE_TX, true, true><<<blocks, threads, 0, st>>>(p);
+            else march_kernel<MODE_TX, false, true><<<blocks, threads, 0, st>>>(p);
+            break;
+        default:
+            return (int)cudaErrorInvalidValue;
+    }
+    return (int)cudaGetLastError();
+}
+
+int march_cv_occupancy(int mode, int threads) {
+    int nb = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    if (mode == MODE_GREY) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false, true>, threads, 0);
+    if (mode == MODE_T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false, true>, threads, 0);
+    if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false, true>, threads, 0);
+    if (e != cudaSuccess) return 1;
+    return nb > 0 ? nb : 1;
+}
+
+// ---------------------------------------------------------------------------
+// Control variate preparation.  Y is the ray's contribution in the medium
+// whose temperature and x_H2O are the mean of each wall-normal plane; its
+// expectation per cell is a 1-D layered-slab integral:
+//   E[Y] = sum_s C_s k_i(s) (Ib_i(s) - Jhat_s(layer)),
+//   Jhat_s(l) = 1/2 int_{-1}^{1} J_s(mu; l) dmu,
+// J_s the intensity absorbed along a ray leaving the centre of layer l with
+// wall-normal cosine mu through the layer-mean medium (same toll cut-off,
+// same wall emission).  The march tallies X - beta*Y and finalize adds
+// beta*E[Y] back, so the estimate is unbiased for any beta.
+// ---------------------------------------------------------------------------
+__constant__ double c_quad_mu[128];
+__constant__ double c_quad_w[128];
+__constant__ int c_nquad;
+
+int upload_quadrature(const double *mu, const double *w, int n) {
+    cudaError_t e = cudaMemcpyToSymbol(c_quad_mu, mu, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_quad_w, w, sizeof(double) * n);
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_nquad, &n, sizeof(int));
+    return (int)e;
+}
+
+__device__ __forceinline__ float cv_k(const CvParams &c, int sid, float T, float x) {
+    int ti, xi = 0;
+    float ft, fx = 0.f;
+    grid_pos(T, c.T0, c.invdT, c.nT, &ti, &ft);
+    if (c.mode == MODE_TX) {
+        grid_pos(x, c.X0, c.invdX, c.nX, &xi, &fx);
+        const float *s = c.ktab + (long long)sid * c.nT * c.nX + ti * c.nX + xi;
+        const float k00 = __ldg(s), k01 = __ldg(s + 1);
+        const float k10 = __ldg(s + c.nX), k11 = __ldg(s + c.nX + 1);
+        const float k0 = fmaf(fx, k01 - k00, k00);
+        const float k1 = fmaf(fx, k11 - k10, k10);
+        return fmaf(ft, k1 - k0, k0);
+    }
+    const float *s = c.ktab + (long long)sid * c.nT + ti;
+    const float k0 = __ldg(s), k1 = __ldg(s + 1);
+    return fmaf(ft, k1 - k0, k0);
+}
+
+__device__ __forceinline__ float cv_ib(const CvParams &c, int band, float T) {
+    int ti;
+    float ft;
+    grid_pos(T, c.T0, c.invdT, c.nT, &ti, &ft);
+    const float *s = c.ibtab + band * c.nT + ti;
+    const float i0 = __ldg(s), i1 = __ldg(s + 1);
+    return fmaf(ft, i1 - i0, i0);
+}
+
+// (T_bar, x_bar) of every wall-normal plane, fixed-order reduction.
+__global__ void cv_layer_kernel(const CvParams c) {
+    const int w = blockIdx.x, f = blockIdx.y;
+    const long long plane = (long long)c.na * c.nb;
+    const long long base = ((long long)f * c.nw + w) * plane;
+    __shared__ double sT[256], sX[256];
+    double aT = 0.0, aX = 0.0;
+    for (long long i = threadIdx.x; i < plane; i += blockDim.x) {
+        if (c.mode == MODE_TX) { const float2 v = c.fieldTX[base + i]; aT += v.x; aX += v.y; }
+        else aT += c.fieldT[base + i];
+    }
+    sT[threadIdx.x] = aT;
+    sX[threadIdx.x] = aX;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) { sT[threadIdx.x] += sT[threadIdx.x + o]; sX[threadIdx.x] += sX[threadIdx.x + o]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) c.layer[(long long)f * c.nw + w] = make_float2((float)(sT[0] / plane), (float)(sX[0] / plane));
+}
+
+// Layer-mean absorption coefficient and band intensity per (field, sample, layer).
+__global__ void cv_sur_kernel(const CvParams c) {
+    const long long n = (long long)c.nfields * c.n_samples * c.nw;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(idx % c.nw);
+        const long long fs = idx / c.nw;
+        const int sid = (int)(fs % c.n_samples);
+        const int f = (int)(fs / c.n_samples);
+        const float2 L = c.layer[(long long)f * c.nw + w];
+        float kb, Ib;
+        if (c.mode == MODE_GREY) {
+            const float t2 = L.x * L.x;
+            kb = c.kappa;
+            Ib = t2 * t2;
+        } else {
+            kb = cv_k(c, sid, L.x, L.y);
+            Ib = cv_ib(c, sid / c.nq, L.x);
+        }
+        c.sur[idx] = make_float2(kb, Ib);
+    }
+}
+
+// Direction-averaged surrogate intensity Jhat per (field, sample, layer):
+// composite Gauss-Legendre in mu on each hemisphere, 1-D march through the
+// layers with the same toll cut-off and wall emission as the 3-D walk.
+__global__ void cv_jhat_kernel(const CvParams c) {
+    const long long n = (long long)c.nfields * c.n_samples * c.nw;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int w = (int)(idx % c.nw);
+        const long long fs = idx / c.nw;
+        const int sid = (int)(fs % c.n_samples);
+        const float2 *sp = c.sur + fs * c.nw;
+        const int band = c.mode == MODE_GREY ? 0 : sid / c.nq;
+        const float oW = (__ldg(c.fw + w) + __ldg(c.fw + w + 1)) * 0.5f;
+        double acc = 0.0;
+        for (int h = 0; h < 2; ++h) {
+            const int dir = h ? 1 : -1;
+            const float Iw = c.mode == MODE_GREY ? c.Tw4[h] : __ldg(c.ibw + h * c.nbands + band);
+            for (int q = 0; q < c_nquad; ++q) {
+                const float inv_mu = (float)(1.0 / c_quad_mu[q]);
+                float tau = 1.0f, J = 0.0f;
+                int l = w;
+                float seg = dir > 0 ? (__ldg(c.fw + w + 1) - oW) : (oW - __ldg(c.fw + w));
+                for (;;) {
+                    const float2 kv = sp[l];
+                    const float a = -expm1f(-(kv.x * seg * inv_mu));
+                    const float ta = tau * a;
+                    J = fmaf(ta, kv.y, J);
+                    tau = tau - ta;
+                    if (tau < c.toll) { J = fmaf(tau, kv.y, J); tau = 0.0f; break; }
+                    l += dir;
+                    if (l < 0 || l >= c.nw) { J = fmaf(tau, Iw, J); break; }
+                    seg = __ldg(c.fw + l + 1) - __ldg(c.fw + l);
+                }
+                acc += c_quad_w[q] * (double)J;
+            }
+        }
+        c.Jhat[idx] = 0.5 * acc;
+    }
+}
+
+// E[Y] per (field, group, cell of the region), tally layout [f][g][i][k][j].
+__global__ void cv_mean_kernel(const CvParams c) {
+    const int niR = c.ew1 - c.ew0, njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0;
+    const long long n = (long long)c.nfields * c.region_cells;
+    const long long plane = (long long)c.na * c.nb;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int f = (int)(idx / c.region_cells);
+        const long long tc = idx - (long long)f * c.region_cells;
+        const int jR = (int)(tc % njR);
+        const long long r = tc / njR;
+        const int kR = (int)(r % nkR);
+        const int iR = (int)(r / nkR);
+        const int w = c.ew0 + iR;
+        const long long cell = (long long)f * c.nw * plane + (long long)w * plane + (long long)(c.eb0 + kR) * c.na + (c.ea0 + jR);
+        float T, x = 0.f;
+        if (c.mode == MODE_TX) { const float2 v = c.fieldTX[cell]; T = v.x; x = v.y; }
+        else T = c.fieldT[cell];
+        const double *Jh = c.Jhat + (long long)f * c.n_samples * c.nw + w;
+        (void)niR;
+        for (int g = 0; g < c.n_groups; ++g) {
+            double acc = 0.0;
+            if (c.mode == MODE_GREY) {
+                const float t2 = T * T;
+                acc = c.Wgrey * ((double)(t2 * t2) - Jh[0]);
+            } else {
+                for (int q = c.grp_start[g]; q < c.grp_start[g + 1]; ++q) {
+                    const int sid = c.samp_id[q];
+                    const float k = cv_k(c, sid, T, x);
+                    const float Ib = cv_ib(c, sid / c.nq, T);
+                    acc += c.samp_C[q] * (double)k * ((double)Ib - Jh[(long long)sid * c.nw]);
+                }
+            }
+            c.muY[((long long)f * c.n_groups + g) * c.region_cells + tc] = acc;
+        }
+    }
+}
+
+int launch_cv_prepare(const CvParams &c, void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    cv_layer_kernel<<<dim3(c.nw, c.nfields), 256, 0, st>>>(c);
+    const long long n = (long long)c.nfields * c.n_samples * c.nw;
+    cv_sur_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
+    cv_jhat_kernel<<<grid_for(n, 128), 128, 0, st>>>(c);
+    return (int)cudaGetLastError();
+}
+
+int launch_cv_mean(const CvParams &c, void *stream) {
+    const long long n = (long long)c.nfields * c.region_cells;
+    cv_mean_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(c);
+    return (int)cudaGetLastError();
+}
+
 int march_occupancy(int mode, int threads) {
     int nb = 0;
     cudaError_t e = cudaErrorInvalidValue;
-    if (mode == MODE_GREY) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false>, threads, 0);
-    if (mode == MODE_T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false>, threads, 0);
-    if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false>, threads, 0);
+    if (mode == MODE_GREY) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false, false>, threads, 0);
+    if (mode == MODE_T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false, false>, threads, 0);
+    if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false, false>, threads, 0);
     if (e != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
 }

@@ -105,6 +105,10 @@ typedef struct dnsmc_config {
                                  /* spectrum at the packet's own temperature     */
                                  /* (per-temperature-bin alias tables); 0: at    */
                                  /* Tmax for every cell, as code/mc_gpu.cu:142   */
+    int   control_variate;       /* 1: tally X - beta*Y with Y the same ray   */
+                                 /* through the plane-averaged T and x_H2O     */
+                                 /* profile; E[Y] from a 1-D layered-slab     */
+                                 /* quadrature is added back (unbiased)        */
     /* kernel shape (0 = automatic) */
     int   block_threads;         /* 128, 256 or 512                              */
     int   tile_a;                /* cells of a packet along j: 8, 16 or 32       */
@@ -226,6 +230,16 @@ int  dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *n_tbins,
 /* Build the sampling tables for a given Tmax and mean x_H2O on the host
  * without solving (no GPU needed); dnsmc_get_sampling then returns them.     */
 int  dnsmc_prepare_sampling(dnsmc_solver *s, float Tmax, float xmean);
+/* Control-variate coefficients beta per (field, band group, cell of the
+ * region), dense i fastest (NULL: beta = 1).  Any finite beta keeps the
+ * estimate unbiased; the variance is smallest near Cov(X,Y)/Var(Y).          */
+int  dnsmc_set_cv_beta(dnsmc_solver *s, const float *beta);
+/* Control-variate data of the last solve (any pointer may be NULL): layer
+ * means (T_bar, x_bar) [f][imax][2], surrogate (k_bar, Ib_bar)
+ * [f][sample][imax][2] (sample = band*nq + g), Jhat [f][sample][imax] and
+ * E[Y] [f][group][cell] dense i fastest.  n_samples receives bands*nq.      */
+int  dnsmc_get_cv_data(dnsmc_solver *s, int *n_samples, float *layer, float *sur,
+                       double *Jhat, double *muY);
 /* Wall-normal faces (imax+1) and periodic cell sizes used by the march.       */
 int  dnsmc_get_geometry(const dnsmc_solver *s, float *xu, float *dy, float *dz);
 

@@ -548,6 +548,10 @@ typedef struct {
     int sampler;              // 0: Philox iid, 1: digitally shifted Sobol' net (RQMC)
     int nbatch;               // RQMC replicates per (packet, group)
     int n_tbins;              // >0: sampling tables per temperature bin
+    int cv;                   // 1: tally X - beta*Y, Y = the same ray through the layer-mean profile
+    const float *sur_k;       // [field][sample][nw] layer-mean absorption coefficient
+    const float *sur_I;       // [field][sample][nw] layer-mean band intensity
+    const float *beta;        // [field][group][k][j][i] dense, or NULL (1)
 } OrcPacketConfig;
 
 }  // extern "C"
@@ -759,19 +763,24 @@ struct Packet {
                 koff = (nbnd * c.nq + c.gq[e]) * c.nT * c.nX;
                 We = (R)c.W[e];
             }
-            R w[32], Ii[32], invI[32], tau[32], D[32];
+            R w[32], wk[32], Ii[32], invI[32], tau[32], D[32];
             for (int l = 0; l < 32; ++l) {
                 if (c.mode == 0) {
-                    Ii[l] = Ti4[l]; invI[l] = invTi4[l]; w[l] = Wgrey * Ti4[l];
+                    Ii[l] = Ti4[l]; invI[l] = invTi4[l]; wk[l] = Wgrey; w[l] = Wgrey * Ti4[l];
                 } else {
                     const R ki = kfun(koff, ti_i[l], ft_i[l], xi_i[l], fx_i[l]);
                     Ii[l] = ibfun(nbnd, ti_i[l], ft_i[l]);
                     invI[l] = Ii[l] > 0 ? (R)1 / Ii[l] : (R)0;
-                    w[l] = We * ki * Ii[l];
+                    wk[l] = We * ki;
+                    w[l] = wk[l] * Ii[l];
                 }
                 tau[l] = act[l] ? (R)1 : (R)0;
                 D[l] = 0;
             }
+            R taus = c.cv ? (R)1 : (R)0, Jbar = 0;
+            const int sid = c.mode != 0 ? koff / (c.nT * c.nX) : 0;
+            const int nsamp = c.mode != 0 ? c.nbands * c.nq : 1;
+            const size_t sbase = ((size_t)f * nsamp + sid) * c.nw;
             const R invW = (R)1 / std::fabs(sW), invA = (R)1 / std::fabs(sA), invB = (R)1 / std::fabs(sB);
             const int dW = sW > 0 ? 1 : -1, dA = sA > 0 ? 1 : -1, dB = sB > 0 ? 1 : -1;
             R tW = (dW > 0 ? ((R)c.fw[w0 + 1] - oW) : (oW - (R)c.fw[w0])) * invW;
@@ -812,6 +821,14 @@ struct Packet {
                     tau[l] = tau[l] - tal;
                     if (tau[l] < (R)c.toll) { D[l] = FMA<R>(tau[l], gj, D[l]); tau[l] = 0; }
                 }
+                if (taus > 0) {  // surrogate: same segment through the layer-mean medium
+                    const R ks = (R)c.sur_k[sbase + cw], Is = (R)c.sur_I[sbase + cw];
+                    const R a = -expm1n(-(ks * ds));
+                    const R ta = taus * a;
+                    Jbar = FMA<R>(ta, Is, Jbar);
+                    taus = taus - ta;
+                    if (taus < (R)c.toll) { Jbar = FMA<R>(taus, Is, Jbar); taus = 0; }
+                }
                 if (rec && stepn < tmax) {
                     int32_t *q = rec + 6 * stepn;
                     q[0] = cw; q[1] = dA * nA; q[2] = dB * nB; q[3] = axis;
@@ -825,6 +842,10 @@ struct Packet {
                     cw += dW;
                     if (cw < 0 || cw >= c.nw) {
                         const int side = cw < 0 ? 0 : 1;
+                        if (taus > 0) {
+                            Jbar = FMA<R>(taus, (R)c.ibw[side * c.nbands + nbnd], Jbar);
+                            taus = 0;
+                        }
                         for (int l = 0; l < 32; ++l) {
                             if (!(tau[l] > 0)) continue;
                             const R Iw = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
@@ -843,7 +864,7 @@ struct Packet {
                     tB = ((R)nB + (R)0.5) * dtB;
                     for (int l = 0; l < 32; ++l) { cb[l] += dB; if (cb[l] == c.nb) cb[l] = 0; else if (cb[l] < 0) cb[l] = c.nb - 1; }
                 }
-                bool any = false;
+                bool any = taus > 0;
                 for (int l = 0; l < 32; ++l) any = any || (tau[l] > 0);
                 if (!any) break;
                 if (stepn >= c.max_steps) break;
@@ -851,7 +872,19 @@ struct Packet {
             if (nrec) *nrec = stepn;
             for (int l = 0; l < 32; ++l) {
                 if (!act[l]) continue;
-                const R X = w[l] * D[l];
+                R X = w[l] * D[l];
+                if (c.cv) {
+                    R beta = 1;
+                    if (c.beta) {
+                        const int nG = c.mode == 0 ? 1 : c.n_groups;
+                        const int niR = c.ew1 - c.ew0, njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0;
+                        const long long rc = (long long)niR * njR * nkR;
+                        beta = (R)c.beta[((long long)f * nG + G) * rc + (w0 - c.ew0) +
+                                         (long long)niR * ((a0[l] - c.ea0) + (long long)njR * (b0[l] - c.eb0))];
+                    }
+                    const R Y = wk[l] * (Ii[l] - Jbar);
+                    X = X - beta * Y;
+                }
                 const double Xd = (double)X;
                 S[l] += Xd;
                 if (c.sampler == 1) {

@@ -61,6 +61,7 @@ class PacketConfig(ctypes.Structure):
         ("rays", ctypes.c_int), ("rays_per_packet", _i), ("seed", ctypes.c_uint64),
         ("toll", ctypes.c_float), ("max_steps", ctypes.c_int), ("use_double", ctypes.c_int),
         ("sampler", ctypes.c_int), ("nbatch", ctypes.c_int), ("n_tbins", ctypes.c_int),
+        ("cv", ctypes.c_int), ("sur_k", _f), ("sur_I", _f), ("beta", _f),
     ]
 
 
@@ -209,9 +210,64 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
         c.alias = s["alias"].ctypes.data_as(_i)
         c.band = s["band"].ctypes.data_as(_i)
         c.gq = s["gq"].ctypes.data_as(_i)
+    if cfg.control_variate:
+        cvd = solver.cv_data()
+        sk = np.ascontiguousarray(cvd["sur"][..., 0], np.float32)
+        sI = np.ascontiguousarray(cvd["sur"][..., 1], np.float32)
+        keep.update(sk=sk, sI=sI)
+        c.cv = 1
+        c.sur_k, c.sur_I = _fp(sk), _fp(sI)
+        if getattr(solver, "_beta", None) is not None:
+            b = np.ascontiguousarray(solver._beta, np.float32)
+            keep["beta"] = b
+            c.beta = _fp(b)
     if mode is not None:
         c.mode = mode
     return c, keep
+
+
+def cv_quadrature():
+    """Composite 16-point Gauss-Legendre in mu on [0,1e-3],[1e-3,1e-2],
+    [1e-2,0.1],[0.1,1] (numpy's nodes, independent of the library's)."""
+    x, w = np.polynomial.legendre.leggauss(16)
+    mu, wt = [], []
+    for a, b in ((0.0, 1e-3), (1e-3, 1e-2), (1e-2, 0.1), (0.1, 1.0)):
+        mu.append(0.5 * (b - a) * x + 0.5 * (b + a))
+        wt.append(0.5 * (b - a) * w)
+    return np.concatenate(mu), np.concatenate(wt)
+
+
+def cv_jhat(sur_k, sur_I, fw, toll, Iw_west, Iw_east):
+    """Direction-averaged intensity absorbed along rays leaving the centre of
+    each layer of a 1-D layered medium (k, Ib per layer; black walls with
+    intensities Iw), truncated at transmissivity toll like the march:
+    Jhat[l] = 1/2 int_{-1}^{1} J(mu; l) dmu, in float64."""
+    nw = len(sur_k)
+    mu, wt = cv_quadrature()
+    fw = np.asarray(fw, np.float64)
+    o = 0.5 * (fw[:-1] + fw[1:])
+    out = np.zeros(nw)
+    for l in range(nw):
+        acc = 0.0
+        for d, Iw in ((-1, Iw_west), (1, Iw_east)):
+            for m, wq in zip(mu, wt):
+                tau, J, i = 1.0, 0.0, l
+                seg = (fw[l + 1] - o[l]) if d > 0 else (o[l] - fw[l])
+                while True:
+                    a = -math.expm1(-float(sur_k[i]) * seg / m)
+                    J += tau * a * float(sur_I[i])
+                    tau -= tau * a
+                    if tau < toll:
+                        J += tau * float(sur_I[i])
+                        break
+                    i += d
+                    if i < 0 or i >= nw:
+                        J += tau * Iw
+                        break
+                    seg = fw[i + 1] - fw[i]
+                acc += wq * J
+        out[l] = 0.5 * acc
+    return out
 
 
 def solver_rays(solver) -> int:

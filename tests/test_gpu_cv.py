@@ -1,0 +1,159 @@
+"""GPU tests of the control variate (CV): Y is the same ray through the
+medium of plane-averaged T and x_H2O; the march tallies X - beta*Y and the
+exact mean beta*E[Y] (1-D layered-slab quadrature) is added back.
+
+* bit-exact tallies vs the oracle's FP32 replay, with beta = 1 and with a
+  per-cell beta array;
+* the device quadrature Jhat and E[Y] against the oracle's float64 versions;
+* isothermal slab: the surrogate is exact, so Q equals the analytic solution
+  with zero variance;
+* unbiased: CV and plain MC agree cell by cell on the correlated-k channel;
+* the variance falls by more than 10x at equal rays.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+import dnsmc_gb300 as D
+from dnsmc_gb300 import synth
+from oracle import oracle as O
+from test_gpu_parity import region_tally_to_dense, rays_per_cell, smooth_field
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_bitexact_cv(s, T, x=None):
+    Q, S = s.solve(timeout_s=120)
+    Qg, Vg = s.group_results()
+    ng = Qg.shape[1]
+    c, keep = O.packet_config(s, T, x)
+    i0, i1, j0, j1, k0, k1 = s._region
+    tal, steps = O.packet_mc(c, ng, (i1 - i0) * (j1 - j0) * (k1 - k0))
+    tal = region_tally_to_dense(tal, s, ng)
+    N = rays_per_cell(s)
+    muY = s.cv_data()["muY"]
+    beta = s._beta if s._beta is not None else np.ones_like(muY, dtype=np.float32)
+    B = s.cfg.nvar
+    for g in range(ng):
+        m = tal[:, g, ..., 0] / N
+        if s.cfg.sampler == D.SAMPLER_RQMC:
+            v = np.maximum(0.0, tal[:, g, ..., 1] / B - m * m) / (B - 1)
+        else:
+            v = np.maximum(0.0, tal[:, g, ..., 1] / N - m * m) / (N - 1)
+        m = m + beta[:, g].astype(np.float64) * muY[:, g]
+        np.testing.assert_array_equal(Qg[:, g], m)
+        np.testing.assert_array_equal(Vg[:, g], v)
+    assert s.counters().steps == steps
+    return Q, S
+
+
+def test_cv_bitexact_grey():
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=16, jmax=32, kmax=8, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=300, T_east=500, kappa=1.5, seed=11, control_variate=1))
+    T = smooth_field(16, 32, 8, 400, 1200, 1)
+    s.set_fields(T)
+    s.set_rays(64)
+    assert_bitexact_cv(s, T)
+    s.close()
+
+
+def test_cv_bitexact_table_x_with_beta():
+    tb = synth.ck_table(nbands=12, nq=8, nT=20, nX=4, seed=6)
+    s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=8, jmax=32, kmax=4, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=400, T_east=450, seed=31, n_groups=3,
+                                  sampler=D.SAMPLER_RQMC, nvar=4, local_sampling=1, control_variate=1))
+    s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+    T = smooth_field(8, 32, 4, 450, 1700, 41)
+    x = (0.1 + 0.05 * np.random.default_rng(3).uniform(-1, 1, (4, 32, 8))).astype(np.float32)
+    s.set_fields(T, x)
+    s.set_rays(32)
+    assert_bitexact_cv(s, T, x)
+    beta = np.random.default_rng(5).uniform(0.5, 1.5, (1, 3, 4, 32, 8)).astype(np.float32)
+    s.set_cv_beta(beta)
+    assert_bitexact_cv(s, T, x)
+    s.close()
+
+
+def test_cv_quadrature_and_mean_match_oracle():
+    tb = synth.ck_table(nbands=6, nq=4, nT=20, nX=4, seed=9)
+    s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=12, jmax=32, kmax=4, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=1, T_west=420, T_east=380, seed=3, n_groups=2, control_variate=1))
+    s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+    T = smooth_field(12, 32, 4, 450, 1700, 12)
+    x = (0.1 + 0.05 * np.random.default_rng(4).uniform(-1, 1, (4, 32, 12))).astype(np.float32)
+    s.set_fields(T, x)
+    s.set_rays(8)
+    s.solve(timeout_s=60)
+    cv = s.cv_data()
+    np.testing.assert_allclose(cv["layer"][0, :, 0], T.mean((0, 1)), rtol=1e-6)
+    np.testing.assert_allclose(cv["layer"][0, :, 1], x.mean((0, 1)), rtol=1e-5)
+    xu, _, _ = s.geometry()
+    smp = s.sampling()
+    ibw = smp["ibw"].reshape(2, -1)
+    nq = 4
+    for sid in (0, 5, 17, 23):
+        J = O.cv_jhat(cv["sur"][0, sid, :, 0], cv["sur"][0, sid, :, 1], xu, s.cfg.toll, ibw[0, sid // nq],
+                      ibw[1, sid // nq])
+        np.testing.assert_allclose(cv["Jhat"][0, sid], J, rtol=2e-5)
+    # E[Y] per cell from its definition: sum over the group's samples of
+    # C_s k_i (Ib_i - Jhat), C_s = W_s * q(s) of the (single-bin) alias table
+    from test_capi import alias_distribution
+    t = s.table()
+    Tg = tb["T0"] + tb["dT"] * np.arange(20)
+    Xg = tb["X0"] + tb["dX"] * np.arange(4)
+    for (i, j, k) in ((0, 0, 0), (5, 17, 2), (11, 31, 3)):
+        for g in range(2):
+            p = alias_distribution(smp, g)
+            a, e_ = int(smp["group_start"][g]), int(smp["group_start"][g + 1])
+            acc = 0.0
+            for e in range(a, e_):
+                b, gq = smp["band"][e], smp["gq"][e]
+                kv = np.array([np.interp(x[k, j, i], Xg, t["k"][b, gq, it]) for it in range(20)])
+                ki = np.interp(T[k, j, i], Tg, kv)
+                ib = np.interp(T[k, j, i], Tg, t["Ib"][b])
+                acc += smp["W"][e] * p[e - a] * ki * (ib - cv["Jhat"][0, b * nq + gq, i])
+            assert abs(cv["muY"][0, g, k, j, i] - acc) <= 1e-4 * abs(acc) + 1e-9 * np.abs(cv["muY"]).max()
+    s.close()
+
+
+def test_cv_isothermal_slab_is_exact():
+    ni, nj, nk = 32, 32, 8
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.2831853, Lz=3.1415927,
+                                  stretched_x=0, T_west=0.0, T_east=300.0, kappa=1.0, seed=3, control_variate=1))
+    s.set_fields(np.full((nk, nj, ni), 1000.0, np.float32))
+    s.set_rays(16)
+    Q, S = s.solve(timeout_s=60)
+    yc = (np.arange(ni) + 0.5) * 2.0 / ni
+    exact = O.slab_divq(yc, 2.0, 1.0, 1000.0, 0.0, 300.0)
+    np.testing.assert_allclose(Q[0][0, 0], exact, rtol=2e-4)
+    assert S.max() <= 1e-5 * np.abs(Q).max()
+    s.close()
+
+
+def _channel_pair(seed_plain, seed_cv, rays, n=32):
+    d = synth.ck_channel(n, 0)
+    tb = synth.ck_table()
+    out = []
+    for cv, seed in ((0, seed_plain), (1, seed_cv)):
+        s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=n, jmax=n, kmax=n, Lx=2.0, Ly=2 * math.pi,
+                                      Lz=math.pi, stretched_x=0, T_west=400, T_east=400, n_groups=8, seed=seed,
+                                      sampler=D.SAMPLER_RQMC, nvar=4, local_sampling=1, control_variate=cv))
+        s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+        s.set_fields(d["T"], d["x"])
+        s.set_rays(rays)
+        out.append(s.solve(timeout_s=120))
+        s.close()
+    return out
+
+
+def test_cv_unbiased_and_variance_reduction_ck_channel():
+    (Qp, Sp), (Qc, Sc) = _channel_pair(101, 202, 64)
+    z = (Qc - Qp) / np.sqrt(Sc ** 2 + Sp ** 2)
+    z = z[0][:, 0, :]  # one cell per packet row: independent estimates
+    assert math.sqrt(float((z ** 2).mean())) < 1.3, z
+    assert np.abs(z).max() < 5.0
+    ratio = float((Sp ** 2).mean() / (Sc ** 2).mean())
+    assert ratio > 10.0, ratio

@@ -161,3 +161,16 @@ def test_reference_reader_matches_fixtures(kind, particle_tables, ck_tables):
         np.testing.assert_allclose(r["kq"][:, 0, 0], fx["kq"], rtol=1e-6)
         kmax_expected = np.interp(1000.0, fx["Tnb"], fx["kP"])
     assert abs(r["kappamax"] / kmax_expected - 1) < 1e-5
+
+
+def test_cv_jhat_quadrature_matches_isothermal_slab():
+    """The oracle's layered-slab quadrature of the control-variate mean against
+    the analytic isothermal result Ib - 1/2 (Ib - Iw1) E2(t1) - 1/2 (Ib - Iw2) E2(t2)."""
+    nw = 24
+    fw = np.linspace(0, 2, nw + 1)
+    I = np.full(nw, 1000.0 ** 4)
+    J = O.cv_jhat(np.full(nw, 1.0), I, fw, 1e-12, 0.0, 300.0 ** 4)
+    o = 0.5 * (fw[:-1] + fw[1:])
+    ex = I[0] - 0.5 * I[0] * np.array([O.expn(2, t) for t in o]) \
+        - 0.5 * (I[0] - 300.0 ** 4) * np.array([O.expn(2, 2 - t) for t in o])
+    np.testing.assert_allclose(J, ex, rtol=1e-9)
