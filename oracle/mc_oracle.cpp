@@ -843,7 +843,8 @@ struct Packet {
                     if (cw < 0 || cw >= c.nw) {
                         const int side = cw < 0 ? 0 : 1;
                         if (taus > 0) {
-                            Jbar = FMA<R>(taus, (R)c.ibw[side * c.nbands + nbnd], Jbar);
+                            const R Iws = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
+                            Jbar = FMA<R>(taus, Iws, Jbar);
                             taus = 0;
                         }
                         for (int l = 0; l < 32; ++l) {

@@ -122,3 +122,25 @@ def test_rqmc_unbiased_and_replicate_variance_is_calibrated():
     se = np.sqrt(emp / (Qs.shape[0] * Qs.shape[1]))
     z = (q - ex) / se
     assert np.abs(z).max() < 4.5, z
+
+
+def test_cv_replay_isothermal_surrogate_cancels():
+    """Replay with the control variate on an isothermal grey slab whose
+    surrogate equals the medium: X - Y vanishes up to FP32 rounding."""
+    import ctypes
+    ni, nj, nk = 16, 32, 2
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=0.0, T_east=300.0, kappa=1.0, seed=4))
+    T = np.full((nk, nj, ni), 1000.0, np.float32)
+    s._rays, s._nfields = 64, 1
+    c, keep = O.packet_config(s, T, None, use_double=0)
+    sk = np.full((1, 1, ni), 1.0, np.float32)
+    sI = np.full((1, 1, ni), np.float32(1000.0) ** 4, np.float32)
+    c.cv = 1
+    c.sur_k = sk.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    c.sur_I = sI.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    tal, _ = O.packet_mc(c, 1, ni * nj * nk)
+    c.cv = 0
+    tal0, _ = O.packet_mc(c, 1, ni * nj * nk)
+    assert np.abs(tal[..., 0]).max() < 1e-4 * np.abs(tal0[..., 0]).max()
+    s.close()
