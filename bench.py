@@ -293,6 +293,13 @@ def main():
         rays, e_pilot = -(-args.rays // REPLICATES) * REPLICATES, None
     else:
         rays, e_pilot = ray_budget(s, 64)
+        # refine once at the predicted budget (RQMC + CV errors fall slightly
+        # slower than 1/N here), aiming 2 % below the target
+        s.set_rays(rays)
+        Qr, Sr = s.solve(timeout_s=600)
+        e1 = rms_error(Qr, Sr)
+        if e1 > 0.98 * TARGET_ERR:
+            rays = -(-int(math.ceil(rays * (e1 / (0.98 * TARGET_ERR)) ** 2)) // REPLICATES) * REPLICATES
     rays = int(barrier_max(pg, rays))
     s.set_rays(rays)
     flushbuf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
@@ -378,7 +385,7 @@ def main():
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_max, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "timing": "wall clock around set_fields + solve + get_results"},
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": (2 if args.plain else 6) * args.steps,
         "clocks": clk.summary(),
     }
     print(json.dumps(out), flush=True)

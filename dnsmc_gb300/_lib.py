@@ -38,7 +38,7 @@ class Config(ctypes.Structure):
         ("toll", ctypes.c_float), ("max_steps", ctypes.c_int), ("grid_num", ctypes.c_int),
         ("model", ctypes.c_int), ("kappa", ctypes.c_float), ("n_groups", ctypes.c_int),
         ("seed", ctypes.c_uint64), ("sampler", ctypes.c_int), ("local_sampling", ctypes.c_int),
-        ("control_variate", ctypes.c_int),
+        ("control_variate", ctypes.c_int), ("cv_moments", ctypes.c_int),
         ("block_threads", ctypes.c_int), ("tile_a", ctypes.c_int),
     ]
 
@@ -88,6 +88,7 @@ SIGNATURES = {
     "dnsmc_prepare_sampling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_float]),
     "dnsmc_set_cv_beta": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
     "dnsmc_get_cv_data": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_float_p, c_float_p, c_double_p, c_double_p]),
+    "dnsmc_get_cv_moments": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "dnsmc_get_geometry": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p, c_float_p]),
     "dnsmc_trace_ray": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, c_int32_p, c_int_p, c_uint32_p]),

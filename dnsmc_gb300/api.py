@@ -255,7 +255,8 @@ class Solver:
         return self.sampling()
 
     def set_cv_beta(self, beta) -> None:
-        """Control-variate coefficients (nfields, n_groups, nk, nj, ni) or None (1)."""
+        """Control-variate coefficient pairs (nfields, n_groups, nk, nj, ni, 2)
+        = (beta_a, beta_b), or None for (1, -1)."""
         if beta is None:
             check(self._lib.dnsmc_set_cv_beta(self._h, None))
             self._beta = None
@@ -274,11 +275,20 @@ class Solver:
         ng = self.sampling()["n_groups"] if c.model != _lib.MODEL_GREY else 1
         layer = np.zeros((nf, c.imax, 2), np.float32)
         sur = np.zeros((nf, S, c.imax, 2), np.float32)
-        Jhat = np.zeros((nf, S, c.imax), np.float64)
+        Jhat = np.zeros((nf, S, c.imax, 2), np.float64)
         shp = self._region_shape()
-        muY = np.zeros((nf, ng) + shp[1:], np.float64)
+        muY = np.zeros((nf, ng) + shp[1:] + (2,), np.float64)
         check(self._lib.dnsmc_get_cv_data(self._h, None, _fp(layer), _fp(sur), _dp(Jhat), _dp(muY)))
         return dict(layer=layer, sur=sur, Jhat=Jhat, muY=muY, n_samples=S)
+
+    def cv_moments(self):
+        """(nfields, n_groups, nk, nj, ni, 9) per-ray moment sums of the last
+        solve with cv_moments=1: X, Ya, Yb, X^2, Ya^2, Yb^2, X Ya, X Yb, Ya Yb."""
+        ng = self.sampling()["n_groups"] if self.cfg.model != _lib.MODEL_GREY else 1
+        shp = self._region_shape()
+        m = np.zeros((shp[0], ng) + shp[1:] + (9,), np.float64)
+        check(self._lib.dnsmc_get_cv_moments(self._h, _dp(m)))
+        return m
 
     def geometry(self):
         xu = np.zeros(self.cfg.imax + 1, np.float32)

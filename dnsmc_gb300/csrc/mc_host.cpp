@@ -286,8 +286,9 @@ struct dnsmc_solver {
     DevBuf<int> d_cv_grp, d_cv_sid;
     DevBuf<double> d_cv_C;
     DevBuf<float2> d_layer, d_sur;
-    DevBuf<double> d_Jhat, d_muY;
-    DevBuf<float> d_beta;
+    DevBuf<double2> d_Jhat, d_muY;
+    DevBuf<float2> d_beta;
+    DevBuf<double> d_moments;
     bool beta_set = false;
     int cv_samples = 0;
 
@@ -356,6 +357,8 @@ int check_config(const dnsmc_config &c) {
     if (c.sampler == DNSMC_SAMPLER_RQMC && c.nvar < 2) return fail(DNSMC_ERR_ARG, "the RQMC sampler needs nvar >= 2 replicates");
     if (c.local_sampling != 0 && c.local_sampling != 1) return fail(DNSMC_ERR_ARG, "local_sampling must be 0 or 1");
     if (c.control_variate != 0 && c.control_variate != 1) return fail(DNSMC_ERR_ARG, "control_variate must be 0 or 1");
+    if (c.cv_moments != 0 && c.cv_moments != 1) return fail(DNSMC_ERR_ARG, "cv_moments must be 0 or 1");
+    if (c.cv_moments && !c.control_variate) return fail(DNSMC_ERR_ARG, "cv_moments needs control_variate = 1");
     if (c.block_threads && c.block_threads != 128 && c.block_threads != 256 && c.block_threads != 512)
         return fail(DNSMC_ERR_ARG, "block_threads must be 0, 128, 256 or 512");
     if (c.tile_a && c.tile_a != 8 && c.tile_a != 16 && c.tile_a != 32)
@@ -825,11 +828,13 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         P.sur = s->d_sur.p;
         P.beta = s->beta_set ? s->d_beta.p : nullptr;
     }
+    const bool mom = cv && c.cv_moments;
     if (trace) {
         P.trace_f = tf; P.trace_g = tg; P.trace_p = tp; P.trace_r = tr; P.trace_max = tmax_steps;
         P.trace_rec = d_trace_rec; P.trace_n = d_trace_n; P.trace_rng = d_trace_rng;
         P.tally = nullptr;
-        const int rc = cv ? launch_march_cv(mode, P, 1, 32, s->stream, true) : launch_march(mode, P, 1, 32, s->stream, true);
+        const int rc = cv ? launch_march_cv(mode, P, 1, 32, s->stream, true, false)
+                          : launch_march(mode, P, 1, 32, s->stream, true);
         if (rc) return fail(DNSMC_ERR_CUDA, "trace launch: %s", cudaGetErrorString((cudaError_t)rc));
         return DNSMC_OK;
     }
@@ -870,16 +875,20 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         if (rc) return fail(DNSMC_ERR_CUDA, "control-variate launch: %s", cudaGetErrorString((cudaError_t)rc));
         s->cv_samples = S;
         P.sur = s->d_sur.p;
+        if (mom) {
+            TRY(s->d_moments.ensure((size_t)s->nfields * P.n_groups * P.region_cells * 9));
+            P.moments = s->d_moments.p;
+        }
     }
     TRY(s->d_tally.ensure((size_t)s->nfields * P.n_groups * P.region_cells));
     P.tally = s->d_tally.p;
     CUDA_TRY(cudaMemsetAsync(s->d_misc.p, 0, 4 * sizeof(unsigned int), s->stream));
     CUDA_TRY(cudaMemsetAsync(s->d_counters.p, 0, 2 * sizeof(unsigned long long), s->stream));
     const int sms = device_sm_count();
-    const int occ = cv ? march_cv_occupancy(mode, threads) : march_occupancy(mode, threads);
+    const int occ = cv ? march_cv_occupancy(mode, threads, mom) : march_occupancy(mode, threads);
     const int blocks = std::max(1, sms * occ);
     CUDA_TRY(cudaEventRecord(s->ev_march0, s->stream));
-    int rc = cv ? launch_march_cv(mode, P, blocks, threads, s->stream, false)
+    int rc = cv ? launch_march_cv(mode, P, blocks, threads, s->stream, false, mom)
                 : launch_march(mode, P, blocks, threads, s->stream, false);
     if (rc) return fail(DNSMC_ERR_CUDA, "march launch: %s", cudaGetErrorString((cudaError_t)rc));
     CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
@@ -1043,6 +1052,7 @@ void dnsmc_set_default_config(dnsmc_config *c) {
     c->sampler = DNSMC_SAMPLER_IID;
     c->local_sampling = 0;
     c->control_variate = 0;
+    c->cv_moments = 0;
     c->block_threads = 0;
     c->tile_a = 0;
 }
@@ -1391,20 +1401,47 @@ int dnsmc_set_cv_beta(dnsmc_solver *s, const float *beta) {
     region_dims(s, &ni, &nj, &nk);
     const long long rc_ = (long long)ni * nj * nk;
     const int nG = s->cfg.model == DNSMC_MODEL_GREY ? 1 : std::min(s->cfg.n_groups, std::max(1, s->tab.nbands));
-    // dense [f][g][k][j][i] -> tally layout [f][g][i][k][j]
-    std::vector<float> tl((size_t)s->nfields * nG * rc_);
+    // dense [f][g][k][j][i][2] -> tally layout [f][g][i][k][j]
+    std::vector<float2> tl((size_t)s->nfields * nG * rc_);
     for (long long fg = 0; fg < (long long)s->nfields * nG; ++fg)
         for (int k = 0; k < nk; ++k)
             for (int j = 0; j < nj; ++j)
                 for (int i = 0; i < ni; ++i) {
-                    const float b = beta[fg * rc_ + i + (long long)ni * (j + (long long)nj * k)];
-                    if (!std::isfinite(b)) return fail(DNSMC_ERR_ARG, "control-variate coefficients must be finite");
-                    tl[fg * rc_ + ((long long)i * nk + k) * nj + j] = b;
+                    const float *b = beta + 2 * (fg * rc_ + i + (long long)ni * (j + (long long)nj * k));
+                    if (!std::isfinite(b[0]) || !std::isfinite(b[1]))
+                        return fail(DNSMC_ERR_ARG, "control-variate coefficients must be finite");
+                    tl[fg * rc_ + ((long long)i * nk + k) * nj + j] = make_float2(b[0], b[1]);
                 }
     TRY(set_device(s));
     TRY(s->d_beta.ensure(tl.size()));
-    CUDA_TRY(cudaMemcpy(s->d_beta.p, tl.data(), tl.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(s->d_beta.p, tl.data(), tl.size() * sizeof(float2), cudaMemcpyHostToDevice));
     s->beta_set = true;
+    return DNSMC_OK;
+}
+
+static void tally_to_dense(const double *src, double *dst, long long nfg, int ni, int nj, int nk, int width) {
+    const long long rc_ = (long long)ni * nj * nk;
+    for (long long fg = 0; fg < nfg; ++fg)
+        for (int i = 0; i < ni; ++i)
+            for (int k = 0; k < nk; ++k)
+                for (int j = 0; j < nj; ++j)
+                    for (int q = 0; q < width; ++q)
+                        dst[width * (fg * rc_ + i + (long long)ni * (j + (long long)nj * k)) + q] =
+                            src[width * (fg * rc_ + ((long long)i * nk + k) * nj + j) + q];
+}
+
+int dnsmc_get_cv_moments(dnsmc_solver *s, double *moments) {
+    if (!s || !moments) return fail(DNSMC_ERR_ARG, "null argument");
+    if (!s->solved || !s->cfg.control_variate || !s->cfg.cv_moments)
+        return fail(DNSMC_ERR_STATE, "no solve with cv_moments = 1 has been run");
+    TRY(wait_done(s, 0));
+    TRY(set_device(s));
+    int ni, nj, nk;
+    region_dims(s, &ni, &nj, &nk);
+    const long long nfg = (long long)s->nfields * s->last.n_groups;
+    std::vector<double> tl((size_t)(nfg * ni * nj * nk * 9));
+    CUDA_TRY(cudaMemcpy(tl.data(), s->d_moments.p, tl.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    tally_to_dense(tl.data(), moments, nfg, ni, nj, nk, 9);
     return DNSMC_OK;
 }
 
@@ -1418,19 +1455,14 @@ int dnsmc_get_cv_data(dnsmc_solver *s, int *n_samples, float *layer, float *sur,
     const size_t nl = (size_t)s->nfields * s->cfg.imax, ns = nl * S;
     if (layer) CUDA_TRY(cudaMemcpy(layer, s->d_layer.p, nl * sizeof(float2), cudaMemcpyDeviceToHost));
     if (sur) CUDA_TRY(cudaMemcpy(sur, s->d_sur.p, ns * sizeof(float2), cudaMemcpyDeviceToHost));
-    if (Jhat) CUDA_TRY(cudaMemcpy(Jhat, s->d_Jhat.p, ns * sizeof(double), cudaMemcpyDeviceToHost));
+    if (Jhat) CUDA_TRY(cudaMemcpy(Jhat, s->d_Jhat.p, ns * sizeof(double2), cudaMemcpyDeviceToHost));
     if (muY) {
         int ni, nj, nk;
         region_dims(s, &ni, &nj, &nk);
-        const long long rc_ = (long long)ni * nj * nk;
         const long long nfg = (long long)s->nfields * s->last.n_groups;
-        std::vector<double> tl((size_t)(nfg * rc_));
+        std::vector<double> tl((size_t)(nfg * ni * nj * nk * 2));
         CUDA_TRY(cudaMemcpy(tl.data(), s->d_muY.p, tl.size() * sizeof(double), cudaMemcpyDeviceToHost));
-        for (long long fg = 0; fg < nfg; ++fg)
-            for (int i = 0; i < ni; ++i)
-                for (int k = 0; k < nk; ++k)
-                    for (int j = 0; j < nj; ++j)
-                        muY[fg * rc_ + i + (long long)ni * (j + (long long)nj * k)] = tl[fg * rc_ + ((long long)i * nk + k) * nj + j];
+        tally_to_dense(tl.data(), muY, nfg, ni, nj, nk, 2);
     }
     return DNSMC_OK;
 }

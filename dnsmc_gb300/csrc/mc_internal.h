@@ -73,7 +73,8 @@ struct MarchParams {
     const float2 *sur;        // [f][sample][nw] (k_bar, Ib_bar) per layer
     int n_samples;            // bands * nq (1 for the grey model)
     int sample_stride;        // nT * nX: k-table offset -> sample index
-    const float *beta;        // [f][group][iR][kR][jR] CV coefficient, or null (1)
+    const float2 *beta;       // [f][group][iR][kR][jR] (beta_a, beta_b), or null: (1, -1)
+    double *moments;          // [f][group][iR][kR][jR][9] per-ray moments (training solves)
     // trace (trace launches only)
     int trace_f, trace_g, trace_p, trace_r, trace_max;
     int *trace_rec;           // 6 words per step
@@ -91,8 +92,8 @@ struct FinalizeParams {
     int batched, nbatch;      // RQMC: variance from nbatch replicate means
     const int *group_empty;   // 1 when the group has no emission
     const double2 *tally;
-    const double *muY;        // control variate mean, tally layout, or null
-    const float *beta;        // CV coefficient, tally layout, or null (1)
+    const double2 *muY;       // (E[Y_a], E[Y_b]), tally layout, or null
+    const float2 *beta;       // (beta_a, beta_b), tally layout, or null: (1, -1)
     double *Q;                // [f][cell] dense region, i fastest
     double *var;              // [f][cell]
     double *Qg;               // [f][group][cell] or nullptr
@@ -116,8 +117,9 @@ int launch_field_stats(const float *fT, const float2 *fTX, long long n,
                        double *partials, float *out, void *stream);
 int field_stats_partials();   // doubles needed in `partials`
 int march_occupancy(int mode, int threads);  // resident blocks per SM
-int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace);
-int march_cv_occupancy(int mode, int threads);
+int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace,
+                    bool moments);
+int march_cv_occupancy(int mode, int threads, bool moments);
 
 // Control-variate preparation (all stream-ordered).
 struct CvParams {
@@ -136,7 +138,8 @@ struct CvParams {
     const float *fw;          // nw+1 faces
     float toll;
     int nquad;                // nodes per hemisphere
-    double *Jhat;             // [f][sample][nw] direction-averaged surrogate intensity
+    double2 *Jhat;            // [f][sample][nw] (Jhat, Ahat): direction-averaged surrogate
+                              // intensity and own-layer absorptance
     // mean of Y per (field, group, cell) in tally layout
     int n_groups;
     const int *grp_start;     // n_groups+1 into samp_id / samp_C
@@ -145,7 +148,7 @@ struct CvParams {
     double Wgrey;
     int ew0, ew1, ea0, ea1, eb0, eb1;
     long long region_cells;
-    double *muY;
+    double2 *muY;
 };
 int launch_cv_prepare(const CvParams &c, void *stream);
 int launch_cv_mean(const CvParams &c, void *stream);

@@ -169,7 +169,7 @@ __device__ __forceinline__ float lookup_ib(const MarchParams &P, int nb, int ti,
 // The march kernel.  Persistent: every warp pulls work items (field, band
 // group, packet) from an atomic counter until the queue is empty.
 // ---------------------------------------------------------------------------
-template <int MODE, bool TRACE, bool CV>
+template <int MODE, bool TRACE, bool CV, bool MOM = false>
 __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -243,8 +243,12 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
         }
         const uint32_t ctr2 = (uint32_t)G | ((uint32_t)(f + P.field_base) << 16);
         const long long tc = ((long long)(w0 - P.ew0) * nkR + (bcl - P.eb0)) * njR + (acl - P.ea0);
-        float beta = 1.0f;
+        float2 beta = make_float2(1.0f, -1.0f);
         if (CV && P.beta) beta = P.beta[fg * P.region_cells + tc];
+        double mo[9];
+        if (MOM)
+#pragma unroll
+            for (int q = 0; q < 9; ++q) mo[q] = 0.0;
         const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
 
         double S = 0.0, S2 = 0.0, Sb = 0.0;
@@ -299,7 +303,7 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
             }
             // surrogate walk (warp-uniform): same segments, layer-mean medium
             const float2 *surp = nullptr;
-            float taus = 0.0f, Jbar = 0.0f;
+            float taus = 0.0f, Jbar = 0.0f, tex0 = -1.0f;
             if (CV) {
                 const int sid = (MODE == MODE_GREY) ? 0 : koff / P.sample_stride;
                 surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
@@ -372,6 +376,7 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                 }
                 t = tn;
                 ++steps;
+                if (CV && axis == 0 && tex0 < 0.0f) tex0 = taus;  // surrogate leaves the own layer
                 if (axis == 0) {
                     cw += dW;
                     if (cw < 0 || cw >= P.nw) {
@@ -410,8 +415,19 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
             if (TRACE && lane == 0) *P.trace_n = steps;
             float X = w * D;
             if (CV) {
-                const float Y = wk * (Ii - Jbar);
-                X = X - beta * Y;  // tallied: X - beta*Y, its mean is added back at finalize
+                // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
+                const float te = tex0 < 0.0f ? 0.0f : tex0;
+                const float Iw0 = __ldg(&surp[w0].y);
+                const float Ya = wk * (Ii - Jbar);
+                const float Yb = wk * ((1.0f - te) * (Ii - Iw0));
+                if (MOM && active) {
+                    const double xd = X, ya = Ya, yb = Yb;
+                    mo[0] += xd; mo[1] += ya; mo[2] += yb;
+                    mo[3] = fma(xd, xd, mo[3]); mo[4] = fma(ya, ya, mo[4]); mo[5] = fma(yb, yb, mo[5]);
+                    mo[6] = fma(xd, ya, mo[6]); mo[7] = fma(xd, yb, mo[7]); mo[8] = fma(ya, yb, mo[8]);
+                }
+                X = X - beta.x * Ya;  // tallied: X - beta_a Y_a - beta_b Y_b; the
+                X = X - beta.y * Yb;  // means beta . E[Y] are added back at finalize
             }
             if (active) {
                 ++my_rays;
@@ -432,6 +448,11 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
         }
         if (TRACE) return;
         if (active) P.tally[fg * P.region_cells + tc] = make_double2(S, S2);
+        if (MOM && active) {
+            double *out = P.moments + (fg * P.region_cells + tc) * 9;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) out[q] = mo[q];
+        }
     }
     // per-warp counters and status
     for (int o = 16; o > 0; o >>= 1) {
@@ -482,8 +503,11 @@ __global__ void finalize_kernel(const FinalizeParams F) {
             }
             if (F.muY && !F.group_empty[g]) {
                 const long long ti = ((long long)f * F.n_groups + g) * F.region_cells + tc;
-                const double b = F.beta ? (double)F.beta[ti] : 1.0;
-                m += b * F.muY[ti];  // Q_g = beta * E[Y] + mean(X - beta * Y)
+                const float2 b = F.beta ? F.beta[ti] : make_float2(1.0f, -1.0f);
+                const double2 mu = F.muY[ti];
+                // Q_g = beta_a E[Y_a] + beta_b E[Y_b] + mean(X - beta_a Y_a - beta_b Y_b)
+                m += (double)b.x * mu.x;
+                m += (double)b.y * mu.y;
             }
             Q += m;
             V += v;
@@ -594,9 +618,19 @@ int launch_march(int mode, const MarchParams &p, int blocks, int threads, void *
     return (int)cudaGetLastError();
 }
 
-int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace) {
+int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace,
+                    bool moments) {
     cudaStream_t st = (cudaStream_t)stream;
     if (trace) { blocks = 1; threads = 32; }
+    if (moments && !trace) {
+        switch (mode) {
+            case MODE_GREY: march_kernel<MODE_GREY, false, true, true><<<blocks, threads, 0, st>>>(p); break;
+            case MODE_T: march_kernel<MODE_T, false, true, true><<<blocks, threads, 0, st>>>(p); break;
+            case MODE_TX: march_kernel<MODE_TX, false, true, true><<<blocks, threads, 0, st>>>(p); break;
+            default: return (int)cudaErrorInvalidValue;
+        }
+        return (int)cudaGetLastError();
+    }
     switch (mode) {
         case MODE_GREY:
             if (trace) march_kernel<MODE_GREY, true, true><<<blocks, threads, 0, st>>>(p);
@@ -616,9 +650,16 @@ int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, voi
     return (int)cudaGetLastError();
 }
 
-int march_cv_occupancy(int mode, int threads) {
+int march_cv_occupancy(int mode, int threads, bool moments) {
     int nb = 0;
     cudaError_t e = cudaErrorInvalidValue;
+    if (moments) {
+        if (mode == MODE_GREY) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false, true, true>, threads, 0);
+        if (mode == MODE_T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false, true, true>, threads, 0);
+        if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false, true, true>, threads, 0);
+        if (e != cudaSuccess) return 1;
+        return nb > 0 ? nb : 1;
+    }
     if (mode == MODE_GREY) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false, true>, threads, 0);
     if (mode == MODE_T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false, true>, threads, 0);
     if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false, true>, threads, 0);
@@ -732,13 +773,13 @@ __global__ void cv_jhat_kernel(const CvParams c) {
         const float2 *sp = c.sur + fs * c.nw;
         const int band = c.mode == MODE_GREY ? 0 : sid / c.nq;
         const float oW = (__ldg(c.fw + w) + __ldg(c.fw + w + 1)) * 0.5f;
-        double acc = 0.0;
+        double acc = 0.0, accA = 0.0;
         for (int h = 0; h < 2; ++h) {
             const int dir = h ? 1 : -1;
             const float Iw = c.mode == MODE_GREY ? c.Tw4[h] : __ldg(c.ibw + h * c.nbands + band);
             for (int q = 0; q < c_nquad; ++q) {
                 const float inv_mu = (float)(1.0 / c_quad_mu[q]);
-                float tau = 1.0f, J = 0.0f;
+                float tau = 1.0f, J = 0.0f, t0 = 0.0f;
                 int l = w;
                 float seg = dir > 0 ? (__ldg(c.fw + w + 1) - oW) : (oW - __ldg(c.fw + w));
                 for (;;) {
@@ -748,14 +789,16 @@ __global__ void cv_jhat_kernel(const CvParams c) {
                     J = fmaf(ta, kv.y, J);
                     tau = tau - ta;
                     if (tau < c.toll) { J = fmaf(tau, kv.y, J); tau = 0.0f; break; }
+                    if (l == w) t0 = tau;  // transmissivity leaving the own layer
                     l += dir;
                     if (l < 0 || l >= c.nw) { J = fmaf(tau, Iw, J); break; }
                     seg = __ldg(c.fw + l + 1) - __ldg(c.fw + l);
                 }
                 acc += c_quad_w[q] * (double)J;
+                accA += c_quad_w[q] * (1.0 - (double)t0);
             }
         }
-        c.Jhat[idx] = 0.5 * acc;
+        c.Jhat[idx] = make_double2(0.5 * acc, 0.5 * accA);
     }
 }
 
@@ -777,22 +820,28 @@ __global__ void cv_mean_kernel(const CvParams c) {
         float T, x = 0.f;
         if (c.mode == MODE_TX) { const float2 v = c.fieldTX[cell]; T = v.x; x = v.y; }
         else T = c.fieldT[cell];
-        const double *Jh = c.Jhat + (long long)f * c.n_samples * c.nw + w;
+        const double2 *Jh = c.Jhat + (long long)f * c.n_samples * c.nw + w;
+        const float2 *Sw = c.sur + (long long)f * c.n_samples * c.nw + w;
         (void)niR;
         for (int g = 0; g < c.n_groups; ++g) {
-            double acc = 0.0;
+            double acc = 0.0, accB = 0.0;
             if (c.mode == MODE_GREY) {
                 const float t2 = T * T;
-                acc = c.Wgrey * ((double)(t2 * t2) - Jh[0]);
+                const double2 jh = Jh[0];
+                acc = c.Wgrey * ((double)(t2 * t2) - jh.x);
+                accB = c.Wgrey * ((double)(t2 * t2) - (double)Sw[0].y) * jh.y;
             } else {
                 for (int q = c.grp_start[g]; q < c.grp_start[g + 1]; ++q) {
                     const int sid = c.samp_id[q];
                     const float k = cv_k(c, sid, T, x);
                     const float Ib = cv_ib(c, sid / c.nq, T);
-                    acc += c.samp_C[q] * (double)k * ((double)Ib - Jh[(long long)sid * c.nw]);
+                    const double2 jh = Jh[(long long)sid * c.nw];
+                    const double ck = c.samp_C[q] * (double)k;
+                    acc += ck * ((double)Ib - jh.x);
+                    accB += ck * ((double)Ib - (double)Sw[(long long)sid * c.nw].y) * jh.y;
                 }
             }
-            c.muY[((long long)f * c.n_groups + g) * c.region_cells + tc] = acc;
+            c.muY[((long long)f * c.n_groups + g) * c.region_cells + tc] = make_double2(acc, accB);
         }
     }
 }

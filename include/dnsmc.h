@@ -109,6 +109,8 @@ typedef struct dnsmc_config {
                                  /* through the plane-averaged T and x_H2O     */
                                  /* profile; E[Y] from a 1-D layered-slab     */
                                  /* quadrature is added back (unbiased)        */
+    int   cv_moments;            /* 1: also tally per-ray moments of X and the  */
+                                 /* two control variates (network training)    */
     /* kernel shape (0 = automatic) */
     int   block_threads;         /* 128, 256 or 512                              */
     int   tile_a;                /* cells of a packet along j: 8, 16 or 32       */
@@ -230,16 +232,24 @@ int  dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *n_tbins,
 /* Build the sampling tables for a given Tmax and mean x_H2O on the host
  * without solving (no GPU needed); dnsmc_get_sampling then returns them.     */
 int  dnsmc_prepare_sampling(dnsmc_solver *s, float Tmax, float xmean);
-/* Control-variate coefficients beta per (field, band group, cell of the
- * region), dense i fastest (NULL: beta = 1).  Any finite beta keeps the
- * estimate unbiased; the variance is smallest near Cov(X,Y)/Var(Y).          */
+/* The control variate has two terms: Y_a, the ray's contribution in the
+ * medium of plane-averaged T and x_H2O, and Y_b, the part of Y_a from the
+ * emitting plane itself.  The march tallies X - beta_a Y_a - beta_b Y_b and
+ * beta_a E[Y_a] + beta_b E[Y_b] is added back.  Coefficients per (field,
+ * band group, cell of the region), dense i fastest, pairs (beta_a, beta_b);
+ * NULL restores (1, -1).  Any finite pair keeps the estimate unbiased.       */
 int  dnsmc_set_cv_beta(dnsmc_solver *s, const float *beta);
 /* Control-variate data of the last solve (any pointer may be NULL): layer
  * means (T_bar, x_bar) [f][imax][2], surrogate (k_bar, Ib_bar)
- * [f][sample][imax][2] (sample = band*nq + g), Jhat [f][sample][imax] and
- * E[Y] [f][group][cell] dense i fastest.  n_samples receives bands*nq.      */
+ * [f][sample][imax][2] (sample = band*nq + g), (Jhat, Ahat) [f][sample][imax][2]
+ * (direction-averaged absorbed intensity, own-plane absorptance) and
+ * (E[Y_a], E[Y_b]) [f][group][cell][2] dense i fastest.                      */
 int  dnsmc_get_cv_data(dnsmc_solver *s, int *n_samples, float *layer, float *sur,
                        double *Jhat, double *muY);
+/* Per-ray moments of the last solve with cv_moments = 1, [f][group][cell][9]
+ * dense i fastest: sums of X, Y_a, Y_b, X^2, Y_a^2, Y_b^2, X Y_a, X Y_b,
+ * Y_a Y_b over the cell's rays (X is the plain OERM ray contribution).       */
+int  dnsmc_get_cv_moments(dnsmc_solver *s, double *moments);
 /* Wall-normal faces (imax+1) and periodic cell sizes used by the march.       */
 int  dnsmc_get_geometry(const dnsmc_solver *s, float *xu, float *dy, float *dz);
 

@@ -551,7 +551,8 @@ typedef struct {
     int cv;                   // 1: tally X - beta*Y, Y = the same ray through the layer-mean profile
     const float *sur_k;       // [field][sample][nw] layer-mean absorption coefficient
     const float *sur_I;       // [field][sample][nw] layer-mean band intensity
-    const float *beta;        // [field][group][k][j][i] dense, or NULL (1)
+    const float *beta;        // [field][group][k][j][i][2] (beta_a, beta_b) dense, or NULL (1, -1)
+    double *moments;          // optional [f][G][tc][9]: sums X, Ya, Yb, X^2, Ya^2, Yb^2, X Ya, X Yb, Ya Yb
 } OrcPacketConfig;
 
 }  // extern "C"
@@ -777,7 +778,7 @@ struct Packet {
                 tau[l] = act[l] ? (R)1 : (R)0;
                 D[l] = 0;
             }
-            R taus = c.cv ? (R)1 : (R)0, Jbar = 0;
+            R taus = c.cv ? (R)1 : (R)0, Jbar = 0, tau_exit0 = -1;
             const int sid = c.mode != 0 ? koff / (c.nT * c.nX) : 0;
             const int nsamp = c.mode != 0 ? c.nbands * c.nq : 1;
             const size_t sbase = ((size_t)f * nsamp + sid) * c.nw;
@@ -838,6 +839,7 @@ struct Packet {
                 }
                 t = tn;
                 ++stepn;
+                if (axis == 0 && tau_exit0 < 0) tau_exit0 = taus;  // surrogate transmissivity leaving the own layer
                 if (axis == 0) {
                     cw += dW;
                     if (cw < 0 || cw >= c.nw) {
@@ -875,16 +877,30 @@ struct Packet {
                 if (!act[l]) continue;
                 R X = w[l] * D[l];
                 if (c.cv) {
-                    R beta = 1;
+                    const int nG = c.mode == 0 ? 1 : c.n_groups;
+                    const int niR = c.ew1 - c.ew0, njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0;
+                    const long long rc = (long long)niR * njR * nkR;
+                    R ba = 1, bb = -1;
                     if (c.beta) {
-                        const int nG = c.mode == 0 ? 1 : c.n_groups;
-                        const int niR = c.ew1 - c.ew0, njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0;
-                        const long long rc = (long long)niR * njR * nkR;
-                        beta = (R)c.beta[((long long)f * nG + G) * rc + (w0 - c.ew0) +
-                                         (long long)niR * ((a0[l] - c.ea0) + (long long)njR * (b0[l] - c.eb0))];
+                        const float *bp = c.beta + 2 * (((long long)f * nG + G) * rc + (w0 - c.ew0) +
+                                                         (long long)niR * ((a0[l] - c.ea0) + (long long)njR * (b0[l] - c.eb0)));
+                        ba = (R)bp[0];
+                        bb = (R)bp[1];
                     }
-                    const R Y = wk[l] * (Ii[l] - Jbar);
-                    X = X - beta * Y;
+                    const R te = tau_exit0 < 0 ? (R)0 : tau_exit0;
+                    const R Iw0 = (R)c.sur_I[sbase + w0];
+                    const R Ya = wk[l] * (Ii[l] - Jbar);
+                    const R Yb = wk[l] * (((R)1 - te) * (Ii[l] - Iw0));
+                    if (c.moments) {
+                        const long long tc = ((long long)(w0 - c.ew0) * nkR + (b0[l] - c.eb0)) * njR + (a0[l] - c.ea0);
+                        double *mo = c.moments + 9 * (((long long)f * nG + G) * rc + tc);
+                        const double xd = (double)X, ya = (double)Ya, yb = (double)Yb;
+                        mo[0] += xd; mo[1] += ya; mo[2] += yb;
+                        mo[3] = std::fma(xd, xd, mo[3]); mo[4] = std::fma(ya, ya, mo[4]); mo[5] = std::fma(yb, yb, mo[5]);
+                        mo[6] = std::fma(xd, ya, mo[6]); mo[7] = std::fma(xd, yb, mo[7]); mo[8] = std::fma(ya, yb, mo[8]);
+                    }
+                    X = X - ba * Ya;
+                    X = X - bb * Yb;
                 }
                 const double Xd = (double)X;
                 S[l] += Xd;

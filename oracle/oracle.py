@@ -61,7 +61,7 @@ class PacketConfig(ctypes.Structure):
         ("rays", ctypes.c_int), ("rays_per_packet", _i), ("seed", ctypes.c_uint64),
         ("toll", ctypes.c_float), ("max_steps", ctypes.c_int), ("use_double", ctypes.c_int),
         ("sampler", ctypes.c_int), ("nbatch", ctypes.c_int), ("n_tbins", ctypes.c_int),
-        ("cv", ctypes.c_int), ("sur_k", _f), ("sur_I", _f), ("beta", _f),
+        ("cv", ctypes.c_int), ("sur_k", _f), ("sur_I", _f), ("beta", _f), ("moments", _d),
     ]
 
 
@@ -238,20 +238,22 @@ def cv_quadrature():
 
 
 def cv_jhat(sur_k, sur_I, fw, toll, Iw_west, Iw_east):
-    """Direction-averaged intensity absorbed along rays leaving the centre of
-    each layer of a 1-D layered medium (k, Ib per layer; black walls with
-    intensities Iw), truncated at transmissivity toll like the march:
-    Jhat[l] = 1/2 int_{-1}^{1} J(mu; l) dmu, in float64."""
+    """For every layer l of a 1-D layered medium (k, Ib per layer; black walls
+    with intensities Iw), rays leaving the layer centre truncated at
+    transmissivity toll like the march, in float64:
+    Jhat[l] = 1/2 int_{-1}^{1} J(mu; l) dmu (absorbed intensity) and
+    Ahat[l] = 1/2 int_{-1}^{1} (1 - t0(mu; l)) dmu (own-layer absorptance).
+    Returns an (nw, 2) array."""
     nw = len(sur_k)
     mu, wt = cv_quadrature()
     fw = np.asarray(fw, np.float64)
     o = 0.5 * (fw[:-1] + fw[1:])
-    out = np.zeros(nw)
+    out = np.zeros((nw, 2))
     for l in range(nw):
-        acc = 0.0
+        acc = accA = 0.0
         for d, Iw in ((-1, Iw_west), (1, Iw_east)):
             for m, wq in zip(mu, wt):
-                tau, J, i = 1.0, 0.0, l
+                tau, J, i, t0 = 1.0, 0.0, l, 0.0
                 seg = (fw[l + 1] - o[l]) if d > 0 else (o[l] - fw[l])
                 while True:
                     a = -math.expm1(-float(sur_k[i]) * seg / m)
@@ -260,13 +262,16 @@ def cv_jhat(sur_k, sur_I, fw, toll, Iw_west, Iw_east):
                     if tau < toll:
                         J += tau * float(sur_I[i])
                         break
+                    if i == l:
+                        t0 = tau
                     i += d
                     if i < 0 or i >= nw:
                         J += tau * Iw
                         break
                     seg = fw[i + 1] - fw[i]
                 acc += wq * J
-        out[l] = 0.5 * acc
+                accA += wq * (1.0 - t0)
+        out[l] = 0.5 * acc, 0.5 * accA
     return out
 
 

@@ -35,7 +35,11 @@ def assert_bitexact_cv(s, T, x=None):
     tal = region_tally_to_dense(tal, s, ng)
     N = rays_per_cell(s)
     muY = s.cv_data()["muY"]
-    beta = s._beta if s._beta is not None else np.ones_like(muY, dtype=np.float32)
+    if s._beta is not None:
+        beta = s._beta
+    else:
+        beta = np.zeros(muY.shape, np.float32)
+        beta[..., 0], beta[..., 1] = 1.0, -1.0
     B = s.cfg.nvar
     for g in range(ng):
         m = tal[:, g, ..., 0] / N
@@ -43,7 +47,8 @@ def assert_bitexact_cv(s, T, x=None):
             v = np.maximum(0.0, tal[:, g, ..., 1] / B - m * m) / (B - 1)
         else:
             v = np.maximum(0.0, tal[:, g, ..., 1] / N - m * m) / (N - 1)
-        m = m + beta[:, g].astype(np.float64) * muY[:, g]
+        m = m + beta[:, g, ..., 0].astype(np.float64) * muY[:, g, ..., 0]
+        m = m + beta[:, g, ..., 1].astype(np.float64) * muY[:, g, ..., 1]
         np.testing.assert_array_equal(Qg[:, g], m)
         np.testing.assert_array_equal(Vg[:, g], v)
     assert s.counters().steps == steps
@@ -71,7 +76,7 @@ def test_cv_bitexact_table_x_with_beta():
     s.set_fields(T, x)
     s.set_rays(32)
     assert_bitexact_cv(s, T, x)
-    beta = np.random.default_rng(5).uniform(0.5, 1.5, (1, 3, 4, 32, 8)).astype(np.float32)
+    beta = np.random.default_rng(5).uniform(-1.5, 1.5, (1, 3, 4, 32, 8, 2)).astype(np.float32)
     s.set_cv_beta(beta)
     assert_bitexact_cv(s, T, x)
     s.close()
@@ -97,7 +102,7 @@ def test_cv_quadrature_and_mean_match_oracle():
     for sid in (0, 5, 17, 23):
         J = O.cv_jhat(cv["sur"][0, sid, :, 0], cv["sur"][0, sid, :, 1], xu, s.cfg.toll, ibw[0, sid // nq],
                       ibw[1, sid // nq])
-        np.testing.assert_allclose(cv["Jhat"][0, sid], J, rtol=2e-5)
+        np.testing.assert_allclose(cv["Jhat"][0, sid], J, rtol=2e-5, atol=1e-12)
     # E[Y] per cell from its definition: sum over the group's samples of
     # C_s k_i (Ib_i - Jhat), C_s = W_s * q(s) of the (single-bin) alias table
     from test_capi import alias_distribution
@@ -108,14 +113,19 @@ def test_cv_quadrature_and_mean_match_oracle():
         for g in range(2):
             p = alias_distribution(smp, g)
             a, e_ = int(smp["group_start"][g]), int(smp["group_start"][g + 1])
-            acc = 0.0
+            acc = accB = 0.0
             for e in range(a, e_):
                 b, gq = smp["band"][e], smp["gq"][e]
                 kv = np.array([np.interp(x[k, j, i], Xg, t["k"][b, gq, it]) for it in range(20)])
                 ki = np.interp(T[k, j, i], Tg, kv)
                 ib = np.interp(T[k, j, i], Tg, t["Ib"][b])
-                acc += smp["W"][e] * p[e - a] * ki * (ib - cv["Jhat"][0, b * nq + gq, i])
-            assert abs(cv["muY"][0, g, k, j, i] - acc) <= 1e-4 * abs(acc) + 1e-9 * np.abs(cv["muY"]).max()
+                sid = b * nq + gq
+                acc += smp["W"][e] * p[e - a] * ki * (ib - cv["Jhat"][0, sid, i, 0])
+                accB += smp["W"][e] * p[e - a] * ki * (ib - cv["sur"][0, sid, i, 1]) * cv["Jhat"][0, sid, i, 1]
+            mu = cv["muY"][0, g, k, j, i]
+            scale = np.abs(cv["muY"]).max()
+            assert abs(mu[0] - acc) <= 1e-4 * abs(acc) + 1e-9 * scale
+            assert abs(mu[1] - accB) <= 1e-4 * abs(accB) + 1e-9 * scale
     s.close()
 
 
@@ -158,3 +168,46 @@ def test_cv_unbiased_and_variance_reduction_ck_channel():
     assert (np.abs(z) > 3).mean() < 0.01 and np.abs(z).max() < 5.5
     ratio = float((Sp ** 2).mean() / (Sc ** 2).mean())
     assert ratio > 10.0, ratio
+
+
+def test_cv_moments_bitexact():
+    import ctypes
+    tb = synth.ck_table(nbands=8, nq=4, nT=20, nX=4, seed=7)
+    s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=6, jmax=32, kmax=4, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=400, T_east=450, seed=8, n_groups=2, control_variate=1,
+                                  cv_moments=1))
+    s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+    T = smooth_field(6, 32, 4, 450, 1700, 2)
+    x = (0.1 + 0.05 * np.random.default_rng(6).uniform(-1, 1, (4, 32, 6))).astype(np.float32)
+    s.set_fields(T, x)
+    s.set_rays(24)
+    s.solve(timeout_s=60)
+    mom = s.cv_moments()
+    c, keep = O.packet_config(s, T, x)
+    rm = np.zeros((1, 2, 6 * 32 * 4, 9))
+    c.moments = rm.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    O.packet_mc(c, 2, 6 * 32 * 4)
+    rm = rm.reshape(1, 2, 6, 4, 32, 9).transpose(0, 1, 3, 4, 2, 5)
+    np.testing.assert_array_equal(mom, rm)
+    assert np.abs(mom[..., 0]).max() > 0
+    s.close()
+
+
+def test_cv_two_term_default_beats_single_term():
+    d = synth.ck_channel(32, 0)
+    tb = synth.ck_table()
+    var = []
+    for beta_b in (0.0, -1.0):
+        s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=32, jmax=32, kmax=32, Lx=2.0, Ly=2 * math.pi,
+                                      Lz=math.pi, stretched_x=0, T_west=400, T_east=400, n_groups=8, seed=5,
+                                      local_sampling=1, control_variate=1))
+        s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+        s.set_fields(d["T"], d["x"])
+        beta = np.zeros((1, 8, 32, 32, 32, 2), np.float32)
+        beta[..., 0], beta[..., 1] = 1.0, beta_b
+        s.set_cv_beta(beta)
+        s.set_rays(128)
+        Q, S = s.solve(timeout_s=120)
+        var.append(float((S ** 2).mean()))
+        s.close()
+    assert var[0] / var[1] > 1.2, var

@@ -173,4 +173,7 @@ def test_cv_jhat_quadrature_matches_isothermal_slab():
     o = 0.5 * (fw[:-1] + fw[1:])
     ex = I[0] - 0.5 * I[0] * np.array([O.expn(2, t) for t in o]) \
         - 0.5 * (I[0] - 300.0 ** 4) * np.array([O.expn(2, 2 - t) for t in o])
-    np.testing.assert_allclose(J, ex, rtol=1e-9)
+    np.testing.assert_allclose(J[:, 0], ex, rtol=1e-9)
+    # own-layer absorptance: 1 - E2(half thickness), same on both sides
+    h = 1.0 / nw
+    np.testing.assert_allclose(J[:, 1], 1 - O.expn(2, h), rtol=1e-9)

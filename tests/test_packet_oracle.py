@@ -139,6 +139,9 @@ def test_cv_replay_isothermal_surrogate_cancels():
     c.cv = 1
     c.sur_k = sk.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
     c.sur_I = sI.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    beta = np.zeros((1, 1, nk, nj, ni, 2), np.float32)
+    beta[..., 0] = 1.0  # Y_a alone: the surrogate equals the medium
+    c.beta = beta.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
     tal, _ = O.packet_mc(c, 1, ni * nj * nk)
     c.cv = 0
     tal0, _ = O.packet_mc(c, 1, ni * nj * nk)
