@@ -48,8 +48,11 @@ def build(verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     inc = ["-I", os.path.join(ROOT, "include"), "-I", CSRC]
     common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo"] + inc
+    # resident 256-thread blocks per SM the march kernels must fit (register cap)
+    minb = int(os.environ.get("DNSMC_MINB", "0"))
+    regs = [f"-DDNSMC_MINB={minb}"] if minb else []
     jobs = [
-        [nvcc, *ARCH, *common, "-fmad=false", "-c", os.path.join(CSRC, "mc_kernels.cu"),
+        [nvcc, *ARCH, *common, *regs, "-fmad=false", "-c", os.path.join(CSRC, "mc_kernels.cu"),
          "-o", os.path.join(bdir, "mc_kernels.o")],
         [nvcc, *common, "-x", "c++", "-c", os.path.join(CSRC, "mc_host.cpp"),
          "-o", os.path.join(bdir, "mc_host.o")],

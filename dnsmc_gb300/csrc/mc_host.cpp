@@ -249,6 +249,9 @@ struct dnsmc_solver {
     // tables
     HostTable tab;
     DevBuf<float> d_k, d_ib, d_ibw;
+    DevBuf<float2> d_kpair, d_ibpair;
+    DevBuf<float> d_posT;
+    DevBuf<float2> d_posTX;
     bool tables_dirty = true;
 
     // fields
@@ -359,8 +362,8 @@ int check_config(const dnsmc_config &c) {
     if (c.control_variate != 0 && c.control_variate != 1) return fail(DNSMC_ERR_ARG, "control_variate must be 0 or 1");
     if (c.cv_moments != 0 && c.cv_moments != 1) return fail(DNSMC_ERR_ARG, "cv_moments must be 0 or 1");
     if (c.cv_moments && !c.control_variate) return fail(DNSMC_ERR_ARG, "cv_moments needs control_variate = 1");
-    if (c.block_threads && c.block_threads != 128 && c.block_threads != 256 && c.block_threads != 512)
-        return fail(DNSMC_ERR_ARG, "block_threads must be 0, 128, 256 or 512");
+    if (c.block_threads && c.block_threads != 128 && c.block_threads != 256)
+        return fail(DNSMC_ERR_ARG, "block_threads must be 0, 128 or 256");
     if (c.tile_a && c.tile_a != 8 && c.tile_a != 16 && c.tile_a != 32)
         return fail(DNSMC_ERR_ARG, "tile_a must be 0, 8, 16 or 32");
     if (!(c.eps_west == 1.0f) || !(c.eps_east == 1.0f))
@@ -700,7 +703,7 @@ int build_sampling(dnsmc_solver *s, float Tmax, float xm) {
                     SpecEntry e;
                     e.prob = thr[j];
                     e.alias_nb = (uint32_t)al[j] | ((uint32_t)b << 16);
-                    e.koff = (int32_t)(((size_t)b * nQ + g) * t.nT * t.nX);
+                    e.koff = (int32_t)sid;
                     e.W = peff[j] > 0 ? (float)(C[sid] / peff[j]) : 0.0f;
                     s->entries.push_back(e);
                 }
@@ -723,6 +726,32 @@ int upload_tables(dnsmc_solver *s) {
     TRY(s->d_ib.ensure(t.Ib.size()));
     CUDA_TRY(cudaMemcpyAsync(s->d_k.p, t.k.data(), t.k.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(cudaMemcpyAsync(s->d_ib.p, t.Ib.data(), t.Ib.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+    // paired tables for two-value loads in the march
+    const int nS = t.nbands * t.nq;
+    std::vector<float2> kp, ip((size_t)t.nbands * (t.nT - 1));
+    if (t.nX > 1) {
+        kp.resize((size_t)nS * t.nT * (t.nX - 1));
+        for (int sid = 0; sid < nS; ++sid)
+            for (int ti = 0; ti < t.nT; ++ti)
+                for (int xi = 0; xi < t.nX - 1; ++xi) {
+                    const float *r = t.k.data() + ((size_t)sid * t.nT + ti) * t.nX + xi;
+                    kp[((size_t)sid * t.nT + ti) * (t.nX - 1) + xi] = make_float2(r[0], r[1]);
+                }
+    } else {
+        kp.resize((size_t)nS * (t.nT - 1));
+        for (int sid = 0; sid < nS; ++sid)
+            for (int ti = 0; ti < t.nT - 1; ++ti) {
+                const float *r = t.k.data() + (size_t)sid * t.nT + ti;
+                kp[(size_t)sid * (t.nT - 1) + ti] = make_float2(r[0], r[1]);
+            }
+    }
+    for (int b = 0; b < t.nbands; ++b)
+        for (int ti = 0; ti < t.nT - 1; ++ti)
+            ip[(size_t)b * (t.nT - 1) + ti] = make_float2(t.Ib[(size_t)b * t.nT + ti], t.Ib[(size_t)b * t.nT + ti + 1]);
+    TRY(s->d_kpair.ensure(kp.size()));
+    TRY(s->d_ibpair.ensure(ip.size()));
+    CUDA_TRY(cudaMemcpyAsync(s->d_kpair.p, kp.data(), kp.size() * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->d_ibpair.p, ip.data(), ip.size() * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     s->tables_dirty = false;
     return DNSMC_OK;
@@ -788,14 +817,13 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     int mode = MODE_GREY;
     if (c.model != DNSMC_MODEL_GREY) mode = (t.nX > 1) ? MODE_TX : MODE_T;
     s->mode = mode;
-    P.fieldT = (mode == MODE_TX) ? nullptr : s->d_fieldT.p;
-    P.fieldTX = (mode == MODE_TX) ? s->d_fieldTX.p : nullptr;
+    P.fieldT = (mode == MODE_GREY) ? s->d_fieldT.p : nullptr;
     if (mode == MODE_TX && !s->have_x) return fail(DNSMC_ERR_STATE, "table has an x_H2O axis but fields were set without x");
     if (mode != MODE_TX && s->have_x)
         return fail(DNSMC_ERR_STATE, "fields carry x_H2O but the spectral model has no x axis: set fields without x");
     P.nbands = t.nbands; P.nT = t.nT; P.nX = t.nX;
     P.T0 = t.T0; P.invdT = 1.0f / t.dT; P.X0 = t.X0; P.invdX = 1.0f / t.dX;
-    P.ktab = s->d_k.p; P.ibtab = s->d_ib.p; P.ibw = s->d_ibw.p;
+    P.kpair = s->d_kpair.p; P.ibpair = s->d_ibpair.p; P.ibw = s->d_ibw.p;
     P.entries = s->d_entries.p; P.group_start = s->d_group_start.p;
     P.n_groups = s->n_groups_used;
     P.n_tbins = s->n_tbins_used;
@@ -814,6 +842,23 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.max_steps = c.max_steps;
     P.region_cells = (long long)ni * nj * nk;
     P.n_items = (long long)s->nfields * P.n_groups * P.n_packets;
+    if (mode != MODE_GREY && !trace) {
+        // table coordinates of the field for this table (once per solve)
+        const long long ncell = (long long)s->nfields * P.field_stride;
+        int rcp;
+        if (mode == MODE_TX) {
+            TRY(s->d_posTX.ensure((size_t)ncell));
+            rcp = launch_field_pos(nullptr, s->d_fieldTX.p, nullptr, s->d_posTX.p, ncell, P.T0, P.invdT, P.nT, P.X0,
+                                   P.invdX, P.nX, s->stream);
+        } else {
+            TRY(s->d_posT.ensure((size_t)ncell));
+            rcp = launch_field_pos(s->d_fieldT.p, nullptr, s->d_posT.p, nullptr, ncell, P.T0, P.invdT, P.nT, P.X0,
+                                   P.invdX, P.nX, s->stream);
+        }
+        if (rcp) return fail(DNSMC_ERR_CUDA, "coordinate launch: %s", cudaGetErrorString((cudaError_t)rcp));
+    }
+    P.fieldP = s->d_posT.p;
+    P.fieldPX = s->d_posTX.p;
     TRY(s->d_misc.ensure(4));
     TRY(s->d_counters.ensure(2));
     P.queue = s->d_misc.p;
@@ -824,7 +869,6 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     const int S = (mode == MODE_GREY) ? 1 : t.nbands * t.nq;
     if (cv) {
         P.n_samples = S;
-        P.sample_stride = t.nT * t.nX;
         P.sur = s->d_sur.p;
         P.beta = s->beta_set ? s->d_beta.p : nullptr;
     }
@@ -856,11 +900,13 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         }
         CvParams cp{};
         cp.nfields = s->nfields; cp.nw = c.imax; cp.na = c.jmax; cp.nb = c.kmax;
-        cp.fieldT = P.fieldT; cp.fieldTX = P.fieldTX; cp.mode = mode;
+        cp.fieldT = (mode == MODE_TX) ? nullptr : s->d_fieldT.p;
+        cp.fieldTX = (mode == MODE_TX) ? s->d_fieldTX.p : nullptr;
+        cp.mode = mode;
         cp.layer = s->d_layer.p;
         cp.nbands = t.nbands; cp.nq = std::max(1, t.nq); cp.nT = t.nT; cp.nX = t.nX;
         cp.T0 = P.T0; cp.invdT = P.invdT; cp.X0 = P.X0; cp.invdX = P.invdX;
-        cp.ktab = P.ktab; cp.ibtab = P.ibtab; cp.ibw = P.ibw;
+        cp.ktab = s->d_k.p; cp.ibtab = s->d_ib.p; cp.ibw = P.ibw;
         cp.kappa = c.kappa; cp.Tw4[0] = P.Tw4[0]; cp.Tw4[1] = P.Tw4[1];
         cp.n_samples = S; cp.sur = s->d_sur.p; cp.fw = s->d_fw.p; cp.toll = c.toll;
         cp.Jhat = s->d_Jhat.p;
@@ -1114,6 +1160,9 @@ int dnsmc_destroy(dnsmc_solver *s) {
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
     s->d_fw.release(); s->d_k.release(); s->d_ib.release(); s->d_ibw.release();
+    s->d_kpair.release(); s->d_ibpair.release(); s->d_posT.release(); s->d_posTX.release();
+    s->d_cv_grp.release(); s->d_cv_sid.release(); s->d_cv_C.release(); s->d_layer.release();
+    s->d_sur.release(); s->d_Jhat.release(); s->d_muY.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();
     s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
@@ -1385,7 +1434,7 @@ int dnsmc_get_sampling(const dnsmc_solver *s, int *n_groups, int *n_tbins, int *
         if (prob) prob[i] = e.prob;
         if (alias) alias[i] = (int)(e.alias_nb & 0xFFFFu);
         if (band) band[i] = (int)(e.alias_nb >> 16);
-        if (gq) gq[i] = (int)((e.koff / (s->tab.nT * s->tab.nX)) % nq);
+        if (gq) gq[i] = (int)(e.koff % nq);
         if (W) W[i] = e.W;
     }
     if (ibw) std::copy(s->ibw.begin(), s->ibw.end(), ibw);

@@ -21,7 +21,7 @@ enum MarchMode { MODE_GREY = 0, MODE_T = 1, MODE_TX = 2 };
 struct SpecEntry {
     float    prob;      // alias threshold (quantised to multiples of 2^-24)
     uint32_t alias_nb;  // alias index (low 16 bits) | band (high 16 bits)
-    int32_t  koff;      // offset of the (band, g) slice in the k table
+    int32_t  koff;      // spectral sample index band*nq + g
     float    W;         // ray weight factor: w = W * k(T_i) * Ib(T_i)
 };
 
@@ -37,13 +37,14 @@ struct MarchParams {
     int n_packets;            // npa * npb * npw
     int nfields;
     long long field_stride;   // cells per field (nw*na*nb)
-    const float  *fieldT;     // MODE_GREY / MODE_T
-    const float2 *fieldTX;    // MODE_TX
+    const float  *fieldT;     // MODE_GREY: temperature
+    const float  *fieldP;     // MODE_T: table temperature coordinate
+    const float2 *fieldPX;    // MODE_TX: (T, x_H2O) table coordinates
     // spectral tables
     int nbands, nT, nX;
     float T0, invdT, X0, invdX;
-    const float *ktab;        // [band][g][t][x]
-    const float *ibtab;       // [band][t]
+    const float2 *kpair;      // [sample][t][x] (k[x], k[x+1]) or [sample][t] (k[t], k[t+1])
+    const float2 *ibpair;     // [band][t] (Ib[t], Ib[t+1])
     const float *ibw;         // [2][band]
     const SpecEntry *entries;
     const int *group_start;   // n_tbins * n_groups + 1, temperature-bin major
@@ -72,7 +73,6 @@ struct MarchParams {
     // control variate: Y = the same ray through the layer-mean medium
     const float2 *sur;        // [f][sample][nw] (k_bar, Ib_bar) per layer
     int n_samples;            // bands * nq (1 for the grey model)
-    int sample_stride;        // nT * nX: k-table offset -> sample index
     const float2 *beta;       // [f][group][iR][kR][jR] (beta_a, beta_b), or null: (1, -1)
     double *moments;          // [f][group][iR][kR][jR][9] per-ray moments (training solves)
     // trace (trace launches only)
@@ -105,6 +105,8 @@ struct FinalizeParams {
 int launch_march(int mode, const MarchParams &p, int blocks, int threads,
                  void *stream, bool trace);
 int launch_finalize(const FinalizeParams &p, void *stream);
+int launch_field_pos(const float *fT, const float2 *fTX, float *outP, float2 *outPX, long long n, float T0,
+                     float invdT, int nT, float X0, float invdX, int nX, void *stream);
 // src element (i, j, k) at src[base + i*si + j*sj + k*sk]; writes dst[f] layout
 int launch_pack_T(const float *src, float *dst, int nw, int na, int nb,
                   long long si, long long sj, long long sk, long long base,

@@ -143,39 +143,66 @@ __device__ __forceinline__ void grid_pos(float v, float v0, float inv, int n, in
     *f = p - (float)ii;
 }
 
+// Split a clamped table coordinate p in [0, n-1] into cell and fraction.
+__device__ __forceinline__ void pos_split(float p, int n, int *i, float *f) {
+    int ii = (int)p;
+    ii = min(ii, n - 2);
+    *i = ii;
+    *f = p - (float)ii;
+}
+
+// Paired tables: kpair holds (k[t][x], k[t][x+1]) (x-tables) or (k[t], k[t+1])
+// and ibpair (Ib[t], Ib[t+1]), so a bilinear lookup is two 8-byte loads.
 template <int MODE>
-__device__ __forceinline__ float lookup_k(const MarchParams &P, int koff, int ti, float ft, int xi, float fx) {
+__device__ __forceinline__ float lookup_k(const MarchParams &P, int sid, int ti, float ft, int xi, float fx) {
     if (MODE == MODE_TX) {
-        const float *s = P.ktab + koff + ti * P.nX + xi;
-        const float k00 = __ldg(s), k01 = __ldg(s + 1);
-        const float k10 = __ldg(s + P.nX), k11 = __ldg(s + P.nX + 1);
-        const float k0 = fmaf(fx, k01 - k00, k00);
-        const float k1 = fmaf(fx, k11 - k10, k10);
+        const int row = P.nX - 1;
+        const float2 *r = P.kpair + (sid * P.nT + ti) * row + xi;
+        const float2 a = __ldg(r), b = __ldg(r + row);
+        const float k0 = fmaf(fx, a.y - a.x, a.x);
+        const float k1 = fmaf(fx, b.y - b.x, b.x);
         return fmaf(ft, k1 - k0, k0);
     } else {
-        const float *s = P.ktab + koff + ti;
-        const float k0 = __ldg(s), k1 = __ldg(s + 1);
-        return fmaf(ft, k1 - k0, k0);
+        const float2 a = __ldg(P.kpair + sid * (P.nT - 1) + ti);
+        return fmaf(ft, a.y - a.x, a.x);
     }
 }
 
 __device__ __forceinline__ float lookup_ib(const MarchParams &P, int nb, int ti, float ft) {
-    const float *s = P.ibtab + nb * P.nT + ti;
-    const float i0 = __ldg(s), i1 = __ldg(s + 1);
-    return fmaf(ft, i1 - i0, i0);
+    const float2 a = __ldg(P.ibpair + nb * (P.nT - 1) + ti);
+    return fmaf(ft, a.y - a.x, a.x);
+}
+
+// Field element type of the march: T (grey), table T coordinate, or (T, x) coordinates.
+template <int MODE> struct FieldT { typedef float type; };
+template <> struct FieldT<MODE_TX> { typedef float2 type; };
+
+template <int MODE>
+__device__ __forceinline__ typename FieldT<MODE>::type load_field(const MarchParams &P, long long fbase, int cell) {
+    if constexpr (MODE == MODE_TX) return __ldg(P.fieldPX + fbase + cell);
+    else if constexpr (MODE == MODE_T) return __ldg(P.fieldP + fbase + cell);
+    else return __ldg(P.fieldT + fbase + cell);
 }
 
 // ---------------------------------------------------------------------------
 // The march kernel.  Persistent: every warp pulls work items (field, band
-// group, packet) from an atomic counter until the queue is empty.
+// group, packet) from an atomic counter until the queue is empty.  The next
+// cell's field value is loaded one step ahead of its use.
 // ---------------------------------------------------------------------------
+// Resident blocks of 256 threads per SM the register allocation must allow
+// (2: up to 128 registers; 3: 85; 4: 64), chosen at build time.
+#ifndef DNSMC_MINB
+#define DNSMC_MINB 2
+#endif
+
 template <int MODE, bool TRACE, bool CV, bool MOM = false>
-__global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
+__global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParams P) {
+    typedef typename FieldT<MODE>::type VT;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int la = lane % P.tile_a, lb = lane / P.tile_a;
     const int njR = P.ea1 - P.ea0, nkR = P.eb1 - P.eb0;
-    const long long plane = (long long)P.na * P.nb;
+    const int plane = P.na * P.nb;
     unsigned long long my_rays = 0, my_steps = 0;
     unsigned int flags = 0;
 
@@ -206,25 +233,25 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
         const int acl = active ? a0 : P.ea0, bcl = active ? b0 : P.eb0;
         const int N = P.rays_per_packet ? P.rays_per_packet[p] : P.rays;
         const long long fbase = (long long)f * P.field_stride;
-        const long long own = fbase + (long long)w0 * plane + (long long)bcl * P.na + acl;
+        const int rowW0 = w0 * plane;
         // own-cell quantities
-        float Ti, Ti4 = 0.f, invTi4 = 0.f;
+        const VT vown = load_field<MODE>(P, fbase, rowW0 + bcl * P.na + acl);
+        float Ti4 = 0.f, invTi4 = 0.f, tpos0 = 0.f;
         int ti_i = 0, xi_i = 0;
         float ft_i = 0.f, fx_i = 0.f;
-        if (MODE == MODE_TX) {
-            const float2 v = __ldg(P.fieldTX + own);
-            Ti = v.x;
-            grid_pos(v.y, P.X0, P.invdX, P.nX, &xi_i, &fx_i);
-        } else {
-            Ti = __ldg(P.fieldT + own);
-        }
-        if (!(Ti > 0.0f) && active) flags |= DNSMC_STATUS_BAD_FIELD;
-        if (MODE == MODE_GREY) {
+        if constexpr (MODE == MODE_GREY) {
+            const float Ti = vown;
+            if (!(Ti > 0.0f) && active) flags |= DNSMC_STATUS_BAD_FIELD;
             const float t2 = Ti * Ti;
             Ti4 = t2 * t2;
             invTi4 = Ti4 > 0.f ? 1.0f / Ti4 : 0.f;
+        } else if constexpr (MODE == MODE_TX) {
+            tpos0 = vown.x;
+            pos_split(vown.x, P.nT, &ti_i, &ft_i);
+            pos_split(vown.y, P.nX, &xi_i, &fx_i);
         } else {
-            grid_pos(Ti, P.T0, P.invdT, P.nT, &ti_i, &ft_i);
+            tpos0 = vown;
+            pos_split(vown, P.nT, &ti_i, &ft_i);
         }
         const float oW = (__ldg(P.fw + w0) + __ldg(P.fw + w0 + 1)) * 0.5f;
         // alias table of this packet: band group G of the temperature bin
@@ -233,8 +260,8 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
         if (MODE != MODE_GREY) {
             int boff = 0;
             if (P.n_tbins > 1) {
-                const float T0v = __shfl_sync(FULL, Ti, 0);
-                int bin = __float2int_rn((T0v - P.T0) * P.invdT);
+                const float tp0 = __shfl_sync(FULL, tpos0, 0);
+                int bin = __float2int_rn(tp0);
                 bin = min(max(bin, 0), P.n_tbins - 1);
                 boff = bin * P.n_groups;
             }
@@ -283,7 +310,7 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
 
             // spectral sample and ray weight
             float w, wk, Ii, invI;
-            int nbnd = 0, koff = 0;
+            int nbnd = 0, sid = 0;
             if (MODE == MODE_GREY) {
                 Ii = Ti4;
                 invI = invTi4;
@@ -294,8 +321,8 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                 SpecEntry e = P.entries[gs + j];
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
-                koff = e.koff;
-                const float ki = lookup_k<MODE>(P, koff, ti_i, ft_i, xi_i, fx_i);
+                sid = e.koff;
+                const float ki = lookup_k<MODE>(P, sid, ti_i, ft_i, xi_i, fx_i);
                 Ii = lookup_ib(P, nbnd, ti_i, ft_i);
                 invI = Ii > 0.f ? 1.0f / Ii : 0.f;
                 wk = e.W * ki;
@@ -305,7 +332,6 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
             const float2 *surp = nullptr;
             float taus = 0.0f, Jbar = 0.0f, tex0 = -1.0f;
             if (CV) {
-                const int sid = (MODE == MODE_GREY) ? 0 : koff / P.sample_stride;
                 surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
                 taus = 1.0f;
             }
@@ -319,11 +345,11 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
             int nA = 0, nB = 0;
             float t = 0.0f;
             int cw = w0, ca = acl, cb = bcl;
-            long long rowW = fbase + (long long)w0 * plane;
-            long long rowB = (long long)cb * P.na;
+            int rowW = rowW0, rowB = cb * P.na;
             float tau = active ? 1.0f : 0.0f;
             float D = 0.0f;
             int steps = 0;
+            VT vcur = vown;
             for (;;) {
                 int axis;
                 float tn;
@@ -331,27 +357,40 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                 else if (tA <= tB)         { axis = 1; tn = tA; }
                 else                       { axis = 2; tn = tB; }
                 const float ds = tn - t;
+                // next cell of the walk, and its field value fetched now
+                int ncw = cw, nca = ca, ncb = cb, nrowW = rowW, nrowB = rowB;
+                bool wall = false;
+                if (axis == 0) {
+                    ncw = cw + dW;
+                    wall = ncw < 0 || ncw >= P.nw;
+                    nrowW = ncw * plane;
+                } else if (axis == 1) {
+                    nca = ca + dA;
+                    if (nca == P.na) nca = 0; else if (nca < 0) nca = P.na - 1;
+                } else {
+                    ncb = cb + dB;
+                    if (ncb == P.nb) ncb = 0; else if (ncb < 0) ncb = P.nb - 1;
+                    nrowB = ncb * P.na;
+                }
+                VT vnext = vcur;
+                if (!wall && tau > 0.0f) vnext = load_field<MODE>(P, fbase, nrowW + nrowB + nca);
                 if (tau > 0.0f) {
                     ++my_steps;
-                    const long long cell = rowW + rowB + ca;
                     float kj, gj;
-                    if (MODE == MODE_GREY) {
-                        const float Tj = __ldg(P.fieldT + cell);
-                        const float t2 = Tj * Tj;
+                    if constexpr (MODE == MODE_GREY) {
+                        const float t2 = vcur * vcur;
                         gj = (Ti4 - t2 * t2) * invI;
                         kj = P.kappa;
                     } else {
                         int tj, xj = 0;
-                        float ftj, fxj = 0.f, Tj;
-                        if (MODE == MODE_TX) {
-                            const float2 v = __ldg(P.fieldTX + cell);
-                            Tj = v.x;
-                            grid_pos(v.y, P.X0, P.invdX, P.nX, &xj, &fxj);
+                        float ftj, fxj = 0.f;
+                        if constexpr (MODE == MODE_TX) {
+                            pos_split(vcur.x, P.nT, &tj, &ftj);
+                            pos_split(vcur.y, P.nX, &xj, &fxj);
                         } else {
-                            Tj = __ldg(P.fieldT + cell);
+                            pos_split(vcur, P.nT, &tj, &ftj);
                         }
-                        grid_pos(Tj, P.T0, P.invdT, P.nT, &tj, &ftj);
-                        kj = lookup_k<MODE>(P, koff, tj, ftj, xj, fxj);
+                        kj = lookup_k<MODE>(P, sid, tj, ftj, xj, fxj);
                         const float Ibj = lookup_ib(P, nbnd, tj, ftj);
                         gj = (Ii - Ibj) * invI;
                     }
@@ -378,9 +417,8 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                 ++steps;
                 if (CV && axis == 0 && tex0 < 0.0f) tex0 = taus;  // surrogate leaves the own layer
                 if (axis == 0) {
-                    cw += dW;
-                    if (cw < 0 || cw >= P.nw) {
-                        const int side = cw < 0 ? 0 : 1;
+                    if (wall) {
+                        const int side = ncw < 0 ? 0 : 1;
                         const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
                         if (tau > 0.0f) {
                             D = fmaf(tau, (Ii - Iw) * invI, D);
@@ -392,20 +430,20 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
                         }
                         break;
                     }
+                    cw = ncw;
+                    rowW = nrowW;
                     tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - oW) : (oW - __ldg(P.fw + cw))) * invW;
-                    rowW = fbase + (long long)cw * plane;
                 } else if (axis == 1) {
                     ++nA;
                     tA = ((float)nA + 0.5f) * dtA;
-                    ca += dA;
-                    if (ca == P.na) ca = 0; else if (ca < 0) ca = P.na - 1;
+                    ca = nca;
                 } else {
                     ++nB;
                     tB = ((float)nB + 0.5f) * dtB;
-                    cb += dB;
-                    if (cb == P.nb) cb = 0; else if (cb < 0) cb = P.nb - 1;
-                    rowB = (long long)cb * P.na;
+                    cb = ncb;
+                    rowB = nrowB;
                 }
+                vcur = vnext;
                 if (!__any_sync(FULL, tau > 0.0f || (CV && taus > 0.0f))) break;
                 if (steps >= P.max_steps) {
                     if (tau > 0.0f || (CV && taus > 0.0f)) flags |= DNSMC_STATUS_STEP_CAP;
@@ -467,6 +505,27 @@ __global__ void __launch_bounds__(512) march_kernel(const MarchParams P) {
     }
 }
 
+// Table coordinates of the field for the march: p = clamp((T - T0)/dT, 0,
+// nT-1) (and the same for x_H2O), computed once per solve with the same FP32
+// operations the march used to apply per step.
+__global__ void field_pos_kernel(const float *fT, const float2 *fTX, float *outP, float2 *outPX, long long n,
+                                 float T0, float invdT, int nT, float X0, float invdX, int nX) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        if (fTX) {
+            const float2 v = fTX[i];
+            float pt = (v.x - T0) * invdT;
+            pt = fminf(fmaxf(pt, 0.0f), (float)(nT - 1));
+            float px = (v.y - X0) * invdX;
+            px = fminf(fmaxf(px, 0.0f), (float)(nX - 1));
+            outPX[i] = make_float2(pt, px);
+        } else {
+            float pt = (fT[i] - T0) * invdT;
+            pt = fminf(fmaxf(pt, 0.0f), (float)(nT - 1));
+            outP[i] = pt;
+        }
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Finalize: per cell of the region, Q = sum over groups of the group means,
@@ -869,6 +928,13 @@ int march_occupancy(int mode, int threads) {
     if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false, false>, threads, 0);
     if (e != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
+}
+
+int launch_field_pos(const float *fT, const float2 *fTX, float *outP, float2 *outPX, long long n, float T0,
+                     float invdT, int nT, float X0, float invdX, int nX, void *stream) {
+    field_pos_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(fT, fTX, outP, outPX, n, T0, invdT, nT,
+                                                                        X0, invdX, nX);
+    return (int)cudaGetLastError();
 }
 
 int launch_finalize(const FinalizeParams &p, void *stream) {

@@ -91,8 +91,8 @@ extern "C" int dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu
     if (!(c.eps_west == 1.0f) || !(c.eps_east == 1.0f)) return report_error(DNSMC_ERR_ARG, "walls must be black");
     if (!(c.kappa >= 0) || !(c.T_west >= 0) || !(c.T_east >= 0)) return report_error(DNSMC_ERR_ARG, "bad kappa or wall T");
     if (!(c.Ly > 0) || !(c.Lz > 0)) return report_error(DNSMC_ERR_ARG, "Ly and Lz must be > 0");
-    if (c.block_threads && c.block_threads != 128 && c.block_threads != 256 && c.block_threads != 512)
-        return report_error(DNSMC_ERR_ARG, "block_threads must be 0, 128, 256 or 512");
+    if (c.block_threads && c.block_threads != 128 && c.block_threads != 256)
+        return report_error(DNSMC_ERR_ARG, "block_threads must be 0, 128 or 256");
     if (c.tile_a && c.tile_a != 8 && c.tile_a != 16 && c.tile_a != 32)
         return report_error(DNSMC_ERR_ARG, "tile_a must be 0, 8, 16 or 32");
     const long long rays = (long long)c.nvar * c.photmax;

@@ -112,7 +112,7 @@ typedef struct dnsmc_config {
     int   cv_moments;            /* 1: also tally per-ray moments of X and the  */
                                  /* two control variates (network training)    */
     /* kernel shape (0 = automatic) */
-    int   block_threads;         /* 128, 256 or 512                              */
+    int   block_threads;         /* 128 or 256                                   */
     int   tile_a;                /* cells of a packet along j: 8, 16 or 32       */
 } dnsmc_config;
 
