@@ -839,6 +839,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.key1 = (uint32_t)(c.seed >> 32);
     P.field_base = 0;
     P.toll = c.toll;
+    P.dtoll = (float)(-log((double)c.toll));
     P.max_steps = c.max_steps;
     P.region_cells = (long long)ni * nj * nk;
     P.n_items = (long long)s->nfields * P.n_groups * P.n_packets;
@@ -908,7 +909,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         cp.T0 = P.T0; cp.invdT = P.invdT; cp.X0 = P.X0; cp.invdX = P.invdX;
         cp.ktab = s->d_k.p; cp.ibtab = s->d_ib.p; cp.ibw = P.ibw;
         cp.kappa = c.kappa; cp.Tw4[0] = P.Tw4[0]; cp.Tw4[1] = P.Tw4[1];
-        cp.n_samples = S; cp.sur = s->d_sur.p; cp.fw = s->d_fw.p; cp.toll = c.toll;
+        cp.n_samples = S; cp.sur = s->d_sur.p; cp.fw = s->d_fw.p; cp.toll = c.toll; cp.dtoll = P.dtoll;
         cp.Jhat = s->d_Jhat.p;
         cp.n_groups = P.n_groups;
         cp.grp_start = s->d_cv_grp.p; cp.samp_id = s->d_cv_sid.p; cp.samp_C = s->d_cv_C.p;

@@ -62,6 +62,7 @@ struct MarchParams {
     int nbatch;               // RQMC replicates per item (rays divisible by it)
     uint32_t field_base;      // field index offset for the RNG counter
     float toll;
+    float dtoll;              // ln(1/toll): optical-depth cut-off of the surrogate walk
     int max_steps;
     // work queue and outputs
     unsigned int *queue;      // atomic item counter (zeroed per launch)
@@ -138,7 +139,7 @@ struct CvParams {
     int n_samples;
     float2 *sur;              // [f][sample][nw]
     const float *fw;          // nw+1 faces
-    float toll;
+    float toll, dtoll;
     int nquad;                // nodes per hemisphere
     double2 *Jhat;            // [f][sample][nw] (Jhat, Ahat): direction-averaged surrogate
                               // intensity and own-layer absorptance

@@ -192,7 +192,7 @@ __device__ __forceinline__ typename FieldT<MODE>::type load_field(const MarchPar
 // Resident blocks of 256 threads per SM the register allocation must allow
 // (2: up to 128 registers; 3: 85; 4: 64), chosen at build time.
 #ifndef DNSMC_MINB
-#define DNSMC_MINB 2
+#define DNSMC_MINB 4
 #endif
 
 template <int MODE, bool TRACE, bool CV, bool MOM = false>
@@ -328,12 +328,21 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 wk = e.W * ki;
                 w = wk * Ii;
             }
-            // surrogate walk (warp-uniform): same segments, layer-mean medium
+            // surrogate walk (warp-uniform): the same ray through the
+            // layer-mean medium.  Its k and Ib are constant inside a wall-
+            // normal layer, so it is advanced once per layer: tauE and tE are
+            // its transmissivity and ray parameter at the layer entry, dcumE
+            // the optical depth from the origin; it stops (dumping the rest
+            // into the current layer) once the optical depth exceeds ln(1/toll).
             const float2 *surp = nullptr;
-            float taus = 0.0f, Jbar = 0.0f, tex0 = -1.0f;
+            float Jbar = 0.0f, tex0 = -1.0f, tauE = 0.0f, tE = 0.0f, dcumE = 0.0f, kS = 0.0f, IS = 0.0f, I0 = 0.0f;
+            bool salive = false;
             if (CV) {
                 surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
-                taus = 1.0f;
+                const float2 kv = __ldg(surp + w0);
+                kS = kv.x; IS = kv.y; I0 = kv.y;
+                tauE = 1.0f;
+                salive = true;
             }
 
             // warp-uniform DDA set-up (origin at the cell centre)
@@ -400,13 +409,24 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                     tau = tau - ta;
                     if (tau < P.toll) { D = fmaf(tau, gj, D); tau = 0.0f; }
                 }
-                if (CV && taus > 0.0f) {
-                    const float2 kv = __ldg(surp + cw);
-                    const float as = -mc_expm1(-(kv.x * ds));
-                    const float tas = taus * as;
-                    Jbar = fmaf(tas, kv.y, Jbar);
-                    taus = taus - tas;
-                    if (taus < P.toll) { Jbar = fmaf(taus, kv.y, Jbar); taus = 0.0f; }
+                if (CV && salive) {
+                    const float opt = kS * (tn - tE);
+                    if (dcumE + opt > P.dtoll) {          // truncated inside this layer
+                        Jbar = fmaf(tauE, IS, Jbar);
+                        salive = false;
+                    } else if (axis == 0) {               // leaves the layer at tn
+                        const float as = -mc_expm1(-opt);
+                        const float tas = tauE * as;
+                        Jbar = fmaf(tas, IS, Jbar);
+                        tauE = tauE - tas;
+                        dcumE = dcumE + opt;
+                        tE = tn;
+                        if (tex0 < 0.0f) tex0 = tauE;     // transmissivity leaving the own layer
+                        if (!wall) {
+                            const float2 kv = __ldg(surp + ncw);
+                            kS = kv.x; IS = kv.y;
+                        }
+                    }
                 }
                 if (TRACE && lane == 0 && steps < P.trace_max) {
                     int *rec = P.trace_rec + 6 * steps;
@@ -415,7 +435,6 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 }
                 t = tn;
                 ++steps;
-                if (CV && axis == 0 && tex0 < 0.0f) tex0 = taus;  // surrogate leaves the own layer
                 if (axis == 0) {
                     if (wall) {
                         const int side = ncw < 0 ? 0 : 1;
@@ -424,9 +443,9 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                             D = fmaf(tau, (Ii - Iw) * invI, D);
                             tau = 0.0f;
                         }
-                        if (CV && taus > 0.0f) {
-                            Jbar = fmaf(taus, Iw, Jbar);
-                            taus = 0.0f;
+                        if (CV && salive) {
+                            Jbar = fmaf(tauE, Iw, Jbar);
+                            salive = false;
                         }
                         break;
                     }
@@ -444,9 +463,9 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                     rowB = nrowB;
                 }
                 vcur = vnext;
-                if (!__any_sync(FULL, tau > 0.0f || (CV && taus > 0.0f))) break;
+                if (!__any_sync(FULL, tau > 0.0f || (CV && salive))) break;
                 if (steps >= P.max_steps) {
-                    if (tau > 0.0f || (CV && taus > 0.0f)) flags |= DNSMC_STATUS_STEP_CAP;
+                    if (tau > 0.0f || (CV && salive)) flags |= DNSMC_STATUS_STEP_CAP;
                     break;
                 }
             }
@@ -455,9 +474,8 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             if (CV) {
                 // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
                 const float te = tex0 < 0.0f ? 0.0f : tex0;
-                const float Iw0 = __ldg(&surp[w0].y);
                 const float Ya = wk * (Ii - Jbar);
-                const float Yb = wk * ((1.0f - te) * (Ii - Iw0));
+                const float Yb = wk * ((1.0f - te) * (Ii - I0));
                 if (MOM && active) {
                     const double xd = X, ya = Ya, yb = Yb;
                     mo[0] += xd; mo[1] += ya; mo[2] += yb;
@@ -838,16 +856,18 @@ __global__ void cv_jhat_kernel(const CvParams c) {
             const float Iw = c.mode == MODE_GREY ? c.Tw4[h] : __ldg(c.ibw + h * c.nbands + band);
             for (int q = 0; q < c_nquad; ++q) {
                 const float inv_mu = (float)(1.0 / c_quad_mu[q]);
-                float tau = 1.0f, J = 0.0f, t0 = 0.0f;
+                float tau = 1.0f, J = 0.0f, t0 = 0.0f, dcum = 0.0f;
                 int l = w;
                 float seg = dir > 0 ? (__ldg(c.fw + w + 1) - oW) : (oW - __ldg(c.fw + w));
                 for (;;) {
                     const float2 kv = sp[l];
-                    const float a = -expm1f(-(kv.x * seg * inv_mu));
+                    const float opt = kv.x * seg * inv_mu;
+                    if (dcum + opt > c.dtoll) { J = fmaf(tau, kv.y, J); break; }  // truncated in layer l
+                    const float a = -expm1f(-opt);
                     const float ta = tau * a;
                     J = fmaf(ta, kv.y, J);
                     tau = tau - ta;
-                    if (tau < c.toll) { J = fmaf(tau, kv.y, J); tau = 0.0f; break; }
+                    dcum = dcum + opt;
                     if (l == w) t0 = tau;  // transmissivity leaving the own layer
                     l += dir;
                     if (l < 0 || l >= c.nw) { J = fmaf(tau, Iw, J); break; }

@@ -15,6 +15,7 @@
 // mc_kernels.cu); only the location of their scratch differs.
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdio>
 #include <mutex>
 
@@ -141,6 +142,7 @@ extern "C" int dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu
     P.sampler = DNSMC_SAMPLER_IID;
     P.nbatch = c.nvar;
     P.toll = c.toll;
+    P.dtoll = (float)(-log((double)c.toll));
     P.max_steps = c.max_steps;
     P.queue = misc;
     P.status = misc + 1;

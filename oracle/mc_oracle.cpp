@@ -778,10 +778,15 @@ struct Packet {
                 tau[l] = act[l] ? (R)1 : (R)0;
                 D[l] = 0;
             }
-            R taus = c.cv ? (R)1 : (R)0, Jbar = 0, tau_exit0 = -1;
+            // surrogate: advanced once per wall-normal layer (constant k, Ib),
+            // stopped when its optical depth exceeds ln(1/toll)
             const int sid = c.mode != 0 ? koff / (c.nT * c.nX) : 0;
             const int nsamp = c.mode != 0 ? c.nbands * c.nq : 1;
             const size_t sbase = ((size_t)f * nsamp + sid) * c.nw;
+            const R dtoll = (R)(float)(-std::log((double)c.toll));
+            bool salive = c.cv != 0;
+            R Jbar = 0, tau_exit0 = -1, tauE = 1, tE = 0, dcumE = 0;
+            R kS = salive ? (R)c.sur_k[sbase + w0] : (R)0, IS = salive ? (R)c.sur_I[sbase + w0] : (R)0;
             const R invW = (R)1 / std::fabs(sW), invA = (R)1 / std::fabs(sA), invB = (R)1 / std::fabs(sB);
             const int dW = sW > 0 ? 1 : -1, dA = sA > 0 ? 1 : -1, dB = sB > 0 ? 1 : -1;
             R tW = (dW > 0 ? ((R)c.fw[w0 + 1] - oW) : (oW - (R)c.fw[w0])) * invW;
@@ -822,13 +827,22 @@ struct Packet {
                     tau[l] = tau[l] - tal;
                     if (tau[l] < (R)c.toll) { D[l] = FMA<R>(tau[l], gj, D[l]); tau[l] = 0; }
                 }
-                if (taus > 0) {  // surrogate: same segment through the layer-mean medium
-                    const R ks = (R)c.sur_k[sbase + cw], Is = (R)c.sur_I[sbase + cw];
-                    const R a = -expm1n(-(ks * ds));
-                    const R ta = taus * a;
-                    Jbar = FMA<R>(ta, Is, Jbar);
-                    taus = taus - ta;
-                    if (taus < (R)c.toll) { Jbar = FMA<R>(taus, Is, Jbar); taus = 0; }
+                const bool wall = axis == 0 && (cw + dW < 0 || cw + dW >= c.nw);
+                if (salive) {
+                    const R opt = kS * (tn - tE);
+                    if (dcumE + opt > dtoll) {
+                        Jbar = FMA<R>(tauE, IS, Jbar);
+                        salive = false;
+                    } else if (axis == 0) {
+                        const R a = -expm1n(-opt);
+                        const R ta = tauE * a;
+                        Jbar = FMA<R>(ta, IS, Jbar);
+                        tauE = tauE - ta;
+                        dcumE = dcumE + opt;
+                        tE = tn;
+                        if (tau_exit0 < 0) tau_exit0 = tauE;
+                        if (!wall) { kS = (R)c.sur_k[sbase + cw + dW]; IS = (R)c.sur_I[sbase + cw + dW]; }
+                    }
                 }
                 if (rec && stepn < tmax) {
                     int32_t *q = rec + 6 * stepn;
@@ -839,15 +853,14 @@ struct Packet {
                 }
                 t = tn;
                 ++stepn;
-                if (axis == 0 && tau_exit0 < 0) tau_exit0 = taus;  // surrogate transmissivity leaving the own layer
                 if (axis == 0) {
                     cw += dW;
                     if (cw < 0 || cw >= c.nw) {
                         const int side = cw < 0 ? 0 : 1;
-                        if (taus > 0) {
+                        if (salive) {
                             const R Iws = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
-                            Jbar = FMA<R>(taus, Iws, Jbar);
-                            taus = 0;
+                            Jbar = FMA<R>(tauE, Iws, Jbar);
+                            salive = false;
                         }
                         for (int l = 0; l < 32; ++l) {
                             if (!(tau[l] > 0)) continue;
@@ -867,7 +880,7 @@ struct Packet {
                     tB = ((R)nB + (R)0.5) * dtB;
                     for (int l = 0; l < 32; ++l) { cb[l] += dB; if (cb[l] == c.nb) cb[l] = 0; else if (cb[l] < 0) cb[l] = c.nb - 1; }
                 }
-                bool any = taus > 0;
+                bool any = salive;
                 for (int l = 0; l < 32; ++l) any = any || (tau[l] > 0);
                 if (!any) break;
                 if (stepn >= c.max_steps) break;

@@ -239,8 +239,9 @@ def cv_quadrature():
 
 def cv_jhat(sur_k, sur_I, fw, toll, Iw_west, Iw_east):
     """For every layer l of a 1-D layered medium (k, Ib per layer; black walls
-    with intensities Iw), rays leaving the layer centre truncated at
-    transmissivity toll like the march, in float64:
+    with intensities Iw), rays leaving the layer centre and stopped once their
+    optical depth exceeds ln(1/toll) (the surrogate walk of the march), in
+    float64:
     Jhat[l] = 1/2 int_{-1}^{1} J(mu; l) dmu (absorbed intensity) and
     Ahat[l] = 1/2 int_{-1}^{1} (1 - t0(mu; l)) dmu (own-layer absorptance).
     Returns an (nw, 2) array."""
@@ -248,20 +249,23 @@ def cv_jhat(sur_k, sur_I, fw, toll, Iw_west, Iw_east):
     mu, wt = cv_quadrature()
     fw = np.asarray(fw, np.float64)
     o = 0.5 * (fw[:-1] + fw[1:])
+    dtoll = -math.log(toll)
     out = np.zeros((nw, 2))
     for l in range(nw):
         acc = accA = 0.0
         for d, Iw in ((-1, Iw_west), (1, Iw_east)):
             for m, wq in zip(mu, wt):
-                tau, J, i, t0 = 1.0, 0.0, l, 0.0
+                tau, J, i, t0, dcum = 1.0, 0.0, l, 0.0, 0.0
                 seg = (fw[l + 1] - o[l]) if d > 0 else (o[l] - fw[l])
                 while True:
-                    a = -math.expm1(-float(sur_k[i]) * seg / m)
-                    J += tau * a * float(sur_I[i])
-                    tau -= tau * a
-                    if tau < toll:
+                    opt = float(sur_k[i]) * seg / m
+                    if dcum + opt > dtoll:  # optical depth beyond ln(1/toll): the rest stays in layer i
                         J += tau * float(sur_I[i])
                         break
+                    a = -math.expm1(-opt)
+                    J += tau * a * float(sur_I[i])
+                    tau -= tau * a
+                    dcum += opt
                     if i == l:
                         t0 = tau
                     i += d
