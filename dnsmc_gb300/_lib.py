@@ -53,6 +53,19 @@ class TableDesc(ctypes.Structure):
     ]
 
 
+class CvNetConfig(ctypes.Structure):
+    """Mirror of dnsmc_cvnet_config."""
+    _fields_ = [
+        ("n_groups", ctypes.c_int), ("T_center", ctypes.c_float), ("T_scale", ctypes.c_float),
+        ("x_center", ctypes.c_float), ("x_scale", ctypes.c_float), ("lr", ctypes.c_float),
+        ("adam_beta1", ctypes.c_float), ("adam_beta2", ctypes.c_float), ("adam_eps", ctypes.c_float),
+        ("ridge", ctypes.c_float), ("batch", ctypes.c_int), ("seed", ctypes.c_uint64),
+    ]
+
+
+CVNET_NFEAT, CVNET_NOUT, CVNET_NLABEL = 67, 32, 8
+CVNET_BETA, CVNET_RAYS = 1, 2
+
 # name -> (restype, argtypes); every symbol include/dnsmc.h declares
 SIGNATURES = {
     "dnsmc_set_default_config": (None, [ctypes.POINTER(Config)]),
@@ -75,6 +88,28 @@ SIGNATURES = {
     "dnsmc_set_region": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_int] * 6),
     "dnsmc_set_rays": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_int_p]),
     "dnsmc_packet_count": (ctypes.c_int, [ctypes.c_void_p, c_int_p]),
+    "dnsmc_set_rays_per_item": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_int_p]),
+    "dnsmc_get_item_steps": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
+    "dnsmc_get_rays_per_item": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p]),
+    "dnsmc_get_cv_beta": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
+    "dnsmc_cvnet_default_config": (None, [ctypes.POINTER(CvNetConfig)]),
+    "dnsmc_cvnet_create": (ctypes.c_int, [ctypes.POINTER(CvNetConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    "dnsmc_cvnet_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "dnsmc_cvnet_param_count": (ctypes.c_longlong, []),
+    "dnsmc_cvnet_get_params": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p]),
+    "dnsmc_cvnet_set_params": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p]),
+    "dnsmc_cvnet_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "dnsmc_cvnet_load": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "dnsmc_cvnet_features": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_float_p]),
+    "dnsmc_cvnet_add_training_data": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "dnsmc_cvnet_clear_training_data": (ctypes.c_int, [ctypes.c_void_p]),
+    "dnsmc_cvnet_training_rows": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "dnsmc_cvnet_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_double_p]),
+    "dnsmc_cvnet_eval": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_longlong, c_float_p]),
+    "dnsmc_cvnet_gradient": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p, ctypes.c_int, ctypes.c_longlong,
+                                            c_float_p, c_double_p]),
+    "dnsmc_cvnet_apply": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_int]),
     "dnsmc_solve_async": (ctypes.c_int, [ctypes.c_void_p]),
     "dnsmc_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "dnsmc_get_results": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),

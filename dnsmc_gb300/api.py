@@ -71,6 +71,7 @@ class Solver:
         self._nfields = 0
         self._keep = []
         self._rays = cfg.nvar * cfg.photmax
+        self._rays_dev = False
         self._beta = None
 
     # -- lifetime -----------------------------------------------------------
@@ -156,6 +157,8 @@ class Solver:
     def set_region(self, i0, i1, j0, j1, k0, k1) -> None:
         check(self._lib.dnsmc_set_region(self._h, i0, i1, j0, j1, k0, k1))
         self._region = (i0, i1, j0, j1, k0, k1)
+        self._keep = []
+        self._rays_dev = False
 
     def packet_count(self) -> int:
         n = ctypes.c_int()
@@ -174,6 +177,42 @@ class Solver:
         check(self._lib.dnsmc_set_rays(self._h, int(rays_per_group),
                                        None if rp is None else rp.ctypes.data_as(_lib.c_int_p)))
         self._rays = int(rays_per_group)
+        self._rays_dev = False
+
+    def set_rays_per_item(self, rays) -> None:
+        """Ray counts per (band group, packet): int array (n_groups, npackets)."""
+        rp = np.ascontiguousarray(rays, dtype=np.int32)
+        if rp.ndim != 2 or rp.shape[1] != self.packet_count():
+            raise ValueError("rays needs shape (n_groups, npackets)")
+        check(self._lib.dnsmc_set_rays_per_item(self._h, rp.shape[0], rp.ctypes.data_as(_lib.c_int_p)))
+        self._keep = [rp]
+        self._rays_dev = False
+
+    def cv_beta(self):
+        """Coefficients in effect: (nfields, n_groups, nk, nj, ni, 2) float32."""
+        ng = self.sampling()["n_groups"] if self.cfg.model != _lib.MODEL_GREY else 1
+        shp = self._region_shape()
+        out = np.zeros((shp[0], ng) + shp[1:] + (2,), np.float32)
+        check(self._lib.dnsmc_get_cv_beta(self._h, _fp(out)))
+        return out
+
+    def rays_per_item(self):
+        """The per-(group, packet) ray table in effect (set here or by a
+        network), or None for uniform / per-packet rays."""
+        ng = ctypes.c_int()
+        check(self._lib.dnsmc_get_rays_per_item(self._h, ctypes.byref(ng), None))
+        if ng.value == 0:
+            return None
+        out = np.zeros((ng.value, self.packet_count()), np.int32)
+        check(self._lib.dnsmc_get_rays_per_item(self._h, ctypes.byref(ng), out.ctypes.data_as(_lib.c_int_p)))
+        return out
+
+    def item_steps(self):
+        """Ray-voxel steps of the last solve per (field, group, packet), summed over rays."""
+        ng = self.sampling()["n_groups"]
+        out = np.zeros((self._nfields, ng, self.packet_count()), np.float64)
+        check(self._lib.dnsmc_get_item_steps(self._h, _dp(out)))
+        return out
 
     # -- solve --------------------------------------------------------------
     def solve_async(self) -> None:
@@ -257,6 +296,7 @@ class Solver:
     def set_cv_beta(self, beta) -> None:
         """Control-variate coefficient pairs (nfields, n_groups, nk, nj, ni, 2)
         = (beta_a, beta_b), or None for (1, -1)."""
+        self._beta_dev = False
         if beta is None:
             check(self._lib.dnsmc_set_cv_beta(self._h, None))
             self._beta = None
@@ -333,3 +373,138 @@ def get_results(Qr: np.ndarray, Vr: np.ndarray) -> None:
         if a.dtype != np.float32 or not a.flags.c_contiguous:
             raise TypeError("outputs must be C-contiguous float32 arrays")
     lib.get_results_(_fp(Qr), _fp(Vr))
+
+
+# ---------------------------------------------------------------------------
+# learned control variate
+# ---------------------------------------------------------------------------
+def cvnet_default_config(**overrides) -> _lib.CvNetConfig:
+    lib = _lib.load()
+    c = _lib.CvNetConfig()
+    lib.dnsmc_cvnet_default_config(ctypes.byref(c))
+    for k, v in overrides.items():
+        if not hasattr(c, k):
+            raise KeyError(f"unknown network config field {k!r}")
+        setattr(c, k, v)
+    return c
+
+
+class CvNet:
+    """The control-variate network of include/dnsmc.h (dnsmc_cvnet_*): features
+    -> per (cell, band group) coefficient pair, log variance and log cost."""
+
+    NFEAT, NOUT, NLABEL = _lib.CVNET_NFEAT, _lib.CVNET_NOUT, _lib.CVNET_NLABEL
+
+    def __init__(self, config: _lib.CvNetConfig | None = None, *, _handle=None, **overrides):
+        self._lib = _lib.load()
+        if _handle is not None:
+            self._h = _handle
+            return
+        cfg = config if config is not None else cvnet_default_config()
+        for k, v in overrides.items():
+            setattr(cfg, k, v)
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        check(self._lib.dnsmc_cvnet_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+
+    @classmethod
+    def load(cls, path: str) -> "CvNet":
+        lib = _lib.load()
+        h = ctypes.c_void_p()
+        check(lib.dnsmc_cvnet_load(path.encode(), ctypes.byref(h)))
+        return cls(_handle=h)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._lib.dnsmc_cvnet_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @staticmethod
+    def param_count() -> int:
+        return int(_lib.load().dnsmc_cvnet_param_count())
+
+    def params(self):
+        """(params float32 [P], scales float32 [3] = S_beta, S_v, S_c)."""
+        p = np.zeros(self.param_count(), np.float32)
+        s = np.zeros(3, np.float32)
+        check(self._lib.dnsmc_cvnet_get_params(self._h, _fp(p), _fp(s)))
+        return p, s
+
+    def set_params(self, params=None, scales=None) -> None:
+        p = None if params is None else np.ascontiguousarray(params, np.float32)
+        s = None if scales is None else np.ascontiguousarray(scales, np.float32)
+        if p is not None and p.size != self.param_count():
+            raise ValueError("wrong parameter count")
+        check(self._lib.dnsmc_cvnet_set_params(self._h, _fp(p), _fp(s)))
+
+    def save(self, path: str) -> None:
+        check(self._lib.dnsmc_cvnet_save(self._h, path.encode()))
+
+    def features(self, solver: "Solver"):
+        """[rows][67] features of the solver's region (tally order: field, i, k, j)."""
+        i0, i1, j0, j1, k0, k1 = solver._region
+        rows = solver._nfields * (i1 - i0) * (j1 - j0) * (k1 - k0)
+        out = np.zeros((rows, self.NFEAT), np.float32)
+        check(self._lib.dnsmc_cvnet_features(self._h, solver._h, _fp(out)))
+        return out
+
+    def add_training_data(self, solver: "Solver") -> None:
+        check(self._lib.dnsmc_cvnet_add_training_data(self._h, solver._h))
+
+    def clear_training_data(self) -> None:
+        check(self._lib.dnsmc_cvnet_clear_training_data(self._h))
+
+    def training_rows(self) -> int:
+        return int(self._lib.dnsmc_cvnet_training_rows(self._h))
+
+    def train(self, epochs: int = 1):
+        """Mean losses of the last pass: (total, beta, variance, cost)."""
+        l = np.zeros(4, np.float64)
+        check(self._lib.dnsmc_cvnet_train(self._h, int(epochs), _dp(l)))
+        return tuple(float(v) for v in l)
+
+    def eval(self, features):
+        x = np.ascontiguousarray(features, np.float32).reshape(-1, self.NFEAT)
+        out = np.zeros((x.shape[0], self.NOUT), np.float32)
+        check(self._lib.dnsmc_cvnet_eval(self._h, _fp(x), x.shape[0], _fp(out)))
+        return out
+
+    def gradient(self, features, labels):
+        """(grad [P], losses (total, beta, variance, cost)) of one forward and
+        backward pass on host features [rows][67] and labels [rows][G][8]."""
+        x = np.ascontiguousarray(features, np.float32).reshape(-1, self.NFEAT)
+        y = np.ascontiguousarray(labels, np.float32)
+        G = y.shape[1]
+        g = np.zeros(self.param_count(), np.float32)
+        l = np.zeros(4, np.float64)
+        check(self._lib.dnsmc_cvnet_gradient(self._h, _fp(x), _fp(y), G, x.shape[0], _fp(g), _dp(l)))
+        return g, tuple(float(v) for v in l)
+
+    def apply(self, solver: "Solver", beta: bool = True, rays: bool = True, mean_rays: int = 64,
+              min_rays: int = 8, max_rays: int = 4096) -> None:
+        flags = (_lib.CVNET_BETA if beta else 0) | (_lib.CVNET_RAYS if rays else 0)
+        check(self._lib.dnsmc_cvnet_apply(self._h, solver._h, flags, int(mean_rays), int(min_rays),
+                                          int(max_rays)))
+        if rays:
+            solver._keep = []
+            solver._rays_dev = True
+        if beta:
+            solver._beta_dev = True
+
+
+def solver_rays_per_item(solver: "Solver"):
+    """The per-(group, packet) ray table in effect, or None."""
+    return solver.rays_per_item()

@@ -2,9 +2,10 @@
 
     python -m dnsmc_gb300.build        # or dnsmc_gb300.build.build()
 
-Compiles the CUDA translation unit with nvcc for sm_103a (-fmad=false: the
-march is written with explicit fmaf so the host replay can reproduce it bit
-for bit) and the host runtime with the same nvcc driver, in parallel, then
+Compiles the CUDA translation units with nvcc for sm_103a (the march with
+-fmad=false: it is written with explicit fmaf so the host replay can
+reproduce it bit for bit; the allocation-free solve; the control-variate
+network) and the host runtime with the same nvcc driver, in parallel, then
 links one shared library with the static CUDA runtime.
 """
 from __future__ import annotations
@@ -58,6 +59,8 @@ def build(verbose: bool = False) -> str:
          "-o", os.path.join(bdir, "mc_host.o")],
         [nvcc, *ARCH, *common, "-c", os.path.join(CSRC, "mc_noalloc.cu"),
          "-o", os.path.join(bdir, "mc_noalloc.o")],
+        [nvcc, *ARCH, *common, "-c", os.path.join(CSRC, "mc_cvnet.cu"),
+         "-o", os.path.join(bdir, "mc_cvnet.o")],
     ]
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(_run, jobs))
@@ -65,7 +68,7 @@ def build(verbose: bool = False) -> str:
     tmp = out + ".tmp"
     _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-Xcompiler", "-fPIC",
           os.path.join(bdir, "mc_kernels.o"), os.path.join(bdir, "mc_host.o"),
-          os.path.join(bdir, "mc_noalloc.o"), "-o", tmp])
+          os.path.join(bdir, "mc_noalloc.o"), os.path.join(bdir, "mc_cvnet.o"), "-o", tmp])
     os.replace(tmp, out)
     if verbose:
         print("built", out)

@@ -269,8 +269,11 @@ struct dnsmc_solver {
     // region and rays
     int r_i0 = 0, r_i1 = 0, r_j0 = 0, r_j1 = 0, r_k0 = 0, r_k1 = 0;
     int rays = 0;
-    std::vector<int> rays_pp;
+    std::vector<int> rays_pp;                // [group][packet] when rays_pg > 0, else [packet]
+    int rays_pg = 0;                         // band groups of a per-item ray table (0: per packet)
+    bool rays_dev = false;                   // d_rays_pp was written on the device (no host copy)
     DevBuf<int> d_rays_pp;
+    DevBuf<unsigned long long> d_item_steps; // steps per (field, group, packet) of the last solve
 
     // sampling of the last solve
     float tmax_used = 0.f;
@@ -834,7 +837,9 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.Tw4[0] = c.T_west * c.T_west * c.T_west * c.T_west;
     P.Tw4[1] = c.T_east * c.T_east * c.T_east * c.T_east;
     P.rays = s->rays;
-    P.rays_per_packet = s->rays_pp.empty() ? nullptr : s->d_rays_pp.p;
+    const bool per_item = !s->rays_pp.empty() || s->rays_dev;
+    P.rays_per_packet = per_item ? s->d_rays_pp.p : nullptr;
+    P.rays_gstride = 0;
     P.key0 = (uint32_t)(c.seed & 0xffffffffu);
     P.key1 = (uint32_t)(c.seed >> 32);
     P.field_base = 0;
@@ -843,6 +848,12 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.max_steps = c.max_steps;
     P.region_cells = (long long)ni * nj * nk;
     P.n_items = (long long)s->nfields * P.n_groups * P.n_packets;
+    if (per_item && s->rays_pg > 0) {
+        if (s->rays_pg != P.n_groups)
+            return fail(DNSMC_ERR_STATE, "per-item ray table has %d band groups, the solve has %d", s->rays_pg,
+                         P.n_groups);
+        P.rays_gstride = P.n_packets;
+    }
     if (mode != MODE_GREY && !trace) {
         // table coordinates of the field for this table (once per solve)
         const long long ncell = (long long)s->nfields * P.field_stride;
@@ -929,6 +940,8 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     }
     TRY(s->d_tally.ensure((size_t)s->nfields * P.n_groups * P.region_cells));
     P.tally = s->d_tally.p;
+    TRY(s->d_item_steps.ensure((size_t)P.n_items));
+    P.item_steps = s->d_item_steps.p;
     CUDA_TRY(cudaMemsetAsync(s->d_misc.p, 0, 4 * sizeof(unsigned int), s->stream));
     CUDA_TRY(cudaMemsetAsync(s->d_counters.p, 0, 2 * sizeof(unsigned long long), s->stream));
     const int sms = device_sm_count();
@@ -945,7 +958,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     F.nfields = s->nfields; F.n_groups = P.n_groups; F.region_cells = P.region_cells;
     F.niR = ni; F.njR = nj; F.nkR = nk;
     F.tile_a = ta; F.tile_b = tb; F.npa = npa; F.npb = npb;
-    F.rays = s->rays; F.rays_per_packet = P.rays_per_packet;
+    F.rays = s->rays; F.rays_per_packet = P.rays_per_packet; F.rays_gstride = P.rays_gstride;
     F.batched = c.sampler == DNSMC_SAMPLER_RQMC;
     F.nbatch = c.nvar;
     F.group_empty = s->d_group_empty.p;
@@ -1070,6 +1083,71 @@ bool g_dropin_cfg_set = false;
 namespace dnsmc {
 // Error reporting for the other translation units of the library.
 int report_error(int code, const char *msg) { return fail(code, "%s", msg); }
+
+int solver_view(dnsmc_solver *s, SolverView *v) {
+    if (!s || !v) return fail(DNSMC_ERR_ARG, "null argument");
+    if (s->nfields < 1) return fail(DNSMC_ERR_STATE, "no fields: call dnsmc_set_fields first");
+    TRY(set_device(s));
+    const dnsmc_config &c = s->cfg;
+    SolverView w{};
+    w.device = s->device;
+    w.stream = s->stream;
+    w.model = c.model;
+    w.mode = c.model == DNSMC_MODEL_GREY ? MODE_GREY : (s->tab.nX > 1 ? MODE_TX : MODE_T);
+    w.imax = c.imax; w.jmax = c.jmax; w.kmax = c.kmax; w.nfields = s->nfields;
+    w.n_groups = c.model == DNSMC_MODEL_GREY ? 1 : std::min(c.n_groups, std::max(1, s->tab.nbands));
+    w.nvar = c.nvar; w.sampler = c.sampler;
+    w.i0 = s->r_i0; w.i1 = s->r_i1; w.j0 = s->r_j0; w.j1 = s->r_j1; w.k0 = s->r_k0; w.k1 = s->r_k1;
+    tiling(s, &w.tile_a, &w.tile_b, &w.npa, &w.npb, &w.npw);
+    w.n_packets = w.npa * w.npb * w.npw;
+    w.region_cells = (long long)(w.i1 - w.i0) * (w.j1 - w.j0) * (w.k1 - w.k0);
+    w.field_stride = (long long)c.imax * c.jmax * c.kmax;
+    w.fieldT = s->d_fieldT.p;
+    w.fieldTX = s->d_fieldTX.p;
+    w.fw = s->d_fw.p;
+    if (c.model != DNSMC_MODEL_GREY) {
+        w.T_lo = s->tab.T0; w.T_hi = s->tab.T0 + (s->tab.nT - 1) * s->tab.dT;
+        w.X_lo = s->tab.X0; w.X_hi = s->tab.X0 + (s->tab.nX - 1) * s->tab.dX;
+    }
+    w.solved = s->solved ? 1 : 0;
+    if (s->solved) {
+        w.last_groups = s->last.n_groups;
+        w.moments = (c.control_variate && c.cv_moments) ? s->d_moments.p : nullptr;
+        w.varg = s->d_varg.p;
+        w.item_steps = s->d_item_steps.p;
+        w.rays = s->last.rays;
+        w.rays_item = s->last.rays_per_packet;
+        w.rays_gstride = s->last.rays_gstride;
+    }
+    *v = w;
+    return DNSMC_OK;
+}
+
+int solver_beta_device(dnsmc_solver *s, float2 **beta, long long *n) {
+    SolverView v;
+    TRY(solver_view(s, &v));
+    TRY(wait_done(s, 0));
+    const long long m = (long long)v.nfields * v.n_groups * v.region_cells;
+    TRY(s->d_beta.ensure((size_t)m));
+    s->beta_set = true;
+    *beta = s->d_beta.p;
+    *n = m;
+    return DNSMC_OK;
+}
+
+int solver_rays_device(dnsmc_solver *s, int n_groups, int **rays) {
+    if (n_groups < 1) return fail(DNSMC_ERR_ARG, "n_groups must be >= 1");
+    TRY(set_device(s));
+    TRY(wait_done(s, 0));
+    int np;
+    TRY(dnsmc_packet_count(s, &np));
+    TRY(s->d_rays_pp.ensure((size_t)n_groups * np));
+    s->rays_pp.clear();
+    s->rays_pg = n_groups;
+    s->rays_dev = true;
+    *rays = s->d_rays_pp.p;
+    return DNSMC_OK;
+}
 }  // namespace dnsmc
 
 // ===========================================================================
@@ -1165,7 +1243,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_cv_grp.release(); s->d_cv_sid.release(); s->d_cv_C.release(); s->d_layer.release();
     s->d_sur.release(); s->d_Jhat.release(); s->d_muY.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();
-    s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release();
+    s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_item_steps.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
     s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_Qg.release(); s->d_varg.release();
     s->h_Q.release(); s->h_var.release(); s->d_misc.release(); s->d_counters.release();
@@ -1323,6 +1401,8 @@ int dnsmc_set_region(dnsmc_solver *s, int i0, int i1, int j0, int j1, int k0, in
     TRY(wait_done(s, 0));
     s->r_i0 = i0; s->r_i1 = i1; s->r_j0 = j0; s->r_j1 = j1; s->r_k0 = k0; s->r_k1 = k1;
     s->rays_pp.clear();
+    s->rays_pg = 0;
+    s->rays_dev = false;
     return DNSMC_OK;
 }
 
@@ -1356,6 +1436,51 @@ int dnsmc_set_rays(dnsmc_solver *s, int rays_per_group, const int *rays_per_pack
     } else {
         s->rays_pp.clear();
     }
+    s->rays_pg = 0;
+    s->rays_dev = false;
+    return DNSMC_OK;
+}
+
+int dnsmc_set_rays_per_item(dnsmc_solver *s, int n_groups, const int *rays) {
+    if (!s || !rays) return fail(DNSMC_ERR_ARG, "null argument");
+    if (n_groups < 1) return fail(DNSMC_ERR_ARG, "n_groups must be >= 1");
+    const int B = s->cfg.sampler == DNSMC_SAMPLER_RQMC ? s->cfg.nvar : 1;
+    int np;
+    TRY(dnsmc_packet_count(s, &np));
+    const size_t n = (size_t)n_groups * np;
+    for (size_t i = 0; i < n; ++i) {
+        if (rays[i] < 0) return fail(DNSMC_ERR_ARG, "negative ray count");
+        if (rays[i] % B) return fail(DNSMC_ERR_ARG, "RQMC: per-item rays must be multiples of nvar");
+    }
+    TRY(set_device(s));
+    TRY(wait_done(s, 0));
+    s->rays_pp.assign(rays, rays + n);
+    s->rays_pg = n_groups;
+    s->rays_dev = false;
+    TRY(s->d_rays_pp.ensure(n));
+    CUDA_TRY(cudaMemcpy(s->d_rays_pp.p, s->rays_pp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    return DNSMC_OK;
+}
+
+int dnsmc_get_rays_per_item(dnsmc_solver *s, int *n_groups, int *rays) {
+    if (!s || !n_groups) return fail(DNSMC_ERR_ARG, "null argument");
+    TRY(wait_done(s, 0));
+    *n_groups = (s->rays_pp.empty() && !s->rays_dev) ? 0 : s->rays_pg;
+    if (!rays || *n_groups == 0) return DNSMC_OK;
+    int np;
+    TRY(dnsmc_packet_count(s, &np));
+    CUDA_TRY(cudaMemcpy(rays, s->d_rays_pp.p, (size_t)*n_groups * np * sizeof(int), cudaMemcpyDeviceToHost));
+    return DNSMC_OK;
+}
+
+int dnsmc_get_item_steps(dnsmc_solver *s, double *steps) {
+    if (!s || !steps) return fail(DNSMC_ERR_ARG, "null argument");
+    TRY(wait_done(s, 0));
+    const long long n = s->last.n_items;
+    if (n <= 0 || !s->d_item_steps.p) return fail(DNSMC_ERR_STATE, "no solve yet");
+    std::vector<unsigned long long> h((size_t)n);
+    CUDA_TRY(cudaMemcpy(h.data(), s->d_item_steps.p, (size_t)n * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < n; ++i) steps[i] = (double)h[(size_t)i];
     return DNSMC_OK;
 }
 
@@ -1466,6 +1591,31 @@ int dnsmc_set_cv_beta(dnsmc_solver *s, const float *beta) {
     TRY(s->d_beta.ensure(tl.size()));
     CUDA_TRY(cudaMemcpy(s->d_beta.p, tl.data(), tl.size() * sizeof(float2), cudaMemcpyHostToDevice));
     s->beta_set = true;
+    return DNSMC_OK;
+}
+
+int dnsmc_get_cv_beta(dnsmc_solver *s, float *beta) {
+    if (!s || !beta) return fail(DNSMC_ERR_ARG, "null argument");
+    TRY(wait_done(s, 0));
+    if (!s->beta_set) return fail(DNSMC_ERR_STATE, "no coefficients set: (1, -1) everywhere");
+    int ni, nj, nk;
+    region_dims(s, &ni, &nj, &nk);
+    const long long rc_ = (long long)ni * nj * nk;
+    const int nG = s->cfg.model == DNSMC_MODEL_GREY ? 1 : std::min(s->cfg.n_groups, std::max(1, s->tab.nbands));
+    const size_t n = (size_t)s->nfields * nG * rc_;
+    if (s->d_beta.n < n) return fail(DNSMC_ERR_STATE, "coefficients were set for another region");
+    std::vector<float2> tl(n);
+    TRY(set_device(s));
+    CUDA_TRY(cudaMemcpy(tl.data(), s->d_beta.p, n * sizeof(float2), cudaMemcpyDeviceToHost));
+    for (long long fg = 0; fg < (long long)s->nfields * nG; ++fg)
+        for (int i = 0; i < ni; ++i)
+            for (int k = 0; k < nk; ++k)
+                for (int j = 0; j < nj; ++j) {
+                    const float2 v = tl[fg * rc_ + ((long long)i * nk + k) * nj + j];
+                    float *b = beta + 2 * (fg * rc_ + i + (long long)ni * (j + (long long)nj * k));
+                    b[0] = v.x;
+                    b[1] = v.y;
+                }
     return DNSMC_OK;
 }
 

@@ -13,6 +13,8 @@
 #pragma once
 #include <cstdint>
 
+#include "../../include/dnsmc.h"
+
 namespace dnsmc {
 
 enum MarchMode { MODE_GREY = 0, MODE_T = 1, MODE_TX = 2 };
@@ -56,7 +58,9 @@ struct MarchParams {
     float Tw4[2];             // wall T^4 (west, east), grey model
     // rays
     int rays;                 // rays per (cell, group) when rays_per_packet == 0
-    const int *rays_per_packet;
+    const int *rays_per_packet;  // [G * rays_gstride + packet]
+    int rays_gstride;         // 0: one count per packet for all groups; n_packets: per (group, packet)
+    unsigned long long *item_steps;  // per item: ray-voxel steps summed over its rays, or null
     uint32_t key0, key1;      // Philox key (seed)
     int sampler;              // 0 iid Philox, 1 RQMC (shifted Sobol' net)
     int nbatch;               // RQMC replicates per item (rays divisible by it)
@@ -89,7 +93,8 @@ struct FinalizeParams {
     int niR, njR, nkR;        // region extents (i, j, k)
     int tile_a, tile_b, npa, npb;
     int rays;
-    const int *rays_per_packet;
+    const int *rays_per_packet;  // [g * rays_gstride + packet]
+    int rays_gstride;
     int batched, nbatch;      // RQMC: variance from nbatch replicate means
     const int *group_empty;   // 1 when the group has no emission
     const double2 *tally;
@@ -101,6 +106,36 @@ struct FinalizeParams {
     double *varg;             // [f][group][cell] or nullptr
     unsigned int *status;
 };
+
+// A read-only view of a solver's device state for the control-variate
+// network (mc_cvnet.cu); filled by solver_view (mc_host.cpp).
+struct SolverView {
+    int device;
+    void *stream;
+    int model, mode;                 // DNSMC_MODEL_*, MODE_*
+    int imax, jmax, kmax, nfields, n_groups, nvar, sampler;
+    int i0, i1, j0, j1, k0, k1;      // region
+    int tile_a, tile_b, npa, npb, npw, n_packets;
+    long long region_cells, field_stride;
+    const float *fieldT;             // [f][i][k][j] (grey, T-only tables)
+    const float2 *fieldTX;           // [f][i][k][j] (T, x_H2O)
+    const float *fw;                 // wall-normal faces
+    float T_lo, T_hi, X_lo, X_hi;    // table ranges (grey: 0, 0, 0, 0)
+    // last solve (solved != 0)
+    int solved, last_groups;
+    const double *moments;           // [f][g][tc][9] or null
+    const double *varg;              // [f][g][cell] dense i fastest
+    const unsigned long long *item_steps;  // [f][g][packet]
+    int rays;                        // uniform rays per (cell, group) when rays_item is null
+    const int *rays_item;            // [g * rays_gstride + packet]
+    int rays_gstride;
+};
+int solver_view(dnsmc_solver *s, SolverView *v);
+// Device buffer of control-variate coefficients [f][g][tc] (tally order) that
+// the next solve uses; the caller fills it on the solver's stream.
+int solver_beta_device(dnsmc_solver *s, float2 **beta, long long *n);
+// Device buffer of per-(group, packet) ray counts that the next solve uses.
+int solver_rays_device(dnsmc_solver *s, int n_groups, int **rays);
 
 // launchers (mc_kernels.cu); all stream-ordered
 int launch_march(int mode, const MarchParams &p, int blocks, int threads,

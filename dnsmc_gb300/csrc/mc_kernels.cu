@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
         const int b0 = P.eb0 + pb * P.tile_b + lb;
         const bool active = (a0 < P.ea1) && (b0 < P.eb1);
         const int acl = active ? a0 : P.ea0, bcl = active ? b0 : P.eb0;
-        const int N = P.rays_per_packet ? P.rays_per_packet[p] : P.rays;
+        const int N = P.rays_per_packet ? P.rays_per_packet[G * P.rays_gstride + p] : P.rays;
         const long long fbase = (long long)f * P.field_stride;
         const int rowW0 = w0 * plane;
         // own-cell quantities
@@ -279,6 +279,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
         const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
 
         double S = 0.0, S2 = 0.0, Sb = 0.0;
+        unsigned long long isteps = 0;
         uint4 shift = make_uint4(0u, 0u, 0u, 0u);
         int bcur = -1;
         const int rbeg = TRACE ? P.trace_r : 0;
@@ -470,6 +471,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 }
             }
             if (TRACE && lane == 0) *P.trace_n = steps;
+            isteps += (unsigned long long)steps;
             float X = w * D;
             if (CV) {
                 // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
@@ -503,6 +505,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             }
         }
         if (TRACE) return;
+        if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
         if (active) P.tally[fg * P.region_cells + tc] = make_double2(S, S2);
         if (MOM && active) {
             double *out = P.moments + (fg * P.region_cells + tc) * 9;
@@ -563,9 +566,9 @@ __global__ void finalize_kernel(const FinalizeParams F) {
         const int kR = (int)(jk / F.njR);
         const long long tc = ((long long)iR * F.nkR + kR) * F.njR + jR;
         const int p = (iR * F.npb + kR / F.tile_b) * F.npa + jR / F.tile_a;
-        const int N = F.rays_per_packet ? F.rays_per_packet[p] : F.rays;
         double Q = 0.0, V = 0.0;
         for (int g = 0; g < F.n_groups; ++g) {
+            const int N = F.rays_per_packet ? F.rays_per_packet[g * F.rays_gstride + p] : F.rays;
             double m = 0.0, v = 0.0;
             if (!F.group_empty[g] && N > 0) {
                 const long long ti = ((long long)f * F.n_groups + g) * F.region_cells + tc;

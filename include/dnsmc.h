@@ -197,6 +197,17 @@ int  dnsmc_set_region(dnsmc_solver *s, int i0, int i1, int j0, int j1, int k0,
  * see dnsmc_packet_count) overrides it per packet of 32 cells when non-NULL.  */
 int  dnsmc_set_rays(dnsmc_solver *s, int rays_per_group,
                     const int *rays_per_packet);
+/* Ray counts per (band group, packet): rays[g * npackets + p], n_groups = the
+ * band groups of the solve.  Each count >= 0 (a multiple of nvar under RQMC);
+ * 0 leaves that group of the packet unsampled (its mean and variance are 0).
+ * Replaced by dnsmc_set_rays / dnsmc_set_region.  No counterpart in the
+ * reference, whose rays per cell are the compile-time photmax
+ * (code/param.h:64).                                                         */
+int  dnsmc_set_rays_per_item(dnsmc_solver *s, int n_groups, const int *rays);
+/* The per-item ray table in effect (set by dnsmc_set_rays_per_item or by a
+ * control-variate network, dnsmc_cvnet_apply): *n_groups = 0 when rays are
+ * uniform or per packet; rays (may be NULL) receives n_groups * npackets.   */
+int  dnsmc_get_rays_per_item(dnsmc_solver *s, int *n_groups, int *rays);
 int  dnsmc_packet_count(const dnsmc_solver *s, int *npackets);
 /* Enqueue a solve of every resident snapshot on the solver's stream and return.*/
 int  dnsmc_solve_async(dnsmc_solver *s);
@@ -214,6 +225,10 @@ int  dnsmc_status(dnsmc_solver *s, uint32_t *status);
  * device time of the march kernel in milliseconds.                             */
 int  dnsmc_get_counters(dnsmc_solver *s, double *rays, double *steps,
                         double *march_ms);
+/* Ray-voxel steps of the last solve per work item (field, band group,
+ * packet), summed over the item's rays: steps[(f * n_groups + g) * npackets
+ * + p].  The cost model of ray allocation.                                   */
+int  dnsmc_get_item_steps(dnsmc_solver *s, double *steps);
 /* Device time of the last solve measured with CUDA events on the solver's
  * stream: from the first enqueued operation (sampling upload) to the end of
  * the result copy into pinned host memory, and of the march kernel alone.    */
@@ -239,6 +254,9 @@ int  dnsmc_prepare_sampling(dnsmc_solver *s, float Tmax, float xmean);
  * band group, cell of the region), dense i fastest, pairs (beta_a, beta_b);
  * NULL restores (1, -1).  Any finite pair keeps the estimate unbiased.       */
 int  dnsmc_set_cv_beta(dnsmc_solver *s, const float *beta);
+/* The coefficients in effect (set by dnsmc_set_cv_beta or by a network,
+ * dnsmc_cvnet_apply), same layout; DNSMC_ERR_STATE when none are set.       */
+int  dnsmc_get_cv_beta(dnsmc_solver *s, float *beta);
 /* Control-variate data of the last solve (any pointer may be NULL): layer
  * means (T_bar, x_bar) [f][imax][2], surrogate (k_bar, Ib_bar)
  * [f][sample][imax][2] (sample = band*nq + g), (Jhat, Ahat) [f][sample][imax][2]
@@ -259,6 +277,86 @@ int  dnsmc_get_geometry(const dnsmc_solver *s, float *xu, float *dy, float *dz);
  * length and lane 0's transmissivity.  Up to max_steps records of 6 words.    */
 int  dnsmc_trace_ray(dnsmc_solver *s, int f, int g, int p, int r, int max_steps,
                      int32_t *rec, int *n_steps, uint32_t *rng4);
+
+/* ---- learned control variate ----------------------------------------------
+ * No counterpart in the reference (its estimator has no control variate).
+ * A small MLP (67 features -> 3 x 128 GELU -> 32 outputs; BF16 weights and
+ * activations, FP32 accumulation on the tensor cores) predicts per cell and
+ * band group (up to 8 groups):
+ *   - the control-variate coefficients (beta_a, beta_b), as offsets from
+ *     (1, -1); any finite pair keeps the estimate unbiased, the network aims
+ *     at the pair of least variance;
+ *   - the log of the estimator variance per ray and of the ray-voxel steps
+ *     per ray, from which ray counts per (band group, packet) follow as
+ *     n ~ sqrt(v / c) at the expected step cost of uniform rays.
+ * Features: T, x_H2O and the signed wall-normal position 2 eta - 1 of the
+ * cell, and T, x_H2O at 32 points of the wall-normal line through the cell
+ * (layers ((2q+1) imax) / 64), as (T - T_center) / T_scale and
+ * (x - x_center) / x_scale, rounded to bf16.
+ * Training data come from solves with control_variate and cv_moments set: per
+ * (cell, group) the per-ray covariances of (X, Y_a, Y_b), the estimator
+ * variance and the packet's steps per ray; losses: the residual variance
+ * (plus ridge * (Var Y_a dbeta_a^2 + Var Y_b dbeta_b^2)) and, for the two log
+ * heads, v e^-o + o (minimised at o = log E[v]).  Adam on FP32 master weights.
+ * The network lives on the device current at dnsmc_cvnet_create.            */
+typedef struct dnsmc_cvnet dnsmc_cvnet;
+typedef struct {
+    int      n_groups;             /* band-group slots, 1..8                    */
+    float    T_center, T_scale;    /* feature map of T [K]                      */
+    float    x_center, x_scale;    /* feature map of x_H2O                      */
+    float    lr, adam_beta1, adam_beta2, adam_eps;
+    float    ridge;                /* pull of the coefficients towards (1, -1)  */
+    int      batch;                /* rows per training step, multiple of 128   */
+    uint64_t seed;                 /* initial weights and row shuffling         */
+} dnsmc_cvnet_config;
+#define DNSMC_CVNET_NFEAT  67
+#define DNSMC_CVNET_NOUT   32
+#define DNSMC_CVNET_NLABEL 8       /* Cxx Caa Cbb Cxa Cxb Cab v c per (cell, group) */
+#define DNSMC_CVNET_BETA   1       /* dnsmc_cvnet_apply: coefficients           */
+#define DNSMC_CVNET_RAYS   2       /* dnsmc_cvnet_apply: ray allocation         */
+void dnsmc_cvnet_default_config(dnsmc_cvnet_config *cfg);
+int  dnsmc_cvnet_create(const dnsmc_cvnet_config *cfg, dnsmc_cvnet **out);
+int  dnsmc_cvnet_destroy(dnsmc_cvnet *net);
+long long dnsmc_cvnet_param_count(void);
+/* FP32 parameters, flat: W1[128][80] b1 W2[128][128] b2 W3[128][128] b3
+ * W4[32][128] b4 (columns 67..79 of W1 are padding and stay 0); scales =
+ * (S_beta, S_v, S_c), the label scales of the losses.  Either may be NULL.
+ * set_params resets the Adam state.                                         */
+int  dnsmc_cvnet_get_params(dnsmc_cvnet *net, float *params, float *scales);
+int  dnsmc_cvnet_set_params(dnsmc_cvnet *net, const float *params,
+                            const float *scales);
+int  dnsmc_cvnet_save(dnsmc_cvnet *net, const char *path);
+int  dnsmc_cvnet_load(const char *path, dnsmc_cvnet **out);
+/* Features of every cell of the solver's region (tally order: i slowest, then
+ * k, j fastest; field slowest), [rows][67] floats (the bf16 values).        */
+int  dnsmc_cvnet_features(dnsmc_cvnet *net, dnsmc_solver *s, float *features);
+/* Append the region's cells of the solver's last solve (control_variate and
+ * cv_moments set, same region) to the network's device-resident data.  The
+ * first call fixes the label scales.                                        */
+int  dnsmc_cvnet_add_training_data(dnsmc_cvnet *net, dnsmc_solver *s);
+int  dnsmc_cvnet_clear_training_data(dnsmc_cvnet *net);
+long long dnsmc_cvnet_training_rows(const dnsmc_cvnet *net);
+/* Adam over the data for `epochs` shuffled passes; loss[4] (may be NULL)
+ * receives the mean losses of the last pass: total, beta, variance, cost.   */
+int  dnsmc_cvnet_train(dnsmc_cvnet *net, int epochs, double *loss);
+/* Forward pass on host features [rows][67] -> out [rows][32].               */
+int  dnsmc_cvnet_eval(dnsmc_cvnet *net, const float *features, long long rows,
+                      float *out);
+/* One forward + backward pass without update on host features and labels
+ * [rows][n_groups][8]: grad receives dnsmc_cvnet_param_count() floats of
+ * d(mean loss)/d(params), loss[4] as dnsmc_cvnet_train.                     */
+int  dnsmc_cvnet_gradient(dnsmc_cvnet *net, const float *features,
+                          const float *labels, int n_groups, long long rows,
+                          float *grad, double *loss);
+/* Evaluate the network on the solver's resident fields and region and set,
+ * on the solver's stream, the control-variate coefficients (flags & BETA)
+ * and/or the per-(group, packet) ray counts (flags & RAYS) of its next
+ * solves: n = clamp(round(lambda sqrt(v/c)), min_rays, max_rays) in multiples
+ * of nvar (RQMC), lambda such that the expected steps equal those of
+ * mean_rays uniform rays.  Requires max(2, nvar) <= min_rays <= mean_rays
+ * <= max_rays.  dnsmc_set_rays / dnsmc_set_cv_beta(NULL) undo it.           */
+int  dnsmc_cvnet_apply(dnsmc_cvnet *net, dnsmc_solver *s, int flags,
+                       int mean_rays, int min_rays, int max_rays);
 
 /* ---- allocation-free grey solve -------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

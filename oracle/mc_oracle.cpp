@@ -540,7 +540,8 @@ typedef struct {
     float kappa;
     float T_west, T_east;
     int rays;
-    const int *rays_per_packet;
+    const int *rays_per_packet;  // [G * rays_gstride + packet]
+    int rays_gstride;            // 0: per packet; npackets: per (group, packet)
     uint64_t seed;
     float toll;
     int max_steps;
@@ -701,7 +702,7 @@ struct Packet {
             if (!act[l]) { a0[l] = c.ea0; b0[l] = c.eb0; }
             S[l] = 0; S2[l] = 0;
         }
-        const int N = c.rays_per_packet ? c.rays_per_packet[p] : c.rays;
+        const int N = c.rays_per_packet ? c.rays_per_packet[G * c.rays_gstride + p] : c.rays;
         int gs = 0, K = 1;
         if (c.mode != 0) {
             int binoff = 0;

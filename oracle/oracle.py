@@ -58,7 +58,7 @@ class PacketConfig(ctypes.Structure):
         ("ktab", _f), ("ibtab", _f), ("ibw", _f), ("n_groups", ctypes.c_int), ("group_start", _i),
         ("prob", _f), ("alias", _i), ("band", _i), ("gq", _i), ("W", _f),
         ("kappa", ctypes.c_float), ("T_west", ctypes.c_float), ("T_east", ctypes.c_float),
-        ("rays", ctypes.c_int), ("rays_per_packet", _i), ("seed", ctypes.c_uint64),
+        ("rays", ctypes.c_int), ("rays_per_packet", _i), ("rays_gstride", ctypes.c_int), ("seed", ctypes.c_uint64),
         ("toll", ctypes.c_float), ("max_steps", ctypes.c_int), ("use_double", ctypes.c_int),
         ("sampler", ctypes.c_int), ("nbatch", ctypes.c_int), ("n_tbins", ctypes.c_int),
         ("cv", ctypes.c_int), ("sur_k", _f), ("sur_I", _f), ("beta", _f), ("moments", _d),
@@ -186,10 +186,17 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
     c.seed, c.toll, c.max_steps, c.use_double = cfg.seed, cfg.toll, cfg.max_steps, use_double
     c.sampler, c.nbatch = cfg.sampler, cfg.nvar
     c.rays = solver_rays(solver)
-    if getattr(solver, "_keep", None):
-        rp = np.ascontiguousarray(solver._keep[0], np.int32)
+    rp = None
+    if getattr(solver, "_rays_dev", False):  # ray table written on the device (network allocation)
+        rp = solver.rays_per_item()
+    elif getattr(solver, "_keep", None):
+        rp = solver._keep[0]
+    if rp is not None:
+        rp = np.ascontiguousarray(rp, np.int32)
         keep["rp"] = rp
         c.rays_per_packet = rp.ctypes.data_as(_i)
+        if rp.ndim == 2:  # per (band group, packet)
+            c.rays_gstride = rp.shape[1]
     if cfg.model == 3:
         c.mode = 0
         c.n_groups = 1
@@ -217,8 +224,9 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
         keep.update(sk=sk, sI=sI)
         c.cv = 1
         c.sur_k, c.sur_I = _fp(sk), _fp(sI)
-        if getattr(solver, "_beta", None) is not None:
-            b = np.ascontiguousarray(solver._beta, np.float32)
+        bsrc = solver.cv_beta() if getattr(solver, "_beta_dev", False) else getattr(solver, "_beta", None)
+        if bsrc is not None:
+            b = np.ascontiguousarray(bsrc, np.float32)
             keep["beta"] = b
             c.beta = _fp(b)
     if mode is not None:

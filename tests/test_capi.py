@@ -20,7 +20,7 @@ from tables_io import write_ck_tables, write_particle_tables
 def header_functions():
     src = open(os.path.join(ROOT, "include", "dnsmc.h")).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*([a-z_][a-z_0-9]*)\s*\(", src, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?(?:long\s+long|[a-z_0-9]+)\s*\*?\s*([a-z_][a-z_0-9]*)\s*\(", src, flags=re.M)))
 
 
 def test_every_declared_function_is_exported():

@@ -33,15 +33,17 @@ def assert_bitexact_cv(s, T, x=None):
     i0, i1, j0, j1, k0, k1 = s._region
     tal, steps = O.packet_mc(c, ng, (i1 - i0) * (j1 - j0) * (k1 - k0))
     tal = region_tally_to_dense(tal, s, ng)
-    N = rays_per_cell(s)
     muY = s.cv_data()["muY"]
-    if s._beta is not None:
+    if getattr(s, "_beta_dev", False):
+        beta = s.cv_beta()
+    elif s._beta is not None:
         beta = s._beta
     else:
         beta = np.zeros(muY.shape, np.float32)
         beta[..., 0], beta[..., 1] = 1.0, -1.0
     B = s.cfg.nvar
     for g in range(ng):
+        N = rays_per_cell(s, g)
         m = tal[:, g, ..., 0] / N
         if s.cfg.sampler == D.SAMPLER_RQMC:
             v = np.maximum(0.0, tal[:, g, ..., 1] / B - m * m) / (B - 1)

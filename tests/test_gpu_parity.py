@@ -51,12 +51,14 @@ def region_tally_to_dense(tal, solver, ng):
     return tal.reshape(nf, ng, ni, nk, nj, 2).transpose(0, 1, 3, 4, 2, 5)
 
 
-def rays_per_cell(solver):
+def rays_per_cell(solver, g=0):
     i0, i1, j0, j1, k0, k1 = solver._region
     ni, nj, nk = i1 - i0, j1 - j0, k1 - k0
     if not solver._keep:
         return np.full((nk, nj, ni), solver._rays, np.float64)
     rp = solver._keep[0]
+    if rp.ndim == 2:  # per (band group, packet)
+        rp = rp[g]
     ta = solver.cfg.tile_a or (32 if nj >= 32 else (16 if nj >= 16 else 8))
     tb = 32 // ta
     npa, npb = -(-nj // ta), -(-nk // tb)
@@ -73,7 +75,6 @@ def assert_bitexact(solver, T, x=None):
     i0, i1, j0, j1, k0, k1 = solver._region
     tal, steps = O.packet_mc(c, ng, (i1 - i0) * (j1 - j0) * (k1 - k0))
     tal = region_tally_to_dense(tal, solver, ng)
-    N = rays_per_cell(solver)
     empty = np.zeros(ng, bool)
     if solver.cfg.model != D.MODEL_GREY:
         gs = solver.sampling()["group_start"]
@@ -82,6 +83,7 @@ def assert_bitexact(solver, T, x=None):
     Vexp = np.zeros_like(Q)
     B = solver.cfg.nvar
     for g in range(ng):
+        N = rays_per_cell(solver, g)
         with np.errstate(invalid="ignore", divide="ignore"):
             m = np.where(N > 0, tal[:, g, ..., 0] / N, 0.0)
             if solver.cfg.sampler == D.SAMPLER_RQMC:
@@ -149,6 +151,30 @@ def test_bitexact_table_x_groups_fields_region():
     npk = s.packet_count()
     s.set_rays(0, np.random.default_rng(0).integers(0, 40, npk))
     assert_bitexact(s, T, x)
+    s.close()
+
+
+def test_bitexact_rays_per_item_and_item_steps():
+    """Ray counts per (band group, packet), zeros included, under RQMC; the
+    per-item step record is positive exactly where rays were cast."""
+    tb = synth.ck_table(nbands=16, nq=8, nT=24, nX=5, seed=4)
+    s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=12, jmax=32, kmax=4, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=400, T_east=400, seed=23, n_groups=4,
+                                  sampler=D.SAMPLER_RQMC, nvar=4))
+    s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+    T = smooth_field(12, 32, 4, 450, 1700, 8)[None]
+    x = (0.1 + 0.05 * np.random.default_rng(3).uniform(-1, 1, (1, 4, 32, 12))).astype(np.float32)
+    s.set_fields(T, x)
+    npk = s.packet_count()
+    rays = 4 * np.random.default_rng(1).integers(0, 12, (4, npk))
+    rays[:, 0] = 0
+    s.set_rays_per_item(rays)
+    assert_bitexact(s, T, x)
+    st = s.item_steps()
+    assert st.shape == (1, 4, npk)
+    assert ((st[0] > 0) == (rays > 0)).all()
+    with pytest.raises(D.DnsmcError):
+        s.set_rays_per_item(rays + 1)  # not multiples of nvar
     s.close()
 
 
