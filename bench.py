@@ -3,16 +3,24 @@ channel (synthetic k(band, g, T, x_H2O) table of 64 bands x 16 g x 50 T x 8 x,
 8 band groups), plus rays/s.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                    [--method net|cv|plain]
 
-A step is one full solve of one Q_r field with the inputs resident in HBM:
-sampling-table upload, the march kernel, the finalize kernel and the copy of
-Q and sigma into pinned host memory, timed with CUDA events on the solver's
-stream.  The ray budget is the smallest one whose estimated RMS error
-sqrt(mean var(Q)) / rms(Q) is <= 1 % (pilot solve, 1/N scaling, then checked
-on the timed solves).  Inputs (16.8 MB) fit in L2, so L2 is flushed (a
-256 MB device write) before every timed step.  `e2e` repeats the step through
-the public API from host arrays: dnsmc_set_fields (host->device) + solve +
-dnsmc_get_results (device->host), wall clock.
+A step is one full solve of one Q_r field with the inputs resident in HBM,
+timed with CUDA events on the solver's stream: for the default network
+control variate, the network's features, forward pass and ray allocation,
+then the sampling-table upload, the control-variate preparation, the march,
+the finalize kernel and the copy of Q and sigma into pinned host memory.  The
+network is the committed one for the grid (dnsmc_gb300/nets/ck128.cvnet) or,
+when absent, trained before the timed region on 16 snapshots the Monte Carlo
+itself produces.  The ray budget (mean rays per cell and group) is the
+smallest one whose estimated RMS error sqrt(mean var(Q)) / rms(Q) is <= 1 %
+(pilot solve, 1/N scaling, refined once, then checked on the timed solves).
+The profile control variate (beta = (1, -1), uniform rays) is timed once at
+its own 1 % budget and plain MC is extrapolated from a pilot, for the
+comparison block.  Inputs (16.8 MB) fit in L2, so L2 is flushed (a 256 MB
+device write) before every timed step.  `e2e` repeats the step through the
+public API from host arrays: dnsmc_set_fields (host->device) + network +
+solve + dnsmc_get_results (device->host), wall clock.
 
 With --gpus N (torchrun), every rank solves its own snapshots (seed = rank):
 cells are independent, no collective is needed; the whole-job value is the
@@ -262,6 +270,110 @@ def run_reference(args):
     return 0
 
 
+def get_network(table, log):
+    """The control-variate network: the committed one for this grid if present,
+    else trained here (untimed) on 16 snapshots the Monte Carlo produces."""
+    from dnsmc_gb300 import CvNet, cvtrain
+    path = os.path.join(ROOT, "dnsmc_gb300", "nets", f"ck{N_CELL}.cvnet")
+    if os.path.exists(path):
+        return CvNet.load(path), {"source": os.path.relpath(path, ROOT)}
+    net, info = cvtrain.train(table, N_CELL, range(1000, 1016), rays=64, epochs=3, j_slab=min(32, N_CELL), log=log)
+    info = {k: v for k, v in info.items() if k != "loss"}
+    info["source"] = "trained in this run before the timed region (16 snapshots, seeds 1000-1015)"
+    return net, info
+
+
+class Arm:
+    """One estimator: plain MC, the profile control variate (beta = (1, -1),
+    uniform rays) or the network control variate (coefficients and rays per
+    (band group, packet) from the network, re-evaluated every step)."""
+
+    def __init__(self, method, table, T, x, Tw, seed, threads, net=None):
+        self.method, self.net = method, net
+        self.s = make_solver(table, Tw, seed=seed, threads=threads, cv=0 if method == "plain" else 1)
+        self.s.set_fields(T, x)
+        self.rays = 0
+
+    def enqueue(self):
+        if self.method == "net":
+            self.net.apply(self.s, beta=True, rays=True, mean_rays=self.rays, min_rays=2 * REPLICATES,
+                           max_rays=4096)
+        else:
+            self.s.set_rays(self.rays)
+        self.s.solve_async()
+
+    def solve(self, rays=None):
+        if rays is not None:
+            self.rays = rays
+        self.enqueue()
+        self.s.wait(600)
+        return self.s.results()
+
+    def budget(self, pilot=64, rays=0):
+        """Rays per cell per group (uniform, or the mean of the network's
+        allocation) for 1 % RMS: pilot solve, 1/N scaling, refined once."""
+        if rays:
+            self.rays = -(-rays // REPLICATES) * REPLICATES
+            return None
+        Q, S = self.solve(pilot)
+        e = rms_error(Q, S)
+        r = int(math.ceil(pilot * (e / TARGET_ERR) ** 2))
+        r = max(2 * REPLICATES, min(1 << 17, -(-r // REPLICATES) * REPLICATES))
+        Q, S = self.solve(r)
+        e1 = rms_error(Q, S)
+        if e1 > 0.98 * TARGET_ERR:
+            r = -(-int(math.ceil(r * (e1 / (0.98 * TARGET_ERR)) ** 2)) // REPLICATES) * REPLICATES
+        self.rays = r
+        return e
+
+    def timed(self, steps, warmup, flushbuf):
+        import torch
+        stream = torch.cuda.ExternalStream(self.s.stream())
+        for _ in range(max(3, warmup)):
+            self.solve()
+        out = dict(ms=[], march_ms=[], steps=0.0, warp_steps=0.0, rays=0.0, errs=[])
+        torch.cuda.synchronize()
+        for _ in range(steps):
+            flush_l2(flushbuf)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            self.enqueue()
+            e1.record(stream)
+            self.s.wait(600)
+            e1.synchronize()
+            Q, S = self.s.results()
+            out["ms"].append(e0.elapsed_time(e1))
+            out["march_ms"].append(self.s.timing()[1])
+            c = self.s.counters()
+            out["steps"] += c.steps
+            out["rays"] += c.rays
+            out["warp_steps"] += float(self.s.item_steps().sum())
+            out["errs"].append(rms_error(Q, S))
+        out["Q"], out["S"] = Q, S
+        return out
+
+    def e2e(self, T, x, steps):
+        ms = []
+        Q = S = None
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            self.s.set_fields(T, x)
+            self.enqueue()
+            Q, S = self.s.results()
+            ms.append((time.perf_counter() - t0) * 1e3)
+        return ms, Q, S
+
+    def close(self):
+        self.s.close()
+
+
+# kernels per step: table coordinates, march, finalize; the control variate adds
+# layer means, surrogate table, 1-D quadrature and E[Y]; the network adds
+# features, MLP, coefficients/costs and three allocation kernels
+LAUNCHES = {"plain": 3, "cv": 7, "net": 13}
+
+
 def main():
     global N_CELL
     ap = argparse.ArgumentParser()
@@ -274,8 +386,10 @@ def main():
     ap.add_argument("--n", type=int, default=128, help="cells per axis (profiling cases)")
     ap.add_argument("--rays", type=int, default=0, help="fixed rays per cell per group (skips the 1%% budget)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--plain", action="store_true", help="time plain MC instead of the control variate")
-    ap.add_argument("--no-plain", action="store_true", help="skip the extrapolated plain-MC comparison")
+    ap.add_argument("--method", default="net", choices=["net", "cv", "plain"],
+                    help="timed estimator: network control variate (default), profile control variate, plain MC")
+    ap.add_argument("--no-compare", action="store_true",
+                    help="skip the profile-CV and extrapolated plain-MC comparison arms")
     args = ap.parse_args()
     N_CELL = args.n
     if args.impl == "reference":
@@ -287,109 +401,100 @@ def main():
     from dnsmc_gb300 import synth
     table = synth.ck_table()
     T, x, Tw = make_inputs(rank)
-    s = make_solver(table, Tw, seed=1000 + rank, threads=args.threads, cv=0 if args.plain else 1)
-    s.set_fields(T, x)
-    if args.rays:
-        rays, e_pilot = -(-args.rays // REPLICATES) * REPLICATES, None
-    else:
-        rays, e_pilot = ray_budget(s, 64)
-        # refine once at the predicted budget (RQMC + CV errors fall slightly
-        # slower than 1/N here), aiming 2 % below the target
-        s.set_rays(rays)
-        Qr, Sr = s.solve(timeout_s=600)
-        e1 = rms_error(Qr, Sr)
-        if e1 > 0.98 * TARGET_ERR:
-            rays = -(-int(math.ceil(rays * (e1 / (0.98 * TARGET_ERR)) ** 2)) // REPLICATES) * REPLICATES
-    rays = int(barrier_max(pg, rays))
-    s.set_rays(rays)
+    net, net_info = (None, None)
+    if args.method == "net":
+        net, net_info = get_network(table, log)
+    arm = Arm(args.method, table, T, x, Tw, 1000 + rank, args.threads, net)
+    e_pilot = arm.budget(64, args.rays)
+    arm.rays = int(barrier_max(pg, arm.rays))
     flushbuf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
-    for _ in range(max(3, args.warmup)):
-        s.solve(timeout_s=600)
     # ---- device-resident timed region --------------------------------------
-    solve_ms, march_ms, errs, steps_tot, rays_tot = [], [], [], 0.0, 0.0
     if pg is not None:
         pg.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush_l2(flushbuf)
-            Q, S = s.solve(timeout_s=600)
-            a, b = s.timing()
-            c = s.counters()
-            solve_ms.append(a)
-            march_ms.append(b)
-            steps_tot += c.steps
-            rays_tot += c.rays
-            errs.append(rms_error(Q, S))
+        r = arm.timed(args.steps, args.warmup, flushbuf)
     torch.cuda.synchronize()
-    t_rank = float(np.sum(solve_ms))
+    t_rank = float(np.sum(r["ms"]))
     t_max = barrier_max(pg, t_rank)
     fields = args.steps * world
     ms_field = t_max / fields
-    rays_s = rays_tot * world / (t_max / 1e3)
-    march_avg = float(np.mean(march_ms))
-    steps_per_launch = steps_tot / args.steps
+    rays_s = r["rays"] * world / (t_max / 1e3)
+    march_avg = float(np.mean(r["march_ms"]))
+    steps_per_launch = r["steps"] / args.steps
     achieved = BYTES_PER_STEP * steps_per_launch / (march_avg / 1e3) / 1e9
     peak, peak_kind = peaks()
     # ---- end to end through the public API from host arrays ------------------
-    e2e_ms = []
-    Qh, Sh = Q, S
-    for i in range(0 if args.no_e2e else args.steps):
-        t0 = time.perf_counter()
-        s.set_fields(T, x)
-        s.solve_async()
-        Qh, Sh = s.results()
-        e2e_ms.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms, Qh, Sh = ([], r["Q"], r["S"]) if args.no_e2e else arm.e2e(T, x, args.steps)
     e2e_rank = float(np.sum(e2e_ms)) if e2e_ms else float("nan")
     e2e_max = barrier_max(pg, e2e_rank) / fields
     h2d = T.nbytes + x.nbytes
     d2h = Qh.nbytes + Sh.nbytes
+    alloc = None
+    if args.method == "net":
+        rp = arm.s.rays_per_item()
+        alloc = {"mean": float(rp.mean()), "min": int(rp.min()), "max": int(rp.max()),
+                 "per_group_mean": [float(v) for v in rp.mean(1)]}
+    arm.close()
     if rank != 0:
-        s.close()
         if pg is not None:
             pg.destroy_process_group()
         return 0
-    plain = None
-    if not args.plain and not args.no_plain and not args.rays:
-        plain = plain_extrapolated(table, T, x, Tw, seed=2000 + rank)
+    compare = {}
+    if not args.no_compare and not args.rays:
+        if args.method != "cv":
+            c = Arm("cv", table, T, x, Tw, 3000 + rank, args.threads)
+            c.budget(64)
+            rc = c.timed(1, 1, flushbuf)
+            compare["cv_profile"] = {"rays_per_cell_per_group": c.rays, "ms_at_1pct": float(rc["ms"][0]),
+                                     "rms_error": rc["errs"][0]}
+            c.close()
+        if args.method != "plain":
+            compare["plain_mc"] = plain_extrapolated(table, T, x, Tw, seed=2000 + rank)
     cpu = None
     if not args.no_cpu:
         try:
-            info = cpu_reference(table, T, x, Tw, rays)
+            info = cpu_reference(table, T, x, Tw, arm.rays)
             cpu = {"value": info["ms_field"], "unit": "ms", "cores": info["cores"], "kind": "port",
                    "sample": info["sample"], "rays_per_s": info["rays_s"]}
         except Exception as ex:  # the baseline must not take the GPU number down
             cpu = {"value": None, "unit": "ms", "cores": os.cpu_count(), "kind": "port", "sample": f"failed: {ex}"}
+    desc = {"plain": "plain MC",
+            "cv": "control variate: the same ray through the plane-averaged profile, exact 1-D mean added back "
+                  "(beta = (1, -1), uniform rays)",
+            "net": "network control variate: the same ray through the plane-averaged profile, exact 1-D mean added "
+                   "back, coefficients (beta_a, beta_b) per cell and band group and rays per (band group, packet) "
+                   "from the BF16 MLP evaluated every step"}[args.method]
     out = {
         "metric": METRIC, "value": ms_field, "unit": "ms", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_field, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "ck channel 128^3 (x,z periodic 2pi x pi, y walls black 400 K), T 400-1800 K + 5% "
                                "Fourier, x_H2O 0.1+0.05f, k table 64 bands x 16 g x 50 T x 8 x, 8 band groups, "
-                               + ("plain MC" if args.plain else
-                                  "control variate: the same ray through the plane-averaged profile, exact 1-D "
-                                  "mean added back (beta = 1, no network)")
-                               + ", RQMC rays (4 shifted Sobol' replicates), spectral sampling at the packet "
-                                 "temperature",
-                   "method": "plain" if args.plain else "cv-profile",
-                   "rays_per_cell_per_group": rays, "rays_per_cell": rays * GROUPS, "target_rms_error": TARGET_ERR,
-                   "rms_error_pilot": e_pilot, "rms_error_timed": float(np.mean(errs)),
-                   "l2": "flushed before every timed step (256 MB device write)", "parallelism": f"cells x{world}"},
-        "plain_mc": plain,
-        "rays_per_s": rays_s, "ray_steps_per_s": steps_tot * world / (t_max / 1e3),
-        "march_ms": march_avg, "solve_ms": float(np.mean(solve_ms)),
+                               + desc + ", RQMC rays (4 shifted Sobol' replicates), spectral sampling at the packet "
+                                        "temperature",
+                   "method": args.method, "n": N_CELL,
+                   "rays_per_cell_per_group": arm.rays, "rays_per_cell": arm.rays * GROUPS,
+                   "target_rms_error": TARGET_ERR, "rms_error_pilot": e_pilot,
+                   "rms_error_timed": float(np.mean(r["errs"])),
+                   "l2": "flushed before every timed step (256 MB device write)", "parallelism": f"cells x{world}",
+                   "network": net_info, "ray_allocation": alloc},
+        "comparison": compare,
+        "rays_per_s": rays_s, "ray_steps_per_s": r["steps"] * world / (t_max / 1e3),
+        "march_ms": march_avg, "step_ms": float(np.mean(r["ms"])),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "peak_kind": peak_kind,
                      "note": f"algorithmic gather bytes {BYTES_PER_STEP} B per ray-voxel step x lane-steps per "
                              f"launch / march kernel time (CUDA events)"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_max, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "timing": "wall clock around set_fields + solve + get_results"},
-        "gpu_launches": (2 if args.plain else 6) * args.steps,
+                "timing": "wall clock around set_fields + (network) + solve + get_results"},
+        "gpu_launches": LAUNCHES[args.method] * args.steps,
         "clocks": clk.summary(),
     }
     print(json.dumps(out), flush=True)
-    s.close()
+    if net is not None:
+        net.close()
     if pg is not None:
         pg.destroy_process_group()
     return 0

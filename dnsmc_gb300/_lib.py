@@ -92,6 +92,7 @@ SIGNATURES = {
     "dnsmc_get_item_steps": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "dnsmc_get_rays_per_item": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p]),
     "dnsmc_get_cv_beta": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
+    "dnsmc_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "dnsmc_cvnet_default_config": (None, [ctypes.POINTER(CvNetConfig)]),
     "dnsmc_cvnet_create": (ctypes.c_int, [ctypes.POINTER(CvNetConfig), ctypes.POINTER(ctypes.c_void_p)]),
     "dnsmc_cvnet_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -188,6 +188,12 @@ class Solver:
         self._keep = [rp]
         self._rays_dev = False
 
+    def stream(self) -> int:
+        """The solver's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        h = ctypes.c_void_p()
+        check(self._lib.dnsmc_get_stream(self._h, ctypes.byref(h)))
+        return int(h.value or 0)
+
     def cv_beta(self):
         """Coefficients in effect: (nfields, n_groups, nk, nj, ni, 2) float32."""
         ng = self.sampling()["n_groups"] if self.cfg.model != _lib.MODEL_GREY else 1

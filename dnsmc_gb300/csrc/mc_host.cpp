@@ -289,10 +289,13 @@ struct dnsmc_solver {
     std::vector<double> Ccoef;               // [band*nq+g] target coefficients
     std::vector<int> cv_grp, cv_sid;
     std::vector<double> cv_C;
+    std::vector<float> cv_Cf;
     DevBuf<int> d_cv_grp, d_cv_sid;
     DevBuf<double> d_cv_C;
     DevBuf<float2> d_layer, d_sur;
     DevBuf<double2> d_Jhat, d_muY;
+    DevBuf<float4> d_Jf;
+    DevBuf<float> d_cv_Cf;
     DevBuf<float2> d_beta;
     DevBuf<double> d_moments;
     bool beta_set = false;
@@ -901,6 +904,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         TRY(s->d_layer.ensure((size_t)s->nfields * c.imax));
         TRY(s->d_sur.ensure(nsur));
         TRY(s->d_Jhat.ensure(nsur));
+        TRY(s->d_Jf.ensure(nsur));
         TRY(s->d_muY.ensure((size_t)s->nfields * P.n_groups * P.region_cells));
         if (mode != MODE_GREY) {
             TRY(s->d_cv_grp.ensure(s->cv_grp.size()));
@@ -909,6 +913,9 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
             CUDA_TRY(cudaMemcpyAsync(s->d_cv_grp.p, s->cv_grp.data(), s->cv_grp.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
             CUDA_TRY(cudaMemcpyAsync(s->d_cv_sid.p, s->cv_sid.data(), s->cv_sid.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
             CUDA_TRY(cudaMemcpyAsync(s->d_cv_C.p, s->cv_C.data(), s->cv_C.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+            s->cv_Cf.assign(s->cv_C.begin(), s->cv_C.end());
+            TRY(s->d_cv_Cf.ensure(std::max<size_t>(1, s->cv_Cf.size())));
+            CUDA_TRY(cudaMemcpyAsync(s->d_cv_Cf.p, s->cv_Cf.data(), s->cv_Cf.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
         }
         CvParams cp{};
         cp.nfields = s->nfields; cp.nw = c.imax; cp.na = c.jmax; cp.nb = c.kmax;
@@ -922,6 +929,8 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         cp.kappa = c.kappa; cp.Tw4[0] = P.Tw4[0]; cp.Tw4[1] = P.Tw4[1];
         cp.n_samples = S; cp.sur = s->d_sur.p; cp.fw = s->d_fw.p; cp.toll = c.toll; cp.dtoll = P.dtoll;
         cp.Jhat = s->d_Jhat.p;
+        cp.Jf = s->d_Jf.p;
+        cp.samp_Cf = s->d_cv_Cf.p;
         cp.n_groups = P.n_groups;
         cp.grp_start = s->d_cv_grp.p; cp.samp_id = s->d_cv_sid.p; cp.samp_C = s->d_cv_C.p;
         cp.Wgrey = 4.0 * c.kappa * kSigma;
@@ -1241,7 +1250,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_fw.release(); s->d_k.release(); s->d_ib.release(); s->d_ibw.release();
     s->d_kpair.release(); s->d_ibpair.release(); s->d_posT.release(); s->d_posTX.release();
     s->d_cv_grp.release(); s->d_cv_sid.release(); s->d_cv_C.release(); s->d_layer.release();
-    s->d_sur.release(); s->d_Jhat.release(); s->d_muY.release(); s->d_beta.release(); s->d_moments.release();
+    s->d_sur.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();
     s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_item_steps.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
@@ -1459,6 +1468,13 @@ int dnsmc_set_rays_per_item(dnsmc_solver *s, int n_groups, const int *rays) {
     s->rays_dev = false;
     TRY(s->d_rays_pp.ensure(n));
     CUDA_TRY(cudaMemcpy(s->d_rays_pp.p, s->rays_pp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    return DNSMC_OK;
+}
+
+int dnsmc_get_stream(dnsmc_solver *s, void **stream) {
+    if (!s || !stream) return fail(DNSMC_ERR_ARG, "null argument");
+    TRY(set_device(s));
+    *stream = (void *)s->stream;
     return DNSMC_OK;
 }
 

@@ -178,11 +178,13 @@ struct CvParams {
     int nquad;                // nodes per hemisphere
     double2 *Jhat;            // [f][sample][nw] (Jhat, Ahat): direction-averaged surrogate
                               // intensity and own-layer absorptance
+    float4 *Jf;               // [f][sample][nw] (Jhat hi, Jhat lo, Ahat, layer-mean Ib) for the mean
     // mean of Y per (field, group, cell) in tally layout
     int n_groups;
     const int *grp_start;     // n_groups+1 into samp_id / samp_C
     const int *samp_id;
     const double *samp_C;
+    const float *samp_Cf;     // samp_C rounded to float
     double Wgrey;
     int ew0, ew1, ea0, ea1, eb0, eb1;
     long long region_cells;

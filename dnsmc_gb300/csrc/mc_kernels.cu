@@ -880,13 +880,35 @@ __global__ void cv_jhat_kernel(const CvParams c) {
                 accA += c_quad_w[q] * (1.0 - (double)t0);
             }
         }
-        c.Jhat[idx] = make_double2(0.5 * acc, 0.5 * accA);
+        const double J = 0.5 * acc;
+        const float Jhi = (float)J;
+        c.Jhat[idx] = make_double2(J, 0.5 * accA);
+        c.Jf[idx] = make_float4(Jhi, (float)(J - (double)Jhi), (float)(0.5 * accA), sp[w].y);
     }
 }
 
-// E[Y] per (field, group, cell of the region), tally layout [f][g][i][k][j].
+// Compensated FP32 accumulation (Kahan): sum - comp carries the exact sum to
+// about 2^-44 relative; the file is compiled without FMA contraction, so the
+// compensation is not folded away.
+struct KahanF {
+    float s = 0.0f, comp = 0.0f;
+    __device__ __forceinline__ void add(float v) {
+        const float y = v - comp;
+        const float t = s + y;
+        comp = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)comp; }
+};
+
+// E[Y] per (field, group, cell of the region), tally layout [f][g][i][k][j]:
+//   E[Y_a] = sum_s C_s k_s(T_i, x_i) (Ib_s(T_i) - Jhat_s(layer)),
+//   E[Y_b] = sum_s C_s k_s(T_i, x_i) (Ib_s(T_i) - Ibar_s(layer)) Ahat_s(layer),
+// over the group's spectral samples, in FP32 with compensated sums (the
+// device's FP64 rate is a small fraction of its FP32 rate); Jhat enters as a
+// double-float pair so Ib - Jhat keeps its digits where they cancel.
 __global__ void cv_mean_kernel(const CvParams c) {
-    const int niR = c.ew1 - c.ew0, njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0;
+    const int njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0;
     const long long n = (long long)c.nfields * c.region_cells;
     const long long plane = (long long)c.na * c.nb;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
@@ -902,28 +924,45 @@ __global__ void cv_mean_kernel(const CvParams c) {
         float T, x = 0.f;
         if (c.mode == MODE_TX) { const float2 v = c.fieldTX[cell]; T = v.x; x = v.y; }
         else T = c.fieldT[cell];
-        const double2 *Jh = c.Jhat + (long long)f * c.n_samples * c.nw + w;
-        const float2 *Sw = c.sur + (long long)f * c.n_samples * c.nw + w;
-        (void)niR;
+        const long long sbase = (long long)f * c.n_samples * c.nw + w;
+        if (c.mode == MODE_GREY) {
+            const float t2 = T * T;
+            const double2 jh = c.Jhat[sbase];
+            const double acc = c.Wgrey * ((double)(t2 * t2) - jh.x);
+            const double accB = c.Wgrey * ((double)(t2 * t2) - (double)c.sur[sbase].y) * jh.y;
+            c.muY[(long long)f * c.n_groups * c.region_cells + tc] = make_double2(acc, accB);
+            continue;
+        }
+        int ti, xi = 0;
+        float ft, fx = 0.f;
+        grid_pos(T, c.T0, c.invdT, c.nT, &ti, &ft);
+        if (c.mode == MODE_TX) grid_pos(x, c.X0, c.invdX, c.nX, &xi, &fx);
         for (int g = 0; g < c.n_groups; ++g) {
-            double acc = 0.0, accB = 0.0;
-            if (c.mode == MODE_GREY) {
-                const float t2 = T * T;
-                const double2 jh = Jh[0];
-                acc = c.Wgrey * ((double)(t2 * t2) - jh.x);
-                accB = c.Wgrey * ((double)(t2 * t2) - (double)Sw[0].y) * jh.y;
-            } else {
-                for (int q = c.grp_start[g]; q < c.grp_start[g + 1]; ++q) {
-                    const int sid = c.samp_id[q];
-                    const float k = cv_k(c, sid, T, x);
-                    const float Ib = cv_ib(c, sid / c.nq, T);
-                    const double2 jh = Jh[(long long)sid * c.nw];
-                    const double ck = c.samp_C[q] * (double)k;
-                    acc += ck * ((double)Ib - jh.x);
-                    accB += ck * ((double)Ib - (double)Sw[(long long)sid * c.nw].y) * jh.y;
+            KahanF sa, sb;
+            for (int q = c.grp_start[g]; q < c.grp_start[g + 1]; ++q) {
+                const int sid = c.samp_id[q];
+                float k;
+                if (c.mode == MODE_TX) {
+                    const float *s = c.ktab + (long long)sid * c.nT * c.nX + ti * c.nX + xi;
+                    const float k00 = __ldg(s), k01 = __ldg(s + 1);
+                    const float k10 = __ldg(s + c.nX), k11 = __ldg(s + c.nX + 1);
+                    const float k0 = fmaf(fx, k01 - k00, k00);
+                    const float k1 = fmaf(fx, k11 - k10, k10);
+                    k = fmaf(ft, k1 - k0, k0);
+                } else {
+                    const float *s = c.ktab + (long long)sid * c.nT + ti;
+                    const float k0 = __ldg(s), k1 = __ldg(s + 1);
+                    k = fmaf(ft, k1 - k0, k0);
                 }
+                const float *ib = c.ibtab + (sid / c.nq) * c.nT + ti;
+                const float i0 = __ldg(ib), i1 = __ldg(ib + 1);
+                const float Ib = fmaf(ft, i1 - i0, i0);
+                const float4 J = __ldg(c.Jf + sbase + (long long)sid * c.nw);
+                const float ck = __ldg(c.samp_Cf + q) * k;
+                sa.add(ck * ((Ib - J.x) - J.y));
+                sb.add(ck * (Ib - J.w) * J.z);
             }
-            c.muY[((long long)f * c.n_groups + g) * c.region_cells + tc] = make_double2(acc, accB);
+            c.muY[((long long)f * c.n_groups + g) * c.region_cells + tc] = make_double2(sa.value(), sb.value());
         }
     }
 }

@@ -73,15 +73,30 @@ def add_snapshots(net: CvNet, table, n: int, seeds, rays: int, j_slab: int | Non
 
 
 def train(table, n: int, seeds, rays: int = 64, epochs: int = 3, j_slab: int | None = None, net: CvNet | None = None,
-          log=None, **cfg) -> tuple[CvNet, dict]:
+          log=None, chunk: int = 0, **cfg) -> tuple[CvNet, dict]:
+    """Train on the snapshots `seeds`; with chunk > 0 the data are streamed:
+    `chunk` snapshots are solved, trained on for `epochs` passes and dropped
+    before the next chunk (device memory stays bounded)."""
     net = net or CvNet(feature_config(table, **cfg))
-    t0 = time.time()
-    ts = add_snapshots(net, table, n, seeds, rays, j_slab, log)
-    t1 = time.time()
-    losses = net.train(epochs)
-    t2 = time.time()
-    info = dict(fields=len(list(seeds)), rows=net.training_rows(), rays=rays, epochs=epochs, n=n,
-                data_s=t1 - t0, solve_s=ts, train_s=t2 - t1, loss=losses)
+    seeds = list(seeds)
+    step = chunk if chunk > 0 else len(seeds)
+    t_data = t_solve = t_train = 0.0
+    rows = 0
+    losses = None
+    for c0 in range(0, len(seeds), step):
+        net.clear_training_data()
+        t0 = time.time()
+        t_solve += add_snapshots(net, table, n, seeds[c0:c0 + step], rays, j_slab, log if chunk == 0 else None)
+        t1 = time.time()
+        rows += net.training_rows()
+        losses = net.train(epochs)
+        t2 = time.time()
+        t_data += t1 - t0
+        t_train += t2 - t1
+        if log and chunk:
+            log(f"snapshots {c0 + 1}-{min(len(seeds), c0 + step)}: loss {losses}")
+    info = dict(fields=len(seeds), rows=rows, rays=rays, epochs=epochs, n=n, chunk=step, data_s=t_data,
+                solve_s=t_solve, train_s=t_train, loss=losses)
     if log:
         log(f"trained: {info}")
     return net, info
@@ -95,11 +110,12 @@ def main(argv=None) -> int:
     ap.add_argument("--rays", type=int, default=64)
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--slab", type=int, default=32, help="j cells per snapshot (0: all)")
+    ap.add_argument("--chunk", type=int, default=0, help="snapshots per streamed training chunk (0: all at once)")
     ap.add_argument("--out", required=True)
     a = ap.parse_args(argv)
     table = synth.ck_table(64, 16, 50, 8, seed=0)
     seeds = range(a.first_seed, a.first_seed + a.fields)
-    net, info = train(table, a.n, seeds, a.rays, a.epochs, a.slab or None,
+    net, info = train(table, a.n, seeds, a.rays, a.epochs, a.slab or None, chunk=a.chunk,
                       log=lambda m: print(m, file=sys.stderr, flush=True))
     net.save(a.out)
     print(info)

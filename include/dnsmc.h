@@ -219,6 +219,10 @@ int  dnsmc_wait(dnsmc_solver *s, double timeout_s);
 int  dnsmc_get_results(dnsmc_solver *s, double *Q, double *sigma);
 /* Per band group: mean and variance of the mean, [field][group][cell].         */
 int  dnsmc_get_group_results(dnsmc_solver *s, double *Qg, double *varg);
+/* The solver's CUDA stream (cudaStream_t; created on first use): every solve,
+ * upload and network evaluation of this solver is ordered on it, so a caller
+ * can order its own work (or CUDA events) against them.                      */
+int  dnsmc_get_stream(dnsmc_solver *s, void **stream);
 /* Bits DNSMC_STATUS_* accumulated by the last solve.                           */
 int  dnsmc_status(dnsmc_solver *s, uint32_t *status);
 /* Counters of the last solve: emitted rays and ray-voxel steps (all lanes),
