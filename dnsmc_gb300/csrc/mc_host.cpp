@@ -1429,10 +1429,10 @@ int dnsmc_set_rays(dnsmc_solver *s, int rays_per_group, const int *rays_per_pack
     const int B = s->cfg.sampler == DNSMC_SAMPLER_RQMC ? s->cfg.nvar : 1;
     if (!rays_per_packet && rays_per_group % B)
         return fail(DNSMC_ERR_ARG, "RQMC: rays per group (%d) must be a multiple of nvar (%d)", rays_per_group, B);
-    TRY(set_device(s));
     TRY(wait_done(s, 0));
     s->rays = rays_per_group;
     if (rays_per_packet) {
+        TRY(set_device(s));
         int np;
         TRY(dnsmc_packet_count(s, &np));
         for (int i = 0; i < np; ++i) {
