@@ -93,6 +93,10 @@ SIGNATURES = {
     "dnsmc_get_rays_per_item": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p]),
     "dnsmc_get_cv_beta": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
     "dnsmc_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
+    "dnsmc_set_graph": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dnsmc_get_graph_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
+                                            ctypes.POINTER(ctypes.c_longlong)]),
+    "dnsmc_set_rays_adaptive": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_int, ctypes.c_int]),
     "dnsmc_cvnet_default_config": (None, [ctypes.POINTER(CvNetConfig)]),
     "dnsmc_cvnet_create": (ctypes.c_int, [ctypes.POINTER(CvNetConfig), ctypes.POINTER(ctypes.c_void_p)]),
     "dnsmc_cvnet_destroy": (ctypes.c_int, [ctypes.c_void_p]),

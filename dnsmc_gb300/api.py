@@ -203,15 +203,31 @@ class Solver:
         return out
 
     def rays_per_item(self):
-        """The per-(group, packet) ray table in effect (set here or by a
-        network), or None for uniform / per-packet rays."""
+        """The ray table in effect: (n_groups, npackets) per (group, packet)
+        (set here or by a network), (npackets,) per packet (adaptive or
+        per-packet rays), or None for uniform rays."""
         ng = ctypes.c_int()
         check(self._lib.dnsmc_get_rays_per_item(self._h, ctypes.byref(ng), None))
         if ng.value == 0:
             return None
-        out = np.zeros((ng.value, self.packet_count()), np.int32)
+        shape = (ng.value, self.packet_count()) if ng.value > 0 else (self.packet_count(),)
+        out = np.zeros(shape, np.int32)
         check(self._lib.dnsmc_get_rays_per_item(self._h, ctypes.byref(ng), out.ctypes.data_as(_lib.c_int_p)))
         return out
+
+    def set_rays_adaptive(self, rays_per_tau: float, min_rays: int = 64, max_rays: int = 4096) -> None:
+        """Rays per packet ~ local optical thickness (device-computed)."""
+        check(self._lib.dnsmc_set_rays_adaptive(self._h, float(rays_per_tau), int(min_rays), int(max_rays)))
+        self._keep = []
+        self._rays_dev = True
+
+    def set_graph(self, enable: bool = True) -> None:
+        check(self._lib.dnsmc_set_graph(self._h, 1 if enable else 0))
+
+    def graph_info(self):
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        check(self._lib.dnsmc_get_graph_info(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def item_steps(self):
         """Ray-voxel steps of the last solve per (field, group, packet), summed over rays."""

@@ -274,6 +274,7 @@ struct dnsmc_solver {
     bool rays_dev = false;                   // d_rays_pp was written on the device (no host copy)
     DevBuf<int> d_rays_pp;
     DevBuf<unsigned long long> d_item_steps; // steps per (field, group, packet) of the last solve
+    DevBuf<float> d_kP;                      // Planck-mean absorption coefficient on the table grid
 
     // sampling of the last solve
     float tmax_used = 0.f;
@@ -312,6 +313,11 @@ struct dnsmc_solver {
     float march_ms = 0.f, solve_ms = 0.f;
     MarchParams last{};
     FinalizeParams lastF{};
+    // CUDA graph of the solve's kernel sequence (dnsmc_set_graph)
+    bool graph_on = false;
+    cudaGraphExec_t graph_exec = nullptr;
+    std::vector<unsigned char> graph_key;
+    long long graph_captures = 0, graph_launches = 0;
 };
 
 namespace {
@@ -812,7 +818,8 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     int ni, nj, nk, ta, tb, npa, npb, npw;
     region_dims(s, &ni, &nj, &nk);
     tiling(s, &ta, &tb, &npa, &npb, &npw);
-    MarchParams P{};
+    MarchParams P;
+    memset(&P, 0, sizeof P);  // the bytes form the graph key: padding included
     P.nw = c.imax; P.na = c.jmax; P.nb = c.kmax;
     P.da = s->da; P.db = s->db; P.fw = s->d_fw.p;
     P.ew0 = s->r_i0; P.ew1 = s->r_i1; P.ea0 = s->r_j0; P.ea1 = s->r_j1; P.eb0 = s->r_k0; P.eb1 = s->r_k1;
@@ -857,21 +864,9 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
                          P.n_groups);
         P.rays_gstride = P.n_packets;
     }
-    if (mode != MODE_GREY && !trace) {
-        // table coordinates of the field for this table (once per solve)
-        const long long ncell = (long long)s->nfields * P.field_stride;
-        int rcp;
-        if (mode == MODE_TX) {
-            TRY(s->d_posTX.ensure((size_t)ncell));
-            rcp = launch_field_pos(nullptr, s->d_fieldTX.p, nullptr, s->d_posTX.p, ncell, P.T0, P.invdT, P.nT, P.X0,
-                                   P.invdX, P.nX, s->stream);
-        } else {
-            TRY(s->d_posT.ensure((size_t)ncell));
-            rcp = launch_field_pos(s->d_fieldT.p, nullptr, s->d_posT.p, nullptr, ncell, P.T0, P.invdT, P.nT, P.X0,
-                                   P.invdX, P.nX, s->stream);
-        }
-        if (rcp) return fail(DNSMC_ERR_CUDA, "coordinate launch: %s", cudaGetErrorString((cudaError_t)rcp));
-    }
+    const long long ncell = (long long)s->nfields * P.field_stride;
+    if (mode == MODE_TX && !trace) TRY(s->d_posTX.ensure((size_t)ncell));
+    if (mode == MODE_T && !trace) TRY(s->d_posT.ensure((size_t)ncell));
     P.fieldP = s->d_posT.p;
     P.fieldPX = s->d_posTX.p;
     TRY(s->d_misc.ensure(4));
@@ -897,6 +892,9 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         if (rc) return fail(DNSMC_ERR_CUDA, "trace launch: %s", cudaGetErrorString((cudaError_t)rc));
         return DNSMC_OK;
     }
+    // ---- buffers and kernel parameters (no kernel is enqueued yet) ----------
+    CvParams cp;
+    memset(&cp, 0, sizeof cp);
     if (cv) {
         // E[Y] per (field, group, cell): layer means -> surrogate table ->
         // 1-D quadrature Jhat -> sum over the group's samples
@@ -917,7 +915,6 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
             TRY(s->d_cv_Cf.ensure(std::max<size_t>(1, s->cv_Cf.size())));
             CUDA_TRY(cudaMemcpyAsync(s->d_cv_Cf.p, s->cv_Cf.data(), s->cv_Cf.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
         }
-        CvParams cp{};
         cp.nfields = s->nfields; cp.nw = c.imax; cp.na = c.jmax; cp.nb = c.kmax;
         cp.fieldT = (mode == MODE_TX) ? nullptr : s->d_fieldT.p;
         cp.fieldTX = (mode == MODE_TX) ? s->d_fieldTX.p : nullptr;
@@ -937,9 +934,6 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         cp.ew0 = P.ew0; cp.ew1 = P.ew1; cp.ea0 = P.ea0; cp.ea1 = P.ea1; cp.eb0 = P.eb0; cp.eb1 = P.eb1;
         cp.region_cells = P.region_cells;
         cp.muY = s->d_muY.p;
-        int rc = launch_cv_prepare(cp, s->stream);
-        if (rc == 0) rc = launch_cv_mean(cp, s->stream);
-        if (rc) return fail(DNSMC_ERR_CUDA, "control-variate launch: %s", cudaGetErrorString((cudaError_t)rc));
         s->cv_samples = S;
         P.sur = s->d_sur.p;
         if (mom) {
@@ -951,19 +945,12 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.tally = s->d_tally.p;
     TRY(s->d_item_steps.ensure((size_t)P.n_items));
     P.item_steps = s->d_item_steps.p;
-    CUDA_TRY(cudaMemsetAsync(s->d_misc.p, 0, 4 * sizeof(unsigned int), s->stream));
-    CUDA_TRY(cudaMemsetAsync(s->d_counters.p, 0, 2 * sizeof(unsigned long long), s->stream));
     const int sms = device_sm_count();
     const int occ = cv ? march_cv_occupancy(mode, threads, mom) : march_occupancy(mode, threads);
     const int blocks = std::max(1, sms * occ);
-    CUDA_TRY(cudaEventRecord(s->ev_march0, s->stream));
-    int rc = cv ? launch_march_cv(mode, P, blocks, threads, s->stream, false, mom)
-                : launch_march(mode, P, blocks, threads, s->stream, false);
-    if (rc) return fail(DNSMC_ERR_CUDA, "march launch: %s", cudaGetErrorString((cudaError_t)rc));
-    CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
-    s->last = P;
 
-    FinalizeParams F{};
+    FinalizeParams F;
+    memset(&F, 0, sizeof F);
     F.nfields = s->nfields; F.n_groups = P.n_groups; F.region_cells = P.region_cells;
     F.niR = ni; F.njR = nj; F.nkR = nk;
     F.tile_a = ta; F.tile_b = tb; F.npa = npa; F.npb = npb;
@@ -981,13 +968,74 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     TRY(s->d_varg.ensure(nout * P.n_groups));
     F.Q = s->d_Q.p; F.var = s->d_var.p; F.Qg = s->d_Qg.p; F.varg = s->d_varg.p;
     F.status = P.status;
-    rc = launch_finalize(F, s->stream);
-    if (rc) return fail(DNSMC_ERR_CUDA, "finalize launch: %s", cudaGetErrorString((cudaError_t)rc));
-    s->lastF = F;
     TRY(s->h_Q.ensure(nout));
     TRY(s->h_var.ensure(nout));
-    CUDA_TRY(cudaMemcpyAsync(s->h_Q.p, s->d_Q.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-    CUDA_TRY(cudaMemcpyAsync(s->h_var.p, s->d_var.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+
+    // ---- the kernel sequence of a solve (stream-ordered; capturable) -------
+    auto kernels = [&](bool events) -> int {
+        if (mode != MODE_GREY) {
+            // table coordinates of the field for this table (once per solve)
+            const int rcp = mode == MODE_TX
+                                ? launch_field_pos(nullptr, s->d_fieldTX.p, nullptr, s->d_posTX.p, ncell, P.T0,
+                                                   P.invdT, P.nT, P.X0, P.invdX, P.nX, s->stream)
+                                : launch_field_pos(s->d_fieldT.p, nullptr, s->d_posT.p, nullptr, ncell, P.T0, P.invdT,
+                                                   P.nT, P.X0, P.invdX, P.nX, s->stream);
+            if (rcp) return fail(DNSMC_ERR_CUDA, "coordinate launch: %s", cudaGetErrorString((cudaError_t)rcp));
+        }
+        if (cv) {
+            int rc = launch_cv_prepare(cp, s->stream);
+            if (rc == 0) rc = launch_cv_mean(cp, s->stream);
+            if (rc) return fail(DNSMC_ERR_CUDA, "control-variate launch: %s", cudaGetErrorString((cudaError_t)rc));
+        }
+        CUDA_TRY(cudaMemsetAsync(s->d_misc.p, 0, 4 * sizeof(unsigned int), s->stream));
+        CUDA_TRY(cudaMemsetAsync(s->d_counters.p, 0, 2 * sizeof(unsigned long long), s->stream));
+        if (events) CUDA_TRY(cudaEventRecord(s->ev_march0, s->stream));
+        int rc = cv ? launch_march_cv(mode, P, blocks, threads, s->stream, false, mom)
+                    : launch_march(mode, P, blocks, threads, s->stream, false);
+        if (rc) return fail(DNSMC_ERR_CUDA, "march launch: %s", cudaGetErrorString((cudaError_t)rc));
+        if (events) CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
+        rc = launch_finalize(F, s->stream);
+        if (rc) return fail(DNSMC_ERR_CUDA, "finalize launch: %s", cudaGetErrorString((cudaError_t)rc));
+        CUDA_TRY(cudaMemcpyAsync(s->h_Q.p, s->d_Q.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(s->h_var.p, s->d_var.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        return DNSMC_OK;
+    };
+
+    if (!s->graph_on) {
+        TRY(kernels(true));
+    } else {
+        // Replay the captured sequence when every parameter it baked in is
+        // unchanged; otherwise capture it again.  The march timing then
+        // brackets the whole graph.
+        std::vector<unsigned char> key(sizeof P + sizeof cp + sizeof F + 4 * sizeof(long long));
+        unsigned char *k = key.data();
+        memcpy(k, &P, sizeof P); k += sizeof P;
+        memcpy(k, &cp, sizeof cp); k += sizeof cp;
+        memcpy(k, &F, sizeof F); k += sizeof F;
+        const long long extra[4] = {blocks, threads, (long long)(cv ? 1 : 0) | (mom ? 2 : 0) | ((long long)mode << 2),
+                                    (long long)(uintptr_t)s->stream};
+        memcpy(k, extra, sizeof extra);
+        if (!s->graph_exec || key != s->graph_key) {
+            if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed));
+            const int rc = kernels(false);
+            const cudaError_t ec = cudaStreamEndCapture(s->stream, &g);
+            if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+            if (ec != cudaSuccess) return fail(DNSMC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ec));
+            const cudaError_t ei = cudaGraphInstantiate(&s->graph_exec, g, 0);
+            cudaGraphDestroy(g);
+            if (ei != cudaSuccess) { s->graph_exec = nullptr; return fail(DNSMC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei)); }
+            s->graph_key = key;
+            s->graph_captures += 1;
+        }
+        CUDA_TRY(cudaEventRecord(s->ev_march0, s->stream));
+        CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
+        CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
+        s->graph_launches += 1;
+    }
+    s->last = P;
+    s->lastF = F;
     CUDA_TRY(cudaEventRecord(s->ev_done, s->stream));
     s->in_flight = true;
     s->solved = true;
@@ -1247,12 +1295,13 @@ int dnsmc_destroy(dnsmc_solver *s) {
     if (!s->dev_ready) { delete s; return DNSMC_OK; }
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     s->d_fw.release(); s->d_k.release(); s->d_ib.release(); s->d_ibw.release();
     s->d_kpair.release(); s->d_ibpair.release(); s->d_posT.release(); s->d_posTX.release();
     s->d_cv_grp.release(); s->d_cv_sid.release(); s->d_cv_C.release(); s->d_layer.release();
     s->d_sur.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();
-    s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_item_steps.release();
+    s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_item_steps.release(); s->d_kP.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
     s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_Qg.release(); s->d_varg.release();
     s->h_Q.release(); s->h_var.release(); s->d_misc.release(); s->d_counters.release();
@@ -1471,6 +1520,96 @@ int dnsmc_set_rays_per_item(dnsmc_solver *s, int n_groups, const int *rays) {
     return DNSMC_OK;
 }
 
+int dnsmc_set_graph(dnsmc_solver *s, int enable) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    TRY(wait_done(s, 0));
+    s->graph_on = enable != 0;
+    if (!s->graph_on && s->graph_exec) {
+        TRY(set_device(s));
+        cudaGraphExecDestroy(s->graph_exec);
+        s->graph_exec = nullptr;
+        s->graph_key.clear();
+    }
+    return DNSMC_OK;
+}
+
+int dnsmc_get_graph_info(const dnsmc_solver *s, long long *captures, long long *launches) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (captures) *captures = s->graph_captures;
+    if (launches) *launches = s->graph_launches;
+    return DNSMC_OK;
+}
+
+int dnsmc_set_rays_adaptive(dnsmc_solver *s, float rays_per_tau, int min_rays, int max_rays) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    const dnsmc_config &c = s->cfg;
+    const int B = c.sampler == DNSMC_SAMPLER_RQMC ? c.nvar : 1;
+    if (!(rays_per_tau > 0) || min_rays < std::max(2, B) || max_rays < min_rays || min_rays % B || max_rays % B)
+        return fail(DNSMC_ERR_ARG, "need rays_per_tau > 0 and max(2, nvar) <= min_rays <= max_rays, multiples of nvar");
+    if (s->nfields < 1) return fail(DNSMC_ERR_STATE, "no fields: call dnsmc_set_fields first");
+    if (c.model != DNSMC_MODEL_GREY && !s->tab.valid && !s->tab.grey_bands)
+        return fail(DNSMC_ERR_STATE, "no tables: load or set tables first");
+    TRY(set_device(s));
+    TRY(wait_done(s, 0));
+    AdaptParams A;
+    memset(&A, 0, sizeof A);
+    const HostTable &t = s->tab;
+    int mode = MODE_GREY;
+    if (c.model != DNSMC_MODEL_GREY) {
+        if (s->tab.grey_bands) {
+            const float Tmax = std::max(s->tmax_fields, std::max(c.T_west, c.T_east));
+            build_grey_band_tables(s->tab, Tmax);
+            s->tables_dirty = true;
+        }
+        if (s->tables_dirty) TRY(upload_tables(s));
+        mode = t.nX > 1 ? MODE_TX : MODE_T;
+        // Planck-mean absorption coefficient on the table grid:
+        // kP(T, x) = pi sum_b sum_g w_g k_bg(T, x) Ib_b(T) dnu_b / (sigma T^4)
+        std::vector<float> kp((size_t)t.nT * t.nX);
+        const int nq = std::max(1, t.nq);
+        for (int ti = 0; ti < t.nT; ++ti) {
+            const double T = t.T0 + ti * (double)t.dT;
+            const double den = kSigma * T * T * T * T;
+            for (int xi = 0; xi < t.nX; ++xi) {
+                double acc = 0.0;
+                for (int b = 0; b < t.nbands; ++b) {
+                    const double ib = t.Ib[(size_t)b * t.nT + ti] * (double)t.dnu[b] * 100.0;
+                    const float *kb = t.k.data() + (size_t)b * nq * t.nT * t.nX;
+                    for (int g = 0; g < nq; ++g)
+                        acc += (double)(t.wq.empty() ? 1.0f : t.wq[g]) *
+                               kb[((size_t)g * t.nT + ti) * t.nX + xi] * ib;
+                }
+                kp[(size_t)ti * t.nX + xi] = den > 0 ? (float)(kPi * acc / den) : 0.0f;
+            }
+        }
+        TRY(s->d_kP.ensure(kp.size()));
+        CUDA_TRY(cudaMemcpyAsync(s->d_kP.p, kp.data(), kp.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(cudaStreamSynchronize(s->stream));
+        A.kP = s->d_kP.p;
+        A.nT = t.nT; A.nX = t.nX;
+        A.T0 = t.T0; A.invdT = 1.0f / t.dT; A.X0 = t.X0; A.invdX = 1.0f / t.dX;
+    }
+    int ni, nj, nk, ta, tb, npa, npb, npw;
+    region_dims(s, &ni, &nj, &nk);
+    tiling(s, &ta, &tb, &npa, &npb, &npw);
+    const int np = npa * npb * npw;
+    TRY(s->d_rays_pp.ensure((size_t)np));
+    A.nfields = s->nfields; A.nw = c.imax; A.na = c.jmax; A.nb = c.kmax; A.mode = mode;
+    A.fT = s->d_fieldT.p; A.fTX = s->d_fieldTX.p; A.fw = s->d_fw.p; A.da = s->da; A.db = s->db;
+    A.ew0 = s->r_i0; A.ea0 = s->r_j0; A.eb0 = s->r_k0; A.njR = nj; A.nkR = nk;
+    A.tile_a = ta; A.tile_b = tb; A.npa = npa; A.npb = npb; A.n_packets = np;
+    A.field_stride = (long long)c.imax * c.jmax * c.kmax;
+    A.kappa = c.kappa;
+    A.per_tau = rays_per_tau; A.B = B; A.nmin = min_rays; A.nmax = max_rays;
+    A.rays = s->d_rays_pp.p;
+    const int rc = launch_adaptive_rays(A, s->stream);
+    if (rc) return fail(DNSMC_ERR_CUDA, "adaptive rays launch: %s", cudaGetErrorString((cudaError_t)rc));
+    s->rays_pp.clear();
+    s->rays_pg = 0;
+    s->rays_dev = true;
+    return DNSMC_OK;
+}
+
 int dnsmc_get_stream(dnsmc_solver *s, void **stream) {
     if (!s || !stream) return fail(DNSMC_ERR_ARG, "null argument");
     TRY(set_device(s));
@@ -1481,11 +1620,18 @@ int dnsmc_get_stream(dnsmc_solver *s, void **stream) {
 int dnsmc_get_rays_per_item(dnsmc_solver *s, int *n_groups, int *rays) {
     if (!s || !n_groups) return fail(DNSMC_ERR_ARG, "null argument");
     TRY(wait_done(s, 0));
-    *n_groups = (s->rays_pp.empty() && !s->rays_dev) ? 0 : s->rays_pg;
+    // -1: one row of per-packet counts shared by all band groups
+    *n_groups = (s->rays_pp.empty() && !s->rays_dev) ? 0 : (s->rays_pg > 0 ? s->rays_pg : -1);
     if (!rays || *n_groups == 0) return DNSMC_OK;
     int np;
     TRY(dnsmc_packet_count(s, &np));
-    CUDA_TRY(cudaMemcpy(rays, s->d_rays_pp.p, (size_t)*n_groups * np * sizeof(int), cudaMemcpyDeviceToHost));
+    const size_t rows = *n_groups > 0 ? (size_t)*n_groups : 1;
+    if (s->rays_dev) {
+        TRY(set_device(s));
+        CUDA_TRY(cudaMemcpy(rays, s->d_rays_pp.p, rows * np * sizeof(int), cudaMemcpyDeviceToHost));
+    } else {
+        memcpy(rays, s->rays_pp.data(), rows * np * sizeof(int));
+    }
     return DNSMC_OK;
 }
 

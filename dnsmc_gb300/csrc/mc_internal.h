@@ -137,6 +137,26 @@ int solver_beta_device(dnsmc_solver *s, float2 **beta, long long *n);
 // Device buffer of per-(group, packet) ray counts that the next solve uses.
 int solver_rays_device(dnsmc_solver *s, int n_groups, int **rays);
 
+// Rays per packet proportional to the packet's mean cell optical thickness
+// kP(T, x) (dx dy dz)^(1/3), clamped and rounded to multiples of B.
+struct AdaptParams {
+    int nfields, nw, na, nb, mode;
+    const float *fT;
+    const float2 *fTX;
+    const float *fw;
+    float da, db;
+    int ew0, ea0, eb0, njR, nkR, tile_a, tile_b, npa, npb, n_packets;
+    long long field_stride;
+    const float *kP;          // [nT][nX] Planck-mean absorption coefficient (null: grey kappa)
+    int nT, nX;
+    float T0, invdT, X0, invdX;
+    float kappa;
+    float per_tau;
+    int B, nmin, nmax;
+    int *rays;                // [packet]
+};
+int launch_adaptive_rays(const AdaptParams &a, void *stream);
+
 // launchers (mc_kernels.cu); all stream-ordered
 int launch_march(int mode, const MarchParams &p, int blocks, int threads,
                  void *stream, bool trace);

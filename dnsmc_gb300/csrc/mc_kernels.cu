@@ -967,6 +967,64 @@ __global__ void cv_mean_kernel(const CvParams c) {
     }
 }
 
+// One warp per packet: lanes are the packet's cells.
+__global__ void adaptive_rays_kernel(const AdaptParams A) {
+    const int lane = threadIdx.x & 31;
+    const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const long long nwarp = ((long long)gridDim.x * blockDim.x) >> 5;
+    const long long plane = (long long)A.na * A.nb;
+    for (long long p = wid; p < A.n_packets; p += nwarp) {
+        const int pa = (int)(p % A.npa);
+        const long long rest = p / A.npa;
+        const int pb = (int)(rest % A.npb), pw = (int)(rest / A.npb);
+        const int jR = pa * A.tile_a + lane % A.tile_a, kR = pb * A.tile_b + lane / A.tile_a;
+        float tsum = 0.0f, cnt = 0.0f;
+        if (jR < A.njR && kR < A.nkR) {
+            const int i = A.ew0 + pw;
+            const float h = cbrtf((A.fw[i + 1] - A.fw[i]) * A.da * A.db);
+            for (int f = 0; f < A.nfields; ++f) {
+                const long long cell = f * A.field_stride + i * plane + (long long)(A.eb0 + kR) * A.na + (A.ea0 + jR);
+                float kp = A.kappa;
+                if (A.kP) {
+                    int ti, xi = 0;
+                    float ft, fx = 0.0f;
+                    if (A.mode == MODE_TX) {
+                        const float2 v = A.fTX[cell];
+                        grid_pos(v.x, A.T0, A.invdT, A.nT, &ti, &ft);
+                        grid_pos(v.y, A.X0, A.invdX, A.nX, &xi, &fx);
+                    } else {
+                        grid_pos(A.fT[cell], A.T0, A.invdT, A.nT, &ti, &ft);
+                    }
+                    const float *k = A.kP + ti * A.nX + xi;
+                    const float dx = (A.nX > 1) ? 1.0f : 0.0f;
+                    const float k00 = k[0], k01 = A.nX > 1 ? k[1] : k[0];
+                    const float k10 = k[A.nX], k11 = A.nX > 1 ? k[A.nX + 1] : k[A.nX];
+                    const float a0 = k00 + fx * dx * (k01 - k00), a1 = k10 + fx * dx * (k11 - k10);
+                    kp = a0 + ft * (a1 - a0);
+                }
+                tsum += kp * h;
+                cnt += 1.0f;
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            tsum += __shfl_xor_sync(0xffffffffu, tsum, o);
+            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+        }
+        if (lane == 0) {
+            const float x = A.per_tau * (cnt > 0.0f ? tsum / cnt : 0.0f);
+            int r = (int)rintf(x / (float)A.B) * A.B;
+            r = min(max(r, A.nmin), A.nmax);
+            A.rays[p] = r;
+        }
+    }
+}
+
+int launch_adaptive_rays(const AdaptParams &a, void *stream) {
+    const long long threads = (long long)a.n_packets * 32;
+    adaptive_rays_kernel<<<grid_for(threads, 256), 256, 0, (cudaStream_t)stream>>>(a);
+    return (int)cudaGetLastError();
+}
+
 int launch_cv_prepare(const CvParams &c, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     cv_layer_kernel<<<dim3(c.nw, c.nfields), 256, 0, st>>>(c);

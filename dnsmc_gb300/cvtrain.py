@@ -25,12 +25,12 @@ REPLICATES = 4
 
 
 def ck_solver(table, n: int, T_wall: float, seed: int, *, moments: bool = False, groups: int = GROUPS,
-              nvar: int = REPLICATES, cv: bool = True, threads: int = 128) -> Solver:
+              nvar: int = REPLICATES, cv: bool = True, threads: int = 128, tile_a: int = 0) -> Solver:
     """Solver of the correlated-k channel workload (x, z periodic 2 pi x pi,
     y walls black at T_wall, RQMC rays, sampling at the packet temperature)."""
     cfg = default_config(model=_lib.MODEL_TABLE, imax=n, jmax=n, kmax=n, Lx=2.0, Ly=2 * math.pi, Lz=math.pi,
                          stretched_x=0, T_west=T_wall, T_east=T_wall, n_groups=groups, seed=seed,
-                         block_threads=threads, sampler=_lib.SAMPLER_RQMC, local_sampling=1, nvar=nvar,
+                         block_threads=threads, tile_a=tile_a, sampler=_lib.SAMPLER_RQMC, local_sampling=1, nvar=nvar,
                          control_variate=1 if cv else 0, cv_moments=1 if (moments and cv) else 0)
     s = Solver(cfg)
     s.set_table(table["k"], table["wvc"], table["T0"], table["dT"], dnu=table["dnu"], wq=table["wq"],

@@ -204,9 +204,22 @@ int  dnsmc_set_rays(dnsmc_solver *s, int rays_per_group,
  * reference, whose rays per cell are the compile-time photmax
  * (code/param.h:64).                                                         */
 int  dnsmc_set_rays_per_item(dnsmc_solver *s, int n_groups, const int *rays);
+/* Rays per packet proportional to local optical thickness: for every packet
+ * the mean over its cells (and the resident snapshots) of
+ * tau = kP(T, x_H2O) (dx dy dz)^(1/3), kP the Planck-mean absorption
+ * coefficient of the tables (kappa for the grey model), gives
+ * n = clamp(round(rays_per_tau * tau), min_rays, max_rays) rays per cell and
+ * band group, in multiples of nvar under RQMC.  Computed on the device on
+ * the solver's stream from the resident fields; replaced by dnsmc_set_rays,
+ * dnsmc_set_rays_per_item or dnsmc_set_region.  No counterpart in the
+ * reference (photmax rays for every cell, code/param.h:64).                 */
+int  dnsmc_set_rays_adaptive(dnsmc_solver *s, float rays_per_tau, int min_rays,
+                             int max_rays);
 /* The per-item ray table in effect (set by dnsmc_set_rays_per_item or by a
- * control-variate network, dnsmc_cvnet_apply): *n_groups = 0 when rays are
- * uniform or per packet; rays (may be NULL) receives n_groups * npackets.   */
+ * control-variate network, dnsmc_cvnet_apply, or dnsmc_set_rays_adaptive):
+ * *n_groups = 0 when rays are uniform, -1 for one row of per-packet counts
+ * shared by all band groups, else the rows of the per-(group, packet) table;
+ * rays (may be NULL) receives max(1, *n_groups) * npackets counts.          */
 int  dnsmc_get_rays_per_item(dnsmc_solver *s, int *n_groups, int *rays);
 int  dnsmc_packet_count(const dnsmc_solver *s, int *npackets);
 /* Enqueue a solve of every resident snapshot on the solver's stream and return.*/
@@ -219,6 +232,18 @@ int  dnsmc_wait(dnsmc_solver *s, double timeout_s);
 int  dnsmc_get_results(dnsmc_solver *s, double *Q, double *sigma);
 /* Per band group: mean and variance of the mean, [field][group][cell].         */
 int  dnsmc_get_group_results(dnsmc_solver *s, double *Qg, double *varg);
+/* CUDA graph replay of the solve: when enabled, the kernel sequence of a
+ * solve (table coordinates, control-variate preparation, the persistent
+ * march, finalize and the result copy) is captured once into a CUDA graph
+ * and replayed by later solves whose launch parameters are unchanged (same
+ * grid, region, ray layout, tables and buffers; the field values, ray counts
+ * and coefficients in device memory may change).  A change of any of them
+ * captures again.  The march timing of dnsmc_get_timing then covers the whole
+ * replayed sequence.                                                        */
+int  dnsmc_set_graph(dnsmc_solver *s, int enable);
+/* Number of graph captures and replays so far.                              */
+int  dnsmc_get_graph_info(const dnsmc_solver *s, long long *captures,
+                          long long *launches);
 /* The solver's CUDA stream (cudaStream_t; created on first use): every solve,
  * upload and network evaluation of this solver is ordered on it, so a caller
  * can order its own work (or CUDA events) against them.                      */
