@@ -97,6 +97,8 @@ SIGNATURES = {
     "dnsmc_get_graph_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
                                             ctypes.POINTER(ctypes.c_longlong)]),
     "dnsmc_set_rays_adaptive": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_int, ctypes.c_int]),
+    "dnsmc_set_particles": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_float_p, c_float_p, ctypes.c_float]),
+    "dnsmc_set_particle_field": (ctypes.c_int, [ctypes.c_void_p, c_float_p, ctypes.c_int]),
     "dnsmc_cvnet_default_config": (None, [ctypes.POINTER(CvNetConfig)]),
     "dnsmc_cvnet_create": (ctypes.c_int, [ctypes.POINTER(CvNetConfig), ctypes.POINTER(ctypes.c_void_p)]),
     "dnsmc_cvnet_destroy": (ctypes.c_int, [ctypes.c_void_p]),

@@ -73,6 +73,8 @@ class Solver:
         self._rays = cfg.nvar * cfg.photmax
         self._rays_dev = False
         self._beta = None
+        self._part = None
+        self._hg = 0.0
 
     # -- lifetime -----------------------------------------------------------
     def close(self) -> None:
@@ -153,6 +155,23 @@ class Solver:
             X = np.ascontiguousarray(x, dtype=np.float32).reshape(T.shape)
         check(self._lib.dnsmc_set_fields(self._h, T.shape[0], _fp(T), _fp(X), layout))
         self._nfields = T.shape[0]
+
+    def set_particles(self, absorption, scattering, hg_g: float = 0.0) -> None:
+        """Per-band absorption / scattering per unit volume fraction [1/m]
+        (None, None removes the particles)."""
+        if absorption is None and scattering is None:
+            check(self._lib.dnsmc_set_particles(self._h, 0, None, None, 0.0))
+            self._part = None
+            return
+        a = np.ascontiguousarray(absorption, np.float32)
+        sc = np.ascontiguousarray(scattering, np.float32)
+        check(self._lib.dnsmc_set_particles(self._h, a.size, _fp(a), _fp(sc), float(hg_g)))
+        self._part = np.stack([a, sc], 1)
+        self._hg = float(hg_g)
+
+    def set_particle_field(self, fv, layout: int = _lib.LAYOUT_DENSE) -> None:
+        v = np.ascontiguousarray(fv, dtype=np.float32)
+        check(self._lib.dnsmc_set_particle_field(self._h, _fp(v), layout))
 
     def set_region(self, i0, i1, j0, j1, k0, k1) -> None:
         check(self._lib.dnsmc_set_region(self._h, i0, i1, j0, j1, k0, k1))

@@ -57,6 +57,8 @@ def build(verbose: bool = False) -> str:
          "-o", os.path.join(bdir, "mc_kernels.o")],
         [nvcc, *common, "-x", "c++", "-c", os.path.join(CSRC, "mc_host.cpp"),
          "-o", os.path.join(bdir, "mc_host.o")],
+        [nvcc, *ARCH, *common, *regs, "-fmad=false", "-c", os.path.join(CSRC, "mc_march_gen.cu"),
+         "-o", os.path.join(bdir, "mc_march_gen.o")],
         [nvcc, *ARCH, *common, "-c", os.path.join(CSRC, "mc_noalloc.cu"),
          "-o", os.path.join(bdir, "mc_noalloc.o")],
         [nvcc, *ARCH, *common, "-c", os.path.join(CSRC, "mc_cvnet.cu"),
@@ -68,7 +70,8 @@ def build(verbose: bool = False) -> str:
     tmp = out + ".tmp"
     _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-Xcompiler", "-fPIC",
           os.path.join(bdir, "mc_kernels.o"), os.path.join(bdir, "mc_host.o"),
-          os.path.join(bdir, "mc_noalloc.o"), os.path.join(bdir, "mc_cvnet.o"), "-o", tmp])
+          os.path.join(bdir, "mc_noalloc.o"), os.path.join(bdir, "mc_cvnet.o"), os.path.join(bdir, "mc_march_gen.o"),
+          "-o", tmp])
     os.replace(tmp, out)
     if verbose:
         print("built", out)

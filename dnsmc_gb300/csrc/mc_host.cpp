@@ -276,6 +276,16 @@ struct dnsmc_solver {
     DevBuf<unsigned long long> d_item_steps; // steps per (field, group, packet) of the last solve
     DevBuf<float> d_kP;                      // Planck-mean absorption coefficient on the table grid
 
+    // particles (general medium): per-band coefficients per unit volume
+    // fraction and the volume-fraction field of the resident snapshots
+    std::vector<float2> part;
+    float hg_g = 0.f;
+    DevBuf<float2> d_part;
+    DevBuf<float> d_fieldV, d_layerV;
+    int fv_fields = 0;
+    float fv_max = 0.f;
+    double fv_mean = 0.0;
+
     // sampling of the last solve
     float tmax_used = 0.f;
     std::vector<SpecEntry> entries;
@@ -378,8 +388,8 @@ int check_config(const dnsmc_config &c) {
         return fail(DNSMC_ERR_ARG, "block_threads must be 0, 128 or 256");
     if (c.tile_a && c.tile_a != 8 && c.tile_a != 16 && c.tile_a != 32)
         return fail(DNSMC_ERR_ARG, "tile_a must be 0, 8, 16 or 32");
-    if (!(c.eps_west == 1.0f) || !(c.eps_east == 1.0f))
-        return fail(DNSMC_ERR_ARG, "grey walls (eps < 1) are not supported by this solver build");
+    if (!(c.eps_west > 0.0f && c.eps_west <= 1.0f) || !(c.eps_east > 0.0f && c.eps_east <= 1.0f))
+        return fail(DNSMC_ERR_ARG, "wall emissivities must be in (0, 1]");
     if (!(c.T_west >= 0) || !(c.T_east >= 0)) return fail(DNSMC_ERR_ARG, "wall temperatures must be >= 0");
     return DNSMC_OK;
 }
@@ -688,7 +698,8 @@ int build_sampling(dnsmc_solver *s, float Tmax, float xm) {
         for (int b = 0; b < nB; ++b)
             for (int g = 0; g < nQ; ++g) {
                 const size_t s_ = (size_t)b * nQ + g;
-                q[s_] = C[s_] > 0 ? C[s_] * k_at(t, b, g, Tbins[ib], xm) * ib_at(t, b, Tbins[ib]) : 0.0;
+                const double kp = s->part.empty() ? 0.0 : s->fv_mean * (double)s->part[(size_t)b].x;
+                q[s_] = C[s_] > 0 ? C[s_] * (k_at(t, b, g, Tbins[ib], xm) + kp) * ib_at(t, b, Tbins[ib]) : 0.0;
                 if (C[s_] > 0) { mean += q[s_]; ++npos; }
             }
         mean /= std::max(1, npos);
@@ -846,6 +857,17 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.Wgrey = (float)(4.0 * c.kappa * kSigma);
     P.Tw4[0] = c.T_west * c.T_west * c.T_west * c.T_west;
     P.Tw4[1] = c.T_east * c.T_east * c.T_east * c.T_east;
+    // general medium: particles (with their field) and/or grey walls
+    const bool have_part = !s->part.empty();
+    if (have_part && s->fv_fields != s->nfields)
+        return fail(DNSMC_ERR_STATE, "particles set: set the particle field of the %d resident snapshots", s->nfields);
+    const bool gen = have_part || c.eps_west < 1.0f || c.eps_east < 1.0f;
+    P.fieldV = have_part ? s->d_fieldV.p : nullptr;
+    P.part = have_part ? s->d_part.p : nullptr;
+    P.fv_max = have_part ? s->fv_max : 0.0f;
+    P.hg_g = s->hg_g;
+    P.eps[0] = c.eps_west; P.eps[1] = c.eps_east;
+    P.W4sig = (float)(4.0 * kSigma);
     P.rays = s->rays;
     const bool per_item = !s->rays_pp.empty() || s->rays_dev;
     P.rays_per_packet = per_item ? s->d_rays_pp.p : nullptr;
@@ -887,8 +909,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         P.trace_f = tf; P.trace_g = tg; P.trace_p = tp; P.trace_r = tr; P.trace_max = tmax_steps;
         P.trace_rec = d_trace_rec; P.trace_n = d_trace_n; P.trace_rng = d_trace_rng;
         P.tally = nullptr;
-        const int rc = cv ? launch_march_cv(mode, P, 1, 32, s->stream, true, false)
-                          : launch_march(mode, P, 1, 32, s->stream, true);
+        const int rc = launch_march_ex(mode, P, 1, 32, s->stream, true, cv, false, gen);
         if (rc) return fail(DNSMC_ERR_CUDA, "trace launch: %s", cudaGetErrorString((cudaError_t)rc));
         return DNSMC_OK;
     }
@@ -934,6 +955,12 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         cp.ew0 = P.ew0; cp.ew1 = P.ew1; cp.ea0 = P.ea0; cp.ea1 = P.ea1; cp.eb0 = P.eb0; cp.eb1 = P.eb1;
         cp.region_cells = P.region_cells;
         cp.muY = s->d_muY.p;
+        if (have_part) {
+            TRY(s->d_layerV.ensure((size_t)s->nfields * c.imax));
+            cp.fieldV = s->d_fieldV.p;
+            cp.part = s->d_part.p;
+            cp.layerV = s->d_layerV.p;
+        }
         s->cv_samples = S;
         P.sur = s->d_sur.p;
         if (mom) {
@@ -946,7 +973,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     TRY(s->d_item_steps.ensure((size_t)P.n_items));
     P.item_steps = s->d_item_steps.p;
     const int sms = device_sm_count();
-    const int occ = cv ? march_cv_occupancy(mode, threads, mom) : march_occupancy(mode, threads);
+    const int occ = march_occupancy_ex(mode, threads, cv, mom, gen);
     const int blocks = std::max(1, sms * occ);
 
     FinalizeParams F;
@@ -990,8 +1017,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         CUDA_TRY(cudaMemsetAsync(s->d_misc.p, 0, 4 * sizeof(unsigned int), s->stream));
         CUDA_TRY(cudaMemsetAsync(s->d_counters.p, 0, 2 * sizeof(unsigned long long), s->stream));
         if (events) CUDA_TRY(cudaEventRecord(s->ev_march0, s->stream));
-        int rc = cv ? launch_march_cv(mode, P, blocks, threads, s->stream, false, mom)
-                    : launch_march(mode, P, blocks, threads, s->stream, false);
+        int rc = launch_march_ex(mode, P, blocks, threads, s->stream, false, cv, mom, gen);
         if (rc) return fail(DNSMC_ERR_CUDA, "march launch: %s", cudaGetErrorString((cudaError_t)rc));
         if (events) CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
         rc = launch_finalize(F, s->stream);
@@ -1302,6 +1328,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_sur.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();
     s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_item_steps.release(); s->d_kP.release();
+    s->d_part.release(); s->d_fieldV.release(); s->d_layerV.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
     s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_Qg.release(); s->d_varg.release();
     s->h_Q.release(); s->h_var.release(); s->d_misc.release(); s->d_counters.release();
@@ -1448,6 +1475,84 @@ int dnsmc_set_fields_device(dnsmc_solver *s, int nfields, const float *dT, const
     s->tmax_fields = st[0];
     s->tmin_fields = st[1];
     s->xsum = st[2];
+    return DNSMC_OK;
+}
+
+int dnsmc_set_particles(dnsmc_solver *s, int nbands, const float *absorption, const float *scattering, float hg_g) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    TRY(wait_done(s, 0));
+    if (!absorption && !scattering) {
+        s->part.clear();
+        s->fv_fields = 0;
+        return DNSMC_OK;
+    }
+    const dnsmc_config &c = s->cfg;
+    if (c.model != DNSMC_MODEL_GREY && c.model != DNSMC_MODEL_TABLE)
+        return fail(DNSMC_ERR_ARG, "particles need the grey model or raw k tables (dnsmc_set_table)");
+    const int nb = c.model == DNSMC_MODEL_GREY ? 1 : s->tab.nbands;
+    if (c.model == DNSMC_MODEL_TABLE && !s->tab.valid) return fail(DNSMC_ERR_STATE, "set the k table before the particles");
+    if (nbands != nb) return fail(DNSMC_ERR_ARG, "particle table has %d bands, the spectral model %d", nbands, nb);
+    if (!(hg_g > -1.0f && hg_g < 1.0f)) return fail(DNSMC_ERR_ARG, "Henyey-Greenstein g must be in (-1, 1)");
+    std::vector<float2> pp((size_t)nb);
+    for (int b = 0; b < nb; ++b) {
+        const float a = absorption ? absorption[b] : 0.0f, sc = scattering ? scattering[b] : 0.0f;
+        if (!(a >= 0.0f) || !(sc >= 0.0f) || !std::isfinite(a) || !std::isfinite(sc))
+            return fail(DNSMC_ERR_ARG, "particle coefficients must be finite and >= 0");
+        pp[(size_t)b] = make_float2(a, sc);
+    }
+    TRY(set_device(s));
+    TRY(s->d_part.ensure(pp.size()));
+    CUDA_TRY(cudaMemcpy(s->d_part.p, pp.data(), pp.size() * sizeof(float2), cudaMemcpyHostToDevice));
+    s->part = pp;
+    s->hg_g = hg_g;
+    return DNSMC_OK;
+}
+
+int dnsmc_set_particle_field(dnsmc_solver *s, const float *fv, int layout) {
+    if (!s || !fv) return fail(DNSMC_ERR_ARG, "null argument");
+    if (s->nfields < 1) return fail(DNSMC_ERR_STATE, "set the temperature fields first");
+    const dnsmc_config &c = s->cfg;
+    const long long ncell = (long long)c.imax * c.jmax * c.kmax;
+    long long sj, sk, base, nsrc;
+    if (layout == DNSMC_LAYOUT_DENSE) {
+        sj = c.imax; sk = (long long)c.imax * c.jmax; base = 0; nsrc = ncell;
+    } else if (layout == DNSMC_LAYOUT_FORTRAN) {
+        sj = c.imax + 2; sk = (long long)(c.imax + 2) * (c.jmax + 2);
+        base = 1 + sj + sk;
+        nsrc = (long long)(c.imax + 2) * (c.jmax + 2) * (c.kmax + 2);
+    } else {
+        return fail(DNSMC_ERR_ARG, "unknown layout %d", layout);
+    }
+    float vmax = 0.0f;
+    double vsum = 0.0;
+    for (int f = 0; f < s->nfields; ++f)
+        for (int k = 0; k < c.kmax; ++k)
+            for (int j = 0; j < c.jmax; ++j) {
+                const long long o = f * nsrc + base + j * sj + k * sk;
+                for (int i = 0; i < c.imax; ++i) {
+                    const float v = fv[o + i];
+                    if (!(v >= 0.0f) || !std::isfinite(v)) return fail(DNSMC_ERR_ARG, "volume fractions must be finite and >= 0");
+                    vmax = std::max(vmax, v);
+                    vsum += v;
+                }
+            }
+    TRY(set_device(s));
+    TRY(wait_done(s, 0));
+    TRY(s->h_stage.ensure((size_t)nsrc));
+    TRY(s->d_raw.ensure((size_t)nsrc));
+    TRY(s->d_fieldV.ensure((size_t)s->nfields * ncell));
+    for (int f = 0; f < s->nfields; ++f) {
+        CUDA_TRY(cudaStreamSynchronize(s->stream));  // staging reuse
+        memcpy(s->h_stage.p, fv + f * nsrc, nsrc * sizeof(float));
+        CUDA_TRY(cudaMemcpyAsync(s->d_raw.p, s->h_stage.p, nsrc * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        const int rc = launch_pack_T(s->d_raw.p, s->d_fieldV.p + f * ncell, c.imax, c.jmax, c.kmax, 1, sj, sk, base,
+                                     s->stream);
+        if (rc) return fail(DNSMC_ERR_CUDA, "pack launch: %s", cudaGetErrorString((cudaError_t)rc));
+    }
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    s->fv_fields = s->nfields;
+    s->fv_max = vmax;
+    s->fv_mean = vsum / ((double)s->nfields * ncell);
     return DNSMC_OK;
 }
 

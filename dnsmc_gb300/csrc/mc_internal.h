@@ -67,6 +67,13 @@ struct MarchParams {
     uint32_t field_base;      // field index offset for the RNG counter
     float toll;
     float dtoll;              // ln(1/toll): optical-depth cut-off of the surrogate walk
+    // general medium (GEN march): particles and grey walls
+    const float *fieldV;      // [f][i][k][j] particle volume fraction, or null
+    const float2 *part;       // [band] (absorption, scattering) per unit volume fraction [1/m], or null
+    float fv_max;             // largest volume fraction of the fields (collision majorant)
+    float hg_g;               // Henyey-Greenstein asymmetry factor
+    float eps[2];             // wall emissivities (west, east)
+    float W4sig;              // 4 sigma (grey model weight per unit absorption coefficient)
     int max_steps;
     // work queue and outputs
     unsigned int *queue;      // atomic item counter (zeroed per launch)
@@ -158,6 +165,13 @@ struct AdaptParams {
 int launch_adaptive_rays(const AdaptParams &a, void *stream);
 
 // launchers (mc_kernels.cu); all stream-ordered
+int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
+                    bool mom, bool gen);
+int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen);
+int launch_march_gen(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
+                     bool mom);                                      // mc_march_gen.cu
+int march_gen_occupancy(int mode, int threads, bool cv, bool mom);    // mc_march_gen.cu
+int upload_sobol_dirs_gen(const uint32_t dirs[4][32]);               // mc_march_gen.cu
 int launch_march(int mode, const MarchParams &p, int blocks, int threads,
                  void *stream, bool trace);
 int launch_finalize(const FinalizeParams &p, void *stream);
@@ -209,6 +223,11 @@ struct CvParams {
     int ew0, ew1, ea0, ea1, eb0, eb1;
     long long region_cells;
     double2 *muY;
+    // particles: absorption per unit volume fraction enters k of the cell and
+    // of the layer-mean medium
+    const float *fieldV;      // [f][i][k][j] volume fraction, or null
+    const float2 *part;       // [band] (absorption, scattering) per unit volume fraction
+    float *layerV;            // [f][nw] layer-mean volume fraction
 };
 int launch_cv_prepare(const CvParams &c, void *stream);
 int launch_cv_mean(const CvParams &c, void *stream);

@@ -36,495 +36,9 @@
 // -fmad=false, so the host replay reproduces every ray bit for bit; exp and
 // sin/cos are the project's own polynomial kernels (mc_expm1 / mc_sincos) for
 // the same reason.  Tallies (sum X, sum X^2) are FP64.
-#include <cuda_runtime.h>
-#include <cstdint>
-#include "mc_internal.h"
-#include "../../include/dnsmc.h"
+#include "mc_march.cuh"
 
 namespace dnsmc {
-
-// ---------------------------------------------------------------------------
-// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
-// "Parallel random numbers: as easy as 1, 2, 3", SC'11).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
-#pragma unroll
-    for (int r = 0; r < 10; ++r) {
-        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
-        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
-        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
-        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
-    }
-    return c;
-}
-
-// ---------------------------------------------------------------------------
-// expm1 for x <= 0: Cody-Waite reduction x = n*ln2 + r, |r| <= ln2/2, Taylor
-// series of expm1(r) to r^8/8!, then 2^n*expm1(r) + (2^n - 1).  Only +, *,
-// fmaf and rintf: bit-identical on any IEEE-754 machine.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float mc_expm1(float x) {
-    x = fmaxf(x, -87.0f);
-    const float n = rintf(x * 1.44269504088896341f);
-    float r = fmaf(-n, 0.693145751953125f, x);
-    r = fmaf(-n, 1.42860682030941723212e-6f, r);
-    float p = 2.48015873015873016e-5f;             // 1/8!
-    p = fmaf(p, r, 1.98412698412698413e-4f);       // 1/7!
-    p = fmaf(p, r, 1.38888888888888889e-3f);       // 1/6!
-    p = fmaf(p, r, 8.33333333333333333e-3f);       // 1/5!
-    p = fmaf(p, r, 4.16666666666666667e-2f);       // 1/4!
-    p = fmaf(p, r, 1.66666666666666667e-1f);       // 1/3!
-    p = fmaf(p, r, 0.5f);
-    p = fmaf(p, r, 1.0f);
-    p = p * r;                                     // expm1(r)
-    const int ni = (int)n;                         // in [-126, 0]
-    const float two_n = __int_as_float((ni + 127) << 23);
-    return fmaf(two_n, p, two_n - 1.0f);
-}
-
-// sin and cos of x in [0, pi/4]: Taylor series to x^11 / x^12.
-__device__ __forceinline__ void mc_sincos_oct(float x, float *s, float *c) {
-    const float z = x * x;
-    float ps = -2.50521083854417188e-8f;           // -1/11!
-    ps = fmaf(ps, z, 2.75573192239858907e-6f);     //  1/9!
-    ps = fmaf(ps, z, -1.98412698412698413e-4f);    // -1/7!
-    ps = fmaf(ps, z, 8.33333333333333333e-3f);     //  1/5!
-    ps = fmaf(ps, z, -1.66666666666666667e-1f);    // -1/3!
-    *s = fmaf(ps * z, x, x);
-    float pc = 2.08767569878680990e-9f;            //  1/12!
-    pc = fmaf(pc, z, -2.75573192239858907e-7f);    // -1/10!
-    pc = fmaf(pc, z, 2.48015873015873016e-5f);     //  1/8!
-    pc = fmaf(pc, z, -1.38888888888888889e-3f);    // -1/6!
-    pc = fmaf(pc, z, 4.16666666666666667e-2f);     //  1/4!
-    pc = fmaf(pc, z, -0.5f);
-    *c = fmaf(pc, z, 1.0f);
-}
-
-// cos and sin of 2*pi*m/2^24 for a 24-bit integer m: exact quadrant and
-// octant reduction on the integer, polynomial on [0, pi/4].
-__device__ __forceinline__ void mc_sincos_turn(uint32_t m, float *cs, float *sn) {
-    const uint32_t q = m >> 22;
-    const uint32_t r = m & 0x3FFFFFu;
-    const bool hi = r > 0x200000u;
-    const float th = (float)(hi ? (0x400000u - r) : r) * 3.74507028e-7f;  // pi*2^-23
-    float s, c;
-    mc_sincos_oct(th, &s, &c);
-    const float cq = hi ? s : c, sq = hi ? c : s;
-    float co, si;
-    switch (q) {
-        case 0: co = cq;  si = sq;  break;
-        case 1: co = -sq; si = cq;  break;
-        case 2: co = -cq; si = -sq; break;
-        default: co = sq; si = -cq; break;
-    }
-    *cs = co; *sn = si;
-}
-
-// Sobol' direction numbers of the four sampled dimensions (host-computed).
-__constant__ uint32_t c_sobol[4][32];
-
-__device__ __forceinline__ uint4 sobol4(uint32_t m) {
-    uint32_t a = 0, b = 0, c = 0, d = 0;
-    for (int k = 0; m; ++k, m >>= 1)
-        if (m & 1u) { a ^= c_sobol[0][k]; b ^= c_sobol[1][k]; c ^= c_sobol[2][k]; d ^= c_sobol[3][k]; }
-    return make_uint4(a, b, c, d);
-}
-
-__device__ __forceinline__ float u24(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
-
-// Linear position in a uniform grid of n points, clamped as the reference's
-// clamp-addressed linear-filter textures (code/memory_copy.cu:245-247).
-__device__ __forceinline__ void grid_pos(float v, float v0, float inv, int n, int *i, float *f) {
-    float p = (v - v0) * inv;
-    p = fminf(fmaxf(p, 0.0f), (float)(n - 1));
-    int ii = (int)p;
-    ii = min(ii, n - 2);
-    *i = ii;
-    *f = p - (float)ii;
-}
-
-// Split a clamped table coordinate p in [0, n-1] into cell and fraction.
-__device__ __forceinline__ void pos_split(float p, int n, int *i, float *f) {
-    int ii = (int)p;
-    ii = min(ii, n - 2);
-    *i = ii;
-    *f = p - (float)ii;
-}
-
-// Paired tables: kpair holds (k[t][x], k[t][x+1]) (x-tables) or (k[t], k[t+1])
-// and ibpair (Ib[t], Ib[t+1]), so a bilinear lookup is two 8-byte loads.
-template <int MODE>
-__device__ __forceinline__ float lookup_k(const MarchParams &P, int sid, int ti, float ft, int xi, float fx) {
-    if (MODE == MODE_TX) {
-        const int row = P.nX - 1;
-        const float2 *r = P.kpair + (sid * P.nT + ti) * row + xi;
-        const float2 a = __ldg(r), b = __ldg(r + row);
-        const float k0 = fmaf(fx, a.y - a.x, a.x);
-        const float k1 = fmaf(fx, b.y - b.x, b.x);
-        return fmaf(ft, k1 - k0, k0);
-    } else {
-        const float2 a = __ldg(P.kpair + sid * (P.nT - 1) + ti);
-        return fmaf(ft, a.y - a.x, a.x);
-    }
-}
-
-__device__ __forceinline__ float lookup_ib(const MarchParams &P, int nb, int ti, float ft) {
-    const float2 a = __ldg(P.ibpair + nb * (P.nT - 1) + ti);
-    return fmaf(ft, a.y - a.x, a.x);
-}
-
-// Field element type of the march: T (grey), table T coordinate, or (T, x) coordinates.
-template <int MODE> struct FieldT { typedef float type; };
-template <> struct FieldT<MODE_TX> { typedef float2 type; };
-
-template <int MODE>
-__device__ __forceinline__ typename FieldT<MODE>::type load_field(const MarchParams &P, long long fbase, int cell) {
-    if constexpr (MODE == MODE_TX) return __ldg(P.fieldPX + fbase + cell);
-    else if constexpr (MODE == MODE_T) return __ldg(P.fieldP + fbase + cell);
-    else return __ldg(P.fieldT + fbase + cell);
-}
-
-// ---------------------------------------------------------------------------
-// The march kernel.  Persistent: every warp pulls work items (field, band
-// group, packet) from an atomic counter until the queue is empty.  The next
-// cell's field value is loaded one step ahead of its use.
-// ---------------------------------------------------------------------------
-// Resident blocks of 256 threads per SM the register allocation must allow
-// (2: up to 128 registers; 3: 85; 4: 64), chosen at build time.
-#ifndef DNSMC_MINB
-#define DNSMC_MINB 4
-#endif
-
-template <int MODE, bool TRACE, bool CV, bool MOM = false>
-__global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParams P) {
-    typedef typename FieldT<MODE>::type VT;
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int la = lane % P.tile_a, lb = lane / P.tile_a;
-    const int njR = P.ea1 - P.ea0, nkR = P.eb1 - P.eb0;
-    const int plane = P.na * P.nb;
-    unsigned long long my_rays = 0, my_steps = 0;
-    unsigned int flags = 0;
-
-    for (;;) {
-        long long item;
-        if (TRACE) {
-            if (threadIdx.x >= 32) return;
-            item = ((long long)P.trace_f * P.n_groups + P.trace_g) * P.n_packets + P.trace_p;
-        } else {
-            unsigned int it = 0;
-            if (lane == 0) it = atomicAdd(P.queue, 1u);
-            it = __shfl_sync(FULL, it, 0);
-            if ((long long)it >= P.n_items) break;
-            item = it;
-        }
-        const int p = (int)(item % P.n_packets);
-        const long long fg = item / P.n_packets;
-        const int G = (int)(fg % P.n_groups);
-        const int f = (int)(fg / P.n_groups);
-        const int pa = p % P.npa;
-        const int rest = p / P.npa;
-        const int pb = rest % P.npb;
-        const int pw = rest / P.npb;
-        const int w0 = P.ew0 + pw;
-        const int a0 = P.ea0 + pa * P.tile_a + la;
-        const int b0 = P.eb0 + pb * P.tile_b + lb;
-        const bool active = (a0 < P.ea1) && (b0 < P.eb1);
-        const int acl = active ? a0 : P.ea0, bcl = active ? b0 : P.eb0;
-        const int N = P.rays_per_packet ? P.rays_per_packet[G * P.rays_gstride + p] : P.rays;
-        const long long fbase = (long long)f * P.field_stride;
-        const int rowW0 = w0 * plane;
-        // own-cell quantities
-        const VT vown = load_field<MODE>(P, fbase, rowW0 + bcl * P.na + acl);
-        float Ti4 = 0.f, invTi4 = 0.f, tpos0 = 0.f;
-        int ti_i = 0, xi_i = 0;
-        float ft_i = 0.f, fx_i = 0.f;
-        if constexpr (MODE == MODE_GREY) {
-            const float Ti = vown;
-            if (!(Ti > 0.0f) && active) flags |= DNSMC_STATUS_BAD_FIELD;
-            const float t2 = Ti * Ti;
-            Ti4 = t2 * t2;
-            invTi4 = Ti4 > 0.f ? 1.0f / Ti4 : 0.f;
-        } else if constexpr (MODE == MODE_TX) {
-            tpos0 = vown.x;
-            pos_split(vown.x, P.nT, &ti_i, &ft_i);
-            pos_split(vown.y, P.nX, &xi_i, &fx_i);
-        } else {
-            tpos0 = vown;
-            pos_split(vown, P.nT, &ti_i, &ft_i);
-        }
-        const float oW = (__ldg(P.fw + w0) + __ldg(P.fw + w0 + 1)) * 0.5f;
-        // alias table of this packet: band group G of the temperature bin
-        // nearest to lane 0's temperature (one bin when sampling at Tmax)
-        int gs = 0, K = 1;
-        if (MODE != MODE_GREY) {
-            int boff = 0;
-            if (P.n_tbins > 1) {
-                const float tp0 = __shfl_sync(FULL, tpos0, 0);
-                int bin = __float2int_rn(tp0);
-                bin = min(max(bin, 0), P.n_tbins - 1);
-                boff = bin * P.n_groups;
-            }
-            gs = P.group_start[boff + G];
-            K = P.group_start[boff + G + 1] - gs;
-        }
-        const uint32_t ctr2 = (uint32_t)G | ((uint32_t)(f + P.field_base) << 16);
-        const long long tc = ((long long)(w0 - P.ew0) * nkR + (bcl - P.eb0)) * njR + (acl - P.ea0);
-        float2 beta = make_float2(1.0f, -1.0f);
-        if (CV && P.beta) beta = P.beta[fg * P.region_cells + tc];
-        double mo[9];
-        if (MOM)
-#pragma unroll
-            for (int q = 0; q < 9; ++q) mo[q] = 0.0;
-        const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
-
-        double S = 0.0, S2 = 0.0, Sb = 0.0;
-        unsigned long long isteps = 0;
-        uint4 shift = make_uint4(0u, 0u, 0u, 0u);
-        int bcur = -1;
-        const int rbeg = TRACE ? P.trace_r : 0;
-        const int rend = TRACE ? P.trace_r + 1 : ((K > 0) ? N : 0);
-        for (int r = rbeg; r < rend; ++r) {
-            uint4 x;
-            int m = 0;
-            if (P.sampler) {
-                const int b = r / M;
-                m = r - b * M;
-                if (b != bcur) {
-                    shift = philox4x32_10(make_uint4((uint32_t)b, (uint32_t)p, ctr2, 0x50B01u), P.key0, P.key1);
-                    bcur = b;
-                }
-                const uint4 sb = sobol4((uint32_t)m);
-                x = make_uint4(sb.x ^ shift.x, sb.y ^ shift.y, sb.z ^ shift.z, sb.w ^ shift.w);
-            } else {
-                x = philox4x32_10(make_uint4((uint32_t)r, (uint32_t)p, ctr2, 0u), P.key0, P.key1);
-            }
-            if (TRACE && lane == 0) {
-                P.trace_rng[0] = x.x; P.trace_rng[1] = x.y; P.trace_rng[2] = x.z; P.trace_rng[3] = x.w;
-            }
-            // isotropic direction: cos(theta) = 1 - 2u, phi = 2*pi*u'
-            const float mu = fmaf((float)(x.y >> 8), -1.1920928955078125e-7f, 1.0f);
-            const float st = sqrtf(fmaxf(0.0f, fmaf(-mu, mu, 1.0f)));
-            float cph, sph;
-            mc_sincos_turn(x.x >> 8, &cph, &sph);
-            const float sW = mu, sA = st * cph, sB = st * sph;
-
-            // spectral sample and ray weight
-            float w, wk, Ii, invI;
-            int nbnd = 0, sid = 0;
-            if (MODE == MODE_GREY) {
-                Ii = Ti4;
-                invI = invTi4;
-                wk = P.Wgrey;
-                w = P.Wgrey * Ti4;
-            } else {
-                const int j = (int)__umulhi(x.z, (uint32_t)K);
-                SpecEntry e = P.entries[gs + j];
-                if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
-                nbnd = (int)(e.alias_nb >> 16);
-                sid = e.koff;
-                const float ki = lookup_k<MODE>(P, sid, ti_i, ft_i, xi_i, fx_i);
-                Ii = lookup_ib(P, nbnd, ti_i, ft_i);
-                invI = Ii > 0.f ? 1.0f / Ii : 0.f;
-                wk = e.W * ki;
-                w = wk * Ii;
-            }
-            // surrogate walk (warp-uniform): the same ray through the
-            // layer-mean medium.  Its k and Ib are constant inside a wall-
-            // normal layer, so it is advanced once per layer: tauE and tE are
-            // its transmissivity and ray parameter at the layer entry, dcumE
-            // the optical depth from the origin; it stops (dumping the rest
-            // into the current layer) once the optical depth exceeds ln(1/toll).
-            const float2 *surp = nullptr;
-            float Jbar = 0.0f, tex0 = -1.0f, tauE = 0.0f, tE = 0.0f, dcumE = 0.0f, kS = 0.0f, IS = 0.0f, I0 = 0.0f;
-            bool salive = false;
-            if (CV) {
-                surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
-                const float2 kv = __ldg(surp + w0);
-                kS = kv.x; IS = kv.y; I0 = kv.y;
-                tauE = 1.0f;
-                salive = true;
-            }
-
-            // warp-uniform DDA set-up (origin at the cell centre)
-            const float invW = 1.0f / fabsf(sW), invA = 1.0f / fabsf(sA), invB = 1.0f / fabsf(sB);
-            const int dW = sW > 0.f ? 1 : -1, dA = sA > 0.f ? 1 : -1, dB = sB > 0.f ? 1 : -1;
-            float tW = (dW > 0 ? (__ldg(P.fw + w0 + 1) - oW) : (oW - __ldg(P.fw + w0))) * invW;
-            const float dtA = P.da * invA, dtB = P.db * invB;
-            float tA = 0.5f * dtA, tB = 0.5f * dtB;
-            int nA = 0, nB = 0;
-            float t = 0.0f;
-            int cw = w0, ca = acl, cb = bcl;
-            int rowW = rowW0, rowB = cb * P.na;
-            float tau = active ? 1.0f : 0.0f;
-            float D = 0.0f;
-            int steps = 0;
-            VT vcur = vown;
-            for (;;) {
-                int axis;
-                float tn;
-                if (tW <= tA && tW <= tB) { axis = 0; tn = tW; }
-                else if (tA <= tB)         { axis = 1; tn = tA; }
-                else                       { axis = 2; tn = tB; }
-                const float ds = tn - t;
-                // next cell of the walk, and its field value fetched now
-                int ncw = cw, nca = ca, ncb = cb, nrowW = rowW, nrowB = rowB;
-                bool wall = false;
-                if (axis == 0) {
-                    ncw = cw + dW;
-                    wall = ncw < 0 || ncw >= P.nw;
-                    nrowW = ncw * plane;
-                } else if (axis == 1) {
-                    nca = ca + dA;
-                    if (nca == P.na) nca = 0; else if (nca < 0) nca = P.na - 1;
-                } else {
-                    ncb = cb + dB;
-                    if (ncb == P.nb) ncb = 0; else if (ncb < 0) ncb = P.nb - 1;
-                    nrowB = ncb * P.na;
-                }
-                VT vnext = vcur;
-                if (!wall && tau > 0.0f) vnext = load_field<MODE>(P, fbase, nrowW + nrowB + nca);
-                if (tau > 0.0f) {
-                    ++my_steps;
-                    float kj, gj;
-                    if constexpr (MODE == MODE_GREY) {
-                        const float t2 = vcur * vcur;
-                        gj = (Ti4 - t2 * t2) * invI;
-                        kj = P.kappa;
-                    } else {
-                        int tj, xj = 0;
-                        float ftj, fxj = 0.f;
-                        if constexpr (MODE == MODE_TX) {
-                            pos_split(vcur.x, P.nT, &tj, &ftj);
-                            pos_split(vcur.y, P.nX, &xj, &fxj);
-                        } else {
-                            pos_split(vcur, P.nT, &tj, &ftj);
-                        }
-                        kj = lookup_k<MODE>(P, sid, tj, ftj, xj, fxj);
-                        const float Ibj = lookup_ib(P, nbnd, tj, ftj);
-                        gj = (Ii - Ibj) * invI;
-                    }
-                    const float alpha = -mc_expm1(-(kj * ds));
-                    const float ta = tau * alpha;
-                    D = fmaf(ta, gj, D);
-                    tau = tau - ta;
-                    if (tau < P.toll) { D = fmaf(tau, gj, D); tau = 0.0f; }
-                }
-                if (CV && salive) {
-                    const float opt = kS * (tn - tE);
-                    if (dcumE + opt > P.dtoll) {          // truncated inside this layer
-                        Jbar = fmaf(tauE, IS, Jbar);
-                        salive = false;
-                    } else if (axis == 0) {               // leaves the layer at tn
-                        const float as = -mc_expm1(-opt);
-                        const float tas = tauE * as;
-                        Jbar = fmaf(tas, IS, Jbar);
-                        tauE = tauE - tas;
-                        dcumE = dcumE + opt;
-                        tE = tn;
-                        if (tex0 < 0.0f) tex0 = tauE;     // transmissivity leaving the own layer
-                        if (!wall) {
-                            const float2 kv = __ldg(surp + ncw);
-                            kS = kv.x; IS = kv.y;
-                        }
-                    }
-                }
-                if (TRACE && lane == 0 && steps < P.trace_max) {
-                    int *rec = P.trace_rec + 6 * steps;
-                    rec[0] = cw; rec[1] = dA * nA; rec[2] = dB * nB; rec[3] = axis;
-                    rec[4] = __float_as_int(ds); rec[5] = __float_as_int(tau);
-                }
-                t = tn;
-                ++steps;
-                if (axis == 0) {
-                    if (wall) {
-                        const int side = ncw < 0 ? 0 : 1;
-                        const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
-                        if (tau > 0.0f) {
-                            D = fmaf(tau, (Ii - Iw) * invI, D);
-                            tau = 0.0f;
-                        }
-                        if (CV && salive) {
-                            Jbar = fmaf(tauE, Iw, Jbar);
-                            salive = false;
-                        }
-                        break;
-                    }
-                    cw = ncw;
-                    rowW = nrowW;
-                    tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - oW) : (oW - __ldg(P.fw + cw))) * invW;
-                } else if (axis == 1) {
-                    ++nA;
-                    tA = ((float)nA + 0.5f) * dtA;
-                    ca = nca;
-                } else {
-                    ++nB;
-                    tB = ((float)nB + 0.5f) * dtB;
-                    cb = ncb;
-                    rowB = nrowB;
-                }
-                vcur = vnext;
-                if (!__any_sync(FULL, tau > 0.0f || (CV && salive))) break;
-                if (steps >= P.max_steps) {
-                    if (tau > 0.0f || (CV && salive)) flags |= DNSMC_STATUS_STEP_CAP;
-                    break;
-                }
-            }
-            if (TRACE && lane == 0) *P.trace_n = steps;
-            isteps += (unsigned long long)steps;
-            float X = w * D;
-            if (CV) {
-                // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
-                const float te = tex0 < 0.0f ? 0.0f : tex0;
-                const float Ya = wk * (Ii - Jbar);
-                const float Yb = wk * ((1.0f - te) * (Ii - I0));
-                if (MOM && active) {
-                    const double xd = X, ya = Ya, yb = Yb;
-                    mo[0] += xd; mo[1] += ya; mo[2] += yb;
-                    mo[3] = fma(xd, xd, mo[3]); mo[4] = fma(ya, ya, mo[4]); mo[5] = fma(yb, yb, mo[5]);
-                    mo[6] = fma(xd, ya, mo[6]); mo[7] = fma(xd, yb, mo[7]); mo[8] = fma(ya, yb, mo[8]);
-                }
-                X = X - beta.x * Ya;  // tallied: X - beta_a Y_a - beta_b Y_b; the
-                X = X - beta.y * Yb;  // means beta . E[Y] are added back at finalize
-            }
-            if (active) {
-                ++my_rays;
-                if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                const double Xd = (double)X;
-                S += Xd;
-                if (P.sampler) {
-                    Sb += Xd;
-                    if (m == M - 1) {  // end of a replicate: accumulate its mean squared
-                        const double mb = Sb / M;
-                        S2 = fma(mb, mb, S2);
-                        Sb = 0.0;
-                    }
-                } else {
-                    S2 = fma(Xd, Xd, S2);
-                }
-            }
-        }
-        if (TRACE) return;
-        if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
-        if (active) P.tally[fg * P.region_cells + tc] = make_double2(S, S2);
-        if (MOM && active) {
-            double *out = P.moments + (fg * P.region_cells + tc) * 9;
-#pragma unroll
-            for (int q = 0; q < 9; ++q) out[q] = mo[q];
-        }
-    }
-    // per-warp counters and status
-    for (int o = 16; o > 0; o >>= 1) {
-        my_rays += __shfl_xor_sync(FULL, my_rays, o);
-        my_steps += __shfl_xor_sync(FULL, my_steps, o);
-        flags |= __shfl_xor_sync(FULL, flags, o);
-    }
-    if (lane == 0) {
-        if (my_rays) atomicAdd(P.counters + 0, my_rays);
-        if (my_steps) atomicAdd(P.counters + 1, my_steps);
-        if (flags) atomicOr(P.status, flags);
-    }
-}
 
 // Table coordinates of the field for the march: p = clamp((T - T0)/dT, 0,
 // nT-1) (and the same for x_H2O), computed once per solve with the same FP32
@@ -676,75 +190,28 @@ static inline int grid_for(long long n, int threads) {
     return (int)b;
 }
 
+int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
+                    bool mom, bool gen) {
+    if (gen) return launch_march_gen(mode, p, blocks, threads, stream, trace, cv, mom);
+    return launch_march_variant<false>(mode, p, blocks, threads, (cudaStream_t)stream, trace, cv, mom);
+}
+
+int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen) {
+    if (gen) return march_gen_occupancy(mode, threads, cv, mom);
+    return march_variant_occupancy<false>(mode, threads, cv, mom);
+}
+
 int launch_march(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace) {
-    cudaStream_t st = (cudaStream_t)stream;
-    if (trace) { blocks = 1; threads = 32; }
-    switch (mode) {
-        case MODE_GREY:
-            if (trace) march_kernel<MODE_GREY, true, false><<<blocks, threads, 0, st>>>(p);
-            else march_kernel<MODE_GREY, false, false><<<blocks, threads, 0, st>>>(p);
-            break;
-        case MODE_T:
-            if (trace) march_kernel<MODE_T, true, false><<<blocks, threads, 0, st>>>(p);
-            else march_kernel<MODE_T, false, false><<<blocks, threads, 0, st>>>(p);
-            break;
-        case MODE_TX:
-            if (trace) march_kernel<MODE_TX, true, false><<<blocks, threads, 0, st>>>(p);
-            else march_kernel<MODE_TX, false, false><<<blocks, threads, 0, st>>>(p);
-            break;
-        default:
-            return (int)cudaErrorInvalidValue;
-    }
-    return (int)cudaGetLastError();
+    return launch_march_ex(mode, p, blocks, threads, stream, trace, false, false, false);
 }
 
 int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace,
                     bool moments) {
-    cudaStream_t st = (cudaStream_t)stream;
-    if (trace) { blocks = 1; threads = 32; }
-    if (moments && !trace) {
-        switch (mode) {
-            case MODE_GREY: march_kernel<MODE_GREY, false, true, true><<<blocks, threads, 0, st>>>(p); break;
-            case MODE_T: march_kernel<MODE_T, false, true, true><<<blocks, threads, 0, st>>>(p); break;
-            case MODE_TX: march_kernel<MODE_TX, false, true, true><<<blocks, threads, 0, st>>>(p); break;
-            default: return (int)cudaErrorInvalidValue;
-        }
-        return (int)cudaGetLastError();
-    }
-    switch (mode) {
-        case MODE_GREY:
-            if (trace) march_kernel<MODE_GREY, true, true><<<blocks, threads, 0, st>>>(p);
-            else march_kernel<MODE_GREY, false, true><<<blocks, threads, 0, st>>>(p);
-            break;
-        case MODE_T:
-            if (trace) march_kernel<MODE_T, true, true><<<blocks, threads, 0, st>>>(p);
-            else march_kernel<MODE_T, false, true><<<blocks, threads, 0, st>>>(p);
-            break;
-        case MODE_TX:
-            if (trace) march_kernel<MODE_TX, true, true><<<blocks, threads, 0, st>>>(p);
-            else march_kernel<MODE_TX, false, true><<<blocks, threads, 0, st>>>(p);
-            break;
-        default:
-            return (int)cudaErrorInvalidValue;
-    }
-    return (int)cudaGetLastError();
+    return launch_march_ex(mode, p, blocks, threads, stream, trace, true, moments, false);
 }
 
 int march_cv_occupancy(int mode, int threads, bool moments) {
-    int nb = 0;
-    cudaError_t e = cudaErrorInvalidValue;
-    if (moments) {
-        if (mode == MODE_GREY) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false, true, true>, threads, 0);
-        if (mode == MODE_T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false, true, true>, threads, 0);
-        if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false, true, true>, threads, 0);
-        if (e != cudaSuccess) return 1;
-        return nb > 0 ? nb : 1;
-    }
-    if (mode == MODE_GREY) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false, true>, threads, 0);
-    if (mode == MODE_T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false, true>, threads, 0);
-    if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false, true>, threads, 0);
-    if (e != cudaSuccess) return 1;
-    return nb > 0 ? nb : 1;
+    return march_occupancy_ex(mode, threads, true, moments, false);
 }
 
 // ---------------------------------------------------------------------------
@@ -801,20 +268,29 @@ __global__ void cv_layer_kernel(const CvParams c) {
     const int w = blockIdx.x, f = blockIdx.y;
     const long long plane = (long long)c.na * c.nb;
     const long long base = ((long long)f * c.nw + w) * plane;
-    __shared__ double sT[256], sX[256];
-    double aT = 0.0, aX = 0.0;
+    __shared__ double sT[256], sX[256], sV[256];
+    double aT = 0.0, aX = 0.0, aV = 0.0;
     for (long long i = threadIdx.x; i < plane; i += blockDim.x) {
         if (c.mode == MODE_TX) { const float2 v = c.fieldTX[base + i]; aT += v.x; aX += v.y; }
         else aT += c.fieldT[base + i];
+        if (c.fieldV) aV += c.fieldV[base + i];
     }
     sT[threadIdx.x] = aT;
     sX[threadIdx.x] = aX;
+    sV[threadIdx.x] = aV;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) { sT[threadIdx.x] += sT[threadIdx.x + o]; sX[threadIdx.x] += sX[threadIdx.x + o]; }
+        if (threadIdx.x < o) {
+            sT[threadIdx.x] += sT[threadIdx.x + o];
+            sX[threadIdx.x] += sX[threadIdx.x + o];
+            sV[threadIdx.x] += sV[threadIdx.x + o];
+        }
         __syncthreads();
     }
-    if (threadIdx.x == 0) c.layer[(long long)f * c.nw + w] = make_float2((float)(sT[0] / plane), (float)(sX[0] / plane));
+    if (threadIdx.x == 0) {
+        c.layer[(long long)f * c.nw + w] = make_float2((float)(sT[0] / plane), (float)(sX[0] / plane));
+        if (c.layerV) c.layerV[(long long)f * c.nw + w] = (float)(sV[0] / plane);
+    }
 }
 
 // Layer-mean absorption coefficient and band intensity per (field, sample, layer).
@@ -836,6 +312,7 @@ __global__ void cv_sur_kernel(const CvParams c) {
             kb = cv_k(c, sid, L.x, L.y);
             Ib = cv_ib(c, sid / c.nq, L.x);
         }
+        if (c.part) kb = fmaf(c.layerV[(long long)f * c.nw + w], c.part[c.mode == MODE_GREY ? 0 : sid / c.nq].x, kb);
         c.sur[idx] = make_float2(kb, Ib);
     }
 }
@@ -925,11 +402,14 @@ __global__ void cv_mean_kernel(const CvParams c) {
         if (c.mode == MODE_TX) { const float2 v = c.fieldTX[cell]; T = v.x; x = v.y; }
         else T = c.fieldT[cell];
         const long long sbase = (long long)f * c.n_samples * c.nw + w;
+        const float fv = c.fieldV ? c.fieldV[cell] : 0.0f;
         if (c.mode == MODE_GREY) {
             const float t2 = T * T;
             const double2 jh = c.Jhat[sbase];
-            const double acc = c.Wgrey * ((double)(t2 * t2) - jh.x);
-            const double accB = c.Wgrey * ((double)(t2 * t2) - (double)c.sur[sbase].y) * jh.y;
+            // the march's own FP32 weight 4 sigma (kappa + fv a) when particles are present
+            const double Wk = c.part ? (double)((float)(4.0 * 5.670373e-08) * fmaf(fv, c.part[0].x, c.kappa)) : c.Wgrey;
+            const double acc = Wk * ((double)(t2 * t2) - jh.x);
+            const double accB = Wk * ((double)(t2 * t2) - (double)c.sur[sbase].y) * jh.y;
             c.muY[(long long)f * c.n_groups * c.region_cells + tc] = make_double2(acc, accB);
             continue;
         }
@@ -954,6 +434,7 @@ __global__ void cv_mean_kernel(const CvParams c) {
                     const float k0 = __ldg(s), k1 = __ldg(s + 1);
                     k = fmaf(ft, k1 - k0, k0);
                 }
+                if (c.part) k = fmaf(fv, __ldg(&c.part[sid / c.nq].x), k);
                 const float *ib = c.ibtab + (sid / c.nq) * c.nT + ti;
                 const float i0 = __ldg(ib), i1 = __ldg(ib + 1);
                 const float Ib = fmaf(ft, i1 - i0, i0);
@@ -1040,15 +521,7 @@ int launch_cv_mean(const CvParams &c, void *stream) {
     return (int)cudaGetLastError();
 }
 
-int march_occupancy(int mode, int threads) {
-    int nb = 0;
-    cudaError_t e = cudaErrorInvalidValue;
-    if (mode == MODE_GREY) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false, false>, threads, 0);
-    if (mode == MODE_T) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false, false>, threads, 0);
-    if (mode == MODE_TX) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_TX, false, false>, threads, 0);
-    if (e != cudaSuccess) return 1;
-    return nb > 0 ? nb : 1;
-}
+int march_occupancy(int mode, int threads) { return march_occupancy_ex(mode, threads, false, false, false); }
 
 int launch_field_pos(const float *fT, const float2 *fTX, float *outP, float2 *outPX, long long n, float T0,
                      float invdT, int nT, float X0, float invdX, int nX, void *stream) {
@@ -1088,7 +561,8 @@ int launch_field_stats(const float *fT, const float2 *fTX, long long n, double *
 int field_stats_partials() { return 3 * kStatBlocks; }
 
 int upload_sobol_dirs(const uint32_t dirs[4][32]) {
-    return (int)cudaMemcpyToSymbol(c_sobol, dirs, sizeof(uint32_t) * 4 * 32);
+    const int rc = (int)cudaMemcpyToSymbol(c_sobol, dirs, sizeof(uint32_t) * 4 * 32);
+    return rc ? rc : upload_sobol_dirs_gen(dirs);
 }
 
 int device_sm_count() {

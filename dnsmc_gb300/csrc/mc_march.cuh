@@ -1,0 +1,719 @@
+// mc_march.cuh -- the march kernel and its device helpers, shared by the
+// translation units that instantiate it: mc_kernels.cu (absorbing gas,
+// black walls) and mc_march_gen.cu (the general medium: particles with
+// scattering, grey walls).  Both are compiled with -fmad=false: the arithmetic
+// is written with explicit fmaf so the host replay (oracle/mc_oracle.cpp)
+// reproduces every ray bit for bit; exp, log, sin and cos are the project's
+// own polynomial kernels for the same reason.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "mc_internal.h"
+#include "../../include/dnsmc.h"
+
+namespace dnsmc {
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 counter-based generator (Salmon, Moraes, Dror, Shaw,
+// "Parallel random numbers: as easy as 1, 2, 3", SC'11).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r > 0) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    }
+    return c;
+}
+
+// ---------------------------------------------------------------------------
+// expm1 for x <= 0: Cody-Waite reduction x = n*ln2 + r, |r| <= ln2/2, Taylor
+// series of expm1(r) to r^8/8!, then 2^n*expm1(r) + (2^n - 1).  Only +, *,
+// fmaf and rintf: bit-identical on any IEEE-754 machine.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float mc_expm1(float x) {
+    x = fmaxf(x, -87.0f);
+    const float n = rintf(x * 1.44269504088896341f);
+    float r = fmaf(-n, 0.693145751953125f, x);
+    r = fmaf(-n, 1.42860682030941723212e-6f, r);
+    float p = 2.48015873015873016e-5f;             // 1/8!
+    p = fmaf(p, r, 1.98412698412698413e-4f);       // 1/7!
+    p = fmaf(p, r, 1.38888888888888889e-3f);       // 1/6!
+    p = fmaf(p, r, 8.33333333333333333e-3f);       // 1/5!
+    p = fmaf(p, r, 4.16666666666666667e-2f);       // 1/4!
+    p = fmaf(p, r, 1.66666666666666667e-1f);       // 1/3!
+    p = fmaf(p, r, 0.5f);
+    p = fmaf(p, r, 1.0f);
+    p = p * r;                                     // expm1(r)
+    const int ni = (int)n;                         // in [-126, 0]
+    const float two_n = __int_as_float((ni + 127) << 23);
+    return fmaf(two_n, p, two_n - 1.0f);
+}
+
+// sin and cos of x in [0, pi/4]: Taylor series to x^11 / x^12.
+__device__ __forceinline__ void mc_sincos_oct(float x, float *s, float *c) {
+    const float z = x * x;
+    float ps = -2.50521083854417188e-8f;           // -1/11!
+    ps = fmaf(ps, z, 2.75573192239858907e-6f);     //  1/9!
+    ps = fmaf(ps, z, -1.98412698412698413e-4f);    // -1/7!
+    ps = fmaf(ps, z, 8.33333333333333333e-3f);     //  1/5!
+    ps = fmaf(ps, z, -1.66666666666666667e-1f);    // -1/3!
+    *s = fmaf(ps * z, x, x);
+    float pc = 2.08767569878680990e-9f;            //  1/12!
+    pc = fmaf(pc, z, -2.75573192239858907e-7f);    // -1/10!
+    pc = fmaf(pc, z, 2.48015873015873016e-5f);     //  1/8!
+    pc = fmaf(pc, z, -1.38888888888888889e-3f);    // -1/6!
+    pc = fmaf(pc, z, 4.16666666666666667e-2f);     //  1/4!
+    pc = fmaf(pc, z, -0.5f);
+    *c = fmaf(pc, z, 1.0f);
+}
+
+// cos and sin of 2*pi*m/2^24 for a 24-bit integer m: exact quadrant and
+// octant reduction on the integer, polynomial on [0, pi/4].
+__device__ __forceinline__ void mc_sincos_turn(uint32_t m, float *cs, float *sn) {
+    const uint32_t q = m >> 22;
+    const uint32_t r = m & 0x3FFFFFu;
+    const bool hi = r > 0x200000u;
+    const float th = (float)(hi ? (0x400000u - r) : r) * 3.74507028e-7f;  // pi*2^-23
+    float s, c;
+    mc_sincos_oct(th, &s, &c);
+    const float cq = hi ? s : c, sq = hi ? c : s;
+    float co, si;
+    switch (q) {
+        case 0: co = cq;  si = sq;  break;
+        case 1: co = -sq; si = cq;  break;
+        case 2: co = -cq; si = -sq; break;
+        default: co = sq; si = -cq; break;
+    }
+    *cs = co; *sn = si;
+}
+
+// Sobol' direction numbers of the four sampled dimensions (host-computed).
+static __constant__ uint32_t c_sobol[4][32];  // one copy per translation unit
+
+__device__ __forceinline__ uint4 sobol4(uint32_t m) {
+    uint32_t a = 0, b = 0, c = 0, d = 0;
+    for (int k = 0; m; ++k, m >>= 1)
+        if (m & 1u) { a ^= c_sobol[0][k]; b ^= c_sobol[1][k]; c ^= c_sobol[2][k]; d ^= c_sobol[3][k]; }
+    return make_uint4(a, b, c, d);
+}
+
+__device__ __forceinline__ float u24(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
+
+// Linear position in a uniform grid of n points, clamped as the reference's
+// clamp-addressed linear-filter textures (code/memory_copy.cu:245-247).
+__device__ __forceinline__ void grid_pos(float v, float v0, float inv, int n, int *i, float *f) {
+    float p = (v - v0) * inv;
+    p = fminf(fmaxf(p, 0.0f), (float)(n - 1));
+    int ii = (int)p;
+    ii = min(ii, n - 2);
+    *i = ii;
+    *f = p - (float)ii;
+}
+
+// Split a clamped table coordinate p in [0, n-1] into cell and fraction.
+__device__ __forceinline__ void pos_split(float p, int n, int *i, float *f) {
+    int ii = (int)p;
+    ii = min(ii, n - 2);
+    *i = ii;
+    *f = p - (float)ii;
+}
+
+// Paired tables: kpair holds (k[t][x], k[t][x+1]) (x-tables) or (k[t], k[t+1])
+// and ibpair (Ib[t], Ib[t+1]), so a bilinear lookup is two 8-byte loads.
+template <int MODE>
+__device__ __forceinline__ float lookup_k(const MarchParams &P, int sid, int ti, float ft, int xi, float fx) {
+    if (MODE == MODE_TX) {
+        const int row = P.nX - 1;
+        const float2 *r = P.kpair + (sid * P.nT + ti) * row + xi;
+        const float2 a = __ldg(r), b = __ldg(r + row);
+        const float k0 = fmaf(fx, a.y - a.x, a.x);
+        const float k1 = fmaf(fx, b.y - b.x, b.x);
+        return fmaf(ft, k1 - k0, k0);
+    } else {
+        const float2 a = __ldg(P.kpair + sid * (P.nT - 1) + ti);
+        return fmaf(ft, a.y - a.x, a.x);
+    }
+}
+
+__device__ __forceinline__ float lookup_ib(const MarchParams &P, int nb, int ti, float ft) {
+    const float2 a = __ldg(P.ibpair + nb * (P.nT - 1) + ti);
+    return fmaf(ft, a.y - a.x, a.x);
+}
+
+// Field element type of the march: T (grey), table T coordinate, or (T, x) coordinates.
+template <int MODE> struct FieldT { typedef float type; };
+template <> struct FieldT<MODE_TX> { typedef float2 type; };
+
+template <int MODE>
+__device__ __forceinline__ typename FieldT<MODE>::type load_field(const MarchParams &P, long long fbase, int cell) {
+    if constexpr (MODE == MODE_TX) return __ldg(P.fieldPX + fbase + cell);
+    else if constexpr (MODE == MODE_T) return __ldg(P.fieldP + fbase + cell);
+    else return __ldg(P.fieldT + fbase + cell);
+}
+
+// ---------------------------------------------------------------------------
+// -ln(u) for u in (0, 1): u = m 2^e with m in [sqrt(1/2), sqrt(2)),
+// ln m = 2 atanh(s), s = (m - 1)/(m + 1), odd series to s^11 (|s| <= 0.1716,
+// truncation below 1e-9); e ln 2 split Cody-Waite.  +, *, /, fmaf only.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float mc_neglog(float u) {
+    uint32_t b = __float_as_uint(u);
+    int e = (int)((b >> 23) & 0xffu) - 127;
+    float m = __uint_as_float((b & 0x7fffffu) | 0x3f800000u);
+    if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float z = s * s;
+    float p = 9.09090909090909091e-2f;            // 1/11
+    p = fmaf(p, z, 1.11111111111111111e-1f);       // 1/9
+    p = fmaf(p, z, 1.42857142857142857e-1f);       // 1/7
+    p = fmaf(p, z, 2.0e-1f);                       // 1/5
+    p = fmaf(p, z, 3.33333333333333333e-1f);       // 1/3
+    p = fmaf(p, z, 1.0f);
+    const float lnm = 2.0f * s * p;
+    const float fe = (float)e;
+    const float ln = fmaf(fe, 0.693145751953125f, fmaf(fe, 1.42860682030941723212e-6f, lnm));
+    return -ln;
+}
+
+// uniform in (0, 1) from the top 24 bits
+__device__ __forceinline__ float u24o(uint32_t x) { return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-8f; }
+
+// Direction scattered by the Henyey-Greenstein phase function (asymmetry g)
+// from (sW, sA, sB): cos(theta) from uc, azimuth 2 pi m / 2^24.
+__device__ __forceinline__ void hg_scatter(float g, uint32_t uc, uint32_t um, float *sW, float *sA, float *sB) {
+    const float u = u24(uc);
+    float ct;
+    if (fabsf(g) < 1e-6f) {
+        ct = 1.0f - 2.0f * u;
+    } else {
+        const float tmp = (1.0f - g * g) / (1.0f - g + 2.0f * g * u);
+        ct = (1.0f + g * g - tmp * tmp) / (2.0f * g);
+    }
+    ct = fminf(fmaxf(ct, -1.0f), 1.0f);
+    const float st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+    float cph, sph;
+    mc_sincos_turn(um >> 8, &cph, &sph);
+    const float w = *sW, a = *sA, b = *sB;
+    float nw, na, nb;
+    if (fabsf(w) > 0.99999f) {
+        na = st * cph;
+        nb = st * sph;
+        nw = w > 0.0f ? ct : -ct;
+    } else {
+        const float tmp = sqrtf(1.0f - w * w);
+        na = st * (a * w * cph - b * sph) / tmp + a * ct;
+        nb = st * (b * w * cph + a * sph) / tmp + b * ct;
+        nw = -st * cph * tmp + w * ct;
+    }
+    *sW = nw; *sA = na; *sB = nb;
+}
+
+// Surrogate of the control variate: the ray's straight flight through the
+// layer-mean medium (k, Ib constant in each wall-normal layer, black walls),
+// advanced layer by layer and stopped when its optical depth exceeds
+// ln(1/toll).  Returns the collected intensity Jbar and the transmissivity
+// leaving the own layer.
+template <int MODE>
+__device__ __forceinline__ void surrogate_walk(const MarchParams &P, const float2 *surp, int w0, float oW, float sW,
+                                               int nbnd, float *Jbar_out, float *tex_out) {
+    const float invW = 1.0f / fabsf(sW);
+    const int dW = sW > 0.f ? 1 : -1;
+    float Jbar = 0.0f, tauE = 1.0f, tE = 0.0f, dcum = 0.0f, tex0 = -1.0f;
+    int l = w0;
+    float2 kv = __ldg(surp + w0);
+    for (;;) {
+        const float tn = (dW > 0 ? (__ldg(P.fw + l + 1) - oW) : (oW - __ldg(P.fw + l))) * invW;
+        const float opt = kv.x * (tn - tE);
+        if (dcum + opt > P.dtoll) { Jbar = fmaf(tauE, kv.y, Jbar); break; }  // truncated in layer l
+        const float as = -mc_expm1(-opt);
+        const float tas = tauE * as;
+        Jbar = fmaf(tas, kv.y, Jbar);
+        tauE = tauE - tas;
+        dcum = dcum + opt;
+        tE = tn;
+        if (tex0 < 0.0f) tex0 = tauE;
+        l += dW;
+        if (l < 0 || l >= P.nw) {
+            const int side = l < 0 ? 0 : 1;
+            const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
+            Jbar = fmaf(tauE, Iw, Jbar);
+            break;
+        }
+        kv = __ldg(surp + l);
+    }
+    *Jbar_out = Jbar;
+    *tex_out = tex0 < 0.0f ? 0.0f : tex0;
+}
+
+// ---------------------------------------------------------------------------
+// The march kernel.  Persistent: every warp pulls work items (field, band
+// group, packet) from an atomic counter until the queue is empty.  The next
+// cell's field value is loaded one step ahead of its use.
+//
+// GEN (the general medium) adds particles and grey walls:
+//   * absorption k = k_gas + fv a_band and scattering fv s_band per cell;
+//   * scattering by weighted delta tracking with a shared decision: flights
+//     to tentative collisions are drawn with the majorant fv_max s_band
+//     (warp-uniform); at a collision the warp scatters with probability q =
+//     mean over live lanes of p_l = fv_l s_band / majorant, and each lane's
+//     throughput is multiplied by p_l / q (scatter) or (1 - p_l)/(1 - q)
+//     (no scatter).  The estimate stays unbiased and the whole walk stays
+//     warp-uniform; the new direction follows Henyey-Greenstein;
+//   * grey diffuse walls: the wall takes eps of the throughput at its own
+//     intensity and reflects the rest into a cosine-distributed direction.
+// Every direction change restarts the DDA from the current point: lanes
+// still differ by whole periodic cells only.
+// ---------------------------------------------------------------------------
+// Resident blocks of 256 threads per SM the register allocation must allow
+// (2: up to 128 registers; 3: 85; 4: 64), chosen at build time.
+#ifndef DNSMC_MINB
+#define DNSMC_MINB 4
+#endif
+template <int MODE, bool TRACE, bool CV, bool MOM, bool GEN>
+__global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParams P) {
+    typedef typename FieldT<MODE>::type VT;
+    const unsigned FULL = 0xffffffffu;
+    const float INF = __int_as_float(0x7f800000);
+    const int lane = threadIdx.x & 31;
+    const int la = lane % P.tile_a, lb = lane / P.tile_a;
+    const int njR = P.ea1 - P.ea0, nkR = P.eb1 - P.eb0;
+    const int plane = P.na * P.nb;
+    unsigned long long my_rays = 0, my_steps = 0;
+    unsigned int flags = 0;
+
+    for (;;) {
+        long long item;
+        if (TRACE) {
+            if (threadIdx.x >= 32) return;
+            item = ((long long)P.trace_f * P.n_groups + P.trace_g) * P.n_packets + P.trace_p;
+        } else {
+            unsigned int it = 0;
+            if (lane == 0) it = atomicAdd(P.queue, 1u);
+            it = __shfl_sync(FULL, it, 0);
+            if ((long long)it >= P.n_items) break;
+            item = it;
+        }
+        const int p = (int)(item % P.n_packets);
+        const long long fg = item / P.n_packets;
+        const int G = (int)(fg % P.n_groups);
+        const int f = (int)(fg / P.n_groups);
+        const int pa = p % P.npa;
+        const int rest = p / P.npa;
+        const int pb = rest % P.npb;
+        const int pw = rest / P.npb;
+        const int w0 = P.ew0 + pw;
+        const int a0 = P.ea0 + pa * P.tile_a + la;
+        const int b0 = P.eb0 + pb * P.tile_b + lb;
+        const bool active = (a0 < P.ea1) && (b0 < P.eb1);
+        const int acl = active ? a0 : P.ea0, bcl = active ? b0 : P.eb0;
+        const int N = P.rays_per_packet ? P.rays_per_packet[G * P.rays_gstride + p] : P.rays;
+        const long long fbase = (long long)f * P.field_stride;
+        const int rowW0 = w0 * plane;
+        // own-cell quantities
+        const VT vown = load_field<MODE>(P, fbase, rowW0 + bcl * P.na + acl);
+        float fvown = 0.0f;
+        if constexpr (GEN) {
+            if (P.fieldV) fvown = __ldg(P.fieldV + fbase + rowW0 + bcl * P.na + acl);
+        }
+        float Ti4 = 0.f, invTi4 = 0.f, tpos0 = 0.f;
+        int ti_i = 0, xi_i = 0;
+        float ft_i = 0.f, fx_i = 0.f;
+        if constexpr (MODE == MODE_GREY) {
+            const float Ti = vown;
+            if (!(Ti > 0.0f) && active) flags |= DNSMC_STATUS_BAD_FIELD;
+            const float t2 = Ti * Ti;
+            Ti4 = t2 * t2;
+            invTi4 = Ti4 > 0.f ? 1.0f / Ti4 : 0.f;
+        } else if constexpr (MODE == MODE_TX) {
+            tpos0 = vown.x;
+            pos_split(vown.x, P.nT, &ti_i, &ft_i);
+            pos_split(vown.y, P.nX, &xi_i, &fx_i);
+        } else {
+            tpos0 = vown;
+            pos_split(vown, P.nT, &ti_i, &ft_i);
+        }
+        const float oW = (__ldg(P.fw + w0) + __ldg(P.fw + w0 + 1)) * 0.5f;
+        // alias table of this packet: band group G of the temperature bin
+        // nearest to lane 0's temperature (one bin when sampling at Tmax)
+        int gs = 0, K = 1;
+        if (MODE != MODE_GREY) {
+            int boff = 0;
+            if (P.n_tbins > 1) {
+                const float tp0 = __shfl_sync(FULL, tpos0, 0);
+                int bin = __float2int_rn(tp0);
+                bin = min(max(bin, 0), P.n_tbins - 1);
+                boff = bin * P.n_groups;
+            }
+            gs = P.group_start[boff + G];
+            K = P.group_start[boff + G + 1] - gs;
+        }
+        const uint32_t ctr2 = (uint32_t)G | ((uint32_t)(f + P.field_base) << 16);
+        const long long tc = ((long long)(w0 - P.ew0) * nkR + (bcl - P.eb0)) * njR + (acl - P.ea0);
+        float2 beta = make_float2(1.0f, -1.0f);
+        if (CV && P.beta) beta = P.beta[fg * P.region_cells + tc];
+        double mo[9];
+        if (MOM)
+#pragma unroll
+            for (int q = 0; q < 9; ++q) mo[q] = 0.0;
+        const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
+
+        double S = 0.0, S2 = 0.0, Sb = 0.0;
+        unsigned long long isteps = 0;
+        uint4 shift = make_uint4(0u, 0u, 0u, 0u);
+        int bcur = -1;
+        const int rbeg = TRACE ? P.trace_r : 0;
+        const int rend = TRACE ? P.trace_r + 1 : ((K > 0) ? N : 0);
+        for (int r = rbeg; r < rend; ++r) {
+            uint4 x;
+            int m = 0;
+            if (P.sampler) {
+                const int b = r / M;
+                m = r - b * M;
+                if (b != bcur) {
+                    shift = philox4x32_10(make_uint4((uint32_t)b, (uint32_t)p, ctr2, 0x50B01u), P.key0, P.key1);
+                    bcur = b;
+                }
+                const uint4 sb = sobol4((uint32_t)m);
+                x = make_uint4(sb.x ^ shift.x, sb.y ^ shift.y, sb.z ^ shift.z, sb.w ^ shift.w);
+            } else {
+                x = philox4x32_10(make_uint4((uint32_t)r, (uint32_t)p, ctr2, 0u), P.key0, P.key1);
+            }
+            if (TRACE && lane == 0) {
+                P.trace_rng[0] = x.x; P.trace_rng[1] = x.y; P.trace_rng[2] = x.z; P.trace_rng[3] = x.w;
+            }
+            // isotropic direction: cos(theta) = 1 - 2u, phi = 2*pi*u'
+            const float mu = fmaf((float)(x.y >> 8), -1.1920928955078125e-7f, 1.0f);
+            const float st = sqrtf(fmaxf(0.0f, fmaf(-mu, mu, 1.0f)));
+            float cph, sph;
+            mc_sincos_turn(x.x >> 8, &cph, &sph);
+            float sW = mu, sA = st * cph, sB = st * sph;
+
+            // spectral sample and ray weight
+            float w, wk, Ii, invI;
+            int nbnd = 0, sid = 0;
+            float pab = 0.0f, psc = 0.0f;  // particle absorption / scattering per unit volume fraction
+            if (MODE == MODE_GREY) {
+                Ii = Ti4;
+                invI = invTi4;
+                if constexpr (GEN) {
+                    if (P.part) { const float2 pp = __ldg(P.part); pab = pp.x; psc = pp.y; }
+                    wk = P.W4sig * fmaf(fvown, pab, P.kappa);
+                } else {
+                    wk = P.Wgrey;
+                }
+                w = wk * Ti4;
+            } else {
+                const int j = (int)__umulhi(x.z, (uint32_t)K);
+                SpecEntry e = P.entries[gs + j];
+                if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
+                nbnd = (int)(e.alias_nb >> 16);
+                sid = e.koff;
+                float ki = lookup_k<MODE>(P, sid, ti_i, ft_i, xi_i, fx_i);
+                if constexpr (GEN) {
+                    if (P.part) { const float2 pp = __ldg(P.part + nbnd); pab = pp.x; psc = pp.y; }
+                    ki = fmaf(fvown, pab, ki);
+                }
+                Ii = lookup_ib(P, nbnd, ti_i, ft_i);
+                invI = Ii > 0.f ? 1.0f / Ii : 0.f;
+                wk = e.W * ki;
+                w = wk * Ii;
+            }
+            // control variate: the straight flight through the layer-mean medium
+            float Jbar = 0.0f, tex0 = 0.0f, I0 = 0.0f;
+            if (CV) {
+                const float2 *surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
+                I0 = __ldg(surp + w0).y;
+                surrogate_walk<MODE>(P, surp, w0, oW, sW, nbnd, &Jbar, &tex0);
+            }
+
+            // warp-uniform DDA from (pw0, fa0, fb0): wall-normal coordinate and
+            // fractional offsets inside the current periodic cells
+            float pw0 = oW, fa0 = 0.5f, fb0 = 0.5f, offA = 0.5f, offB = 0.5f;
+            float invW, invA, invB, tW, dtA, dtB, tA, tB;
+            int dW, dA, dB, nA, nB;
+            int cw = w0, ca = acl, cb = bcl;
+            auto dda_init = [&]() {
+                invW = 1.0f / fabsf(sW); invA = 1.0f / fabsf(sA); invB = 1.0f / fabsf(sB);
+                dW = sW > 0.f ? 1 : -1; dA = sA > 0.f ? 1 : -1; dB = sB > 0.f ? 1 : -1;
+                tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - pw0) : (pw0 - __ldg(P.fw + cw))) * invW;
+                dtA = P.da * invA; dtB = P.db * invB;
+                if constexpr (GEN) {
+                    offA = dA > 0 ? 1.0f - fa0 : fa0;
+                    offB = dB > 0 ? 1.0f - fb0 : fb0;
+                }
+                tA = offA * dtA; tB = offB * dtB;
+                nA = 0; nB = 0;
+            };
+            dda_init();
+            float t = 0.0f;
+            int rowW = rowW0, rowB = cb * P.na;
+            float tau = active ? 1.0f : 0.0f;
+            float D = 0.0f;
+            int steps = 0;
+            VT vcur = vown;
+            float fvcur = fvown;
+            // scattering events (GEN): one Philox word quadruple per event
+            uint32_t ev = 0;
+            uint4 evx = make_uint4(0u, 0u, 0u, 0u);
+            float sigbar = 0.0f, tcol = INF;
+            auto draw = [&]() {
+                evx = philox4x32_10(make_uint4((uint32_t)r, (uint32_t)p, ctr2, 0x5CA70000u + ev), P.key0, P.key1);
+                ++ev;
+            };
+            if constexpr (GEN) {
+                sigbar = P.fv_max * psc;
+                if (sigbar > 0.0f) { draw(); tcol = mc_neglog(u24o(evx.x)) / sigbar; }
+            }
+            for (;;) {
+                int axis;
+                float tn;
+                if (tW <= tA && tW <= tB) { axis = 0; tn = tW; }
+                else if (tA <= tB)         { axis = 1; tn = tA; }
+                else                       { axis = 2; tn = tB; }
+                if (GEN && tcol < tn) { axis = 3; tn = tcol; }
+                const float ds = tn - t;
+                // next cell of the walk, and its field value fetched now
+                int ncw = cw, nca = ca, ncb = cb, nrowW = rowW, nrowB = rowB;
+                bool wall = false;
+                if (axis == 0) {
+                    ncw = cw + dW;
+                    wall = ncw < 0 || ncw >= P.nw;
+                    nrowW = ncw * plane;
+                } else if (axis == 1) {
+                    nca = ca + dA;
+                    if (nca == P.na) nca = 0; else if (nca < 0) nca = P.na - 1;
+                } else if (axis == 2) {
+                    ncb = cb + dB;
+                    if (ncb == P.nb) ncb = 0; else if (ncb < 0) ncb = P.nb - 1;
+                    nrowB = ncb * P.na;
+                }
+                VT vnext = vcur;
+                float fvnext = fvcur;
+                if (axis < 3 && !wall && tau > 0.0f) {
+                    vnext = load_field<MODE>(P, fbase, nrowW + nrowB + nca);
+                    if constexpr (GEN) {
+                        if (P.fieldV) fvnext = __ldg(P.fieldV + fbase + nrowW + nrowB + nca);
+                    }
+                }
+                float gj = 0.0f;
+                if (tau > 0.0f) {
+                    ++my_steps;
+                    float kj;
+                    if constexpr (MODE == MODE_GREY) {
+                        const float t2 = vcur * vcur;
+                        gj = (Ti4 - t2 * t2) * invI;
+                        kj = P.kappa;
+                    } else {
+                        int tj, xj = 0;
+                        float ftj, fxj = 0.f;
+                        if constexpr (MODE == MODE_TX) {
+                            pos_split(vcur.x, P.nT, &tj, &ftj);
+                            pos_split(vcur.y, P.nX, &xj, &fxj);
+                        } else {
+                            pos_split(vcur, P.nT, &tj, &ftj);
+                        }
+                        kj = lookup_k<MODE>(P, sid, tj, ftj, xj, fxj);
+                        const float Ibj = lookup_ib(P, nbnd, tj, ftj);
+                        gj = (Ii - Ibj) * invI;
+                    }
+                    if constexpr (GEN) kj = fmaf(fvcur, pab, kj);
+                    const float alpha = -mc_expm1(-(kj * ds));
+                    const float ta = tau * alpha;
+                    D = fmaf(ta, gj, D);
+                    tau = tau - ta;
+                    if (tau < P.toll) { D = fmaf(tau, gj, D); tau = 0.0f; }
+                }
+                if (TRACE && lane == 0 && steps < P.trace_max) {
+                    int *rec = P.trace_rec + 6 * steps;
+                    rec[0] = cw; rec[1] = dA * nA; rec[2] = dB * nB; rec[3] = axis;
+                    rec[4] = __float_as_int(ds); rec[5] = __float_as_int(tau);
+                }
+                t = tn;
+                ++steps;
+                if (axis == 0) {
+                    if (wall) {
+                        const int side = ncw < 0 ? 0 : 1;
+                        const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
+                        if constexpr (GEN) {
+                            const float eps = P.eps[side];
+                            if (tau > 0.0f) {
+                                const float gw = (Ii - Iw) * invI;
+                                D = fmaf(tau * eps, gw, D);
+                                tau = eps >= 1.0f ? 0.0f : tau * (1.0f - eps);
+                                if (tau > 0.0f && tau < P.toll) { D = fmaf(tau, gw, D); tau = 0.0f; }
+                            }
+                            if (!__any_sync(FULL, tau > 0.0f)) break;
+                            // diffuse reflection from the wall point
+                            const float ta_ = t / dtA, tb_ = t / dtB;
+                            fa0 = dA > 0 ? fa0 + (ta_ - (float)nA) : fa0 - (ta_ - (float)nA);
+                            fb0 = dB > 0 ? fb0 + (tb_ - (float)nB) : fb0 - (tb_ - (float)nB);
+                            fa0 = fminf(fmaxf(fa0, 0.0f), 1.0f);
+                            fb0 = fminf(fmaxf(fb0, 0.0f), 1.0f);
+                            pw0 = side == 0 ? __ldg(P.fw) : __ldg(P.fw + P.nw);
+                            draw();  // this event's words: the reflected direction only
+                            const float cmu = sqrtf(u24(evx.z));
+                            const float smu = sqrtf(fmaxf(0.0f, 1.0f - cmu * cmu));
+                            float cp, sp;
+                            mc_sincos_turn(evx.w >> 8, &cp, &sp);
+                            sW = side == 0 ? cmu : -cmu;
+                            sA = smu * cp;
+                            sB = smu * sp;
+                            dda_init();
+                            t = 0.0f;
+                            if (sigbar > 0.0f) { draw(); tcol = mc_neglog(u24o(evx.x)) / sigbar; }
+                            if (steps >= P.max_steps) {
+                                if (tau > 0.0f) flags |= DNSMC_STATUS_STEP_CAP;
+                                break;
+                            }
+                            continue;
+                        } else {
+                            if (tau > 0.0f) {
+                                D = fmaf(tau, (Ii - Iw) * invI, D);
+                                tau = 0.0f;
+                            }
+                            break;
+                        }
+                    }
+                    cw = ncw;
+                    rowW = nrowW;
+                    tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - pw0) : (pw0 - __ldg(P.fw + cw))) * invW;
+                } else if (axis == 1) {
+                    ++nA;
+                    tA = ((float)nA + offA) * dtA;
+                    ca = nca;
+                } else if (axis == 2) {
+                    ++nB;
+                    tB = ((float)nB + offB) * dtB;
+                    cb = ncb;
+                    rowB = nrowB;
+                } else if constexpr (GEN) {
+                    // tentative collision: shared decision, per-lane weights
+                    const float pl = tau > 0.0f ? fminf(1.0f, fvcur * psc / sigbar) : 0.0f;
+                    float ps = pl, pc = tau > 0.0f ? 1.0f : 0.0f;
+                    for (int o = 16; o > 0; o >>= 1) {
+                        ps += __shfl_xor_sync(FULL, ps, o);
+                        pc += __shfl_xor_sync(FULL, pc, o);
+                    }
+                    const float q = pc > 0.0f ? ps / pc : 0.0f;
+                    if (u24(evx.y) < q) {
+                        if (tau > 0.0f) tau = tau * (pl / q);
+                        const float ta_ = t / dtA, tb_ = t / dtB;
+                        fa0 = dA > 0 ? fa0 + (ta_ - (float)nA) : fa0 - (ta_ - (float)nA);
+                        fb0 = dB > 0 ? fb0 + (tb_ - (float)nB) : fb0 - (tb_ - (float)nB);
+                        fa0 = fminf(fmaxf(fa0, 0.0f), 1.0f);
+                        fb0 = fminf(fmaxf(fb0, 0.0f), 1.0f);
+                        pw0 = fminf(fmaxf(fmaf(sW, t, pw0), __ldg(P.fw + cw)), __ldg(P.fw + cw + 1));
+                        hg_scatter(P.hg_g, evx.z, evx.w, &sW, &sA, &sB);
+                        dda_init();
+                        t = 0.0f;
+                    } else {
+                        if (tau > 0.0f) tau = tau * ((1.0f - pl) / (1.0f - q));
+                    }
+                    draw();
+                    tcol = t + mc_neglog(u24o(evx.x)) / sigbar;
+                }
+                vcur = vnext;
+                if constexpr (GEN) fvcur = fvnext;
+                if (!__any_sync(FULL, tau > 0.0f)) break;
+                if (steps >= P.max_steps) {
+                    if (tau > 0.0f) flags |= DNSMC_STATUS_STEP_CAP;
+                    break;
+                }
+            }
+            if (TRACE && lane == 0) *P.trace_n = steps;
+            isteps += (unsigned long long)steps;
+            float X = w * D;
+            if (CV) {
+                // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
+                const float Ya = wk * (Ii - Jbar);
+                const float Yb = wk * ((1.0f - tex0) * (Ii - I0));
+                if (MOM && active) {
+                    const double xd = X, ya = Ya, yb = Yb;
+                    mo[0] += xd; mo[1] += ya; mo[2] += yb;
+                    mo[3] = fma(xd, xd, mo[3]); mo[4] = fma(ya, ya, mo[4]); mo[5] = fma(yb, yb, mo[5]);
+                    mo[6] = fma(xd, ya, mo[6]); mo[7] = fma(xd, yb, mo[7]); mo[8] = fma(ya, yb, mo[8]);
+                }
+                X = X - beta.x * Ya;  // tallied: X - beta_a Y_a - beta_b Y_b; the
+                X = X - beta.y * Yb;  // means beta . E[Y] are added back at finalize
+            }
+            if (active) {
+                ++my_rays;
+                if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
+                const double Xd = (double)X;
+                S += Xd;
+                if (P.sampler) {
+                    Sb += Xd;
+                    if (m == M - 1) {  // end of a replicate: accumulate its mean squared
+                        const double mb = Sb / M;
+                        S2 = fma(mb, mb, S2);
+                        Sb = 0.0;
+                    }
+                } else {
+                    S2 = fma(Xd, Xd, S2);
+                }
+            }
+        }
+        if (TRACE) return;
+        if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
+        if (active) P.tally[fg * P.region_cells + tc] = make_double2(S, S2);
+        if (MOM && active) {
+            double *out = P.moments + (fg * P.region_cells + tc) * 9;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) out[q] = mo[q];
+        }
+    }
+    // per-warp counters and status
+    for (int o = 16; o > 0; o >>= 1) {
+        my_rays += __shfl_xor_sync(FULL, my_rays, o);
+        my_steps += __shfl_xor_sync(FULL, my_steps, o);
+        flags |= __shfl_xor_sync(FULL, flags, o);
+    }
+    if (lane == 0) {
+        if (my_rays) atomicAdd(P.counters + 0, my_rays);
+        if (my_steps) atomicAdd(P.counters + 1, my_steps);
+        if (flags) atomicOr(P.status, flags);
+    }
+}
+
+// Launch one march variant: the dispatch over (mode, trace, control variate,
+// moments) of one value of GEN; march_occupancy_gen the matching occupancy.
+template <bool GEN>
+int launch_march_variant(int mode, const MarchParams &p, int blocks, int threads, cudaStream_t st, bool trace, bool cv,
+                         bool mom) {
+    if (trace) { blocks = 1; threads = 32; mom = false; }
+#define DNSMC_L(M, T, C, O) march_kernel<M, T, C, O, GEN><<<blocks, threads, 0, st>>>(p)
+#define DNSMC_MODE(M)                                       \
+    if (trace) { if (cv) DNSMC_L(M, true, true, false); else DNSMC_L(M, true, false, false); } \
+    else if (cv) { if (mom) DNSMC_L(M, false, true, true); else DNSMC_L(M, false, true, false); } \
+    else DNSMC_L(M, false, false, false);
+    switch (mode) {
+        case MODE_GREY: DNSMC_MODE(MODE_GREY) break;
+        case MODE_T: DNSMC_MODE(MODE_T) break;
+        case MODE_TX: DNSMC_MODE(MODE_TX) break;
+        default: return (int)cudaErrorInvalidValue;
+    }
+#undef DNSMC_MODE
+#undef DNSMC_L
+    return (int)cudaGetLastError();
+}
+
+template <bool GEN>
+int march_variant_occupancy(int mode, int threads, bool cv, bool mom) {
+    int nb = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+#define DNSMC_O(M)                                                                                              \
+    e = cv ? (mom ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<M, false, true, true, GEN>, threads, 0) \
+                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<M, false, true, false, GEN>, threads, 0)) \
+           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<M, false, false, false, GEN>, threads, 0)
+    if (mode == MODE_GREY) DNSMC_O(MODE_GREY);
+    if (mode == MODE_T) DNSMC_O(MODE_T);
+    if (mode == MODE_TX) DNSMC_O(MODE_TX);
+#undef DNSMC_O
+    if (e != cudaSuccess) return 1;
+    return nb > 0 ? nb : 1;
+}
+
+}  // namespace dnsmc

@@ -189,6 +189,20 @@ int  dnsmc_set_fields(dnsmc_solver *s, int nfields, const float *T,
  * stream; no host copy.                                                        */
 int  dnsmc_set_fields_device(dnsmc_solver *s, int nfields, const float *dT,
                              const float *dx);
+/* Particles (the general medium; no counterpart in the reference's GPU path,
+ * which has neither scattering, code/param.h:71, nor grey walls,
+ * code/param.h:77): per band the absorption and scattering coefficients per
+ * unit particle volume fraction [1/m] (nbands = the k table's bands, 1 for the
+ * grey model) and the Henyey-Greenstein asymmetry g in (-1, 1).  A cell with
+ * volume fraction fv absorbs k_gas + fv a_band and scatters fv s_band; the
+ * particles emit at the cell temperature.  Scattering is tracked by weighted
+ * delta tracking (majorant max(fv) s_band).  Both arrays NULL removes the
+ * particles.  Requires MODEL_GREY or MODEL_TABLE; set the k table first.   */
+int  dnsmc_set_particles(dnsmc_solver *s, int nbands, const float *absorption,
+                         const float *scattering, float hg_g);
+/* Volume fraction of every resident snapshot (host, the layout of
+ * dnsmc_set_fields); after dnsmc_set_fields, again after every new fields.  */
+int  dnsmc_set_particle_field(dnsmc_solver *s, const float *fv, int layout);
 /* Cells to compute: i in [i0,i1), j in [j0,j1), k in [k0,k1) (0-based); the
  * march always sees the whole field.  Default: all cells.                      */
 int  dnsmc_set_region(dnsmc_solver *s, int i0, int i1, int j0, int j1, int k0,

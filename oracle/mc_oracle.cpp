@@ -30,6 +30,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <limits>
 #include <vector>
 #include <algorithm>
 #ifdef _OPENMP
@@ -554,6 +555,12 @@ typedef struct {
     const float *sur_I;       // [field][sample][nw] layer-mean band intensity
     const float *beta;        // [field][group][k][j][i][2] (beta_a, beta_b) dense, or NULL (1, -1)
     double *moments;          // optional [f][G][tc][9]: sums X, Ya, Yb, X^2, Ya^2, Yb^2, X Ya, X Yb, Ya Yb
+    // general medium (particles with scattering, grey walls)
+    int gen;
+    const float *fieldV;      // dense like fieldT: particle volume fraction, or NULL
+    const float *part;        // [band][2]: absorption, scattering per unit volume fraction
+    float fv_max, hg_g;
+    float eps[2];
 } OrcPacketConfig;
 
 }  // extern "C"
@@ -653,6 +660,63 @@ inline void p_gpos(R v, R v0, R inv, int n, int *i, R *f) {
 template <class R> inline R FMA(R a, R b, R c) { return std::fma(a, b, c); }
 template <> inline float FMA<float>(float a, float b, float c) { return fmaf(a, b, c); }
 
+inline float p_u24(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
+inline float p_u24o(uint32_t x) { return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-8f; }
+
+// -ln(u), the device's mc_neglog: u = m 2^e, m in [sqrt(1/2), sqrt(2)),
+// ln m = 2 atanh((m-1)/(m+1)) by its odd series to s^11.
+inline float p_neglog(float u) {
+    uint32_t b;
+    memcpy(&b, &u, 4);
+    int e = (int)((b >> 23) & 0xffu) - 127;
+    const uint32_t mb = (b & 0x7fffffu) | 0x3f800000u;
+    float m;
+    memcpy(&m, &mb, 4);
+    if (m > 1.41421356f) { m = m * 0.5f; e += 1; }
+    const float s = (m - 1.0f) / (m + 1.0f);
+    const float z = s * s;
+    float p = 9.09090909090909091e-2f;
+    p = fmaf(p, z, 1.11111111111111111e-1f);
+    p = fmaf(p, z, 1.42857142857142857e-1f);
+    p = fmaf(p, z, 2.0e-1f);
+    p = fmaf(p, z, 3.33333333333333333e-1f);
+    p = fmaf(p, z, 1.0f);
+    const float lnm = 2.0f * s * p;
+    const float fe = (float)e;
+    return -fmaf(fe, 0.693145751953125f, fmaf(fe, 1.42860682030941723212e-6f, lnm));
+}
+
+// Henyey-Greenstein scattering of (sW, sA, sB), the device's hg_scatter.
+template <class R>
+inline void hg_scatter(R g, uint32_t uc, uint32_t um, R *sW, R *sA, R *sB) {
+    const R u = (R)p_u24(uc);
+    R ct;
+    if (std::fabs(g) < (R)1e-6f) {
+        ct = (R)1 - (R)2 * u;
+    } else {
+        const R tmp = ((R)1 - g * g) / ((R)1 - g + (R)2 * g * u);
+        ct = ((R)1 + g * g - tmp * tmp) / ((R)2 * g);
+    }
+    ct = std::fmin(std::fmax(ct, (R)-1), (R)1);
+    const R st = std::sqrt(std::fmax((R)0, (R)1 - ct * ct));
+    float cphf, sphf;
+    p_sincos_turn(um >> 8, &cphf, &sphf);
+    const R cph = cphf, sph = sphf;
+    const R w = *sW, a = *sA, b = *sB;
+    R nw, na, nb;
+    if (std::fabs(w) > (R)0.99999f) {
+        na = st * cph;
+        nb = st * sph;
+        nw = w > 0 ? ct : -ct;
+    } else {
+        const R tmp = std::sqrt((R)1 - w * w);
+        na = st * (a * w * cph - b * sph) / tmp + a * ct;
+        nb = st * (b * w * cph + a * sph) / tmp + b * ct;
+        nw = -st * cph * tmp + w * ct;
+    }
+    *sW = nw; *sA = na; *sB = nb;
+}
+
 template <class R>
 struct Packet {
     const OrcPacketConfig &c;
@@ -732,6 +796,9 @@ struct Packet {
         }
         const R oW = ((R)c.fw[w0] + (R)c.fw[w0 + 1]) * (R)0.5;
         const R Wgrey = (R)(float)(4.0 * c.kappa * 5.670373e-08);
+        const R W4sig = (R)(float)(4.0 * 5.670373e-08);
+        R fvown[32];
+        for (int l = 0; l < 32; ++l) fvown[l] = (c.gen && c.fieldV) ? (R)c.fieldV[cidx(f, w0, a0[l], b0[l])] : (R)0;
         const float tw = c.T_west, te = c.T_east;
         const R Tw4[2] = {(R)(tw * tw * tw * tw), (R)(te * te * te * te)};
         const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
@@ -765,12 +832,18 @@ struct Packet {
                 koff = (nbnd * c.nq + c.gq[e]) * c.nT * c.nX;
                 We = (R)c.W[e];
             }
+            // general medium: particle coefficients of the band
+            R pab = 0, psc = 0;
+            if (c.gen && c.part) { pab = (R)c.part[2 * nbnd]; psc = (R)c.part[2 * nbnd + 1]; }
             R w[32], wk[32], Ii[32], invI[32], tau[32], D[32];
             for (int l = 0; l < 32; ++l) {
                 if (c.mode == 0) {
-                    Ii[l] = Ti4[l]; invI[l] = invTi4[l]; wk[l] = Wgrey; w[l] = Wgrey * Ti4[l];
+                    Ii[l] = Ti4[l]; invI[l] = invTi4[l];
+                    wk[l] = c.gen ? W4sig * FMA<R>(fvown[l], pab, (R)c.kappa) : Wgrey;
+                    w[l] = wk[l] * Ti4[l];
                 } else {
-                    const R ki = kfun(koff, ti_i[l], ft_i[l], xi_i[l], fx_i[l]);
+                    R ki = kfun(koff, ti_i[l], ft_i[l], xi_i[l], fx_i[l]);
+                    if (c.gen) ki = FMA<R>(fvown[l], pab, ki);
                     Ii[l] = ibfun(nbnd, ti_i[l], ft_i[l]);
                     invI[l] = Ii[l] > 0 ? (R)1 / Ii[l] : (R)0;
                     wk[l] = We * ki;
@@ -779,71 +852,120 @@ struct Packet {
                 tau[l] = act[l] ? (R)1 : (R)0;
                 D[l] = 0;
             }
-            // surrogate: advanced once per wall-normal layer (constant k, Ib),
-            // stopped when its optical depth exceeds ln(1/toll)
+            // surrogate: the straight flight through the layer-mean medium,
+            // advanced once per layer, stopped beyond optical depth ln(1/toll)
             const int sid = c.mode != 0 ? koff / (c.nT * c.nX) : 0;
             const int nsamp = c.mode != 0 ? c.nbands * c.nq : 1;
             const size_t sbase = ((size_t)f * nsamp + sid) * c.nw;
-            const R dtoll = (R)(float)(-std::log((double)c.toll));
-            bool salive = c.cv != 0;
-            R Jbar = 0, tau_exit0 = -1, tauE = 1, tE = 0, dcumE = 0;
-            R kS = salive ? (R)c.sur_k[sbase + w0] : (R)0, IS = salive ? (R)c.sur_I[sbase + w0] : (R)0;
-            const R invW = (R)1 / std::fabs(sW), invA = (R)1 / std::fabs(sA), invB = (R)1 / std::fabs(sB);
-            const int dW = sW > 0 ? 1 : -1, dA = sA > 0 ? 1 : -1, dB = sB > 0 ? 1 : -1;
-            R tW = (dW > 0 ? ((R)c.fw[w0 + 1] - oW) : (oW - (R)c.fw[w0])) * invW;
-            const R dtA = (R)c.da * invA, dtB = (R)c.db * invB;
-            R tA = (R)0.5 * dtA, tB = (R)0.5 * dtB;
-            int nA = 0, nB = 0, cw = w0, stepn = 0;
+            R Jbar = 0, tex0 = 0;
+            if (c.cv) {
+                const R dtoll = (R)(float)(-std::log((double)c.toll));
+                const R invWs = (R)1 / std::fabs(sW);
+                const int dWs = sW > 0 ? 1 : -1;
+                R tauE = 1, tE = 0, dcum = 0, te0 = -1;
+                int l = w0;
+                R kS = (R)c.sur_k[sbase + w0], IS = (R)c.sur_I[sbase + w0];
+                for (;;) {
+                    const R tn = (dWs > 0 ? ((R)c.fw[l + 1] - oW) : (oW - (R)c.fw[l])) * invWs;
+                    const R opt = kS * (tn - tE);
+                    if (dcum + opt > dtoll) { Jbar = FMA<R>(tauE, IS, Jbar); break; }
+                    const R a = -expm1n(-opt);
+                    const R ta = tauE * a;
+                    Jbar = FMA<R>(ta, IS, Jbar);
+                    tauE = tauE - ta;
+                    dcum = dcum + opt;
+                    tE = tn;
+                    if (te0 < 0) te0 = tauE;
+                    l += dWs;
+                    if (l < 0 || l >= c.nw) {
+                        const int side = l < 0 ? 0 : 1;
+                        const R Iws = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
+                        Jbar = FMA<R>(tauE, Iws, Jbar);
+                        break;
+                    }
+                    kS = (R)c.sur_k[sbase + l];
+                    IS = (R)c.sur_I[sbase + l];
+                }
+                tex0 = te0 < 0 ? (R)0 : te0;
+            }
+            // warp-uniform DDA from (pw0, fa0, fb0)
+            R pw0 = oW, fa0 = (R)0.5, fb0 = (R)0.5, offA = (R)0.5, offB = (R)0.5;
+            R invW, invA, invB, tW, dtA, dtB, tA, tB;
+            int dW, dA, dB, nA, nB;
+            int cw = w0, stepn = 0;
+            auto dda_init = [&]() {
+                invW = (R)1 / std::fabs(sW); invA = (R)1 / std::fabs(sA); invB = (R)1 / std::fabs(sB);
+                dW = sW > 0 ? 1 : -1; dA = sA > 0 ? 1 : -1; dB = sB > 0 ? 1 : -1;
+                tW = (dW > 0 ? ((R)c.fw[cw + 1] - pw0) : (pw0 - (R)c.fw[cw])) * invW;
+                dtA = (R)c.da * invA; dtB = (R)c.db * invB;
+                if (c.gen) {
+                    offA = dA > 0 ? (R)1 - fa0 : fa0;
+                    offB = dB > 0 ? (R)1 - fb0 : fb0;
+                }
+                tA = offA * dtA; tB = offB * dtB;
+                nA = 0; nB = 0;
+            };
+            dda_init();
             int ca[32], cb[32];
             for (int l = 0; l < 32; ++l) { ca[l] = a0[l]; cb[l] = b0[l]; }
             R t = 0;
+            // scattering events
+            uint32_t ev = 0, evx[4] = {0, 0, 0, 0};
+            auto draw = [&]() {
+                const uint32_t ctr[4] = {(uint32_t)r, (uint32_t)p, (uint32_t)G | ((uint32_t)f << 16), 0x5CA70000u + ev};
+                philox(ctr, k0, k1, evx);
+                ++ev;
+            };
+            const R INF = std::numeric_limits<R>::infinity();
+            R sigbar = 0, tcol = INF;
+            if (c.gen) {
+                sigbar = (R)c.fv_max * psc;
+                if (sigbar > 0) { draw(); tcol = (R)p_neglog(p_u24o(evx[0])) / sigbar; }
+            }
+            auto field_k = [&](int l, long long o, R *gj) -> R {
+                R kj;
+                if (c.mode == 0) {
+                    const R Tj = (R)c.fieldT[o];
+                    const R t2 = Tj * Tj;
+                    *gj = (Ti4[l] - t2 * t2) * invI[l];
+                    kj = (R)c.kappa;
+                } else {
+                    int tj, xj = 0;
+                    R ftj, fxj = 0;
+                    if (c.mode == 2) p_gpos<R>((R)c.fieldX[o], (R)c.X0, invdX, c.nX, &xj, &fxj);
+                    p_gpos<R>((R)c.fieldT[o], (R)c.T0, invdT, c.nT, &tj, &ftj);
+                    kj = kfun(koff, tj, ftj, xj, fxj);
+                    *gj = (Ii[l] - ibfun(nbnd, tj, ftj)) * invI[l];
+                }
+                if (c.gen && c.fieldV) kj = FMA<R>((R)c.fieldV[o], pab, kj);
+                return kj;
+            };
+            auto shift_point = [&]() {  // fractional offsets at parameter t of the current segment
+                const R ta_ = t / dtA, tb_ = t / dtB;
+                fa0 = dA > 0 ? fa0 + (ta_ - (R)nA) : fa0 - (ta_ - (R)nA);
+                fb0 = dB > 0 ? fb0 + (tb_ - (R)nB) : fb0 - (tb_ - (R)nB);
+                fa0 = std::fmin(std::fmax(fa0, (R)0), (R)1);
+                fb0 = std::fmin(std::fmax(fb0, (R)0), (R)1);
+            };
             for (;;) {
                 int axis;
                 R tn;
                 if (tW <= tA && tW <= tB) { axis = 0; tn = tW; }
                 else if (tA <= tB) { axis = 1; tn = tA; }
                 else { axis = 2; tn = tB; }
+                if (c.gen && tcol < tn) { axis = 3; tn = tcol; }
                 const R ds = tn - t;
                 for (int l = 0; l < 32; ++l) {
                     if (!(tau[l] > 0)) continue;
                     *steps += 1;
                     const long long o = cidx(f, cw, ca[l], cb[l]);
-                    R kj, gj;
-                    if (c.mode == 0) {
-                        const R Tj = (R)c.fieldT[o];
-                        const R t2 = Tj * Tj;
-                        gj = (Ti4[l] - t2 * t2) * invI[l];
-                        kj = (R)c.kappa;
-                    } else {
-                        int tj, xj = 0;
-                        R ftj, fxj = 0;
-                        if (c.mode == 2) p_gpos<R>((R)c.fieldX[o], (R)c.X0, invdX, c.nX, &xj, &fxj);
-                        p_gpos<R>((R)c.fieldT[o], (R)c.T0, invdT, c.nT, &tj, &ftj);
-                        kj = kfun(koff, tj, ftj, xj, fxj);
-                        gj = (Ii[l] - ibfun(nbnd, tj, ftj)) * invI[l];
-                    }
+                    R gj;
+                    const R kj = field_k(l, o, &gj);
                     const R alpha = -expm1n(-(kj * ds));
                     const R tal = tau[l] * alpha;
                     D[l] = FMA<R>(tal, gj, D[l]);
                     tau[l] = tau[l] - tal;
                     if (tau[l] < (R)c.toll) { D[l] = FMA<R>(tau[l], gj, D[l]); tau[l] = 0; }
-                }
-                const bool wall = axis == 0 && (cw + dW < 0 || cw + dW >= c.nw);
-                if (salive) {
-                    const R opt = kS * (tn - tE);
-                    if (dcumE + opt > dtoll) {
-                        Jbar = FMA<R>(tauE, IS, Jbar);
-                        salive = false;
-                    } else if (axis == 0) {
-                        const R a = -expm1n(-opt);
-                        const R ta = tauE * a;
-                        Jbar = FMA<R>(ta, IS, Jbar);
-                        tauE = tauE - ta;
-                        dcumE = dcumE + opt;
-                        tE = tn;
-                        if (tau_exit0 < 0) tau_exit0 = tauE;
-                        if (!wall) { kS = (R)c.sur_k[sbase + cw + dW]; IS = (R)c.sur_I[sbase + cw + dW]; }
-                    }
                 }
                 if (rec && stepn < tmax) {
                     int32_t *q = rec + 6 * stepn;
@@ -855,33 +977,87 @@ struct Packet {
                 t = tn;
                 ++stepn;
                 if (axis == 0) {
-                    cw += dW;
-                    if (cw < 0 || cw >= c.nw) {
-                        const int side = cw < 0 ? 0 : 1;
-                        if (salive) {
-                            const R Iws = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
-                            Jbar = FMA<R>(tauE, Iws, Jbar);
-                            salive = false;
+                    if (cw + dW < 0 || cw + dW >= c.nw) {
+                        const int side = cw + dW < 0 ? 0 : 1;
+                        const R Iw = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
+                        if (c.gen) {
+                            const R eps = (R)c.eps[side];
+                            bool any = false;
+                            for (int l = 0; l < 32; ++l) {
+                                if (tau[l] > 0) {
+                                    const R gw = (Ii[l] - Iw) * invI[l];
+                                    D[l] = FMA<R>(tau[l] * eps, gw, D[l]);
+                                    tau[l] = eps >= (R)1 ? (R)0 : tau[l] * ((R)1 - eps);
+                                    if (tau[l] > 0 && tau[l] < (R)c.toll) { D[l] = FMA<R>(tau[l], gw, D[l]); tau[l] = 0; }
+                                }
+                                any = any || tau[l] > 0;
+                            }
+                            if (!any) break;
+                            shift_point();
+                            pw0 = side == 0 ? (R)c.fw[0] : (R)c.fw[c.nw];
+                            draw();
+                            const R cmu = std::sqrt((R)p_u24(evx[2]));
+                            const R smu = std::sqrt(std::fmax((R)0, (R)1 - cmu * cmu));
+                            float cpf, spf;
+                            p_sincos_turn(evx[3] >> 8, &cpf, &spf);
+                            sW = side == 0 ? cmu : -cmu;
+                            sA = smu * (R)cpf;
+                            sB = smu * (R)spf;
+                            dda_init();
+                            t = 0;
+                            if (sigbar > 0) { draw(); tcol = (R)p_neglog(p_u24o(evx[0])) / sigbar; }
+                            if (stepn >= c.max_steps) break;
+                            continue;
                         }
                         for (int l = 0; l < 32; ++l) {
                             if (!(tau[l] > 0)) continue;
-                            const R Iw = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
                             D[l] = FMA<R>(tau[l], (Ii[l] - Iw) * invI[l], D[l]);
                             tau[l] = 0;
                         }
                         break;
                     }
-                    tW = (dW > 0 ? ((R)c.fw[cw + 1] - oW) : (oW - (R)c.fw[cw])) * invW;
+                    cw += dW;
+                    tW = (dW > 0 ? ((R)c.fw[cw + 1] - pw0) : (pw0 - (R)c.fw[cw])) * invW;
                 } else if (axis == 1) {
                     ++nA;
-                    tA = ((R)nA + (R)0.5) * dtA;
+                    tA = ((R)nA + offA) * dtA;
                     for (int l = 0; l < 32; ++l) { ca[l] += dA; if (ca[l] == c.na) ca[l] = 0; else if (ca[l] < 0) ca[l] = c.na - 1; }
-                } else {
+                } else if (axis == 2) {
                     ++nB;
-                    tB = ((R)nB + (R)0.5) * dtB;
+                    tB = ((R)nB + offB) * dtB;
                     for (int l = 0; l < 32; ++l) { cb[l] += dB; if (cb[l] == c.nb) cb[l] = 0; else if (cb[l] < 0) cb[l] = c.nb - 1; }
+                } else {
+                    // tentative collision: shared decision, per-lane weights;
+                    // q is the butterfly (xor 16, 8, 4, 2, 1) sum of the device
+                    R pl[32], ps[32], pc[32];
+                    for (int l = 0; l < 32; ++l) {
+                        const R fvl = c.fieldV ? (R)c.fieldV[cidx(f, cw, ca[l], cb[l])] : (R)0;
+                        pl[l] = tau[l] > 0 ? std::fmin((R)1, fvl * psc / sigbar) : (R)0;
+                        ps[l] = pl[l];
+                        pc[l] = tau[l] > 0 ? (R)1 : (R)0;
+                    }
+                    for (int o = 16; o > 0; o >>= 1) {
+                        R ns[32], nc[32];
+                        for (int l = 0; l < 32; ++l) { ns[l] = ps[l] + ps[l ^ o]; nc[l] = pc[l] + pc[l ^ o]; }
+                        for (int l = 0; l < 32; ++l) { ps[l] = ns[l]; pc[l] = nc[l]; }
+                    }
+                    const R q = pc[0] > 0 ? ps[0] / pc[0] : (R)0;
+                    if ((R)p_u24(evx[1]) < q) {
+                        for (int l = 0; l < 32; ++l)
+                            if (tau[l] > 0) tau[l] = tau[l] * (pl[l] / q);
+                        shift_point();
+                        pw0 = std::fmin(std::fmax(FMA<R>(sW, t, pw0), (R)c.fw[cw]), (R)c.fw[cw + 1]);
+                        hg_scatter<R>((R)c.hg_g, evx[2], evx[3], &sW, &sA, &sB);
+                        dda_init();
+                        t = 0;
+                    } else {
+                        for (int l = 0; l < 32; ++l)
+                            if (tau[l] > 0) tau[l] = tau[l] * (((R)1 - pl[l]) / ((R)1 - q));
+                    }
+                    draw();
+                    tcol = t + (R)p_neglog(p_u24o(evx[0])) / sigbar;
                 }
-                bool any = salive;
+                bool any = false;
                 for (int l = 0; l < 32; ++l) any = any || (tau[l] > 0);
                 if (!any) break;
                 if (stepn >= c.max_steps) break;
@@ -901,10 +1077,9 @@ struct Packet {
                         ba = (R)bp[0];
                         bb = (R)bp[1];
                     }
-                    const R te = tau_exit0 < 0 ? (R)0 : tau_exit0;
                     const R Iw0 = (R)c.sur_I[sbase + w0];
                     const R Ya = wk[l] * (Ii[l] - Jbar);
-                    const R Yb = wk[l] * (((R)1 - te) * (Ii[l] - Iw0));
+                    const R Yb = wk[l] * (((R)1 - tex0) * (Ii[l] - Iw0));
                     if (c.moments) {
                         const long long tc = ((long long)(w0 - c.ew0) * nkR + (b0[l] - c.eb0)) * njR + (a0[l] - c.ea0);
                         double *mo = c.moments + 9 * (((long long)f * nG + G) * rc + tc);

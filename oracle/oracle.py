@@ -62,6 +62,8 @@ class PacketConfig(ctypes.Structure):
         ("toll", ctypes.c_float), ("max_steps", ctypes.c_int), ("use_double", ctypes.c_int),
         ("sampler", ctypes.c_int), ("nbatch", ctypes.c_int), ("n_tbins", ctypes.c_int),
         ("cv", ctypes.c_int), ("sur_k", _f), ("sur_I", _f), ("beta", _f), ("moments", _d),
+        ("gen", ctypes.c_int), ("fieldV", _f), ("part", _f), ("fv_max", ctypes.c_float), ("hg_g", ctypes.c_float),
+        ("eps", ctypes.c_float * 2),
     ]
 
 
@@ -162,7 +164,8 @@ def coarsen(T_fort, imax, jmax, kmax, Lx, Ly, Lz, stretched, grid_num, level):
 # ---------------------------------------------------------------------------
 # packet replay: takes the solver's own geometry, tables and sampling
 # ---------------------------------------------------------------------------
-def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: int = 0, mode: int | None = None):
+def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: int = 0, mode: int | None = None,
+                  fv: np.ndarray | None = None):
     """Build a PacketConfig mirroring `solver`'s last solve (tables, sampling,
     geometry, region, rays).  T, x: (nfields, kmax, jmax, imax) dense."""
     cfg = solver.cfg
@@ -183,6 +186,19 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
         keep["X"] = X
         c.fieldX = _fp(X)
     c.kappa, c.T_west, c.T_east = cfg.kappa, cfg.T_west, cfg.T_east
+    # general medium: particles (the solver's table, the caller's field) and grey walls
+    part = getattr(solver, "_part", None)
+    c.gen = 1 if (part is not None or cfg.eps_west < 1 or cfg.eps_east < 1) else 0
+    c.eps[0], c.eps[1] = cfg.eps_west, cfg.eps_east
+    if part is not None:
+        if fv is None:
+            raise ValueError("the solver has particles: pass their volume-fraction field")
+        P = np.ascontiguousarray(part, np.float32)
+        V = np.ascontiguousarray(fv, np.float32).reshape(T.shape)
+        keep["part"], keep["fv"] = P, V
+        c.part, c.fieldV = _fp(P), _fp(V)
+        c.fv_max = float(V.max())
+        c.hg_g = solver._hg
     c.seed, c.toll, c.max_steps, c.use_double = cfg.seed, cfg.toll, cfg.max_steps, use_double
     c.sampler, c.nbatch = cfg.sampler, cfg.nvar
     c.rays = solver_rays(solver)
@@ -394,3 +410,54 @@ def ref_readT(kind: str, table_root: str, Tmax: float) -> dict:
         os.chdir(cwd)
     out["kappamax"] = km.value
     return out
+
+
+# ---------------------------------------------------------------------------
+# 1-D references of the general medium
+# ---------------------------------------------------------------------------
+def slab_grey_walls_divq(y, L: float, kappa: float, T: float, T_wall: float, eps: float) -> np.ndarray:
+    """div q of an isothermal grey non-scattering slab between two diffuse grey
+    walls of emissivity eps at T_wall (both sides), at positions y:
+    wall radiosity J = (eps s Tw^4 + (1-eps) pi Ib (1 - 2 E3(tL))) / (1 - 2 (1-eps) E3(tL)),
+    Q = 2 pi kappa (Ib - J/pi)(E2(tau) + E2(tL - tau)), Ib = s T^4 / pi."""
+    Ib = SIGMA * T ** 4 / math.pi
+    tL = kappa * L
+    E3 = expn(3, tL)
+    J = (eps * SIGMA * T_wall ** 4 + (1 - eps) * math.pi * Ib * (1 - 2 * E3)) / (1 - 2 * (1 - eps) * E3)
+    tau = kappa * np.asarray(y, np.float64)
+    e2 = np.array([expn(2, t) + expn(2, tL - t) for t in tau])
+    return 2 * math.pi * kappa * (Ib - J / math.pi) * e2
+
+
+def slab_scatter_divq(faces, kappa_a: float, sigma_s: float, T: float, Tw0: float, Tw1: float,
+                      refine: int = 8) -> np.ndarray:
+    """Cell means of div q = kappa_a (4 pi Ib - G) in an isothermal, isotropically
+    scattering slab with black walls (cells between `faces`): the integral
+    equation for the source function S = (1 - w) Ib + w G / (4 pi),
+    G(t) = 2 pi [Iw0 E2(t) + Iw1 E2(tL - t) + int_0^tL S(t') E1(|t - t'|) dt'],
+    solved by Nystrom with piecewise-constant S on `refine` sub-cells per cell
+    (exact E1 integrals over each sub-cell via E2)."""
+    faces = np.asarray(faces, np.float64)
+    beta = kappa_a + sigma_s
+    w = sigma_s / beta
+    fine = np.concatenate([np.linspace(faces[i], faces[i + 1], refine + 1)[:-1] for i in range(len(faces) - 1)]
+                          + [faces[-1:]])
+    tf = beta * (fine - fine[0])
+    tL = tf[-1]
+    tc = 0.5 * (tf[1:] + tf[:-1])
+    a, b = tf[:-1], tf[1:]
+    E2 = np.vectorize(lambda x: expn(2, x))
+    M = len(tc)
+    K = np.empty((M, M))
+    for i in range(M):
+        da = np.abs(tc[i] - a)
+        db = np.abs(tc[i] - b)
+        K[i] = np.abs(E2(da) - E2(db))
+        K[i, i] = 2.0 - expn(2, tc[i] - a[i]) - expn(2, b[i] - tc[i])
+    Ib = SIGMA * T ** 4 / math.pi
+    Iw0, Iw1 = SIGMA * Tw0 ** 4 / math.pi, SIGMA * Tw1 ** 4 / math.pi
+    wall = Iw0 * E2(tc) + Iw1 * E2(tL - tc)
+    S = np.linalg.solve(np.eye(M) - 0.5 * w * K, (1 - w) * Ib + 0.5 * w * wall)
+    G = 2 * math.pi * (wall + K @ S)
+    Q = kappa_a * (4 * math.pi * Ib - G)
+    return Q.reshape(-1, refine).mean(1)

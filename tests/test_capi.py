@@ -42,7 +42,7 @@ def test_default_config_is_reference_param_h():
     assert c.model == D.MODEL_PARTICLE and c.stretched_x == 1
 
 
-@pytest.mark.parametrize("field,value", [("imax", 0), ("p_row", 3), ("toll", 0.0), ("model", 9), ("eps_west", 0.8),
+@pytest.mark.parametrize("field,value", [("imax", 0), ("p_row", 3), ("toll", 0.0), ("model", 9), ("eps_west", 0.0), ("eps_east", 1.5),
                                          ("grid_num", 5), ("block_threads", 100), ("tile_a", 12), ("nvar", 0)])
 def test_bad_config_is_an_error_code(field, value):
     c = D.default_config()

@@ -177,3 +177,23 @@ def test_cv_jhat_quadrature_matches_isothermal_slab():
     # own-layer absorptance: 1 - E2(half thickness), same on both sides
     h = 1.0 / nw
     np.testing.assert_allclose(J[:, 1], 1 - O.expn(2, h), rtol=1e-9)
+
+
+def test_slab_references_reduce_to_the_black_non_scattering_slab():
+    """The grey-wall formula at eps = 1 and the scattering Nystrom solution at
+    vanishing scattering both equal the black non-scattering E2 solution; the
+    Nystrom solution is converged in its sub-cell refinement."""
+    faces = np.linspace(0.0, 2.0, 33)
+    yc = 0.5 * (faces[1:] + faces[:-1])
+    black = O.slab_divq(yc, 2.0, 1.0, 1000.0, 400.0, 400.0)
+    np.testing.assert_allclose(O.slab_grey_walls_divq(yc, 2.0, 1.0, 1000.0, 400.0, 1.0), black, rtol=1e-12)
+    fine = np.linspace(0.0, 2.0, 32 * 64 + 1)
+    cell_avg = O.slab_divq(0.5 * (fine[1:] + fine[:-1]), 2.0, 0.5, 1000.0, 0.0, 0.0).reshape(32, 64).mean(1)
+    thin = O.slab_scatter_divq(faces, 0.5, 1e-9, 1000.0, 0.0, 0.0, refine=8)
+    np.testing.assert_allclose(thin, cell_avg, rtol=2e-3)
+    a = O.slab_scatter_divq(faces, 0.5, 1.0, 1000.0, 0.0, 0.0, refine=8)
+    b = O.slab_scatter_divq(faces, 0.5, 1.0, 1000.0, 0.0, 0.0, refine=16)
+    np.testing.assert_allclose(a, b, rtol=2e-4)
+    # grey walls at T_w: emission from the medium is partly returned
+    grey = O.slab_grey_walls_divq(yc, 2.0, 1.0, 1000.0, 400.0, 0.6)
+    assert np.all(grey < black) and np.all(grey > 0)
