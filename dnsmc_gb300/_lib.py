@@ -63,7 +63,7 @@ class CvNetConfig(ctypes.Structure):
     ]
 
 
-CVNET_NFEAT, CVNET_NOUT, CVNET_NLABEL = 67, 32, 8
+CVNET_NFEAT, CVNET_NOUT, CVNET_NLABEL = 67, 64, 8
 CVNET_BETA, CVNET_RAYS = 1, 2
 
 # name -> (restype, argtypes); every symbol include/dnsmc.h declares

@@ -3,7 +3,7 @@
 // A small MLP maps, per cell and band group, local features of the medium to
 // the quantities the Monte Carlo estimator needs but cannot know in advance:
 //
-//   out[4g+0], out[4g+1]: offsets of the control-variate coefficients from
+//   out[4g+0], out[4g+1] (g < 16 band-group slots): offsets of the control-variate coefficients from
 //       (beta_a, beta_b) = (1, -1); any finite pair keeps the estimate
 //       unbiased (E[Y_a], E[Y_b] are exact), the best pair minimises the
 //       variance of X - beta_a Y_a - beta_b Y_b;
@@ -17,7 +17,7 @@
 // Features (67, padded with zeros to 80): T and x_H2O of the cell, its signed
 // wall-normal position 2 eta - 1, and T and x_H2O at 32 points of the
 // wall-normal line through the cell (layers ((2q+1) nw) / 64), all mapped to
-// [-1, 1] by the table's T and x ranges.  Layers 67 -> 128 -> 128 -> 128 -> 32
+// [-1, 1] by the table's T and x ranges.  Layers 67 -> 128 -> 128 -> 128 -> 64
 // with exact GELU, BF16 weights and activations, FP32 accumulation
 // (mma.sync m16n8k16 bf16 tensor-core instructions).
 //
@@ -56,8 +56,9 @@ typedef __nv_bfloat16 bf16;
 constexpr int NFEAT = 67;
 constexpr int K0 = 80;       // padded input width (multiple of 16)
 constexpr int HID = 128;
-constexpr int NOUT = 32;     // 8 group slots x 4 heads
-constexpr int MAXG = 8;
+constexpr int NOUT = 64;     // 16 group slots x 4 heads
+constexpr int MAXG = 16;
+constexpr int NT4 = NOUT / 8;  // n8 tiles of the output layer
 constexpr int NPROF = 32;
 constexpr int NLAB = 8;      // labels per (cell, group): Cxx Caa Cbb Cxa Cxb Cab v c
 
@@ -309,10 +310,10 @@ __global__ void __launch_bounds__(256) mlp_forward_kernel(const FwdParams F) {
         hidden_epilogue(acc, a, bs + HID, r0, F.rows, g, t, F.Z2, F.H2);
         layer_mma<16, 8>(acc, a, W3s, LDH, g, t);
         hidden_epilogue(acc, a, bs + 2 * HID, r0, F.rows, g, t, F.Z3, F.H3);
-        float o[4][4];
-        layer_mma<4, 8>(o, a, W4s, LDH, g, t);
+        float o[NT4][4];
+        layer_mma<NT4, 8>(o, a, W4s, LDH, g, t);
 #pragma unroll
-        for (int n = 0; n < 4; ++n) {
+        for (int n = 0; n < NT4; ++n) {
             const int col = n * 8 + 2 * t;
             const float b0 = bs[3 * HID + col], b1 = bs[3 * HID + col + 1];
             const long long ra = r0 + g, rb = r0 + g + 8;
@@ -925,7 +926,7 @@ void dnsmc_cvnet_default_config(dnsmc_cvnet_config *c) {
 int dnsmc_cvnet_create(const dnsmc_cvnet_config *cfg, dnsmc_cvnet **out) {
     if (!cfg || !out) return arg_fail("null argument");
     *out = nullptr;
-    if (cfg->n_groups < 1 || cfg->n_groups > MAXG) return arg_fail("n_groups must be 1..8");
+    if (cfg->n_groups < 1 || cfg->n_groups > MAXG) return arg_fail("n_groups must be 1..16");
     if (!(cfg->T_scale > 0) || !(cfg->x_scale > 0)) return arg_fail("feature scales must be > 0");
     if (cfg->batch < 128 || cfg->batch % 128) return arg_fail("batch must be a positive multiple of 128");
     if (!(cfg->lr > 0) || !(cfg->ridge >= 0)) return arg_fail("bad lr or ridge");

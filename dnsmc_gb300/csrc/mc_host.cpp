@@ -250,8 +250,8 @@ struct dnsmc_solver {
     HostTable tab;
     DevBuf<float> d_k, d_ib, d_ibw;
     DevBuf<float2> d_kpair, d_ibpair;
-    DevBuf<float> d_posT;
-    DevBuf<float2> d_posTX;
+    DevBuf<int2> d_posT;   // per cell (ti, ft) for T-only tables
+    DevBuf<int4> d_posTX;  // per cell (ti*(nX-1)+xi, ft, fx, ti)
     bool tables_dirty = true;
 
     // fields
@@ -749,7 +749,7 @@ int upload_tables(dnsmc_solver *s) {
     TRY(s->d_ib.ensure(t.Ib.size()));
     CUDA_TRY(cudaMemcpyAsync(s->d_k.p, t.k.data(), t.k.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(cudaMemcpyAsync(s->d_ib.p, t.Ib.data(), t.Ib.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    // paired tables for two-value loads in the march
+    // paired tables for two-value loads in the march: (value, difference to the next)
     const int nS = t.nbands * t.nq;
     std::vector<float2> kp, ip((size_t)t.nbands * (t.nT - 1));
     if (t.nX > 1) {
@@ -758,19 +758,20 @@ int upload_tables(dnsmc_solver *s) {
             for (int ti = 0; ti < t.nT; ++ti)
                 for (int xi = 0; xi < t.nX - 1; ++xi) {
                     const float *r = t.k.data() + ((size_t)sid * t.nT + ti) * t.nX + xi;
-                    kp[((size_t)sid * t.nT + ti) * (t.nX - 1) + xi] = make_float2(r[0], r[1]);
+                    kp[((size_t)sid * t.nT + ti) * (t.nX - 1) + xi] = make_float2(r[0], r[1] - r[0]);
                 }
     } else {
         kp.resize((size_t)nS * (t.nT - 1));
         for (int sid = 0; sid < nS; ++sid)
             for (int ti = 0; ti < t.nT - 1; ++ti) {
                 const float *r = t.k.data() + (size_t)sid * t.nT + ti;
-                kp[(size_t)sid * (t.nT - 1) + ti] = make_float2(r[0], r[1]);
+                kp[(size_t)sid * (t.nT - 1) + ti] = make_float2(r[0], r[1] - r[0]);
             }
     }
     for (int b = 0; b < t.nbands; ++b)
         for (int ti = 0; ti < t.nT - 1; ++ti)
-            ip[(size_t)b * (t.nT - 1) + ti] = make_float2(t.Ib[(size_t)b * t.nT + ti], t.Ib[(size_t)b * t.nT + ti + 1]);
+            ip[(size_t)b * (t.nT - 1) + ti] = make_float2(t.Ib[(size_t)b * t.nT + ti],
+                                                          t.Ib[(size_t)b * t.nT + ti + 1] - t.Ib[(size_t)b * t.nT + ti]);
     TRY(s->d_kpair.ensure(kp.size()));
     TRY(s->d_ibpair.ensure(ip.size()));
     CUDA_TRY(cudaMemcpyAsync(s->d_kpair.p, kp.data(), kp.size() * sizeof(float2), cudaMemcpyHostToDevice, s->stream));

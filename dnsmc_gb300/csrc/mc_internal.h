@@ -40,8 +40,8 @@ struct MarchParams {
     int nfields;
     long long field_stride;   // cells per field (nw*na*nb)
     const float  *fieldT;     // MODE_GREY: temperature
-    const float  *fieldP;     // MODE_T: table temperature coordinate
-    const float2 *fieldPX;    // MODE_TX: (T, x_H2O) table coordinates
+    const int2   *fieldP;     // MODE_T: (ti, ft) table temperature cell and fraction
+    const int4   *fieldPX;    // MODE_TX: (ti*(nX-1)+xi | ti<<16 ... see CellPos) per cell
     // spectral tables
     int nbands, nT, nX;
     float T0, invdT, X0, invdX;
@@ -164,6 +164,11 @@ struct AdaptParams {
 };
 int launch_adaptive_rays(const AdaptParams &a, void *stream);
 
+// Table coordinates of a cell, computed once per solve (field_pos_kernel):
+// p = clamp((v - v0)/dv, 0, n-1) split into cell i = min((int)p, n-2) and
+// fraction p - i, for T and (MODE_TX) x_H2O.  MODE_TX packs
+// {ti*(nX-1) + xi, ft, fx, ti} into an int4 (fractions as float bits), MODE_T
+// {ti, ft} into an int2, so a march step needs no float-to-int split.
 // launchers (mc_kernels.cu); all stream-ordered
 int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                     bool mom, bool gen);
@@ -175,7 +180,7 @@ int upload_sobol_dirs_gen(const uint32_t dirs[4][32]);               // mc_march
 int launch_march(int mode, const MarchParams &p, int blocks, int threads,
                  void *stream, bool trace);
 int launch_finalize(const FinalizeParams &p, void *stream);
-int launch_field_pos(const float *fT, const float2 *fTX, float *outP, float2 *outPX, long long n, float T0,
+int launch_field_pos(const float *fT, const float2 *fTX, int2 *outP, int4 *outPX, long long n, float T0,
                      float invdT, int nT, float X0, float invdX, int nX, void *stream);
 // src element (i, j, k) at src[base + i*si + j*sj + k*sk]; writes dst[f] layout
 int launch_pack_T(const float *src, float *dst, int nw, int na, int nb,

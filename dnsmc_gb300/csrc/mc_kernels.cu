@@ -43,21 +43,26 @@ namespace dnsmc {
 // Table coordinates of the field for the march: p = clamp((T - T0)/dT, 0,
 // nT-1) (and the same for x_H2O), computed once per solve with the same FP32
 // operations the march used to apply per step.
-__global__ void field_pos_kernel(const float *fT, const float2 *fTX, float *outP, float2 *outPX, long long n,
+__global__ void field_pos_kernel(const float *fT, const float2 *fTX, int2 *outP, int4 *outPX, long long n,
                                  float T0, float invdT, int nT, float X0, float invdX, int nX) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
+        int ti, xi;
+        float ft, fx;
         if (fTX) {
             const float2 v = fTX[i];
             float pt = (v.x - T0) * invdT;
             pt = fminf(fmaxf(pt, 0.0f), (float)(nT - 1));
             float px = (v.y - X0) * invdX;
             px = fminf(fmaxf(px, 0.0f), (float)(nX - 1));
-            outPX[i] = make_float2(pt, px);
+            pos_split(pt, nT, &ti, &ft);
+            pos_split(px, nX, &xi, &fx);
+            outPX[i] = make_int4(ti * (nX - 1) + xi, __float_as_int(ft), __float_as_int(fx), ti);
         } else {
             float pt = (fT[i] - T0) * invdT;
             pt = fminf(fmaxf(pt, 0.0f), (float)(nT - 1));
-            outP[i] = pt;
+            pos_split(pt, nT, &ti, &ft);
+            outP[i] = make_int2(ti, __float_as_int(ft));
         }
     }
 }
@@ -523,7 +528,7 @@ int launch_cv_mean(const CvParams &c, void *stream) {
 
 int march_occupancy(int mode, int threads) { return march_occupancy_ex(mode, threads, false, false, false); }
 
-int launch_field_pos(const float *fT, const float2 *fTX, float *outP, float2 *outPX, long long n, float T0,
+int launch_field_pos(const float *fT, const float2 *fTX, int2 *outP, int4 *outPX, long long n, float T0,
                      float invdT, int nT, float X0, float invdX, int nX, void *stream) {
     field_pos_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(fT, fTX, outP, outPX, n, T0, invdT, nT,
                                                                         X0, invdX, nX);

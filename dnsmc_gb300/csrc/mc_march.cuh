@@ -121,31 +121,45 @@ __device__ __forceinline__ void pos_split(float p, int n, int *i, float *f) {
     *f = p - (float)ii;
 }
 
-// Paired tables: kpair holds (k[t][x], k[t][x+1]) (x-tables) or (k[t], k[t+1])
-// and ibpair (Ib[t], Ib[t+1]), so a bilinear lookup is two 8-byte loads.
+// Paired tables: kpair holds (k[t][x], k[t][x+1] - k[t][x]) (x-tables) or
+// (k[t], k[t+1] - k[t]) and ibpair (Ib[t], Ib[t+1] - Ib[t]), so a bilinear
+// lookup is two 8-byte loads and three fmaf (the differences are the same
+// FP32 subtractions the interpolation would do).  kidx = ti*(nX-1) + xi.
 template <int MODE>
-__device__ __forceinline__ float lookup_k(const MarchParams &P, int sid, int ti, float ft, int xi, float fx) {
+__device__ __forceinline__ float lookup_k(const MarchParams &P, int sid, int kidx, float ft, float fx) {
     if (MODE == MODE_TX) {
         const int row = P.nX - 1;
-        const float2 *r = P.kpair + (sid * P.nT + ti) * row + xi;
+        const float2 *r = P.kpair + sid * (P.nT * row) + kidx;
         const float2 a = __ldg(r), b = __ldg(r + row);
-        const float k0 = fmaf(fx, a.y - a.x, a.x);
-        const float k1 = fmaf(fx, b.y - b.x, b.x);
+        const float k0 = fmaf(fx, a.y, a.x);
+        const float k1 = fmaf(fx, b.y, b.x);
         return fmaf(ft, k1 - k0, k0);
     } else {
-        const float2 a = __ldg(P.kpair + sid * (P.nT - 1) + ti);
-        return fmaf(ft, a.y - a.x, a.x);
+        const float2 a = __ldg(P.kpair + sid * (P.nT - 1) + kidx);
+        return fmaf(ft, a.y, a.x);
     }
 }
 
 __device__ __forceinline__ float lookup_ib(const MarchParams &P, int nb, int ti, float ft) {
     const float2 a = __ldg(P.ibpair + nb * (P.nT - 1) + ti);
-    return fmaf(ft, a.y - a.x, a.x);
+    return fmaf(ft, a.y, a.x);
 }
 
-// Field element type of the march: T (grey), table T coordinate, or (T, x) coordinates.
+// Field element type of the march: T (grey), or the cell's table coordinates.
 template <int MODE> struct FieldT { typedef float type; };
-template <> struct FieldT<MODE_TX> { typedef float2 type; };
+template <> struct FieldT<MODE_T> { typedef int2 type; };
+template <> struct FieldT<MODE_TX> { typedef int4 type; };
+
+// (k index, T cell, T fraction, x fraction) of a table-coordinate element
+template <int MODE>
+__device__ __forceinline__ void cell_coords(const typename FieldT<MODE>::type &v, int *kidx, int *ti, float *ft,
+                                            float *fx) {
+    if constexpr (MODE == MODE_TX) {
+        *kidx = v.x; *ft = __int_as_float(v.y); *fx = __int_as_float(v.z); *ti = v.w;
+    } else if constexpr (MODE == MODE_T) {
+        *kidx = v.x; *ti = v.x; *ft = __int_as_float(v.y); *fx = 0.0f;
+    }
+}
 
 template <int MODE>
 __device__ __forceinline__ typename FieldT<MODE>::type load_field(const MarchParams &P, long long fbase, int cell) {
@@ -319,7 +333,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             if (P.fieldV) fvown = __ldg(P.fieldV + fbase + rowW0 + bcl * P.na + acl);
         }
         float Ti4 = 0.f, invTi4 = 0.f, tpos0 = 0.f;
-        int ti_i = 0, xi_i = 0;
+        int ti_i = 0, ki_i = 0;
         float ft_i = 0.f, fx_i = 0.f;
         if constexpr (MODE == MODE_GREY) {
             const float Ti = vown;
@@ -327,13 +341,9 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             const float t2 = Ti * Ti;
             Ti4 = t2 * t2;
             invTi4 = Ti4 > 0.f ? 1.0f / Ti4 : 0.f;
-        } else if constexpr (MODE == MODE_TX) {
-            tpos0 = vown.x;
-            pos_split(vown.x, P.nT, &ti_i, &ft_i);
-            pos_split(vown.y, P.nX, &xi_i, &fx_i);
         } else {
-            tpos0 = vown;
-            pos_split(vown, P.nT, &ti_i, &ft_i);
+            cell_coords<MODE>(vown, &ki_i, &ti_i, &ft_i, &fx_i);
+            tpos0 = (float)ti_i + ft_i;  // the clamped table coordinate, exactly
         }
         const float oW = (__ldg(P.fw + w0) + __ldg(P.fw + w0 + 1)) * 0.5f;
         // alias table of this packet: band group G of the temperature bin
@@ -362,6 +372,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
 
         double S = 0.0, S2 = 0.0, Sb = 0.0;
         unsigned long long isteps = 0;
+        unsigned int lsteps = 0;  // this lane's active steps in the item
         uint4 shift = make_uint4(0u, 0u, 0u, 0u);
         int bcur = -1;
         const int rbeg = TRACE ? P.trace_r : 0;
@@ -411,7 +422,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
                 sid = e.koff;
-                float ki = lookup_k<MODE>(P, sid, ti_i, ft_i, xi_i, fx_i);
+                float ki = lookup_k<MODE>(P, sid, ki_i, ft_i, fx_i);
                 if constexpr (GEN) {
                     if (P.part) { const float2 pp = __ldg(P.part + nbnd); pab = pp.x; psc = pp.y; }
                     ki = fmaf(fvown, pab, ki);
@@ -500,22 +511,17 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 }
                 float gj = 0.0f;
                 if (tau > 0.0f) {
-                    ++my_steps;
+                    ++lsteps;
                     float kj;
                     if constexpr (MODE == MODE_GREY) {
                         const float t2 = vcur * vcur;
                         gj = (Ti4 - t2 * t2) * invI;
                         kj = P.kappa;
                     } else {
-                        int tj, xj = 0;
-                        float ftj, fxj = 0.f;
-                        if constexpr (MODE == MODE_TX) {
-                            pos_split(vcur.x, P.nT, &tj, &ftj);
-                            pos_split(vcur.y, P.nX, &xj, &fxj);
-                        } else {
-                            pos_split(vcur, P.nT, &tj, &ftj);
-                        }
-                        kj = lookup_k<MODE>(P, sid, tj, ftj, xj, fxj);
+                        int kx, tj;
+                        float ftj, fxj;
+                        cell_coords<MODE>(vcur, &kx, &tj, &ftj, &fxj);
+                        kj = lookup_k<MODE>(P, sid, kx, ftj, fxj);
                         const float Ibj = lookup_ib(P, nbnd, tj, ftj);
                         gj = (Ii - Ibj) * invI;
                     }
@@ -656,6 +662,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 }
             }
         }
+        my_steps += lsteps;
         if (TRACE) return;
         if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
         if (active) P.tally[fg * P.region_cells + tc] = make_double2(S, S2);

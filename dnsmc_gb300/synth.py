@@ -123,3 +123,27 @@ def ck_table(nbands: int = 64, nq: int = 16, nT: int = 50, nX: int = 8, seed: in
                 dnu=np.diff(nu).astype(np.float32), wq=wq.astype(np.float32), gq=gq,
                 T0=float(T_range[0]), dT=float((T_range[1] - T_range[0]) / (nT - 1)),
                 X0=float(X_range[0]), dX=float((X_range[1] - X_range[0]) / (nX - 1)))
+
+
+def particle_fraction(n: int, seed: int) -> np.ndarray:
+    """Particle volume fraction fv = 1e-5 (1 + 0.5 f), f an independent
+    fluctuation field (seed + 2000), shape (n, n, n)."""
+    return np.ascontiguousarray(1e-5 * (1.0 + 0.5 * fourier_fluct(n, n, n, seed + 2000)), dtype=np.float32)
+
+
+def particle_table(nbands: int = 64, seed: int = 0, diameter: float = 1e-5) -> dict:
+    """Smooth synthetic particle optics per band: extinction efficiency
+    Q_ext in [1.0, 2.2] and single-scattering albedo in [0.3, 0.9], both slowly
+    varying with the band index (sums of two sinusoids with seeded phases);
+    coefficients per unit volume fraction for spheres of the given diameter:
+    a = 3 Q_abs / (2 d), s = 3 Q_sca / (2 d) [1/m]."""
+    rng = np.random.default_rng(seed + 3000)
+    u = np.linspace(0.0, 1.0, nbands)
+    ph = rng.uniform(0, 2 * math.pi, 4)
+    qext = 1.6 + 0.4 * np.sin(2 * math.pi * u + ph[0]) + 0.2 * np.sin(5 * math.pi * u + ph[1])
+    alb = 0.6 + 0.2 * np.sin(2 * math.pi * u + ph[2]) + 0.1 * np.sin(3 * math.pi * u + ph[3])
+    qext = np.clip(qext, 1.0, 2.2)
+    alb = np.clip(alb, 0.3, 0.9)
+    f = 1.5 / diameter
+    return dict(absorption=(f * qext * (1 - alb)).astype(np.float32), scattering=(f * qext * alb).astype(np.float32),
+                albedo=alb, qext=qext, g=0.6)

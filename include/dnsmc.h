@@ -323,9 +323,9 @@ int  dnsmc_trace_ray(dnsmc_solver *s, int f, int g, int p, int r, int max_steps,
 
 /* ---- learned control variate ----------------------------------------------
  * No counterpart in the reference (its estimator has no control variate).
- * A small MLP (67 features -> 3 x 128 GELU -> 32 outputs; BF16 weights and
+ * A small MLP (67 features -> 3 x 128 GELU -> 64 outputs; BF16 weights and
  * activations, FP32 accumulation on the tensor cores) predicts per cell and
- * band group (up to 8 groups):
+ * band group (up to 16 groups):
  *   - the control-variate coefficients (beta_a, beta_b), as offsets from
  *     (1, -1); any finite pair keeps the estimate unbiased, the network aims
  *     at the pair of least variance;
@@ -344,7 +344,7 @@ int  dnsmc_trace_ray(dnsmc_solver *s, int f, int g, int p, int r, int max_steps,
  * The network lives on the device current at dnsmc_cvnet_create.            */
 typedef struct dnsmc_cvnet dnsmc_cvnet;
 typedef struct {
-    int      n_groups;             /* band-group slots, 1..8                    */
+    int      n_groups;             /* band-group slots, 1..16                   */
     float    T_center, T_scale;    /* feature map of T [K]                      */
     float    x_center, x_scale;    /* feature map of x_H2O                      */
     float    lr, adam_beta1, adam_beta2, adam_eps;
@@ -353,7 +353,7 @@ typedef struct {
     uint64_t seed;                 /* initial weights and row shuffling         */
 } dnsmc_cvnet_config;
 #define DNSMC_CVNET_NFEAT  67
-#define DNSMC_CVNET_NOUT   32
+#define DNSMC_CVNET_NOUT   64
 #define DNSMC_CVNET_NLABEL 8       /* Cxx Caa Cbb Cxa Cxb Cab v c per (cell, group) */
 #define DNSMC_CVNET_BETA   1       /* dnsmc_cvnet_apply: coefficients           */
 #define DNSMC_CVNET_RAYS   2       /* dnsmc_cvnet_apply: ray allocation         */
@@ -362,7 +362,7 @@ int  dnsmc_cvnet_create(const dnsmc_cvnet_config *cfg, dnsmc_cvnet **out);
 int  dnsmc_cvnet_destroy(dnsmc_cvnet *net);
 long long dnsmc_cvnet_param_count(void);
 /* FP32 parameters, flat: W1[128][80] b1 W2[128][128] b2 W3[128][128] b3
- * W4[32][128] b4 (columns 67..79 of W1 are padding and stay 0); scales =
+ * W4[64][128] b4 (columns 67..79 of W1 are padding and stay 0); scales =
  * (S_beta, S_v, S_c), the label scales of the losses.  Either may be NULL.
  * set_params resets the Adam state.                                         */
 int  dnsmc_cvnet_get_params(dnsmc_cvnet *net, float *params, float *scales);
@@ -382,7 +382,7 @@ long long dnsmc_cvnet_training_rows(const dnsmc_cvnet *net);
 /* Adam over the data for `epochs` shuffled passes; loss[4] (may be NULL)
  * receives the mean losses of the last pass: total, beta, variance, cost.   */
 int  dnsmc_cvnet_train(dnsmc_cvnet *net, int epochs, double *loss);
-/* Forward pass on host features [rows][67] -> out [rows][32].               */
+/* Forward pass on host features [rows][67] -> out [rows][64].               */
 int  dnsmc_cvnet_eval(dnsmc_cvnet *net, const float *features, long long rows,
                       float *out);
 /* One forward + backward pass without update on host features and labels

@@ -25,7 +25,7 @@ import math
 
 import numpy as np
 
-NFEAT, K0, HID, NOUT, NPROF, NLAB = 67, 80, 128, 32, 32, 8
+NFEAT, K0, HID, NOUT, NPROF, NLAB = 67, 80, 128, 64, 32, 8
 
 # flat parameter layout (mc_cvnet.cu)
 OFF_W1 = 0

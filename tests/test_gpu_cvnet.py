@@ -112,8 +112,8 @@ def test_gradient_matches_oracle(rows):
     """Gradients of the tensor-core backward pass: per parameter block,
     relative Frobenius error <= 1.5e-2 against the bf16-mimicking oracle and
     <= 6e-2 against the exact float64 gradient; losses to 1e-4."""
-    G = 8
-    net = D.CvNet(D.cvnet_default_config(ridge=0.05))
+    G = 16
+    net = D.CvNet(D.cvnet_default_config(ridge=0.05, n_groups=16))
     p = random_params(7)
     scales = np.array([2.0, 1.3, 0.8], np.float32)
     net.set_params(p, scales)
