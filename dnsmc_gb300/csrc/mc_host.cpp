@@ -274,6 +274,7 @@ struct dnsmc_solver {
     bool rays_dev = false;                   // d_rays_pp was written on the device (no host copy)
     DevBuf<int> d_rays_pp;
     DevBuf<unsigned long long> d_item_steps; // steps per (field, group, packet) of the last solve
+    DevBuf<unsigned int> d_order, d_order_hist;  // longest-first queue order (per-item ray tables)
     DevBuf<float> d_kP;                      // Planck-mean absorption coefficient on the table grid
 
     // particles (general medium): per-band coefficients per unit volume
@@ -973,6 +974,11 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.tally = s->d_tally.p;
     TRY(s->d_item_steps.ensure((size_t)P.n_items));
     P.item_steps = s->d_item_steps.p;
+    if (P.rays_per_packet) {  // uneven items: longest first
+        TRY(s->d_order.ensure((size_t)P.n_items));
+        TRY(s->d_order_hist.ensure(kOrderBuckets));
+        P.item_order = s->d_order.p;
+    }
     const int sms = device_sm_count();
     const int occ = march_occupancy_ex(mode, threads, cv, mom, gen);
     const int blocks = std::max(1, sms * occ);
@@ -1017,6 +1023,12 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         }
         CUDA_TRY(cudaMemsetAsync(s->d_misc.p, 0, 4 * sizeof(unsigned int), s->stream));
         CUDA_TRY(cudaMemsetAsync(s->d_counters.p, 0, 2 * sizeof(unsigned long long), s->stream));
+        if (P.item_order) {
+            const int rco = launch_item_order(P.rays_per_packet, P.rays_gstride, P.n_packets, P.n_groups, P.n_items,
+                                              std::max(1, c.sampler == DNSMC_SAMPLER_RQMC ? c.nvar : 1),
+                                              s->d_order_hist.p, s->d_order.p, s->stream);
+            if (rco) return fail(DNSMC_ERR_CUDA, "queue order launch: %s", cudaGetErrorString((cudaError_t)rco));
+        }
         if (events) CUDA_TRY(cudaEventRecord(s->ev_march0, s->stream));
         int rc = launch_march_ex(mode, P, blocks, threads, s->stream, false, cv, mom, gen);
         if (rc) return fail(DNSMC_ERR_CUDA, "march launch: %s", cudaGetErrorString((cudaError_t)rc));
@@ -1329,6 +1341,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_sur.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();
     s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_item_steps.release(); s->d_kP.release();
+    s->d_order.release(); s->d_order_hist.release();
     s->d_part.release(); s->d_fieldV.release(); s->d_layerV.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
     s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_Qg.release(); s->d_varg.release();

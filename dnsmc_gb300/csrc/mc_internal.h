@@ -61,6 +61,7 @@ struct MarchParams {
     const int *rays_per_packet;  // [G * rays_gstride + packet]
     int rays_gstride;         // 0: one count per packet for all groups; n_packets: per (group, packet)
     unsigned long long *item_steps;  // per item: ray-voxel steps summed over its rays, or null
+    const unsigned int *item_order;  // queue position -> item (longest first), or null: natural order
     uint32_t key0, key1;      // Philox key (seed)
     int sampler;              // 0 iid Philox, 1 RQMC (shifted Sobol' net)
     int nbatch;               // RQMC replicates per item (rays divisible by it)
@@ -169,6 +170,13 @@ int launch_adaptive_rays(const AdaptParams &a, void *stream);
 // fraction p - i, for T and (MODE_TX) x_H2O.  MODE_TX packs
 // {ti*(nX-1) + xi, ft, fx, ti} into an int4 (fractions as float bits), MODE_T
 // {ti, ft} into an int2, so a march step needs no float-to-int split.
+// Queue order of the march's items, longest first: a counting sort of the
+// items by their ray count (n_items = nfields * n_groups * n_packets; rays of
+// item (f, g, p) = rays[g * gstride + p]).  hist needs kOrderBuckets + 1 words.
+constexpr int kOrderBuckets = 4096;
+int launch_item_order(const int *rays, int gstride, int n_packets, int n_groups, long long n_items, int B,
+                      unsigned int *hist, unsigned int *order, void *stream);
+
 // launchers (mc_kernels.cu); all stream-ordered
 int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                     bool mom, bool gen);

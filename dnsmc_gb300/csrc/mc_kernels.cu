@@ -511,6 +511,65 @@ int launch_adaptive_rays(const AdaptParams &a, void *stream) {
     return (int)cudaGetLastError();
 }
 
+// Longest-first queue order.  Bucket of an item = min(rays / B, buckets - 1),
+// counted in descending bucket order; items of one bucket keep no particular
+// order (results do not depend on the processing order).
+__global__ void order_hist_kernel(const int *rays, int gstride, int n_packets, int n_groups, long long n_items, int B,
+                                  unsigned int *hist) {
+    const long long per_field = (long long)n_groups * n_packets;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_items;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long gp = i % per_field;
+        const int g = (int)(gp / n_packets), p = (int)(gp % n_packets);
+        const int b = min(rays[g * gstride + p] / B, kOrderBuckets - 1);
+        atomicAdd(hist + (kOrderBuckets - 1 - b), 1u);
+    }
+}
+
+// exclusive scan of the kOrderBuckets counts in place (one block of 1024)
+__global__ void order_scan_kernel(unsigned int *hist) {
+    __shared__ unsigned int part[1024];
+    constexpr int per = kOrderBuckets / 1024;
+    const int t = threadIdx.x;
+    unsigned int loc[per], run = 0;
+    for (int q = 0; q < per; ++q) { loc[q] = hist[t * per + q]; run += loc[q]; }
+    part[t] = run;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const unsigned int v = t >= o ? part[t - o] : 0u;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    unsigned int base = t ? part[t - 1] : 0u;
+    for (int q = 0; q < per; ++q) { const unsigned int v = loc[q]; hist[t * per + q] = base; base += v; }
+}
+
+__global__ void order_scatter_kernel(const int *rays, int gstride, int n_packets, int n_groups, long long n_items,
+                                     int B, unsigned int *hist, unsigned int *order) {
+    const long long per_field = (long long)n_groups * n_packets;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n_items;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long gp = i % per_field;
+        const int g = (int)(gp / n_packets), p = (int)(gp % n_packets);
+        const int b = min(rays[g * gstride + p] / B, kOrderBuckets - 1);
+        const unsigned int pos = atomicAdd(hist + (kOrderBuckets - 1 - b), 1u);
+        order[pos] = (unsigned int)i;
+    }
+}
+
+int launch_item_order(const int *rays, int gstride, int n_packets, int n_groups, long long n_items, int B,
+                      unsigned int *hist, unsigned int *order, void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned int), st);
+    if (e != cudaSuccess) return (int)e;
+    order_hist_kernel<<<grid_for(n_items, 256), 256, 0, st>>>(rays, gstride, n_packets, n_groups, n_items, B, hist);
+    order_scan_kernel<<<1, 1024, 0, st>>>(hist);
+    order_scatter_kernel<<<grid_for(n_items, 256), 256, 0, st>>>(rays, gstride, n_packets, n_groups, n_items, B,
+                                                                 hist, order);
+    return (int)cudaGetLastError();
+}
+
 int launch_cv_prepare(const CvParams &c, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     cv_layer_kernel<<<dim3(c.nw, c.nfields), 256, 0, st>>>(c);

@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             if (lane == 0) it = atomicAdd(P.queue, 1u);
             it = __shfl_sync(FULL, it, 0);
             if ((long long)it >= P.n_items) break;
-            item = it;
+            item = P.item_order ? (long long)__ldg(P.item_order + it) : (long long)it;
         }
         const int p = (int)(item % P.n_packets);
         const long long fg = item / P.n_packets;
