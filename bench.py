@@ -10,7 +10,7 @@ timed with CUDA events on the solver's stream: for the default network
 control variate, the network's features, forward pass and ray allocation,
 then the sampling-table upload, the control-variate preparation, the march,
 the finalize kernel and the copy of Q and sigma into pinned host memory.  The
-network is the committed one for the grid (dnsmc_gb300/nets/ck128.cvnet) or,
+network is the committed one for the grid (dnsmc_gb300/nets/ck128_g8.cvnet) or,
 when absent, trained before the timed region on 16 snapshots the Monte Carlo
 itself produces.  The ray budget (mean rays per cell and group) is the
 smallest one whose estimated RMS error sqrt(mean var(Q)) / rms(Q) is <= 1 %

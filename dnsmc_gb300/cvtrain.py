@@ -2,7 +2,7 @@
 snapshots the Monte Carlo itself produces.
 
     python -m dnsmc_gb300.cvtrain --n 128 --fields 64 --rays 64 --epochs 3 \\
-        --out dnsmc_gb300/nets/ck128.cvnet
+        --out dnsmc_gb300/nets/ck128_g8.cvnet
 
 Every snapshot (synth.ck_channel with its own seed) is solved with the
 control variate and per-ray moments on a sub-region of cells (full wall-normal
