@@ -551,10 +551,16 @@ def run_c4(args):
     return 0
 
 
+# DRAM bytes (read + write) of one march launch measured by an ncu capture of
+# the default command (128^3, network control variate): the tallies and L2
+# refills, not the gathers, which L1/L2 serve
+MARCH_DRAM_BYTES = {("net", 128): 432.6e6 + 775.07e6}
+
 # kernels per step: table coordinates, march, finalize; the control variate adds
 # layer means, surrogate table, 1-D quadrature and E[Y]; the network adds
-# features, MLP, coefficients/costs and three allocation kernels
-LAUNCHES = {"plain": 3, "cv": 7, "net": 13}
+# features, MLP, coefficients/costs, three allocation kernels and the three
+# kernels of the longest-first queue order
+LAUNCHES = {"plain": 3, "cv": 7, "net": 16}
 
 
 def main():
@@ -675,9 +681,10 @@ def main():
         "rays_per_s": rays_s, "ray_steps_per_s": r["steps"] * world / (t_max / 1e3),
         "march_ms": march_avg, "step_ms": float(np.mean(r["ms"])),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind,
+                     "traffic": MARCH_DRAM_BYTES.get((args.method, N_CELL)), "peak_kind": peak_kind,
                      "note": f"algorithmic gather bytes {BYTES_PER_STEP} B per ray-voxel step x lane-steps per "
-                             f"launch / march kernel time (CUDA events)"},
+                             f"launch / march kernel time (CUDA events); traffic = ncu DRAM read+write bytes "
+                             f"per march launch"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_max, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "timing": "wall clock around set_fields + (network) + solve + get_results"},
