@@ -39,7 +39,7 @@ class Config(ctypes.Structure):
         ("model", ctypes.c_int), ("kappa", ctypes.c_float), ("n_groups", ctypes.c_int),
         ("seed", ctypes.c_uint64), ("sampler", ctypes.c_int), ("local_sampling", ctypes.c_int),
         ("control_variate", ctypes.c_int), ("cv_moments", ctypes.c_int),
-        ("block_threads", ctypes.c_int), ("tile_a", ctypes.c_int),
+        ("block_threads", ctypes.c_int), ("tile_a", ctypes.c_int), ("mg_steps", ctypes.c_int),
     ]
 
 
@@ -94,6 +94,7 @@ SIGNATURES = {
     "dnsmc_get_cv_beta": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
     "dnsmc_get_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p)]),
     "dnsmc_set_graph": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dnsmc_get_coarse_field": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, c_float_p]),
     "dnsmc_get_graph_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
                                             ctypes.POINTER(ctypes.c_longlong)]),
     "dnsmc_set_rays_adaptive": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_int, ctypes.c_int]),

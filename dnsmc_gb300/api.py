@@ -240,6 +240,13 @@ class Solver:
         self._keep = []
         self._rays_dev = True
 
+    def coarse_field(self, field: int, level: int):
+        """Spline-coarsened T of a multigrid level, (nk, nj, ni) >> level."""
+        c = self.cfg
+        out = np.zeros((c.kmax >> level, c.jmax >> level, c.imax >> level), np.float32)
+        check(self._lib.dnsmc_get_coarse_field(self._h, field, level, _fp(out)))
+        return out
+
     def set_graph(self, enable: bool = True) -> None:
         check(self._lib.dnsmc_set_graph(self._h, 1 if enable else 0))
 

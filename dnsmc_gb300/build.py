@@ -55,7 +55,8 @@ def build(verbose: bool = False) -> str:
     jobs = [
         [nvcc, *ARCH, *common, *regs, "-fmad=false", "-c", os.path.join(CSRC, "mc_kernels.cu"),
          "-o", os.path.join(bdir, "mc_kernels.o")],
-        [nvcc, *common, "-x", "c++", "-c", os.path.join(CSRC, "mc_host.cpp"),
+        # no FMA contraction in host arithmetic: identical results on x86 and Arm hosts
+        [nvcc, *common, "-Xcompiler", "-ffp-contract=off", "-x", "c++", "-c", os.path.join(CSRC, "mc_host.cpp"),
          "-o", os.path.join(bdir, "mc_host.o")],
         [nvcc, *ARCH, *common, *regs, "-fmad=false", "-c", os.path.join(CSRC, "mc_march_gen.cu"),
          "-o", os.path.join(bdir, "mc_march_gen.o")],

@@ -170,6 +170,119 @@ void make_faces(int im, float L, int stretched, std::vector<float> &xu) {
     for (int i = 1; i < im + 1; ++i) xu[i] = xu0[i * im0 / im];
 }
 
+// ---- multigrid: coarse grids and spline-coarsened temperature --------------
+// Level l has (imax, jmax, kmax) >> l cells.  Its wall-normal faces are the
+// reference grid at that resolution (code/definitions.h:68-136): every
+// 2^l-th fine face when stretched, i * Lx / im when uniform; j and k faces
+// are i * L / n.  The temperature of a coarse cell is the fine field
+// interpolated at the coarse cell centre by separable natural cubic splines
+// through the fine cell centres, x first, then y, then z (the reference's
+// interp3D, code/spline.cpp:35-116, with spline/splint, :119-170).
+void coarse_faces(int im0, int l, float L, int stretched, std::vector<float> &xu) {
+    const int im = im0 >> l;
+    xu.assign(im + 1, 0.0f);
+    if (!stretched) {
+        for (int i = 0; i <= im; ++i) xu[i] = (float)i * (L / (float)im);
+        xu[im] = L;
+        return;
+    }
+    std::vector<float> f;
+    make_faces(im0, L, 1, f);
+    for (int i = 0; i <= im; ++i) xu[i] = f[(size_t)i * im0 / im];
+}
+
+// centres c[1..n] of faces u[0..n] (1-based, as the splines below)
+void centres(const std::vector<float> &u, std::vector<float> &c) {
+    const int n = (int)u.size() - 1;
+    c.assign(n + 2, 0.0f);
+    for (int i = 1; i <= n; ++i) c[i] = (u[i - 1] + u[i]) * 0.5f;
+}
+
+void uniform_faces(int n, float L, std::vector<float> &u) {
+    u.assign(n + 1, 0.0f);
+    const float d = L / (float)n;
+    for (int i = 0; i <= n; ++i) u[i] = (float)i * d;
+}
+
+// Natural cubic spline second derivatives y2[1..n] of y[1..n] at x[1..n].
+void nat_spline(const float *x, const float *y, int n, float *y2, std::vector<float> &u) {
+    u.assign(n + 1, 0.0f);
+    y2[1] = u[1] = 0.0f;
+    for (int i = 2; i <= n - 1; ++i) {
+        const float sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+        const float p = sig * y2[i - 1] + 2.0f;
+        y2[i] = (sig - 1.0f) / p;
+        const float ui = (y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]);
+        u[i] = (float)((6.0 * ui / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p);
+    }
+    y2[n] = 0.0f;
+    for (int k = n - 1; k >= 1; --k) y2[k] = y2[k] * y2[k + 1] + u[k];
+}
+
+// Cubic spline value at v (bisection for the bracketing interval).
+float nat_splint(const float *xa, const float *ya, const float *y2a, int n, float v) {
+    int lo = 1, hi = n;
+    while (hi - lo > 1) {
+        const int k = (hi + lo) >> 1;
+        if (xa[k] > v) hi = k; else lo = k;
+    }
+    const float h = xa[hi] - xa[lo];
+    const float a = (xa[hi] - v) / h, b = (v - xa[lo]) / h;
+    return (float)(a * ya[lo] + b * ya[hi] + ((a * a * a - a) * y2a[lo] + (b * b * b - b) * y2a[hi]) * (h * h) / 6.0);
+}
+
+// Coarsen one dense fine field T[k][j][i] (i fastest) to levels 1..L-1;
+// out[l] receives (im>>l)*(jm>>l)*(km>>l) values in the march layout
+// [i][k][j] (j fastest).
+void spline_coarsen(const float *T, int I, int J, int K, float Lx, float Ly, float Lz, int stretched, int levels,
+                    std::vector<std::vector<float>> &out) {
+    std::vector<float> xu, yu, zu, xc, yc, zc;
+    make_faces(I, Lx, stretched, xu);
+    uniform_faces(J, Ly, yu);
+    uniform_faces(K, Lz, zu);
+    centres(xu, xc);
+    centres(yu, yc);
+    centres(zu, zc);
+    out.assign(levels, {});
+    std::vector<float> a(std::max({I, J, K}) + 2), a2(std::max({I, J, K}) + 2), u;
+    for (int l = 1; l < levels; ++l) {
+        const int im = I >> l, jm = J >> l, km = K >> l;
+        std::vector<float> cxu, cyu, czu, cx, cy, cz;
+        coarse_faces(I, l, Lx, stretched, cxu);
+        uniform_faces(jm, Ly, cyu);
+        uniform_faces(km, Lz, czu);
+        centres(cxu, cx);
+        centres(cyu, cy);
+        centres(czu, cz);
+        // along x: tx[k][j][ic]
+        std::vector<float> tx((size_t)im * J * K), txy((size_t)im * jm * K);
+        for (int k = 0; k < K; ++k)
+            for (int j = 0; j < J; ++j) {
+                for (int i = 1; i <= I; ++i) a[i] = T[(size_t)i - 1 + (size_t)I * (j + (size_t)J * k)];
+                nat_spline(xc.data(), a.data(), I, a2.data(), u);
+                for (int i = 1; i <= im; ++i)
+                    tx[(size_t)i - 1 + (size_t)im * (j + (size_t)J * k)] = nat_splint(xc.data(), a.data(), a2.data(), I, cx[i]);
+            }
+        // along y: txy[k][jc][ic]
+        for (int i = 0; i < im; ++i)
+            for (int k = 0; k < K; ++k) {
+                for (int j = 1; j <= J; ++j) a[j] = tx[(size_t)i + (size_t)im * (j - 1 + (size_t)J * k)];
+                nat_spline(yc.data(), a.data(), J, a2.data(), u);
+                for (int j = 1; j <= jm; ++j)
+                    txy[(size_t)i + (size_t)im * (j - 1 + (size_t)jm * k)] = nat_splint(yc.data(), a.data(), a2.data(), J, cy[j]);
+            }
+        // along z, into the march layout [ic][kc][jc]
+        out[l].assign((size_t)im * jm * km, 0.0f);
+        for (int i = 0; i < im; ++i)
+            for (int j = 0; j < jm; ++j) {
+                for (int k = 1; k <= K; ++k) a[k] = txy[(size_t)i + (size_t)im * (j + (size_t)jm * (k - 1))];
+                nat_spline(zc.data(), a.data(), K, a2.data(), u);
+                for (int k = 1; k <= km; ++k)
+                    out[l][((size_t)i * km + (k - 1)) * jm + j] = nat_splint(zc.data(), a.data(), a2.data(), K, cz[k]);
+            }
+    }
+}
+
 // Sobol' direction numbers of four dimensions (Bratley-Fox recurrence on the
 // primitive polynomials 1, x+1, x^2+x+1, x^3+x+1 with initial m = 1 | 1 |
 // 1,3 | 1,3,1), 32 bits.
@@ -277,6 +390,12 @@ struct dnsmc_solver {
     DevBuf<unsigned int> d_order, d_order_hist;  // longest-first queue order (per-item ray tables)
     DevBuf<float> d_kP;                      // Planck-mean absorption coefficient on the table grid
 
+    // multigrid: spline-coarsened temperatures of levels 1..grid_num-1
+    DevBuf<float> d_mgT, d_mgfw;
+    long long mg_off[kMaxLevels] = {0};
+    int mg_fwoff[kMaxLevels] = {0};
+    int mg_fields = 0;
+
     // particles (general medium): per-band coefficients per unit volume
     // fraction and the volume-fraction field of the resident snapshots
     std::vector<float2> part;
@@ -376,7 +495,13 @@ int check_config(const dnsmc_config &c) {
     if (c.nvar < 1 || c.photmax < 1) return fail(DNSMC_ERR_ARG, "nvar and photmax must be >= 1");
     if (!(c.toll > 0) || c.toll >= 1) return fail(DNSMC_ERR_ARG, "toll must be in (0,1)");
     if (c.max_steps < 1) return fail(DNSMC_ERR_ARG, "max_steps must be >= 1");
-    if (c.grid_num != 1) return fail(DNSMC_ERR_ARG, "grid_num %d: only the fine grid (grid_num = 1) is marched", c.grid_num);
+    if (c.grid_num < 1 || c.grid_num > kMaxLevels) return fail(DNSMC_ERR_ARG, "grid_num must be 1..%d", kMaxLevels);
+    if (c.grid_num > 1) {
+        const int r = 1 << (c.grid_num - 1);
+        if (c.imax % r || c.jmax % r || c.kmax % r)
+            return fail(DNSMC_ERR_ARG, "grid_num %d needs imax, jmax, kmax divisible by %d", c.grid_num, r);
+        if (c.mg_steps < 1) return fail(DNSMC_ERR_ARG, "mg_steps must be >= 1");
+    }
     if (c.model < 0 || c.model > 4) return fail(DNSMC_ERR_ARG, "unknown model %d", c.model);
     if (c.n_groups < 1) return fail(DNSMC_ERR_ARG, "n_groups must be >= 1");
     if (c.sampler != DNSMC_SAMPLER_IID && c.sampler != DNSMC_SAMPLER_RQMC) return fail(DNSMC_ERR_ARG, "unknown sampler %d", c.sampler);
@@ -870,6 +995,26 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.hg_g = s->hg_g;
     P.eps[0] = c.eps_west; P.eps[1] = c.eps_east;
     P.W4sig = (float)(4.0 * kSigma);
+    // multigrid: the reference's plain estimator only
+    const bool mg = c.grid_num > 1;
+    if (mg) {
+        if (mode == MODE_TX) return fail(DNSMC_ERR_STATE, "multigrid needs a table without an x_H2O axis");
+        if (c.control_variate) return fail(DNSMC_ERR_STATE, "multigrid is not combined with the control variate");
+        if (gen) return fail(DNSMC_ERR_STATE, "multigrid is not combined with particles or grey walls");
+        if (s->mg_fields != s->nfields) return fail(DNSMC_ERR_STATE, "coarse fields missing: set the fields again");
+        P.mg_levels = c.grid_num;
+        P.mg_steps = c.mg_steps;
+        P.mgT = s->d_mgT.p;
+        P.mgfw = s->d_mgfw.p;
+        for (int l = 1; l < c.grid_num; ++l) {
+            P.mg_off[l] = s->mg_off[l];
+            P.mg_fwoff[l] = s->mg_fwoff[l];
+            P.mg_da[l] = c.Ly / (float)(c.jmax >> l);
+            P.mg_db[l] = c.Lz / (float)(c.kmax >> l);
+        }
+        P.Ly = c.Ly;
+        P.Lz = c.Lz;
+    }
     P.rays = s->rays;
     const bool per_item = !s->rays_pp.empty() || s->rays_dev;
     P.rays_per_packet = per_item ? s->d_rays_pp.p : nullptr;
@@ -911,7 +1056,8 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         P.trace_f = tf; P.trace_g = tg; P.trace_p = tp; P.trace_r = tr; P.trace_max = tmax_steps;
         P.trace_rec = d_trace_rec; P.trace_n = d_trace_n; P.trace_rng = d_trace_rng;
         P.tally = nullptr;
-        const int rc = launch_march_ex(mode, P, 1, 32, s->stream, true, cv, false, gen);
+        const int rc = mg ? launch_march_mg(mode, P, 1, 32, s->stream, true)
+                          : launch_march_ex(mode, P, 1, 32, s->stream, true, cv, false, gen);
         if (rc) return fail(DNSMC_ERR_CUDA, "trace launch: %s", cudaGetErrorString((cudaError_t)rc));
         return DNSMC_OK;
     }
@@ -980,7 +1126,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         P.item_order = s->d_order.p;
     }
     const int sms = device_sm_count();
-    const int occ = march_occupancy_ex(mode, threads, cv, mom, gen);
+    const int occ = mg ? march_mg_occupancy(mode, threads) : march_occupancy_ex(mode, threads, cv, mom, gen);
     const int blocks = std::max(1, sms * occ);
 
     FinalizeParams F;
@@ -1030,7 +1176,8 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
             if (rco) return fail(DNSMC_ERR_CUDA, "queue order launch: %s", cudaGetErrorString((cudaError_t)rco));
         }
         if (events) CUDA_TRY(cudaEventRecord(s->ev_march0, s->stream));
-        int rc = launch_march_ex(mode, P, blocks, threads, s->stream, false, cv, mom, gen);
+        int rc = mg ? launch_march_mg(mode, P, blocks, threads, s->stream, false)
+                    : launch_march_ex(mode, P, blocks, threads, s->stream, false, cv, mom, gen);
         if (rc) return fail(DNSMC_ERR_CUDA, "march launch: %s", cudaGetErrorString((cudaError_t)rc));
         if (events) CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
         rc = launch_finalize(F, s->stream);
@@ -1105,6 +1252,41 @@ int wait_done(dnsmc_solver *s, double timeout_s) {
     return DNSMC_OK;
 }
 
+// Coarse temperatures of every field for the multigrid march; Tdense(f)
+// gives field f dense, i fastest.
+template <class Get>
+int upload_coarse(dnsmc_solver *s, int nfields, Get Tdense) {
+    const dnsmc_config &c = s->cfg;
+    const int G = c.grid_num;
+    long long off = 0;
+    for (int l = 1; l < G; ++l) {
+        s->mg_off[l] = off;
+        off += (long long)nfields * (c.imax >> l) * (c.jmax >> l) * (c.kmax >> l);
+    }
+    std::vector<float> all((size_t)std::max(1LL, off));
+    std::vector<std::vector<float>> lv;
+    for (int f = 0; f < nfields; ++f) {
+        spline_coarsen(Tdense(f), c.imax, c.jmax, c.kmax, c.Lx, c.Ly, c.Lz, c.stretched_x, G, lv);
+        for (int l = 1; l < G; ++l)
+            std::copy(lv[l].begin(), lv[l].end(), all.begin() + s->mg_off[l] + (long long)f * lv[l].size());
+    }
+    std::vector<float> faces;
+    int fo = 0;
+    for (int l = 1; l < G; ++l) {
+        std::vector<float> xu;
+        coarse_faces(c.imax, l, c.Lx, c.stretched_x, xu);
+        s->mg_fwoff[l] = fo;
+        faces.insert(faces.end(), xu.begin(), xu.end());
+        fo += (int)xu.size();
+    }
+    TRY(s->d_mgT.ensure(all.size()));
+    TRY(s->d_mgfw.ensure(faces.size()));
+    CUDA_TRY(cudaMemcpy(s->d_mgT.p, all.data(), all.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(cudaMemcpy(s->d_mgfw.p, faces.data(), faces.size() * sizeof(float), cudaMemcpyHostToDevice));
+    s->mg_fields = nfields;
+    return DNSMC_OK;
+}
+
 int upload_fields_host(dnsmc_solver *s, int nfields, const float *T, const float *x, int layout) {
     const dnsmc_config &c = s->cfg;
     const long long ncell = (long long)c.imax * c.jmax * c.kmax;
@@ -1155,6 +1337,18 @@ int upload_fields_host(dnsmc_solver *s, int nfields, const float *T, const float
         if (rc) return fail(DNSMC_ERR_CUDA, "pack launch: %s", cudaGetErrorString((cudaError_t)rc));
     }
     CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (c.grid_num > 1) {
+        std::vector<float> dense;
+        TRY(upload_coarse(s, nfields, [&](int f) -> const float * {
+            if (layout == DNSMC_LAYOUT_DENSE) return T + f * nsrc;
+            dense.resize((size_t)ncell);
+            for (int k = 0; k < c.kmax; ++k)
+                for (int j = 0; j < c.jmax; ++j)
+                    for (int i = 0; i < c.imax; ++i)
+                        dense[(size_t)i + (size_t)c.imax * (j + (size_t)c.jmax * k)] = T[f * nsrc + base + j * sj + k * sk + i];
+            return dense.data();
+        }));
+    }
     s->nfields = nfields;
     s->have_x = want_x;
     s->tmax_fields = tmax;
@@ -1276,6 +1470,7 @@ void dnsmc_set_default_config(dnsmc_config *c) {
     c->cv_moments = 0;
     c->block_threads = 0;
     c->tile_a = 0;
+    c->mg_steps = 5;  // code/param.h:18-37 (maxs of every grid but the last)
 }
 
 int dnsmc_config_from_env(dnsmc_config *c) {
@@ -1284,6 +1479,7 @@ int dnsmc_config_from_env(dnsmc_config *c) {
         {"DNSMC_IMAX", &c->imax, nullptr}, {"DNSMC_JMAX", &c->jmax, nullptr}, {"DNSMC_KMAX", &c->kmax, nullptr},
         {"DNSMC_PROW", &c->p_row, nullptr}, {"DNSMC_NVAR", &c->nvar, nullptr}, {"DNSMC_PHOTMAX", &c->photmax, nullptr},
         {"DNSMC_MODEL", &c->model, nullptr}, {"DNSMC_GRID_NUM", &c->grid_num, nullptr},
+        {"DNSMC_MG_STEPS", &c->mg_steps, nullptr},
         {"DNSMC_STRETCHED", &c->stretched_x, nullptr}, {"DNSMC_GROUPS", &c->n_groups, nullptr},
         {"DNSMC_LX", nullptr, &c->Lx}, {"DNSMC_LY", nullptr, &c->Ly}, {"DNSMC_LZ", nullptr, &c->Lz},
         {"DNSMC_TWEST", nullptr, &c->T_west}, {"DNSMC_TEAST", nullptr, &c->T_east},
@@ -1342,6 +1538,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();
     s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_item_steps.release(); s->d_kP.release();
     s->d_order.release(); s->d_order_hist.release();
+    s->d_mgT.release(); s->d_mgfw.release();
     s->d_part.release(); s->d_fieldV.release(); s->d_layerV.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
     s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_Qg.release(); s->d_varg.release();
@@ -1484,6 +1681,13 @@ int dnsmc_set_fields_device(dnsmc_solver *s, int nfields, const float *dT, const
     CUDA_TRY(cudaMemcpyAsync(st, s->d_stat_out.p, sizeof st, cudaMemcpyDeviceToHost, s->stream));
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     if (!(st[1] > 0) || !std::isfinite(st[0])) return fail(DNSMC_ERR_ARG, "temperature field has non-positive or non-finite values");
+    if (c.grid_num > 1) {  // the spline coarsening runs on the host
+        std::vector<float> h((size_t)ncell);
+        TRY(upload_coarse(s, nfields, [&](int f) -> const float * {
+            cudaMemcpy(h.data(), dT + f * ncell, (size_t)ncell * sizeof(float), cudaMemcpyDeviceToHost);
+            return h.data();
+        }));
+    }
     s->nfields = nfields;
     s->have_x = dx != nullptr;
     s->tmax_fields = st[0];
@@ -1636,6 +1840,24 @@ int dnsmc_set_rays_per_item(dnsmc_solver *s, int n_groups, const int *rays) {
     s->rays_dev = false;
     TRY(s->d_rays_pp.ensure(n));
     CUDA_TRY(cudaMemcpy(s->d_rays_pp.p, s->rays_pp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+    return DNSMC_OK;
+}
+
+int dnsmc_get_coarse_field(dnsmc_solver *s, int field, int level, float *T) {
+    if (!s || !T) return fail(DNSMC_ERR_ARG, "null argument");
+    const dnsmc_config &c = s->cfg;
+    if (level < 1 || level >= c.grid_num) return fail(DNSMC_ERR_ARG, "level must be 1..grid_num-1");
+    if (field < 0 || field >= s->mg_fields) return fail(DNSMC_ERR_ARG, "no such field");
+    TRY(set_device(s));
+    TRY(wait_done(s, 0));
+    const int im = c.imax >> level, jm = c.jmax >> level, km = c.kmax >> level;
+    const size_t n = (size_t)im * jm * km;
+    std::vector<float> h(n);
+    CUDA_TRY(cudaMemcpy(h.data(), s->d_mgT.p + s->mg_off[level] + (long long)field * n, n * sizeof(float),
+                        cudaMemcpyDeviceToHost));
+    for (int i = 0; i < im; ++i)
+        for (int k = 0; k < km; ++k)
+            for (int j = 0; j < jm; ++j) T[(size_t)i + (size_t)im * (j + (size_t)jm * k)] = h[((size_t)i * km + k) * jm + j];
     return DNSMC_OK;
 }
 

@@ -19,6 +19,8 @@ namespace dnsmc {
 
 enum MarchMode { MODE_GREY = 0, MODE_T = 1, MODE_TX = 2 };
 
+constexpr int kMaxLevels = 6;  // multigrid levels (grid_num)
+
 // One alias-table entry of a spectral sample (band, g) inside a band group.
 struct SpecEntry {
     float    prob;      // alias threshold (quantised to multiples of 2^-24)
@@ -75,6 +77,15 @@ struct MarchParams {
     float hg_g;               // Henyey-Greenstein asymmetry factor
     float eps[2];             // wall emissivities (west, east)
     float W4sig;              // 4 sigma (grey model weight per unit absorption coefficient)
+    // multigrid (MG march): after mg_steps steps a ray continues on the next
+    // grid, 2x coarser per axis; level l has (nw, na, nb) >> l cells
+    int mg_levels, mg_steps;
+    const float *mgT;                  // coarse temperatures, level l at mg_off[l]: [f][i][k][j]
+    const float *mgfw;                 // coarse wall-normal faces, level l at mg_fwoff[l]
+    long long mg_off[kMaxLevels];
+    int mg_fwoff[kMaxLevels];
+    float mg_da[kMaxLevels], mg_db[kMaxLevels];  // periodic cell sizes per level
+    float Ly, Lz;
     int max_steps;
     // work queue and outputs
     unsigned int *queue;      // atomic item counter (zeroed per launch)
@@ -181,6 +192,8 @@ int launch_item_order(const int *rays, int gstride, int n_packets, int n_groups,
 int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                     bool mom, bool gen);
 int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen);
+int launch_march_mg(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace);
+int march_mg_occupancy(int mode, int threads);
 int launch_march_gen(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                      bool mom);                                      // mc_march_gen.cu
 int march_gen_occupancy(int mode, int threads, bool cv, bool mom);    // mc_march_gen.cu

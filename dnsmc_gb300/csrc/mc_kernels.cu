@@ -206,6 +206,36 @@ int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen) {
     return march_variant_occupancy<false>(mode, threads, cv, mom);
 }
 
+// Multigrid march (reference tables or grey model; no control variate, no
+// particles, black walls).
+int launch_march_mg(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace) {
+    cudaStream_t st = (cudaStream_t)stream;
+    if (trace) { blocks = 1; threads = 32; }
+    if (mode == MODE_GREY) {
+        if (trace) march_kernel<MODE_GREY, true, false, false, false, true><<<blocks, threads, 0, st>>>(p);
+        else march_kernel<MODE_GREY, false, false, false, false, true><<<blocks, threads, 0, st>>>(p);
+    } else if (mode == MODE_T) {
+        if (trace) march_kernel<MODE_T, true, false, false, false, true><<<blocks, threads, 0, st>>>(p);
+        else march_kernel<MODE_T, false, false, false, false, true><<<blocks, threads, 0, st>>>(p);
+    } else {
+        return (int)cudaErrorInvalidValue;
+    }
+    return (int)cudaGetLastError();
+}
+
+int march_mg_occupancy(int mode, int threads) {
+    int nb = 0;
+    cudaError_t e = cudaErrorInvalidValue;
+    if (mode == MODE_GREY)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false, false, false, false, true>,
+                                                          threads, 0);
+    if (mode == MODE_T)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false, false, false, false, true>,
+                                                          threads, 0);
+    if (e != cudaSuccess) return 1;
+    return nb > 0 ? nb : 1;
+}
+
 int launch_march(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace) {
     return launch_march_ex(mode, p, blocks, threads, stream, trace, false, false, false);
 }

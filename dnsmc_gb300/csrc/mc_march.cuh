@@ -286,7 +286,7 @@ __device__ __forceinline__ void surrogate_walk(const MarchParams &P, const float
 #ifndef DNSMC_MINB
 #define DNSMC_MINB 4
 #endif
-template <int MODE, bool TRACE, bool CV, bool MOM, bool GEN>
+template <int MODE, bool TRACE, bool CV, bool MOM, bool GEN, bool MG = false>
 __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParams P) {
     typedef typename FieldT<MODE>::type VT;
     const unsigned FULL = 0xffffffffu;
@@ -624,9 +624,103 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 vcur = vnext;
                 if constexpr (GEN) fvcur = fvnext;
                 if (!__any_sync(FULL, tau > 0.0f)) break;
-                if (steps >= P.max_steps) {
-                    if (tau > 0.0f) flags |= DNSMC_STATUS_STEP_CAP;
+                if (steps >= (MG ? P.mg_steps : P.max_steps)) {
+                    if (!MG && tau > 0.0f) flags |= DNSMC_STATUS_STEP_CAP;
                     break;
+                }
+            }
+            if constexpr (MG) {
+                // Coarse grids (the reference's grid switch, code/mc_gpu.cu:193-207):
+                // every lane continues from its own point with the reference's
+                // position-update march; lanes no longer share their cell
+                // faces, but they step in lockstep and leave a level together.
+                if (__any_sync(FULL, tau > 0.0f)) {
+                    const float ua = t / dtA - (float)nA, ub = t / dtB - (float)nB;
+                    const float fa = fminf(fmaxf(dA > 0 ? 0.5f + ua : 0.5f - ua, 0.0f), 1.0f);
+                    const float fb = fminf(fmaxf(dB > 0 ? 0.5f + ub : 0.5f - ub, 0.0f), 1.0f);
+                    float xp = fmaf(sW, t, oW);
+                    float yp = ((float)ca + fa) * P.da;
+                    float zp = ((float)cb + fb) * P.db;
+                    int ic = cw, jc = ca, kc = cb;
+                    const float isx = 1.0f / sW, isy = 1.0f / sA, isz = 1.0f / sB;
+                    int counter = 0, cap = 0;
+                    for (int l = 1; l < P.mg_levels; ++l) {
+                        ic >>= 1; jc >>= 1; kc >>= 1;
+                        const int nwL = P.nw >> l, naL = P.na >> l, nbL = P.nb >> l;
+                        const float *fwL = P.mgfw + P.mg_fwoff[l];
+                        const float daL = P.mg_da[l], dbL = P.mg_db[l];
+                        const float *TL = P.mgT + P.mg_off[l] + (long long)f * nwL * naL * nbL;
+                        cap = (l == P.mg_levels - 1) ? P.max_steps : P.mg_steps;
+                        counter = 0;
+                        while (__any_sync(FULL, tau > 0.0f && counter < cap)) {
+                            float dsr = 0.0f;  // this lane's segment (0 when it idles)
+                            if (tau > 0.0f && counter < cap) {
+                                const float fx = __ldg(fwL + (dW > 0 ? ic + 1 : ic));
+                                const float fy = (float)(dA > 0 ? jc + 1 : jc) * daL;
+                                const float fz = (float)(dB > 0 ? kc + 1 : kc) * dbL;
+                                const float dsx = sW != 0.0f ? (fx - xp) * isx : INF;
+                                const float dsy = sA != 0.0f ? (fy - yp) * isy : INF;
+                                const float dsz = sB != 0.0f ? (fz - zp) * isz : INF;
+                                const float Tc = __ldg(TL + ((long long)ic * nbL + kc) * naL + jc);
+                                float kj, gj;
+                                if constexpr (MODE == MODE_GREY) {
+                                    const float t2 = Tc * Tc;
+                                    gj = (Ti4 - t2 * t2) * invI;
+                                    kj = P.kappa;
+                                } else {
+                                    float pt = (Tc - P.T0) * P.invdT;
+                                    pt = fminf(fmaxf(pt, 0.0f), (float)(P.nT - 1));
+                                    int tj;
+                                    float ftj;
+                                    pos_split(pt, P.nT, &tj, &ftj);
+                                    kj = lookup_k<MODE_T>(P, sid, tj, ftj, 0.0f);
+                                    gj = (Ii - lookup_ib(P, nbnd, tj, ftj)) * invI;
+                                }
+                                float dmin = dsx;
+                                if (dmin > dsy) dmin = dsy;
+                                if (dmin > dsz) dmin = dsz;
+                                const float ds = fmaxf(dmin, 0.0f);
+                                dsr = ds;
+                                xp = (dmin == dsx) ? fx : fmaf(ds, sW, xp);
+                                yp = (dmin == dsy) ? fy : fmaf(ds, sA, yp);
+                                zp = (dmin == dsz) ? fz : fmaf(ds, sB, zp);
+                                const float alpha = -mc_expm1(-(kj * ds));
+                                const float ta = tau * alpha;
+                                D = fmaf(ta, gj, D);
+                                tau = tau - ta;
+                                if (tau < P.toll) { D = fmaf(tau, gj, D); tau = 0.0f; }
+                                int axis;
+                                if (dsx < dsy) axis = (dsx < dsz) ? 0 : 2;
+                                else axis = (dsy < dsz) ? 1 : 2;
+                                if (axis == 0) {
+                                    ic += dW;
+                                    if (ic < 0 || ic >= nwL) {
+                                        const int side = ic < 0 ? 0 : 1;
+                                        const float Iw = (MODE == MODE_GREY) ? P.Tw4[side]
+                                                                             : __ldg(P.ibw + side * P.nbands + nbnd);
+                                        if (tau > 0.0f) D = fmaf(tau, (Ii - Iw) * invI, D);
+                                        tau = 0.0f;
+                                        ic = ic < 0 ? 0 : nwL - 1;
+                                    }
+                                } else if (axis == 1) {
+                                    jc += dA;
+                                    if (jc >= naL) { jc = 0; yp = 0.0f; } else if (jc < 0) { jc = naL - 1; yp = P.Ly; }
+                                } else {
+                                    kc += dB;
+                                    if (kc >= nbL) { kc = 0; zp = 0.0f; } else if (kc < 0) { kc = nbL - 1; zp = P.Lz; }
+                                }
+                                ++lsteps;
+                            }
+                            if (TRACE && lane == 0 && steps < P.trace_max) {  // every iteration
+                                int *rec = P.trace_rec + 6 * steps;
+                                rec[0] = ic; rec[1] = jc; rec[2] = kc; rec[3] = 16 + l;
+                                rec[4] = __float_as_int(dsr); rec[5] = __float_as_int(tau);
+                            }
+                            ++counter;
+                            ++steps;
+                        }
+                    }
+                    if (tau > 0.0f) flags |= DNSMC_STATUS_STEP_CAP;
                 }
             }
             if (TRACE && lane == 0) *P.trace_n = steps;

@@ -93,7 +93,10 @@ typedef struct dnsmc_config {
     /* march (code/param.h:72, :25-37) */
     float toll;                  /* transmissivity cut-off                      */
     int   max_steps;             /* per-ray step cap                             */
-    int   grid_num;              /* multigrid levels; 1 = fine grid only        */
+    int   grid_num;              /* multigrid levels (code/param.h:18-37): rays  */
+                                 /* march mg_steps steps on each grid, then    */
+                                 /* continue on the next grid, 2x coarser per  */
+                                 /* axis (spline-coarsened T); 1 = fine only   */
     /* spectral model */
     int   model;                 /* DNSMC_MODEL_*                                */
     float kappa;                 /* grey absorption coefficient [1/m] (GREY)     */
@@ -114,6 +117,10 @@ typedef struct dnsmc_config {
     /* kernel shape (0 = automatic) */
     int   block_threads;         /* 128 or 256                                   */
     int   tile_a;                /* cells of a packet along j: 8, 16 or 32       */
+    /* multigrid */
+    int   mg_steps;              /* steps per grid before the next coarser one  */
+                                 /* (the reference's maxs, 5); the last grid    */
+                                 /* marches up to max_steps                     */
 } dnsmc_config;
 
 /* Raw spectral table for DNSMC_MODEL_TABLE (and the internal representation of
@@ -144,7 +151,9 @@ typedef struct dnsmc_solver dnsmc_solver;
 /* ---- configuration -------------------------------------------------------- */
 /* The reference's shipped code/param.h values (64^3, particle tables, black
  * x-walls at 500 K, Lx=Ly=Lz=1, nVar=3, photmax=20000), except grid_num = 1:
- * rays march on the fine grid only.                                          */
+ * rays march on the fine grid only (grid_num = 5 with mg_steps = 5 is the
+ * reference's shipped multigrid; it needs the reference tables or the grey
+ * model, no control variate, black walls and no particles).                 */
 void dnsmc_set_default_config(dnsmc_config *cfg);
 /* Overlay DNSMC_* environment variables (DNSMC_IMAX, DNSMC_JMAX, DNSMC_KMAX,
  * DNSMC_PROW, DNSMC_LX, DNSMC_LY, DNSMC_LZ, DNSMC_NVAR, DNSMC_PHOTMAX,
@@ -246,6 +255,10 @@ int  dnsmc_wait(dnsmc_solver *s, double timeout_s);
 int  dnsmc_get_results(dnsmc_solver *s, double *Q, double *sigma);
 /* Per band group: mean and variance of the mean, [field][group][cell].         */
 int  dnsmc_get_group_results(dnsmc_solver *s, double *Qg, double *varg);
+/* Spline-coarsened temperature of multigrid level 1..grid_num-1 of resident
+ * snapshot `field`: (imax>>level)*(jmax>>level)*(kmax>>level) values, dense,
+ * i fastest (the reference's interp3D, code/spline.cpp:35-116).             */
+int  dnsmc_get_coarse_field(dnsmc_solver *s, int field, int level, float *T);
 /* CUDA graph replay of the solve: when enabled, the kernel sequence of a
  * solve (table coordinates, control-variate preparation, the persistent
  * march, finalize and the result copy) is captured once into a CUDA graph

@@ -561,6 +561,14 @@ typedef struct {
     const float *part;        // [band][2]: absorption, scattering per unit volume fraction
     float fv_max, hg_g;
     float eps[2];
+    // multigrid: levels 1..mg_levels-1, 2x coarser per axis each
+    int mg_levels, mg_steps;
+    const float *mgT;         // coarse T, level l at mg_off[l]: [f][i][k][j]
+    const float *mgfw;        // coarse wall-normal faces, level l at mg_fwoff[l]
+    long long mg_off[6];
+    int mg_fwoff[6];
+    float mg_da[6], mg_db[6];
+    float Ly, Lz;
 } OrcPacketConfig;
 
 }  // extern "C"
@@ -1060,7 +1068,105 @@ struct Packet {
                 bool any = false;
                 for (int l = 0; l < 32; ++l) any = any || (tau[l] > 0);
                 if (!any) break;
-                if (stepn >= c.max_steps) break;
+                if (stepn >= (c.mg_levels > 1 ? c.mg_steps : c.max_steps)) break;
+            }
+            if (c.mg_levels > 1) {
+                // coarse grids: per-lane position-update march in lockstep
+                bool any = false;
+                for (int l = 0; l < 32; ++l) any = any || (tau[l] > 0);
+                if (any) {
+                    const R ua = t / dtA - (R)nA, ub = t / dtB - (R)nB;
+                    const R fa = std::fmin(std::fmax(dA > 0 ? (R)0.5 + ua : (R)0.5 - ua, (R)0), (R)1);
+                    const R fb = std::fmin(std::fmax(dB > 0 ? (R)0.5 + ub : (R)0.5 - ub, (R)0), (R)1);
+                    R xp[32], yp[32], zp[32];
+                    int ic[32], jc[32], kc[32];
+                    for (int l = 0; l < 32; ++l) {
+                        xp[l] = FMA<R>(sW, t, oW);
+                        yp[l] = ((R)ca[l] + fa) * (R)c.da;
+                        zp[l] = ((R)cb[l] + fb) * (R)c.db;
+                        ic[l] = cw; jc[l] = ca[l]; kc[l] = cb[l];
+                    }
+                    const R isx = (R)1 / sW, isy = (R)1 / sA, isz = (R)1 / sB;
+                    for (int lv = 1; lv < c.mg_levels; ++lv) {
+                        const int nwL = c.nw >> lv, naL = c.na >> lv, nbL = c.nb >> lv;
+                        const float *fwL = c.mgfw + c.mg_fwoff[lv];
+                        const R daL = (R)c.mg_da[lv], dbL = (R)c.mg_db[lv];
+                        const float *TL = c.mgT + c.mg_off[lv] + (long long)f * nwL * naL * nbL;
+                        const int cap = (lv == c.mg_levels - 1) ? c.max_steps : c.mg_steps;
+                        for (int l = 0; l < 32; ++l) { ic[l] >>= 1; jc[l] >>= 1; kc[l] >>= 1; }
+                        int counter = 0;
+                        for (;;) {
+                            bool go = false;
+                            for (int l = 0; l < 32; ++l) go = go || (tau[l] > 0 && counter < cap);
+                            if (!go) break;
+                            R dsr0 = 0;  // lane 0's segment this iteration (0 when it idles)
+                            for (int l = 0; l < 32; ++l) {
+                                if (!(tau[l] > 0 && counter < cap)) continue;
+                                *steps += 1;
+                                const R fx = (R)fwL[dW > 0 ? ic[l] + 1 : ic[l]];
+                                const R fy = (R)(float)(dA > 0 ? jc[l] + 1 : jc[l]) * daL;
+                                const R fz = (R)(float)(dB > 0 ? kc[l] + 1 : kc[l]) * dbL;
+                                const R dsx = sW != 0 ? (fx - xp[l]) * isx : INF;
+                                const R dsy = sA != 0 ? (fy - yp[l]) * isy : INF;
+                                const R dsz = sB != 0 ? (fz - zp[l]) * isz : INF;
+                                const R Tc = (R)TL[((long long)ic[l] * nbL + kc[l]) * naL + jc[l]];
+                                R kj, gj;
+                                if (c.mode == 0) {
+                                    const R t2 = Tc * Tc;
+                                    gj = (Ti4[l] - t2 * t2) * invI[l];
+                                    kj = (R)c.kappa;
+                                } else {
+                                    int tj;
+                                    R ftj;
+                                    p_gpos<R>(Tc, (R)c.T0, invdT, c.nT, &tj, &ftj);
+                                    kj = kfun(koff, tj, ftj, 0, 0);
+                                    gj = (Ii[l] - ibfun(nbnd, tj, ftj)) * invI[l];
+                                }
+                                R dmin = dsx;
+                                if (dmin > dsy) dmin = dsy;
+                                if (dmin > dsz) dmin = dsz;
+                                const R ds = std::fmax(dmin, (R)0);
+                                if (l == 0) dsr0 = ds;
+                                xp[l] = (dmin == dsx) ? fx : FMA<R>(ds, sW, xp[l]);
+                                yp[l] = (dmin == dsy) ? fy : FMA<R>(ds, sA, yp[l]);
+                                zp[l] = (dmin == dsz) ? fz : FMA<R>(ds, sB, zp[l]);
+                                const R alpha = -expm1n(-(kj * ds));
+                                const R tal = tau[l] * alpha;
+                                D[l] = FMA<R>(tal, gj, D[l]);
+                                tau[l] = tau[l] - tal;
+                                if (tau[l] < (R)c.toll) { D[l] = FMA<R>(tau[l], gj, D[l]); tau[l] = 0; }
+                                int axis;
+                                if (dsx < dsy) axis = (dsx < dsz) ? 0 : 2;
+                                else axis = (dsy < dsz) ? 1 : 2;
+                                if (axis == 0) {
+                                    ic[l] += dW;
+                                    if (ic[l] < 0 || ic[l] >= nwL) {
+                                        const int side = ic[l] < 0 ? 0 : 1;
+                                        const R Iw = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
+                                        if (tau[l] > 0) D[l] = FMA<R>(tau[l], (Ii[l] - Iw) * invI[l], D[l]);
+                                        tau[l] = 0;
+                                        ic[l] = ic[l] < 0 ? 0 : nwL - 1;
+                                    }
+                                } else if (axis == 1) {
+                                    jc[l] += dA;
+                                    if (jc[l] >= naL) { jc[l] = 0; yp[l] = 0; } else if (jc[l] < 0) { jc[l] = naL - 1; yp[l] = (R)c.Ly; }
+                                } else {
+                                    kc[l] += dB;
+                                    if (kc[l] >= nbL) { kc[l] = 0; zp[l] = 0; } else if (kc[l] < 0) { kc[l] = nbL - 1; zp[l] = (R)c.Lz; }
+                                }
+                            }
+                            if (rec && stepn < tmax) {  // lane 0, every iteration
+                                int32_t *q = rec + 6 * stepn;
+                                q[0] = ic[0]; q[1] = jc[0]; q[2] = kc[0]; q[3] = 16 + lv;
+                                const float dsf = (float)dsr0, tf = (float)tau[0];
+                                memcpy(&q[4], &dsf, 4);
+                                memcpy(&q[5], &tf, 4);
+                            }
+                            ++counter;
+                            ++stepn;
+                        }
+                    }
+                }
             }
             if (nrec) *nrec = stepn;
             for (int l = 0; l < 32; ++l) {

@@ -64,6 +64,9 @@ class PacketConfig(ctypes.Structure):
         ("cv", ctypes.c_int), ("sur_k", _f), ("sur_I", _f), ("beta", _f), ("moments", _d),
         ("gen", ctypes.c_int), ("fieldV", _f), ("part", _f), ("fv_max", ctypes.c_float), ("hg_g", ctypes.c_float),
         ("eps", ctypes.c_float * 2),
+        ("mg_levels", ctypes.c_int), ("mg_steps", ctypes.c_int), ("mgT", _f), ("mgfw", _f),
+        ("mg_off", ctypes.c_longlong * 6), ("mg_fwoff", ctypes.c_int * 6), ("mg_da", ctypes.c_float * 6),
+        ("mg_db", ctypes.c_float * 6), ("Ly", ctypes.c_float), ("Lz", ctypes.c_float),
     ]
 
 
@@ -186,6 +189,32 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
         keep["X"] = X
         c.fieldX = _fp(X)
     c.kappa, c.T_west, c.T_east = cfg.kappa, cfg.T_west, cfg.T_east
+    # multigrid: the oracle's own spline coarsening (interp3D restated) and
+    # the reference's coarse faces, in the march's layout
+    c.mg_levels, c.mg_steps = cfg.grid_num, cfg.mg_steps
+    if cfg.grid_num > 1:
+        ni_, nj_, nk_ = cfg.imax, cfg.jmax, cfg.kmax
+        blocks, faces, off, foff = [], [], 0, 0
+        for lv in range(1, cfg.grid_num):
+            c.mg_off[lv] = off
+            for f in range(T.shape[0]):
+                Tf = np.zeros((nk_ + 2, nj_ + 2, ni_ + 2), np.float32)
+                Tf[1:-1, 1:-1, 1:-1] = T[f]
+                co = coarsen(Tf.ravel(), ni_, nj_, nk_, cfg.Lx, cfg.Ly, cfg.Lz, cfg.stretched_x, cfg.grid_num,
+                             lv)[1:-1, 1:-1, 1:-1]
+                blocks.append(np.ascontiguousarray(co.transpose(2, 0, 1)).ravel())
+                off += co.size
+            fw = ref_faces(ni_ >> lv, cfg.Lx, cfg.stretched_x, im0=ni_)
+            c.mg_fwoff[lv] = foff
+            faces.append(fw)
+            foff += fw.size
+            c.mg_da[lv] = np.float32(cfg.Ly) / np.float32(nj_ >> lv)
+            c.mg_db[lv] = np.float32(cfg.Lz) / np.float32(nk_ >> lv)
+        MT = np.concatenate(blocks).astype(np.float32)
+        MF = np.concatenate(faces).astype(np.float32)
+        keep["mgT"], keep["mgfw"] = MT, MF
+        c.mgT, c.mgfw = _fp(MT), _fp(MF)
+        c.Ly, c.Lz = cfg.Ly, cfg.Lz
     # general medium: particles (the solver's table, the caller's field) and grey walls
     part = getattr(solver, "_part", None)
     c.gen = 1 if (part is not None or cfg.eps_west < 1 or cfg.eps_east < 1) else 0

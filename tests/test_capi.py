@@ -43,7 +43,7 @@ def test_default_config_is_reference_param_h():
 
 
 @pytest.mark.parametrize("field,value", [("imax", 0), ("p_row", 3), ("toll", 0.0), ("model", 9), ("eps_west", 0.0), ("eps_east", 1.5),
-                                         ("grid_num", 5), ("block_threads", 100), ("tile_a", 12), ("nvar", 0)])
+                                         ("grid_num", 7), ("block_threads", 100), ("tile_a", 12), ("nvar", 0)])
 def test_bad_config_is_an_error_code(field, value):
     c = D.default_config()
     setattr(c, field, value)
@@ -254,3 +254,12 @@ def test_rqmc_requires_replicates_and_divisible_rays():
         s.set_rays(10)
     assert e.value.code == _lib.ERR_ARG
     s.close()
+
+
+def test_multigrid_config_checks():
+    """grid_num > 1 needs grid sizes divisible by 2^(grid_num - 1) and
+    mg_steps >= 1; the reference's shipped 5 levels on 64^3 are valid."""
+    D.Solver(D.default_config(grid_num=5)).close()
+    for kw in (dict(grid_num=3, mg_steps=0), dict(grid_num=4, imax=36), dict(grid_num=2, kmax=33)):
+        with pytest.raises(D.DnsmcError):
+            D.Solver(D.default_config(**kw))
