@@ -48,11 +48,11 @@ def feature_config(table, groups: int = GROUPS, **kw):
 
 
 def add_snapshots(net: CvNet, table, n: int, seeds, rays: int, j_slab: int | None = None, log=None,
-                  groups: int = GROUPS) -> float:
+                  groups: int = GROUPS, nvar: int = REPLICATES) -> float:
     """Solve every snapshot (moments on) on cells [0,n) x [j0, j0+j_slab) x
     [0,n) and append them to the network's data; returns the solve seconds."""
     T_wall = synth.ck_channel(8, 0)["T_wall"]
-    s = ck_solver(table, n, T_wall, seed=7919, moments=True, groups=groups)
+    s = ck_solver(table, n, T_wall, seed=7919, moments=True, groups=groups, nvar=nvar)
     t_solve = 0.0
     try:
         for q, seed in enumerate(seeds):
@@ -74,7 +74,7 @@ def add_snapshots(net: CvNet, table, n: int, seeds, rays: int, j_slab: int | Non
 
 
 def train(table, n: int, seeds, rays: int = 64, epochs: int = 3, j_slab: int | None = None, net: CvNet | None = None,
-          log=None, chunk: int = 0, groups: int = GROUPS, **cfg) -> tuple[CvNet, dict]:
+          log=None, chunk: int = 0, groups: int = GROUPS, nvar: int = REPLICATES, **cfg) -> tuple[CvNet, dict]:
     """Train on the snapshots `seeds`; with chunk > 0 the data are streamed:
     `chunk` snapshots are solved, trained on for `epochs` passes and dropped
     before the next chunk (device memory stays bounded)."""
@@ -88,7 +88,7 @@ def train(table, n: int, seeds, rays: int = 64, epochs: int = 3, j_slab: int | N
         net.clear_training_data()
         t0 = time.time()
         t_solve += add_snapshots(net, table, n, seeds[c0:c0 + step], rays, j_slab, log if chunk == 0 else None,
-                                 groups=groups)
+                                 groups=groups, nvar=nvar)
         t1 = time.time()
         rows += net.training_rows()
         losses = net.train(epochs)
@@ -97,7 +97,8 @@ def train(table, n: int, seeds, rays: int = 64, epochs: int = 3, j_slab: int | N
         t_train += t2 - t1
         if log and chunk:
             log(f"snapshots {c0 + 1}-{min(len(seeds), c0 + step)}: loss {losses}")
-    info = dict(fields=len(seeds), rows=rows, rays=rays, epochs=epochs, n=n, chunk=step, groups=groups, data_s=t_data,
+    info = dict(fields=len(seeds), rows=rows, rays=rays, epochs=epochs, n=n, chunk=step, groups=groups, nvar=nvar,
+                data_s=t_data,
                 solve_s=t_solve, train_s=t_train, loss=losses)
     if log:
         log(f"trained: {info}")
@@ -114,11 +115,12 @@ def main(argv=None) -> int:
     ap.add_argument("--slab", type=int, default=32, help="j cells per snapshot (0: all)")
     ap.add_argument("--chunk", type=int, default=0, help="snapshots per streamed training chunk (0: all at once)")
     ap.add_argument("--groups", type=int, default=GROUPS, help="band groups of the solves (<= 16)")
+    ap.add_argument("--nvar", type=int, default=REPLICATES, help="RQMC replicates of the training solves")
     ap.add_argument("--out", required=True)
     a = ap.parse_args(argv)
     table = synth.ck_table(64, 16, 50, 8, seed=0)
     seeds = range(a.first_seed, a.first_seed + a.fields)
-    net, info = train(table, a.n, seeds, a.rays, a.epochs, a.slab or None, chunk=a.chunk, groups=a.groups,
+    net, info = train(table, a.n, seeds, a.rays, a.epochs, a.slab or None, chunk=a.chunk, groups=a.groups, nvar=a.nvar,
                       log=lambda m: print(m, file=sys.stderr, flush=True))
     net.save(a.out)
     print(info)
