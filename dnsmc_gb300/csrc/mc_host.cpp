@@ -362,7 +362,8 @@ struct dnsmc_solver {
     // tables
     HostTable tab;
     DevBuf<float> d_k, d_ib, d_ibw;
-    DevBuf<float2> d_kpair, d_ibpair;
+    DevBuf<float2> d_slab;   // per spectral sample: k pairs then the band's Ib pairs
+    int slab_len = 0, slab_klen = 0;
     DevBuf<int2> d_posT;   // per cell (ti, ft) for T-only tables
     DevBuf<int4> d_posTX;  // per cell (ti*(nX-1)+xi, ft, fx, ti)
     bool tables_dirty = true;
@@ -875,33 +876,33 @@ int upload_tables(dnsmc_solver *s) {
     TRY(s->d_ib.ensure(t.Ib.size()));
     CUDA_TRY(cudaMemcpyAsync(s->d_k.p, t.k.data(), t.k.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(cudaMemcpyAsync(s->d_ib.p, t.Ib.data(), t.Ib.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-    // paired tables for two-value loads in the march: (value, difference to the next)
+    // the march's per-sample slabs of paired values (value, difference to the
+    // next): k over [t][x] (or [t]), then Ib over [t] of the sample's band
     const int nS = t.nbands * t.nq;
-    std::vector<float2> kp, ip((size_t)t.nbands * (t.nT - 1));
-    if (t.nX > 1) {
-        kp.resize((size_t)nS * t.nT * (t.nX - 1));
-        for (int sid = 0; sid < nS; ++sid)
+    const int klen = t.nX > 1 ? t.nT * (t.nX - 1) : t.nT - 1;
+    const int len = (klen + (t.nT - 1) + 1) & ~1;
+    std::vector<float2> sl((size_t)nS * len, make_float2(0.f, 0.f));
+    for (int sid = 0; sid < nS; ++sid) {
+        float2 *o = sl.data() + (size_t)sid * len;
+        if (t.nX > 1) {
             for (int ti = 0; ti < t.nT; ++ti)
                 for (int xi = 0; xi < t.nX - 1; ++xi) {
                     const float *r = t.k.data() + ((size_t)sid * t.nT + ti) * t.nX + xi;
-                    kp[((size_t)sid * t.nT + ti) * (t.nX - 1) + xi] = make_float2(r[0], r[1] - r[0]);
+                    o[ti * (t.nX - 1) + xi] = make_float2(r[0], r[1] - r[0]);
                 }
-    } else {
-        kp.resize((size_t)nS * (t.nT - 1));
-        for (int sid = 0; sid < nS; ++sid)
+        } else {
             for (int ti = 0; ti < t.nT - 1; ++ti) {
                 const float *r = t.k.data() + (size_t)sid * t.nT + ti;
-                kp[(size_t)sid * (t.nT - 1) + ti] = make_float2(r[0], r[1] - r[0]);
+                o[ti] = make_float2(r[0], r[1] - r[0]);
             }
+        }
+        const float *ib = t.Ib.data() + (size_t)(sid / t.nq) * t.nT;
+        for (int ti = 0; ti < t.nT - 1; ++ti) o[klen + ti] = make_float2(ib[ti], ib[ti + 1] - ib[ti]);
     }
-    for (int b = 0; b < t.nbands; ++b)
-        for (int ti = 0; ti < t.nT - 1; ++ti)
-            ip[(size_t)b * (t.nT - 1) + ti] = make_float2(t.Ib[(size_t)b * t.nT + ti],
-                                                          t.Ib[(size_t)b * t.nT + ti + 1] - t.Ib[(size_t)b * t.nT + ti]);
-    TRY(s->d_kpair.ensure(kp.size()));
-    TRY(s->d_ibpair.ensure(ip.size()));
-    CUDA_TRY(cudaMemcpyAsync(s->d_kpair.p, kp.data(), kp.size() * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
-    CUDA_TRY(cudaMemcpyAsync(s->d_ibpair.p, ip.data(), ip.size() * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+    TRY(s->d_slab.ensure(sl.size()));
+    CUDA_TRY(cudaMemcpyAsync(s->d_slab.p, sl.data(), sl.size() * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+    s->slab_len = len;
+    s->slab_klen = klen;
     CUDA_TRY(cudaStreamSynchronize(s->stream));
     s->tables_dirty = false;
     return DNSMC_OK;
@@ -974,7 +975,8 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         return fail(DNSMC_ERR_STATE, "fields carry x_H2O but the spectral model has no x axis: set fields without x");
     P.nbands = t.nbands; P.nT = t.nT; P.nX = t.nX;
     P.T0 = t.T0; P.invdT = 1.0f / t.dT; P.X0 = t.X0; P.invdX = 1.0f / t.dX;
-    P.kpair = s->d_kpair.p; P.ibpair = s->d_ibpair.p; P.ibw = s->d_ibw.p;
+    if (mode != MODE_GREY) { P.slab = s->d_slab.p; P.slab_len = s->slab_len; P.slab_klen = s->slab_klen; }
+    P.ibw = s->d_ibw.p;
     P.entries = s->d_entries.p; P.group_start = s->d_group_start.p;
     P.n_groups = s->n_groups_used;
     P.n_tbins = s->n_tbins_used;
@@ -1043,7 +1045,17 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.queue = s->d_misc.p;
     P.status = s->d_misc.p + 1;
     P.counters = s->d_counters.p;
-    const int threads = c.block_threads ? c.block_threads : 256;
+    int threads = c.block_threads ? c.block_threads : 256;
+    {
+        // every warp holds its ray's table slab in shared memory
+        int smax = 0;
+        if (cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device) != cudaSuccess)
+            smax = 48 * 1024;
+        if (march_smem(P, threads) > (size_t)smax) threads = 128;
+        if (march_smem(P, threads) > (size_t)smax)
+            return fail(DNSMC_ERR_TABLE, "a spectral sample's table slab (%d bytes) exceeds the shared memory of the march",
+                        P.slab_len * 8);
+    }
     const bool cv = c.control_variate != 0;
     const int S = (mode == MODE_GREY) ? 1 : t.nbands * t.nq;
     if (cv) {
@@ -1126,7 +1138,8 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         P.item_order = s->d_order.p;
     }
     const int sms = device_sm_count();
-    const int occ = mg ? march_mg_occupancy(mode, threads) : march_occupancy_ex(mode, threads, cv, mom, gen);
+    const size_t smem = march_smem(P, threads);
+    const int occ = mg ? march_mg_occupancy(mode, threads, smem) : march_occupancy_ex(mode, threads, cv, mom, gen, smem);
     const int blocks = std::max(1, sms * occ);
 
     FinalizeParams F;
@@ -1532,7 +1545,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     if (s->stream) cudaStreamSynchronize(s->stream);
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     s->d_fw.release(); s->d_k.release(); s->d_ib.release(); s->d_ibw.release();
-    s->d_kpair.release(); s->d_ibpair.release(); s->d_posT.release(); s->d_posTX.release();
+    s->d_slab.release(); s->d_posT.release(); s->d_posTX.release();
     s->d_cv_grp.release(); s->d_cv_sid.release(); s->d_cv_C.release(); s->d_layer.release();
     s->d_sur.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();

@@ -47,8 +47,13 @@ struct MarchParams {
     // spectral tables
     int nbands, nT, nX;
     float T0, invdT, X0, invdX;
-    const float2 *kpair;      // [sample][t][x] (k[x], k[x+1]) or [sample][t] (k[t], k[t+1])
-    const float2 *ibpair;     // [band][t] (Ib[t], Ib[t+1])
+    // per spectral sample (band*nq + g) one slab of slab_len float2: the k
+    // pairs [t][x] (k[x], k[x+1] - k[x]) or [t] (k[t], k[t+1] - k[t]) in the
+    // first slab_klen, then the band's Ib pairs [t] (Ib[t], Ib[t+1] - Ib[t]);
+    // slab_len is even (16-byte rows).  Each warp copies its ray's slab into
+    // shared memory: the march launches with warps * slab_len * 8 bytes.
+    const float2 *slab;
+    int slab_len, slab_klen;
     const float *ibw;         // [2][band]
     const SpecEntry *entries;
     const int *group_start;   // n_tbins * n_groups + 1, temperature-bin major
@@ -191,12 +196,16 @@ int launch_item_order(const int *rays, int gstride, int n_packets, int n_groups,
 // launchers (mc_kernels.cu); all stream-ordered
 int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                     bool mom, bool gen);
-int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen);
+int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen, size_t smem);
 int launch_march_mg(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace);
-int march_mg_occupancy(int mode, int threads);
+int march_mg_occupancy(int mode, int threads, size_t smem);
+// dynamic shared memory of a march launch: each warp's table slab
+inline size_t march_smem(const MarchParams &p, int threads) {
+    return (size_t)((threads + 31) / 32) * (size_t)p.slab_len * 8u;
+}
 int launch_march_gen(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                      bool mom);                                      // mc_march_gen.cu
-int march_gen_occupancy(int mode, int threads, bool cv, bool mom);    // mc_march_gen.cu
+int march_gen_occupancy(int mode, int threads, bool cv, bool mom, size_t smem);  // mc_march_gen.cu
 int upload_sobol_dirs_gen(const uint32_t dirs[4][32]);               // mc_march_gen.cu
 int launch_march(int mode, const MarchParams &p, int blocks, int threads,
                  void *stream, bool trace);
@@ -215,9 +224,6 @@ int launch_field_stats(const float *fT, const float2 *fTX, long long n,
                        double *partials, float *out, void *stream);
 int field_stats_partials();   // doubles needed in `partials`
 int march_occupancy(int mode, int threads);  // resident blocks per SM
-int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace,
-                    bool moments);
-int march_cv_occupancy(int mode, int threads, bool moments);
 
 // Control-variate preparation (all stream-ordered).
 struct CvParams {

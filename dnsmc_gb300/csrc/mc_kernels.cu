@@ -201,9 +201,9 @@ int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, voi
     return launch_march_variant<false>(mode, p, blocks, threads, (cudaStream_t)stream, trace, cv, mom);
 }
 
-int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen) {
-    if (gen) return march_gen_occupancy(mode, threads, cv, mom);
-    return march_variant_occupancy<false>(mode, threads, cv, mom);
+int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen, size_t smem) {
+    if (gen) return march_gen_occupancy(mode, threads, cv, mom, smem);
+    return march_variant_occupancy<false>(mode, threads, cv, mom, smem);
 }
 
 // Multigrid march (reference tables or grey model; no control variate, no
@@ -211,42 +211,31 @@ int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen) {
 int launch_march_mg(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace) {
     cudaStream_t st = (cudaStream_t)stream;
     if (trace) { blocks = 1; threads = 32; }
+    const size_t smem = march_smem(p, threads);
     if (mode == MODE_GREY) {
-        if (trace) march_kernel<MODE_GREY, true, false, false, false, true><<<blocks, threads, 0, st>>>(p);
-        else march_kernel<MODE_GREY, false, false, false, false, true><<<blocks, threads, 0, st>>>(p);
-    } else if (mode == MODE_T) {
-        if (trace) march_kernel<MODE_T, true, false, false, false, true><<<blocks, threads, 0, st>>>(p);
-        else march_kernel<MODE_T, false, false, false, false, true><<<blocks, threads, 0, st>>>(p);
-    } else {
-        return (int)cudaErrorInvalidValue;
+        if (trace) return march_launch_one(march_kernel<MODE_GREY, true, false, false, false, true>, blocks, threads,
+                                           smem, st, p);
+        return march_launch_one(march_kernel<MODE_GREY, false, false, false, false, true>, blocks, threads, smem, st,
+                                p);
     }
-    return (int)cudaGetLastError();
+    if (mode == MODE_T) {
+        if (trace) return march_launch_one(march_kernel<MODE_T, true, false, false, false, true>, blocks, threads,
+                                           smem, st, p);
+        return march_launch_one(march_kernel<MODE_T, false, false, false, false, true>, blocks, threads, smem, st, p);
+    }
+    return (int)cudaErrorInvalidValue;
 }
 
-int march_mg_occupancy(int mode, int threads) {
+int march_mg_occupancy(int mode, int threads, size_t smem) {
     int nb = 0;
-    cudaError_t e = cudaErrorInvalidValue;
     if (mode == MODE_GREY)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_GREY, false, false, false, false, true>,
-                                                          threads, 0);
-    if (mode == MODE_T)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<MODE_T, false, false, false, false, true>,
-                                                          threads, 0);
-    if (e != cudaSuccess) return 1;
+        nb = march_occupancy_one(march_kernel<MODE_GREY, false, false, false, false, true>, threads, smem);
+    if (mode == MODE_T) nb = march_occupancy_one(march_kernel<MODE_T, false, false, false, false, true>, threads, smem);
     return nb > 0 ? nb : 1;
 }
 
 int launch_march(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace) {
     return launch_march_ex(mode, p, blocks, threads, stream, trace, false, false, false);
-}
-
-int launch_march_cv(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace,
-                    bool moments) {
-    return launch_march_ex(mode, p, blocks, threads, stream, trace, true, moments, false);
-}
-
-int march_cv_occupancy(int mode, int threads, bool moments) {
-    return march_occupancy_ex(mode, threads, true, moments, false);
 }
 
 // ---------------------------------------------------------------------------
@@ -615,7 +604,7 @@ int launch_cv_mean(const CvParams &c, void *stream) {
     return (int)cudaGetLastError();
 }
 
-int march_occupancy(int mode, int threads) { return march_occupancy_ex(mode, threads, false, false, false); }
+int march_occupancy(int mode, int threads) { return march_occupancy_ex(mode, threads, false, false, false, 0); }
 
 int launch_field_pos(const float *fT, const float2 *fTX, int2 *outP, int4 *outPX, long long n, float T0,
                      float invdT, int nT, float X0, float invdX, int nX, void *stream) {

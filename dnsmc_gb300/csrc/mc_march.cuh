@@ -121,27 +121,27 @@ __device__ __forceinline__ void pos_split(float p, int n, int *i, float *f) {
     *f = p - (float)ii;
 }
 
-// Paired tables: kpair holds (k[t][x], k[t][x+1] - k[t][x]) (x-tables) or
-// (k[t], k[t+1] - k[t]) and ibpair (Ib[t], Ib[t+1] - Ib[t]), so a bilinear
-// lookup is two 8-byte loads and three fmaf (the differences are the same
-// FP32 subtractions the interpolation would do).  kidx = ti*(nX-1) + xi.
+// Paired tables: the k part of a sample's slab holds (k[t][x], k[t][x+1] -
+// k[t][x]) (x-tables) or (k[t], k[t+1] - k[t]), its Ib part (Ib[t], Ib[t+1] -
+// Ib[t]) of the sample's band, so a bilinear lookup is two 8-byte loads and
+// three fmaf (the differences are the same FP32 subtractions the
+// interpolation would do).  kidx = ti*(nX-1) + xi; row = nX - 1.  The march
+// reads them from the warp's copy of the slab in shared memory.
 template <int MODE>
-__device__ __forceinline__ float lookup_k(const MarchParams &P, int sid, int kidx, float ft, float fx) {
+__device__ __forceinline__ float lookup_k(const float2 *ks, int row, int kidx, float ft, float fx) {
     if (MODE == MODE_TX) {
-        const int row = P.nX - 1;
-        const float2 *r = P.kpair + sid * (P.nT * row) + kidx;
-        const float2 a = __ldg(r), b = __ldg(r + row);
+        const float2 a = ks[kidx], b = ks[kidx + row];
         const float k0 = fmaf(fx, a.y, a.x);
         const float k1 = fmaf(fx, b.y, b.x);
         return fmaf(ft, k1 - k0, k0);
     } else {
-        const float2 a = __ldg(P.kpair + sid * (P.nT - 1) + kidx);
+        const float2 a = ks[kidx];
         return fmaf(ft, a.y, a.x);
     }
 }
 
-__device__ __forceinline__ float lookup_ib(const MarchParams &P, int nb, int ti, float ft) {
-    const float2 a = __ldg(P.ibpair + nb * (P.nT - 1) + ti);
+__device__ __forceinline__ float lookup_ib(const float2 *ibs, int ti, float ft) {
+    const float2 a = ibs[ti];
     return fmaf(ft, a.y, a.x);
 }
 
@@ -297,6 +297,19 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
     const int plane = P.na * P.nb;
     unsigned long long my_rays = 0, my_steps = 0;
     unsigned int flags = 0;
+    // this warp's copy of the current ray's table slab (tabulated models)
+    extern __shared__ float4 s_slab[];
+    float2 *const slk = reinterpret_cast<float2 *>(s_slab) + (threadIdx.x >> 5) * P.slab_len;
+    const float2 *const sli = slk + P.slab_klen;
+    const int krow = P.nX - 1;
+    // Per-lane state that is not needed while a ray marches lives in shared
+    // memory, so the march keeps its own working set in registers: the
+    // item's FP64 sums (ray sum, sum of squares or of squared replicate
+    // means, current replicate sum), its moment sums, the replicate's shift.
+    __shared__ double s_acc[3][256];
+    __shared__ double s_mo[MOM ? 9 : 1][MOM ? 256 : 1];
+    __shared__ uint4 s_shift[256];
+    const int tid = threadIdx.x;
 
     for (;;) {
         long long item;
@@ -362,18 +375,15 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
         }
         const uint32_t ctr2 = (uint32_t)G | ((uint32_t)(f + P.field_base) << 16);
         const long long tc = ((long long)(w0 - P.ew0) * nkR + (bcl - P.eb0)) * njR + (acl - P.ea0);
-        float2 beta = make_float2(1.0f, -1.0f);
-        if (CV && P.beta) beta = P.beta[fg * P.region_cells + tc];
-        double mo[9];
+        const long long cell_out = fg * P.region_cells + tc;  // tally index of this lane's cell
         if (MOM)
 #pragma unroll
-            for (int q = 0; q < 9; ++q) mo[q] = 0.0;
+            for (int q = 0; q < 9; ++q) s_mo[q][tid] = 0.0;
         const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
 
-        double S = 0.0, S2 = 0.0, Sb = 0.0;
+        s_acc[0][tid] = 0.0; s_acc[1][tid] = 0.0; s_acc[2][tid] = 0.0;
         unsigned long long isteps = 0;
         unsigned int lsteps = 0;  // this lane's active steps in the item
-        uint4 shift = make_uint4(0u, 0u, 0u, 0u);
         int bcur = -1;
         const int rbeg = TRACE ? P.trace_r : 0;
         const int rend = TRACE ? P.trace_r + 1 : ((K > 0) ? N : 0);
@@ -384,9 +394,10 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 const int b = r / M;
                 m = r - b * M;
                 if (b != bcur) {
-                    shift = philox4x32_10(make_uint4((uint32_t)b, (uint32_t)p, ctr2, 0x50B01u), P.key0, P.key1);
+                    s_shift[tid] = philox4x32_10(make_uint4((uint32_t)b, (uint32_t)p, ctr2, 0x50B01u), P.key0, P.key1);
                     bcur = b;
                 }
+                const uint4 shift = s_shift[tid];
                 const uint4 sb = sobol4((uint32_t)m);
                 x = make_uint4(sb.x ^ shift.x, sb.y ^ shift.y, sb.z ^ shift.z, sb.w ^ shift.w);
             } else {
@@ -401,9 +412,10 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             float cph, sph;
             mc_sincos_turn(x.x >> 8, &cph, &sph);
             float sW = mu, sA = st * cph, sB = st * sph;
+            const float sW0 = sW;  // initial direction, for the control variate's straight flight
 
-            // spectral sample and ray weight
-            float w, wk, Ii, invI;
+            // spectral sample and ray weight (the ray's weight is wk * Ii)
+            float wk, Ii, invI;
             int nbnd = 0, sid = 0;
             float pab = 0.0f, psc = 0.0f;  // particle absorption / scattering per unit volume fraction
             if (MODE == MODE_GREY) {
@@ -415,29 +427,29 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 } else {
                     wk = P.Wgrey;
                 }
-                w = wk * Ti4;
             } else {
                 const int j = (int)__umulhi(x.z, (uint32_t)K);
                 SpecEntry e = P.entries[gs + j];
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
                 sid = e.koff;
-                float ki = lookup_k<MODE>(P, sid, ki_i, ft_i, fx_i);
+                // the sample's slab (k, then Ib of its band) into this warp's
+                // shared copy; the previous ray's lookups are done first
+                __syncwarp();
+                {
+                    const float4 *src = reinterpret_cast<const float4 *>(P.slab + (long long)sid * P.slab_len);
+                    float4 *dst = reinterpret_cast<float4 *>(slk);
+                    for (int q = lane; q < (P.slab_len >> 1); q += 32) dst[q] = __ldg(src + q);
+                }
+                __syncwarp();
+                float ki = lookup_k<MODE>(slk, krow, ki_i, ft_i, fx_i);
                 if constexpr (GEN) {
                     if (P.part) { const float2 pp = __ldg(P.part + nbnd); pab = pp.x; psc = pp.y; }
                     ki = fmaf(fvown, pab, ki);
                 }
-                Ii = lookup_ib(P, nbnd, ti_i, ft_i);
+                Ii = lookup_ib(sli, ti_i, ft_i);
                 invI = Ii > 0.f ? 1.0f / Ii : 0.f;
                 wk = e.W * ki;
-                w = wk * Ii;
-            }
-            // control variate: the straight flight through the layer-mean medium
-            float Jbar = 0.0f, tex0 = 0.0f, I0 = 0.0f;
-            if (CV) {
-                const float2 *surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
-                I0 = __ldg(surp + w0).y;
-                surrogate_walk<MODE>(P, surp, w0, oW, sW, nbnd, &Jbar, &tex0);
             }
 
             // warp-uniform DDA from (pw0, fa0, fb0): wall-normal coordinate and
@@ -521,8 +533,8 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                         int kx, tj;
                         float ftj, fxj;
                         cell_coords<MODE>(vcur, &kx, &tj, &ftj, &fxj);
-                        kj = lookup_k<MODE>(P, sid, kx, ftj, fxj);
-                        const float Ibj = lookup_ib(P, nbnd, tj, ftj);
+                        kj = lookup_k<MODE>(slk, krow, kx, ftj, fxj);
+                        const float Ibj = lookup_ib(sli, tj, ftj);
                         gj = (Ii - Ibj) * invI;
                     }
                     if constexpr (GEN) kj = fmaf(fvcur, pab, kj);
@@ -673,8 +685,8 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                                     int tj;
                                     float ftj;
                                     pos_split(pt, P.nT, &tj, &ftj);
-                                    kj = lookup_k<MODE_T>(P, sid, tj, ftj, 0.0f);
-                                    gj = (Ii - lookup_ib(P, nbnd, tj, ftj)) * invI;
+                                    kj = lookup_k<MODE_T>(slk, 0, tj, ftj, 0.0f);
+                                    gj = (Ii - lookup_ib(sli, tj, ftj)) * invI;
                                 }
                                 float dmin = dsx;
                                 if (dmin > dsy) dmin = dsy;
@@ -725,17 +737,25 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             }
             if (TRACE && lane == 0) *P.trace_n = steps;
             isteps += (unsigned long long)steps;
-            float X = w * D;
+            float X = (wk * Ii) * D;
             if (CV) {
+                // control variate: the ray's straight flight through the
+                // layer-mean medium (it does not depend on the march above)
+                float Jbar = 0.0f, tex0 = 0.0f;
+                const float2 *surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
+                const float I0 = __ldg(surp + w0).y;
+                surrogate_walk<MODE>(P, surp, w0, oW, sW0, nbnd, &Jbar, &tex0);
                 // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
                 const float Ya = wk * (Ii - Jbar);
                 const float Yb = wk * ((1.0f - tex0) * (Ii - I0));
                 if (MOM && active) {
                     const double xd = X, ya = Ya, yb = Yb;
-                    mo[0] += xd; mo[1] += ya; mo[2] += yb;
-                    mo[3] = fma(xd, xd, mo[3]); mo[4] = fma(ya, ya, mo[4]); mo[5] = fma(yb, yb, mo[5]);
-                    mo[6] = fma(xd, ya, mo[6]); mo[7] = fma(xd, yb, mo[7]); mo[8] = fma(ya, yb, mo[8]);
+                    s_mo[0][tid] += xd; s_mo[1][tid] += ya; s_mo[2][tid] += yb;
+                    s_mo[3][tid] = fma(xd, xd, s_mo[3][tid]); s_mo[4][tid] = fma(ya, ya, s_mo[4][tid]);
+                    s_mo[5][tid] = fma(yb, yb, s_mo[5][tid]); s_mo[6][tid] = fma(xd, ya, s_mo[6][tid]);
+                    s_mo[7][tid] = fma(xd, yb, s_mo[7][tid]); s_mo[8][tid] = fma(ya, yb, s_mo[8][tid]);
                 }
+                const float2 beta = P.beta ? P.beta[cell_out] : make_float2(1.0f, -1.0f);
                 X = X - beta.x * Ya;  // tallied: X - beta_a Y_a - beta_b Y_b; the
                 X = X - beta.y * Yb;  // means beta . E[Y] are added back at finalize
             }
@@ -743,27 +763,29 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 ++my_rays;
                 if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
                 const double Xd = (double)X;
-                S += Xd;
+                s_acc[0][tid] += Xd;
                 if (P.sampler) {
-                    Sb += Xd;
+                    const double Sb = s_acc[2][tid] + Xd;
                     if (m == M - 1) {  // end of a replicate: accumulate its mean squared
                         const double mb = Sb / M;
-                        S2 = fma(mb, mb, S2);
-                        Sb = 0.0;
+                        s_acc[1][tid] = fma(mb, mb, s_acc[1][tid]);
+                        s_acc[2][tid] = 0.0;
+                    } else {
+                        s_acc[2][tid] = Sb;
                     }
                 } else {
-                    S2 = fma(Xd, Xd, S2);
+                    s_acc[1][tid] = fma(Xd, Xd, s_acc[1][tid]);
                 }
             }
         }
         my_steps += lsteps;
         if (TRACE) return;
         if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
-        if (active) P.tally[fg * P.region_cells + tc] = make_double2(S, S2);
+        if (active) P.tally[cell_out] = make_double2(s_acc[0][tid], s_acc[1][tid]);
         if (MOM && active) {
-            double *out = P.moments + (fg * P.region_cells + tc) * 9;
+            double *out = P.moments + cell_out * 9;
 #pragma unroll
-            for (int q = 0; q < 9; ++q) out[q] = mo[q];
+            for (int q = 0; q < 9; ++q) out[q] = s_mo[q][tid];
         }
     }
     // per-warp counters and status
@@ -779,13 +801,36 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
     }
 }
 
+// One launch of a march kernel with `smem` bytes of dynamic shared memory
+// (raising the kernel's limit above the default 48 KB when needed), and its
+// resident blocks per SM.
+inline int march_launch_one(void (*k)(const MarchParams), int blocks, int threads, size_t smem, cudaStream_t st,
+                            const MarchParams &p) {
+    if (smem > 48u * 1024u) {
+        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
+    k<<<blocks, threads, smem, st>>>(p);
+    return (int)cudaGetLastError();
+}
+
+inline int march_occupancy_one(void (*k)(const MarchParams), int threads, size_t smem) {
+    if (smem > 48u * 1024u &&
+        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return 0;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, threads, smem) != cudaSuccess) return 0;
+    return nb;
+}
+
 // Launch one march variant: the dispatch over (mode, trace, control variate,
 // moments) of one value of GEN; march_occupancy_gen the matching occupancy.
 template <bool GEN>
 int launch_march_variant(int mode, const MarchParams &p, int blocks, int threads, cudaStream_t st, bool trace, bool cv,
                          bool mom) {
     if (trace) { blocks = 1; threads = 32; mom = false; }
-#define DNSMC_L(M, T, C, O) march_kernel<M, T, C, O, GEN><<<blocks, threads, 0, st>>>(p)
+    const size_t smem = march_smem(p, threads);
+#define DNSMC_L(M, T, C, O) return march_launch_one(march_kernel<M, T, C, O, GEN>, blocks, threads, smem, st, p)
 #define DNSMC_MODE(M)                                       \
     if (trace) { if (cv) DNSMC_L(M, true, true, false); else DNSMC_L(M, true, false, false); } \
     else if (cv) { if (mom) DNSMC_L(M, false, true, true); else DNSMC_L(M, false, true, false); } \
@@ -794,26 +839,24 @@ int launch_march_variant(int mode, const MarchParams &p, int blocks, int threads
         case MODE_GREY: DNSMC_MODE(MODE_GREY) break;
         case MODE_T: DNSMC_MODE(MODE_T) break;
         case MODE_TX: DNSMC_MODE(MODE_TX) break;
-        default: return (int)cudaErrorInvalidValue;
+        default: break;
     }
 #undef DNSMC_MODE
 #undef DNSMC_L
-    return (int)cudaGetLastError();
+    return (int)cudaErrorInvalidValue;
 }
 
 template <bool GEN>
-int march_variant_occupancy(int mode, int threads, bool cv, bool mom) {
+int march_variant_occupancy(int mode, int threads, bool cv, bool mom, size_t smem) {
     int nb = 0;
-    cudaError_t e = cudaErrorInvalidValue;
-#define DNSMC_O(M)                                                                                              \
-    e = cv ? (mom ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<M, false, true, true, GEN>, threads, 0) \
-                  : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<M, false, true, false, GEN>, threads, 0)) \
-           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_kernel<M, false, false, false, GEN>, threads, 0)
+#define DNSMC_O(M)                                                                                    \
+    nb = cv ? (mom ? march_occupancy_one(march_kernel<M, false, true, true, GEN>, threads, smem)      \
+                   : march_occupancy_one(march_kernel<M, false, true, false, GEN>, threads, smem))    \
+            : march_occupancy_one(march_kernel<M, false, false, false, GEN>, threads, smem)
     if (mode == MODE_GREY) DNSMC_O(MODE_GREY);
     if (mode == MODE_T) DNSMC_O(MODE_T);
     if (mode == MODE_TX) DNSMC_O(MODE_TX);
 #undef DNSMC_O
-    if (e != cudaSuccess) return 1;
     return nb > 0 ? nb : 1;
 }
 

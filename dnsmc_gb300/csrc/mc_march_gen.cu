@@ -10,8 +10,8 @@ int launch_march_gen(int mode, const MarchParams &p, int blocks, int threads, vo
     return launch_march_variant<true>(mode, p, blocks, threads, (cudaStream_t)stream, trace, cv, mom);
 }
 
-int march_gen_occupancy(int mode, int threads, bool cv, bool mom) {
-    return march_variant_occupancy<true>(mode, threads, cv, mom);
+int march_gen_occupancy(int mode, int threads, bool cv, bool mom, size_t smem) {
+    return march_variant_occupancy<true>(mode, threads, cv, mom, smem);
 }
 
 int upload_sobol_dirs_gen(const uint32_t dirs[4][32]) {
