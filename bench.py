@@ -359,6 +359,8 @@ class Arm:
             out["warp_steps"] += float(self.s.item_steps().sum())
             out["errs"].append(rms_error(Q, S))
         out["Q"], out["S"] = Q, S
+        ta, tb = self.s.packet_shape()
+        out["packet_cells"] = ta * tb  # cells of a packet: one warp marches them together
         return out
 
     def e2e(self, T, x, steps):
@@ -701,7 +703,7 @@ def main():
         "validation": validation,
         "rays_per_s": rays_s, "ray_steps_per_s": r["steps"] * world / (t_max / 1e3),
         "march_ms": march_avg, "step_ms": float(np.mean(r["ms"])),
-        "lane_efficiency": r["steps"] / (32.0 * r["warp_steps"]) if r["warp_steps"] else None,
+        "lane_efficiency": r["steps"] / (r["packet_cells"] * r["warp_steps"]) if r["warp_steps"] else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": MARCH_DRAM_BYTES.get((args.method, N_CELL)), "peak_kind": peak_kind,
                      "note": f"algorithmic gather bytes {BYTES_PER_STEP} B per ray-voxel step x lane-steps per "

@@ -88,6 +88,7 @@ SIGNATURES = {
     "dnsmc_set_region": (ctypes.c_int, [ctypes.c_void_p] + [ctypes.c_int] * 6),
     "dnsmc_set_rays": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_int_p]),
     "dnsmc_packet_count": (ctypes.c_int, [ctypes.c_void_p, c_int_p]),
+    "dnsmc_packet_shape": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p]),
     "dnsmc_set_rays_per_item": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, c_int_p]),
     "dnsmc_get_item_steps": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "dnsmc_get_rays_per_item": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p]),

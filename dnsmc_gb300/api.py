@@ -179,6 +179,13 @@ class Solver:
         self._keep = []
         self._rays_dev = False
 
+    def packet_shape(self) -> tuple[int, int]:
+        """(tile_a, tile_b): cells of a packet along j and along k (64-cell
+        packets for the absorbing gas with black walls, 32 otherwise)."""
+        a, b = ctypes.c_int(), ctypes.c_int()
+        check(self._lib.dnsmc_packet_shape(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def packet_count(self) -> int:
         n = ctypes.c_int()
         check(self._lib.dnsmc_packet_count(self._h, ctypes.byref(n)))

@@ -2,7 +2,7 @@
 
     python -m dnsmc_gb300.build        # or dnsmc_gb300.build.build()
 
-Compiles the CUDA translation units with nvcc for sm_103a (the march with
+Compiles the CUDA translation units with nvcc for sm_103a (the marches with
 -fmad=false: it is written with explicit fmaf so the host replay can
 reproduce it bit for bit; the allocation-free solve; the control-variate
 network) and the host runtime with the same nvcc driver, in parallel, then
@@ -60,6 +60,8 @@ def build(verbose: bool = False) -> str:
          "-o", os.path.join(bdir, "mc_host.o")],
         [nvcc, *ARCH, *common, *regs, "-fmad=false", "-c", os.path.join(CSRC, "mc_march_gen.cu"),
          "-o", os.path.join(bdir, "mc_march_gen.o")],
+        [nvcc, *ARCH, *common, *regs, "-fmad=false", "-c", os.path.join(CSRC, "mc_march_pair.cu"),
+         "-o", os.path.join(bdir, "mc_march_pair.o")],
         [nvcc, *ARCH, *common, "-c", os.path.join(CSRC, "mc_noalloc.cu"),
          "-o", os.path.join(bdir, "mc_noalloc.o")],
         [nvcc, *ARCH, *common, "-c", os.path.join(CSRC, "mc_cvnet.cu"),
@@ -72,6 +74,7 @@ def build(verbose: bool = False) -> str:
     _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-Xcompiler", "-fPIC",
           os.path.join(bdir, "mc_kernels.o"), os.path.join(bdir, "mc_host.o"),
           os.path.join(bdir, "mc_noalloc.o"), os.path.join(bdir, "mc_cvnet.o"), os.path.join(bdir, "mc_march_gen.o"),
+          os.path.join(bdir, "mc_march_pair.o"),
           "-o", tmp])
     os.replace(tmp, out)
     if verbose:

@@ -626,9 +626,10 @@ __global__ void alloc_weights_kernel(const AllocParams A) {
     for (long long it = wid; it < (long long)A.G * A.n_packets; it += nw) {
         const int g = (int)(it / A.n_packets), p = (int)(it % A.n_packets);
         const int pa = p % A.npa, rest = p / A.npa, pb = rest % A.npb, pw = rest / A.npb;
-        const int jR = pa * A.tile_a + lane % A.tile_a, kR = pb * A.tile_b + lane / A.tile_a;
         float vs = 0.0f, cs = 0.0f, na = 0.0f;
-        if (jR < A.njR && kR < A.nkR) {
+        for (int cl = lane; cl < A.tile_a * A.tile_b; cl += 32) {  // the packet's cells
+            const int jR = pa * A.tile_a + cl % A.tile_a, kR = pb * A.tile_b + cl / A.tile_a;
+            if (jR >= A.njR || kR >= A.nkR) continue;
             const long long tc = ((long long)pw * A.nkR + kR) * A.njR + jR;
             for (int f = 0; f < A.nfields; ++f) {
                 const float2 x = A.vc[((long long)f * A.G + g) * A.region_cells + tc];

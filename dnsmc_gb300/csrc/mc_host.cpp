@@ -386,6 +386,7 @@ struct dnsmc_solver {
     std::vector<int> rays_pp;                // [group][packet] when rays_pg > 0, else [packet]
     int rays_pg = 0;                         // band groups of a per-item ray table (0: per packet)
     bool rays_dev = false;                   // d_rays_pp was written on the device (no host copy)
+    int rays_np = 0;                         // packets the per-packet / per-item rays were set for
     DevBuf<int> d_rays_pp;
     DevBuf<unsigned long long> d_item_steps; // steps per (field, group, packet) of the last solve
     DevBuf<unsigned int> d_order, d_order_hist;  // longest-first queue order (per-item ray tables)
@@ -915,13 +916,24 @@ int region_dims(const dnsmc_solver *s, int *ni, int *nj, int *nk) {
     return DNSMC_OK;
 }
 
+// Cells per lane of the march: 2 for the absorbing gas with black walls on
+// the fine grid (64-cell packets), 1 for the general medium (particles,
+// grey walls) and the multigrid march (32-cell packets).
+int lane_cells(const dnsmc_solver *s) {
+    const dnsmc_config &c = s->cfg;
+    const bool gen = !s->part.empty() || c.eps_west < 1.0f || c.eps_east < 1.0f;
+    return (gen || c.grid_num > 1) ? 1 : 2;
+}
+
+// Packet tiling of the region: tile_a cells along j (a divisor of 32), by
+// tile_b = 32 * lane_cells / tile_a along k.
 void tiling(const dnsmc_solver *s, int *ta, int *tb, int *npa, int *npb, int *npw) {
     int ni, nj, nk;
     region_dims(s, &ni, &nj, &nk);
     int a = s->cfg.tile_a;
     if (!a) a = nj >= 32 ? 32 : (nj >= 16 ? 16 : 8);
     *ta = a;
-    *tb = 32 / a;
+    *tb = 32 / a * lane_cells(s);
     *npa = (nj + a - 1) / a;
     *npb = (nk + *tb - 1) / *tb;
     *npw = ni;
@@ -1029,6 +1041,11 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.max_steps = c.max_steps;
     P.region_cells = (long long)ni * nj * nk;
     P.n_items = (long long)s->nfields * P.n_groups * P.n_packets;
+    if (per_item && s->rays_np != P.n_packets)
+        return fail(DNSMC_ERR_STATE,
+                    "per-packet rays were set for %d packets, the solve has %d (the packet shape follows the "
+                    "march: particles, grey walls and grid levels use 32-cell packets): set the rays again",
+                    s->rays_np, P.n_packets);
     if (per_item && s->rays_pg > 0) {
         if (s->rays_pg != P.n_groups)
             return fail(DNSMC_ERR_STATE, "per-item ray table has %d band groups, the solve has %d", s->rays_pg,
@@ -1448,6 +1465,7 @@ int solver_rays_device(dnsmc_solver *s, int n_groups, int **rays) {
     s->rays_pp.clear();
     s->rays_pg = n_groups;
     s->rays_dev = true;
+    s->rays_np = np;
     *rays = s->d_rays_pp.p;
     return DNSMC_OK;
 }
@@ -1800,6 +1818,13 @@ int dnsmc_set_region(dnsmc_solver *s, int i0, int i1, int j0, int j1, int k0, in
     return DNSMC_OK;
 }
 
+int dnsmc_packet_shape(const dnsmc_solver *s, int *tile_a, int *tile_b) {
+    if (!s || !tile_a || !tile_b) return fail(DNSMC_ERR_ARG, "null argument");
+    int npa, npb, npw;
+    tiling(s, tile_a, tile_b, &npa, &npb, &npw);
+    return DNSMC_OK;
+}
+
 int dnsmc_packet_count(const dnsmc_solver *s, int *npackets) {
     if (!s || !npackets) return fail(DNSMC_ERR_ARG, "null argument");
     int ta, tb, npa, npb, npw;
@@ -1825,6 +1850,7 @@ int dnsmc_set_rays(dnsmc_solver *s, int rays_per_group, const int *rays_per_pack
             if (rays_per_packet[i] % B) return fail(DNSMC_ERR_ARG, "RQMC: per-packet rays must be multiples of nvar");
         }
         s->rays_pp.assign(rays_per_packet, rays_per_packet + np);
+        s->rays_np = np;
         TRY(s->d_rays_pp.ensure(np));
         CUDA_TRY(cudaMemcpy(s->d_rays_pp.p, s->rays_pp.data(), np * sizeof(int), cudaMemcpyHostToDevice));
     } else {
@@ -1851,6 +1877,7 @@ int dnsmc_set_rays_per_item(dnsmc_solver *s, int n_groups, const int *rays) {
     s->rays_pp.assign(rays, rays + n);
     s->rays_pg = n_groups;
     s->rays_dev = false;
+    s->rays_np = np;
     TRY(s->d_rays_pp.ensure(n));
     CUDA_TRY(cudaMemcpy(s->d_rays_pp.p, s->rays_pp.data(), n * sizeof(int), cudaMemcpyHostToDevice));
     return DNSMC_OK;
@@ -1961,6 +1988,7 @@ int dnsmc_set_rays_adaptive(dnsmc_solver *s, float rays_per_tau, int min_rays, i
     s->rays_pp.clear();
     s->rays_pg = 0;
     s->rays_dev = true;
+    s->rays_np = np;
     return DNSMC_OK;
 }
 

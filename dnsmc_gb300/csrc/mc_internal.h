@@ -207,6 +207,11 @@ int launch_march_gen(int mode, const MarchParams &p, int blocks, int threads, vo
                      bool mom);                                      // mc_march_gen.cu
 int march_gen_occupancy(int mode, int threads, bool cv, bool mom, size_t smem);  // mc_march_gen.cu
 int upload_sobol_dirs_gen(const uint32_t dirs[4][32]);               // mc_march_gen.cu
+// the absorbing-gas march with two cells per lane (64-cell packets)    // mc_march_pair.cu
+int launch_march_pair(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
+                      bool mom);
+int march_pair_occupancy(int mode, int threads, bool cv, bool mom, size_t smem);
+int upload_sobol_dirs_pair(const uint32_t dirs[4][32]);
 int launch_march(int mode, const MarchParams &p, int blocks, int threads,
                  void *stream, bool trace);
 int launch_finalize(const FinalizeParams &p, void *stream);

@@ -198,12 +198,12 @@ static inline int grid_for(long long n, int threads) {
 int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                     bool mom, bool gen) {
     if (gen) return launch_march_gen(mode, p, blocks, threads, stream, trace, cv, mom);
-    return launch_march_variant<false>(mode, p, blocks, threads, (cudaStream_t)stream, trace, cv, mom);
+    return launch_march_pair(mode, p, blocks, threads, stream, trace, cv, mom);
 }
 
 int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen, size_t smem) {
     if (gen) return march_gen_occupancy(mode, threads, cv, mom, smem);
-    return march_variant_occupancy<false>(mode, threads, cv, mom, smem);
+    return march_pair_occupancy(mode, threads, cv, mom, smem);
 }
 
 // Multigrid march (reference tables or grey model; no control variate, no
@@ -472,7 +472,7 @@ __global__ void cv_mean_kernel(const CvParams c) {
     }
 }
 
-// One warp per packet: lanes are the packet's cells.
+// One warp per packet: lane l takes the packet's cells l, l + 32, ...
 __global__ void adaptive_rays_kernel(const AdaptParams A) {
     const int lane = threadIdx.x & 31;
     const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -482,9 +482,10 @@ __global__ void adaptive_rays_kernel(const AdaptParams A) {
         const int pa = (int)(p % A.npa);
         const long long rest = p / A.npa;
         const int pb = (int)(rest % A.npb), pw = (int)(rest / A.npb);
-        const int jR = pa * A.tile_a + lane % A.tile_a, kR = pb * A.tile_b + lane / A.tile_a;
         float tsum = 0.0f, cnt = 0.0f;
-        if (jR < A.njR && kR < A.nkR) {
+        for (int cl = lane; cl < A.tile_a * A.tile_b; cl += 32) {
+            const int jR = pa * A.tile_a + cl % A.tile_a, kR = pb * A.tile_b + cl / A.tile_a;
+            if (jR >= A.njR || kR >= A.nkR) continue;
             const int i = A.ew0 + pw;
             const float h = cbrtf((A.fw[i + 1] - A.fw[i]) * A.da * A.db);
             for (int f = 0; f < A.nfields; ++f) {
@@ -644,8 +645,10 @@ int launch_field_stats(const float *fT, const float2 *fTX, long long n, double *
 int field_stats_partials() { return 3 * kStatBlocks; }
 
 int upload_sobol_dirs(const uint32_t dirs[4][32]) {
-    const int rc = (int)cudaMemcpyToSymbol(c_sobol, dirs, sizeof(uint32_t) * 4 * 32);
-    return rc ? rc : upload_sobol_dirs_gen(dirs);
+    int rc = (int)cudaMemcpyToSymbol(c_sobol, dirs, sizeof(uint32_t) * 4 * 32);
+    if (rc) return rc;
+    rc = upload_sobol_dirs_gen(dirs);
+    return rc ? rc : upload_sobol_dirs_pair(dirs);
 }
 
 int device_sm_count() {

@@ -245,6 +245,12 @@ int  dnsmc_set_rays_adaptive(dnsmc_solver *s, float rays_per_tau, int min_rays,
  * rays (may be NULL) receives max(1, *n_groups) * npackets counts.          */
 int  dnsmc_get_rays_per_item(dnsmc_solver *s, int *n_groups, int *rays);
 int  dnsmc_packet_count(const dnsmc_solver *s, int *npackets);
+/* Packet shape of the next solve: tile_a cells along j by tile_b along k.  A
+ * packet is 64 cells (two per lane of a warp) for the absorbing gas with
+ * black walls on the fine grid, 32 cells with particles, grey walls or
+ * grid_num > 1; the packet count and per-packet ray tables follow it.  No
+ * reference counterpart (the reference runs one thread per cell).           */
+int  dnsmc_packet_shape(const dnsmc_solver *s, int *tile_a, int *tile_b);
 /* Enqueue a solve of every resident snapshot on the solver's stream and return.*/
 int  dnsmc_solve_async(dnsmc_solver *s);
 /* Wait for the last solve, at most timeout_s seconds (<=0: no limit).          */

@@ -569,6 +569,7 @@ typedef struct {
     int mg_fwoff[6];
     float mg_da[6], mg_db[6];
     float Ly, Lz;
+    int cpl;                  // cells per lane: a packet is 32 * cpl cells (tile_a x tile_b)
 } OrcPacketConfig;
 
 }  // extern "C"
@@ -758,16 +759,18 @@ struct Packet {
     void dirs(uint32_t x0, uint32_t x1, R *sW, R *sA, R *sB) const;
 
     // One work item: returns per-lane S, S2; optional trace of ray tr.
-    void item(int f, int G, int p, double S[32], double S2[32], double *steps, int tr, int tmax, int32_t *rec,
+    void item(int f, int G, int p, double S[64], double S2[64], double *steps, int tr, int tmax, int32_t *rec,
               int *nrec, uint32_t *rng) const {
-        const int ta = c.tile_a, tb = 32 / ta;
+        // a packet is nl = 32 * cpl cells; cell l sits at (l % tile_a, l / tile_a)
+        const int nl = 32 * (c.cpl > 1 ? c.cpl : 1);
+        const int ta = c.tile_a, tb = nl / ta;
         const int njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0;
         const int npa = (njR + ta - 1) / ta, npb = (nkR + tb - 1) / tb;
         const int pa = p % npa, rest = p / npa, pb = rest % npb, pw = rest / npb;
         const int w0 = c.ew0 + pw;
-        int a0[32], b0[32];
-        bool act[32];
-        for (int l = 0; l < 32; ++l) {
+        int a0[64], b0[64];
+        bool act[64];
+        for (int l = 0; l < nl; ++l) {
             a0[l] = c.ea0 + pa * ta + l % ta;
             b0[l] = c.eb0 + pb * tb + l / ta;
             act[l] = a0[l] < c.ea1 && b0[l] < c.eb1;
@@ -787,9 +790,9 @@ struct Packet {
             gs = c.group_start[binoff + G];
             K = c.group_start[binoff + G + 1] - gs;
         }
-        R Ti4[32], invTi4[32], ft_i[32], fx_i[32];
-        int ti_i[32], xi_i[32];
-        for (int l = 0; l < 32; ++l) {
+        R Ti4[64], invTi4[64], ft_i[64], fx_i[64];
+        int ti_i[64], xi_i[64];
+        for (int l = 0; l < nl; ++l) {
             const long long o = cidx(f, w0, a0[l], b0[l]);
             const R Ti = (R)c.fieldT[o];
             ti_i[l] = xi_i[l] = 0; ft_i[l] = fx_i[l] = 0; Ti4[l] = invTi4[l] = 0;
@@ -805,15 +808,15 @@ struct Packet {
         const R oW = ((R)c.fw[w0] + (R)c.fw[w0 + 1]) * (R)0.5;
         const R Wgrey = (R)(float)(4.0 * c.kappa * 5.670373e-08);
         const R W4sig = (R)(float)(4.0 * 5.670373e-08);
-        R fvown[32];
-        for (int l = 0; l < 32; ++l) fvown[l] = (c.gen && c.fieldV) ? (R)c.fieldV[cidx(f, w0, a0[l], b0[l])] : (R)0;
+        R fvown[64];
+        for (int l = 0; l < nl; ++l) fvown[l] = (c.gen && c.fieldV) ? (R)c.fieldV[cidx(f, w0, a0[l], b0[l])] : (R)0;
         const float tw = c.T_west, te = c.T_east;
         const R Tw4[2] = {(R)(tw * tw * tw * tw), (R)(te * te * te * te)};
         const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
         const int rb = tr >= 0 ? tr : 0, re = tr >= 0 ? tr + 1 : (K > 0 ? N : 0);
         const int Mb = c.sampler == 1 ? std::max(1, N / std::max(1, c.nbatch)) : 1;
-        double Sb[32];
-        for (int l = 0; l < 32; ++l) Sb[l] = 0.0;
+        double Sb[64];
+        for (int l = 0; l < nl; ++l) Sb[l] = 0.0;
         for (int r = rb; r < re; ++r) {
             uint32_t x[4];
             if (c.sampler == 1) {
@@ -843,8 +846,8 @@ struct Packet {
             // general medium: particle coefficients of the band
             R pab = 0, psc = 0;
             if (c.gen && c.part) { pab = (R)c.part[2 * nbnd]; psc = (R)c.part[2 * nbnd + 1]; }
-            R w[32], wk[32], Ii[32], invI[32], tau[32], D[32];
-            for (int l = 0; l < 32; ++l) {
+            R w[64], wk[64], Ii[64], invI[64], tau[64], D[64];
+            for (int l = 0; l < nl; ++l) {
                 if (c.mode == 0) {
                     Ii[l] = Ti4[l]; invI[l] = invTi4[l];
                     wk[l] = c.gen ? W4sig * FMA<R>(fvown[l], pab, (R)c.kappa) : Wgrey;
@@ -914,8 +917,8 @@ struct Packet {
                 nA = 0; nB = 0;
             };
             dda_init();
-            int ca[32], cb[32];
-            for (int l = 0; l < 32; ++l) { ca[l] = a0[l]; cb[l] = b0[l]; }
+            int ca[64], cb[64];
+            for (int l = 0; l < nl; ++l) { ca[l] = a0[l]; cb[l] = b0[l]; }
             R t = 0;
             // scattering events
             uint32_t ev = 0, evx[4] = {0, 0, 0, 0};
@@ -963,7 +966,7 @@ struct Packet {
                 else { axis = 2; tn = tB; }
                 if (c.gen && tcol < tn) { axis = 3; tn = tcol; }
                 const R ds = tn - t;
-                for (int l = 0; l < 32; ++l) {
+                for (int l = 0; l < nl; ++l) {
                     if (!(tau[l] > 0)) continue;
                     *steps += 1;
                     const long long o = cidx(f, cw, ca[l], cb[l]);
@@ -991,7 +994,7 @@ struct Packet {
                         if (c.gen) {
                             const R eps = (R)c.eps[side];
                             bool any = false;
-                            for (int l = 0; l < 32; ++l) {
+                            for (int l = 0; l < nl; ++l) {
                                 if (tau[l] > 0) {
                                     const R gw = (Ii[l] - Iw) * invI[l];
                                     D[l] = FMA<R>(tau[l] * eps, gw, D[l]);
@@ -1017,7 +1020,7 @@ struct Packet {
                             if (stepn >= c.max_steps) break;
                             continue;
                         }
-                        for (int l = 0; l < 32; ++l) {
+                        for (int l = 0; l < nl; ++l) {
                             if (!(tau[l] > 0)) continue;
                             D[l] = FMA<R>(tau[l], (Ii[l] - Iw) * invI[l], D[l]);
                             tau[l] = 0;
@@ -1029,29 +1032,29 @@ struct Packet {
                 } else if (axis == 1) {
                     ++nA;
                     tA = ((R)nA + offA) * dtA;
-                    for (int l = 0; l < 32; ++l) { ca[l] += dA; if (ca[l] == c.na) ca[l] = 0; else if (ca[l] < 0) ca[l] = c.na - 1; }
+                    for (int l = 0; l < nl; ++l) { ca[l] += dA; if (ca[l] == c.na) ca[l] = 0; else if (ca[l] < 0) ca[l] = c.na - 1; }
                 } else if (axis == 2) {
                     ++nB;
                     tB = ((R)nB + offB) * dtB;
-                    for (int l = 0; l < 32; ++l) { cb[l] += dB; if (cb[l] == c.nb) cb[l] = 0; else if (cb[l] < 0) cb[l] = c.nb - 1; }
+                    for (int l = 0; l < nl; ++l) { cb[l] += dB; if (cb[l] == c.nb) cb[l] = 0; else if (cb[l] < 0) cb[l] = c.nb - 1; }
                 } else {
                     // tentative collision: shared decision, per-lane weights;
                     // q is the butterfly (xor 16, 8, 4, 2, 1) sum of the device
-                    R pl[32], ps[32], pc[32];
-                    for (int l = 0; l < 32; ++l) {
+                    R pl[64], ps[64], pc[64];
+                    for (int l = 0; l < nl; ++l) {
                         const R fvl = c.fieldV ? (R)c.fieldV[cidx(f, cw, ca[l], cb[l])] : (R)0;
                         pl[l] = tau[l] > 0 ? std::fmin((R)1, fvl * psc / sigbar) : (R)0;
                         ps[l] = pl[l];
                         pc[l] = tau[l] > 0 ? (R)1 : (R)0;
                     }
                     for (int o = 16; o > 0; o >>= 1) {
-                        R ns[32], nc[32];
-                        for (int l = 0; l < 32; ++l) { ns[l] = ps[l] + ps[l ^ o]; nc[l] = pc[l] + pc[l ^ o]; }
-                        for (int l = 0; l < 32; ++l) { ps[l] = ns[l]; pc[l] = nc[l]; }
+                        R ns[64], nc[64];
+                        for (int l = 0; l < nl; ++l) { ns[l] = ps[l] + ps[l ^ o]; nc[l] = pc[l] + pc[l ^ o]; }
+                        for (int l = 0; l < nl; ++l) { ps[l] = ns[l]; pc[l] = nc[l]; }
                     }
                     const R q = pc[0] > 0 ? ps[0] / pc[0] : (R)0;
                     if ((R)p_u24(evx[1]) < q) {
-                        for (int l = 0; l < 32; ++l)
+                        for (int l = 0; l < nl; ++l)
                             if (tau[l] > 0) tau[l] = tau[l] * (pl[l] / q);
                         shift_point();
                         pw0 = std::fmin(std::fmax(FMA<R>(sW, t, pw0), (R)c.fw[cw]), (R)c.fw[cw + 1]);
@@ -1059,28 +1062,28 @@ struct Packet {
                         dda_init();
                         t = 0;
                     } else {
-                        for (int l = 0; l < 32; ++l)
+                        for (int l = 0; l < nl; ++l)
                             if (tau[l] > 0) tau[l] = tau[l] * (((R)1 - pl[l]) / ((R)1 - q));
                     }
                     draw();
                     tcol = t + (R)p_neglog(p_u24o(evx[0])) / sigbar;
                 }
                 bool any = false;
-                for (int l = 0; l < 32; ++l) any = any || (tau[l] > 0);
+                for (int l = 0; l < nl; ++l) any = any || (tau[l] > 0);
                 if (!any) break;
                 if (stepn >= (c.mg_levels > 1 ? c.mg_steps : c.max_steps)) break;
             }
             if (c.mg_levels > 1) {
                 // coarse grids: per-lane position-update march in lockstep
                 bool any = false;
-                for (int l = 0; l < 32; ++l) any = any || (tau[l] > 0);
+                for (int l = 0; l < nl; ++l) any = any || (tau[l] > 0);
                 if (any) {
                     const R ua = t / dtA - (R)nA, ub = t / dtB - (R)nB;
                     const R fa = std::fmin(std::fmax(dA > 0 ? (R)0.5 + ua : (R)0.5 - ua, (R)0), (R)1);
                     const R fb = std::fmin(std::fmax(dB > 0 ? (R)0.5 + ub : (R)0.5 - ub, (R)0), (R)1);
-                    R xp[32], yp[32], zp[32];
-                    int ic[32], jc[32], kc[32];
-                    for (int l = 0; l < 32; ++l) {
+                    R xp[64], yp[64], zp[64];
+                    int ic[64], jc[64], kc[64];
+                    for (int l = 0; l < nl; ++l) {
                         xp[l] = FMA<R>(sW, t, oW);
                         yp[l] = ((R)ca[l] + fa) * (R)c.da;
                         zp[l] = ((R)cb[l] + fb) * (R)c.db;
@@ -1093,14 +1096,14 @@ struct Packet {
                         const R daL = (R)c.mg_da[lv], dbL = (R)c.mg_db[lv];
                         const float *TL = c.mgT + c.mg_off[lv] + (long long)f * nwL * naL * nbL;
                         const int cap = (lv == c.mg_levels - 1) ? c.max_steps : c.mg_steps;
-                        for (int l = 0; l < 32; ++l) { ic[l] >>= 1; jc[l] >>= 1; kc[l] >>= 1; }
+                        for (int l = 0; l < nl; ++l) { ic[l] >>= 1; jc[l] >>= 1; kc[l] >>= 1; }
                         int counter = 0;
                         for (;;) {
                             bool go = false;
-                            for (int l = 0; l < 32; ++l) go = go || (tau[l] > 0 && counter < cap);
+                            for (int l = 0; l < nl; ++l) go = go || (tau[l] > 0 && counter < cap);
                             if (!go) break;
                             R dsr0 = 0;  // lane 0's segment this iteration (0 when it idles)
-                            for (int l = 0; l < 32; ++l) {
+                            for (int l = 0; l < nl; ++l) {
                                 if (!(tau[l] > 0 && counter < cap)) continue;
                                 *steps += 1;
                                 const R fx = (R)fwL[dW > 0 ? ic[l] + 1 : ic[l]];
@@ -1169,7 +1172,7 @@ struct Packet {
                 }
             }
             if (nrec) *nrec = stepn;
-            for (int l = 0; l < 32; ++l) {
+            for (int l = 0; l < nl; ++l) {
                 if (!act[l]) continue;
                 R X = w[l] * D[l];
                 if (c.cv) {
@@ -1236,8 +1239,11 @@ extern "C" {
 
 // Tally [f][G][iR][kR][jR][2] (sum X, sum X^2) exactly as the device stores it.
 int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double *steps_out) {
-    if (!c || c->tile_a < 1 || 32 % c->tile_a) return 1;
-    const int ta = c->tile_a, tb = 32 / ta;
+    if (!c || c->tile_a < 1 || 32 % c->tile_a || c->cpl < 0 || c->cpl > 2) return 1;
+    // the general medium and the multigrid march run 32-cell packets only
+    if (c->cpl > 1 && (c->gen || c->mg_levels > 1)) return 1;
+    const int nl = 32 * (c->cpl > 1 ? c->cpl : 1);
+    const int ta = c->tile_a, tb = nl / ta;
     const int niR = c->ew1 - c->ew0, njR = c->ea1 - c->ea0, nkR = c->eb1 - c->eb0;
     const int npa = (njR + ta - 1) / ta, npb = (nkR + tb - 1) / tb;
     const int np = npa * npb * niR;
@@ -1253,12 +1259,12 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
         const int p = (int)(it % np);
         const long long fg = it / np;
         const int G = (int)(fg % nG), f = (int)(fg / nG);
-        double S[32], S2[32], st = 0;
+        double S[64], S2[64], st = 0;
         if (c->use_double) Packet<double>(*c).item(f, G, p, S, S2, &st, -1, 0, nullptr, nullptr, nullptr);
         else Packet<float>(*c).item(f, G, p, S, S2, &st, -1, 0, nullptr, nullptr, nullptr);
         steps += st;
         const int pa = p % npa, rest = p / npa, pb = rest % npb, pw = rest / npb;
-        for (int l = 0; l < 32; ++l) {
+        for (int l = 0; l < nl; ++l) {
             const int a = c->ea0 + pa * ta + l % ta, b = c->eb0 + pb * tb + l / ta;
             if (a >= c->ea1 || b >= c->eb1) continue;
             const long long tc = ((long long)pw * nkR + (b - c->eb0)) * njR + (a - c->ea0);
@@ -1272,7 +1278,9 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
 
 int orc_packet_trace(const OrcPacketConfig *c, int f, int G, int p, int r, int max_steps, int32_t *rec, int *n,
                      uint32_t rng[4]) {
-    double S[32], S2[32], st = 0;
+    if (!c || c->tile_a < 1 || 32 % c->tile_a || c->cpl < 0 || c->cpl > 2) return 1;
+    if (c->cpl > 1 && (c->gen || c->mg_levels > 1)) return 1;
+    double S[64], S2[64], st = 0;
     Packet<float>(*c).item(f, G, p, S, S2, &st, r, max_steps, rec, n, rng);
     return 0;
 }

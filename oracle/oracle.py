@@ -67,6 +67,7 @@ class PacketConfig(ctypes.Structure):
         ("mg_levels", ctypes.c_int), ("mg_steps", ctypes.c_int), ("mgT", _f), ("mgfw", _f),
         ("mg_off", ctypes.c_longlong * 6), ("mg_fwoff", ctypes.c_int * 6), ("mg_da", ctypes.c_float * 6),
         ("mg_db", ctypes.c_float * 6), ("Ly", ctypes.c_float), ("Lz", ctypes.c_float),
+        ("cpl", ctypes.c_int),
     ]
 
 
@@ -181,7 +182,8 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
     i0, i1, j0, j1, k0, k1 = solver._region
     c.ew0, c.ew1, c.ea0, c.ea1, c.eb0, c.eb1 = i0, i1, j0, j1, k0, k1
     nj = j1 - j0
-    c.tile_a = cfg.tile_a or (32 if nj >= 32 else (16 if nj >= 16 else 8))
+    ta, tb = solver.packet_shape()
+    c.tile_a, c.cpl = ta, ta * tb // 32
     c.nfields = T.shape[0]
     c.fieldT = _fp(T)
     if x is not None:

@@ -249,7 +249,8 @@ def test_rqmc_requires_replicates_and_divisible_rays():
     with pytest.raises(D.DnsmcError):
         D.Solver(D.default_config(sampler=D.SAMPLER_RQMC, nvar=1))
     s = D.Solver(D.default_config(model=D.MODEL_GREY, sampler=D.SAMPLER_RQMC, nvar=4, imax=8, jmax=8, kmax=8))
-    assert s.packet_count() == 8 * 2  # 8x4 tiles: 2 packets per wall-normal plane
+    assert s.packet_shape() == (8, 8)  # the grey black-wall march: 64-cell packets, two cells per lane
+    assert s.packet_count() == 8        # one packet per wall-normal plane
     with pytest.raises(D.DnsmcError) as e:
         s.set_rays(10)
     assert e.value.code == _lib.ERR_ARG

@@ -11,7 +11,7 @@ import pytest
 import dnsmc_gb300 as D
 from dnsmc_gb300 import autotune, cvtrain, synth
 from test_gpu_cv import assert_bitexact_cv
-from test_gpu_parity import assert_bitexact, smooth_field
+from test_gpu_parity import assert_bitexact, packet_index, smooth_field
 
 pytestmark = pytest.mark.gpu
 
@@ -46,8 +46,10 @@ def test_adaptive_rays_follow_optical_thickness():
     f = RegularGridInterpolator((Tg, Xg), kp)
     tau = f(np.stack([np.clip(T, Tg[0], Tg[-1]), np.clip(x, Xg[0], Xg[-1])], -1).reshape(-1, 2)).reshape(T.shape)
     tau = tau * h[None, None, None, :]
-    # packets: (i, k) lines of 32 j cells; mean over cells and both snapshots
-    tau_p = tau.mean(axis=(0, 2)).T.reshape(-1)                  # p = i * nk + k
+    # per packet: mean over its cells and both snapshots
+    pidx = packet_index(s).ravel()                               # (k, j, i) like tau[f]
+    npk = s.packet_count()
+    tau_p = np.bincount(pidx, tau.mean(axis=0).ravel(), npk) / np.bincount(pidx, minlength=npk)
     expect = np.clip(np.rint(40.0 * tau_p / 4) * 4, 8, 256)
     assert np.abs(rp - expect).max() <= 4
     assert (rp == expect).mean() > 0.95

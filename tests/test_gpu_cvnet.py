@@ -23,7 +23,7 @@ import dnsmc_gb300 as D
 from dnsmc_gb300 import cvtrain, synth
 from oracle import cvnet_oracle as NO
 from test_gpu_cv import assert_bitexact_cv
-from test_gpu_parity import smooth_field
+from test_gpu_parity import packet_index, smooth_field
 
 pytestmark = pytest.mark.gpu
 
@@ -186,8 +186,12 @@ def test_apply_sets_coefficients_and_rays_then_solves_bitexact():
     # the allocation from the outputs, in float64: n ~ sqrt(v_sum / c), expected steps = 16 x uniform
     v = np.exp(np.clip(out[:, 2:16:4], -15, 15)).reshape(12, 4, 32, 4)     # (i, k, j, g)
     cst = 30.0 * np.exp(np.clip(out[:, 3:16:4], -15, 15)).reshape(12, 4, 32, 4)
-    # a packet is one (i, k) line of 32 j cells: p = i * 4 + k
-    vs, cs = v.sum(axis=2).reshape(48, 4).T, cst.mean(axis=2).reshape(48, 4).T   # (g, packet)
+    # per packet: v summed, c averaged over its cells
+    pt = packet_index(s).transpose(2, 0, 1).ravel()                          # (i, k, j) tally order
+    npk = s.packet_count()
+    cnt = np.bincount(pt, minlength=npk)
+    vs = np.stack([np.bincount(pt, v[..., g].ravel(), npk) for g in range(4)])       # (g, packet)
+    cs = np.stack([np.bincount(pt, cst[..., g].ravel(), npk) / cnt for g in range(4)])
     w = np.sqrt(vs / np.maximum(cs, 1e-3))
     lam = 16 * cs.sum() / (w * cs).sum()
     expect = np.clip(np.rint(lam * w / 4) * 4, 4, 64)

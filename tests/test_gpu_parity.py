@@ -51,6 +51,17 @@ def region_tally_to_dense(tal, solver, ng):
     return tal.reshape(nf, ng, ni, nk, nj, 2).transpose(0, 1, 3, 4, 2, 5)
 
 
+def packet_index(solver):
+    """Packet of every region cell, (nk, nj, ni): tile_a x tile_b tiles of
+    each wall-normal plane, j fastest."""
+    i0, i1, j0, j1, k0, k1 = solver._region
+    ni, nj, nk = i1 - i0, j1 - j0, k1 - k0
+    ta, tb = solver.packet_shape()
+    npa, npb = -(-nj // ta), -(-nk // tb)
+    kk, jj, ii = np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni), indexing="ij")
+    return (ii * npb + kk // tb) * npa + jj // ta
+
+
 def rays_per_cell(solver, g=0):
     i0, i1, j0, j1, k0, k1 = solver._region
     ni, nj, nk = i1 - i0, j1 - j0, k1 - k0
@@ -59,12 +70,7 @@ def rays_per_cell(solver, g=0):
     rp = solver._keep[0]
     if rp.ndim == 2:  # per (band group, packet)
         rp = rp[g]
-    ta = solver.cfg.tile_a or (32 if nj >= 32 else (16 if nj >= 16 else 8))
-    tb = 32 // ta
-    npa, npb = -(-nj // ta), -(-nk // tb)
-    kk, jj, ii = np.meshgrid(np.arange(nk), np.arange(nj), np.arange(ni), indexing="ij")
-    p = (ii * npb + kk // tb) * npa + jj // ta
-    return rp[p].astype(np.float64)
+    return rp[packet_index(solver)].astype(np.float64)
 
 
 def assert_bitexact(solver, T, x=None):
@@ -282,9 +288,10 @@ def test_grey_slab_matches_analytic_solution():
     Q, S = s.solve(timeout_s=120)
     yc = (np.arange(ni) + 0.5) * 2.0 / ni
     exact = O.slab_divq(yc, 2.0, 1.0, 1000.0, 0.0, 300.0)
-    # one cell per packet is independent (lanes of a packet share rays)
-    q = Q[0][:, 0, :].mean(0)
-    se = np.sqrt((S[0][:, 0, :] ** 2).sum(0)) / nk
+    # one cell per packet is independent (the cells of a packet share rays)
+    tb = s.packet_shape()[1]
+    q = Q[0][::tb, 0, :].mean(0)
+    se = np.sqrt((S[0][::tb, 0, :] ** 2).sum(0)) / (nk // tb)
     z = (q - exact) / se
     assert np.abs(z).max() < 4.0, z
     assert math.sqrt((z ** 2).mean()) < 1.5
@@ -306,8 +313,9 @@ def test_golden_resfortm_on_gpu(tmp_path, particle_tables, resfortm):
     s.set_region(0, 64, 0, 32, 0, 32)
     s.set_rays(3000)
     Q, S = s.solve(timeout_s=300)
-    q = Q[0][:, 0, :].mean(0)  # one lane per packet: 32 independent packets per row
-    se = np.sqrt((S[0][:, 0, :] ** 2).sum(0)) / 32
+    tb = s.packet_shape()[1]
+    q = Q[0][::tb, 0, :].mean(0)  # one cell per packet: independent packets of each row
+    se = np.sqrt((S[0][::tb, 0, :] ** 2).sum(0)) / (32 // tb)
     gse = resfortm["plane_std"] / 64
     z = (q - resfortm["Q"]) / np.sqrt(se ** 2 + gse ** 2)
     assert math.sqrt((z ** 2).mean()) < 1.6, z
@@ -431,7 +439,8 @@ def test_bitexact_rqmc_local_bins_and_trace():
     assert_bitexact(s, T, x)
     assert s.sampling()["n_tbins"] == 20
     c, keep = O.packet_config(s, T, x)
-    for p, r in [(0, 0), (3, 13), (31, 47)]:
+    npk = s.packet_count()
+    for p, r in [(0, 0), (3, 13), (npk - 1, 47)]:
         rec, n, rng = s.trace(0, 1, p, r)
         rec2, n2, rng2 = O.packet_trace(c, 0, 1, p, r)
         assert n == n2
