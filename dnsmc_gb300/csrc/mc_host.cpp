@@ -916,13 +916,13 @@ int region_dims(const dnsmc_solver *s, int *ni, int *nj, int *nk) {
     return DNSMC_OK;
 }
 
-// Cells per lane of the march: 2 for the absorbing gas with black walls on
-// the fine grid (64-cell packets), 1 for the general medium (particles,
-// grey walls) and the multigrid march (32-cell packets).
+// Cells per lane of the march: kLaneCells for the absorbing gas with black
+// walls on the fine grid, 1 for the general medium (particles, grey walls)
+// and the multigrid march (32-cell packets).
 int lane_cells(const dnsmc_solver *s) {
     const dnsmc_config &c = s->cfg;
     const bool gen = !s->part.empty() || c.eps_west < 1.0f || c.eps_east < 1.0f;
-    return (gen || c.grid_num > 1) ? 1 : 2;
+    return (gen || c.grid_num > 1) ? 1 : kLaneCells;
 }
 
 // Packet tiling of the region: tile_a cells along j (a divisor of 32), by
@@ -1068,8 +1068,9 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         int smax = 0;
         if (cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device) != cudaSuccess)
             smax = 48 * 1024;
-        if (march_smem(P, threads) > (size_t)smax) threads = 128;
-        if (march_smem(P, threads) > (size_t)smax)
+        const size_t stat = 32 * 1024;  // the march kernels' static shared memory, at most
+        if (march_smem(P, threads) + stat > (size_t)smax) threads = 128;
+        if (march_smem(P, threads) + stat > (size_t)smax)
             return fail(DNSMC_ERR_TABLE, "a spectral sample's table slab (%d bytes) exceeds the shared memory of the march",
                         P.slab_len * 8);
     }

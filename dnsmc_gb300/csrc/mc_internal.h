@@ -29,6 +29,10 @@ struct SpecEntry {
     float    W;         // ray weight factor: w = W * k(T_i) * Ib(T_i)
 };
 
+// Cells per lane of the absorbing-gas march (mc_march_pair.cu): a packet is
+// 32 * kLaneCells cells; the general-medium and multigrid marches use 1.
+constexpr int kLaneCells = 2;
+
 struct MarchParams {
     // geometry: nw wall-normal cells (reference i), na (j) and nb (k) periodic
     int nw, na, nb;

@@ -801,23 +801,29 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
     }
 }
 
-// One launch of a march kernel with `smem` bytes of dynamic shared memory
-// (raising the kernel's limit above the default 48 KB when needed), and its
-// resident blocks per SM.
+// Dynamic shared memory of a march kernel: a kernel whose static plus
+// dynamic shared memory exceeds the default 48 KB per block needs its limit
+// raised once (queried first, so a launch inside a graph capture only reads).
+inline int march_prepare_smem(void (*k)(const MarchParams), size_t smem) {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k);
+    if (e != cudaSuccess) return (int)e;
+    if (fa.sharedSizeBytes + smem > 48u * 1024u && (size_t)fa.maxDynamicSharedSizeBytes < smem)
+        e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return (int)e;
+}
+
+// One launch of a march kernel with `smem` bytes of dynamic shared memory,
+// and its resident blocks per SM.
 inline int march_launch_one(void (*k)(const MarchParams), int blocks, int threads, size_t smem, cudaStream_t st,
                             const MarchParams &p) {
-    if (smem > 48u * 1024u) {
-        const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return (int)e;
-    }
+    if (const int e = march_prepare_smem(k, smem)) return e;
     k<<<blocks, threads, smem, st>>>(p);
     return (int)cudaGetLastError();
 }
 
 inline int march_occupancy_one(void (*k)(const MarchParams), int threads, size_t smem) {
-    if (smem > 48u * 1024u &&
-        cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return 0;
+    if (march_prepare_smem(k, smem)) return 0;
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, threads, smem) != cudaSuccess) return 0;
     return nb;

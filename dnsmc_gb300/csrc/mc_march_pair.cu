@@ -18,10 +18,15 @@
 
 namespace dnsmc {
 
+// Resident 256-thread blocks per SM of this march (2: up to 128 registers a
+// thread; its two cells per lane carry twice the per-cell state).
+#ifndef DNSMC_PAIR_MINB
+#define DNSMC_PAIR_MINB 2
+#endif
 template <int MODE, bool TRACE, bool CV, bool MOM>
-__global__ void __launch_bounds__(256, DNSMC_MINB) march_pair_kernel(const MarchParams P) {
+__global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const MarchParams P) {
     typedef typename FieldT<MODE>::type VT;
-    constexpr int C = 2;  // cells per lane
+    constexpr int C = kLaneCells;  // cells per lane
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int tid = threadIdx.x;
@@ -295,7 +300,9 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_pair_kernel(const March
                 }
 #pragma unroll
                 for (int k = 0; k < C; ++k) vcur[k] = vnext[k];
-                const bool alive = tau[0] > 0.0f || tau[1] > 0.0f;
+                bool alive = false;
+#pragma unroll
+                for (int k = 0; k < C; ++k) alive = alive || tau[k] > 0.0f;
                 if (!__any_sync(FULL, alive)) break;
                 if (steps >= P.max_steps) {
                     if (alive) flags |= DNSMC_STATUS_STEP_CAP;

@@ -117,9 +117,9 @@ extern "C" int dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu
     int rc = launch_pack_T(dT, field, c.imax, c.jmax, c.kmax, 1, c.imax, (long long)c.imax * c.jmax, 0, st);
     if (rc) return report_error(DNSMC_ERR_CUDA, cudaGetErrorString((cudaError_t)rc));
 
-    // 64-cell packets: the grey black-wall march runs two cells per lane
+    // the grey black-wall march runs kLaneCells cells per lane
     const int ta = c.tile_a ? c.tile_a : (c.jmax >= 32 ? 32 : (c.jmax >= 16 ? 16 : 8));
-    const int tb = 32 / ta * 2;
+    const int tb = 32 / ta * kLaneCells;
     MarchParams P{};
     P.nw = c.imax; P.na = c.jmax; P.nb = c.kmax;
     P.da = c.Ly / (float)c.jmax; P.db = c.Lz / (float)c.kmax;

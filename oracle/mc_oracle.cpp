@@ -569,7 +569,7 @@ typedef struct {
     int mg_fwoff[6];
     float mg_da[6], mg_db[6];
     float Ly, Lz;
-    int cpl;                  // cells per lane: a packet is 32 * cpl cells (tile_a x tile_b)
+    int cpl;                  // cells per lane (1, 2 or 4): a packet is 32 * cpl cells (tile_a x tile_b)
 } OrcPacketConfig;
 
 }  // extern "C"
@@ -759,7 +759,7 @@ struct Packet {
     void dirs(uint32_t x0, uint32_t x1, R *sW, R *sA, R *sB) const;
 
     // One work item: returns per-lane S, S2; optional trace of ray tr.
-    void item(int f, int G, int p, double S[64], double S2[64], double *steps, int tr, int tmax, int32_t *rec,
+    void item(int f, int G, int p, double S[128], double S2[128], double *steps, int tr, int tmax, int32_t *rec,
               int *nrec, uint32_t *rng) const {
         // a packet is nl = 32 * cpl cells; cell l sits at (l % tile_a, l / tile_a)
         const int nl = 32 * (c.cpl > 1 ? c.cpl : 1);
@@ -768,8 +768,8 @@ struct Packet {
         const int npa = (njR + ta - 1) / ta, npb = (nkR + tb - 1) / tb;
         const int pa = p % npa, rest = p / npa, pb = rest % npb, pw = rest / npb;
         const int w0 = c.ew0 + pw;
-        int a0[64], b0[64];
-        bool act[64];
+        int a0[128], b0[128];
+        bool act[128];
         for (int l = 0; l < nl; ++l) {
             a0[l] = c.ea0 + pa * ta + l % ta;
             b0[l] = c.eb0 + pb * tb + l / ta;
@@ -790,8 +790,8 @@ struct Packet {
             gs = c.group_start[binoff + G];
             K = c.group_start[binoff + G + 1] - gs;
         }
-        R Ti4[64], invTi4[64], ft_i[64], fx_i[64];
-        int ti_i[64], xi_i[64];
+        R Ti4[128], invTi4[128], ft_i[128], fx_i[128];
+        int ti_i[128], xi_i[128];
         for (int l = 0; l < nl; ++l) {
             const long long o = cidx(f, w0, a0[l], b0[l]);
             const R Ti = (R)c.fieldT[o];
@@ -808,14 +808,14 @@ struct Packet {
         const R oW = ((R)c.fw[w0] + (R)c.fw[w0 + 1]) * (R)0.5;
         const R Wgrey = (R)(float)(4.0 * c.kappa * 5.670373e-08);
         const R W4sig = (R)(float)(4.0 * 5.670373e-08);
-        R fvown[64];
+        R fvown[128];
         for (int l = 0; l < nl; ++l) fvown[l] = (c.gen && c.fieldV) ? (R)c.fieldV[cidx(f, w0, a0[l], b0[l])] : (R)0;
         const float tw = c.T_west, te = c.T_east;
         const R Tw4[2] = {(R)(tw * tw * tw * tw), (R)(te * te * te * te)};
         const uint32_t k0 = (uint32_t)c.seed, k1 = (uint32_t)(c.seed >> 32);
         const int rb = tr >= 0 ? tr : 0, re = tr >= 0 ? tr + 1 : (K > 0 ? N : 0);
         const int Mb = c.sampler == 1 ? std::max(1, N / std::max(1, c.nbatch)) : 1;
-        double Sb[64];
+        double Sb[128];
         for (int l = 0; l < nl; ++l) Sb[l] = 0.0;
         for (int r = rb; r < re; ++r) {
             uint32_t x[4];
@@ -846,7 +846,7 @@ struct Packet {
             // general medium: particle coefficients of the band
             R pab = 0, psc = 0;
             if (c.gen && c.part) { pab = (R)c.part[2 * nbnd]; psc = (R)c.part[2 * nbnd + 1]; }
-            R w[64], wk[64], Ii[64], invI[64], tau[64], D[64];
+            R w[128], wk[128], Ii[128], invI[128], tau[128], D[128];
             for (int l = 0; l < nl; ++l) {
                 if (c.mode == 0) {
                     Ii[l] = Ti4[l]; invI[l] = invTi4[l];
@@ -917,7 +917,7 @@ struct Packet {
                 nA = 0; nB = 0;
             };
             dda_init();
-            int ca[64], cb[64];
+            int ca[128], cb[128];
             for (int l = 0; l < nl; ++l) { ca[l] = a0[l]; cb[l] = b0[l]; }
             R t = 0;
             // scattering events
@@ -1040,7 +1040,7 @@ struct Packet {
                 } else {
                     // tentative collision: shared decision, per-lane weights;
                     // q is the butterfly (xor 16, 8, 4, 2, 1) sum of the device
-                    R pl[64], ps[64], pc[64];
+                    R pl[128], ps[128], pc[128];
                     for (int l = 0; l < nl; ++l) {
                         const R fvl = c.fieldV ? (R)c.fieldV[cidx(f, cw, ca[l], cb[l])] : (R)0;
                         pl[l] = tau[l] > 0 ? std::fmin((R)1, fvl * psc / sigbar) : (R)0;
@@ -1048,7 +1048,7 @@ struct Packet {
                         pc[l] = tau[l] > 0 ? (R)1 : (R)0;
                     }
                     for (int o = 16; o > 0; o >>= 1) {
-                        R ns[64], nc[64];
+                        R ns[128], nc[128];
                         for (int l = 0; l < nl; ++l) { ns[l] = ps[l] + ps[l ^ o]; nc[l] = pc[l] + pc[l ^ o]; }
                         for (int l = 0; l < nl; ++l) { ps[l] = ns[l]; pc[l] = nc[l]; }
                     }
@@ -1081,8 +1081,8 @@ struct Packet {
                     const R ua = t / dtA - (R)nA, ub = t / dtB - (R)nB;
                     const R fa = std::fmin(std::fmax(dA > 0 ? (R)0.5 + ua : (R)0.5 - ua, (R)0), (R)1);
                     const R fb = std::fmin(std::fmax(dB > 0 ? (R)0.5 + ub : (R)0.5 - ub, (R)0), (R)1);
-                    R xp[64], yp[64], zp[64];
-                    int ic[64], jc[64], kc[64];
+                    R xp[128], yp[128], zp[128];
+                    int ic[128], jc[128], kc[128];
                     for (int l = 0; l < nl; ++l) {
                         xp[l] = FMA<R>(sW, t, oW);
                         yp[l] = ((R)ca[l] + fa) * (R)c.da;
@@ -1239,7 +1239,7 @@ extern "C" {
 
 // Tally [f][G][iR][kR][jR][2] (sum X, sum X^2) exactly as the device stores it.
 int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double *steps_out) {
-    if (!c || c->tile_a < 1 || 32 % c->tile_a || c->cpl < 0 || c->cpl > 2) return 1;
+    if (!c || c->tile_a < 1 || 32 % c->tile_a || c->cpl < 0 || c->cpl > 4) return 1;
     // the general medium and the multigrid march run 32-cell packets only
     if (c->cpl > 1 && (c->gen || c->mg_levels > 1)) return 1;
     const int nl = 32 * (c->cpl > 1 ? c->cpl : 1);
@@ -1259,7 +1259,7 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
         const int p = (int)(it % np);
         const long long fg = it / np;
         const int G = (int)(fg % nG), f = (int)(fg / nG);
-        double S[64], S2[64], st = 0;
+        double S[128], S2[128], st = 0;
         if (c->use_double) Packet<double>(*c).item(f, G, p, S, S2, &st, -1, 0, nullptr, nullptr, nullptr);
         else Packet<float>(*c).item(f, G, p, S, S2, &st, -1, 0, nullptr, nullptr, nullptr);
         steps += st;
@@ -1278,9 +1278,9 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
 
 int orc_packet_trace(const OrcPacketConfig *c, int f, int G, int p, int r, int max_steps, int32_t *rec, int *n,
                      uint32_t rng[4]) {
-    if (!c || c->tile_a < 1 || 32 % c->tile_a || c->cpl < 0 || c->cpl > 2) return 1;
+    if (!c || c->tile_a < 1 || 32 % c->tile_a || c->cpl < 0 || c->cpl > 4) return 1;
     if (c->cpl > 1 && (c->gen || c->mg_levels > 1)) return 1;
-    double S[64], S2[64], st = 0;
+    double S[128], S2[128], st = 0;
     Packet<float>(*c).item(f, G, p, S, S2, &st, r, max_steps, rec, n, rng);
     return 0;
 }
