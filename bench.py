@@ -560,7 +560,7 @@ def run_c4(args):
 # DRAM bytes (read + write) of one march launch measured by an ncu capture of
 # the default command (128^3, network control variate): the tallies and L2
 # refills, not the gathers, which L1/L2 serve
-MARCH_DRAM_BYTES = {("net", 128): 432.6e6 + 775.07e6}
+MARCH_DRAM_BYTES = {("net", 128): 187.70e6 + 251.20e6}
 
 # kernels per step: table coordinates, march, finalize; the control variate adds
 # layer means, surrogate table, 1-D quadrature and E[Y]; the network adds
@@ -707,8 +707,10 @@ def main():
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": MARCH_DRAM_BYTES.get((args.method, N_CELL)), "peak_kind": peak_kind,
                      "note": f"algorithmic gather bytes {BYTES_PER_STEP} B per ray-voxel step x lane-steps per "
-                             f"launch / march kernel time (CUDA events); traffic = ncu DRAM read+write bytes "
-                             f"per march launch"},
+                             f"launch / march kernel time (CUDA events); the gathers are served on chip (field "
+                             f"and tables in L2, each ray's table slab in shared memory), so frac above 1 is "
+                             f"on-chip reuse; the march is bound by instruction issue; traffic = ncu DRAM "
+                             f"read+write bytes per march launch"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_max, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "timing": "wall clock around set_fields + (network) + solve + get_results"},

@@ -4,8 +4,9 @@ Sweeps, per workload, the knobs that change speed but not the estimator's
 expectation:
 
 * block_threads  -- threads per block of the persistent march (128, 256);
-* tile_a         -- packet shape: 32 lanes tile tile_a x (32 / tile_a) cells
-                    of the periodic (j, k) plane (8, 16, 32);
+* tile_a         -- packet shape: a warp's packet tiles tile_a x
+                    (32 * cells per lane / tile_a) cells of the periodic
+                    (j, k) plane (8, 16, 32);
 * n_groups       -- band-group count, i.e. band-group size (bands per
                     group) for the spectral stratification (4, 8, 16 bands).
 

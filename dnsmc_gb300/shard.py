@@ -9,9 +9,9 @@ hands each node the j-slab [xstart(2), xend(2)] of its decomp_2d pencil
 (code/fix_var.f:95-121); here the slab is a solver region and the gather a
 torch.distributed collective on host tensors (gloo or NCCL process group).
 
-Slabs are whole packet rows (multiples of the 32-lane packet tile along j),
-so no packet straddles two ranks, and every rank uses its own RNG key so the
-slabs' random streams are independent.
+Slabs are whole packet rows (multiples of the packet width along j, at
+most 32 cells), so no packet straddles two ranks, and every rank uses its
+own RNG key so the slabs' random streams are independent.
 """
 from __future__ import annotations
 
