@@ -269,7 +269,13 @@ struct CvParams {
     const float *fieldV;      // [f][i][k][j] volume fraction, or null
     const float2 *part;       // [band] (absorption, scattering) per unit volume fraction
     float *layerV;            // [f][nw] layer-mean volume fraction
+    // node sums of E[Y] (tables without particles): per (field, group,
+    // region layer) the sums over the group's samples at every table node,
+    // then per group the layer-independent ones; cv_node_count() doubles
+    double *nodes;
+    const double *ktab_d, *ibtab_d;  // FP64 copies of ktab and ibtab
 };
+long long cv_node_count(const CvParams &c);
 int launch_cv_prepare(const CvParams &c, void *stream);
 int launch_cv_mean(const CvParams &c, void *stream);
 int upload_quadrature(const double *mu, const double *w, int n);  // once per device

@@ -472,6 +472,198 @@ __global__ void cv_mean_kernel(const CvParams c) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// E[Y] through node sums (tables without particles).  With k_s(T, x) the
+// bilinear and Ib_s(T) the linear interpolant of the tables at the cell's
+// table coordinates (weights wt_a in T, wx_b in x),
+//   E[Y_a] = sum_s C_s k_s Ib_s - sum_s C_s Jhat_s(w) k_s,
+//   E[Y_b] = sum_s C_s Ahat_s(w) k_s Ib_s - sum_s C_s Ahat_s(w) Ibar_s(w) k_s,
+// and every sum is a fixed combination of sums over the samples taken at
+// the table nodes:
+//   GJ(w)[t][x]          = sum_s C_s Jhat_s(w) k_s[t][x]
+//   GB(w)[t][x]          = sum_s C_s Ahat_s(w) Ibar_s(w) k_s[t][x]
+//   MB(w)[t][x][a][a']   = sum_s C_s Ahat_s(w) k_s[t+a][x] Ib_s[t+a']
+//   M[t][x][a][a']       = sum_s C_s k_s[t+a][x] Ib_s[t+a']      (no layer)
+// so a cell needs 24 node sums per group instead of a pass over the group's
+// samples.  FP64 throughout (sums over the samples, and the cell's
+// combination): exact to the FP32 rounding of the march's own lookups.
+// ---------------------------------------------------------------------------
+struct NodeLayout {
+    int nTX, nM, per;  // nodes, (t cell, x node, a, a') entries, doubles per (field, group, layer)
+};
+__host__ __device__ inline NodeLayout node_layout(const CvParams &c) {
+    NodeLayout L;
+    L.nTX = c.nT * c.nX;
+    L.nM = (c.nT - 1) * c.nX * 4;
+    L.per = 2 * L.nTX + L.nM;
+    return L;
+}
+
+long long cv_node_count(const CvParams &c) {
+    const NodeLayout L = node_layout(c);
+    const long long niR = c.ew1 - c.ew0;
+    return (long long)c.nfields * c.n_groups * niR * L.per + (long long)c.n_groups * L.nM;
+}
+
+// Blocks: (field, group, region layer), then one per group for M.  Work
+// units of a block: the nodes of GJ and of GB (one sum each), and the table
+// cells (t, x) of MB or M (the four sums over a, a' together).  The tables
+// are read as FP64 copies, the per-sample weights come from shared memory,
+// so a sum costs one FP64 fma per sample (1.5 for MB / M).
+__global__ void cv_nodes_kernel(const CvParams c) {
+    __shared__ int s_band[256];
+    __shared__ int s_koff[256];
+    __shared__ double s_wJ[256], s_wB[256], s_wM[256];
+    const NodeLayout L = node_layout(c);
+    const int niR = c.ew1 - c.ew0;
+    const int nTc = c.nT - 1;  // table cells along T
+    const long long nlay = (long long)c.nfields * c.n_groups * niR;
+    const long long b = blockIdx.x;
+    const bool layered = b < nlay;
+    int f = 0, g, w = 0;
+    double *out;
+    if (layered) {
+        const int wR = (int)(b % niR);
+        const long long fg = b / niR;
+        g = (int)(fg % c.n_groups);
+        f = (int)(fg / c.n_groups);
+        w = c.ew0 + wR;
+        out = c.nodes + b * L.per;
+    } else {
+        g = (int)(b - nlay);
+        out = c.nodes + nlay * L.per + (long long)g * L.nM;
+    }
+    // units: [GJ nodes | GB nodes] (layered only), then (t, x) table cells
+    const int nnode = layered ? 2 * L.nTX : 0;
+    const int nunit = nnode + nTc * c.nX;
+    const int q0 = c.grp_start[g], q1 = c.grp_start[g + 1];
+    constexpr int kMaxUnits = 8;
+    double acc[kMaxUnits][4];
+#pragma unroll
+    for (int i = 0; i < kMaxUnits; ++i)
+#pragma unroll
+        for (int r = 0; r < 4; ++r) acc[i][r] = 0.0;
+    for (int qc = q0; qc < q1; qc += 256) {
+        const int nq = min(256, q1 - qc);
+        __syncthreads();
+        if ((int)threadIdx.x < nq) {
+            const int q = qc + threadIdx.x;
+            const int sid = c.samp_id[q];
+            const double C = c.samp_C[q];
+            s_band[threadIdx.x] = (sid / c.nq) * c.nT;
+            s_koff[threadIdx.x] = sid * c.nT * c.nX;
+            if (layered) {
+                const long long o = ((long long)f * c.n_samples + sid) * c.nw + w;
+                const double2 jh = c.Jhat[o];
+                s_wJ[threadIdx.x] = C * jh.x;
+                s_wB[threadIdx.x] = C * jh.y * (double)c.sur[o].y;
+                s_wM[threadIdx.x] = C * jh.y;
+            } else {
+                s_wM[threadIdx.x] = C;
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < kMaxUnits; ++i) {
+            const int u = threadIdx.x + i * blockDim.x;
+            if (u >= nunit) break;
+            if (u < nnode) {  // GJ or GB at node n
+                const bool gb = u >= L.nTX;
+                const int n = gb ? u - L.nTX : u;
+                const double *wv = gb ? s_wB : s_wJ;
+                double sum = acc[i][0];
+                for (int j = 0; j < nq; ++j) sum = fma(wv[j], __ldg(c.ktab_d + s_koff[j] + n), sum);
+                acc[i][0] = sum;
+            } else {  // table cell (t, x): sums over a, a' of k[t+a][x] Ib[t+a']
+                const int m = u - nnode;
+                const int t = m / c.nX, x = m - t * c.nX;
+                double s00 = acc[i][0], s01 = acc[i][1], s10 = acc[i][2], s11 = acc[i][3];
+                for (int j = 0; j < nq; ++j) {
+                    const double *kk = c.ktab_d + s_koff[j] + t * c.nX + x;
+                    const double *ib = c.ibtab_d + s_band[j] + t;
+                    const double k0 = s_wM[j] * __ldg(kk), k1 = s_wM[j] * __ldg(kk + c.nX);
+                    const double i0 = __ldg(ib), i1 = __ldg(ib + 1);
+                    s00 = fma(k0, i0, s00);
+                    s01 = fma(k0, i1, s01);
+                    s10 = fma(k1, i0, s10);
+                    s11 = fma(k1, i1, s11);
+                }
+                acc[i][0] = s00; acc[i][1] = s01; acc[i][2] = s10; acc[i][3] = s11;
+            }
+        }
+    }
+    // layout: GJ [nTX], GB [nTX], then MB / M [t][x][a*2 + a']
+    double *mout = out + (layered ? 2 * L.nTX : 0);
+#pragma unroll
+    for (int i = 0; i < kMaxUnits; ++i) {
+        const int u = threadIdx.x + i * blockDim.x;
+        if (u >= nunit) break;
+        if (u < nnode) {
+            out[u] = acc[i][0];
+        } else {
+            double *o = mout + (long long)(u - nnode) * 4;
+            o[0] = acc[i][0]; o[1] = acc[i][1]; o[2] = acc[i][2]; o[3] = acc[i][3];
+        }
+    }
+}
+
+// E[Y] per (field, cell) from the node sums, all groups.
+__global__ void cv_mean_nodes_kernel(const CvParams c) {
+    const NodeLayout L = node_layout(c);
+    const int njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0, niR = c.ew1 - c.ew0;
+    const long long n = (long long)c.nfields * c.region_cells;
+    const long long plane = (long long)c.na * c.nb;
+    const double *M = c.nodes + (long long)c.nfields * c.n_groups * niR * L.per;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int f = (int)(idx / c.region_cells);
+        const long long tc = idx - (long long)f * c.region_cells;
+        const int jR = (int)(tc % njR);
+        const long long r = tc / njR;
+        const int kR = (int)(r % nkR);
+        const int iR = (int)(r / nkR);
+        const long long cell = (long long)f * c.nw * plane + (long long)(c.ew0 + iR) * plane +
+                               (long long)(c.eb0 + kR) * c.na + (c.ea0 + jR);
+        float T, x = 0.f;
+        if (c.mode == MODE_TX) { const float2 v = c.fieldTX[cell]; T = v.x; x = v.y; }
+        else T = c.fieldT[cell];
+        int ti, xi = 0;
+        float ftf, fxf = 0.f;
+        grid_pos(T, c.T0, c.invdT, c.nT, &ti, &ftf);
+        if (c.mode == MODE_TX) grid_pos(x, c.X0, c.invdX, c.nX, &xi, &fxf);
+        const double ft = ftf, fx = fxf;
+        const double wt[2] = {1.0 - ft, ft};
+        const double wx[2] = {1.0 - fx, fx};
+        const int nb = c.nX > 1 ? 2 : 1;
+        for (int g = 0; g < c.n_groups; ++g) {
+            const double *lay = c.nodes + (((long long)f * c.n_groups + g) * niR + iR) * L.per;
+            const double *GJ = lay, *GB = lay + L.nTX, *MB = lay + 2 * L.nTX;
+            const double *Mg = M + (long long)g * L.nM;
+            double kI = 0.0, kJ = 0.0, kIA = 0.0, kB = 0.0;
+            for (int bx = 0; bx < nb; ++bx) {
+                const int xn = xi + bx;
+                const double *m = Mg + ((long long)ti * c.nX + xn) * 4;
+                const double *mb = MB + ((long long)ti * c.nX + xn) * 4;
+                double sI = 0.0, sIA = 0.0, sJ = 0.0, sB = 0.0;
+                for (int a = 0; a < 2; ++a) {
+                    for (int a2 = 0; a2 < 2; ++a2) {
+                        const double ww = wt[a] * wt[a2];
+                        sI = fma(ww, m[a * 2 + a2], sI);
+                        sIA = fma(ww, mb[a * 2 + a2], sIA);
+                    }
+                    sJ = fma(wt[a], GJ[(ti + a) * c.nX + xn], sJ);
+                    sB = fma(wt[a], GB[(ti + a) * c.nX + xn], sB);
+                }
+                kI = fma(wx[bx], sI, kI);
+                kIA = fma(wx[bx], sIA, kIA);
+                kJ = fma(wx[bx], sJ, kJ);
+                kB = fma(wx[bx], sB, kB);
+            }
+            c.muY[((long long)f * c.n_groups + g) * c.region_cells + tc] = make_double2(kI - kJ, kIA - kB);
+        }
+    }
+}
+
 // One warp per packet: lane l takes the packet's cells l, l + 32, ...
 __global__ void adaptive_rays_kernel(const AdaptParams A) {
     const int lane = threadIdx.x & 31;
@@ -601,7 +793,14 @@ int launch_cv_prepare(const CvParams &c, void *stream) {
 
 int launch_cv_mean(const CvParams &c, void *stream) {
     const long long n = (long long)c.nfields * c.region_cells;
-    cv_mean_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(c);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (c.nodes) {  // tables without particles: node sums, then the cells
+        const long long blocks = (long long)c.nfields * c.n_groups * (c.ew1 - c.ew0) + c.n_groups;
+        cv_nodes_kernel<<<(unsigned)blocks, 256, 0, st>>>(c);
+        cv_mean_nodes_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
+    } else {
+        cv_mean_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
+    }
     return (int)cudaGetLastError();
 }
 

@@ -209,6 +209,9 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             }
             float t = 0.0f;
             int steps = 0;
+            // unrolled by two: the current / next field values alternate
+            // registers instead of being copied every step
+#pragma unroll 2
             for (;;) {
                 int axis;
                 float tn;
