@@ -9,7 +9,8 @@ A step is one full solve of one Q_r field with the inputs resident in HBM,
 timed with CUDA events on the solver's stream: for the default network
 control variate, the network's features, forward pass and ray allocation,
 then the sampling-table upload, the control-variate preparation, the march,
-the finalize kernel and the copy of Q and sigma into pinned host memory.  The
+the finalize kernel (Q and sigma = sqrt(var) on the device) and the copy of
+Q and sigma into pinned host memory.  The
 network is the committed one for the grid (dnsmc_gb300/nets/ck128_g8.cvnet) or,
 when absent, trained before the timed region on 16 snapshots the Monte Carlo
 itself produces.  The ray budget (mean rays per cell and group) is the
@@ -19,8 +20,9 @@ The profile control variate (beta = (1, -1), uniform rays) is timed once at
 its own 1 % budget and plain MC is extrapolated from a pilot, for the
 comparison block.  Inputs (16.8 MB) fit in L2, so L2 is flushed (a 256 MB
 device write) before every timed step.  `e2e` repeats the step through the
-public API from host arrays: dnsmc_set_fields (host->device) + network +
-solve + dnsmc_get_results (device->host), wall clock.
+public API from host arrays: dnsmc_set_fields (host->device, packing and
+the field checks on the device) + network + solve + dnsmc_get_results
+(pinned host memory -> the caller's arrays), wall clock.
 
 With --gpus N (torchrun), every rank solves its own snapshots (seed = rank):
 cells are independent, no collective is needed; the whole-job value is the

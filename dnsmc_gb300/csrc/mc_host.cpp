@@ -376,9 +376,8 @@ struct dnsmc_solver {
     DevBuf<float> d_fieldT;
     DevBuf<float2> d_fieldTX;
     DevBuf<float> d_raw;
-    PinBuf<float> h_stage;
     DevBuf<double> d_stat_part;
-    DevBuf<float> d_stat_out;
+    DevBuf<double> d_stat_out;
 
     // region and rays
     int r_i0 = 0, r_i1 = 0, r_j0 = 0, r_j1 = 0, r_k0 = 0, r_k1 = 0;
@@ -438,8 +437,9 @@ struct dnsmc_solver {
 
     // outputs
     DevBuf<double2> d_tally;
-    DevBuf<double> d_Q, d_var, d_Qg, d_varg;
-    PinBuf<double> h_Q, h_var;
+    DevBuf<double> d_Q, d_var, d_sig, d_Qg, d_varg;
+    PinBuf<double> h_Q, h_sig, h_var;
+    bool keep_var = false;                   // copy the variances to the host too (drop-in solver)
     DevBuf<unsigned int> d_misc;  // [0] queue, [1] status
     DevBuf<unsigned long long> d_counters;
     unsigned long long h_counters[2] = {0, 0};
@@ -1195,12 +1195,14 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     const size_t nout = (size_t)s->nfields * P.region_cells;
     TRY(s->d_Q.ensure(nout));
     TRY(s->d_var.ensure(nout));
+    TRY(s->d_sig.ensure(nout));
     TRY(s->d_Qg.ensure(nout * P.n_groups));
     TRY(s->d_varg.ensure(nout * P.n_groups));
-    F.Q = s->d_Q.p; F.var = s->d_var.p; F.Qg = s->d_Qg.p; F.varg = s->d_varg.p;
+    F.Q = s->d_Q.p; F.var = s->d_var.p; F.sigma = s->d_sig.p; F.Qg = s->d_Qg.p; F.varg = s->d_varg.p;
     F.status = P.status;
     TRY(s->h_Q.ensure(nout));
-    TRY(s->h_var.ensure(nout));
+    TRY(s->h_sig.ensure(nout));
+    if (s->keep_var) TRY(s->h_var.ensure(nout));  // the drop-in scales the variances itself
 
     // ---- the kernel sequence of a solve (stream-ordered; capturable) -------
     auto kernels = [&](bool events) -> int {
@@ -1234,7 +1236,9 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         rc = launch_finalize(F, s->stream);
         if (rc) return fail(DNSMC_ERR_CUDA, "finalize launch: %s", cudaGetErrorString((cudaError_t)rc));
         CUDA_TRY(cudaMemcpyAsync(s->h_Q.p, s->d_Q.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-        CUDA_TRY(cudaMemcpyAsync(s->h_var.p, s->d_var.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(s->h_sig.p, s->d_sig.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        if (s->keep_var)
+            CUDA_TRY(cudaMemcpyAsync(s->h_var.p, s->d_var.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         return DNSMC_OK;
     };
 
@@ -1338,6 +1342,26 @@ int upload_coarse(dnsmc_solver *s, int nfields, Get Tdense) {
     return DNSMC_OK;
 }
 
+// Tmax / Tmin / sum x over the packed resident fields (code/mc_gpu.cu:470-486),
+// on the device; fails (and drops the fields) when a temperature is not
+// positive and finite.
+int field_stats_checked(dnsmc_solver *s, int nfields, bool with_x, double st[4]) {
+    const dnsmc_config &c = s->cfg;
+    const long long ncell = (long long)c.imax * c.jmax * c.kmax;
+    TRY(s->d_stat_part.ensure(field_stats_partials()));
+    TRY(s->d_stat_out.ensure(4));
+    const int rc = launch_field_stats(with_x ? nullptr : s->d_fieldT.p, with_x ? s->d_fieldTX.p : nullptr,
+                                      nfields * ncell, s->d_stat_part.p, s->d_stat_out.p, s->stream);
+    if (rc) return fail(DNSMC_ERR_CUDA, "stats launch: %s", cudaGetErrorString((cudaError_t)rc));
+    CUDA_TRY(cudaMemcpyAsync(st, s->d_stat_out.p, 4 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    if (st[3] > 0.0 || !(st[1] > 0.0) || !std::isfinite(st[0])) {
+        s->nfields = 0;
+        return fail(DNSMC_ERR_ARG, "temperature field has non-positive or non-finite values");
+    }
+    return DNSMC_OK;
+}
+
 int upload_fields_host(dnsmc_solver *s, int nfields, const float *T, const float *x, int layout) {
     const dnsmc_config &c = s->cfg;
     const long long ncell = (long long)c.imax * c.jmax * c.kmax;
@@ -1351,35 +1375,19 @@ int upload_fields_host(dnsmc_solver *s, int nfields, const float *T, const float
     } else {
         return fail(DNSMC_ERR_ARG, "unknown layout %d", layout);
     }
-    // Tmax / Tmin / sum x over interior cells (code/mc_gpu.cu:470-486)
-    float tmax = -1e30f, tmin = 1e30f;
-    double xs = 0.0;
-    bool bad = false;
-    for (int f = 0; f < nfields; ++f)
-        for (int k = 0; k < c.kmax; ++k)
-            for (int j = 0; j < c.jmax; ++j) {
-                const long long o = f * nsrc + base + j * sj + k * sk;
-                for (int i = 0; i < c.imax; ++i) {
-                    const float v = T[o + i];
-                    if (!(v > 0.0f) || !std::isfinite(v)) bad = true;
-                    tmax = std::max(tmax, v);
-                    tmin = std::min(tmin, v);
-                    if (x) xs += x[o + i];
-                }
-            }
-    if (bad) return fail(DNSMC_ERR_ARG, "temperature field has non-positive or non-finite values");
     TRY(set_device(s));
     TRY(wait_done(s, 0));
     const bool want_x = (x != nullptr);
-    TRY(s->h_stage.ensure((size_t)nsrc * (want_x ? 2 : 1)));
     TRY(s->d_raw.ensure((size_t)nsrc * (want_x ? 2 : 1)));
     if (want_x) TRY(s->d_fieldTX.ensure((size_t)nfields * ncell));
     else TRY(s->d_fieldT.ensure((size_t)nfields * ncell));
+    // each snapshot straight from the caller's arrays into the raw buffer
+    // (stream order serialises the buffer's reuse), then packed on the device
     for (int f = 0; f < nfields; ++f) {
-        CUDA_TRY(cudaStreamSynchronize(s->stream));  // staging reuse
-        memcpy(s->h_stage.p, T + f * nsrc, nsrc * sizeof(float));
-        if (want_x) memcpy(s->h_stage.p + nsrc, x + f * nsrc, nsrc * sizeof(float));
-        CUDA_TRY(cudaMemcpyAsync(s->d_raw.p, s->h_stage.p, nsrc * (want_x ? 2 : 1) * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(s->d_raw.p, T + f * nsrc, nsrc * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        if (want_x)
+            CUDA_TRY(cudaMemcpyAsync(s->d_raw.p + nsrc, x + f * nsrc, nsrc * sizeof(float), cudaMemcpyHostToDevice,
+                                     s->stream));
         int rc;
         if (want_x)
             rc = launch_pack_TX(s->d_raw.p, s->d_raw.p + nsrc, s->d_fieldTX.p + f * ncell, c.imax, c.jmax, c.kmax, si, sj, sk, base, s->stream);
@@ -1387,7 +1395,8 @@ int upload_fields_host(dnsmc_solver *s, int nfields, const float *T, const float
             rc = launch_pack_T(s->d_raw.p, s->d_fieldT.p + f * ncell, c.imax, c.jmax, c.kmax, si, sj, sk, base, s->stream);
         if (rc) return fail(DNSMC_ERR_CUDA, "pack launch: %s", cudaGetErrorString((cudaError_t)rc));
     }
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
+    double st[4];
+    TRY(field_stats_checked(s, nfields, want_x, st));
     if (c.grid_num > 1) {
         std::vector<float> dense;
         TRY(upload_coarse(s, nfields, [&](int f) -> const float * {
@@ -1402,9 +1411,9 @@ int upload_fields_host(dnsmc_solver *s, int nfields, const float *T, const float
     }
     s->nfields = nfields;
     s->have_x = want_x;
-    s->tmax_fields = tmax;
-    s->tmin_fields = tmin;
-    s->xsum = xs;
+    s->tmax_fields = (float)st[0];
+    s->tmin_fields = (float)st[1];
+    s->xsum = st[2];
     return DNSMC_OK;
 }
 
@@ -1587,13 +1596,13 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_slab.release(); s->d_posT.release(); s->d_posTX.release();
     s->d_cv_grp.release(); s->d_cv_sid.release(); s->d_cv_C.release(); s->d_layer.release();
     s->d_sur.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_cvnodes.release(); s->d_kd.release(); s->d_ibd.release(); s->d_beta.release(); s->d_moments.release();
-    s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release(); s->h_stage.release();
+    s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release();
     s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_item_steps.release(); s->d_kP.release();
     s->d_order.release(); s->d_order_hist.release();
     s->d_mgT.release(); s->d_mgfw.release();
     s->d_part.release(); s->d_fieldV.release(); s->d_layerV.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
-    s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_Qg.release(); s->d_varg.release();
+    s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_sig.release(); s->h_sig.release(); s->d_Qg.release(); s->d_varg.release();
     s->h_Q.release(); s->h_var.release(); s->d_misc.release(); s->d_counters.release();
     if (s->ev_march0) cudaEventDestroy(s->ev_march0);
     if (s->ev_march1) cudaEventDestroy(s->ev_march1);
@@ -1725,14 +1734,8 @@ int dnsmc_set_fields_device(dnsmc_solver *s, int nfields, const float *dT, const
             rc = launch_pack_T(dT + f * ncell, s->d_fieldT.p + f * ncell, c.imax, c.jmax, c.kmax, 1, c.imax, (long long)c.imax * c.jmax, 0, s->stream);
         if (rc) return fail(DNSMC_ERR_CUDA, "pack launch: %s", cudaGetErrorString((cudaError_t)rc));
     }
-    TRY(s->d_stat_part.ensure(field_stats_partials()));
-    TRY(s->d_stat_out.ensure(4));
-    int rc = launch_field_stats(dx ? nullptr : s->d_fieldT.p, dx ? s->d_fieldTX.p : nullptr, nfields * ncell, s->d_stat_part.p, s->d_stat_out.p, s->stream);
-    if (rc) return fail(DNSMC_ERR_CUDA, "stats launch: %s", cudaGetErrorString((cudaError_t)rc));
-    float st[3];
-    CUDA_TRY(cudaMemcpyAsync(st, s->d_stat_out.p, sizeof st, cudaMemcpyDeviceToHost, s->stream));
-    CUDA_TRY(cudaStreamSynchronize(s->stream));
-    if (!(st[1] > 0) || !std::isfinite(st[0])) return fail(DNSMC_ERR_ARG, "temperature field has non-positive or non-finite values");
+    double st[4];
+    TRY(field_stats_checked(s, nfields, dx != nullptr, st));
     if (c.grid_num > 1) {  // the spline coarsening runs on the host
         std::vector<float> h((size_t)ncell);
         TRY(upload_coarse(s, nfields, [&](int f) -> const float * {
@@ -1742,8 +1745,8 @@ int dnsmc_set_fields_device(dnsmc_solver *s, int nfields, const float *dT, const
     }
     s->nfields = nfields;
     s->have_x = dx != nullptr;
-    s->tmax_fields = st[0];
-    s->tmin_fields = st[1];
+    s->tmax_fields = (float)st[0];
+    s->tmin_fields = (float)st[1];
     s->xsum = st[2];
     return DNSMC_OK;
 }
@@ -1808,13 +1811,10 @@ int dnsmc_set_particle_field(dnsmc_solver *s, const float *fv, int layout) {
             }
     TRY(set_device(s));
     TRY(wait_done(s, 0));
-    TRY(s->h_stage.ensure((size_t)nsrc));
     TRY(s->d_raw.ensure((size_t)nsrc));
     TRY(s->d_fieldV.ensure((size_t)s->nfields * ncell));
     for (int f = 0; f < s->nfields; ++f) {
-        CUDA_TRY(cudaStreamSynchronize(s->stream));  // staging reuse
-        memcpy(s->h_stage.p, fv + f * nsrc, nsrc * sizeof(float));
-        CUDA_TRY(cudaMemcpyAsync(s->d_raw.p, s->h_stage.p, nsrc * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        CUDA_TRY(cudaMemcpyAsync(s->d_raw.p, fv + f * nsrc, nsrc * sizeof(float), cudaMemcpyHostToDevice, s->stream));
         const int rc = launch_pack_T(s->d_raw.p, s->d_fieldV.p + f * ncell, c.imax, c.jmax, c.kmax, 1, sj, sk, base,
                                      s->stream);
         if (rc) return fail(DNSMC_ERR_CUDA, "pack launch: %s", cudaGetErrorString((cudaError_t)rc));
@@ -2060,14 +2060,31 @@ int dnsmc_wait(dnsmc_solver *s, double timeout_s) {
     return wait_done(s, timeout_s);
 }
 
+// Host copy of a large result array on several threads: the caller's array
+// is often freshly allocated, and its first-touch page faults dominate a
+// single-threaded copy.
+static void parallel_copy(void *dst, const void *src, size_t bytes) {
+    const size_t chunk = (size_t)2 << 20;
+    const unsigned nt = (unsigned)std::min<size_t>(8, (bytes + chunk - 1) / chunk);
+    if (nt <= 1) { memcpy(dst, src, bytes); return; }
+    std::vector<std::thread> th;
+    const size_t per = (bytes / nt + 4095) & ~(size_t)4095;
+    for (unsigned t = 0; t < nt; ++t) {
+        const size_t o = (size_t)t * per;
+        if (o >= bytes) break;
+        const size_t len = std::min(per, bytes - o);
+        th.emplace_back([=] { memcpy((char *)dst + o, (const char *)src + o, len); });
+    }
+    for (auto &x : th) x.join();
+}
+
 int dnsmc_get_results(dnsmc_solver *s, double *Q, double *sigma) {
     if (!s) return fail(DNSMC_ERR_ARG, "null solver");
     if (!s->solved) return fail(DNSMC_ERR_STATE, "no solve has been run");
     TRY(wait_done(s, 0));
     const size_t n = (size_t)s->nfields * s->last.region_cells;
-    if (Q) memcpy(Q, s->h_Q.p, n * sizeof(double));
-    if (sigma)
-        for (size_t i = 0; i < n; ++i) sigma[i] = sqrt(s->h_var.p[i]);
+    if (Q) parallel_copy(Q, s->h_Q.p, n * sizeof(double));
+    if (sigma) parallel_copy(sigma, s->h_sig.p, n * sizeof(double));
     return DNSMC_OK;
 }
 
@@ -2307,6 +2324,7 @@ void mc_gpu_(float *Tfort, int *ystart) {
             if (dnsmc_config_from_env(&c)) dropin_die("mc_gpu_ configuration");
         }
         if (dnsmc_create(&c, &g_dropin)) dropin_die("mc_gpu_ set-up");
+        g_dropin->keep_var = true;  // get_results_ scales the variances itself
         std::string dir = g_dropin_tables;
         if (dir.empty()) { const char *e = getenv("DNSMC_TABLES"); dir = e && *e ? e : "../distr/tables"; }
         int rc = DNSMC_OK;

@@ -130,6 +130,7 @@ struct FinalizeParams {
     const float2 *beta;       // (beta_a, beta_b), tally layout, or null: (1, -1)
     double *Q;                // [f][cell] dense region, i fastest
     double *var;              // [f][cell]
+    double *sigma;            // [f][cell]: sqrt(var)
     double *Qg;               // [f][group][cell] or nullptr
     double *varg;             // [f][group][cell] or nullptr
     unsigned int *status;
@@ -228,9 +229,10 @@ int launch_pack_T(const float *src, float *dst, int nw, int na, int nb,
 int launch_pack_TX(const float *srcT, const float *srcX, float2 *dst, int nw,
                    int na, int nb, long long si, long long sj, long long sk,
                    long long base, void *stream);
-// max T, min T, sum x over n cells into out[0..2] (device), deterministic
+// max T, min T, sum x and the count of non-positive or non-finite T over n
+// cells into out[0..3] (device), deterministic
 int launch_field_stats(const float *fT, const float2 *fTX, long long n,
-                       double *partials, float *out, void *stream);
+                       double *partials, double *out, void *stream);
 int field_stats_partials();   // doubles needed in `partials`
 int march_occupancy(int mode, int threads);  // resident blocks per SM
 

@@ -118,6 +118,7 @@ __global__ void finalize_kernel(const FinalizeParams F) {
         }
         F.Q[idx] = Q;
         F.var[idx] = V;
+        if (F.sigma) F.sigma[idx] = sqrt(V);
     }
 }
 
@@ -153,36 +154,41 @@ __global__ void pack_TX_kernel(const float *srcT, const float *srcX, float2 *dst
 // Deterministic two-pass reduction: max T, min T, sum x (fixed block count,
 // fixed order), used when fields arrive as device pointers.
 constexpr int kStatBlocks = 256, kStatThreads = 256;
+// Tmax, Tmin, sum of x and the count of temperatures that are not positive
+// and finite, over n cells; two passes in a fixed order (deterministic).
 __global__ void field_stats_pass1(const float *fT, const float2 *fTX, long long n, double *part) {
-    __shared__ double smax[kStatThreads], smin[kStatThreads], ssum[kStatThreads];
-    double mx = -1e300, mn = 1e300, sm = 0.0;
+    __shared__ double smax[kStatThreads], smin[kStatThreads], ssum[kStatThreads], sbad[kStatThreads];
+    double mx = -1e300, mn = 1e300, sm = 0.0, bad = 0.0;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         float T, x = 0.f;
         if (fTX) { const float2 v = fTX[i]; T = v.x; x = v.y; } else { T = fT[i]; }
+        if (!(T > 0.0f) || !isfinite(T)) bad += 1.0;
         mx = fmax(mx, (double)T); mn = fmin(mn, (double)T); sm += x;
     }
-    smax[threadIdx.x] = mx; smin[threadIdx.x] = mn; ssum[threadIdx.x] = sm;
+    smax[threadIdx.x] = mx; smin[threadIdx.x] = mn; ssum[threadIdx.x] = sm; sbad[threadIdx.x] = bad;
     __syncthreads();
     for (int o = blockDim.x / 2; o > 0; o >>= 1) {
         if (threadIdx.x < o) {
             smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
             smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
             ssum[threadIdx.x] += ssum[threadIdx.x + o];
+            sbad[threadIdx.x] += sbad[threadIdx.x + o];
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        part[3 * blockIdx.x] = smax[0]; part[3 * blockIdx.x + 1] = smin[0]; part[3 * blockIdx.x + 2] = ssum[0];
+        double *p = part + 4 * blockIdx.x;
+        p[0] = smax[0]; p[1] = smin[0]; p[2] = ssum[0]; p[3] = sbad[0];
     }
 }
-__global__ void field_stats_pass2(const double *part, int nparts, float *out) {
+__global__ void field_stats_pass2(const double *part, int nparts, double *out) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double mx = -1e300, mn = 1e300, sm = 0.0;
+    double mx = -1e300, mn = 1e300, sm = 0.0, bad = 0.0;
     for (int i = 0; i < nparts; ++i) {
-        mx = fmax(mx, part[3 * i]); mn = fmin(mn, part[3 * i + 1]); sm += part[3 * i + 2];
+        mx = fmax(mx, part[4 * i]); mn = fmin(mn, part[4 * i + 1]); sm += part[4 * i + 2]; bad += part[4 * i + 3];
     }
-    out[0] = (float)mx; out[1] = (float)mn; out[2] = (float)sm;
+    out[0] = mx; out[1] = mn; out[2] = sm; out[3] = bad;
 }
 
 // ---------------------------------------------------------------------------
@@ -833,7 +839,7 @@ int launch_pack_TX(const float *srcT, const float *srcX, float2 *dst, int nw, in
     return (int)cudaGetLastError();
 }
 
-int launch_field_stats(const float *fT, const float2 *fTX, long long n, double *partials, float *out,
+int launch_field_stats(const float *fT, const float2 *fTX, long long n, double *partials, double *out,
                        void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     field_stats_pass1<<<kStatBlocks, kStatThreads, 0, st>>>(fT, fTX, n, partials);
@@ -841,7 +847,7 @@ int launch_field_stats(const float *fT, const float2 *fTX, long long n, double *
     return (int)cudaGetLastError();
 }
 
-int field_stats_partials() { return 3 * kStatBlocks; }
+int field_stats_partials() { return 4 * kStatBlocks; }
 
 int upload_sobol_dirs(const uint32_t dirs[4][32]) {
     int rc = (int)cudaMemcpyToSymbol(c_sobol, dirs, sizeof(uint32_t) * 4 * 32);
