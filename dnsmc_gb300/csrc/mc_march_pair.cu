@@ -193,7 +193,15 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             // warp-uniform DDA from the cell centres
             const float invW = 1.0f / fabsf(sW), invA = 1.0f / fabsf(sA), invB = 1.0f / fabsf(sB);
             const int dW = sW > 0.f ? 1 : -1, dA = sA > 0.f ? 1 : -1, dB = sB > 0.f ? 1 : -1;
-            float tW = (dW > 0 ? (__ldg(P.fw + w0 + 1) - oW) : (oW - __ldg(P.fw + w0))) * invW;
+            // crossing parameter of the next wall-normal face: (fw[c + 1] - o) / s
+            // going up, (o - fw[c]) / |s| = (fw[c] - o) * (-1/|s|) going down
+            // (negation is exact: the same values)
+            const float *fwn = P.fw + (dW > 0 ? 1 : 0);
+            const float sinvW = dW > 0 ? invW : -invW;
+            float tW = (__ldg(fwn + w0) - oW) * sinvW;
+            // periodic wrap of the next j / k index: one compare per step
+            const int wrapA = dA > 0 ? P.na : -1, resetA = dA > 0 ? 0 : P.na - 1;
+            const int wrapB = dB > 0 ? P.nb : -1, resetB = dB > 0 ? 0 : P.nb - 1;
             const float dtA = P.da * invA, dtB = P.db * invB;
             float tA = 0.5f * dtA, tB = 0.5f * dtB;
             int nA = 0, nB = 0;
@@ -231,12 +239,12 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     nrowW = ncw * plane;
                 } else if (axis == 1) {
                     nca = ca + dA;
-                    if (nca == P.na) nca = 0; else if (nca < 0) nca = P.na - 1;
+                    if (nca == wrapA) nca = resetA;
                 } else {
 #pragma unroll
                     for (int k = 0; k < C; ++k) {
                         ncb[k] = cb[k] + dB;
-                        if (ncb[k] == P.nb) ncb[k] = 0; else if (ncb[k] < 0) ncb[k] = P.nb - 1;
+                        if (ncb[k] == wrapB) ncb[k] = resetB;
                         nrowB[k] = ncb[k] * P.na;
                     }
                 }
@@ -290,7 +298,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     }
                     cw = ncw;
                     rowW = nrowW;
-                    tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - oW) : (oW - __ldg(P.fw + cw))) * invW;
+                    tW = (__ldg(fwn + cw) - oW) * sinvW;
                 } else if (axis == 1) {
                     ++nA;
                     tA = ((float)nA + 0.5f) * dtA;
