@@ -498,7 +498,8 @@ int check_config(const dnsmc_config &c) {
     if (!(c.Lx > 0) || !(c.Ly > 0) || !(c.Lz > 0)) return fail(DNSMC_ERR_ARG, "Lx, Ly, Lz must be > 0");
     if (c.nvar < 1 || c.photmax < 1) return fail(DNSMC_ERR_ARG, "nvar and photmax must be >= 1");
     if (!(c.toll > 0) || c.toll >= 1) return fail(DNSMC_ERR_ARG, "toll must be in (0,1)");
-    if (c.max_steps < 1) return fail(DNSMC_ERR_ARG, "max_steps must be >= 1");
+    // the march counts crossings in FP32 (exact below 2^22 per axis)
+    if (c.max_steps < 1 || c.max_steps > (1 << 22)) return fail(DNSMC_ERR_ARG, "max_steps must be in [1, 4194304]");
     if (c.grid_num < 1 || c.grid_num > kMaxLevels) return fail(DNSMC_ERR_ARG, "grid_num must be 1..%d", kMaxLevels);
     if (c.grid_num > 1) {
         const int r = 1 << (c.grid_num - 1);

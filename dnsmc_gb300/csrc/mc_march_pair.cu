@@ -202,9 +202,14 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             // periodic wrap of the next j / k index: one compare per step
             const int wrapA = dA > 0 ? P.na : -1, resetA = dA > 0 ? 0 : P.na - 1;
             const int wrapB = dB > 0 ? P.nb : -1, resetB = dB > 0 ? 0 : P.nb - 1;
+            const int wallW = dW > 0 ? P.nw : -1;  // the wall-normal index beyond the wall
             const float dtA = P.da * invA, dtB = P.db * invB;
             float tA = 0.5f * dtA, tB = 0.5f * dtB;
-            int nA = 0, nB = 0;
+            // crossing counts plus one half, as floats: (float)n + 0.5f is
+            // exact and so is adding 1 to it below 2^22 crossings, so these
+            // are the values the integer counts would give, without a
+            // conversion per step
+            float hA = 0.5f, hB = 0.5f;
             int cw = w0, ca = acl, rowW = rowW0;
             int cb[C], rowB[C];
             float tau[C], D[C];
@@ -235,7 +240,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 bool wall = false;
                 if (axis == 0) {
                     ncw = cw + dW;
-                    wall = ncw < 0 || ncw >= P.nw;
+                    wall = ncw == wallW;
                     nrowW = ncw * plane;
                 } else if (axis == 1) {
                     nca = ca + dA;
@@ -280,7 +285,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 }
                 if (TRACE && lane == 0 && steps < P.trace_max) {
                     int *rec = P.trace_rec + 6 * steps;
-                    rec[0] = cw; rec[1] = dA * nA; rec[2] = dB * nB; rec[3] = axis;
+                    rec[0] = cw; rec[1] = dA * (int)(hA - 0.5f); rec[2] = dB * (int)(hB - 0.5f); rec[3] = axis;
                     rec[4] = __float_as_int(ds); rec[5] = __float_as_int(tau[0]);
                 }
                 t = tn;
@@ -300,12 +305,12 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     rowW = nrowW;
                     tW = (__ldg(fwn + cw) - oW) * sinvW;
                 } else if (axis == 1) {
-                    ++nA;
-                    tA = ((float)nA + 0.5f) * dtA;
+                    hA = hA + 1.0f;
+                    tA = hA * dtA;
                     ca = nca;
                 } else {
-                    ++nB;
-                    tB = ((float)nB + 0.5f) * dtB;
+                    hB = hB + 1.0f;
+                    tB = hB * dtB;
 #pragma unroll
                     for (int k = 0; k < C; ++k) { cb[k] = ncb[k]; rowB[k] = nrowB[k]; }
                 }

@@ -92,7 +92,7 @@ typedef struct dnsmc_config {
     float eps_west, eps_east;    /* wall emissivity, 1 = black (bdw=bde=2)      */
     /* march (code/param.h:72, :25-37) */
     float toll;                  /* transmissivity cut-off                      */
-    int   max_steps;             /* per-ray step cap                             */
+    int   max_steps;             /* per-ray step cap, 1 .. 4194304               */
     int   grid_num;              /* multigrid levels (code/param.h:18-37): rays  */
                                  /* march mg_steps steps on each grid, then    */
                                  /* continue on the next grid, 2x coarser per  */
