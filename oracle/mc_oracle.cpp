@@ -582,10 +582,13 @@ inline float p_expm1(float x) {
     const float n = rintf(x * 1.44269504088896341f);
     float r = fmaf(-n, 0.693145751953125f, x);
     r = fmaf(-n, 1.42860682030941723212e-6f, r);
-    const float cf[8] = {2.48015873015873016e-5f, 1.98412698412698413e-4f, 1.38888888888888889e-3f,
-                         8.33333333333333333e-3f, 4.16666666666666667e-2f, 1.66666666666666667e-1f, 0.5f, 1.0f};
-    float p = cf[0];
-    for (int i = 1; i < 8; ++i) p = fmaf(p, r, cf[i]);
+    // expm1(r) = r (1 + r g(r)), g the degree-4 minimax polynomial of
+    // (e^r - 1 - r)/r^2 on [-ln2/2, ln2/2] (the march's mc_expm1)
+    const float cf[5] = {1.39411131385713816e-3f, 8.36317520588636398e-3f, 4.16663736104965210e-2f,
+                         1.66665762662887573e-1f, 0.5f};
+    float q = cf[0];
+    for (int i = 1; i < 5; ++i) q = fmaf(q, r, cf[i]);
+    float p = fmaf(q, r, 1.0f);
     p = p * r;
     const int ni = (int)n;
     uint32_t bits = (uint32_t)(ni + 127) << 23;
