@@ -203,6 +203,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             const int wrapA = dA > 0 ? P.na : -1, resetA = dA > 0 ? 0 : P.na - 1;
             const int wrapB = dB > 0 ? P.nb : -1, resetB = dB > 0 ? 0 : P.nb - 1;
             const int wallW = dW > 0 ? P.nw : -1;  // the wall-normal index beyond the wall
+            const int dRowW = dW * plane;
             const float dtA = P.da * invA, dtB = P.db * invB;
             float tA = 0.5f * dtA, tB = 0.5f * dtB;
             // crossing counts plus one half, as floats: (float)n + 0.5f is
@@ -226,33 +227,33 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             // registers instead of being copied every step
 #pragma unroll 2
             for (;;) {
-                int axis;
-                float tn;
-                if (tW <= tA && tW <= tB) { axis = 0; tn = tW; }
-                else if (tA <= tB)         { axis = 1; tn = tA; }
-                else                       { axis = 2; tn = tB; }
+                const bool sW_ = tW <= tA && tW <= tB;
+                const bool sA_ = !sW_ && tA <= tB;
+                const int axis = sW_ ? 0 : (sA_ ? 1 : 2);
+                const float tn = sW_ ? tW : (sA_ ? tA : tB);
                 const float ds = tn - t;
-                // next cell of the walk, and its field values fetched now
-                int ncw = cw, nca = ca, nrowW = rowW;
+                // next cell of the walk, and its field values fetched now; the
+                // axis is the same in every lane, but selects cost fewer
+                // instructions here than branches the compiler must treat as
+                // divergent
+                int ncw, nca, nrowW;
                 int ncb[C], nrowB[C];
-#pragma unroll
-                for (int k = 0; k < C; ++k) { ncb[k] = cb[k]; nrowB[k] = rowB[k]; }
-                bool wall = false;
-                if (axis == 0) {
-                    ncw = cw + dW;
-                    wall = ncw == wallW;
-                    nrowW = ncw * plane;
-                } else if (axis == 1) {
-                    nca = ca + dA;
-                    if (nca == wrapA) nca = resetA;
-                } else {
-#pragma unroll
-                    for (int k = 0; k < C; ++k) {
-                        ncb[k] = cb[k] + dB;
-                        if (ncb[k] == wrapB) ncb[k] = resetB;
-                        nrowB[k] = ncb[k] * P.na;
-                    }
+                const bool aW = axis == 0, aA = axis == 1, aB = axis == 2;
+                ncw = aW ? cw + dW : cw;
+                nrowW = aW ? rowW + dRowW : rowW;
+                {
+                    int u = ca + dA;
+                    u = u == wrapA ? resetA : u;
+                    nca = aA ? u : ca;
                 }
+#pragma unroll
+                for (int k = 0; k < C; ++k) {
+                    int u = cb[k] + dB;
+                    u = u == wrapB ? resetB : u;
+                    ncb[k] = aB ? u : cb[k];
+                    nrowB[k] = aB ? u * P.na : rowB[k];
+                }
+                const bool wall = aW && ncw == wallW;
                 VT vnext[C];
 #pragma unroll
                 for (int k = 0; k < C; ++k) {
@@ -290,7 +291,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 }
                 t = tn;
                 ++steps;
-                if (axis == 0) {
+                {
                     if (wall) {
                         const int side = ncw < 0 ? 0 : 1;
                         const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
@@ -303,13 +304,11 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     }
                     cw = ncw;
                     rowW = nrowW;
-                    tW = (__ldg(fwn + cw) - oW) * sinvW;
-                } else if (axis == 1) {
-                    hA = hA + 1.0f;
+                    if (aW) tW = (__ldg(fwn + cw) - oW) * sinvW;
+                    hA = aA ? hA + 1.0f : hA;
                     tA = hA * dtA;
                     ca = nca;
-                } else {
-                    hB = hB + 1.0f;
+                    hB = aB ? hB + 1.0f : hB;
                     tB = hB * dtB;
 #pragma unroll
                     for (int k = 0; k < C; ++k) { cb[k] = ncb[k]; rowB[k] = nrowB[k]; }
