@@ -235,28 +235,37 @@ __device__ __forceinline__ void surrogate_walk(const MarchParams &P, const float
                                                int nbnd, float *Jbar_out, float *tex_out) {
     const float invW = 1.0f / fabsf(sW);
     const int dW = sW > 0.f ? 1 : -1;
+    // exit face of layer l at parameter (fw[l + 1] - o)/s going up and
+    // (fw[l] - o) * (-1/|s|) going down (the same values as (o - fw[l])/|s|)
+    const float *fwn = P.fw + (dW > 0 ? 1 : 0);
+    const float sinvW = dW > 0 ? invW : -invW;
+    const int lwall = dW > 0 ? P.nw : -1;
     float Jbar = 0.0f, tauE = 1.0f, tE = 0.0f, dcum = 0.0f, tex0 = -1.0f;
     int l = w0;
     float2 kv = __ldg(surp + w0);
+    bool trunc;
     for (;;) {
-        const float tn = (dW > 0 ? (__ldg(P.fw + l + 1) - oW) : (oW - __ldg(P.fw + l))) * invW;
+        const float tn = (__ldg(fwn + l) - oW) * sinvW;
         const float opt = kv.x * (tn - tE);
-        if (dcum + opt > P.dtoll) { Jbar = fmaf(tauE, kv.y, Jbar); break; }  // truncated in layer l
+        trunc = dcum + opt > P.dtoll;
+        if (trunc) break;  // truncated in layer l
         const float as = -mc_expm1(-opt);
         const float tas = tauE * as;
         Jbar = fmaf(tas, kv.y, Jbar);
         tauE = tauE - tas;
         dcum = dcum + opt;
         tE = tn;
-        if (tex0 < 0.0f) tex0 = tauE;
+        tex0 = tex0 < 0.0f ? tauE : tex0;
         l += dW;
-        if (l < 0 || l >= P.nw) {
-            const int side = l < 0 ? 0 : 1;
-            const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
-            Jbar = fmaf(tauE, Iw, Jbar);
-            break;
-        }
+        if (l == lwall) break;  // reached the wall
         kv = __ldg(surp + l);
+    }
+    if (trunc) {
+        Jbar = fmaf(tauE, kv.y, Jbar);
+    } else {
+        const int side = dW > 0 ? 1 : 0;
+        const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
+        Jbar = fmaf(tauE, Iw, Jbar);
     }
     *Jbar_out = Jbar;
     *tex_out = tex0 < 0.0f ? 0.0f : tex0;
