@@ -95,8 +95,11 @@ static __constant__ uint32_t c_sobol[4][32];  // one copy per translation unit
 
 __device__ __forceinline__ uint4 sobol4(uint32_t m) {
     uint32_t a = 0, b = 0, c = 0, d = 0;
-    for (int k = 0; m; ++k, m >>= 1)
-        if (m & 1u) { a ^= c_sobol[0][k]; b ^= c_sobol[1][k]; c ^= c_sobol[2][k]; d ^= c_sobol[3][k]; }
+    while (m) {  // one pass per set bit of m
+        const int k = __ffs(m) - 1;
+        a ^= c_sobol[0][k]; b ^= c_sobol[1][k]; c ^= c_sobol[2][k]; d ^= c_sobol[3][k];
+        m &= m - 1u;
+    }
     return make_uint4(a, b, c, d);
 }
 

@@ -447,3 +447,33 @@ def test_bitexact_rqmc_local_bins_and_trace():
         np.testing.assert_array_equal(rng, rng2)
         np.testing.assert_array_equal(rec, rec2)
     s.close()
+
+
+def test_fields_checked_on_the_device():
+    """Temperatures that are not positive and finite are rejected (host and
+    device inputs, checked by the device statistics pass); the solver then
+    holds no fields, so a solve fails instead of using them."""
+    import torch
+    ni, nj, nk = 8, 32, 4
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=300, T_east=300, seed=2))
+    T = smooth_field(ni, nj, nk, 400, 1200, 3)
+    s.set_fields(T)
+    s.set_rays(4)
+    s.solve(timeout_s=60)
+    assert s.tmax() == float(T.max())
+    for bad in (np.nan, -5.0, np.inf, 0.0):
+        Tb = T.copy()
+        Tb[1, 7, 3] = bad
+        with pytest.raises(D.DnsmcError) as e:
+            s.set_fields(Tb)
+        assert e.value.code == _lib.ERR_ARG
+        with pytest.raises(D.DnsmcError):
+            s.solve(timeout_s=60)
+        dT = torch.from_numpy(Tb).cuda().contiguous()
+        with pytest.raises(D.DnsmcError):
+            _lib.check(s._lib.dnsmc_set_fields_device(s._h, 1, ctypes.c_void_p(dT.data_ptr()), None))
+    s.set_fields(T)
+    Q, _ = s.solve(timeout_s=60)
+    assert np.isfinite(Q).all()
+    s.close()
