@@ -275,6 +275,75 @@ __device__ __forceinline__ void surrogate_walk(const MarchParams &P, const float
 }
 
 // ---------------------------------------------------------------------------
+// Pieces shared by the marches (mc_march.cuh's one-cell kernel and
+// mc_march_pair.cu's two-cell kernel): the words of a packet-ray, its
+// direction, the copy of its spectral sample's table slab, one ray's tally.
+// ---------------------------------------------------------------------------
+
+// The ray's four uniform words.  RQMC: point m of replicate b = r / M of a
+// Sobol' net, XOR-shifted by the replicate's Philox word (kept in *shift and
+// recomputed when the replicate changes, *bcur); iid: one Philox call.
+__device__ __forceinline__ uint4 ray_words(const MarchParams &P, int r, int M, int p, uint32_t ctr2, int *bcur,
+                                          uint4 *shift, int *m_out) {
+    if (P.sampler) {
+        const int b = r / M;
+        const int m = r - b * M;
+        if (b != *bcur) {
+            *shift = philox4x32_10(make_uint4((uint32_t)b, (uint32_t)p, ctr2, 0x50B01u), P.key0, P.key1);
+            *bcur = b;
+        }
+        const uint4 sh = *shift;
+        const uint4 sb = sobol4((uint32_t)m);
+        *m_out = m;
+        return make_uint4(sb.x ^ sh.x, sb.y ^ sh.y, sb.z ^ sh.z, sb.w ^ sh.w);
+    }
+    *m_out = 0;
+    return philox4x32_10(make_uint4((uint32_t)r, (uint32_t)p, ctr2, 0u), P.key0, P.key1);
+}
+
+// Isotropic direction (the reference's emiss_ang, code/mc_gpu.cu:813-820):
+// cos(theta) = 1 - 2u from the top 24 bits of x.y, phi = 2 pi u' from x.x.
+__device__ __forceinline__ void ray_direction(uint4 x, float *sW, float *sA, float *sB) {
+    const float mu = fmaf((float)(x.y >> 8), -1.1920928955078125e-7f, 1.0f);
+    const float st = sqrtf(fmaxf(0.0f, fmaf(-mu, mu, 1.0f)));
+    float cph, sph;
+    mc_sincos_turn(x.x >> 8, &cph, &sph);
+    *sW = mu;
+    *sA = st * cph;
+    *sB = st * sph;
+}
+
+// The sample's slab (k, then Ib of its band) into this warp's shared copy;
+// the previous ray's lookups are done first.
+__device__ __forceinline__ void load_slab(const MarchParams &P, int sid, float2 *slk, int lane) {
+    __syncwarp();
+    const float4 *src = reinterpret_cast<const float4 *>(P.slab + (long long)sid * P.slab_len);
+    float4 *dst = reinterpret_cast<float4 *>(slk);
+    for (int q = lane; q < (P.slab_len >> 1); q += 32) dst[q] = __ldg(src + q);
+    __syncwarp();
+}
+
+// One ray of a cell into its FP64 sums: the sum, and the sum of squares
+// (iid) or of the squared replicate means (RQMC: *rep holds the running
+// replicate sum, m the ray's index in its replicate of M rays).
+__device__ __forceinline__ void tally_ray(const MarchParams &P, double Xd, int m, int M, double *sum, double *sq,
+                                          double *rep) {
+    *sum += Xd;
+    if (P.sampler) {
+        const double Sb = *rep + Xd;
+        if (m == M - 1) {  // end of a replicate: accumulate its mean squared
+            const double mb = Sb / M;
+            *sq = fma(mb, mb, *sq);
+            *rep = 0.0;
+        } else {
+            *rep = Sb;
+        }
+    } else {
+        *sq = fma(Xd, Xd, *sq);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // The march kernel.  Persistent: every warp pulls work items (field, band
 // group, packet) from an atomic counter until the queue is empty.  The next
 // cell's field value is loaded one step ahead of its use.
@@ -400,30 +469,13 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
         const int rbeg = TRACE ? P.trace_r : 0;
         const int rend = TRACE ? P.trace_r + 1 : ((K > 0) ? N : 0);
         for (int r = rbeg; r < rend; ++r) {
-            uint4 x;
-            int m = 0;
-            if (P.sampler) {
-                const int b = r / M;
-                m = r - b * M;
-                if (b != bcur) {
-                    s_shift[tid] = philox4x32_10(make_uint4((uint32_t)b, (uint32_t)p, ctr2, 0x50B01u), P.key0, P.key1);
-                    bcur = b;
-                }
-                const uint4 shift = s_shift[tid];
-                const uint4 sb = sobol4((uint32_t)m);
-                x = make_uint4(sb.x ^ shift.x, sb.y ^ shift.y, sb.z ^ shift.z, sb.w ^ shift.w);
-            } else {
-                x = philox4x32_10(make_uint4((uint32_t)r, (uint32_t)p, ctr2, 0u), P.key0, P.key1);
-            }
+            int m;
+            const uint4 x = ray_words(P, r, M, p, ctr2, &bcur, &s_shift[tid], &m);
             if (TRACE && lane == 0) {
                 P.trace_rng[0] = x.x; P.trace_rng[1] = x.y; P.trace_rng[2] = x.z; P.trace_rng[3] = x.w;
             }
-            // isotropic direction: cos(theta) = 1 - 2u, phi = 2*pi*u'
-            const float mu = fmaf((float)(x.y >> 8), -1.1920928955078125e-7f, 1.0f);
-            const float st = sqrtf(fmaxf(0.0f, fmaf(-mu, mu, 1.0f)));
-            float cph, sph;
-            mc_sincos_turn(x.x >> 8, &cph, &sph);
-            float sW = mu, sA = st * cph, sB = st * sph;
+            float sW, sA, sB;
+            ray_direction(x, &sW, &sA, &sB);
             const float sW0 = sW;  // initial direction, for the control variate's straight flight
 
             // spectral sample and ray weight (the ray's weight is wk * Ii)
@@ -445,15 +497,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
                 sid = e.koff;
-                // the sample's slab (k, then Ib of its band) into this warp's
-                // shared copy; the previous ray's lookups are done first
-                __syncwarp();
-                {
-                    const float4 *src = reinterpret_cast<const float4 *>(P.slab + (long long)sid * P.slab_len);
-                    float4 *dst = reinterpret_cast<float4 *>(slk);
-                    for (int q = lane; q < (P.slab_len >> 1); q += 32) dst[q] = __ldg(src + q);
-                }
-                __syncwarp();
+                load_slab(P, sid, slk, lane);
                 float ki = lookup_k<MODE>(slk, krow, ki_i, ft_i, fx_i);
                 if constexpr (GEN) {
                     if (P.part) { const float2 pp = __ldg(P.part + nbnd); pab = pp.x; psc = pp.y; }
@@ -774,20 +818,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             if (active) {
                 ++my_rays;
                 if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                const double Xd = (double)X;
-                s_acc[0][tid] += Xd;
-                if (P.sampler) {
-                    const double Sb = s_acc[2][tid] + Xd;
-                    if (m == M - 1) {  // end of a replicate: accumulate its mean squared
-                        const double mb = Sb / M;
-                        s_acc[1][tid] = fma(mb, mb, s_acc[1][tid]);
-                        s_acc[2][tid] = 0.0;
-                    } else {
-                        s_acc[2][tid] = Sb;
-                    }
-                } else {
-                    s_acc[1][tid] = fma(Xd, Xd, s_acc[1][tid]);
-                }
+                tally_ray(P, (double)X, m, M, &s_acc[0][tid], &s_acc[1][tid], &s_acc[2][tid]);
             }
         }
         my_steps += lsteps;

@@ -123,30 +123,13 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
         const int rbeg = TRACE ? P.trace_r : 0;
         const int rend = TRACE ? P.trace_r + 1 : ((K > 0) ? N : 0);
         for (int r = rbeg; r < rend; ++r) {
-            uint4 x;
-            int m = 0;
-            if (P.sampler) {
-                const int b = r / M;
-                m = r - b * M;
-                if (b != bcur) {
-                    s_shift[tid] = philox4x32_10(make_uint4((uint32_t)b, (uint32_t)p, ctr2, 0x50B01u), P.key0, P.key1);
-                    bcur = b;
-                }
-                const uint4 shift = s_shift[tid];
-                const uint4 sb = sobol4((uint32_t)m);
-                x = make_uint4(sb.x ^ shift.x, sb.y ^ shift.y, sb.z ^ shift.z, sb.w ^ shift.w);
-            } else {
-                x = philox4x32_10(make_uint4((uint32_t)r, (uint32_t)p, ctr2, 0u), P.key0, P.key1);
-            }
+            int m;
+            const uint4 x = ray_words(P, r, M, p, ctr2, &bcur, &s_shift[tid], &m);
             if (TRACE && lane == 0) {
                 P.trace_rng[0] = x.x; P.trace_rng[1] = x.y; P.trace_rng[2] = x.z; P.trace_rng[3] = x.w;
             }
-            // isotropic direction: cos(theta) = 1 - 2u, phi = 2*pi*u'
-            const float mu = fmaf((float)(x.y >> 8), -1.1920928955078125e-7f, 1.0f);
-            const float st = sqrtf(fmaxf(0.0f, fmaf(-mu, mu, 1.0f)));
-            float cph, sph;
-            mc_sincos_turn(x.x >> 8, &cph, &sph);
-            const float sW = mu, sA = st * cph, sB = st * sph;
+            float sW, sA, sB;
+            ray_direction(x, &sW, &sA, &sB);
 
             // spectral sample, each cell's own k, Ib and weight (wk * Ii)
             int nbnd = 0, sid = 0;
@@ -169,15 +152,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
                 sid = e.koff;
-                // the sample's slab (k, then Ib of its band) into this warp's
-                // shared copy; the previous ray's lookups are done first
-                __syncwarp();
-                {
-                    const float4 *src = reinterpret_cast<const float4 *>(P.slab + (long long)sid * P.slab_len);
-                    float4 *dst = reinterpret_cast<float4 *>(slk);
-                    for (int q = lane; q < (P.slab_len >> 1); q += 32) dst[q] = __ldg(src + q);
-                }
-                __syncwarp();
+                load_slab(P, sid, slk, lane);
 #pragma unroll
                 for (int k = 0; k < C; ++k) {
                     int kx, ti;
@@ -355,20 +330,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 if (active[k]) {
                     ++my_rays;
                     if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                    const double Xd = (double)X;
-                    s_acc[0][k][tid] += Xd;
-                    if (P.sampler) {
-                        const double Sb = s_acc[2][k][tid] + Xd;
-                        if (m == M - 1) {  // end of a replicate: accumulate its mean squared
-                            const double mb = Sb / M;
-                            s_acc[1][k][tid] = fma(mb, mb, s_acc[1][k][tid]);
-                            s_acc[2][k][tid] = 0.0;
-                        } else {
-                            s_acc[2][k][tid] = Sb;
-                        }
-                    } else {
-                        s_acc[1][k][tid] = fma(Xd, Xd, s_acc[1][k][tid]);
-                    }
+                    tally_ray(P, (double)X, m, M, &s_acc[0][k][tid], &s_acc[1][k][tid], &s_acc[2][k][tid]);
                 }
             }
         }
