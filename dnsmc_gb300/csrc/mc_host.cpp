@@ -927,13 +927,11 @@ int region_dims(const dnsmc_solver *s, int *ni, int *nj, int *nk) {
     return DNSMC_OK;
 }
 
-// Cells per lane of the march: kLaneCells for the absorbing gas with black
-// walls on the fine grid, 1 for the general medium (particles, grey walls)
-// and the multigrid march (32-cell packets).
+// Cells per lane of the march: kLaneCells on the fine grid (absorbing gas
+// with black walls, and the general medium with particles / grey walls), 1
+// for the multigrid march (32-cell packets).
 int lane_cells(const dnsmc_solver *s) {
-    const dnsmc_config &c = s->cfg;
-    const bool gen = !s->part.empty() || c.eps_west < 1.0f || c.eps_east < 1.0f;
-    return (gen || c.grid_num > 1) ? 1 : kLaneCells;
+    return s->cfg.grid_num > 1 ? 1 : kLaneCells;
 }
 
 // Packet tiling of the region: tile_a cells along j (a divisor of 32), by

@@ -29,8 +29,8 @@ struct SpecEntry {
     float    W;         // ray weight factor: w = W * k(T_i) * Ib(T_i)
 };
 
-// Cells per lane of the absorbing-gas march (mc_march_pair.cu): a packet is
-// 32 * kLaneCells cells; the general-medium and multigrid marches use 1.
+// Cells per lane of the fine-grid march (mc_march_pair.cuh): a packet is
+// 32 * kLaneCells cells; the multigrid march uses 1.
 constexpr int kLaneCells = 2;
 
 struct MarchParams {
@@ -213,6 +213,7 @@ int launch_march_gen(int mode, const MarchParams &p, int blocks, int threads, vo
 int march_gen_occupancy(int mode, int threads, bool cv, bool mom, size_t smem);  // mc_march_gen.cu
 int upload_sobol_dirs_gen(const uint32_t dirs[4][32]);               // mc_march_gen.cu
 // the absorbing-gas march with two cells per lane (64-cell packets)    // mc_march_pair.cu
+// (launch_march_gen: the same march with the general medium)
 int launch_march_pair(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                       bool mom);
 int march_pair_occupancy(int mode, int threads, bool cv, bool mom, size_t smem);

@@ -1,399 +1,18 @@
-// mc_march_pair.cu -- the march of the absorbing gas with black walls on the
-// fine grid (the reference's kernel_fluid + march_ray, code/mc_gpu.cu:44-438),
-// two cells per lane.
-//
-// A packet here is 64 cells of one wall-normal plane: tile_a cells along j
-// by tile_b = 64 / tile_a along k.  Lane l owns packet cells l and l + 32,
-// which share their j index and lie 32 / tile_a rows apart in k.  Every ray
-// of the packet shares one direction and one spectral sample, so the voxel
-// walk (which face is crossed next, every segment length) is the same for
-// all 64 cells: it is computed once per lane for two cells, and only the
-// per-cell work (field gather, k and Ib lookups, attenuation, tallies) is
-// done twice.  The arithmetic of each cell is exactly that of the one-cell
-// march in mc_march.cuh (which the particle / grey-wall and multigrid
-// marches keep), so the host replay reproduces every cell bit for bit.
-//
-// Compiled with -fmad=false like the other march translation units.
-#include "mc_march.cuh"
+// mc_march_pair.cu -- the two-cell march of the absorbing gas with black
+// walls (mc_march_pair.cuh), instantiated apart from the general-medium
+// variants (mc_march_gen.cu) so both compile in parallel.  Compiled with
+// -fmad=false like the other march translation units.
+#include "mc_march_pair.cuh"
 
 namespace dnsmc {
 
-// Resident 256-thread blocks per SM of this march (2: up to 128 registers a
-// thread; its two cells per lane carry twice the per-cell state).
-#ifndef DNSMC_PAIR_MINB
-#define DNSMC_PAIR_MINB 2
-#endif
-template <int MODE, bool TRACE, bool CV, bool MOM>
-__global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const MarchParams P) {
-    typedef typename FieldT<MODE>::type VT;
-    constexpr int C = kLaneCells;  // cells per lane
-    const unsigned FULL = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const int tid = threadIdx.x;
-    const int la = lane % P.tile_a, lb = lane / P.tile_a;
-    const int hb = 32 / P.tile_a;  // k rows between a lane's two cells
-    const int njR = P.ea1 - P.ea0, nkR = P.eb1 - P.eb0;
-    const int plane = P.na * P.nb;
-    unsigned long long my_rays = 0, my_steps = 0;
-    unsigned int flags = 0;
-    // this warp's copy of the current ray's table slab (tabulated models)
-    extern __shared__ float4 s_slab[];
-    float2 *const slk = reinterpret_cast<float2 *>(s_slab) + (threadIdx.x >> 5) * P.slab_len;
-    const float2 *const sli = slk + P.slab_klen;
-    const int krow = P.nX - 1;
-    // per-cell FP64 sums of the item (ray sum, sum of squares or of squared
-    // replicate means, current replicate sum) and the replicate's shift:
-    // shared memory, so registers hold the march's own working set
-    __shared__ double s_acc[3][C][256];
-    __shared__ uint4 s_shift[256];
-
-    for (;;) {
-        long long item;
-        if (TRACE) {
-            if (threadIdx.x >= 32) return;
-            item = ((long long)P.trace_f * P.n_groups + P.trace_g) * P.n_packets + P.trace_p;
-        } else {
-            unsigned int it = 0;
-            if (lane == 0) it = atomicAdd(P.queue, 1u);
-            it = __shfl_sync(FULL, it, 0);
-            if ((long long)it >= P.n_items) break;
-            item = P.item_order ? (long long)__ldg(P.item_order + it) : (long long)it;
-        }
-        const int p = (int)(item % P.n_packets);
-        const long long fg = item / P.n_packets;
-        const int G = (int)(fg % P.n_groups);
-        const int f = (int)(fg / P.n_groups);
-        const int pa = p % P.npa;
-        const int rest = p / P.npa;
-        const int pb = rest % P.npb;
-        const int pw = rest / P.npb;
-        const int w0 = P.ew0 + pw;
-        const int a0 = P.ea0 + pa * P.tile_a + la;
-        const bool act_a = a0 < P.ea1;
-        const int acl = act_a ? a0 : P.ea0;  // cells outside the region march a valid cell, untallied
-        bool active[C];
-        int bcl[C], tcell[C];
-#pragma unroll
-        for (int k = 0; k < C; ++k) {
-            const int b0 = P.eb0 + pb * P.tile_b + lb + k * hb;
-            active[k] = act_a && b0 < P.eb1;
-            bcl[k] = active[k] ? b0 : P.eb0;
-            tcell[k] = ((w0 - P.ew0) * nkR + (bcl[k] - P.eb0)) * njR + (acl - P.ea0);
-        }
-        const int N = P.rays_per_packet ? P.rays_per_packet[G * P.rays_gstride + p] : P.rays;
-        const long long fbase = (long long)f * P.field_stride;
-        const int rowW0 = w0 * plane;
-        const float oW = (__ldg(P.fw + w0) + __ldg(P.fw + w0 + 1)) * 0.5f;
-        // alias table of this packet: band group G of the temperature bin
-        // nearest to the temperature of the packet's first cell
-        int gs = 0, K = 1;
-        if constexpr (MODE == MODE_GREY) {
-#pragma unroll
-            for (int k = 0; k < C; ++k) {
-                const float Ti = load_field<MODE>(P, fbase, rowW0 + bcl[k] * P.na + acl);
-                if (!(Ti > 0.0f) && active[k]) flags |= DNSMC_STATUS_BAD_FIELD;
-            }
-        } else {
-            int boff = 0;
-            if (P.n_tbins > 1) {
-                int kx, ti;
-                float ft, fx;
-                cell_coords<MODE>(load_field<MODE>(P, fbase, rowW0 + bcl[0] * P.na + acl), &kx, &ti, &ft, &fx);
-                const float tp0 = __shfl_sync(FULL, (float)ti + ft, 0);
-                int bin = __float2int_rn(tp0);
-                bin = min(max(bin, 0), P.n_tbins - 1);
-                boff = bin * P.n_groups;
-            }
-            gs = P.group_start[boff + G];
-            K = P.group_start[boff + G + 1] - gs;
-        }
-        const uint32_t ctr2 = (uint32_t)G | ((uint32_t)(f + P.field_base) << 16);
-        double mo[C][9];
-        if (MOM)
-#pragma unroll
-            for (int k = 0; k < C; ++k)
-#pragma unroll
-                for (int q = 0; q < 9; ++q) mo[k][q] = 0.0;
-        const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
-#pragma unroll
-        for (int k = 0; k < C; ++k) { s_acc[0][k][tid] = 0.0; s_acc[1][k][tid] = 0.0; s_acc[2][k][tid] = 0.0; }
-        unsigned long long isteps = 0;
-        unsigned int lsteps = 0;  // this lane's active cell-steps in the item
-        int bcur = -1;
-        const int rbeg = TRACE ? P.trace_r : 0;
-        const int rend = TRACE ? P.trace_r + 1 : ((K > 0) ? N : 0);
-        for (int r = rbeg; r < rend; ++r) {
-            int m;
-            const uint4 x = ray_words(P, r, M, p, ctr2, &bcur, &s_shift[tid], &m);
-            if (TRACE && lane == 0) {
-                P.trace_rng[0] = x.x; P.trace_rng[1] = x.y; P.trace_rng[2] = x.z; P.trace_rng[3] = x.w;
-            }
-            float sW, sA, sB;
-            ray_direction(x, &sW, &sA, &sB);
-
-            // spectral sample, each cell's own k, Ib and weight (wk * Ii)
-            int nbnd = 0, sid = 0;
-            float wk[C], Ii[C], invI[C];
-            VT vcur[C];
-#pragma unroll
-            for (int k = 0; k < C; ++k) vcur[k] = load_field<MODE>(P, fbase, rowW0 + bcl[k] * P.na + acl);
-            if constexpr (MODE == MODE_GREY) {
-#pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    const float Ti = vcur[k];
-                    const float t2 = Ti * Ti;
-                    Ii[k] = t2 * t2;
-                    invI[k] = Ii[k] > 0.f ? 1.0f / Ii[k] : 0.f;
-                    wk[k] = P.Wgrey;
-                }
-            } else {
-                const int j = (int)__umulhi(x.z, (uint32_t)K);
-                SpecEntry e = P.entries[gs + j];
-                if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
-                nbnd = (int)(e.alias_nb >> 16);
-                sid = e.koff;
-                load_slab(P, sid, slk, lane);
-#pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    int kx, ti;
-                    float ft, fx;
-                    cell_coords<MODE>(vcur[k], &kx, &ti, &ft, &fx);
-                    const float ki = lookup_k<MODE>(slk, krow, kx, ft, fx);
-                    Ii[k] = lookup_ib(sli, ti, ft);
-                    invI[k] = Ii[k] > 0.f ? 1.0f / Ii[k] : 0.f;
-                    wk[k] = e.W * ki;
-                }
-            }
-
-            // warp-uniform DDA from the cell centres
-            const float invW = 1.0f / fabsf(sW), invA = 1.0f / fabsf(sA), invB = 1.0f / fabsf(sB);
-            const int dW = sW > 0.f ? 1 : -1, dA = sA > 0.f ? 1 : -1, dB = sB > 0.f ? 1 : -1;
-            // crossing parameter of the next wall-normal face: (fw[c + 1] - o) / s
-            // going up, (o - fw[c]) / |s| = (fw[c] - o) * (-1/|s|) going down
-            // (negation is exact: the same values)
-            const float *fwn = P.fw + (dW > 0 ? 1 : 0);
-            const float sinvW = dW > 0 ? invW : -invW;
-            float tW = (__ldg(fwn + w0) - oW) * sinvW;
-            // periodic wrap of the next j / k index: one compare per step
-            const int wrapA = dA > 0 ? P.na : -1, resetA = dA > 0 ? 0 : P.na - 1;
-            const int wrapB = dB > 0 ? P.nb : -1, resetB = dB > 0 ? 0 : P.nb - 1;
-            const int wallW = dW > 0 ? P.nw : -1;  // the wall-normal index beyond the wall
-            const int dRowW = dW * plane;
-            const float dtA = P.da * invA, dtB = P.db * invB;
-            float tA = 0.5f * dtA, tB = 0.5f * dtB;
-            // crossing counts plus one half, as floats: (float)n + 0.5f is
-            // exact and so is adding 1 to it below 2^22 crossings, so these
-            // are the values the integer counts would give, without a
-            // conversion per step
-            float hA = 0.5f, hB = 0.5f;
-            int cw = w0, ca = acl, rowW = rowW0;
-            int cb[C], rowB[C];
-            float tau[C], D[C];
-#pragma unroll
-            for (int k = 0; k < C; ++k) {
-                cb[k] = bcl[k];
-                rowB[k] = bcl[k] * P.na;
-                tau[k] = active[k] ? 1.0f : 0.0f;
-                D[k] = 0.0f;
-            }
-            float t = 0.0f;
-            int steps = 0;
-            // unrolled by two: the current / next field values alternate
-            // registers instead of being copied every step
-#pragma unroll 2
-            for (;;) {
-                const bool sW_ = tW <= tA && tW <= tB;
-                const bool sA_ = !sW_ && tA <= tB;
-                const int axis = sW_ ? 0 : (sA_ ? 1 : 2);
-                const float tn = sW_ ? tW : (sA_ ? tA : tB);
-                const float ds = tn - t;
-                // next cell of the walk, and its field values fetched now; the
-                // axis is the same in every lane, but selects cost fewer
-                // instructions here than branches the compiler must treat as
-                // divergent
-                int ncw, nca, nrowW;
-                int ncb[C], nrowB[C];
-                const bool aW = axis == 0, aA = axis == 1, aB = axis == 2;
-                ncw = aW ? cw + dW : cw;
-                nrowW = aW ? rowW + dRowW : rowW;
-                {
-                    int u = ca + dA;
-                    u = u == wrapA ? resetA : u;
-                    nca = aA ? u : ca;
-                }
-#pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    int u = cb[k] + dB;
-                    u = u == wrapB ? resetB : u;
-                    ncb[k] = aB ? u : cb[k];
-                    nrowB[k] = aB ? u * P.na : rowB[k];
-                }
-                const bool wall = aW && ncw == wallW;
-                VT vnext[C];
-#pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    vnext[k] = vcur[k];
-                    if (!wall && tau[k] > 0.0f) vnext[k] = load_field<MODE>(P, fbase, nrowW + nrowB[k] + nca);
-                }
-                // attenuation and collected intensity of this segment; a cell
-                // already dumped (tau 0) adds exactly nothing
-#pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    lsteps += tau[k] > 0.0f ? 1u : 0u;
-                    float kj, gj;
-                    if constexpr (MODE == MODE_GREY) {
-                        const float t2 = vcur[k] * vcur[k];
-                        gj = (Ii[k] - t2 * t2) * invI[k];
-                        kj = P.kappa;
-                    } else {
-                        int kx, tj;
-                        float ftj, fxj;
-                        cell_coords<MODE>(vcur[k], &kx, &tj, &ftj, &fxj);
-                        kj = lookup_k<MODE>(slk, krow, kx, ftj, fxj);
-                        const float Ibj = lookup_ib(sli, tj, ftj);
-                        gj = (Ii[k] - Ibj) * invI[k];
-                    }
-                    const float alpha = -mc_expm1(-(kj * ds));
-                    const float ta = tau[k] * alpha;
-                    D[k] = fmaf(ta, gj, D[k]);
-                    tau[k] = tau[k] - ta;
-                    if (tau[k] < P.toll) { D[k] = fmaf(tau[k], gj, D[k]); tau[k] = 0.0f; }
-                }
-                if (TRACE && lane == 0 && steps < P.trace_max) {
-                    int *rec = P.trace_rec + 6 * steps;
-                    rec[0] = cw; rec[1] = dA * (int)(hA - 0.5f); rec[2] = dB * (int)(hB - 0.5f); rec[3] = axis;
-                    rec[4] = __float_as_int(ds); rec[5] = __float_as_int(tau[0]);
-                }
-                t = tn;
-                ++steps;
-                {
-                    if (wall) {
-                        const int side = ncw < 0 ? 0 : 1;
-                        const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
-#pragma unroll
-                        for (int k = 0; k < C; ++k) {
-                            D[k] = fmaf(tau[k], (Ii[k] - Iw) * invI[k], D[k]);
-                            tau[k] = 0.0f;
-                        }
-                        break;
-                    }
-                    cw = ncw;
-                    rowW = nrowW;
-                    if (aW) tW = (__ldg(fwn + cw) - oW) * sinvW;
-                    hA = aA ? hA + 1.0f : hA;
-                    tA = hA * dtA;
-                    ca = nca;
-                    hB = aB ? hB + 1.0f : hB;
-                    tB = hB * dtB;
-#pragma unroll
-                    for (int k = 0; k < C; ++k) { cb[k] = ncb[k]; rowB[k] = nrowB[k]; }
-                }
-#pragma unroll
-                for (int k = 0; k < C; ++k) vcur[k] = vnext[k];
-                bool alive = false;
-#pragma unroll
-                for (int k = 0; k < C; ++k) alive = alive || tau[k] > 0.0f;
-                if (!__any_sync(FULL, alive)) break;
-                if (steps >= P.max_steps) {
-                    if (alive) flags |= DNSMC_STATUS_STEP_CAP;
-                    break;
-                }
-            }
-            if (TRACE && lane == 0) *P.trace_n = steps;
-            isteps += (unsigned long long)steps;
-            // control variate: the ray's straight flight through the
-            // layer-mean medium, the same for both cells (same layer)
-            float Jbar = 0.0f, tex0 = 0.0f, I0 = 0.0f;
-            if (CV) {
-                const float2 *surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
-                I0 = __ldg(surp + w0).y;
-                surrogate_walk<MODE>(P, surp, w0, oW, sW, nbnd, &Jbar, &tex0);
-            }
-#pragma unroll
-            for (int k = 0; k < C; ++k) {
-                float X = (wk[k] * Ii[k]) * D[k];
-                if (CV) {
-                    // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
-                    const float Ya = wk[k] * (Ii[k] - Jbar);
-                    const float Yb = wk[k] * ((1.0f - tex0) * (Ii[k] - I0));
-                    if (MOM && active[k]) {
-                        const double xd = X, ya = Ya, yb = Yb;
-                        mo[k][0] += xd; mo[k][1] += ya; mo[k][2] += yb;
-                        mo[k][3] = fma(xd, xd, mo[k][3]); mo[k][4] = fma(ya, ya, mo[k][4]);
-                        mo[k][5] = fma(yb, yb, mo[k][5]); mo[k][6] = fma(xd, ya, mo[k][6]);
-                        mo[k][7] = fma(xd, yb, mo[k][7]); mo[k][8] = fma(ya, yb, mo[k][8]);
-                    }
-                    const float2 beta = P.beta ? P.beta[fg * P.region_cells + tcell[k]] : make_float2(1.0f, -1.0f);
-                    X = X - beta.x * Ya;  // tallied: X - beta_a Y_a - beta_b Y_b; the
-                    X = X - beta.y * Yb;  // means beta . E[Y] are added back at finalize
-                }
-                if (active[k]) {
-                    ++my_rays;
-                    if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                    tally_ray(P, (double)X, m, M, &s_acc[0][k][tid], &s_acc[1][k][tid], &s_acc[2][k][tid]);
-                }
-            }
-        }
-        my_steps += lsteps;
-        if (TRACE) return;
-        if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
-#pragma unroll
-        for (int k = 0; k < C; ++k) {
-            if (!active[k]) continue;
-            const long long o = fg * P.region_cells + tcell[k];
-            P.tally[o] = make_double2(s_acc[0][k][tid], s_acc[1][k][tid]);
-            if (MOM) {
-                double *out = P.moments + o * 9;
-#pragma unroll
-                for (int q = 0; q < 9; ++q) out[q] = mo[k][q];
-            }
-        }
-    }
-    // per-warp counters and status
-    for (int o = 16; o > 0; o >>= 1) {
-        my_rays += __shfl_xor_sync(FULL, my_rays, o);
-        my_steps += __shfl_xor_sync(FULL, my_steps, o);
-        flags |= __shfl_xor_sync(FULL, flags, o);
-    }
-    if (lane == 0) {
-        if (my_rays) atomicAdd(P.counters + 0, my_rays);
-        if (my_steps) atomicAdd(P.counters + 1, my_steps);
-        if (flags) atomicOr(P.status, flags);
-    }
-}
-
 int launch_march_pair(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                       bool mom) {
-    cudaStream_t st = (cudaStream_t)stream;
-    if (trace) { blocks = 1; threads = 32; mom = false; }
-    const size_t smem = march_smem(p, threads);
-#define DNSMC_L(M, T, CV_, O) return march_launch_one(march_pair_kernel<M, T, CV_, O>, blocks, threads, smem, st, p)
-#define DNSMC_MODE(M)                                                                                  \
-    if (trace) { if (cv) DNSMC_L(M, true, true, false); else DNSMC_L(M, true, false, false); }         \
-    else if (cv) { if (mom) DNSMC_L(M, false, true, true); else DNSMC_L(M, false, true, false); }      \
-    else DNSMC_L(M, false, false, false);
-    switch (mode) {
-        case MODE_GREY: DNSMC_MODE(MODE_GREY) break;
-        case MODE_T: DNSMC_MODE(MODE_T) break;
-        case MODE_TX: DNSMC_MODE(MODE_TX) break;
-        default: break;
-    }
-#undef DNSMC_MODE
-#undef DNSMC_L
-    return (int)cudaErrorInvalidValue;
+    return launch_march_cells<false>(mode, p, blocks, threads, stream, trace, cv, mom);
 }
 
 int march_pair_occupancy(int mode, int threads, bool cv, bool mom, size_t smem) {
-    int nb = 0;
-#define DNSMC_O(M)                                                                                   \
-    nb = cv ? (mom ? march_occupancy_one(march_pair_kernel<M, false, true, true>, threads, smem)     \
-                   : march_occupancy_one(march_pair_kernel<M, false, true, false>, threads, smem))   \
-            : march_occupancy_one(march_pair_kernel<M, false, false, false>, threads, smem)
-    if (mode == MODE_GREY) DNSMC_O(MODE_GREY);
-    if (mode == MODE_T) DNSMC_O(MODE_T);
-    if (mode == MODE_TX) DNSMC_O(MODE_TX);
-#undef DNSMC_O
-    return nb > 0 ? nb : 1;
+    return march_cells_occupancy<false>(mode, threads, cv, mom, smem);
 }
 
 int upload_sobol_dirs_pair(const uint32_t dirs[4][32]) {

@@ -1041,19 +1041,26 @@ struct Packet {
                     tB = ((R)nB + offB) * dtB;
                     for (int l = 0; l < nl; ++l) { cb[l] += dB; if (cb[l] == c.nb) cb[l] = 0; else if (cb[l] < 0) cb[l] = c.nb - 1; }
                 } else {
-                    // tentative collision: shared decision, per-lane weights;
-                    // q is the butterfly (xor 16, 8, 4, 2, 1) sum of the device
-                    R pl[128], ps[128], pc[128];
+                    // tentative collision: shared decision, per-cell weights;
+                    // q is the device's sum: each lane adds its cells l, l + 32,
+                    // ... in order, then the butterfly (xor 16, 8, 4, 2, 1)
+                    R pl[128], ps[32], pc[32];
                     for (int l = 0; l < nl; ++l) {
                         const R fvl = c.fieldV ? (R)c.fieldV[cidx(f, cw, ca[l], cb[l])] : (R)0;
                         pl[l] = tau[l] > 0 ? std::fmin((R)1, fvl * psc / sigbar) : (R)0;
+                    }
+                    for (int l = 0; l < 32; ++l) {
                         ps[l] = pl[l];
                         pc[l] = tau[l] > 0 ? (R)1 : (R)0;
+                        for (int k = l + 32; k < nl; k += 32) {
+                            ps[l] = ps[l] + pl[k];
+                            pc[l] = pc[l] + (tau[k] > 0 ? (R)1 : (R)0);
+                        }
                     }
                     for (int o = 16; o > 0; o >>= 1) {
-                        R ns[128], nc[128];
-                        for (int l = 0; l < nl; ++l) { ns[l] = ps[l] + ps[l ^ o]; nc[l] = pc[l] + pc[l ^ o]; }
-                        for (int l = 0; l < nl; ++l) { ps[l] = ns[l]; pc[l] = nc[l]; }
+                        R ns[32], nc[32];
+                        for (int l = 0; l < 32; ++l) { ns[l] = ps[l] + ps[l ^ o]; nc[l] = pc[l] + pc[l ^ o]; }
+                        for (int l = 0; l < 32; ++l) { ps[l] = ns[l]; pc[l] = nc[l]; }
                     }
                     const R q = pc[0] > 0 ? ps[0] / pc[0] : (R)0;
                     if ((R)p_u24(evx[1]) < q) {
@@ -1243,8 +1250,7 @@ extern "C" {
 // Tally [f][G][iR][kR][jR][2] (sum X, sum X^2) exactly as the device stores it.
 int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double *steps_out) {
     if (!c || c->tile_a < 1 || 32 % c->tile_a || c->cpl < 0 || c->cpl > 4) return 1;
-    // the general medium and the multigrid march run 32-cell packets only
-    if (c->cpl > 1 && (c->gen || c->mg_levels > 1)) return 1;
+    if (c->cpl > 1 && c->mg_levels > 1) return 1;  // the multigrid march runs 32-cell packets
     const int nl = 32 * (c->cpl > 1 ? c->cpl : 1);
     const int ta = c->tile_a, tb = nl / ta;
     const int niR = c->ew1 - c->ew0, njR = c->ea1 - c->ea0, nkR = c->eb1 - c->eb0;
@@ -1282,7 +1288,7 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
 int orc_packet_trace(const OrcPacketConfig *c, int f, int G, int p, int r, int max_steps, int32_t *rec, int *n,
                      uint32_t rng[4]) {
     if (!c || c->tile_a < 1 || 32 % c->tile_a || c->cpl < 0 || c->cpl > 4) return 1;
-    if (c->cpl > 1 && (c->gen || c->mg_levels > 1)) return 1;
+    if (c->cpl > 1 && c->mg_levels > 1) return 1;  // the multigrid march runs 32-cell packets
     double S[128], S2[128], st = 0;
     Packet<float>(*c).item(f, G, p, S, S2, &st, r, max_steps, rec, n, rng);
     return 0;

@@ -124,8 +124,8 @@ def test_equilibrium_is_exactly_zero():
 
 
 def plane_means(Q, S, packets_per_plane):
-    """Plane means and their standard errors.  In a uniform medium the 32
-    cells of a packet share every ray, so their errors are identical: the
+    """Plane means and their standard errors.  In a uniform medium the cells
+    of a packet share every ray, so their errors are identical: the
     independent samples of a plane are its packets, not its cells."""
     return Q[0].mean(axis=(0, 1)), np.sqrt((S[0] ** 2).mean(axis=(0, 1)) / packets_per_plane)
 
@@ -138,7 +138,7 @@ def test_grey_wall_slab_matches_analytic():
     s.set_fields(np.full((8, 32, ni), 1000.0, np.float32))
     s.set_rays(256)
     Q, S = s.solve(timeout_s=120)
-    q, e = plane_means(Q, S, 8)
+    q, e = plane_means(Q, S, s.packet_count() // ni)
     xu, _, _ = s.geometry()
     yc = 0.5 * (xu[1:] + xu[:-1])
     ex = O.slab_grey_walls_divq(yc, 2.0, 1.0, 1000.0, 400.0, 0.6)
@@ -160,9 +160,9 @@ def test_isotropic_scattering_slab_matches_integral_equation():
     s.set_fields(np.full((8, 32, ni), 1000.0, np.float32))
     s.set_particles(np.array([0.0], np.float32), np.array([ss / 1e-5], np.float32), 0.0)
     s.set_particle_field(np.full((8, 32, ni), 1e-5, np.float32))
-    s.set_rays(256)
+    s.set_rays(512)  # four independent 64-cell packets per plane
     Q, S = s.solve(timeout_s=120)
-    q, e = plane_means(Q, S, 8)
+    q, e = plane_means(Q, S, s.packet_count() // ni)
     xu, _, _ = s.geometry()
     ref = O.slab_scatter_divq(xu.astype(np.float64), ka, ss, 1000.0, 0.0, 0.0)
     z = (q - ref) / np.sqrt(e ** 2 + (2e-4 * np.abs(ref)) ** 2)
