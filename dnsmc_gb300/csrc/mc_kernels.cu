@@ -219,15 +219,15 @@ int launch_march_mg(int mode, const MarchParams &p, int blocks, int threads, voi
     if (trace) { blocks = 1; threads = 32; }
     const size_t smem = march_smem(p, threads);
     if (mode == MODE_GREY) {
-        if (trace) return march_launch_one(march_kernel<MODE_GREY, true, false, false, false, true>, blocks, threads,
+        if (trace) return march_launch_one(march_mg_kernel<MODE_GREY, true>, blocks, threads,
                                            smem, st, p);
-        return march_launch_one(march_kernel<MODE_GREY, false, false, false, false, true>, blocks, threads, smem, st,
+        return march_launch_one(march_mg_kernel<MODE_GREY, false>, blocks, threads, smem, st,
                                 p);
     }
     if (mode == MODE_T) {
-        if (trace) return march_launch_one(march_kernel<MODE_T, true, false, false, false, true>, blocks, threads,
+        if (trace) return march_launch_one(march_mg_kernel<MODE_T, true>, blocks, threads,
                                            smem, st, p);
-        return march_launch_one(march_kernel<MODE_T, false, false, false, false, true>, blocks, threads, smem, st, p);
+        return march_launch_one(march_mg_kernel<MODE_T, false>, blocks, threads, smem, st, p);
     }
     return (int)cudaErrorInvalidValue;
 }
@@ -235,8 +235,8 @@ int launch_march_mg(int mode, const MarchParams &p, int blocks, int threads, voi
 int march_mg_occupancy(int mode, int threads, size_t smem) {
     int nb = 0;
     if (mode == MODE_GREY)
-        nb = march_occupancy_one(march_kernel<MODE_GREY, false, false, false, false, true>, threads, smem);
-    if (mode == MODE_T) nb = march_occupancy_one(march_kernel<MODE_T, false, false, false, false, true>, threads, smem);
+        nb = march_occupancy_one(march_mg_kernel<MODE_GREY, false>, threads, smem);
+    if (mode == MODE_T) nb = march_occupancy_one(march_mg_kernel<MODE_T, false>, threads, smem);
     return nb > 0 ? nb : 1;
 }
 

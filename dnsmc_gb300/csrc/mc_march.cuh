@@ -1,10 +1,12 @@
-// mc_march.cuh -- the march kernel and its device helpers, shared by the
-// translation units that instantiate it: mc_kernels.cu (absorbing gas,
-// black walls) and mc_march_gen.cu (the general medium: particles with
-// scattering, grey walls).  Both are compiled with -fmad=false: the arithmetic
-// is written with explicit fmaf so the host replay (oracle/mc_oracle.cpp)
-// reproduces every ray bit for bit; exp, log, sin and cos are the project's
-// own polynomial kernels for the same reason.
+// mc_march.cuh -- the device helpers of the marches (Philox, Sobol', the
+// attenuation and trigonometric polynomials, table lookups, the control
+// variate's straight flight, the ray's words, direction, slab and tally),
+// the multigrid march (march_mg_kernel, instantiated in mc_kernels.cu) and
+// the launch helpers; the fine-grid two-cell marches are in
+// mc_march_pair.cuh.  The march translation units are compiled with
+// -fmad=false: the arithmetic is written with explicit fmaf so the host
+// replay (oracle/mc_oracle.cpp) reproduces every ray bit for bit; exp, log,
+// sin and cos are the project's own polynomial kernels for the same reason.
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
@@ -275,9 +277,9 @@ __device__ __forceinline__ void surrogate_walk(const MarchParams &P, const float
 }
 
 // ---------------------------------------------------------------------------
-// Pieces shared by the marches (mc_march.cuh's one-cell kernel and
-// mc_march_pair.cu's two-cell kernel): the words of a packet-ray, its
-// direction, the copy of its spectral sample's table slab, one ray's tally.
+// Pieces shared by the marches (the multigrid march below and the two-cell
+// marches of mc_march_pair.cuh): the words of a packet-ray, its direction,
+// the copy of its spectral sample's table slab, one ray's tally.
 // ---------------------------------------------------------------------------
 
 // The ray's four uniform words.  RQMC: point m of replicate b = r / M of a
@@ -344,31 +346,21 @@ __device__ __forceinline__ void tally_ray(const MarchParams &P, double Xd, int m
 }
 
 // ---------------------------------------------------------------------------
-// The march kernel.  Persistent: every warp pulls work items (field, band
-// group, packet) from an atomic counter until the queue is empty.  The next
-// cell's field value is loaded one step ahead of its use.
-//
-// GEN (the general medium) adds particles and grey walls:
-//   * absorption k = k_gas + fv a_band and scattering fv s_band per cell;
-//   * scattering by weighted delta tracking with a shared decision: flights
-//     to tentative collisions are drawn with the majorant fv_max s_band
-//     (warp-uniform); at a collision the warp scatters with probability q =
-//     mean over live lanes of p_l = fv_l s_band / majorant, and each lane's
-//     throughput is multiplied by p_l / q (scatter) or (1 - p_l)/(1 - q)
-//     (no scatter).  The estimate stays unbiased and the whole walk stays
-//     warp-uniform; the new direction follows Henyey-Greenstein;
-//   * grey diffuse walls: the wall takes eps of the throughput at its own
-//     intensity and reflects the rest into a cosine-distributed direction.
-// Every direction change restarts the DDA from the current point: lanes
-// still differ by whole periodic cells only.
+// The multigrid march (grid_num > 1; the reference's grid switch,
+// code/mc_gpu.cu:193-207), one cell per lane, 32-cell packets: the absorbing
+// gas with black walls, grey or T tables, no control variate.  Persistent:
+// every warp pulls work items (field, band group, packet) from an atomic
+// counter.  The fine phase is the warp-uniform walk of the two-cell march
+// (mc_march_pair.cuh) for mg_steps steps; then every lane continues from its
+// own point on the coarser grids with the reference's position-update march.
 // ---------------------------------------------------------------------------
 // Resident blocks of 256 threads per SM the register allocation must allow
 // (2: up to 128 registers; 3: 85; 4: 64), chosen at build time.
 #ifndef DNSMC_MINB
 #define DNSMC_MINB 4
 #endif
-template <int MODE, bool TRACE, bool CV, bool MOM, bool GEN, bool MG = false>
-__global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParams P) {
+template <int MODE, bool TRACE>
+__global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchParams P) {
     typedef typename FieldT<MODE>::type VT;
     const unsigned FULL = 0xffffffffu;
     const float INF = __int_as_float(0x7f800000);
@@ -383,12 +375,8 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
     float2 *const slk = reinterpret_cast<float2 *>(s_slab) + (threadIdx.x >> 5) * P.slab_len;
     const float2 *const sli = slk + P.slab_klen;
     const int krow = P.nX - 1;
-    // Per-lane state that is not needed while a ray marches lives in shared
-    // memory, so the march keeps its own working set in registers: the
-    // item's FP64 sums (ray sum, sum of squares or of squared replicate
-    // means, current replicate sum), its moment sums, the replicate's shift.
+    // the item's FP64 sums and the replicate's shift, in shared memory
     __shared__ double s_acc[3][256];
-    __shared__ double s_mo[MOM ? 9 : 1][MOM ? 256 : 1];
     __shared__ uint4 s_shift[256];
     const int tid = threadIdx.x;
 
@@ -422,10 +410,6 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
         const int rowW0 = w0 * plane;
         // own-cell quantities
         const VT vown = load_field<MODE>(P, fbase, rowW0 + bcl * P.na + acl);
-        float fvown = 0.0f;
-        if constexpr (GEN) {
-            if (P.fieldV) fvown = __ldg(P.fieldV + fbase + rowW0 + bcl * P.na + acl);
-        }
         float Ti4 = 0.f, invTi4 = 0.f, tpos0 = 0.f;
         int ti_i = 0, ki_i = 0;
         float ft_i = 0.f, fx_i = 0.f;
@@ -457,11 +441,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
         const uint32_t ctr2 = (uint32_t)G | ((uint32_t)(f + P.field_base) << 16);
         const long long tc = ((long long)(w0 - P.ew0) * nkR + (bcl - P.eb0)) * njR + (acl - P.ea0);
         const long long cell_out = fg * P.region_cells + tc;  // tally index of this lane's cell
-        if (MOM)
-#pragma unroll
-            for (int q = 0; q < 9; ++q) s_mo[q][tid] = 0.0;
         const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
-
         s_acc[0][tid] = 0.0; s_acc[1][tid] = 0.0; s_acc[2][tid] = 0.0;
         unsigned long long isteps = 0;
         unsigned int lsteps = 0;  // this lane's active steps in the item
@@ -476,83 +456,46 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             }
             float sW, sA, sB;
             ray_direction(x, &sW, &sA, &sB);
-            const float sW0 = sW;  // initial direction, for the control variate's straight flight
 
             // spectral sample and ray weight (the ray's weight is wk * Ii)
             float wk, Ii, invI;
-            int nbnd = 0, sid = 0;
-            float pab = 0.0f, psc = 0.0f;  // particle absorption / scattering per unit volume fraction
+            int nbnd = 0;
             if (MODE == MODE_GREY) {
                 Ii = Ti4;
                 invI = invTi4;
-                if constexpr (GEN) {
-                    if (P.part) { const float2 pp = __ldg(P.part); pab = pp.x; psc = pp.y; }
-                    wk = P.W4sig * fmaf(fvown, pab, P.kappa);
-                } else {
-                    wk = P.Wgrey;
-                }
+                wk = P.Wgrey;
             } else {
                 const int j = (int)__umulhi(x.z, (uint32_t)K);
                 SpecEntry e = P.entries[gs + j];
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
-                sid = e.koff;
-                load_slab(P, sid, slk, lane);
-                float ki = lookup_k<MODE>(slk, krow, ki_i, ft_i, fx_i);
-                if constexpr (GEN) {
-                    if (P.part) { const float2 pp = __ldg(P.part + nbnd); pab = pp.x; psc = pp.y; }
-                    ki = fmaf(fvown, pab, ki);
-                }
+                load_slab(P, e.koff, slk, lane);
+                const float ki = lookup_k<MODE>(slk, krow, ki_i, ft_i, fx_i);
                 Ii = lookup_ib(sli, ti_i, ft_i);
                 invI = Ii > 0.f ? 1.0f / Ii : 0.f;
                 wk = e.W * ki;
             }
 
-            // warp-uniform DDA from (pw0, fa0, fb0): wall-normal coordinate and
-            // fractional offsets inside the current periodic cells
-            float pw0 = oW, fa0 = 0.5f, fb0 = 0.5f, offA = 0.5f, offB = 0.5f;
-            float invW, invA, invB, tW, dtA, dtB, tA, tB;
-            int dW, dA, dB, nA, nB;
+            // fine phase: the warp-uniform DDA from the cell centres
+            const float invW = 1.0f / fabsf(sW), invA = 1.0f / fabsf(sA), invB = 1.0f / fabsf(sB);
+            const int dW = sW > 0.f ? 1 : -1, dA = sA > 0.f ? 1 : -1, dB = sB > 0.f ? 1 : -1;
             int cw = w0, ca = acl, cb = bcl;
-            auto dda_init = [&]() {
-                invW = 1.0f / fabsf(sW); invA = 1.0f / fabsf(sA); invB = 1.0f / fabsf(sB);
-                dW = sW > 0.f ? 1 : -1; dA = sA > 0.f ? 1 : -1; dB = sB > 0.f ? 1 : -1;
-                tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - pw0) : (pw0 - __ldg(P.fw + cw))) * invW;
-                dtA = P.da * invA; dtB = P.db * invB;
-                if constexpr (GEN) {
-                    offA = dA > 0 ? 1.0f - fa0 : fa0;
-                    offB = dB > 0 ? 1.0f - fb0 : fb0;
-                }
-                tA = offA * dtA; tB = offB * dtB;
-                nA = 0; nB = 0;
-            };
-            dda_init();
+            float tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - oW) : (oW - __ldg(P.fw + cw))) * invW;
+            const float dtA = P.da * invA, dtB = P.db * invB;
+            float tA = 0.5f * dtA, tB = 0.5f * dtB;
+            int nA = 0, nB = 0;
             float t = 0.0f;
             int rowW = rowW0, rowB = cb * P.na;
             float tau = active ? 1.0f : 0.0f;
             float D = 0.0f;
             int steps = 0;
             VT vcur = vown;
-            float fvcur = fvown;
-            // scattering events (GEN): one Philox word quadruple per event
-            uint32_t ev = 0;
-            uint4 evx = make_uint4(0u, 0u, 0u, 0u);
-            float sigbar = 0.0f, tcol = INF;
-            auto draw = [&]() {
-                evx = philox4x32_10(make_uint4((uint32_t)r, (uint32_t)p, ctr2, 0x5CA70000u + ev), P.key0, P.key1);
-                ++ev;
-            };
-            if constexpr (GEN) {
-                sigbar = P.fv_max * psc;
-                if (sigbar > 0.0f) { draw(); tcol = mc_neglog(u24o(evx.x)) / sigbar; }
-            }
             for (;;) {
                 int axis;
                 float tn;
                 if (tW <= tA && tW <= tB) { axis = 0; tn = tW; }
                 else if (tA <= tB)         { axis = 1; tn = tA; }
                 else                       { axis = 2; tn = tB; }
-                if (GEN && tcol < tn) { axis = 3; tn = tcol; }
                 const float ds = tn - t;
                 // next cell of the walk, and its field value fetched now
                 int ncw = cw, nca = ca, ncb = cb, nrowW = rowW, nrowB = rowB;
@@ -564,23 +507,16 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                 } else if (axis == 1) {
                     nca = ca + dA;
                     if (nca == P.na) nca = 0; else if (nca < 0) nca = P.na - 1;
-                } else if (axis == 2) {
+                } else {
                     ncb = cb + dB;
                     if (ncb == P.nb) ncb = 0; else if (ncb < 0) ncb = P.nb - 1;
                     nrowB = ncb * P.na;
                 }
                 VT vnext = vcur;
-                float fvnext = fvcur;
-                if (axis < 3 && !wall && tau > 0.0f) {
-                    vnext = load_field<MODE>(P, fbase, nrowW + nrowB + nca);
-                    if constexpr (GEN) {
-                        if (P.fieldV) fvnext = __ldg(P.fieldV + fbase + nrowW + nrowB + nca);
-                    }
-                }
-                float gj = 0.0f;
+                if (!wall && tau > 0.0f) vnext = load_field<MODE>(P, fbase, nrowW + nrowB + nca);
                 if (tau > 0.0f) {
                     ++lsteps;
-                    float kj;
+                    float kj, gj;
                     if constexpr (MODE == MODE_GREY) {
                         const float t2 = vcur * vcur;
                         gj = (Ti4 - t2 * t2) * invI;
@@ -593,7 +529,6 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                         const float Ibj = lookup_ib(sli, tj, ftj);
                         gj = (Ii - Ibj) * invI;
                     }
-                    if constexpr (GEN) kj = fmaf(fvcur, pab, kj);
                     const float alpha = -mc_expm1(-(kj * ds));
                     const float ta = tau * alpha;
                     D = fmaf(ta, gj, D);
@@ -611,93 +546,30 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
                     if (wall) {
                         const int side = ncw < 0 ? 0 : 1;
                         const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
-                        if constexpr (GEN) {
-                            const float eps = P.eps[side];
-                            if (tau > 0.0f) {
-                                const float gw = (Ii - Iw) * invI;
-                                D = fmaf(tau * eps, gw, D);
-                                tau = eps >= 1.0f ? 0.0f : tau * (1.0f - eps);
-                                if (tau > 0.0f && tau < P.toll) { D = fmaf(tau, gw, D); tau = 0.0f; }
-                            }
-                            if (!__any_sync(FULL, tau > 0.0f)) break;
-                            // diffuse reflection from the wall point
-                            const float ta_ = t / dtA, tb_ = t / dtB;
-                            fa0 = dA > 0 ? fa0 + (ta_ - (float)nA) : fa0 - (ta_ - (float)nA);
-                            fb0 = dB > 0 ? fb0 + (tb_ - (float)nB) : fb0 - (tb_ - (float)nB);
-                            fa0 = fminf(fmaxf(fa0, 0.0f), 1.0f);
-                            fb0 = fminf(fmaxf(fb0, 0.0f), 1.0f);
-                            pw0 = side == 0 ? __ldg(P.fw) : __ldg(P.fw + P.nw);
-                            draw();  // this event's words: the reflected direction only
-                            const float cmu = sqrtf(u24(evx.z));
-                            const float smu = sqrtf(fmaxf(0.0f, 1.0f - cmu * cmu));
-                            float cp, sp;
-                            mc_sincos_turn(evx.w >> 8, &cp, &sp);
-                            sW = side == 0 ? cmu : -cmu;
-                            sA = smu * cp;
-                            sB = smu * sp;
-                            dda_init();
-                            t = 0.0f;
-                            if (sigbar > 0.0f) { draw(); tcol = mc_neglog(u24o(evx.x)) / sigbar; }
-                            if (steps >= P.max_steps) {
-                                if (tau > 0.0f) flags |= DNSMC_STATUS_STEP_CAP;
-                                break;
-                            }
-                            continue;
-                        } else {
-                            if (tau > 0.0f) {
-                                D = fmaf(tau, (Ii - Iw) * invI, D);
-                                tau = 0.0f;
-                            }
-                            break;
+                        if (tau > 0.0f) {
+                            D = fmaf(tau, (Ii - Iw) * invI, D);
+                            tau = 0.0f;
                         }
+                        break;
                     }
                     cw = ncw;
                     rowW = nrowW;
-                    tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - pw0) : (pw0 - __ldg(P.fw + cw))) * invW;
+                    tW = (dW > 0 ? (__ldg(P.fw + cw + 1) - oW) : (oW - __ldg(P.fw + cw))) * invW;
                 } else if (axis == 1) {
                     ++nA;
-                    tA = ((float)nA + offA) * dtA;
+                    tA = ((float)nA + 0.5f) * dtA;
                     ca = nca;
-                } else if (axis == 2) {
+                } else {
                     ++nB;
-                    tB = ((float)nB + offB) * dtB;
+                    tB = ((float)nB + 0.5f) * dtB;
                     cb = ncb;
                     rowB = nrowB;
-                } else if constexpr (GEN) {
-                    // tentative collision: shared decision, per-lane weights
-                    const float pl = tau > 0.0f ? fminf(1.0f, fvcur * psc / sigbar) : 0.0f;
-                    float ps = pl, pc = tau > 0.0f ? 1.0f : 0.0f;
-                    for (int o = 16; o > 0; o >>= 1) {
-                        ps += __shfl_xor_sync(FULL, ps, o);
-                        pc += __shfl_xor_sync(FULL, pc, o);
-                    }
-                    const float q = pc > 0.0f ? ps / pc : 0.0f;
-                    if (u24(evx.y) < q) {
-                        if (tau > 0.0f) tau = tau * (pl / q);
-                        const float ta_ = t / dtA, tb_ = t / dtB;
-                        fa0 = dA > 0 ? fa0 + (ta_ - (float)nA) : fa0 - (ta_ - (float)nA);
-                        fb0 = dB > 0 ? fb0 + (tb_ - (float)nB) : fb0 - (tb_ - (float)nB);
-                        fa0 = fminf(fmaxf(fa0, 0.0f), 1.0f);
-                        fb0 = fminf(fmaxf(fb0, 0.0f), 1.0f);
-                        pw0 = fminf(fmaxf(fmaf(sW, t, pw0), __ldg(P.fw + cw)), __ldg(P.fw + cw + 1));
-                        hg_scatter(P.hg_g, evx.z, evx.w, &sW, &sA, &sB);
-                        dda_init();
-                        t = 0.0f;
-                    } else {
-                        if (tau > 0.0f) tau = tau * ((1.0f - pl) / (1.0f - q));
-                    }
-                    draw();
-                    tcol = t + mc_neglog(u24o(evx.x)) / sigbar;
                 }
                 vcur = vnext;
-                if constexpr (GEN) fvcur = fvnext;
                 if (!__any_sync(FULL, tau > 0.0f)) break;
-                if (steps >= (MG ? P.mg_steps : P.max_steps)) {
-                    if (!MG && tau > 0.0f) flags |= DNSMC_STATUS_STEP_CAP;
-                    break;
-                }
+                if (steps >= P.mg_steps) break;
             }
-            if constexpr (MG) {
+            {
                 // Coarse grids (the reference's grid switch, code/mc_gpu.cu:193-207):
                 // every lane continues from its own point with the reference's
                 // position-update march; lanes no longer share their cell
@@ -793,28 +665,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
             }
             if (TRACE && lane == 0) *P.trace_n = steps;
             isteps += (unsigned long long)steps;
-            float X = (wk * Ii) * D;
-            if (CV) {
-                // control variate: the ray's straight flight through the
-                // layer-mean medium (it does not depend on the march above)
-                float Jbar = 0.0f, tex0 = 0.0f;
-                const float2 *surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
-                const float I0 = __ldg(surp + w0).y;
-                surrogate_walk<MODE>(P, surp, w0, oW, sW0, nbnd, &Jbar, &tex0);
-                // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
-                const float Ya = wk * (Ii - Jbar);
-                const float Yb = wk * ((1.0f - tex0) * (Ii - I0));
-                if (MOM && active) {
-                    const double xd = X, ya = Ya, yb = Yb;
-                    s_mo[0][tid] += xd; s_mo[1][tid] += ya; s_mo[2][tid] += yb;
-                    s_mo[3][tid] = fma(xd, xd, s_mo[3][tid]); s_mo[4][tid] = fma(ya, ya, s_mo[4][tid]);
-                    s_mo[5][tid] = fma(yb, yb, s_mo[5][tid]); s_mo[6][tid] = fma(xd, ya, s_mo[6][tid]);
-                    s_mo[7][tid] = fma(xd, yb, s_mo[7][tid]); s_mo[8][tid] = fma(ya, yb, s_mo[8][tid]);
-                }
-                const float2 beta = P.beta ? P.beta[cell_out] : make_float2(1.0f, -1.0f);
-                X = X - beta.x * Ya;  // tallied: X - beta_a Y_a - beta_b Y_b; the
-                X = X - beta.y * Yb;  // means beta . E[Y] are added back at finalize
-            }
+            const float X = (wk * Ii) * D;
             if (active) {
                 ++my_rays;
                 if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
@@ -825,11 +676,6 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_kernel(const MarchParam
         if (TRACE) return;
         if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
         if (active) P.tally[cell_out] = make_double2(s_acc[0][tid], s_acc[1][tid]);
-        if (MOM && active) {
-            double *out = P.moments + cell_out * 9;
-#pragma unroll
-            for (int q = 0; q < 9; ++q) out[q] = s_mo[q][tid];
-        }
     }
     // per-warp counters and status
     for (int o = 16; o > 0; o >>= 1) {
@@ -870,43 +716,6 @@ inline int march_occupancy_one(void (*k)(const MarchParams), int threads, size_t
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, threads, smem) != cudaSuccess) return 0;
     return nb;
-}
-
-// Launch one march variant: the dispatch over (mode, trace, control variate,
-// moments) of one value of GEN; march_occupancy_gen the matching occupancy.
-template <bool GEN>
-int launch_march_variant(int mode, const MarchParams &p, int blocks, int threads, cudaStream_t st, bool trace, bool cv,
-                         bool mom) {
-    if (trace) { blocks = 1; threads = 32; mom = false; }
-    const size_t smem = march_smem(p, threads);
-#define DNSMC_L(M, T, C, O) return march_launch_one(march_kernel<M, T, C, O, GEN>, blocks, threads, smem, st, p)
-#define DNSMC_MODE(M)                                       \
-    if (trace) { if (cv) DNSMC_L(M, true, true, false); else DNSMC_L(M, true, false, false); } \
-    else if (cv) { if (mom) DNSMC_L(M, false, true, true); else DNSMC_L(M, false, true, false); } \
-    else DNSMC_L(M, false, false, false);
-    switch (mode) {
-        case MODE_GREY: DNSMC_MODE(MODE_GREY) break;
-        case MODE_T: DNSMC_MODE(MODE_T) break;
-        case MODE_TX: DNSMC_MODE(MODE_TX) break;
-        default: break;
-    }
-#undef DNSMC_MODE
-#undef DNSMC_L
-    return (int)cudaErrorInvalidValue;
-}
-
-template <bool GEN>
-int march_variant_occupancy(int mode, int threads, bool cv, bool mom, size_t smem) {
-    int nb = 0;
-#define DNSMC_O(M)                                                                                    \
-    nb = cv ? (mom ? march_occupancy_one(march_kernel<M, false, true, true, GEN>, threads, smem)      \
-                   : march_occupancy_one(march_kernel<M, false, true, false, GEN>, threads, smem))    \
-            : march_occupancy_one(march_kernel<M, false, false, false, GEN>, threads, smem)
-    if (mode == MODE_GREY) DNSMC_O(MODE_GREY);
-    if (mode == MODE_T) DNSMC_O(MODE_T);
-    if (mode == MODE_TX) DNSMC_O(MODE_TX);
-#undef DNSMC_O
-    return nb > 0 ? nb : 1;
 }
 
 }  // namespace dnsmc

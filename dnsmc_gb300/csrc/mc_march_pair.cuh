@@ -1,7 +1,7 @@
 // mc_march_pair.cuh -- the march on the fine grid (the reference's
 // kernel_fluid + march_ray, code/mc_gpu.cu:44-438), two cells per lane: the
-// absorbing gas with black walls, and (GEN) the general medium with
-// scattering particles and grey walls.
+// absorbing gas with black walls (march_pair_kernel), and the general medium
+// with scattering particles and grey walls (march_gen_kernel).
 //
 // A packet here is 64 cells of one wall-normal plane: tile_a cells along j
 // by tile_b = 64 / tile_a along k.  Lane l owns packet cells l and l + 32,
@@ -10,13 +10,18 @@
 // walk (which face is crossed next, every segment length) is the same for
 // all 64 cells: it is computed once per lane for two cells, and only the
 // per-cell work (field gather, k and Ib lookups, attenuation, tallies) is
-// done twice.  The arithmetic of each cell is exactly that of the one-cell
-// march in mc_march.cuh (which the multigrid march keeps), so the host
-// replay reproduces every cell bit for bit.  GEN adds, as in that march:
-// absorption k + fv a_band and scattering fv s_band per cell; weighted delta
-// tracking with a warp-shared decision (q = mean over the packet's live cells
-// of fv s_band / majorant, summed by each lane over its cells in order and
-// then across lanes); Henyey-Greenstein directions; grey diffuse walls.
+// done twice.  Every cell's arithmetic is the reference estimator's update
+// written with explicit fmaf, and the host replay (oracle/mc_oracle.cpp)
+// marches the same 64-cell packets, so it reproduces every cell bit for bit.
+//
+// march_gen_kernel is the same march for the general medium: absorption
+// k + fv a_band and scattering fv s_band per cell; weighted delta tracking
+// with a warp-shared decision (q = mean over the packet's live cells of
+// fv s_band / majorant, summed by each lane over its cells in order and then
+// across lanes; each cell's throughput is multiplied by p / q on a scatter
+// and (1 - p) / (1 - q) otherwise, so every cell's expectation is that of
+// ordinary delta tracking); Henyey-Greenstein directions; grey diffuse walls.
+// Every direction change restarts the walk from the current point.
 //
 // Its translation units (mc_march_pair.cu, mc_march_gen.cu) are compiled
 // with -fmad=false like the other march translation units.
