@@ -181,7 +181,7 @@ class Solver:
 
     def packet_shape(self) -> tuple[int, int]:
         """(tile_a, tile_b): cells of a packet along j and along k (64-cell
-        packets for the absorbing gas with black walls, 32 otherwise)."""
+        packets on the fine grid, 32 with grid_num > 1)."""
         a, b = ctypes.c_int(), ctypes.c_int()
         check(self._lib.dnsmc_packet_shape(self._h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value

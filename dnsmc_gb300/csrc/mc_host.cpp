@@ -1053,7 +1053,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     if (per_item && s->rays_np != P.n_packets)
         return fail(DNSMC_ERR_STATE,
                     "per-packet rays were set for %d packets, the solve has %d (the packet shape follows the "
-                    "march: particles, grey walls and grid levels use 32-cell packets): set the rays again",
+                    "march: grid levels use 32-cell packets): set the rays again",
                     s->rays_np, P.n_packets);
     if (per_item && s->rays_pg > 0) {
         if (s->rays_pg != P.n_groups)

@@ -217,7 +217,7 @@ int  dnsmc_set_particle_field(dnsmc_solver *s, const float *fv, int layout);
 int  dnsmc_set_region(dnsmc_solver *s, int i0, int i1, int j0, int j1, int k0,
                       int k1);
 /* Rays per cell per band group.  rays_per_packet (length = number of packets,
- * see dnsmc_packet_count) overrides it per packet of 32 cells when non-NULL.  */
+ * see dnsmc_packet_count) overrides it per packet when non-NULL.            */
 int  dnsmc_set_rays(dnsmc_solver *s, int rays_per_group,
                     const int *rays_per_packet);
 /* Ray counts per (band group, packet): rays[g * npackets + p], n_groups = the
@@ -246,10 +246,9 @@ int  dnsmc_set_rays_adaptive(dnsmc_solver *s, float rays_per_tau, int min_rays,
 int  dnsmc_get_rays_per_item(dnsmc_solver *s, int *n_groups, int *rays);
 int  dnsmc_packet_count(const dnsmc_solver *s, int *npackets);
 /* Packet shape of the next solve: tile_a cells along j by tile_b along k.  A
- * packet is 64 cells (two per lane of a warp) for the absorbing gas with
- * black walls on the fine grid, 32 cells with particles, grey walls or
- * grid_num > 1; the packet count and per-packet ray tables follow it.  No
- * reference counterpart (the reference runs one thread per cell).           */
+ * packet is 64 cells (two per lane of a warp) on the fine grid, 32 cells
+ * with grid_num > 1; the packet count and per-packet ray tables follow it.
+ * No reference counterpart (the reference runs one thread per cell).        */
 int  dnsmc_packet_shape(const dnsmc_solver *s, int *tile_a, int *tile_b);
 /* Enqueue a solve of every resident snapshot on the solver's stream and return.*/
 int  dnsmc_solve_async(dnsmc_solver *s);
