@@ -280,11 +280,19 @@ class Solver:
         i0, i1, j0, j1, k0, k1 = self._region
         return (self._nfields, k1 - k0, j1 - j0, i1 - i0)
 
-    def results(self):
-        """(Q, sigma): float64 arrays (nfields, nk, nj, ni) over the region."""
+    def results(self, out=None):
+        """(Q, sigma): float64 arrays (nfields, nk, nj, ni) over the region,
+        written into `out` = (Q, sigma) when given (C-contiguous float64 arrays
+        of that shape, e.g. the caller's persistent result arrays)."""
         shp = self._region_shape()
-        Q = np.zeros(shp, np.float64)
-        S = np.zeros(shp, np.float64)
+        if out is None:
+            Q = np.zeros(shp, np.float64)
+            S = np.zeros(shp, np.float64)
+        else:
+            Q, S = out
+            for a in (Q, S):
+                if a.shape != shp or a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"result arrays must be C-contiguous float64 of shape {shp}")
         check(self._lib.dnsmc_get_results(self._h, _dp(Q), _dp(S)))
         return Q, S
 

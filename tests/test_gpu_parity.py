@@ -477,3 +477,20 @@ def test_fields_checked_on_the_device():
     Q, _ = s.solve(timeout_s=60)
     assert np.isfinite(Q).all()
     s.close()
+
+
+def test_results_into_caller_arrays():
+    ni, nj, nk = 8, 32, 4
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=300, T_east=300, seed=4))
+    s.set_fields(smooth_field(ni, nj, nk, 400, 1200, 6))
+    s.set_rays(8)
+    Q, S = s.solve(timeout_s=60)
+    Qo, So = np.full_like(Q, np.nan), np.full_like(S, np.nan)
+    Q2, S2 = s.results(out=(Qo, So))
+    assert Q2 is Qo and S2 is So
+    np.testing.assert_array_equal(Qo, Q)
+    np.testing.assert_array_equal(So, S)
+    with pytest.raises(ValueError):
+        s.results(out=(np.zeros(5), So))
+    s.close()
