@@ -84,6 +84,45 @@ def test_cv_bitexact_table_x_with_beta():
     s.close()
 
 
+def test_cv_bitexact_table_t_only():
+    """A table without an x_H2O axis (k(band, g, T)): the march reads one
+    column per row and E[Y] comes from the T-only node sums; tallies stay
+    bit-exact and E[Y] matches its per-sample float64 definition."""
+    tb = synth.ck_table(nbands=8, nq=4, nT=20, nX=4, seed=13)
+    k3 = np.ascontiguousarray(tb["k"][..., 2])                 # x = 0.1 slice
+    s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=12, jmax=32, kmax=4, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=1, T_west=420, T_east=380, seed=17, n_groups=2, control_variate=1))
+    s.set_table(k3, tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"])
+    assert s.table_info()["nX"] == 1
+    T = smooth_field(12, 32, 4, 450, 1700, 23)
+    s.set_fields(T)
+    s.set_rays(32)
+    assert_bitexact_cv(s, T)
+    cv = s.cv_data()
+    from test_capi import alias_distribution
+    smp = s.sampling()
+    t = s.table()
+    Tg = tb["T0"] + tb["dT"] * np.arange(20)
+    nq = 4
+    scale = np.abs(cv["muY"]).max()
+    for (i, j, k) in ((0, 0, 0), (6, 9, 1), (11, 31, 3)):
+        for g in range(2):
+            p = alias_distribution(smp, g)
+            a, e_ = int(smp["group_start"][g]), int(smp["group_start"][g + 1])
+            acc = accB = 0.0
+            for e in range(a, e_):
+                b, gq = smp["band"][e], smp["gq"][e]
+                ki = np.interp(T[k, j, i], Tg, t["k"][b, gq, :, 0])
+                ib = np.interp(T[k, j, i], Tg, t["Ib"][b])
+                sid = b * nq + gq
+                acc += smp["W"][e] * p[e - a] * ki * (ib - cv["Jhat"][0, sid, i, 0])
+                accB += smp["W"][e] * p[e - a] * ki * (ib - cv["sur"][0, sid, i, 1]) * cv["Jhat"][0, sid, i, 1]
+            mu = cv["muY"][0, g, k, j, i]
+            assert abs(mu[0] - acc) <= 1e-4 * abs(acc) + 1e-9 * scale
+            assert abs(mu[1] - accB) <= 1e-4 * abs(accB) + 1e-9 * scale
+    s.close()
+
+
 def test_cv_quadrature_and_mean_match_oracle():
     tb = synth.ck_table(nbands=6, nq=4, nT=20, nX=4, seed=9)
     s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=12, jmax=32, kmax=4, Lx=2.0, Ly=6.28, Lz=3.14,
