@@ -54,6 +54,30 @@ __device__ __forceinline__ float mc_expm1(float x) {
     return fmaf(two_n, p, two_n - 1.0f);
 }
 
+// mc_expm1 of two arguments at once with paired FP32 instructions
+// (f32x2 add / mul / fma, each half rounded to nearest like its scalar
+// form): the same operations in the same order, so each half is
+// bit-identical to mc_expm1 of it.  Used for the two cells of a lane.
+__device__ __forceinline__ float2 mc_expm1_x2(float2 x) {
+    x.x = fmaxf(x.x, -87.0f);
+    x.y = fmaxf(x.y, -87.0f);
+    float2 n = __fmul2_rn(x, make_float2(1.44269504088896341f, 1.44269504088896341f));
+    n.x = rintf(n.x);
+    n.y = rintf(n.y);
+    // fmaf(-n, c, x) == fmaf(n, -c, x): the product only changes sign
+    float2 r = __ffma2_rn(n, make_float2(-0.693145751953125f, -0.693145751953125f), x);
+    r = __ffma2_rn(n, make_float2(-1.42860682030941723212e-6f, -1.42860682030941723212e-6f), r);
+    float2 q = __ffma2_rn(make_float2(1.39411131385713816e-3f, 1.39411131385713816e-3f), r,
+                          make_float2(8.36317520588636398e-3f, 8.36317520588636398e-3f));
+    q = __ffma2_rn(q, r, make_float2(4.16663736104965210e-2f, 4.16663736104965210e-2f));
+    q = __ffma2_rn(q, r, make_float2(1.66665762662887573e-1f, 1.66665762662887573e-1f));
+    q = __ffma2_rn(q, r, make_float2(0.5f, 0.5f));
+    float2 p = __ffma2_rn(q, r, make_float2(1.0f, 1.0f));
+    p = __fmul2_rn(p, r);
+    const float2 two_n = make_float2(__int_as_float(((int)n.x + 127) << 23), __int_as_float(((int)n.y + 127) << 23));
+    return __ffma2_rn(two_n, p, __fadd2_rn(two_n, make_float2(-1.0f, -1.0f)));
+}
+
 // sin and cos of x in [0, pi/4]: Taylor series to x^11 / x^12.
 __device__ __forceinline__ void mc_sincos_oct(float x, float *s, float *c) {
     const float z = x * x;

@@ -39,6 +39,7 @@ template <int MODE, bool TRACE, bool CV, bool MOM>
 __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const MarchParams P) {
     typedef typename FieldT<MODE>::type VT;
     constexpr int C = kLaneCells;  // cells per lane
+    static_assert(C % 2 == 0, "the attenuation goes through cell pairs");
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int tid = threadIdx.x;
@@ -219,6 +220,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 const int axis = sW_ ? 0 : (sA_ ? 1 : 2);
                 const float tn = sW_ ? tW : (sA_ ? tA : tB);
                 const float ds = tn - t;
+                const float nds = t - tn;  // minus the segment length (exact negation)
                 // next cell of the walk, and its field values fetched now; the
                 // axis is the same in every lane, but selects cost fewer
                 // instructions here than branches the compiler must treat as
@@ -241,35 +243,49 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     nrowB[k] = aB ? u * P.na : rowB[k];
                 }
                 const bool wall = aW && ncw == wallW;
+                // fetched for every cell, live or not (a dumped cell's value
+                // is never used): no default copy, no per-cell predicate; at
+                // a wall the row stays inside the grid and the walk ends
+                const int lrowW = wall ? rowW : nrowW;
                 VT vnext[C];
 #pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    vnext[k] = vcur[k];
-                    if (!wall && tau[k] > 0.0f) vnext[k] = load_field<MODE>(P, fbase, nrowW + nrowB[k] + nca);
-                }
+                for (int k = 0; k < C; ++k) vnext[k] = load_field<MODE>(P, fbase, lrowW + nrowB[k] + nca);
                 // attenuation and collected intensity of this segment; a cell
-                // already dumped (tau 0) adds exactly nothing
+                // already dumped (tau 0) adds exactly nothing.  Per cell:
+                // alpha = -expm1(-k ds), ta = tau alpha, D += ta g,
+                // tau -= ta, with g = (Ii - Ib_j) / Ii.  The two cells of a
+                // pair go through paired FP32 instructions with every sign
+                // moved onto an operand whose negation is exact: e =
+                // expm1(k * (t - tn)) = -alpha, nta = tau e = -ta,
+                // D += nta (-g), tau += nta -- the same roundings.
 #pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    lsteps += tau[k] > 0.0f ? 1u : 0u;
-                    float kj, gj;
-                    if constexpr (MODE == MODE_GREY) {
-                        const float t2 = vcur[k] * vcur[k];
-                        gj = (Ii[k] - t2 * t2) * invI[k];
-                        kj = P.kappa;
-                    } else {
-                        int kx, tj;
-                        float ftj, fxj;
-                        cell_coords<MODE>(vcur[k], &kx, &tj, &ftj, &fxj);
-                        kj = lookup_k<MODE>(slk, krow, kx, ftj, fxj);
-                        const float Ibj = lookup_ib(sli, tj, ftj);
-                        gj = (Ii[k] - Ibj) * invI[k];
+                for (int k = 0; k < C; k += 2) {
+                    float kj[2], ngj[2];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        lsteps += tau[k + h] > 0.0f ? 1u : 0u;
+                        if constexpr (MODE == MODE_GREY) {
+                            const float t2 = vcur[k + h] * vcur[k + h];
+                            ngj[h] = (t2 * t2 - Ii[k + h]) * invI[k + h];
+                            kj[h] = P.kappa;
+                        } else {
+                            int kx, tj;
+                            float ftj, fxj;
+                            cell_coords<MODE>(vcur[k + h], &kx, &tj, &ftj, &fxj);
+                            kj[h] = lookup_k<MODE>(slk, krow, kx, ftj, fxj);
+                            const float Ibj = lookup_ib(sli, tj, ftj);
+                            ngj[h] = (Ibj - Ii[k + h]) * invI[k + h];
+                        }
                     }
-                    const float alpha = -mc_expm1(-(kj * ds));
-                    const float ta = tau[k] * alpha;
-                    D[k] = fmaf(ta, gj, D[k]);
-                    tau[k] = tau[k] - ta;
-                    if (tau[k] < P.toll) { D[k] = fmaf(tau[k], gj, D[k]); tau[k] = 0.0f; }
+                    const float2 e = mc_expm1_x2(__fmul2_rn(make_float2(kj[0], kj[1]), make_float2(nds, nds)));
+                    const float2 nta = __fmul2_rn(make_float2(tau[k], tau[k + 1]), e);
+                    const float2 d2 = __ffma2_rn(nta, make_float2(ngj[0], ngj[1]), make_float2(D[k], D[k + 1]));
+                    const float2 t2 = __fadd2_rn(make_float2(tau[k], tau[k + 1]), nta);
+                    D[k] = d2.x; D[k + 1] = d2.y;
+                    tau[k] = t2.x; tau[k + 1] = t2.y;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                        if (tau[k + h] < P.toll) { D[k + h] = fmaf(-tau[k + h], ngj[h], D[k + h]); tau[k + h] = 0.0f; }
                 }
                 if (TRACE && lane == 0 && steps < P.trace_max) {
                     int *rec = P.trace_rec + 6 * steps;
@@ -384,6 +400,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
     typedef typename FieldT<MODE>::type VT;
     const float INF = __int_as_float(0x7f800000);
     constexpr int C = kLaneCells;  // cells per lane
+    static_assert(C % 2 == 0, "the attenuation goes through cell pairs");
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int tid = threadIdx.x;
@@ -597,6 +614,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                     tn = col ? tcol : tn;
                 }
                 const float ds = tn - t;
+                const float nds = t - tn;  // minus the segment length (exact negation)
                 // next cell of the walk, and its field values fetched now; the
                 // axis is the same in every lane, but selects cost fewer
                 // instructions here than branches the compiler must treat as
@@ -619,41 +637,51 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                     nrowB[k] = aB ? u * P.na : rowB[k];
                 }
                 const bool wall = aW && ncw == wallW;
+                // fetched for every cell, live or not (a dumped cell's value
+                // is never used); a collision keeps the cell, so the address
+                // is the current one, and at a wall the row stays inside the
+                // grid and the walk restarts or ends
+                const int lrowW = wall ? rowW : nrowW;
                 VT vnext[C];
                 float fvnext[C];
 #pragma unroll
                 for (int k = 0; k < C; ++k) {
-                    vnext[k] = vcur[k];
-                    fvnext[k] = fvcur[k];
-                    if (!wall && tau[k] > 0.0f && axis < 3) {
-                        vnext[k] = load_field<MODE>(P, fbase, nrowW + nrowB[k] + nca);
-                        if (P.fieldV) fvnext[k] = __ldg(P.fieldV + fbase + nrowW + nrowB[k] + nca);
-                    }
+                    vnext[k] = load_field<MODE>(P, fbase, lrowW + nrowB[k] + nca);
+                    fvnext[k] = P.fieldV ? __ldg(P.fieldV + fbase + lrowW + nrowB[k] + nca) : fvcur[k];
                 }
                 // attenuation and collected intensity of this segment; a cell
-                // already dumped (tau 0) adds exactly nothing
+                // already dumped (tau 0) adds exactly nothing.  The same
+                // paired update as the gas march: e = expm1(k * (t - tn)) =
+                // -alpha, nta = tau e = -ta, D += nta (-g), tau += nta.
 #pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    lsteps += tau[k] > 0.0f ? 1u : 0u;
-                    float kj, gj;
-                    if constexpr (MODE == MODE_GREY) {
-                        const float t2 = vcur[k] * vcur[k];
-                        gj = (Ii[k] - t2 * t2) * invI[k];
-                        kj = P.kappa;
-                    } else {
-                        int kx, tj;
-                        float ftj, fxj;
-                        cell_coords<MODE>(vcur[k], &kx, &tj, &ftj, &fxj);
-                        kj = lookup_k<MODE>(slk, krow, kx, ftj, fxj);
-                        const float Ibj = lookup_ib(sli, tj, ftj);
-                        gj = (Ii[k] - Ibj) * invI[k];
+                for (int k = 0; k < C; k += 2) {
+                    float kj[2], ngj[2];
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        lsteps += tau[k + h] > 0.0f ? 1u : 0u;
+                        if constexpr (MODE == MODE_GREY) {
+                            const float t2 = vcur[k + h] * vcur[k + h];
+                            ngj[h] = (t2 * t2 - Ii[k + h]) * invI[k + h];
+                            kj[h] = P.kappa;
+                        } else {
+                            int kx, tj;
+                            float ftj, fxj;
+                            cell_coords<MODE>(vcur[k + h], &kx, &tj, &ftj, &fxj);
+                            kj[h] = lookup_k<MODE>(slk, krow, kx, ftj, fxj);
+                            const float Ibj = lookup_ib(sli, tj, ftj);
+                            ngj[h] = (Ibj - Ii[k + h]) * invI[k + h];
+                        }
+                        kj[h] = fmaf(fvcur[k + h], pab, kj[h]);
                     }
-                    kj = fmaf(fvcur[k], pab, kj);
-                    const float alpha = -mc_expm1(-(kj * ds));
-                    const float ta = tau[k] * alpha;
-                    D[k] = fmaf(ta, gj, D[k]);
-                    tau[k] = tau[k] - ta;
-                    if (tau[k] < P.toll) { D[k] = fmaf(tau[k], gj, D[k]); tau[k] = 0.0f; }
+                    const float2 e = mc_expm1_x2(__fmul2_rn(make_float2(kj[0], kj[1]), make_float2(nds, nds)));
+                    const float2 nta = __fmul2_rn(make_float2(tau[k], tau[k + 1]), e);
+                    const float2 d2 = __ffma2_rn(nta, make_float2(ngj[0], ngj[1]), make_float2(D[k], D[k + 1]));
+                    const float2 t2 = __fadd2_rn(make_float2(tau[k], tau[k + 1]), nta);
+                    D[k] = d2.x; D[k + 1] = d2.y;
+                    tau[k] = t2.x; tau[k + 1] = t2.y;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                        if (tau[k + h] < P.toll) { D[k + h] = fmaf(-tau[k + h], ngj[h], D[k + h]); tau[k + h] = 0.0f; }
                 }
                 if (TRACE && lane == 0 && steps < P.trace_max) {
                     int *rec = P.trace_rec + 6 * steps;
