@@ -881,18 +881,22 @@ int upload_tables(dnsmc_solver *s) {
     CUDA_TRY(cudaMemcpyAsync(s->d_k.p, t.k.data(), t.k.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     CUDA_TRY(cudaMemcpyAsync(s->d_ib.p, t.Ib.data(), t.Ib.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
     // the march's per-sample slabs of paired values (value, difference to the
-    // next): k over [t][x] (or [t]), then Ib over [t] of the sample's band
+    // next): k over [t][x] -- rows t and t+1 side by side, one 16-byte entry
+    // per table cell -- (or over [t]), then Ib over [t] of the sample's band
     const int nS = t.nbands * t.nq;
-    const int klen = t.nX > 1 ? t.nT * (t.nX - 1) : t.nT - 1;
+    const int klen = t.nX > 1 ? 2 * (t.nT - 1) * (t.nX - 1) : t.nT - 1;
     const int len = (klen + (t.nT - 1) + 1) & ~1;
     std::vector<float2> sl((size_t)nS * len, make_float2(0.f, 0.f));
     for (int sid = 0; sid < nS; ++sid) {
         float2 *o = sl.data() + (size_t)sid * len;
         if (t.nX > 1) {
-            for (int ti = 0; ti < t.nT; ++ti)
+            for (int ti = 0; ti < t.nT - 1; ++ti)
                 for (int xi = 0; xi < t.nX - 1; ++xi) {
                     const float *r = t.k.data() + ((size_t)sid * t.nT + ti) * t.nX + xi;
-                    o[ti * (t.nX - 1) + xi] = make_float2(r[0], r[1] - r[0]);
+                    const float *r1 = r + t.nX;
+                    const int e = ti * (t.nX - 1) + xi;
+                    o[2 * e] = make_float2(r[0], r[1] - r[0]);
+                    o[2 * e + 1] = make_float2(r1[0], r1[1] - r1[0]);
                 }
         } else {
             for (int ti = 0; ti < t.nT - 1; ++ti) {

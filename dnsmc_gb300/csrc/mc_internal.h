@@ -51,9 +51,11 @@ struct MarchParams {
     // spectral tables
     int nbands, nT, nX;
     float T0, invdT, X0, invdX;
-    // per spectral sample (band*nq + g) one slab of slab_len float2: the k
-    // pairs [t][x] (k[x], k[x+1] - k[x]) or [t] (k[t], k[t+1] - k[t]) in the
-    // first slab_klen, then the band's Ib pairs [t] (Ib[t], Ib[t+1] - Ib[t]);
+    // per spectral sample (band*nq + g) one slab of slab_len float2: in the
+    // first slab_klen the k entries [t < nT-1][x < nX-1] of two pairs each,
+    // (k[t][x], k[t][x+1] - k[t][x]) and the same of row t+1, or the pairs
+    // [t] (k[t], k[t+1] - k[t]); then the band's Ib pairs [t] (Ib[t], Ib[t+1]
+    // - Ib[t]);
     // slab_len is even (16-byte rows).  Each warp copies its ray's slab into
     // shared memory: the march launches with warps * slab_len * 8 bytes.
     const float2 *slab;

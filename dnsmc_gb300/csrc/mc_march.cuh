@@ -150,16 +150,19 @@ __device__ __forceinline__ void pos_split(float p, int n, int *i, float *f) {
     *f = p - (float)ii;
 }
 
-// Paired tables: the k part of a sample's slab holds (k[t][x], k[t][x+1] -
-// k[t][x]) (x-tables) or (k[t], k[t+1] - k[t]), its Ib part (Ib[t], Ib[t+1] -
-// Ib[t]) of the sample's band, so a bilinear lookup is two 8-byte loads and
-// three fmaf (the differences are the same FP32 subtractions the
-// interpolation would do).  kidx = ti*(nX-1) + xi; row = nX - 1.  The march
-// reads them from the warp's copy of the slab in shared memory.
+// Paired tables: the k part of a sample's slab holds, per table cell
+// kidx = ti*(nX-1) + xi of an x-table, the 16-byte entry (k[t][x],
+// k[t][x+1] - k[t][x], k[t+1][x], k[t+1][x+1] - k[t+1][x]) for t = ti <=
+// nT - 2, or per ti the pair (k[t], k[t+1] - k[t]); its Ib part holds (Ib[t],
+// Ib[t+1] - Ib[t]) of the sample's band.  A bilinear lookup is one 16-byte
+// load and three fmaf (the differences are the same FP32 subtractions the
+// interpolation would do).  The march reads them from the warp's copy of the
+// slab in shared memory.
 template <int MODE>
-__device__ __forceinline__ float lookup_k(const float2 *ks, int row, int kidx, float ft, float fx) {
+__device__ __forceinline__ float lookup_k(const float2 *ks, int kidx, float ft, float fx) {
     if (MODE == MODE_TX) {
-        const float2 a = ks[kidx], b = ks[kidx + row];
+        const float4 v = reinterpret_cast<const float4 *>(ks)[kidx];
+        const float2 a = make_float2(v.x, v.y), b = make_float2(v.z, v.w);
         const float k0 = fmaf(fx, a.y, a.x);
         const float k1 = fmaf(fx, b.y, b.x);
         return fmaf(ft, k1 - k0, k0);
@@ -398,7 +401,6 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
     extern __shared__ float4 s_slab[];
     float2 *const slk = reinterpret_cast<float2 *>(s_slab) + (threadIdx.x >> 5) * P.slab_len;
     const float2 *const sli = slk + P.slab_klen;
-    const int krow = P.nX - 1;
     // the item's FP64 sums and the replicate's shift, in shared memory
     __shared__ double s_acc[3][256];
     __shared__ uint4 s_shift[256];
@@ -494,7 +496,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
                 load_slab(P, e.koff, slk, lane);
-                const float ki = lookup_k<MODE>(slk, krow, ki_i, ft_i, fx_i);
+                const float ki = lookup_k<MODE>(slk, ki_i, ft_i, fx_i);
                 Ii = lookup_ib(sli, ti_i, ft_i);
                 invI = Ii > 0.f ? 1.0f / Ii : 0.f;
                 wk = e.W * ki;
@@ -549,7 +551,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                         int kx, tj;
                         float ftj, fxj;
                         cell_coords<MODE>(vcur, &kx, &tj, &ftj, &fxj);
-                        kj = lookup_k<MODE>(slk, krow, kx, ftj, fxj);
+                        kj = lookup_k<MODE>(slk, kx, ftj, fxj);
                         const float Ibj = lookup_ib(sli, tj, ftj);
                         gj = (Ii - Ibj) * invI;
                     }
@@ -637,7 +639,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                                     int tj;
                                     float ftj;
                                     pos_split(pt, P.nT, &tj, &ftj);
-                                    kj = lookup_k<MODE_T>(slk, 0, tj, ftj, 0.0f);
+                                    kj = lookup_k<MODE_T>(slk, tj, ftj, 0.0f);
                                     gj = (Ii - lookup_ib(sli, tj, ftj)) * invI;
                                 }
                                 float dmin = dsx;

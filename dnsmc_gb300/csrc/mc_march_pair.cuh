@@ -53,7 +53,6 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
     extern __shared__ float4 s_slab[];
     float2 *const slk = reinterpret_cast<float2 *>(s_slab) + (threadIdx.x >> 5) * P.slab_len;
     const float2 *const sli = slk + P.slab_klen;
-    const int krow = P.nX - 1;
     // per-cell FP64 sums of the item (ray sum, sum of squares or of squared
     // replicate means, current replicate sum) and the replicate's shift:
     // shared memory, so registers hold the march's own working set
@@ -171,7 +170,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     int kx, ti;
                     float ft, fx;
                     cell_coords<MODE>(vcur[k], &kx, &ti, &ft, &fx);
-                    const float ki = lookup_k<MODE>(slk, krow, kx, ft, fx);
+                    const float ki = lookup_k<MODE>(slk, kx, ft, fx);
                     Ii[k] = lookup_ib(sli, ti, ft);
                     invI[k] = Ii[k] > 0.f ? 1.0f / Ii[k] : 0.f;
                     wk[k] = e.W * ki;
@@ -272,7 +271,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                             int kx, tj;
                             float ftj, fxj;
                             cell_coords<MODE>(vcur[k + h], &kx, &tj, &ftj, &fxj);
-                            kj[h] = lookup_k<MODE>(slk, krow, kx, ftj, fxj);
+                            kj[h] = lookup_k<MODE>(slk, kx, ftj, fxj);
                             const float Ibj = lookup_ib(sli, tj, ftj);
                             ngj[h] = (Ibj - Ii[k + h]) * invI[k + h];
                         }
@@ -414,7 +413,6 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
     extern __shared__ float4 s_slab[];
     float2 *const slk = reinterpret_cast<float2 *>(s_slab) + (threadIdx.x >> 5) * P.slab_len;
     const float2 *const sli = slk + P.slab_klen;
-    const int krow = P.nX - 1;
     // per-cell FP64 sums of the item (ray sum, sum of squares or of squared
     // replicate means, current replicate sum) and the replicate's shift:
     // shared memory, so registers hold the march's own working set
@@ -539,7 +537,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                     int kx, ti;
                     float ft, fx;
                     cell_coords<MODE>(vcur[k], &kx, &ti, &ft, &fx);
-                    float ki = lookup_k<MODE>(slk, krow, kx, ft, fx);
+                    float ki = lookup_k<MODE>(slk, kx, ft, fx);
                     ki = fmaf(fvcur[k], pab, ki);
                     Ii[k] = lookup_ib(sli, ti, ft);
                     invI[k] = Ii[k] > 0.f ? 1.0f / Ii[k] : 0.f;
@@ -667,7 +665,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                             int kx, tj;
                             float ftj, fxj;
                             cell_coords<MODE>(vcur[k + h], &kx, &tj, &ftj, &fxj);
-                            kj[h] = lookup_k<MODE>(slk, krow, kx, ftj, fxj);
+                            kj[h] = lookup_k<MODE>(slk, kx, ftj, fxj);
                             const float Ibj = lookup_ib(sli, tj, ftj);
                             ngj[h] = (Ibj - Ii[k + h]) * invI[k + h];
                         }
