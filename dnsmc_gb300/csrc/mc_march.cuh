@@ -31,17 +31,28 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1
 }
 
 // ---------------------------------------------------------------------------
-// expm1 for x <= 0: Cody-Waite reduction x = n*ln2 + r, |r| <= ln2/2, then
-// expm1(r) = r (1 + r g(r)) with g(r) = (e^r - 1 - r)/r^2 replaced by its
-// degree-4 minimax polynomial on [-ln2/2, ln2/2] (Remez exchange computed for
-// this project; |error| 6.2e-8 on g), then 2^n expm1(r) + (2^n - 1).  Only +,
-// *, fmaf and rintf: bit-identical on any IEEE-754 machine; within 2 ulp.
+// expm1 for x <= 0: Cody-Waite reduction x = n*ln2 + r, then expm1(r) =
+// r (1 + r g(r)) with g(r) = (e^r - 1 - r)/r^2 replaced by its degree-4
+// minimax polynomial on [-ln2/2, ln2/2] (Remez exchange computed for this
+// project; |error| 6.2e-8 on g), then 2^n expm1(r) + (2^n - 1).  n is
+// rounded by the shifter sh = fmaf(x, log2(e), 1.5 * 2^23): the sum lies in
+// [2^23, 2^24), where the float spacing is 1, so sh - 1.5 * 2^23 is an
+// integer within 1/2 (plus the fma's rounding) of x log2(e), and the low bits
+// of sh hold n itself, so 2^n is one integer multiply-add on them.  Only +,
+// *, fmaf and integer bit operations: bit-identical on any IEEE-754 machine.
 // ---------------------------------------------------------------------------
+constexpr float kExpShift = 12582912.0f;           // 1.5 * 2^23, bits 0x4B400000
+__device__ __forceinline__ float mc_pow2_from_shift(float sh) {
+    // bits(sh) = 0x4B400000 + n, so (n + 127) << 23 is bits(sh) << 23 plus a
+    // constant, modulo 2^32
+    return __uint_as_float((__float_as_uint(sh) << 23) + ((127u - 0x4B400000u) << 23));
+}
 __device__ __forceinline__ float mc_expm1(float x) {
-    x = fmaxf(x, -87.0f);
-    const float n = rintf(x * 1.44269504088896341f);
-    float r = fmaf(-n, 0.693145751953125f, x);
-    r = fmaf(-n, 1.42860682030941723212e-6f, r);
+    x = fmaxf(x, -87.0f);                          // n in [-126, 0]
+    const float sh = fmaf(x, 1.44269504088896341f, kExpShift);
+    const float n = sh - kExpShift;
+    float r = fmaf(n, -0.693145751953125f, x);
+    r = fmaf(n, -1.42860682030941723212e-6f, r);
     float q = 1.39411131385713816e-3f;
     q = fmaf(q, r, 8.36317520588636398e-3f);
     q = fmaf(q, r, 4.16663736104965210e-2f);
@@ -49,8 +60,7 @@ __device__ __forceinline__ float mc_expm1(float x) {
     q = fmaf(q, r, 0.5f);
     float p = fmaf(q, r, 1.0f);
     p = p * r;                                     // expm1(r)
-    const int ni = (int)n;                         // in [-126, 0]
-    const float two_n = __int_as_float((ni + 127) << 23);
+    const float two_n = mc_pow2_from_shift(sh);
     return fmaf(two_n, p, two_n - 1.0f);
 }
 
@@ -61,10 +71,9 @@ __device__ __forceinline__ float mc_expm1(float x) {
 __device__ __forceinline__ float2 mc_expm1_x2(float2 x) {
     x.x = fmaxf(x.x, -87.0f);
     x.y = fmaxf(x.y, -87.0f);
-    float2 n = __fmul2_rn(x, make_float2(1.44269504088896341f, 1.44269504088896341f));
-    n.x = rintf(n.x);
-    n.y = rintf(n.y);
-    // fmaf(-n, c, x) == fmaf(n, -c, x): the product only changes sign
+    const float2 sh = __ffma2_rn(x, make_float2(1.44269504088896341f, 1.44269504088896341f),
+                                 make_float2(kExpShift, kExpShift));
+    const float2 n = __fadd2_rn(sh, make_float2(-kExpShift, -kExpShift));
     float2 r = __ffma2_rn(n, make_float2(-0.693145751953125f, -0.693145751953125f), x);
     r = __ffma2_rn(n, make_float2(-1.42860682030941723212e-6f, -1.42860682030941723212e-6f), r);
     float2 q = __ffma2_rn(make_float2(1.39411131385713816e-3f, 1.39411131385713816e-3f), r,
@@ -74,7 +83,7 @@ __device__ __forceinline__ float2 mc_expm1_x2(float2 x) {
     q = __ffma2_rn(q, r, make_float2(0.5f, 0.5f));
     float2 p = __ffma2_rn(q, r, make_float2(1.0f, 1.0f));
     p = __fmul2_rn(p, r);
-    const float2 two_n = make_float2(__int_as_float(((int)n.x + 127) << 23), __int_as_float(((int)n.y + 127) << 23));
+    const float2 two_n = make_float2(mc_pow2_from_shift(sh.x), mc_pow2_from_shift(sh.y));
     return __ffma2_rn(two_n, p, __fadd2_rn(two_n, make_float2(-1.0f, -1.0f)));
 }
 

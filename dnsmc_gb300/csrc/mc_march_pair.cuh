@@ -188,7 +188,10 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             float tW = (__ldg(fwn + w0) - oW) * sinvW;
             // periodic wrap of the next j / k index: one compare per step
             const int wrapA = dA > 0 ? P.na : -1, resetA = dA > 0 ? 0 : P.na - 1;
-            const int wrapB = dB > 0 ? P.nb : -1, resetB = dB > 0 ? 0 : P.nb - 1;
+            // k moves as its row offset k * na: one step is +-na, the wrap
+            // compares against the offset one row past the end
+            const int dRowB = dB * P.na;
+            const int wrapRowB = dB > 0 ? P.nb * P.na : -P.na, resetRowB = dB > 0 ? 0 : (P.nb - 1) * P.na;
             const int wallW = dW > 0 ? P.nw : -1;  // the wall-normal index beyond the wall
             const int dRowW = dW * plane;
             const float dtA = P.da * invA, dtB = P.db * invB;
@@ -199,11 +202,10 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             // conversion per step
             float hA = 0.5f, hB = 0.5f;
             int cw = w0, ca = acl, rowW = rowW0;
-            int cb[C], rowB[C];
+            int rowB[C];
             float tau[C], D[C];
 #pragma unroll
             for (int k = 0; k < C; ++k) {
-                cb[k] = bcl[k];
                 rowB[k] = bcl[k] * P.na;
                 tau[k] = active[k] ? 1.0f : 0.0f;
                 D[k] = 0.0f;
@@ -225,7 +227,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 // instructions here than branches the compiler must treat as
                 // divergent
                 int ncw, nca, nrowW;
-                int ncb[C], nrowB[C];
+                int nrowB[C];
                 const bool aW = axis == 0, aA = axis == 1, aB = axis == 2;
                 ncw = aW ? cw + dW : cw;
                 nrowW = aW ? rowW + dRowW : rowW;
@@ -236,10 +238,9 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 }
 #pragma unroll
                 for (int k = 0; k < C; ++k) {
-                    int u = cb[k] + dB;
-                    u = u == wrapB ? resetB : u;
-                    ncb[k] = aB ? u : cb[k];
-                    nrowB[k] = aB ? u * P.na : rowB[k];
+                    int u = rowB[k] + dRowB;
+                    u = u == wrapRowB ? resetRowB : u;
+                    nrowB[k] = aB ? u : rowB[k];
                 }
                 const bool wall = aW && ncw == wallW;
                 // fetched for every cell, live or not (a dumped cell's value
@@ -313,7 +314,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     hB = aB ? hB + 1.0f : hB;
                     tB = hB * dtB;
 #pragma unroll
-                    for (int k = 0; k < C; ++k) { cb[k] = ncb[k]; rowB[k] = nrowB[k]; }
+                    for (int k = 0; k < C; ++k) rowB[k] = nrowB[k];
                 }
 #pragma unroll
                 for (int k = 0; k < C; ++k) vcur[k] = vnext[k];

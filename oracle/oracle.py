@@ -89,6 +89,7 @@ def load():
         lib.orc_packet_mc.argtypes = [ctypes.POINTER(PacketConfig), ctypes.c_int, _d, _d]
         lib.orc_packet_mc.restype = ctypes.c_int
         lib.orc_packet_trace.argtypes = [ctypes.POINTER(PacketConfig)] + [ctypes.c_int] * 5 + [_i32, _i, _u32]
+        lib.orc_expm1n.argtypes = [_f, _f, ctypes.c_longlong]
         _lib = lib
     return _lib
 
@@ -103,6 +104,15 @@ def philox(ctr, key):
     o = (ctypes.c_uint32 * 4)()
     load().orc_philox(c, k, o)
     return list(o)
+
+
+def expm1n(x) -> np.ndarray:
+    """The march's FP32 expm1 of x <= 0 (the same operations as the device's
+    mc_expm1), element by element."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    out = np.empty_like(x)
+    load().orc_expm1n(_fp(x), _fp(out), x.size)
+    return out
 
 
 def ref_faces(im: int, L: float, stretched: int = 1, im0: int | None = None) -> np.ndarray:

@@ -147,3 +147,20 @@ def test_cv_replay_isothermal_surrogate_cancels():
     tal0, _ = O.packet_mc(c, 1, ni * nj * nk)
     assert np.abs(tal[..., 0]).max() < 1e-4 * np.abs(tal0[..., 0]).max()
     s.close()
+
+
+def test_march_expm1_within_1p5_ulp():
+    """The march's FP32 expm1 (shifter-rounded Cody-Waite reduction, degree-4
+    minimax polynomial; the device runs the same operations) against float64
+    expm1 over x in [-90, 0], magnitudes from 1e-30 up: within 1.5 ulp of the
+    float32 result, and -1 exactly below the clamp at -87."""
+    rng = np.random.default_rng(0)
+    x = np.concatenate([-np.logspace(-30, np.log10(87.0), 200001), -rng.uniform(0, 90, 200000),
+                        [0.0, -0.0, -87.0, -100.0, -1e-45]]).astype(np.float32)
+    y = O.expm1n(x).astype(np.float64)
+    e = np.expm1(x.astype(np.float64))
+    ulp = np.spacing(np.abs(e).astype(np.float32)).astype(np.float64)
+    ulp[ulp == 0] = np.spacing(np.float32(0))
+    err = np.abs(y - e) / ulp
+    assert err.max() <= 1.5, (err.max(), x[np.argmax(err)])
+    assert np.all(O.expm1n(np.array([-88.0, -200.0, -1e30], np.float32)) == -1.0)
