@@ -1307,6 +1307,8 @@ int wait_done(dnsmc_solver *s, double timeout_s) {
     CUDA_TRY(cudaMemcpy(misc, s->d_misc.p, sizeof misc, cudaMemcpyDeviceToHost));
     CUDA_TRY(cudaMemcpy(s->h_counters, s->d_counters.p, sizeof s->h_counters, cudaMemcpyDeviceToHost));
     s->h_status = misc[1];
+    if (s->h_status & DNSMC_STATUS_COPY_TIMEOUT)
+        return fail(DNSMC_ERR_TIMEOUT, "solve failed: a march's table copy did not arrive within its bounded wait");
     return DNSMC_OK;
 }
 

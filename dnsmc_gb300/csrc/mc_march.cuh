@@ -351,14 +351,71 @@ __device__ __forceinline__ void ray_direction(uint4 x, float *sW, float *sA, flo
     *sB = st * sph;
 }
 
-// The sample's slab (k, then Ib of its band) into this warp's shared copy;
-// the previous ray's lookups are done first.
-__device__ __forceinline__ void load_slab(const MarchParams &P, int sid, float2 *slk, int lane) {
+// ---------------------------------------------------------------------------
+// The ray's table slab arrives by one bulk copy of the TMA engine
+// (cp.async.bulk, global -> this CTA's shared memory) that signals the warp's
+// transaction barrier (mbarrier) in shared memory; the warp waits on the
+// barrier's phase parity.  Each warp owns one barrier and one slab buffer.
+// ---------------------------------------------------------------------------
+// try_wait polls of the slab barrier before giving up (each poll may suspend
+// the thread for a while; the whole wait stays well under a second)
+constexpr int kSlabWaitPolls = 1 << 16;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Lane 0 initialises the warp's barrier (one arrival per phase: the issuing
+// lane's arrive.expect_tx) before the warp's first copy.
+__device__ __forceinline__ void slab_bar_init(uint64_t *bar, int lane) {
+    if (lane == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     __syncwarp();
-    const float4 *src = reinterpret_cast<const float4 *>(P.slab + (long long)sid * P.slab_len);
-    float4 *dst = reinterpret_cast<float4 *>(slk);
-    for (int q = lane; q < (P.slab_len >> 1); q += 32) dst[q] = __ldg(src + q);
+}
+
+// Bounded wait for the barrier phase of the given parity to complete.
+__device__ __forceinline__ bool slab_bar_wait(const uint64_t *bar, uint32_t parity) {
+    const uint32_t b = smem_addr(bar);
+    for (int it = 0; it < kSlabWaitPolls; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(b), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// The sample's slab (k, then Ib of its band; slab_len * 8 bytes, a multiple
+// of 16 at a 16-byte aligned address on both sides) into this warp's shared
+// copy.  The previous ray's lookups are done first (the warp converges, and
+// the async proxy is ordered after the generic one).  *phase is the warp's
+// barrier parity, flipped per copy.  A wait that runs out sets
+// DNSMC_STATUS_COPY_TIMEOUT, waits once more for the copy still in flight,
+// and the march carries on: the host reports the solve as failed.
+__device__ __forceinline__ void load_slab(const MarchParams &P, int sid, float2 *slk, int lane, uint64_t *bar,
+                                          uint32_t *phase, unsigned int *flags) {
     __syncwarp();
+    if (lane == 0) {
+        const uint32_t bytes = (uint32_t)P.slab_len * 8u;
+        const float2 *src = P.slab + (long long)sid * P.slab_len;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                     : "memory");
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_addr(slk)),
+                     "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                     : "memory");
+    }
+    if (!slab_bar_wait(bar, *phase)) {
+        *flags |= DNSMC_STATUS_COPY_TIMEOUT;
+        slab_bar_wait(bar, *phase);
+    }
+    *phase ^= 1u;
 }
 
 // One ray of a cell into its FP64 sums: the sum, and the sum of squares
@@ -413,6 +470,11 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
     // the item's FP64 sums and the replicate's shift, in shared memory
     __shared__ double s_acc[3][256];
     __shared__ uint4 s_shift[256];
+    // each warp's transaction barrier of its slab copies, and its parity
+    __shared__ uint64_t s_bar[8];
+    uint64_t *const sbar = &s_bar[threadIdx.x >> 5];
+    uint32_t sphase = 0;
+    slab_bar_init(sbar, lane);
     const int tid = threadIdx.x;
 
     for (;;) {
@@ -504,7 +566,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                 SpecEntry e = P.entries[gs + j];
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
-                load_slab(P, e.koff, slk, lane);
+                load_slab(P, e.koff, slk, lane, sbar, &sphase, &flags);
                 const float ki = lookup_k<MODE>(slk, ki_i, ft_i, fx_i);
                 Ii = lookup_ib(sli, ti_i, ft_i);
                 invI = Ii > 0.f ? 1.0f / Ii : 0.f;

@@ -58,6 +58,11 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
     // shared memory, so registers hold the march's own working set
     __shared__ double s_acc[3][C][256];
     __shared__ uint4 s_shift[256];
+    // each warp's transaction barrier of its slab copies, and its parity
+    __shared__ uint64_t s_bar[8];
+    uint64_t *const sbar = &s_bar[threadIdx.x >> 5];
+    uint32_t sphase = 0;
+    slab_bar_init(sbar, lane);
 
     for (;;) {
         long long item;
@@ -164,7 +169,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
                 sid = e.koff;
-                load_slab(P, sid, slk, lane);
+                load_slab(P, sid, slk, lane, sbar, &sphase, &flags);
 #pragma unroll
                 for (int k = 0; k < C; ++k) {
                     int kx, ti;
@@ -212,6 +217,11 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             }
             float t = 0.0f;
             int steps = 0;
+            // the step at which each cell was dumped (its live steps are that
+            // plus one; cells never dumped were live for every step)
+            int life[C];
+#pragma unroll
+            for (int k = 0; k < C; ++k) life[k] = 1 << 30;
             // unrolled by two: the current / next field values alternate
             // registers instead of being copied every step
 #pragma unroll 2
@@ -258,12 +268,12 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 // moved onto an operand whose negation is exact: e =
                 // expm1(k * (t - tn)) = -alpha, nta = tau e = -ta,
                 // D += nta (-g), tau += nta -- the same roundings.
+                bool dumped[C];  // after this step: tau 0 (dumped now or before)
 #pragma unroll
                 for (int k = 0; k < C; k += 2) {
                     float kj[2], ngj[2];
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        lsteps += tau[k + h] > 0.0f ? 1u : 0u;
                         if constexpr (MODE == MODE_GREY) {
                             const float t2 = vcur[k + h] * vcur[k + h];
                             ngj[h] = (t2 * t2 - Ii[k + h]) * invI[k + h];
@@ -284,8 +294,14 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     D[k] = d2.x; D[k + 1] = d2.y;
                     tau[k] = t2.x; tau[k + 1] = t2.y;
 #pragma unroll
-                    for (int h = 0; h < 2; ++h)
-                        if (tau[k + h] < P.toll) { D[k + h] = fmaf(-tau[k + h], ngj[h], D[k + h]); tau[k + h] = 0.0f; }
+                    for (int h = 0; h < 2; ++h) {
+                        dumped[k + h] = tau[k + h] < P.toll;
+                        if (dumped[k + h]) {
+                            D[k + h] = fmaf(-tau[k + h], ngj[h], D[k + h]);
+                            tau[k + h] = 0.0f;
+                            life[k + h] = min(life[k + h], steps);
+                        }
+                    }
                 }
                 if (TRACE && lane == 0 && steps < P.trace_max) {
                     int *rec = P.trace_rec + 6 * steps;
@@ -318,9 +334,10 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 }
 #pragma unroll
                 for (int k = 0; k < C; ++k) vcur[k] = vnext[k];
+                // a cell not dumped has tau >= toll > 0
                 bool alive = false;
 #pragma unroll
-                for (int k = 0; k < C; ++k) alive = alive || tau[k] > 0.0f;
+                for (int k = 0; k < C; ++k) alive = alive || !dumped[k];
                 if (!__any_sync(FULL, alive)) break;
                 if (steps >= P.max_steps) {
                     if (alive) flags |= DNSMC_STATUS_STEP_CAP;
@@ -328,6 +345,8 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 }
             }
             if (TRACE && lane == 0) *P.trace_n = steps;
+#pragma unroll
+            for (int k = 0; k < C; ++k) lsteps += active[k] ? (unsigned)min(life[k] + 1, steps) : 0u;
             isteps += (unsigned long long)steps;
             // control variate: the ray's straight flight through the
             // layer-mean medium, the same for both cells (same layer)
@@ -419,6 +438,11 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
     // shared memory, so registers hold the march's own working set
     __shared__ double s_acc[3][C][256];
     __shared__ uint4 s_shift[256];
+    // each warp's transaction barrier of its slab copies, and its parity
+    __shared__ uint64_t s_bar[8];
+    uint64_t *const sbar = &s_bar[threadIdx.x >> 5];
+    uint32_t sphase = 0;
+    slab_bar_init(sbar, lane);
 
     for (;;) {
         long long item;
@@ -531,7 +555,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
                 sid = e.koff;
-                load_slab(P, sid, slk, lane);
+                load_slab(P, sid, slk, lane, sbar, &sphase, &flags);
                 if (P.part) { const float2 pp = __ldg(P.part + nbnd); pab = pp.x; psc = pp.y; }
 #pragma unroll
                 for (int k = 0; k < C; ++k) {

@@ -53,6 +53,8 @@ extern "C" {
 #define DNSMC_STATUS_STEP_CAP   0x1u  /* a ray stopped at the per-ray step cap   */
 #define DNSMC_STATUS_NONFINITE  0x2u  /* a non-finite ray contribution was seen  */
 #define DNSMC_STATUS_BAD_FIELD  0x4u  /* a temperature <= 0 or NaN was supplied  */
+#define DNSMC_STATUS_COPY_TIMEOUT 0x8u /* a bounded wait for an on-chip table copy
+                                          ran out; the solve reports an error  */
 
 /* ---- spectral models (reference code/param.h:48-49, `grey`) -------------- */
 #define DNSMC_MODEL_CK         0  /* narrow-band correlated-k gas tables        */
