@@ -1081,9 +1081,9 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         int smax = 0;
         if (cudaDeviceGetAttribute(&smax, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device) != cudaSuccess)
             smax = 48 * 1024;
-        const size_t stat = 32 * 1024;  // the march kernels' static shared memory, at most
-        if (march_smem(P, threads) + stat > (size_t)smax) threads = 128;
-        if (march_smem(P, threads) + stat > (size_t)smax)
+        const size_t stat = 1024;  // the march kernels' static shared memory (barriers), at most
+        if (march_smem(P, threads, kLaneCells) + stat > (size_t)smax) threads = 128;
+        if (march_smem(P, threads, kLaneCells) + stat > (size_t)smax)
             return fail(DNSMC_ERR_TABLE, "a spectral sample's table slab (%d bytes) exceeds the shared memory of the march",
                         P.slab_len * 8);
     }
@@ -1179,7 +1179,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         P.item_order = s->d_order.p;
     }
     const int sms = device_sm_count();
-    const size_t smem = march_smem(P, threads);
+    const size_t smem = march_smem(P, threads, mg ? 1 : kLaneCells);
     const int occ = mg ? march_mg_occupancy(mode, threads, smem) : march_occupancy_ex(mode, threads, cv, mom, gen, smem);
     const int blocks = std::max(1, sms * occ);
 

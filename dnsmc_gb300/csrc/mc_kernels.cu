@@ -217,7 +217,7 @@ int march_occupancy_ex(int mode, int threads, bool cv, bool mom, bool gen, size_
 int launch_march_mg(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace) {
     cudaStream_t st = (cudaStream_t)stream;
     if (trace) { blocks = 1; threads = 32; }
-    const size_t smem = march_smem(p, threads);
+    const size_t smem = march_smem(p, threads, 1);
     if (mode == MODE_GREY) {
         if (trace) return march_launch_one(march_mg_kernel<MODE_GREY, true>, blocks, threads,
                                            smem, st, p);

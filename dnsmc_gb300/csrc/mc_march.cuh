@@ -463,19 +463,21 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
     const int plane = P.na * P.nb;
     unsigned long long my_rays = 0, my_steps = 0;
     unsigned int flags = 0;
-    // this warp's copy of the current ray's table slab (tabulated models)
-    extern __shared__ float4 s_slab[];
-    float2 *const slk = reinterpret_cast<float2 *>(s_slab) + (threadIdx.x >> 5) * P.slab_len;
+    const int tid = threadIdx.x;
+    // dynamic shared memory (march_smem, one cell per lane): this warp's copy
+    // of the current ray's table slab (tabulated models), the item's FP64
+    // sums [3][threads] and the replicate's shift [threads]
+    extern __shared__ float4 s_dyn[];
+    const int nthr = blockDim.x;
+    float2 *const slk = reinterpret_cast<float2 *>(s_dyn) + (threadIdx.x >> 5) * P.slab_len;
     const float2 *const sli = slk + P.slab_klen;
-    // the item's FP64 sums and the replicate's shift, in shared memory
-    __shared__ double s_acc[3][256];
-    __shared__ uint4 s_shift[256];
+    double *const s_acc = reinterpret_cast<double *>(reinterpret_cast<float2 *>(s_dyn) + ((nthr + 31) >> 5) * P.slab_len);
+    uint4 *const s_shift = reinterpret_cast<uint4 *>(s_acc + 3 * nthr);
     // each warp's transaction barrier of its slab copies, and its parity
     __shared__ uint64_t s_bar[8];
     uint64_t *const sbar = &s_bar[threadIdx.x >> 5];
     uint32_t sphase = 0;
     slab_bar_init(sbar, lane);
-    const int tid = threadIdx.x;
 
     for (;;) {
         long long item;
@@ -539,7 +541,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
         const long long tc = ((long long)(w0 - P.ew0) * nkR + (bcl - P.eb0)) * njR + (acl - P.ea0);
         const long long cell_out = fg * P.region_cells + tc;  // tally index of this lane's cell
         const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
-        s_acc[0][tid] = 0.0; s_acc[1][tid] = 0.0; s_acc[2][tid] = 0.0;
+        s_acc[tid] = 0.0; s_acc[nthr + tid] = 0.0; s_acc[2 * nthr + tid] = 0.0;
         unsigned long long isteps = 0;
         unsigned int lsteps = 0;  // this lane's active steps in the item
         int bcur = -1;
@@ -766,13 +768,13 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
             if (active) {
                 ++my_rays;
                 if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                tally_ray(P, (double)X, m, M, &s_acc[0][tid], &s_acc[1][tid], &s_acc[2][tid]);
+                tally_ray(P, (double)X, m, M, &s_acc[tid], &s_acc[nthr + tid], &s_acc[2 * nthr + tid]);
             }
         }
         my_steps += lsteps;
         if (TRACE) return;
         if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
-        if (active) P.tally[cell_out] = make_double2(s_acc[0][tid], s_acc[1][tid]);
+        if (active) P.tally[cell_out] = make_double2(s_acc[tid], s_acc[nthr + tid]);
     }
     // per-warp counters and status
     for (int o = 16; o > 0; o >>= 1) {

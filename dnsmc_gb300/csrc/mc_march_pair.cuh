@@ -49,15 +49,18 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
     const int plane = P.na * P.nb;
     unsigned long long my_rays = 0, my_steps = 0;
     unsigned int flags = 0;
-    // this warp's copy of the current ray's table slab (tabulated models)
-    extern __shared__ float4 s_slab[];
-    float2 *const slk = reinterpret_cast<float2 *>(s_slab) + (threadIdx.x >> 5) * P.slab_len;
-    const float2 *const sli = slk + P.slab_klen;
-    // per-cell FP64 sums of the item (ray sum, sum of squares or of squared
-    // replicate means, current replicate sum) and the replicate's shift:
+    // dynamic shared memory (march_smem): this warp's copy of the current
+    // ray's table slab (tabulated models); per-cell FP64 sums of the item
+    // (ray sum, sum of squares or of squared replicate means, current
+    // replicate sum) [3][C][threads] and the replicate's shift [threads] --
     // shared memory, so registers hold the march's own working set
-    __shared__ double s_acc[3][C][256];
-    __shared__ uint4 s_shift[256];
+    extern __shared__ float4 s_dyn[];
+    const int nthr = blockDim.x;
+    float2 *const slk = reinterpret_cast<float2 *>(s_dyn) + (threadIdx.x >> 5) * P.slab_len;
+    const float2 *const sli = slk + P.slab_klen;
+    double *const s_acc = reinterpret_cast<double *>(reinterpret_cast<float2 *>(s_dyn) + ((nthr + 31) >> 5) * P.slab_len);
+    uint4 *const s_shift = reinterpret_cast<uint4 *>(s_acc + 3 * C * nthr);
+    auto acc = [&](int q, int k) { return s_acc + (q * C + k) * nthr + tid; };
     // each warp's transaction barrier of its slab copies, and its parity
     __shared__ uint64_t s_bar[8];
     uint64_t *const sbar = &s_bar[threadIdx.x >> 5];
@@ -133,7 +136,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 for (int q = 0; q < 9; ++q) mo[k][q] = 0.0;
         const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
 #pragma unroll
-        for (int k = 0; k < C; ++k) { s_acc[0][k][tid] = 0.0; s_acc[1][k][tid] = 0.0; s_acc[2][k][tid] = 0.0; }
+        for (int k = 0; k < C; ++k) { *acc(0, k) = 0.0; *acc(1, k) = 0.0; *acc(2, k) = 0.0; }
         unsigned long long isteps = 0;
         unsigned int lsteps = 0;  // this lane's active cell-steps in the item
         int bcur = -1;
@@ -377,7 +380,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 if (active[k]) {
                     ++my_rays;
                     if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                    tally_ray(P, (double)X, m, M, &s_acc[0][k][tid], &s_acc[1][k][tid], &s_acc[2][k][tid]);
+                    tally_ray(P, (double)X, m, M, acc(0, k), acc(1, k), acc(2, k));
                 }
             }
         }
@@ -388,7 +391,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
         for (int k = 0; k < C; ++k) {
             if (!active[k]) continue;
             const long long o = fg * P.region_cells + tcell[k];
-            P.tally[o] = make_double2(s_acc[0][k][tid], s_acc[1][k][tid]);
+            P.tally[o] = make_double2(*acc(0, k), *acc(1, k));
             if (MOM) {
                 double *out = P.moments + o * 9;
 #pragma unroll
@@ -429,15 +432,18 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
     const int plane = P.na * P.nb;
     unsigned long long my_rays = 0, my_steps = 0;
     unsigned int flags = 0;
-    // this warp's copy of the current ray's table slab (tabulated models)
-    extern __shared__ float4 s_slab[];
-    float2 *const slk = reinterpret_cast<float2 *>(s_slab) + (threadIdx.x >> 5) * P.slab_len;
-    const float2 *const sli = slk + P.slab_klen;
-    // per-cell FP64 sums of the item (ray sum, sum of squares or of squared
-    // replicate means, current replicate sum) and the replicate's shift:
+    // dynamic shared memory (march_smem): this warp's copy of the current
+    // ray's table slab (tabulated models); per-cell FP64 sums of the item
+    // (ray sum, sum of squares or of squared replicate means, current
+    // replicate sum) [3][C][threads] and the replicate's shift [threads] --
     // shared memory, so registers hold the march's own working set
-    __shared__ double s_acc[3][C][256];
-    __shared__ uint4 s_shift[256];
+    extern __shared__ float4 s_dyn[];
+    const int nthr = blockDim.x;
+    float2 *const slk = reinterpret_cast<float2 *>(s_dyn) + (threadIdx.x >> 5) * P.slab_len;
+    const float2 *const sli = slk + P.slab_klen;
+    double *const s_acc = reinterpret_cast<double *>(reinterpret_cast<float2 *>(s_dyn) + ((nthr + 31) >> 5) * P.slab_len);
+    uint4 *const s_shift = reinterpret_cast<uint4 *>(s_acc + 3 * C * nthr);
+    auto acc = [&](int q, int k) { return s_acc + (q * C + k) * nthr + tid; };
     // each warp's transaction barrier of its slab copies, and its parity
     __shared__ uint64_t s_bar[8];
     uint64_t *const sbar = &s_bar[threadIdx.x >> 5];
@@ -513,7 +519,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                 for (int q = 0; q < 9; ++q) mo[k][q] = 0.0;
         const int M = P.sampler ? max(1, N / max(1, P.nbatch)) : 1;
 #pragma unroll
-        for (int k = 0; k < C; ++k) { s_acc[0][k][tid] = 0.0; s_acc[1][k][tid] = 0.0; s_acc[2][k][tid] = 0.0; }
+        for (int k = 0; k < C; ++k) { *acc(0, k) = 0.0; *acc(1, k) = 0.0; *acc(2, k) = 0.0; }
         unsigned long long isteps = 0;
         unsigned int lsteps = 0;  // this lane's active cell-steps in the item
         int bcur = -1;
@@ -850,7 +856,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                 if (active[k]) {
                     ++my_rays;
                     if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                    tally_ray(P, (double)X, m, M, &s_acc[0][k][tid], &s_acc[1][k][tid], &s_acc[2][k][tid]);
+                    tally_ray(P, (double)X, m, M, acc(0, k), acc(1, k), acc(2, k));
                 }
             }
         }
@@ -861,7 +867,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
         for (int k = 0; k < C; ++k) {
             if (!active[k]) continue;
             const long long o = fg * P.region_cells + tcell[k];
-            P.tally[o] = make_double2(s_acc[0][k][tid], s_acc[1][k][tid]);
+            P.tally[o] = make_double2(*acc(0, k), *acc(1, k));
             if (MOM) {
                 double *out = P.moments + o * 9;
 #pragma unroll
@@ -896,7 +902,7 @@ int launch_march_cells(int mode, const MarchParams &p, int blocks, int threads, 
                        bool mom) {
     cudaStream_t st = (cudaStream_t)stream;
     if (trace) { blocks = 1; threads = 32; mom = false; }
-    const size_t smem = march_smem(p, threads);
+    const size_t smem = march_smem(p, threads, kLaneCells);
 #define DNSMC_L(M, T, CV_, O) \
     return march_launch_one(march_cells_kernel<M, T, CV_, O, GEN>::fn, blocks, threads, smem, st, p)
 #define DNSMC_MODE(M)                                                                                  \
