@@ -565,7 +565,7 @@ def run_c4(args):
 # DRAM bytes (read + write) of one march launch measured by an ncu capture of
 # the default command (128^3, network control variate): the tallies and L2
 # refills, not the gathers, which L1/L2 serve
-MARCH_DRAM_BYTES = {("net", 128): 185.43e6 + 250.26e6}
+MARCH_DRAM_BYTES = {("net", 128): 189.37e6 + 252.66e6}
 
 # kernels per step: table coordinates, march, finalize; the control variate adds
 # layer means, surrogate table, 1-D quadrature and E[Y]; the network adds
