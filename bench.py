@@ -463,7 +463,9 @@ def run_batched(args, flushbuf_mb=256):
                      "traffic": None, "peak_kind": peak_kind},
         "cpu_baseline": None,
         "e2e": None,
-        "gpu_launches": 7 * args.steps,
+        # per replay: coordinates, 3 + 2 control-variate kernels, 3 queue-order
+        # kernels (adaptive per-packet rays), march, reciprocals, finalize
+        "gpu_launches": 12 * args.steps,
         "clocks": clk.summary(),
     }
     print(json.dumps(out), flush=True)
@@ -568,10 +570,11 @@ def run_c4(args):
 MARCH_DRAM_BYTES = {("net", 128): 189.37e6 + 252.66e6}
 
 # kernels per step: table coordinates, march, finalize; the control variate adds
-# layer means, surrogate table, 1-D quadrature and E[Y]; the network adds
-# features, MLP, coefficients/costs, three allocation kernels and the three
-# kernels of the longest-first queue order
-LAUNCHES = {"plain": 3, "cv": 7, "net": 16}
+# layer means, surrogate table, 1-D quadrature and the two E[Y] kernels (node
+# sums, cells); per-packet ray counts (the network's) add the three kernels of
+# the longest-first queue order and the finalize's reciprocals of the counts;
+# the network adds features, MLP, coefficients and three allocation kernels
+LAUNCHES = {"plain": 3, "cv": 8, "net": 18}
 
 
 def main():

@@ -387,6 +387,7 @@ struct dnsmc_solver {
     bool rays_dev = false;                   // d_rays_pp was written on the device (no host copy)
     int rays_np = 0;                         // packets the per-packet / per-item rays were set for
     DevBuf<int> d_rays_pp;
+    DevBuf<double2> d_rays_rcp;              // (1/N, 1/(N-1)) of d_rays_pp, written by the finalize launch
     DevBuf<unsigned long long> d_item_steps; // steps per (field, group, packet) of the last solve
     DevBuf<unsigned int> d_order, d_order_hist;  // longest-first queue order (per-item ray tables)
     DevBuf<float> d_kP;                      // Planck-mean absorption coefficient on the table grid
@@ -1191,6 +1192,10 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     F.rays = s->rays; F.rays_per_packet = P.rays_per_packet; F.rays_gstride = P.rays_gstride;
     F.batched = c.sampler == DNSMC_SAMPLER_RQMC;
     F.nbatch = c.nvar;
+    if (F.rays_per_packet) {
+        TRY(s->d_rays_rcp.ensure((size_t)finalize_rcp_count(F)));
+        F.rcp = s->d_rays_rcp.p;
+    }
     F.group_empty = s->d_group_empty.p;
     F.tally = s->d_tally.p;
     F.muY = cv ? s->d_muY.p : nullptr;
@@ -1602,7 +1607,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_cv_grp.release(); s->d_cv_sid.release(); s->d_cv_C.release(); s->d_layer.release();
     s->d_sur.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_cvnodes.release(); s->d_kd.release(); s->d_ibd.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release();
-    s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_item_steps.release(); s->d_kP.release();
+    s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_rays_rcp.release(); s->d_item_steps.release(); s->d_kP.release();
     s->d_order.release(); s->d_order_hist.release();
     s->d_mgT.release(); s->d_mgfw.release();
     s->d_part.release(); s->d_fieldV.release(); s->d_layerV.release();

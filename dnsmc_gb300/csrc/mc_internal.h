@@ -126,6 +126,11 @@ struct FinalizeParams {
     const int *rays_per_packet;  // [g * rays_gstride + packet]
     int rays_gstride;
     int batched, nbatch;      // RQMC: variance from nbatch replicate means
+    // reciprocals (1/N, 1/(N-1)) of the ray counts: per [g * rays_gstride +
+    // packet] of rays_per_packet (device scratch, filled by launch_finalize),
+    // of the uniform count and of nbatch (set by launch_finalize)
+    double2 *rcp;
+    double2 rcp_uniform, rcp_batch;
     const int *group_empty;   // 1 when the group has no emission
     const double2 *tally;
     const double2 *muY;       // (E[Y_a], E[Y_b]), tally layout, or null
@@ -137,6 +142,12 @@ struct FinalizeParams {
     double *varg;             // [f][group][cell] or nullptr
     unsigned int *status;
 };
+
+// Entries of FinalizeParams::rcp: the indices g * rays_gstride + packet
+// (rays_gstride 0: one count per packet for every group).
+inline long long finalize_rcp_count(const FinalizeParams &f) {
+    return (long long)(f.n_groups - 1) * f.rays_gstride + (long long)f.niR * f.npb * f.npa;
+}
 
 // A read-only view of a solver's device state for the control-variate
 // network (mc_cvnet.cu); filled by solver_view (mc_host.cpp).

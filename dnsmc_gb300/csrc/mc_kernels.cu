@@ -90,14 +90,16 @@ __global__ void finalize_kernel(const FinalizeParams F) {
             const int N = F.rays_per_packet ? F.rays_per_packet[g * F.rays_gstride + p] : F.rays;
             double m = 0.0, v = 0.0;
             if (!F.group_empty[g] && N > 0) {
+                // divisions by the ray counts as products with their
+                // reciprocals (FP64 division is a long sequence on this GPU)
+                const double2 r = F.rays_per_packet ? F.rcp[g * F.rays_gstride + p] : F.rcp_uniform;
                 const long long ti = ((long long)f * F.n_groups + g) * F.region_cells + tc;
                 const double2 t = F.tally[ti];
-                m = t.x / N;
+                m = t.x * r.x;
                 if (F.batched) {
-                    const int B = F.nbatch;
-                    if (B > 1) v = fmax(0.0, t.y / B - m * m) / (B - 1);
+                    if (F.nbatch > 1) v = fmax(0.0, t.y * F.rcp_batch.x - m * m) * F.rcp_batch.y;
                 } else if (N > 1) {
-                    v = fmax(0.0, t.y / N - m * m) / (N - 1);
+                    v = fmax(0.0, t.y * r.x - m * m) * r.y;
                 }
             }
             if (F.muY && !F.group_empty[g]) {
@@ -349,11 +351,16 @@ __global__ void cv_sur_kernel(const CvParams c) {
 
 // Direction-averaged surrogate intensity Jhat per (field, sample, layer):
 // composite Gauss-Legendre in mu on each hemisphere, 1-D march through the
-// layers with the same toll cut-off and wall emission as the 3-D walk.
+// layers with the same toll cut-off and wall emission as the 3-D walk.  One
+// warp per (field, sample, layer): lane l takes the paths (hemisphere, node)
+// l, l + 32, ... of the 2 * nquad, and the FP64 weighted sums are reduced
+// across the warp (butterfly order).
 __global__ void cv_jhat_kernel(const CvParams c) {
     const long long n = (long long)c.nfields * c.n_samples * c.nw;
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
-         idx += (long long)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const long long wpb = blockDim.x >> 5;
+    const int npath = 2 * c_nquad;
+    for (long long idx = blockIdx.x * wpb + (threadIdx.x >> 5); idx < n; idx += (long long)gridDim.x * wpb) {
         const int w = (int)(idx % c.nw);
         const long long fs = idx / c.nw;
         const int sid = (int)(fs % c.n_samples);
@@ -361,36 +368,42 @@ __global__ void cv_jhat_kernel(const CvParams c) {
         const int band = c.mode == MODE_GREY ? 0 : sid / c.nq;
         const float oW = (__ldg(c.fw + w) + __ldg(c.fw + w + 1)) * 0.5f;
         double acc = 0.0, accA = 0.0;
-        for (int h = 0; h < 2; ++h) {
+        for (int path = lane; path < npath; path += 32) {
+            const int h = path >= c_nquad ? 1 : 0;
+            const int q = path - h * c_nquad;
             const int dir = h ? 1 : -1;
             const float Iw = c.mode == MODE_GREY ? c.Tw4[h] : __ldg(c.ibw + h * c.nbands + band);
-            for (int q = 0; q < c_nquad; ++q) {
-                const float inv_mu = (float)(1.0 / c_quad_mu[q]);
-                float tau = 1.0f, J = 0.0f, t0 = 0.0f, dcum = 0.0f;
-                int l = w;
-                float seg = dir > 0 ? (__ldg(c.fw + w + 1) - oW) : (oW - __ldg(c.fw + w));
-                for (;;) {
-                    const float2 kv = sp[l];
-                    const float opt = kv.x * seg * inv_mu;
-                    if (dcum + opt > c.dtoll) { J = fmaf(tau, kv.y, J); break; }  // truncated in layer l
-                    const float a = -expm1f(-opt);
-                    const float ta = tau * a;
-                    J = fmaf(ta, kv.y, J);
-                    tau = tau - ta;
-                    dcum = dcum + opt;
-                    if (l == w) t0 = tau;  // transmissivity leaving the own layer
-                    l += dir;
-                    if (l < 0 || l >= c.nw) { J = fmaf(tau, Iw, J); break; }
-                    seg = __ldg(c.fw + l + 1) - __ldg(c.fw + l);
-                }
-                acc += c_quad_w[q] * (double)J;
-                accA += c_quad_w[q] * (1.0 - (double)t0);
+            const float inv_mu = (float)(1.0 / c_quad_mu[q]);
+            float tau = 1.0f, J = 0.0f, t0 = 0.0f, dcum = 0.0f;
+            int l = w;
+            float seg = dir > 0 ? (__ldg(c.fw + w + 1) - oW) : (oW - __ldg(c.fw + w));
+            for (;;) {
+                const float2 kv = sp[l];
+                const float opt = kv.x * seg * inv_mu;
+                if (dcum + opt > c.dtoll) { J = fmaf(tau, kv.y, J); break; }  // truncated in layer l
+                const float a = -expm1f(-opt);
+                const float ta = tau * a;
+                J = fmaf(ta, kv.y, J);
+                tau = tau - ta;
+                dcum = dcum + opt;
+                if (l == w) t0 = tau;  // transmissivity leaving the own layer
+                l += dir;
+                if (l < 0 || l >= c.nw) { J = fmaf(tau, Iw, J); break; }
+                seg = __ldg(c.fw + l + 1) - __ldg(c.fw + l);
             }
+            acc += c_quad_w[q] * (double)J;
+            accA += c_quad_w[q] * (1.0 - (double)t0);
         }
-        const double J = 0.5 * acc;
-        const float Jhi = (float)J;
-        c.Jhat[idx] = make_double2(J, 0.5 * accA);
-        c.Jf[idx] = make_float4(Jhi, (float)(J - (double)Jhi), (float)(0.5 * accA), sp[w].y);
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            accA += __shfl_xor_sync(0xffffffffu, accA, o);
+        }
+        if (lane == 0) {
+            const double J = 0.5 * acc;
+            const float Jhi = (float)J;
+            c.Jhat[idx] = make_double2(J, 0.5 * accA);
+            c.Jf[idx] = make_float4(Jhi, (float)(J - (double)Jhi), (float)(0.5 * accA), sp[w].y);
+        }
     }
 }
 
@@ -793,7 +806,7 @@ int launch_cv_prepare(const CvParams &c, void *stream) {
     cv_layer_kernel<<<dim3(c.nw, c.nfields), 256, 0, st>>>(c);
     const long long n = (long long)c.nfields * c.n_samples * c.nw;
     cv_sur_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
-    cv_jhat_kernel<<<grid_for(n, 128), 128, 0, st>>>(c);
+    cv_jhat_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(c);  // one warp per (field, sample, layer)
     return (int)cudaGetLastError();
 }
 
@@ -819,9 +832,28 @@ int launch_field_pos(const float *fT, const float2 *fTX, int2 *outP, int4 *outPX
     return (int)cudaGetLastError();
 }
 
+// (1/N, 1/(N-1)) of every ray count (0 where undefined)
+__global__ void ray_reciprocals_kernel(const int *rays, long long n, double2 *out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int N = rays[i];
+        out[i] = make_double2(N > 0 ? 1.0 / N : 0.0, N > 1 ? 1.0 / (N - 1) : 0.0);
+    }
+}
+
+static double2 reciprocals(int N) { return make_double2(N > 0 ? 1.0 / N : 0.0, N > 1 ? 1.0 / (N - 1) : 0.0); }
+
 int launch_finalize(const FinalizeParams &p, void *stream) {
-    const long long n = (long long)p.nfields * p.region_cells;
-    finalize_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(p);
+    FinalizeParams q = p;
+    q.rcp_uniform = reciprocals(p.rays);
+    q.rcp_batch = reciprocals(p.nbatch);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (q.rays_per_packet) {
+        if (!q.rcp) return (int)cudaErrorInvalidValue;
+        const long long nr = finalize_rcp_count(q);
+        ray_reciprocals_kernel<<<grid_for(nr, 256), 256, 0, st>>>(q.rays_per_packet, nr, q.rcp);
+    }
+    const long long n = (long long)q.nfields * q.region_cells;
+    finalize_kernel<<<grid_for(n, 256), 256, 0, st>>>(q);
     return (int)cudaGetLastError();
 }
 

@@ -20,7 +20,7 @@ import pytest
 import dnsmc_gb300 as D
 from dnsmc_gb300 import synth
 from oracle import oracle as O
-from test_gpu_parity import region_tally_to_dense, rays_per_cell, smooth_field
+from test_gpu_parity import group_mean_var, region_tally_to_dense, rays_per_cell, smooth_field
 
 pytestmark = pytest.mark.gpu
 
@@ -44,11 +44,7 @@ def assert_bitexact_cv(s, T, x=None):
     B = s.cfg.nvar
     for g in range(ng):
         N = rays_per_cell(s, g)
-        m = tal[:, g, ..., 0] / N
-        if s.cfg.sampler == D.SAMPLER_RQMC:
-            v = np.maximum(0.0, tal[:, g, ..., 1] / B - m * m) / (B - 1)
-        else:
-            v = np.maximum(0.0, tal[:, g, ..., 1] / N - m * m) / (N - 1)
+        m, v = group_mean_var(tal[:, g], N, B, s.cfg.sampler == D.SAMPLER_RQMC)
         m = m + beta[:, g, ..., 0].astype(np.float64) * muY[:, g, ..., 0]
         m = m + beta[:, g, ..., 1].astype(np.float64) * muY[:, g, ..., 1]
         np.testing.assert_array_equal(Qg[:, g], m)

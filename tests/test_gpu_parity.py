@@ -62,6 +62,23 @@ def packet_index(solver):
     return (ii * npb + kk // tb) * npa + jj // ta
 
 
+def group_mean_var(tal_g, N, B, rqmc):
+    """The finalize's mean and variance of the mean of one band group from
+    its (sum, sum of squares | sum of squared replicate means) tally, with
+    the divisions by the ray counts done as products with the float64
+    reciprocals, as the device does."""
+    N = np.asarray(N)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        rN = np.where(N > 0, 1.0 / N, 0.0)
+        rN1 = np.where(N > 1, 1.0 / (N - 1), 0.0)
+        m = np.where(N > 0, tal_g[..., 0] * rN, 0.0)
+        if rqmc:
+            v = np.where(N > 0, np.maximum(0.0, tal_g[..., 1] * (1.0 / B) - m * m) * (1.0 / (B - 1)), 0.0)
+        else:
+            v = np.where(N > 1, np.maximum(0.0, tal_g[..., 1] * rN - m * m) * rN1, 0.0)
+    return m, v
+
+
 def rays_per_cell(solver, g=0):
     i0, i1, j0, j1, k0, k1 = solver._region
     ni, nj, nk = i1 - i0, j1 - j0, k1 - k0
@@ -90,12 +107,7 @@ def assert_bitexact(solver, T, x=None):
     B = solver.cfg.nvar
     for g in range(ng):
         N = rays_per_cell(solver, g)
-        with np.errstate(invalid="ignore", divide="ignore"):
-            m = np.where(N > 0, tal[:, g, ..., 0] / N, 0.0)
-            if solver.cfg.sampler == D.SAMPLER_RQMC:
-                v = np.where(N > 0, np.maximum(0.0, tal[:, g, ..., 1] / B - m * m) / (B - 1), 0.0)
-            else:
-                v = np.where(N > 1, np.maximum(0.0, tal[:, g, ..., 1] / N - m * m) / (N - 1), 0.0)
+        m, v = group_mean_var(tal[:, g], N, B, solver.cfg.sampler == D.SAMPLER_RQMC)
         if empty[g]:
             m, v = np.zeros_like(m), np.zeros_like(v)
         np.testing.assert_array_equal(Qg[:, g], m)

@@ -21,7 +21,7 @@ import pytest
 import dnsmc_gb300 as D
 from dnsmc_gb300 import synth
 from oracle import oracle as O
-from test_gpu_parity import region_tally_to_dense, rays_per_cell, smooth_field
+from test_gpu_parity import group_mean_var, region_tally_to_dense, rays_per_cell, smooth_field
 
 pytestmark = pytest.mark.gpu
 
@@ -44,11 +44,7 @@ def check_bitexact(s, T, x=None, fv=None):
     muY = s.cv_data()["muY"] if cv else None
     for g in range(ng):
         N = rays_per_cell(s, g)
-        m = tal[:, g, ..., 0] / N
-        if s.cfg.sampler == D.SAMPLER_RQMC:
-            v = np.maximum(0.0, tal[:, g, ..., 1] / B - m * m) / (B - 1)
-        else:
-            v = np.maximum(0.0, tal[:, g, ..., 1] / N - m * m) / (N - 1)
+        m, v = group_mean_var(tal[:, g], N, B, s.cfg.sampler == D.SAMPLER_RQMC)
         if cv:
             m = m + 1.0 * muY[:, g, ..., 0]
             m = m + (-1.0) * muY[:, g, ..., 1]
