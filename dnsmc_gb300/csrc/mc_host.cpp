@@ -940,12 +940,16 @@ int lane_cells(const dnsmc_solver *s) {
 }
 
 // Packet tiling of the region: tile_a cells along j (a divisor of 32), by
-// tile_b = 32 * lane_cells / tile_a along k.
+// tile_b = 32 * lane_cells / tile_a along k.  Automatic: square 8 x 8
+// packets for the two-cell march (its cells lie closest together: more even
+// costs inside a packet for the per-packet ray counts, fewer idle lanes),
+// 16 x 4 or 32 x 2 when k has fewer than 8 / 4 cells; the widest row that
+// fits for the one-cell multigrid march.
 void tiling(const dnsmc_solver *s, int *ta, int *tb, int *npa, int *npb, int *npw) {
     int ni, nj, nk;
     region_dims(s, &ni, &nj, &nk);
     int a = s->cfg.tile_a;
-    if (!a) a = nj >= 32 ? 32 : (nj >= 16 ? 16 : 8);
+    if (!a) a = lane_cells(s) > 1 ? (nk >= 8 ? 8 : (nk >= 4 ? 16 : 32)) : (nj >= 32 ? 32 : (nj >= 16 ? 16 : 8));
     *ta = a;
     *tb = 32 / a * lane_cells(s);
     *npa = (nj + a - 1) / a;

@@ -118,7 +118,9 @@ extern "C" int dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu
     if (rc) return report_error(DNSMC_ERR_CUDA, cudaGetErrorString((cudaError_t)rc));
 
     // the grey black-wall march runs kLaneCells cells per lane
-    const int ta = c.tile_a ? c.tile_a : (c.jmax >= 32 ? 32 : (c.jmax >= 16 ? 16 : 8));
+    // the handle API's automatic packet shape (8 x 8, or 16 x 4 / 32 x 2 for
+    // fewer than 8 / 4 cells along k)
+    const int ta = c.tile_a ? c.tile_a : (c.kmax >= 8 ? 8 : (c.kmax >= 4 ? 16 : 32));
     const int tb = 32 / ta * kLaneCells;
     MarchParams P{};
     P.nw = c.imax; P.na = c.jmax; P.nb = c.kmax;

@@ -118,7 +118,10 @@ typedef struct dnsmc_config {
                                  /* two control variates (network training)    */
     /* kernel shape (0 = automatic) */
     int   block_threads;         /* 128 or 256                                   */
-    int   tile_a;                /* cells of a packet along j: 8, 16 or 32       */
+    int   tile_a;                /* cells of a packet along j: 8, 16 or 32;     */
+                                 /* automatic: 8 (8 x 8 packets) on the fine    */
+                                 /* grid when k has 8 cells or more, else 16   */
+                                 /* or 32; the widest row with grid_num > 1     */
     /* multigrid */
     int   mg_steps;              /* steps per grid before the next coarser one  */
                                  /* (the reference's maxs, 5); the last grid    */

@@ -301,9 +301,10 @@ def test_grey_slab_matches_analytic_solution():
     yc = (np.arange(ni) + 0.5) * 2.0 / ni
     exact = O.slab_divq(yc, 2.0, 1.0, 1000.0, 0.0, 300.0)
     # one cell per packet is independent (the cells of a packet share rays)
-    tb = s.packet_shape()[1]
-    q = Q[0][::tb, 0, :].mean(0)
-    se = np.sqrt((S[0][::tb, 0, :] ** 2).sum(0)) / (nk // tb)
+    ta, tb = s.packet_shape()
+    npk = (nk // tb) * (nj // ta)
+    q = Q[0][::tb, ::ta, :].mean((0, 1))
+    se = np.sqrt((S[0][::tb, ::ta, :] ** 2).sum((0, 1))) / npk
     z = (q - exact) / se
     assert np.abs(z).max() < 4.0, z
     assert math.sqrt((z ** 2).mean()) < 1.5
@@ -325,9 +326,9 @@ def test_golden_resfortm_on_gpu(tmp_path, particle_tables, resfortm):
     s.set_region(0, 64, 0, 32, 0, 32)
     s.set_rays(3000)
     Q, S = s.solve(timeout_s=300)
-    tb = s.packet_shape()[1]
-    q = Q[0][::tb, 0, :].mean(0)  # one cell per packet: independent packets of each row
-    se = np.sqrt((S[0][::tb, 0, :] ** 2).sum(0)) / (32 // tb)
+    ta, tb = s.packet_shape()
+    q = Q[0][::tb, ::ta, :].mean((0, 1))  # one cell per packet: independent packets of each row
+    se = np.sqrt((S[0][::tb, ::ta, :] ** 2).sum((0, 1))) / ((32 // tb) * (32 // ta))
     gse = resfortm["plane_std"] / 64
     z = (q - resfortm["Q"]) / np.sqrt(se ** 2 + gse ** 2)
     assert math.sqrt((z ** 2).mean()) < 1.6, z

@@ -187,6 +187,7 @@ def test_control_variate_with_particles_is_unbiased():
         s.set_particle_field(fv)
         s.set_rays(128)
         out.append(s.solve(timeout_s=300))
+        ppp = s.packet_count() // 32  # packets per wall-normal plane
         s.close()
     (Qp, Sp), (Qc, Sc) = out
     z = (Qc - Qp) / np.sqrt(Sp ** 2 + Sc ** 2)
@@ -194,10 +195,10 @@ def test_control_variate_with_particles_is_unbiased():
     # the scattering weights make sigma from 128 rays heavy-tailed: more
     # |z| > 3 than a Gaussian's 0.27 %
     assert (np.abs(z) > 3).mean() < 0.03
-    # no shift between the estimators: wall-normal plane means, the 32 packets
+    # no shift between the estimators: wall-normal plane means, the packets
     # of a plane as the independent samples (cells of a packet share rays)
     dq = (Qc - Qp)[0].mean(axis=(0, 1))
-    sq = np.sqrt(((Sp ** 2 + Sc ** 2)[0]).mean(axis=(0, 1)) / 32)
+    sq = np.sqrt(((Sp ** 2 + Sc ** 2)[0]).mean(axis=(0, 1)) / ppp)
     zp = dq / sq
     assert math.sqrt(float((zp ** 2).mean())) < 1.6, zp
     assert np.abs(zp).max() < 4.5, zp

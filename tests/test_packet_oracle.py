@@ -52,8 +52,10 @@ def test_packet_replay_grey_slab_analytic():
     s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.2831853, Lz=3.1415927,
                                   stretched_x=0, T_west=0.0, T_east=300.0, kappa=1.0, seed=3))
     Q, S, _ = replay(s, np.full((nk, nj, ni), 1000.0, np.float32), None, 1024, 1)
-    q = Q[:, 0, :].mean(0)
-    se = np.sqrt((S[:, 0, :] ** 2).sum(0)) / nk
+    ta, tb = s.packet_shape()  # one cell per packet: the cells of a packet share rays
+    npk = (nk // tb) * (nj // ta)
+    q = Q[::tb, ::ta, :].mean((0, 1))
+    se = np.sqrt((S[::tb, ::ta, :] ** 2).sum((0, 1))) / npk
     ex = O.slab_divq((np.arange(ni) + 0.5) * 2.0 / ni, 2.0, 1.0, 1000.0, 0.0, 300.0)
     z = (q - ex) / se
     assert np.abs(z).max() < 4.0 and math.sqrt((z ** 2).mean()) < 1.5, z
@@ -111,8 +113,9 @@ def test_rqmc_unbiased_and_replicate_variance_is_calibrated():
                                       sampler=D.SAMPLER_RQMC, nvar=4))
         Q, S, _ = replay(s, np.full((nk, nj, ni), 1000.0, np.float32), None, 256, 1)
         m = S ** 2
-        Qs.append(Q[:, 0, :])
-        Vs.append(m[:, 0, :])
+        ta, tb = s.packet_shape()  # one cell per packet: the cells of a packet share rays
+        Qs.append(Q[::tb, ::ta, :].reshape(-1, ni))
+        Vs.append(m[::tb, ::ta, :].reshape(-1, ni))
         s.close()
     Qs, Vs = np.array(Qs), np.array(Vs)
     emp = Qs.var(0, ddof=1).mean()
