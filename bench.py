@@ -501,13 +501,17 @@ def run_c4(args):
         return s
 
     s = solver(1, 41)
-    r, e = ray_budget(s, 32)
-    s.set_rays(r)
-    Q, S = s.solve(timeout_s=1800)
-    e1 = rms_error(Q, S)
-    if e1 > 0.98 * TARGET_ERR:
-        r = -(-int(math.ceil(r * (e1 / (0.98 * TARGET_ERR)) ** 2)) // REPLICATES) * REPLICATES
+    if args.rays:  # fixed rays (profiling cases): no 1 % budget
+        r, e = args.rays, None
         s.set_rays(r)
+    else:
+        r, e = ray_budget(s, 32)
+        s.set_rays(r)
+        Q, S = s.solve(timeout_s=1800)
+        e1 = rms_error(Q, S)
+        if e1 > 0.98 * TARGET_ERR:
+            r = -(-int(math.ceil(r * (e1 / (0.98 * TARGET_ERR)) ** 2)) // REPLICATES) * REPLICATES
+            s.set_rays(r)
     for _ in range(max(3, args.warmup)):
         s.solve(timeout_s=1800)
     stream = torch.cuda.ExternalStream(s.stream())
