@@ -19,7 +19,7 @@ c_int32_p = ctypes.POINTER(ctypes.c_int32)
 
 OK = 0
 ERR_ARG, ERR_STATE, ERR_CUDA, ERR_IO, ERR_TIMEOUT, ERR_NOMEM, ERR_TABLE, ERR_NODEVICE = 1, 2, 3, 4, 5, 6, 7, 8
-STATUS_STEP_CAP, STATUS_NONFINITE, STATUS_BAD_FIELD = 0x1, 0x2, 0x4
+STATUS_STEP_CAP, STATUS_NONFINITE, STATUS_BAD_FIELD, STATUS_COPY_TIMEOUT = 0x1, 0x2, 0x4, 0x8
 MODEL_CK, MODEL_GREY_BANDS, MODEL_PARTICLE, MODEL_GREY, MODEL_TABLE = 0, 1, 2, 3, 4
 LAYOUT_DENSE, LAYOUT_FORTRAN = 0, 1
 SAMPLER_IID, SAMPLER_RQMC = 0, 1

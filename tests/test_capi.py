@@ -32,6 +32,18 @@ def test_every_declared_function_is_exported():
     assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
 
 
+def test_python_constants_match_the_header():
+    """Every DNSMC_STATUS_*, DNSMC_MODEL_*, DNSMC_SAMPLER_* and DNSMC_LAYOUT_*
+    value of include/dnsmc.h is the package's constant of the same name."""
+    src = open(os.path.join(ROOT, "include", "dnsmc.h")).read()
+    defs = dict(re.findall(r"^#define DNSMC_((?:STATUS|MODEL|SAMPLER|LAYOUT)_[A-Z_0-9]+)\s+(0x[0-9a-fA-F]+|\d+)u?",
+                           src, flags=re.M))
+    assert {"STATUS_STEP_CAP", "STATUS_NONFINITE", "STATUS_BAD_FIELD", "STATUS_COPY_TIMEOUT"} <= set(defs)
+    for name, val in defs.items():
+        assert hasattr(_lib, name), name
+        assert getattr(_lib, name) == int(val, 0), name
+
+
 def test_default_config_is_reference_param_h():
     c = D.default_config()
     assert (c.imax, c.jmax, c.kmax, c.p_row) == (64, 64, 64, 1)
