@@ -111,17 +111,15 @@ def features(T, X, fw, region, T_center, T_scale, x_center, x_scale) -> np.ndarr
 # ---------------------------------------------------------------------------
 # network
 # ---------------------------------------------------------------------------
-def _erf(z):
-    from scipy.special import erf
-    return erf(z)
-
-
 def gelu(z):
-    return 0.5 * z * (1.0 + _erf(z / math.sqrt(2.0)))
+    """GELU in its tanh form (Hendrycks & Gimpel 2016), as the device:
+    0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3)))."""
+    return 0.5 * z * (1.0 + np.tanh(math.sqrt(2.0 / math.pi) * (z + 0.044715 * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + _erf(z / math.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / math.sqrt(2.0 * math.pi)
+    t = np.tanh(math.sqrt(2.0 / math.pi) * (z + 0.044715 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * math.sqrt(2.0 / math.pi) * (1.0 + 3 * 0.044715 * z * z)
 
 
 def forward(p, feats, mimic=True):
