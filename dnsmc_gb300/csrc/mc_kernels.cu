@@ -654,6 +654,15 @@ __global__ void cv_mean_nodes_kernel(const CvParams c) {
         const double wt[2] = {1.0 - ft, ft};
         const double wx[2] = {1.0 - fx, fx};
         const int nb = c.nX > 1 ? 2 : 1;
+        // the cell's interpolation weights, formed once for all groups:
+        // w4[bx][a][a'] = wx[bx] wt[a] wt[a'] (the product of the k and Ib
+        // interpolations) and w2[bx][a] = wx[bx] wt[a]
+        double w4[2][4], w2[2][2];
+        for (int bx = 0; bx < nb; ++bx)
+            for (int a = 0; a < 2; ++a) {
+                w2[bx][a] = wx[bx] * wt[a];
+                for (int a2 = 0; a2 < 2; ++a2) w4[bx][a * 2 + a2] = w2[bx][a] * wt[a2];
+            }
         for (int g = 0; g < c.n_groups; ++g) {
             const double *lay = c.nodes + (((long long)f * c.n_groups + g) * niR + iR) * L.per;
             const double *GJ = lay, *GB = lay + L.nTX, *MB = lay + 2 * L.nTX;
@@ -663,20 +672,14 @@ __global__ void cv_mean_nodes_kernel(const CvParams c) {
                 const int xn = xi + bx;
                 const double *m = Mg + ((long long)ti * c.nX + xn) * 4;
                 const double *mb = MB + ((long long)ti * c.nX + xn) * 4;
-                double sI = 0.0, sIA = 0.0, sJ = 0.0, sB = 0.0;
-                for (int a = 0; a < 2; ++a) {
-                    for (int a2 = 0; a2 < 2; ++a2) {
-                        const double ww = wt[a] * wt[a2];
-                        sI = fma(ww, m[a * 2 + a2], sI);
-                        sIA = fma(ww, mb[a * 2 + a2], sIA);
-                    }
-                    sJ = fma(wt[a], GJ[(ti + a) * c.nX + xn], sJ);
-                    sB = fma(wt[a], GB[(ti + a) * c.nX + xn], sB);
+                for (int q = 0; q < 4; ++q) {
+                    kI = fma(w4[bx][q], m[q], kI);
+                    kIA = fma(w4[bx][q], mb[q], kIA);
                 }
-                kI = fma(wx[bx], sI, kI);
-                kIA = fma(wx[bx], sIA, kIA);
-                kJ = fma(wx[bx], sJ, kJ);
-                kB = fma(wx[bx], sB, kB);
+                for (int a = 0; a < 2; ++a) {
+                    kJ = fma(w2[bx][a], GJ[(ti + a) * c.nX + xn], kJ);
+                    kB = fma(w2[bx][a], GB[(ti + a) * c.nX + xn], kB);
+                }
             }
             c.muY[((long long)f * c.n_groups + g) * c.region_cells + tc] = make_double2(kI - kJ, kIA - kB);
         }
