@@ -269,6 +269,25 @@ def test_rqmc_requires_replicates_and_divisible_rays():
     s.close()
 
 
+@pytest.mark.parametrize("jmax,kmax,grid_num,tile_a,shape", [
+    (32, 32, 1, 0, (8, 8)), (32, 8, 1, 0, (8, 8)), (32, 6, 1, 0, (16, 4)), (32, 4, 1, 0, (16, 4)),
+    (32, 2, 1, 0, (32, 2)), (32, 32, 1, 16, (16, 4)), (32, 32, 1, 32, (32, 2)),
+    (64, 64, 5, 0, (32, 1)), (64, 64, 5, 8, (8, 4))])
+def test_automatic_packet_shape(jmax, kmax, grid_num, tile_a, shape):
+    """64-cell packets of the two-cell march: 8 x 8 unless k is shorter than
+    8 (16 x 4) or 4 (32 x 2) cells or tile_a asks otherwise; 32-cell packets
+    of the multigrid march: the widest row.  The packet count covers every
+    cell of every wall-normal plane."""
+    cfg = D.default_config(model=D.MODEL_GREY, imax=16, jmax=jmax, kmax=kmax, grid_num=grid_num, tile_a=tile_a)
+    if grid_num > 1:
+        cfg.imax = 64
+    s = D.Solver(cfg)
+    assert s.packet_shape() == shape
+    ta, tb = shape
+    assert s.packet_count() == cfg.imax * -(-jmax // ta) * -(-kmax // tb)
+    s.close()
+
+
 def test_multigrid_config_checks():
     """grid_num > 1 needs grid sizes divisible by 2^(grid_num - 1) and
     mg_steps >= 1; the reference's shipped 5 levels on 64^3 are valid."""
