@@ -172,6 +172,26 @@ def test_bitexact_table_x_groups_fields_region():
     s.close()
 
 
+def test_bitexact_square_packets_ragged_region():
+    """The automatic 8 x 8 packets over a region whose j and k extents are
+    not multiples of 8 (20 x 11 cells: packets of 8, 8, 4 along j and 8, 3
+    along k), with the control variate and RQMC: tallies bit-exact."""
+    tb = synth.ck_table(nbands=12, nq=8, nT=20, nX=4, seed=8)
+    s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=6, jmax=24, kmax=12, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=1, T_west=420, T_east=400, seed=29, n_groups=3,
+                                  sampler=D.SAMPLER_RQMC, nvar=2, local_sampling=1, control_variate=1))
+    s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+    T = smooth_field(6, 24, 12, 450, 1700, 33)
+    x = (0.1 + 0.05 * np.random.default_rng(12).uniform(-1, 1, (12, 24, 6))).astype(np.float32)
+    s.set_fields(T, x)
+    s.set_region(0, 6, 2, 22, 1, 12)
+    assert s.packet_shape() == (8, 8)
+    s.set_rays(16)
+    from test_gpu_cv import assert_bitexact_cv
+    assert_bitexact_cv(s, T, x)
+    s.close()
+
+
 def test_bitexact_rays_per_item_and_item_steps():
     """Ray counts per (band group, packet), zeros included, under RQMC; the
     per-item step record is positive exactly where rays were cast."""
