@@ -20,6 +20,7 @@ c_int32_p = ctypes.POINTER(ctypes.c_int32)
 OK = 0
 ERR_ARG, ERR_STATE, ERR_CUDA, ERR_IO, ERR_TIMEOUT, ERR_NOMEM, ERR_TABLE, ERR_NODEVICE = 1, 2, 3, 4, 5, 6, 7, 8
 STATUS_STEP_CAP, STATUS_NONFINITE, STATUS_BAD_FIELD, STATUS_COPY_TIMEOUT = 0x1, 0x2, 0x4, 0x8
+RESULT_F64, RESULT_F32 = 0, 1
 MODEL_CK, MODEL_GREY_BANDS, MODEL_PARTICLE, MODEL_GREY, MODEL_TABLE = 0, 1, 2, 3, 4
 LAYOUT_DENSE, LAYOUT_FORTRAN = 0, 1
 SAMPLER_IID, SAMPLER_RQMC = 0, 1
@@ -122,6 +123,8 @@ SIGNATURES = {
     "dnsmc_solve_async": (ctypes.c_int, [ctypes.c_void_p]),
     "dnsmc_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "dnsmc_get_results": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
+    "dnsmc_set_result_type": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "dnsmc_get_results_float": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p]),
     "dnsmc_get_group_results": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
     "dnsmc_status": (ctypes.c_int, [ctypes.c_void_p, c_uint32_p]),
     "dnsmc_get_counters": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p, c_double_p]),
@@ -137,7 +140,7 @@ SIGNATURES = {
     "dnsmc_trace_ray": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                        ctypes.c_int, c_int32_p, c_int_p, c_uint32_p]),
     "dnsmc_solve_grey_noalloc": (ctypes.c_int, [ctypes.POINTER(Config), c_float_p, ctypes.c_void_p, ctypes.c_void_p,
-                                                ctypes.c_void_p, ctypes.c_void_p]),
+                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "mc_gpu_": (None, [c_float_p, c_int_p]),
     "get_results_": (None, [c_float_p, c_float_p]),
     "dnsmc_dropin_configure": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_char_p]),

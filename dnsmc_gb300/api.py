@@ -296,9 +296,34 @@ class Solver:
         check(self._lib.dnsmc_get_results(self._h, _dp(Q), _dp(S)))
         return Q, S
 
+    def set_result_type(self, result_type: int) -> None:
+        """RESULT_F64 (default) or RESULT_F32: with F32 the device rounds Q and
+        sigma to float and only those cross to the host; read them with
+        results_float()."""
+        check(self._lib.dnsmc_set_result_type(self._h, int(result_type)))
+        self._result_type = int(result_type)
+
+    def results_float(self, out=None):
+        """(Q, sigma) as float32 arrays (nfields, nk, nj, ni), into `out` when
+        given (C-contiguous float32 arrays of that shape)."""
+        shp = self._region_shape()
+        if out is None:
+            Q = np.zeros(shp, np.float32)
+            S = np.zeros(shp, np.float32)
+        else:
+            Q, S = out
+            for a in (Q, S):
+                if a.shape != shp or a.dtype != np.float32 or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError(f"result arrays must be C-contiguous float32 of shape {shp}")
+        check(self._lib.dnsmc_get_results_float(self._h, Q.ctypes.data_as(_lib.c_float_p),
+                                                S.ctypes.data_as(_lib.c_float_p)))
+        return Q, S
+
     def solve(self, timeout_s: float = 0.0):
         self.solve_async()
         self.wait(timeout_s)
+        if getattr(self, "_result_type", 0) == _lib.RESULT_F32:
+            return self.results_float()
         return self.results()
 
     def group_results(self):

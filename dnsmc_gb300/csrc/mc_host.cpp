@@ -353,6 +353,7 @@ struct dnsmc_solver {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_march0 = nullptr, ev_march1 = nullptr, ev_done = nullptr, ev_solve0 = nullptr;
     bool solved = false, in_flight = false;
+    int solved_result_type = 0;               // result type of the last solve
 
     // geometry
     std::vector<float> fw;
@@ -439,8 +440,13 @@ struct dnsmc_solver {
     // outputs
     DevBuf<double2> d_tally;
     DevBuf<double> d_Q, d_var, d_sig, d_Qg, d_varg;
-    PinBuf<double> h_Q, h_sig, h_var;
-    bool keep_var = false;                   // copy the variances to the host too (drop-in solver)
+    PinBuf<double> h_Q, h_sig;
+    // DNSMC_RESULT_F32: the finalize also writes Q and sqrt(var * sig_scale)
+    // as floats and only those cross to the host (8 bytes per cell)
+    int result_type = DNSMC_RESULT_F64;
+    double sig_scale = 1.0;
+    DevBuf<float> d_Qf, d_sigf;
+    PinBuf<float> h_Qf, h_sigf;
     DevBuf<unsigned int> d_misc;  // [0] queue, [1] status
     DevBuf<unsigned long long> d_counters;
     unsigned long long h_counters[2] = {0, 0};
@@ -1006,6 +1012,13 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     P.nbands = t.nbands; P.nT = t.nT; P.nX = t.nX;
     P.T0 = t.T0; P.invdT = 1.0f / t.dT; P.X0 = t.X0; P.invdX = 1.0f / t.dX;
     if (mode != MODE_GREY) { P.slab = s->d_slab.p; P.slab_len = s->slab_len; P.slab_klen = s->slab_klen; }
+    // polls of the first bounded wait for a ray's slab copy; the environment
+    // variable DNSMC_TEST_SLAB_FIRST_POLLS lowers it only to drive the
+    // time-out path in tests (0: every first wait runs out at once, the
+    // second one receives the copy, and the solve reports DNSMC_ERR_TIMEOUT)
+    P.slab_polls0 = kSlabWaitPolls;
+    if (const char *ev = getenv("DNSMC_TEST_SLAB_FIRST_POLLS"))
+        if (*ev) P.slab_polls0 = std::min(std::max(atoi(ev), 0), kSlabWaitPolls);
     P.ibw = s->d_ibw.p;
     P.entries = s->d_entries.p; P.group_start = s->d_group_start.p;
     P.n_groups = s->n_groups_used;
@@ -1212,9 +1225,17 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     TRY(s->d_varg.ensure(nout * P.n_groups));
     F.Q = s->d_Q.p; F.var = s->d_var.p; F.sigma = s->d_sig.p; F.Qg = s->d_Qg.p; F.varg = s->d_varg.p;
     F.status = P.status;
-    TRY(s->h_Q.ensure(nout));
-    TRY(s->h_sig.ensure(nout));
-    if (s->keep_var) TRY(s->h_var.ensure(nout));  // the drop-in scales the variances itself
+    const bool f32 = s->result_type == DNSMC_RESULT_F32;
+    if (f32) {
+        TRY(s->d_Qf.ensure(nout));
+        TRY(s->d_sigf.ensure(nout));
+        TRY(s->h_Qf.ensure(nout));
+        TRY(s->h_sigf.ensure(nout));
+        F.Qf = s->d_Qf.p; F.sigf = s->d_sigf.p; F.sig_scale = s->sig_scale;
+    } else {
+        TRY(s->h_Q.ensure(nout));
+        TRY(s->h_sig.ensure(nout));
+    }
 
     // ---- the kernel sequence of a solve (stream-ordered; capturable) -------
     auto kernels = [&](bool events) -> int {
@@ -1247,10 +1268,15 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         if (events) CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
         rc = launch_finalize(F, s->stream);
         if (rc) return fail(DNSMC_ERR_CUDA, "finalize launch: %s", cudaGetErrorString((cudaError_t)rc));
-        CUDA_TRY(cudaMemcpyAsync(s->h_Q.p, s->d_Q.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-        CUDA_TRY(cudaMemcpyAsync(s->h_sig.p, s->d_sig.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
-        if (s->keep_var)
-            CUDA_TRY(cudaMemcpyAsync(s->h_var.p, s->d_var.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        if (f32) {
+            CUDA_TRY(cudaMemcpyAsync(s->h_Qf.p, s->d_Qf.p, nout * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(s->h_sigf.p, s->d_sigf.p, nout * sizeof(float), cudaMemcpyDeviceToHost,
+                                     s->stream));
+        } else {
+            CUDA_TRY(cudaMemcpyAsync(s->h_Q.p, s->d_Q.p, nout * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(s->h_sig.p, s->d_sig.p, nout * sizeof(double), cudaMemcpyDeviceToHost,
+                                     s->stream));
+        }
         return DNSMC_OK;
     };
 
@@ -1292,6 +1318,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     CUDA_TRY(cudaEventRecord(s->ev_done, s->stream));
     s->in_flight = true;
     s->solved = true;
+    s->solved_result_type = s->result_type;
     return DNSMC_OK;
 }
 
@@ -1617,7 +1644,8 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_part.release(); s->d_fieldV.release(); s->d_layerV.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
     s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_sig.release(); s->h_sig.release(); s->d_Qg.release(); s->d_varg.release();
-    s->h_Q.release(); s->h_var.release(); s->d_misc.release(); s->d_counters.release();
+    s->h_Q.release(); s->d_misc.release(); s->d_counters.release();
+    s->d_Qf.release(); s->d_sigf.release(); s->h_Qf.release(); s->h_sigf.release();
     if (s->ev_march0) cudaEventDestroy(s->ev_march0);
     if (s->ev_march1) cudaEventDestroy(s->ev_march1);
     if (s->ev_done) cudaEventDestroy(s->ev_done);
@@ -2092,13 +2120,57 @@ static void parallel_copy(void *dst, const void *src, size_t bytes) {
     for (auto &x : th) x.join();
 }
 
+// Rows of imax floats of a dense (imax, jl, kmax) block into the interior
+// of a Fortran array (0:imax+1, 0:jl+1, 0:kmax+1), several threads over k.
+static void scatter_fortran(float *dst, const float *src, int imax, int jl, int kmax) {
+    if (!dst) return;
+    const unsigned nt = (unsigned)std::max(1, std::min(8, kmax / 8));
+    auto part = [=](int k0, int k1) {
+        for (int k = k0; k < k1; ++k)
+            for (int j = 0; j < jl; ++j)
+                memcpy(dst + 1 + (size_t)(imax + 2) * ((j + 1) + (size_t)(jl + 2) * (k + 1)),
+                       src + (size_t)imax * (j + (size_t)jl * k), (size_t)imax * sizeof(float));
+    };
+    if (nt <= 1) { part(0, kmax); return; }
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < nt; ++t) th.emplace_back(part, (int)(t * kmax / nt), (int)((t + 1) * kmax / nt));
+    for (auto &x : th) x.join();
+}
+
 int dnsmc_get_results(dnsmc_solver *s, double *Q, double *sigma) {
     if (!s) return fail(DNSMC_ERR_ARG, "null solver");
     if (!s->solved) return fail(DNSMC_ERR_STATE, "no solve has been run");
     TRY(wait_done(s, 0));
+    if (s->solved_result_type != DNSMC_RESULT_F64)
+        return fail(DNSMC_ERR_STATE, "the last solve returned float results: use dnsmc_get_results_float");
     const size_t n = (size_t)s->nfields * s->last.region_cells;
     if (Q) parallel_copy(Q, s->h_Q.p, n * sizeof(double));
     if (sigma) parallel_copy(sigma, s->h_sig.p, n * sizeof(double));
+    return DNSMC_OK;
+}
+
+int dnsmc_set_result_type(dnsmc_solver *s, int type) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (type != DNSMC_RESULT_F64 && type != DNSMC_RESULT_F32) return fail(DNSMC_ERR_ARG, "unknown result type %d", type);
+    TRY(wait_done(s, 0));
+    s->result_type = type;
+    return DNSMC_OK;
+}
+
+int dnsmc_get_results_float(dnsmc_solver *s, float *Q, float *sigma) {
+    if (!s) return fail(DNSMC_ERR_ARG, "null solver");
+    if (!s->solved) return fail(DNSMC_ERR_STATE, "no solve has been run");
+    TRY(wait_done(s, 0));
+    const size_t n = (size_t)s->nfields * s->last.region_cells;
+    if (s->solved_result_type == DNSMC_RESULT_F32) {
+        if (Q) parallel_copy(Q, s->h_Qf.p, n * sizeof(float));
+        if (sigma) parallel_copy(sigma, s->h_sigf.p, n * sizeof(float));
+    } else {
+        for (size_t i = 0; i < n; ++i) {
+            if (Q) Q[i] = (float)s->h_Q.p[i];
+            if (sigma) sigma[i] = (float)s->h_sig.p[i];
+        }
+    }
     return DNSMC_OK;
 }
 
@@ -2338,7 +2410,10 @@ void mc_gpu_(float *Tfort, int *ystart) {
             if (dnsmc_config_from_env(&c)) dropin_die("mc_gpu_ configuration");
         }
         if (dnsmc_create(&c, &g_dropin)) dropin_die("mc_gpu_ set-up");
-        g_dropin->keep_var = true;  // get_results_ scales the variances itself
+        // float results with the reference's sigma normaliser, computed on
+        // the device: only Q and sigma as floats cross to the host
+        g_dropin->result_type = DNSMC_RESULT_F32;
+        g_dropin->sig_scale = c.nvar > 1 ? (double)c.nvar / (c.nvar - 0.5) : 1.0;
         std::string dir = g_dropin_tables;
         if (dir.empty()) { const char *e = getenv("DNSMC_TABLES"); dir = e && *e ? e : "../distr/tables"; }
         int rc = DNSMC_OK;
@@ -2364,16 +2439,10 @@ void get_results_(float *resfort, float *varfort) {
     if (wait_done(g_dropin, 0)) dropin_die("get_results_");
     const dnsmc_config &c = g_dropin->cfg;
     const int jl = c.jmax / c.p_row;
-    const double vscale = c.nvar > 1 ? (double)c.nvar / (c.nvar - 0.5) : 1.0;
-    const double *Q = g_dropin->h_Q.p, *V = g_dropin->h_var.p;
-    for (int k = 1; k <= c.kmax; ++k)
-        for (int j = 1; j <= jl; ++j)
-            for (int i = 1; i <= c.imax; ++i) {
-                const size_t src = (size_t)(i - 1) + (size_t)c.imax * ((j - 1) + (size_t)jl * (k - 1));
-                const size_t dst = (size_t)i + (size_t)(c.imax + 2) * (j + (size_t)(jl + 2) * k);
-                if (resfort) resfort[dst] = (float)Q[src];
-                if (varfort) varfort[dst] = (float)sqrt(V[src] * vscale);
-            }
+    // interior rows of imax floats into the (imax+2)(jl+2)(kmax+2) arrays
+    // (code/param.h:110-111 idx_F); ghost cells stay untouched
+    scatter_fortran(resfort, g_dropin->h_Qf.p, c.imax, jl, c.kmax);
+    scatter_fortran(varfort, g_dropin->h_sigf.p, c.imax, jl, c.kmax);
 }
 
 }  // extern "C"

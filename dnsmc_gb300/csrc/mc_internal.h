@@ -29,6 +29,10 @@ struct SpecEntry {
     float    W;         // ray weight factor: w = W * k(T_i) * Ib(T_i)
 };
 
+// try_wait polls of a march's slab barrier before it gives up (each poll may
+// suspend the thread for a while; the whole wait stays well under a second)
+constexpr int kSlabWaitPolls = 1 << 16;
+
 // Cells per lane of the fine-grid march (mc_march_pair.cuh): a packet is
 // 32 * kLaneCells cells; the multigrid march uses 1.
 constexpr int kLaneCells = 2;
@@ -60,6 +64,8 @@ struct MarchParams {
     // shared memory: the march launches with warps * slab_len * 8 bytes.
     const float2 *slab;
     int slab_len, slab_klen;
+    int slab_polls0;          // polls of the first wait for a slab copy: kSlabWaitPolls
+                              // (fewer only in tests of the time-out path)
     const float *ibw;         // [2][band]
     const SpecEntry *entries;
     const int *group_start;   // n_tbins * n_groups + 1, temperature-bin major
@@ -138,6 +144,9 @@ struct FinalizeParams {
     double *Q;                // [f][cell] dense region, i fastest
     double *var;              // [f][cell]
     double *sigma;            // [f][cell]: sqrt(var)
+    float *Qf;                // [f][cell] Q rounded to float, or nullptr
+    float *sigf;              // [f][cell] sqrt(var * sig_scale) rounded to float (with Qf)
+    double sig_scale;         // 1, or the drop-in's nVar / (nVar - 0.5) (code/mc_gpu.cu:221)
     double *Qg;               // [f][group][cell] or nullptr
     double *varg;             // [f][group][cell] or nullptr
     unsigned int *status;

@@ -121,6 +121,10 @@ __global__ void finalize_kernel(const FinalizeParams F) {
         F.Q[idx] = Q;
         F.var[idx] = V;
         if (F.sigma) F.sigma[idx] = sqrt(V);
+        if (F.Qf) {  // the float results the host receives (8 bytes per cell)
+            F.Qf[idx] = (float)Q;
+            F.sigf[idx] = (float)sqrt(V * F.sig_scale);
+        }
     }
 }
 

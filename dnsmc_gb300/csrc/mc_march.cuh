@@ -357,9 +357,6 @@ __device__ __forceinline__ void ray_direction(uint4 x, float *sW, float *sA, flo
 // transaction barrier (mbarrier) in shared memory; the warp waits on the
 // barrier's phase parity.  Each warp owns one barrier and one slab buffer.
 // ---------------------------------------------------------------------------
-// try_wait polls of the slab barrier before giving up (each poll may suspend
-// the thread for a while; the whole wait stays well under a second)
-constexpr int kSlabWaitPolls = 1 << 16;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -373,10 +370,11 @@ __device__ __forceinline__ void slab_bar_init(uint64_t *bar, int lane) {
     __syncwarp();
 }
 
-// Bounded wait for the barrier phase of the given parity to complete.
-__device__ __forceinline__ bool slab_bar_wait(const uint64_t *bar, uint32_t parity) {
+// Bounded wait (at most `polls` polls) for the barrier phase of the given
+// parity to complete.
+__device__ __forceinline__ bool slab_bar_wait(const uint64_t *bar, uint32_t parity, int polls) {
     const uint32_t b = smem_addr(bar);
-    for (int it = 0; it < kSlabWaitPolls; ++it) {
+    for (int it = 0; it < polls; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -394,10 +392,14 @@ __device__ __forceinline__ bool slab_bar_wait(const uint64_t *bar, uint32_t pari
 // of 16 at a 16-byte aligned address on both sides) into this warp's shared
 // copy.  The previous ray's lookups are done first (the warp converges, and
 // the async proxy is ordered after the generic one).  *phase is the warp's
-// barrier parity, flipped per copy.  A wait that runs out sets
-// DNSMC_STATUS_COPY_TIMEOUT, waits once more for the copy still in flight,
-// and the march carries on: the host reports the solve as failed.
-__device__ __forceinline__ void load_slab(const MarchParams &P, int sid, float2 *slk, int lane, uint64_t *bar,
+// barrier parity, flipped per completed copy.  The first wait polls
+// P.slab_polls0 times (kSlabWaitPolls; fewer only in tests of this path).
+// A wait that runs out sets DNSMC_STATUS_COPY_TIMEOUT (the host reports the
+// solve as failed) and waits once more; if the copy has still not arrived,
+// returns false with the phase unchanged: the warp then takes no further
+// copies or items and calls slab_drain before it exits.  The outcome is
+// the same in every lane of the warp.
+__device__ __forceinline__ bool load_slab(const MarchParams &P, int sid, float2 *slk, int lane, uint64_t *bar,
                                           uint32_t *phase, unsigned int *flags) {
     __syncwarp();
     if (lane == 0) {
@@ -411,11 +413,19 @@ __device__ __forceinline__ void load_slab(const MarchParams &P, int sid, float2 
                      "l"(src), "r"(bytes), "r"(smem_addr(bar))
                      : "memory");
     }
-    if (!slab_bar_wait(bar, *phase)) {
+    if (!__all_sync(0xffffffffu, slab_bar_wait(bar, *phase, P.slab_polls0))) {
         *flags |= DNSMC_STATUS_COPY_TIMEOUT;
-        slab_bar_wait(bar, *phase);
+        if (!__all_sync(0xffffffffu, slab_bar_wait(bar, *phase, kSlabWaitPolls))) return false;
     }
     *phase ^= 1u;
+    return true;
+}
+
+// Before a warp whose copy did not arrive exits: one more bounded wait for
+// that copy, so that it does not land in shared memory the next block on
+// this SM may own.
+__device__ __forceinline__ void slab_drain(const uint64_t *bar, uint32_t phase) {
+    slab_bar_wait(bar, phase, kSlabWaitPolls);
 }
 
 // One ray of a cell into its FP64 sums: the sum, and the sum of squares
@@ -478,6 +488,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
     uint64_t *const sbar = &s_bar[threadIdx.x >> 5];
     uint32_t sphase = 0;
     slab_bar_init(sbar, lane);
+    bool dead = false;  // a slab copy did not arrive: this warp stops marching
 
     for (;;) {
         long long item;
@@ -568,7 +579,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                 SpecEntry e = P.entries[gs + j];
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
-                load_slab(P, e.koff, slk, lane, sbar, &sphase, &flags);
+                if (!load_slab(P, e.koff, slk, lane, sbar, &sphase, &flags)) { dead = true; break; }
                 const float ki = lookup_k<MODE>(slk, ki_i, ft_i, fx_i);
                 Ii = lookup_ib(sli, ti_i, ft_i);
                 invI = Ii > 0.f ? 1.0f / Ii : 0.f;
@@ -771,11 +782,13 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                 tally_ray(P, (double)X, m, M, &s_acc[tid], &s_acc[nthr + tid], &s_acc[2 * nthr + tid]);
             }
         }
+        if (dead) break;  // the item's sums are incomplete; the solve fails
         my_steps += lsteps;
         if (TRACE) return;
         if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
         if (active) P.tally[cell_out] = make_double2(s_acc[tid], s_acc[nthr + tid]);
     }
+    if (dead) slab_drain(sbar, sphase);
     // per-warp counters and status
     for (int o = 16; o > 0; o >>= 1) {
         my_rays += __shfl_xor_sync(FULL, my_rays, o);

@@ -66,6 +66,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
     uint64_t *const sbar = &s_bar[threadIdx.x >> 5];
     uint32_t sphase = 0;
     slab_bar_init(sbar, lane);
+    bool dead = false;  // a slab copy did not arrive: this warp stops marching
 
     for (;;) {
         long long item;
@@ -172,7 +173,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
                 sid = e.koff;
-                load_slab(P, sid, slk, lane, sbar, &sphase, &flags);
+                if (!load_slab(P, sid, slk, lane, sbar, &sphase, &flags)) { dead = true; break; }
 #pragma unroll
                 for (int k = 0; k < C; ++k) {
                     int kx, ti;
@@ -384,6 +385,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 }
             }
         }
+        if (dead) break;  // the item's sums are incomplete; the solve fails
         my_steps += lsteps;
         if (TRACE) return;
         if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
@@ -399,6 +401,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             }
         }
     }
+    if (dead) slab_drain(sbar, sphase);
     // per-warp counters and status
     for (int o = 16; o > 0; o >>= 1) {
         my_rays += __shfl_xor_sync(FULL, my_rays, o);
@@ -449,6 +452,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
     uint64_t *const sbar = &s_bar[threadIdx.x >> 5];
     uint32_t sphase = 0;
     slab_bar_init(sbar, lane);
+    bool dead = false;  // a slab copy did not arrive: this warp stops marching
 
     for (;;) {
         long long item;
@@ -561,7 +565,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                 if (!(u24(x.w) < e.prob)) e = P.entries[gs + (int)(e.alias_nb & 0xFFFFu)];
                 nbnd = (int)(e.alias_nb >> 16);
                 sid = e.koff;
-                load_slab(P, sid, slk, lane, sbar, &sphase, &flags);
+                if (!load_slab(P, sid, slk, lane, sbar, &sphase, &flags)) { dead = true; break; }
                 if (P.part) { const float2 pp = __ldg(P.part + nbnd); pab = pp.x; psc = pp.y; }
 #pragma unroll
                 for (int k = 0; k < C; ++k) {
@@ -860,6 +864,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                 }
             }
         }
+        if (dead) break;  // the item's sums are incomplete; the solve fails
         my_steps += lsteps;
         if (TRACE) return;
         if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
@@ -875,6 +880,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
             }
         }
     }
+    if (dead) slab_drain(sbar, sphase);
     // per-warp counters and status
     for (int o = 16; o > 0; o >>= 1) {
         my_rays += __shfl_xor_sync(FULL, my_rays, o);

@@ -72,7 +72,7 @@ int scratch_address(unsigned char **out) {
 using namespace dnsmc;
 
 extern "C" int dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu, const float *dT, double *dQ,
-                                        double *dvar, void *stream) {
+                                        double *dvar, uint32_t *dstatus, void *stream) {
     if (!cfg || !xu || !dT || !dQ || !dvar) return report_error(DNSMC_ERR_ARG, "null argument");
     const dnsmc_config &c = *cfg;
     if (c.model != DNSMC_MODEL_GREY) return report_error(DNSMC_ERR_ARG, "the allocation-free solve is grey only");
@@ -88,7 +88,10 @@ extern "C" int dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu
     if (c.grid_num != 1) return report_error(DNSMC_ERR_ARG, "grid_num must be 1");
     if (c.sampler != DNSMC_SAMPLER_IID) return report_error(DNSMC_ERR_ARG, "the allocation-free solve uses the IID sampler");
     if (c.nvar < 1 || c.photmax < 1) return report_error(DNSMC_ERR_ARG, "nvar and photmax must be >= 1");
-    if (!(c.toll > 0) || c.toll >= 1 || c.max_steps < 1) return report_error(DNSMC_ERR_ARG, "bad toll or max_steps");
+    if (!(c.toll > 0) || c.toll >= 1) return report_error(DNSMC_ERR_ARG, "toll must be in (0, 1)");
+    // the march counts crossings in FP32, exact below 2^22 (as the handle API)
+    if (c.max_steps < 1 || c.max_steps > (1 << 22))
+        return report_error(DNSMC_ERR_ARG, "max_steps must be in [1, 4194304]");
     if (!(c.eps_west == 1.0f) || !(c.eps_east == 1.0f)) return report_error(DNSMC_ERR_ARG, "walls must be black");
     if (!(c.kappa >= 0) || !(c.T_west >= 0) || !(c.T_east >= 0)) return report_error(DNSMC_ERR_ARG, "bad kappa or wall T");
     if (!(c.Ly > 0) || !(c.Lz > 0)) return report_error(DNSMC_ERR_ARG, "Ly and Lz must be > 0");
@@ -147,6 +150,7 @@ extern "C" int dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu
     P.toll = c.toll;
     P.dtoll = (float)(-log((double)c.toll));
     P.max_steps = c.max_steps;
+    P.slab_polls0 = kSlabWaitPolls;  // grey: no table slab is copied
     P.queue = misc;
     P.status = misc + 1;
     P.counters = counters;
@@ -154,7 +158,9 @@ extern "C" int dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu
     P.n_items = P.n_packets;
     P.tally = tally;
     const int threads = c.block_threads ? c.block_threads : 256;
-    const int blocks = device_sm_count() * march_occupancy(MODE_GREY, threads);
+    // persistent grid: resident blocks at the launch's dynamic shared memory
+    const size_t smem = march_smem(P, threads, kLaneCells);
+    const int blocks = device_sm_count() * march_occupancy_ex(MODE_GREY, threads, false, false, false, smem);
     rc = launch_march(MODE_GREY, P, blocks > 0 ? blocks : 1, threads, st, false);
     if (rc) return report_error(DNSMC_ERR_CUDA, cudaGetErrorString((cudaError_t)rc));
 
@@ -170,5 +176,12 @@ extern "C" int dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu
     F.status = misc + 1;
     rc = launch_finalize(F, st);
     if (rc) return report_error(DNSMC_ERR_CUDA, cudaGetErrorString((cudaError_t)rc));
+    // the status bits of this solve (bad temperature, step cap, non-finite
+    // contribution) into the caller's word: a device-to-device copy on the
+    // stream, after the finalize
+    if (dstatus) {
+        e = cudaMemcpyAsync(dstatus, misc + 1, sizeof(uint32_t), cudaMemcpyDeviceToDevice, st);
+        if (e != cudaSuccess) return report_error(DNSMC_ERR_CUDA, cudaGetErrorString(e));
+    }
     return DNSMC_OK;
 }

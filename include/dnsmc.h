@@ -263,6 +263,22 @@ int  dnsmc_wait(dnsmc_solver *s, double timeout_s);
  * snapshot slowest) the radiative source Q [W/m^3] (emission minus absorption)
  * and the standard error of Q.  Either pointer may be NULL.                    */
 int  dnsmc_get_results(dnsmc_solver *s, double *Q, double *sigma);
+/* Host result type of the next solves.  DNSMC_RESULT_F64 (default): Q and
+ * sigma cross to the host as doubles (16 bytes per cell), read with
+ * dnsmc_get_results.  DNSMC_RESULT_F32: the finalize kernel rounds Q and
+ * sigma to float on the device and only those cross (8 bytes per cell), read
+ * with dnsmc_get_results_float (the reference returns real(4) arrays,
+ * code/mc_gpu.cu:762-776; the drop-in pair uses this type).  No counterpart
+ * in the reference, which copies float solution and variance back and takes
+ * the square root on the host.                                              */
+#define DNSMC_RESULT_F64 0
+#define DNSMC_RESULT_F32 1
+int  dnsmc_set_result_type(dnsmc_solver *s, int type);
+/* Results of the last solve as floats, blocking (either pointer may be
+ * NULL); after a DNSMC_RESULT_F64 solve the doubles are rounded here.
+ * dnsmc_get_results fails with DNSMC_ERR_STATE after a DNSMC_RESULT_F32
+ * solve.                                                                    */
+int  dnsmc_get_results_float(dnsmc_solver *s, float *Q, float *sigma);
 /* Per band group: mean and variance of the mean, [field][group][cell].         */
 int  dnsmc_get_group_results(dnsmc_solver *s, double *Qg, double *varg);
 /* Spline-coarsened temperature of multigrid level 1..grid_num-1 of resident
@@ -434,14 +450,21 @@ int  dnsmc_cvnet_apply(dnsmc_cvnet *net, dnsmc_solver *s, int flags,
  * live in one fixed file-scope device array of about 5.3 MB that every GPU
  * loading the library holds until the process exits.
  *   xu   : host, imax+1 wall-normal face coordinates [m] (e.g. from
- *          dnsmc_get_geometry or the caller's own grid)
+ *          dnsmc_get_geometry or the caller's own grid), copied to the
+ *          device at every call, in stream order
  *   dT   : device, imax*jmax*kmax temperatures [K], dense, i fastest
  *   dQ   : device, imax*jmax*kmax doubles out: Q [W/m^3], dense, i fastest
  *   dvar : device, imax*jmax*kmax doubles out: variance of Q
+ *   dstatus: device, one uint32 out, or NULL: the DNSMC_STATUS_* bits of
+ *          this solve (DNSMC_STATUS_BAD_FIELD for a temperature <= 0 or
+ *          NaN, DNSMC_STATUS_STEP_CAP, DNSMC_STATUS_NONFINITE), written on
+ *          the stream after Q and var; read it once the stream has finished.
+ *          Q and var are not to be used when it is non-zero.
  *   stream: CUDA stream (NULL: default stream); the call only enqueues.
  * Limits: at most DNSMC_NOALLOC_MAX_CELLS cells and imax <= DNSMC_NOALLOC_MAX_IMAX;
- * larger grids return DNSMC_ERR_ARG.  The first call on a device looks up the
- * device address of the array (cudaGetSymbolAddress) with that device
+ * larger grids return DNSMC_ERR_ARG, as does max_steps outside
+ * [1, 4194304] (the handle API's bound).  The first call on a device looks
+ * up the device address of the array (cudaGetSymbolAddress) with that device
  * current; make that first call before any stream capture.  All calls share
  * the one array and it keeps the previous call's contents (each call clears
  * what must start at zero); calls whose work overlaps on the GPU (different
@@ -450,7 +473,7 @@ int  dnsmc_cvnet_apply(dnsmc_cvnet *net, dnsmc_solver *s, int flags,
 #define DNSMC_NOALLOC_MAX_IMAX  1024
 int  dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu,
                               const float *dT, double *dQ, double *dvar,
-                              void *stream);
+                              uint32_t *dstatus, void *stream);
 
 /* ---- reference drop-in (code/mc_gpu.cu:440, :640) -------------------------- */
 /* Tfort: real(4) TMC(0:imax+1,0:jmax+1,0:kmax+1), i fastest, whole domain with

@@ -9,7 +9,8 @@
   code/read_tables.cpp and code/spline.cpp compiled from where they lie under
   the reference tree with oracle/ref_shim/param.h standing in for the
   reference's compile-time code/param.h (-I- keeps the reference's own param.h
-  out of the search path).  Only built when the reference tree is present.
+  out of the search path).  Only built when the reference tree is present
+  (at $DNSMC_REFERENCE, default /root/reference).
 """
 from __future__ import annotations
 
@@ -18,7 +19,9 @@ import subprocess
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_CODE = "/root/reference/code"
+# the reference tree: DNSMC_REFERENCE, else the location in this build container
+REF_ROOT = os.environ.get("DNSMC_REFERENCE", "/root/reference")
+REF_CODE = os.path.join(REF_ROOT, "code")
 REF_DIR = os.path.join(HERE, "_ref")
 
 

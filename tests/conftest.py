@@ -14,7 +14,8 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
-REFERENCE = "/root/reference"
+# the reference tree (only the CPU tests that read it as text use it)
+REFERENCE = os.environ.get("DNSMC_REFERENCE", "/root/reference")
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 

@@ -385,6 +385,33 @@ def test_dropin_pair_layouts_and_ghosts():
     s.close()
 
 
+def test_float_results_are_the_rounded_double_results():
+    """DNSMC_RESULT_F32: the finalize kernel rounds Q and sigma to float on
+    the device and only those cross to the host; they equal the double
+    results rounded on the host, and the double getter refuses them."""
+    ni, nj, nk = 16, 24, 8
+    cfg = D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.28, Lz=3.14,
+                           stretched_x=1, T_west=300, T_east=500, kappa=0.7, nvar=2, photmax=16, seed=8)
+    T = smooth_field(ni, nj, nk, 400, 1200, 22)
+    s = D.Solver(cfg)
+    s.set_fields(T)
+    s.set_rays(32)
+    Q, S = s.solve(timeout_s=60)
+    s.set_result_type(D.RESULT_F32)
+    Qf, Sf = s.solve(timeout_s=60)
+    assert Qf.dtype == np.float32 and Sf.dtype == np.float32
+    np.testing.assert_array_equal(Qf, Q.astype(np.float32))
+    np.testing.assert_array_equal(Sf, S.astype(np.float32))
+    with pytest.raises(D.DnsmcError) as e:
+        s.results()
+    assert e.value.code == _lib.ERR_STATE
+    s.set_result_type(D.RESULT_F64)
+    Q2, _ = s.solve(timeout_s=60)
+    np.testing.assert_array_equal(Q2, Q)
+    np.testing.assert_array_equal(s.results_float()[0], Qf)
+    s.close()
+
+
 def test_dropin_reads_reference_tables_by_default(tmp_path, particle_tables, monkeypatch):
     write_particle_tables(str(tmp_path), particle_tables)
     monkeypatch.setenv("DNSMC_IMAX", "16")
