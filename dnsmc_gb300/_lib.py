@@ -123,6 +123,8 @@ SIGNATURES = {
     "dnsmc_solve_async": (ctypes.c_int, [ctypes.c_void_p]),
     "dnsmc_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "dnsmc_get_results": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
+    "dnsmc_save_table": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "dnsmc_load_table": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "dnsmc_set_result_type": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dnsmc_get_results_float": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p]),
     "dnsmc_get_group_results": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),

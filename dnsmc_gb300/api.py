@@ -16,6 +16,7 @@ CPU fallback: every call goes through libdnsmc.so.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -120,6 +121,14 @@ class Solver:
         for n, a in conv.items():
             setattr(d, n, _fp(a))
         check(self._lib.dnsmc_set_table(self._h, ctypes.byref(d)))
+
+    def save_table(self, path: str) -> None:
+        """Write the current table to a binary table file (dnsmc_save_table)."""
+        check(self._lib.dnsmc_save_table(self._h, os.fsencode(path)))
+
+    def load_table(self, path: str) -> None:
+        """Set the table from a binary table file (dnsmc_load_table)."""
+        check(self._lib.dnsmc_load_table(self._h, os.fsencode(path)))
 
     def table_info(self) -> dict:
         vals = [ctypes.c_int() for _ in range(4)] + [ctypes.c_float() for _ in range(4)]

@@ -204,85 +204,6 @@ void uniform_faces(int n, float L, std::vector<float> &u) {
     for (int i = 0; i <= n; ++i) u[i] = (float)i * d;
 }
 
-// Natural cubic spline second derivatives y2[1..n] of y[1..n] at x[1..n].
-void nat_spline(const float *x, const float *y, int n, float *y2, std::vector<float> &u) {
-    u.assign(n + 1, 0.0f);
-    y2[1] = u[1] = 0.0f;
-    for (int i = 2; i <= n - 1; ++i) {
-        const float sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
-        const float p = sig * y2[i - 1] + 2.0f;
-        y2[i] = (sig - 1.0f) / p;
-        const float ui = (y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]);
-        u[i] = (float)((6.0 * ui / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p);
-    }
-    y2[n] = 0.0f;
-    for (int k = n - 1; k >= 1; --k) y2[k] = y2[k] * y2[k + 1] + u[k];
-}
-
-// Cubic spline value at v (bisection for the bracketing interval).
-float nat_splint(const float *xa, const float *ya, const float *y2a, int n, float v) {
-    int lo = 1, hi = n;
-    while (hi - lo > 1) {
-        const int k = (hi + lo) >> 1;
-        if (xa[k] > v) hi = k; else lo = k;
-    }
-    const float h = xa[hi] - xa[lo];
-    const float a = (xa[hi] - v) / h, b = (v - xa[lo]) / h;
-    return (float)(a * ya[lo] + b * ya[hi] + ((a * a * a - a) * y2a[lo] + (b * b * b - b) * y2a[hi]) * (h * h) / 6.0);
-}
-
-// Coarsen one dense fine field T[k][j][i] (i fastest) to levels 1..L-1;
-// out[l] receives (im>>l)*(jm>>l)*(km>>l) values in the march layout
-// [i][k][j] (j fastest).
-void spline_coarsen(const float *T, int I, int J, int K, float Lx, float Ly, float Lz, int stretched, int levels,
-                    std::vector<std::vector<float>> &out) {
-    std::vector<float> xu, yu, zu, xc, yc, zc;
-    make_faces(I, Lx, stretched, xu);
-    uniform_faces(J, Ly, yu);
-    uniform_faces(K, Lz, zu);
-    centres(xu, xc);
-    centres(yu, yc);
-    centres(zu, zc);
-    out.assign(levels, {});
-    std::vector<float> a(std::max({I, J, K}) + 2), a2(std::max({I, J, K}) + 2), u;
-    for (int l = 1; l < levels; ++l) {
-        const int im = I >> l, jm = J >> l, km = K >> l;
-        std::vector<float> cxu, cyu, czu, cx, cy, cz;
-        coarse_faces(I, l, Lx, stretched, cxu);
-        uniform_faces(jm, Ly, cyu);
-        uniform_faces(km, Lz, czu);
-        centres(cxu, cx);
-        centres(cyu, cy);
-        centres(czu, cz);
-        // along x: tx[k][j][ic]
-        std::vector<float> tx((size_t)im * J * K), txy((size_t)im * jm * K);
-        for (int k = 0; k < K; ++k)
-            for (int j = 0; j < J; ++j) {
-                for (int i = 1; i <= I; ++i) a[i] = T[(size_t)i - 1 + (size_t)I * (j + (size_t)J * k)];
-                nat_spline(xc.data(), a.data(), I, a2.data(), u);
-                for (int i = 1; i <= im; ++i)
-                    tx[(size_t)i - 1 + (size_t)im * (j + (size_t)J * k)] = nat_splint(xc.data(), a.data(), a2.data(), I, cx[i]);
-            }
-        // along y: txy[k][jc][ic]
-        for (int i = 0; i < im; ++i)
-            for (int k = 0; k < K; ++k) {
-                for (int j = 1; j <= J; ++j) a[j] = tx[(size_t)i + (size_t)im * (j - 1 + (size_t)J * k)];
-                nat_spline(yc.data(), a.data(), J, a2.data(), u);
-                for (int j = 1; j <= jm; ++j)
-                    txy[(size_t)i + (size_t)im * (j - 1 + (size_t)jm * k)] = nat_splint(yc.data(), a.data(), a2.data(), J, cy[j]);
-            }
-        // along z, into the march layout [ic][kc][jc]
-        out[l].assign((size_t)im * jm * km, 0.0f);
-        for (int i = 0; i < im; ++i)
-            for (int j = 0; j < jm; ++j) {
-                for (int k = 1; k <= K; ++k) a[k] = txy[(size_t)i + (size_t)im * (j + (size_t)jm * (k - 1))];
-                nat_spline(zc.data(), a.data(), K, a2.data(), u);
-                for (int k = 1; k <= km; ++k)
-                    out[l][((size_t)i * km + (k - 1)) * jm + j] = nat_splint(zc.data(), a.data(), a2.data(), K, cz[k]);
-            }
-    }
-}
-
 // Sobol' direction numbers of four dimensions (Bratley-Fox recurrence on the
 // primitive polynomials 1, x+1, x^2+x+1, x^3+x+1 with initial m = 1 | 1 |
 // 1,3 | 1,3,1), 32 bits.
@@ -395,6 +316,7 @@ struct dnsmc_solver {
 
     // multigrid: spline-coarsened temperatures of levels 1..grid_num-1
     DevBuf<float> d_mgT, d_mgfw;
+    DevBuf<float> d_mgpos, d_mgtmp;          // spline positions; coarsening passes' scratch
     long long mg_off[kMaxLevels] = {0};
     int mg_fwoff[kMaxLevels] = {0};
     int mg_fields = 0;
@@ -1348,37 +1270,94 @@ int wait_done(dnsmc_solver *s, double timeout_s) {
     return DNSMC_OK;
 }
 
-// Coarse temperatures of every field for the multigrid march; Tdense(f)
-// gives field f dense, i fastest.
-template <class Get>
-int upload_coarse(dnsmc_solver *s, int nfields, Get Tdense) {
+// Coarse temperatures of every field for the multigrid march: the spline
+// coarsening (interp3D) on the device from the packed fine temperatures
+// (src: [f][i][k][j], T every src_step floats), three passes per level and
+// field on the solver's stream; the coarse wall-normal faces of every level.
+int upload_coarse(dnsmc_solver *s, int nfields, const float *src, int src_step) {
     const dnsmc_config &c = s->cfg;
     const int G = c.grid_num;
+    const int I = c.imax, J = c.jmax, K = c.kmax;
+    const long long ncell = (long long)I * J * K;
     long long off = 0;
     for (int l = 1; l < G; ++l) {
         s->mg_off[l] = off;
-        off += (long long)nfields * (c.imax >> l) * (c.jmax >> l) * (c.kmax >> l);
+        off += (long long)nfields * (I >> l) * (J >> l) * (K >> l);
     }
-    std::vector<float> all((size_t)std::max(1LL, off));
-    std::vector<std::vector<float>> lv;
-    for (int f = 0; f < nfields; ++f) {
-        spline_coarsen(Tdense(f), c.imax, c.jmax, c.kmax, c.Lx, c.Ly, c.Lz, c.stretched_x, G, lv);
-        for (int l = 1; l < G; ++l)
-            std::copy(lv[l].begin(), lv[l].end(), all.begin() + s->mg_off[l] + (long long)f * lv[l].size());
-    }
+    // cell-centre positions, 1-based: fine x, y, z, then per level coarse x, y, z
+    std::vector<float> xu, yu, zu, pos, cen;
+    make_faces(I, c.Lx, c.stretched_x, xu);
+    uniform_faces(J, c.Ly, yu);
+    uniform_faces(K, c.Lz, zu);
+    long long po[kMaxLevels][3] = {}, pf[3];
+    auto put = [&](const std::vector<float> &u) {
+        centres(u, cen);
+        const long long o = (long long)pos.size();
+        pos.insert(pos.end(), cen.begin(), cen.end());
+        return o;
+    };
+    pf[0] = put(xu); pf[1] = put(yu); pf[2] = put(zu);
     std::vector<float> faces;
     int fo = 0;
     for (int l = 1; l < G; ++l) {
-        std::vector<float> xu;
-        coarse_faces(c.imax, l, c.Lx, c.stretched_x, xu);
+        std::vector<float> cxu, cyu, czu;
+        coarse_faces(I, l, c.Lx, c.stretched_x, cxu);
+        uniform_faces(J >> l, c.Ly, cyu);
+        uniform_faces(K >> l, c.Lz, czu);
+        po[l][0] = put(cxu); po[l][1] = put(cyu); po[l][2] = put(czu);
         s->mg_fwoff[l] = fo;
-        faces.insert(faces.end(), xu.begin(), xu.end());
-        fo += (int)xu.size();
+        faces.insert(faces.end(), cxu.begin(), cxu.end());
+        fo += (int)cxu.size();
     }
-    TRY(s->d_mgT.ensure(all.size()));
+    const int im1 = I >> 1, jm1 = J >> 1;
+    const long long ntmp = (long long)im1 * J * K + (long long)im1 * jm1 * K;  // level 1 is the largest
+    const long long nwork = 3 * std::max({(long long)(I + 2) * J * K, (long long)(J + 2) * im1 * K,
+                                          (long long)(K + 2) * im1 * jm1});
+    TRY(s->d_mgT.ensure((size_t)std::max(1LL, off)));
     TRY(s->d_mgfw.ensure(faces.size()));
-    CUDA_TRY(cudaMemcpy(s->d_mgT.p, all.data(), all.size() * sizeof(float), cudaMemcpyHostToDevice));
-    CUDA_TRY(cudaMemcpy(s->d_mgfw.p, faces.data(), faces.size() * sizeof(float), cudaMemcpyHostToDevice));
+    TRY(s->d_mgpos.ensure(pos.size()));
+    TRY(s->d_mgtmp.ensure((size_t)(ntmp + nwork)));
+    CUDA_TRY(cudaMemcpyAsync(s->d_mgfw.p, faces.data(), faces.size() * sizeof(float), cudaMemcpyHostToDevice,
+                             s->stream));
+    CUDA_TRY(cudaMemcpyAsync(s->d_mgpos.p, pos.data(), pos.size() * sizeof(float), cudaMemcpyHostToDevice,
+                             s->stream));
+    const float *P = s->d_mgpos.p;
+    float *tx = s->d_mgtmp.p;
+    float *work = tx + ntmp;
+    for (int f = 0; f < nfields; ++f)
+        for (int l = 1; l < G; ++l) {
+            const int im = I >> l, jm = J >> l, km = K >> l;
+            float *txy = tx + (long long)im * J * K;
+            SplinePass q{};
+            q.work = work;
+            // along x: fine [i][k][j] -> tx [ic][k][j], lines (j, k)
+            q.src = src + (long long)f * ncell * src_step; q.src_step = src_step;
+            q.s_a = 1; q.s_b = J; q.s_e = (long long)J * K;
+            q.dst = tx; q.d_a = 1; q.d_b = J; q.d_e = (long long)J * K;
+            q.na = J; q.nlines = (long long)J * K; q.n = I; q.m = im;
+            q.xf = P + pf[0]; q.xc = P + po[l][0];
+            int rc = launch_spline_pass(q, s->stream);
+            // along y: tx [ic][k][j] -> txy [ic][k][jc], lines (ic, k)
+            if (!rc) {
+                q.src = tx; q.src_step = 1;
+                q.s_a = (long long)K * J; q.s_b = J; q.s_e = 1;
+                q.dst = txy; q.d_a = (long long)K * jm; q.d_b = jm; q.d_e = 1;
+                q.na = im; q.nlines = (long long)im * K; q.n = J; q.m = jm;
+                q.xf = P + pf[1]; q.xc = P + po[l][1];
+                rc = launch_spline_pass(q, s->stream);
+            }
+            // along z: txy [ic][k][jc] -> the march layout [ic][kc][jc], lines (jc, ic)
+            if (!rc) {
+                q.src = txy;
+                q.s_a = 1; q.s_b = (long long)K * jm; q.s_e = jm;
+                q.dst = s->d_mgT.p + s->mg_off[l] + (long long)f * im * jm * km;
+                q.d_a = 1; q.d_b = (long long)km * jm; q.d_e = jm;
+                q.na = jm; q.nlines = (long long)jm * im; q.n = K; q.m = km;
+                q.xf = P + pf[2]; q.xc = P + po[l][2];
+                rc = launch_spline_pass(q, s->stream);
+            }
+            if (rc) return fail(DNSMC_ERR_CUDA, "spline coarsening launch: %s", cudaGetErrorString((cudaError_t)rc));
+        }
     s->mg_fields = nfields;
     return DNSMC_OK;
 }
@@ -1438,18 +1417,8 @@ int upload_fields_host(dnsmc_solver *s, int nfields, const float *T, const float
     }
     double st[4];
     TRY(field_stats_checked(s, nfields, want_x, st));
-    if (c.grid_num > 1) {
-        std::vector<float> dense;
-        TRY(upload_coarse(s, nfields, [&](int f) -> const float * {
-            if (layout == DNSMC_LAYOUT_DENSE) return T + f * nsrc;
-            dense.resize((size_t)ncell);
-            for (int k = 0; k < c.kmax; ++k)
-                for (int j = 0; j < c.jmax; ++j)
-                    for (int i = 0; i < c.imax; ++i)
-                        dense[(size_t)i + (size_t)c.imax * (j + (size_t)c.jmax * k)] = T[f * nsrc + base + j * sj + k * sk + i];
-            return dense.data();
-        }));
-    }
+    if (c.grid_num > 1)
+        TRY(upload_coarse(s, nfields, want_x ? (const float *)s->d_fieldTX.p : s->d_fieldT.p, want_x ? 2 : 1));
     s->nfields = nfields;
     s->have_x = want_x;
     s->tmax_fields = (float)st[0];
@@ -1640,7 +1609,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release();
     s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_rays_rcp.release(); s->d_item_steps.release(); s->d_kP.release();
     s->d_order.release(); s->d_order_hist.release();
-    s->d_mgT.release(); s->d_mgfw.release();
+    s->d_mgT.release(); s->d_mgfw.release(); s->d_mgpos.release(); s->d_mgtmp.release();
     s->d_part.release(); s->d_fieldV.release(); s->d_layerV.release();
     s->d_entries.release(); s->d_group_start.release(); s->d_group_empty.release();
     s->d_tally.release(); s->d_Q.release(); s->d_var.release(); s->d_sig.release(); s->h_sig.release(); s->d_Qg.release(); s->d_varg.release();
@@ -1715,6 +1684,104 @@ int dnsmc_set_table(dnsmc_solver *s, const dnsmc_table_desc *d) {
     return DNSMC_OK;
 }
 
+// ---- binary table file (no counterpart in the reference) -------------------
+// The reference reads its tables from text every call (code/read_tables.cpp,
+// written by distr/write_tables.cpp:23-107) and has no x_H2O axis.  This
+// file holds the whole k(band, g, T, x) table once, little-endian:
+//   72-byte header: magic "DNSMCKT1", u32 version (1), u32 header bytes (72),
+//   i32 nbands, nq, nT, nX, f32 T0, dT, X0, dX, u32 flags (1: Ib, 2: the
+//   reference CDFs prob and kP, 4: the g CDF probg), u32 0, u64 payload
+//   bytes, u64 FNV-1a hash of the payload;
+//   payload, float32: k[nbands][nq][nT][nX], wvc[nbands], dnu[nbands],
+//   wq[nq], then Ib[nbands][nT], prob[nT][nbands] and kP[nT],
+//   probg[nT][nbands][nq] as flagged.
+namespace {
+constexpr char kTabMagic[8] = {'D', 'N', 'S', 'M', 'C', 'K', 'T', '1'};
+constexpr uint32_t kTabHeader = 72;
+
+uint64_t fnv1a(const unsigned char *p, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
+    for (size_t i = 0; i < n; ++i) { h ^= p[i]; h *= 0x100000001b3ull; }
+    return h;
+}
+void put_u32(std::vector<unsigned char> &b, uint32_t v) { for (int i = 0; i < 4; ++i) b.push_back((unsigned char)(v >> (8 * i))); }
+void put_u64(std::vector<unsigned char> &b, uint64_t v) { for (int i = 0; i < 8; ++i) b.push_back((unsigned char)(v >> (8 * i))); }
+void put_f32(std::vector<unsigned char> &b, float f) { uint32_t v; memcpy(&v, &f, 4); put_u32(b, v); }
+uint32_t get_u32(const unsigned char *p) { return (uint32_t)p[0] | (uint32_t)p[1] << 8 | (uint32_t)p[2] << 16 | (uint32_t)p[3] << 24; }
+uint64_t get_u64(const unsigned char *p) { return (uint64_t)get_u32(p) | (uint64_t)get_u32(p + 4) << 32; }
+float get_f32(const unsigned char *p) { const uint32_t v = get_u32(p); float f; memcpy(&f, &v, 4); return f; }
+}  // namespace
+
+int dnsmc_save_table(const dnsmc_solver *s, const char *path) {
+    if (!s || !path) return fail(DNSMC_ERR_ARG, "null argument");
+    if (s->tab.grey_bands) return fail(DNSMC_ERR_STATE, "the reference grey tables are rebuilt at every solve");
+    if (!s->tab.valid) return fail(DNSMC_ERR_STATE, "no table to save");
+    const HostTable &t = s->tab;
+    const uint32_t flags = (t.Ib.empty() ? 0u : 1u) | (t.ref_sampling ? 2u : 0u) | (t.probg.empty() ? 0u : 4u);
+    std::vector<unsigned char> pay;
+    auto arr = [&](const std::vector<float> &v) { for (float f : v) put_f32(pay, f); };
+    arr(t.k); arr(t.wvc); arr(t.dnu); arr(t.wq);
+    if (flags & 1u) arr(t.Ib);
+    if (flags & 2u) { arr(t.prob); arr(t.kP); }
+    if (flags & 4u) arr(t.probg);
+    std::vector<unsigned char> h(kTabMagic, kTabMagic + 8);
+    put_u32(h, 1); put_u32(h, kTabHeader);
+    put_u32(h, (uint32_t)t.nbands); put_u32(h, (uint32_t)t.nq); put_u32(h, (uint32_t)t.nT); put_u32(h, (uint32_t)t.nX);
+    put_f32(h, t.T0); put_f32(h, t.dT); put_f32(h, t.X0); put_f32(h, t.dX);
+    put_u32(h, flags); put_u32(h, 0);
+    put_u64(h, (uint64_t)pay.size()); put_u64(h, fnv1a(pay.data(), pay.size()));
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(DNSMC_ERR_IO, "cannot open %s for writing", path);
+    const bool ok = fwrite(h.data(), 1, h.size(), f) == h.size() && fwrite(pay.data(), 1, pay.size(), f) == pay.size();
+    if (fclose(f) != 0 || !ok) return fail(DNSMC_ERR_IO, "short write to %s", path);
+    return DNSMC_OK;
+}
+
+int dnsmc_load_table(dnsmc_solver *s, const char *path) {
+    if (!s || !path) return fail(DNSMC_ERR_ARG, "null argument");
+    FILE *f = fopen(path, "rb");
+    if (!f) return fail(DNSMC_ERR_IO, "cannot open %s", path);
+    unsigned char h[kTabHeader];
+    if (fread(h, 1, kTabHeader, f) != kTabHeader) { fclose(f); return fail(DNSMC_ERR_IO, "%s: short header", path); }
+    if (memcmp(h, kTabMagic, 8) != 0) { fclose(f); return fail(DNSMC_ERR_IO, "%s: not a dnsmc table file", path); }
+    if (get_u32(h + 8) != 1 || get_u32(h + 12) != kTabHeader) {
+        fclose(f);
+        return fail(DNSMC_ERR_IO, "%s: unsupported table file version", path);
+    }
+    const int nb = (int)get_u32(h + 16), nq = (int)get_u32(h + 20), nT = (int)get_u32(h + 24), nX = (int)get_u32(h + 28);
+    const uint32_t flags = get_u32(h + 48);
+    const uint64_t nbytes = get_u64(h + 56), hash = get_u64(h + 64);
+    if (nb < 1 || nq < 1 || nT < 2 || nX < 1 || nb > 65535 || nq > 4096 || nT > 1000000 || nX > 1000000 || (flags & ~7u)) {
+        fclose(f);
+        return fail(DNSMC_ERR_IO, "%s: bad table sizes in the header", path);
+    }
+    const uint64_t nk = (uint64_t)nb * nq * nT * nX;
+    uint64_t nf = nk + 2ull * nb + nq;
+    if (flags & 1u) nf += (uint64_t)nb * nT;
+    if (flags & 2u) nf += (uint64_t)nT * nb + nT;
+    if (flags & 4u) nf += (uint64_t)nT * nb * nq;
+    if (nbytes != 4 * nf || nf > (1ull << 32)) { fclose(f); return fail(DNSMC_ERR_IO, "%s: payload size does not match the header", path); }
+    std::vector<unsigned char> pay((size_t)nbytes);
+    const size_t got = fread(pay.data(), 1, pay.size(), f);
+    const bool extra = fgetc(f) != EOF;
+    fclose(f);
+    if (got != pay.size() || extra) return fail(DNSMC_ERR_IO, "%s: payload length differs from the header", path);
+    if (fnv1a(pay.data(), pay.size()) != hash) return fail(DNSMC_ERR_IO, "%s: payload checksum mismatch", path);
+    std::vector<float> v((size_t)nf);
+    for (size_t i = 0; i < v.size(); ++i) v[i] = get_f32(pay.data() + 4 * i);
+    const float *p = v.data();
+    dnsmc_table_desc d{};
+    d.nbands = nb; d.nq = nq; d.nT = nT; d.nX = nX;
+    d.T0 = get_f32(h + 32); d.dT = get_f32(h + 36); d.X0 = get_f32(h + 40); d.dX = get_f32(h + 44);
+    d.k = p; p += nk;
+    d.wvc = p; p += nb;
+    d.dnu = p; p += nb;
+    d.wq = p; p += nq;
+    if (flags & 1u) { d.Ib = p; p += (size_t)nb * nT; }
+    if (flags & 2u) { d.prob = p; p += (size_t)nT * nb; d.kP = p; p += nT; }
+    if (flags & 4u) { d.probg = p; p += (size_t)nT * nb * nq; }
+    return dnsmc_set_table(s, &d);
+}
+
 int dnsmc_get_table_info(const dnsmc_solver *s, int *nbands, int *nq, int *nT, int *nX, float *T0, float *dT,
                          float *X0, float *dX) {
     if (!s) return fail(DNSMC_ERR_ARG, "null solver");
@@ -1778,13 +1845,8 @@ int dnsmc_set_fields_device(dnsmc_solver *s, int nfields, const float *dT, const
     }
     double st[4];
     TRY(field_stats_checked(s, nfields, dx != nullptr, st));
-    if (c.grid_num > 1) {  // the spline coarsening runs on the host
-        std::vector<float> h((size_t)ncell);
-        TRY(upload_coarse(s, nfields, [&](int f) -> const float * {
-            cudaMemcpy(h.data(), dT + f * ncell, (size_t)ncell * sizeof(float), cudaMemcpyDeviceToHost);
-            return h.data();
-        }));
-    }
+    if (c.grid_num > 1)
+        TRY(upload_coarse(s, nfields, dx ? (const float *)s->d_fieldTX.p : s->d_fieldT.p, dx ? 2 : 1));
     s->nfields = nfields;
     s->have_x = dx != nullptr;
     s->tmax_fields = (float)st[0];
@@ -1956,6 +2018,7 @@ int dnsmc_get_coarse_field(dnsmc_solver *s, int field, int level, float *T) {
     const int im = c.imax >> level, jm = c.jmax >> level, km = c.kmax >> level;
     const size_t n = (size_t)im * jm * km;
     std::vector<float> h(n);
+    CUDA_TRY(cudaStreamSynchronize(s->stream));  // the coarsening runs on the solver's stream
     CUDA_TRY(cudaMemcpy(h.data(), s->d_mgT.p + s->mg_off[level] + (long long)field * n, n * sizeof(float),
                         cudaMemcpyDeviceToHost));
     for (int i = 0; i < im; ++i)

@@ -220,6 +220,24 @@ constexpr int kOrderBuckets = 4096;
 int launch_item_order(const int *rays, int gstride, int n_packets, int n_groups, long long n_items, int B,
                       unsigned int *hist, unsigned int *order, void *stream);
 
+// One pass of the spline coarsening (interp3D, code/spline.cpp:35-116) over
+// nlines = na * nb lines: line (la, lb) reads n fine values at
+// src[(la*s_a + lb*s_b + (i-1)*s_e) * src_step] (positions xf[1..n]) and
+// writes m coarse values at dst[la*d_a + lb*d_b + (c-1)*d_e] (positions
+// xc[1..m]); work holds 3 * (n + 2) * nlines floats.
+struct SplinePass {
+    const float *src;
+    long long s_a, s_b, s_e;
+    int src_step;             // floats per source element (2: T of a (T, x) pair)
+    float *dst;
+    long long d_a, d_b, d_e;
+    long long na, nlines;
+    int n, m;
+    const float *xf, *xc;     // 1-based device arrays of n + 2 and m + 2 floats
+    float *work;
+};
+int launch_spline_pass(const SplinePass &q, void *stream);
+
 // launchers (mc_kernels.cu); all stream-ordered
 int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                     bool mom, bool gen);

@@ -864,6 +864,67 @@ int launch_finalize(const FinalizeParams &p, void *stream) {
     return (int)cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Spline coarsening of the temperature for the multigrid march: the
+// reference's interp3D (code/spline.cpp:35-116), a separable natural cubic
+// spline through the fine cell centres along x, then y, then z, evaluated at
+// the coarse cell centres.  One thread per spline line; each pass is one
+// launch.  The arithmetic is the Numerical Recipes spline / splint of
+// code/spline.cpp:119-170 written as the oracle restates it (float with the
+// same double sub-expressions; this translation unit is compiled with
+// -fmad=false), so the coarse fields are bit-identical to the oracle's.
+// ---------------------------------------------------------------------------
+__global__ void spline_pass_kernel(SplinePass q) {
+    for (long long L = blockIdx.x * (long long)blockDim.x + threadIdx.x; L < q.nlines;
+         L += (long long)gridDim.x * blockDim.x) {
+        const long long la = L % q.na, lb = L / q.na;
+        const float *src = q.src + (la * q.s_a + lb * q.s_b) * q.src_step;
+        float *dst = q.dst + la * q.d_a + lb * q.d_b;
+        // this line's work arrays, interleaved across lines (1-based, n + 2)
+        float *a = q.work + L;
+        float *y2 = a + (long long)(q.n + 2) * q.nlines;
+        float *u = y2 + (long long)(q.n + 2) * q.nlines;
+        const long long w = q.nlines;
+        const float *x = q.xf;
+        const int n = q.n;
+        for (int i = 1; i <= n; ++i) a[i * w] = src[(long long)(i - 1) * q.s_e * q.src_step];
+        // second derivatives (natural end conditions)
+        y2[1 * w] = 0.0f;
+        u[1 * w] = 0.0f;
+        for (int i = 2; i <= n - 1; ++i) {
+            const float sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+            const float p = sig * y2[(i - 1) * w] + 2.0f;
+            y2[i * w] = (sig - 1.0f) / p;
+            const float ui = (a[(i + 1) * w] - a[i * w]) / (x[i + 1] - x[i]) -
+                             (a[i * w] - a[(i - 1) * w]) / (x[i] - x[i - 1]);
+            u[i * w] = (float)((6.0 * ui / (x[i + 1] - x[i - 1]) - sig * u[(i - 1) * w]) / p);
+        }
+        y2[n * w] = 0.0f;
+        for (int k = n - 1; k >= 1; --k) y2[k * w] = y2[k * w] * y2[(k + 1) * w] + u[k * w];
+        // values at the coarse centres (bisection for the bracket)
+        for (int c = 1; c <= q.m; ++c) {
+            const float v = q.xc[c];
+            int lo = 1, hi = n;
+            while (hi - lo > 1) {
+                const int k = (hi + lo) >> 1;
+                if (x[k] > v) hi = k; else lo = k;
+            }
+            const float h = x[hi] - x[lo];
+            const float aa = (x[hi] - v) / h, bb = (v - x[lo]) / h;
+            const float ylo = a[lo * w], yhi = a[hi * w];
+            dst[(long long)(c - 1) * q.d_e] =
+                (float)(aa * ylo + bb * yhi +
+                        ((aa * aa * aa - aa) * y2[lo * w] + (bb * bb * bb - bb) * y2[hi * w]) * (h * h) / 6.0);
+        }
+    }
+}
+
+int launch_spline_pass(const SplinePass &q, void *stream) {
+    if (q.nlines <= 0) return 0;
+    spline_pass_kernel<<<grid_for(q.nlines, 128), 128, 0, (cudaStream_t)stream>>>(q);
+    return (int)cudaGetLastError();
+}
+
 int launch_pack_T(const float *src, float *dst, int nw, int na, int nb, long long si, long long sj,
                   long long sk, long long base, void *stream) {
     const long long n = (long long)nw * na * nb;

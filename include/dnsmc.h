@@ -186,6 +186,17 @@ int  dnsmc_load_tables_ref(dnsmc_solver *s, const char *dir, int model,
 int  dnsmc_use_grey_band_tables(dnsmc_solver *s, int nB, int nT, float wvmax,
                                 float Tmin);
 int  dnsmc_set_table(dnsmc_solver *s, const dnsmc_table_desc *t);
+/* Binary table file (no counterpart in the reference, which parses its text
+ * tables at every call, code/read_tables.cpp, as distr/write_tables.cpp:23-107
+ * wrote them, and has no x_H2O axis): the solver's current table -- k(band, g,
+ * T, x_H2O), band centres and widths, g weights, and the optional band Ib and
+ * reference CDFs -- in one little-endian file with a 72-byte header (magic
+ * "DNSMCKT1", version, sizes, grids, flags, payload length and its FNV-1a
+ * hash) followed by float32 arrays.  dnsmc_load_table checks the header,
+ * length and hash (DNSMC_ERR_IO) and then sets the table as dnsmc_set_table
+ * does.  Parsed once, a table file serves every later solver.               */
+int  dnsmc_save_table(const dnsmc_solver *s, const char *path);
+int  dnsmc_load_table(dnsmc_solver *s, const char *path);
 /* Copy of the parsed table (host arrays of the sizes in the desc); any pointer
  * may be NULL.  For tests of the parsers.                                      */
 int  dnsmc_get_table_info(const dnsmc_solver *s, int *nbands, int *nq, int *nT,

@@ -40,6 +40,32 @@ def test_coarse_fields_match_the_oracle(stretched):
     s.close()
 
 
+def test_coarse_fields_from_device_inputs_and_with_x():
+    """The coarsening reads the packed device field: fields given as device
+    arrays, and fields carrying x_H2O (the T of each (T, x) pair), give the
+    same coarse temperatures as host temperatures alone."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from dnsmc_gb300 import _lib
+    ni, nj, nk = 24, 16, 8
+    cfg = D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.28, Lz=3.14,
+                           stretched_x=1, grid_num=3, kappa=1.0, T_west=300, T_east=300)
+    T = smooth_field(ni, nj, nk, 450, 1300, 9)
+    ref = D.Solver(cfg)
+    ref.set_fields(T)
+    a = D.Solver(cfg)
+    dT = torch.from_numpy(T).cuda()
+    torch.cuda.synchronize()
+    _lib.check(a._lib.dnsmc_set_fields_device(a._h, 1, ctypes.c_void_p(dT.data_ptr()), None))
+    b = D.Solver(cfg)
+    b.set_fields(T, np.full(T.shape, 0.1, np.float32))
+    for lv in (1, 2):
+        np.testing.assert_array_equal(a.coarse_field(0, lv), ref.coarse_field(0, lv))
+        np.testing.assert_array_equal(b.coarse_field(0, lv), ref.coarse_field(0, lv))
+    for s in (ref, a, b):
+        s.close()
+
+
 def traces_reach_coarse_levels(s, T, x=None, n=12):
     c, keep = O.packet_config(s, T, x)
     npk = s.packet_count()
