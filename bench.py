@@ -3,14 +3,14 @@ channel (synthetic k(band, g, T, x_H2O) table of 64 bands x 16 g x 50 T x 8 x,
 8 band groups), plus rays/s.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
-                    [--method net|cv|plain]
+                    [--method net|cv|plain] [--workload ck128|grey64|batched|particles]
 
 A step is one full solve of one Q_r field with the inputs resident in HBM,
 timed with CUDA events on the solver's stream: for the default network
 control variate, the network's features, forward pass and ray allocation,
 then the sampling-table upload, the control-variate preparation, the march,
-the finalize kernel (Q and sigma = sqrt(var) on the device) and the copy of
-Q and sigma into pinned host memory.  The
+the finalize kernel (Q and sigma = sqrt(var), rounded to float on the
+device) and the copy of the float Q and sigma into pinned host memory.  The
 network is the committed one for the grid (dnsmc_gb300/nets/ck128_g8.cvnet) or,
 when absent, trained before the timed region on 16 snapshots the Monte Carlo
 itself produces.  The ray budget (mean rays per cell and group) is the
@@ -21,8 +21,21 @@ its own 1 % budget and plain MC is extrapolated from a pilot, for the
 comparison block.  Inputs (16.8 MB) fit in L2, so L2 is flushed (a 256 MB
 device write) before every timed step.  `e2e` repeats the step through the
 public API from host arrays: dnsmc_set_fields (host->device, packing and
-the field checks on the device) + network + solve + dnsmc_get_results
-(pinned host memory -> the caller's arrays), wall clock.
+the field checks on the device) + network + solve +
+dnsmc_get_results_float (the float results into the caller's arrays), wall
+clock.  `gpu_launches` counts this library's kernels in the timed region
+(dnsmc_get_launch_count).
+
+`validation` states the timed field's error against the oracle's FP64
+solution (64 x the timed rays, its own control variate and exact means, on
+2048 cells) and against a GPU solution of the whole field at 1024 rays per
+cell and group.  `roofline` is the march's instruction-issue bound:
+warp instructions per SM cycle from the per-lane-step counts of the
+committed ncu capture (profiles/march_pair_kernel_ck128_counters.md) and
+the lane-steps and march time of this run, beside its gather rate and DRAM
+traffic.  `c0` is the grey 64^3 channel (plain MC at 1 %, the reference's
+grey-band representation beside the CPU reference on the same tables, and
+the isothermal slab against its analytic E2 solution).
 
 With --gpus N (torchrun), every rank solves its own snapshots (seed = rank):
 cells are independent, no collective is needed; the whole-job value is the
@@ -138,7 +151,19 @@ def make_solver(table, T_wall, seed, threads=0, cv=1):
 
 
 def rms_error(Q, S):
+    Q = np.asarray(Q, np.float64)
+    S = np.asarray(S, np.float64)
     return float(math.sqrt(float((S ** 2).mean())) / math.sqrt(float((Q ** 2).mean())))
+
+
+def _result_f32():
+    from dnsmc_gb300 import _lib
+    return _lib.RESULT_F32
+
+
+def _launches():
+    from dnsmc_gb300 import _lib
+    return _lib.launch_count()
 
 
 def plain_extrapolated(table, T, x, T_wall, seed, pilot=128):
@@ -197,62 +222,216 @@ def barrier_max(pg, value):
     return float(t.item())
 
 
-def cpu_reference(table, T, x, T_wall, rays_per_cell, sample_cells=96, budget_s=20.0):
-    """Reference estimator (oracle port, FP32 as the reference build) on all
-    host cores over a sample of cells; returns rays/s and ms per field at 1 %."""
+def _ref_sample(Tf, n, cells, kw, budget_s):
+    """Time the oracle's reference estimator on `cells` with photmax grown
+    until one run takes about budget_s / 4; returns (result, seconds, photmax)."""
     from oracle import oracle as O
-    from dnsmc_gb300 import synth  # noqa: F401
-    n = N_CELL
-    xbar = float(x.mean())
-    # x-uniform slice of the table in the reference layout (the reference has
-    # no x_H2O axis): k(band, T, g) at xbar, CDFs and Planck mean from it.
-    X = table["X0"] + table["dX"] * np.arange(table["k"].shape[3])
-    kx = np.empty(table["k"].shape[:3], np.float64)
-    for b in range(kx.shape[0]):
-        for g in range(kx.shape[1]):
-            kx[b, g] = [np.interp(xbar, X, table["k"][b, g, t]) for t in range(kx.shape[2])]
-    nT = kx.shape[2]
-    Tnb = (table["T0"] + table["dT"] * np.arange(nT)).astype(np.float32)
-    C1, C2 = 3.741771790075259e-16, 0.014387741858429
-    nu = table["wvc"].astype(np.float64)
-    Ib = C1 * (nu[None, :] * 100) ** 3 / (np.pi * (np.exp(C2 * nu[None, :] * 100 / Tnb[:, None]) - 1))  # [nT][nB]
-    e = kx.transpose(2, 0, 1) * Ib[:, :, None] * table["dnu"][None, :, None] * 100 * table["wq"][None, None, :]
-    eb = e.sum(2)
-    prob = np.cumsum(eb, 1) / eb.sum(1, keepdims=True)
-    probg = np.cumsum(e, 2) / np.maximum(e.sum(2, keepdims=True), 1e-300)
-    kP = np.pi * eb.sum(1) / (5.670373e-08 * Tnb.astype(np.float64) ** 4)
-    tables = dict(Tnb=Tnb, kq=kx.transpose(0, 2, 1).astype(np.float32), wvc=table["wvc"],
-                  prob=prob.astype(np.float32), probg=probg.astype(np.float32), kP=kP.astype(np.float32))
-    Tf = np.zeros((n + 2, n + 2, n + 2), np.float32)
-    Tf[1:-1, 1:-1, 1:-1] = T
-    rng = np.random.default_rng(0)
-    cells = np.stack([rng.integers(1, n + 1, sample_cells) for _ in range(3)], 1)
-    cores = os.cpu_count() or 1
     photmax = 64
-    kw = dict(imax=n, jmax=n, kmax=n, Lx=2.0, Ly=2 * math.pi, Lz=math.pi, T_west=T_wall, T_east=T_wall, model=0,
-              tables=tables, nvar=2, grid_num=1, stretched=0, use_double=0, seed=5, threads=cores)
     while True:
         t0 = time.perf_counter()
         r = O.ref_mc(Tf.ravel(), cells, photmax=photmax, **kw)
         dt = time.perf_counter() - t0
         if dt > budget_s / 4 or photmax >= 1 << 16:
-            break
+            return r, dt, photmax
         photmax = int(photmax * max(2.0, min(8.0, budget_s / 4 / max(dt, 1e-3))))
-    rays = sample_cells * 2 * photmax
+
+
+def _ref_field_ms(r, dt, photmax, nvar, ncell_field, sample_cells):
+    """ms per field at 1 % RMS from a timed sample: per-ray variance of each
+    sampled cell, rays per cell for 1 % of the sample's RMS Q, time per ray."""
+    rays = sample_cells * nvar * photmax
     rays_s = rays / dt
-    nr = 2 * photmax
-    var_ray = (r["se"] ** 2 * nr)  # per-ray variance of each sampled cell
+    var_ray = r["se"] ** 2 * (nvar * photmax)
     qrms = math.sqrt(float((r["Q"] ** 2).mean()))
     n_needed = float(var_ray.mean()) / (TARGET_ERR * qrms) ** 2
-    ms_field = n_needed * n ** 3 / rays_s * 1e3
+    return n_needed * ncell_field / rays_s * 1e3, rays_s, n_needed
+
+
+def cpu_reference(table, T, x, T_wall, rays_per_cell, sample_cells=96, budget_s=20.0):
+    """Reference estimator (oracle port, FP32 as the reference build) on all
+    host cores over a sample of cells; returns rays/s and ms per field at 1 %."""
+    from oracle import oracle as O
+    n = N_CELL
+    xbar = float(x.mean())
+    # x-uniform slice of the table in the reference layout (the reference has
+    # no x_H2O axis): k(band, T, g) at xbar, CDFs and Planck mean from it
+    tables = O.ref_tables_x_slice(table, xbar)
+    Tf = np.zeros((n + 2, n + 2, n + 2), np.float32)
+    Tf[1:-1, 1:-1, 1:-1] = T
+    rng = np.random.default_rng(0)
+    cells = np.stack([rng.integers(1, n + 1, sample_cells) for _ in range(3)], 1)
+    cores = os.cpu_count() or 1
+    kw = dict(imax=n, jmax=n, kmax=n, Lx=2.0, Ly=2 * math.pi, Lz=math.pi, T_west=T_wall, T_east=T_wall, model=0,
+              tables=tables, nvar=2, grid_num=1, stretched=0, use_double=0, seed=5, threads=cores)
+    r, dt, photmax = _ref_sample(Tf, n, cells, kw, budget_s)
+    ms_field, rays_s, n_needed = _ref_field_ms(r, dt, photmax, 2, n ** 3, sample_cells)
     return dict(rays_s=rays_s, steps_s=float(r["steps"].sum()) / dt, ms_field=ms_field, rays_per_cell_1pct=n_needed,
-                cores=cores, sample=f"{sample_cells} random cells x {nr} rays of the 128^3 field (x-uniform table "
-                                     f"slice at mean x_H2O), {dt:.1f} s, FP32 oracle port")
+                cores=cores, sample=f"{sample_cells} random cells x {2 * photmax} rays of the 128^3 field (x-uniform "
+                                     f"table slice at mean x_H2O), {dt:.1f} s, FP32 oracle port")
+
+
+# ---- the grey 64^3 channel (the reference's grey path) -------------------------
+C0_N = 64
+
+
+def c0_inputs():
+    from dnsmc_gb300 import synth
+    return synth.grey_channel(C0_N, 0)
+
+
+def cpu_reference_c0(T, T_wall, sample_cells=96, budget_s=12.0):
+    """The reference estimator on the grey channel as the reference runs it:
+    its grey tables (code/grey_tables.cpp:19-109: 1000 equal bands to 15000
+    1/cm, kappa in every band, T grid from 0.9 x 500 K to 1.1 Tmax), band
+    drawn from the emission CDF at Tmax, FP32 like the reference build, all
+    host cores, a sample of cells; ms per field at 1 % RMS extrapolated."""
+    n = C0_N
+    Tf = np.zeros((n + 2, n + 2, n + 2), np.float32)
+    Tf[1:-1, 1:-1, 1:-1] = T
+    rng = np.random.default_rng(0)
+    cells = np.stack([rng.integers(1, n + 1, sample_cells) for _ in range(3)], 1)
+    cores = os.cpu_count() or 1
+    kw = dict(imax=n, jmax=n, kmax=n, Lx=2.0, Ly=2 * math.pi, Lz=math.pi, T_west=T_wall, T_east=T_wall, model=1,
+              kappa=1.0, nvar=2, grid_num=1, stretched=0, use_double=0, seed=5, threads=cores)
+    r, dt, photmax = _ref_sample(Tf, n, cells, kw, budget_s)
+    ms_field, rays_s, n_needed = _ref_field_ms(r, dt, photmax, 2, n ** 3, sample_cells)
+    return dict(value=ms_field, unit="ms", cores=cores, kind="port", rays_per_s=rays_s,
+                rays_per_cell_1pct=n_needed,
+                sample=f"{sample_cells} random cells x {2 * photmax} rays of the grey 64^3 channel, {dt:.1f} s, "
+                       "FP32 oracle port of the reference estimator with its grey-band tables")
+
+
+def c0_solver(seed, bands=False):
+    import dnsmc_gb300 as D
+    cfg = D.default_config(model=D.MODEL_GREY_BANDS if bands else D.MODEL_GREY, imax=C0_N, jmax=C0_N, kmax=C0_N,
+                           Lx=2.0, Ly=2 * math.pi, Lz=math.pi, stretched_x=0, T_west=300.0, T_east=300.0, kappa=1.0,
+                           seed=seed, sampler=D.SAMPLER_RQMC, nvar=REPLICATES)
+    s = D.Solver(cfg)
+    if bands:
+        s.use_grey_band_tables(1000, 55, 15000.0, 500.0)
+    s.set_result_type(D.RESULT_F32)
+    return s
+
+
+def c0_timed(s, rays, steps, warmup, flushbuf):
+    """Device time (CUDA events on the solver's stream) of `steps` solves."""
+    import torch
+    s.set_rays(rays)
+    for _ in range(max(3, warmup)):
+        s.solve(timeout_s=300)
+    stream = torch.cuda.ExternalStream(s.stream())
+    ms, errs, rays_tot, steps_tot = [], [], 0.0, 0.0
+    for _ in range(steps):
+        flush_l2(flushbuf)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.solve_async()
+        e1.record(stream)
+        s.wait(300)
+        e1.synchronize()
+        Q, S = s.results_float()
+        ms.append(e0.elapsed_time(e1))
+        errs.append(rms_error(Q.astype(np.float64), S.astype(np.float64)))
+        c = s.counters()
+        rays_tot += c.rays
+        steps_tot += c.steps
+    t = float(np.sum(ms)) / 1e3
+    return dict(ms=float(np.mean(ms)), rms_error=float(np.mean(errs)), rays_per_s=rays_tot / t,
+                ray_steps_per_s=steps_tot / t, Q=Q, S=S)
+
+
+def c0_budget(s, pilot=256):
+    """Rays per cell for 1 % RMS: pilot at the config's 256 rays per cell,
+    1/N scaling, refined once."""
+    s.set_rays(pilot)
+    Q, S = s.solve(timeout_s=300)
+    e = rms_error(Q.astype(np.float64), S.astype(np.float64))
+    r = max(2 * REPLICATES, -(-int(math.ceil(pilot * (e / TARGET_ERR) ** 2)) // REPLICATES) * REPLICATES)
+    s.set_rays(r)
+    Q, S = s.solve(timeout_s=300)
+    e1 = rms_error(Q.astype(np.float64), S.astype(np.float64))
+    if e1 > 0.98 * TARGET_ERR:
+        r = -(-int(math.ceil(r * (e1 / (0.98 * TARGET_ERR)) ** 2)) // REPLICATES) * REPLICATES
+    return r, e
+
+
+def run_c0(steps, warmup, flushbuf, with_cpu=True):
+    """The grey 64^3 channel: T = 300 + 700 (1 - y^2) K + 5 % Fourier
+    fluctuation, kappa = 1 per half-height, black walls at 300 K, plain MC
+    (RQMC rays, no control variate) at its 1 % RMS budget and at the
+    config's 256 rays per cell; the same channel with the reference's grey
+    band tables (its representation of a grey gas) beside the CPU reference
+    estimator on those tables; and the isothermal slab (T = 1000 K, kappa =
+    1, tau_L = 2, walls 0 K and 300 K) against its analytic E2 solution."""
+    from oracle import oracle as O
+    g = c0_inputs()
+    out = {"workload": "grey channel 64^3 (x,z periodic 2pi x pi, y walls black 300 K), T 300 + 700 (1 - y^2) K "
+                       "+ 5% Fourier, kappa = 1 per half-height, plain MC (RQMC rays, 2 replicates), FP32 march, "
+                       "FP64 tallies", "n": C0_N}
+    s = c0_solver(101)
+    s.set_fields(g["T"])
+    r, e_pilot = c0_budget(s)
+    t = c0_timed(s, r, steps, warmup, flushbuf)
+    t256 = c0_timed(s, 256, max(1, steps // 4), 1, flushbuf)
+    s.close()
+    out["gpu_grey"] = {"rays_per_cell": r, "ms_at_1pct": t["ms"], "rms_error": t["rms_error"],
+                       "rms_error_pilot_256": e_pilot, "rays_per_s": t["rays_per_s"],
+                       "ray_steps_per_s": t["ray_steps_per_s"],
+                       "at_256_rays": {"ms": t256["ms"], "rms_error": t256["rms_error"]}}
+    # the reference's representation: 1000 grey bands, band drawn at Tmax
+    sb = c0_solver(102, bands=True)
+    sb.set_fields(g["T"])
+    rb, _ = c0_budget(sb)
+    tb = c0_timed(sb, rb, max(1, steps // 2), warmup, flushbuf)
+    sb.close()
+    out["gpu_grey_bands"] = {"rays_per_cell": rb, "ms_at_1pct": tb["ms"], "rms_error": tb["rms_error"],
+                             "rays_per_s": tb["rays_per_s"],
+                             "tables": "the reference's grey tables (code/grey_tables.cpp:19-109), as the CPU arm"}
+    # isothermal slab against E2
+    import dnsmc_gb300 as D
+    sl = D.Solver(D.default_config(model=D.MODEL_GREY, imax=C0_N, jmax=C0_N, kmax=C0_N, Lx=2.0, Ly=2 * math.pi,
+                                   Lz=math.pi, stretched_x=0, T_west=0.0, T_east=300.0, kappa=1.0, seed=103,
+                                   sampler=D.SAMPLER_RQMC, nvar=REPLICATES))
+    sl.set_fields(np.full((C0_N, C0_N, C0_N), 1000.0, np.float32))
+    sl.set_rays(256)
+    Qs, Ss = sl.solve(timeout_s=300)
+    sl.close()
+    yc = (np.arange(C0_N) + 0.5) * 2.0 / C0_N
+    exact = O.slab_divq(yc, 2.0, 1.0, 1000.0, 0.0, 300.0)[None, None, None, :]
+    erms = math.sqrt(float((exact ** 2).mean()))
+    out["slab_e2"] = {"case": "isothermal slab T 1000 K, kappa 1, tau_L 2, walls 0 K and 300 K, 64^3, 256 rays",
+                      "rms_error_vs_analytic": math.sqrt(float(((Qs - exact) ** 2).mean())) / erms,
+                      "rms_error_estimated": math.sqrt(float((Ss ** 2).mean())) / erms,
+                      "oracle": "analytic E2 solution of the isothermal grey slab"}
+    if with_cpu:
+        try:
+            cpu = cpu_reference_c0(g["T"], g["T_wall"])
+            out["cpu_baseline"] = cpu
+            out["same_config"] = True
+            out["speedup_vs_cpu_same_tables"] = cpu["value"] / tb["ms"]
+        except Exception as ex:  # the baseline must not take the GPU number down
+            out["cpu_baseline"] = {"value": None, "sample": f"failed: {ex}"}
+    return out
 
 
 def run_reference(args):
     world, rank, local, pg = dist_setup(args)
     if rank != 0:
+        return 0
+    if args.workload == "grey64":
+        g = c0_inputs()
+        vals = [cpu_reference_c0(g["T"], g["T_wall"], budget_s=max(4.0, 40.0 / (args.warmup + args.steps)))
+                for _ in range(args.warmup + args.steps)][args.warmup:]
+        v = float(np.mean([c["value"] for c in vals]))
+        out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "ms", "n_gpus": args.gpus,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": v, "higher_is_better": False,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+               "config": {"workload": "grey channel 64^3, the reference's grey-band tables, extrapolated from a "
+                                      "sample", "parallelism": "host threads"},
+               "cpu_baseline": dict(vals[-1], value=v), "rays_per_s": vals[-1]["rays_per_s"],
+               "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(out), flush=True)
         return 0
     from dnsmc_gb300 import synth
     T, x, Tw = make_inputs(0)
@@ -272,6 +451,13 @@ def run_reference(args):
            "cpu_baseline": {"value": v, "unit": "ms", "cores": info["cores"], "kind": "port", "sample": info["sample"]},
            "rays_per_s": info["rays_s"],
            "e2e": {"value": v, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if args.workload == "ck128":
+        # the grey 64^3 channel on the reference's own grey tables: the
+        # configuration the reference covers completely
+        g = c0_inputs()
+        c0 = cpu_reference_c0(g["T"], g["T_wall"])
+        out["c0"] = {"workload": "grey channel 64^3, the reference's grey-band tables", "ms_at_1pct": c0["value"],
+                     "cpu_baseline": c0}
     print(json.dumps(out), flush=True)
     return 0
 
@@ -301,6 +487,9 @@ class Arm:
     def __init__(self, method, table, T, x, Tw, seed, threads, net=None):
         self.method, self.net = method, net
         self.s = make_solver(table, Tw, seed=seed, threads=threads, cv=0 if method == "plain" else 1)
+        # Q and sigma rounded to float on the device: 8 bytes per cell reach
+        # the host, like the reference's real(4) result arrays
+        self.s.set_result_type(_result_f32())
         self.s.set_fields(T, x)
         self.rays = 0
 
@@ -317,7 +506,11 @@ class Arm:
             self.rays = rays
         self.enqueue()
         self.s.wait(600)
-        return self.s.results()
+        return self.results()
+
+    def results(self, out=None):
+        Q, S = self.s.results_float(out)
+        return Q, S
 
     def budget(self, pilot=64, rays=0):
         """Rays per cell per group (uniform, or the mean of the network's
@@ -341,18 +534,20 @@ class Arm:
         stream = torch.cuda.ExternalStream(self.s.stream())
         for _ in range(max(3, warmup)):
             self.solve()
-        out = dict(ms=[], march_ms=[], steps=0.0, warp_steps=0.0, rays=0.0, errs=[])
+        out = dict(ms=[], march_ms=[], steps=0.0, warp_steps=0.0, rays=0.0, errs=[], launches=0)
         torch.cuda.synchronize()
         for _ in range(steps):
             flush_l2(flushbuf)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            n0 = _launches()
             e0.record(stream)
             self.enqueue()
             e1.record(stream)
             self.s.wait(600)
             e1.synchronize()
-            Q, S = self.s.results()
+            out["launches"] += _launches() - n0  # this library's kernels in the timed region
+            Q, S = self.results()
             out["ms"].append(e0.elapsed_time(e1))
             out["march_ms"].append(self.s.timing()[1])
             c = self.s.counters()
@@ -370,12 +565,12 @@ class Arm:
         results land in persistent arrays, as in a DNS that keeps its Q_r
         field from step to step."""
         ms = []
-        Q, S = self.s.results()  # the persistent result arrays (touched once)
+        Q, S = self.results()  # the persistent result arrays (touched once)
         for _ in range(steps):
             t0 = time.perf_counter()
             self.s.set_fields(T, x)
             self.enqueue()
-            self.s.results(out=(Q, S))
+            self.results(out=(Q, S))
             ms.append((time.perf_counter() - t0) * 1e3)
         return ms, Q, S
 
@@ -422,17 +617,20 @@ def run_batched(args, flushbuf_mb=256):
     for _ in range(max(3, args.warmup)):
         s.solve(timeout_s=900)
     ms, errs, steps, rays_tot, march = [], [], 0.0, 0.0, []
+    launches = 0
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             flush_l2(flushbuf)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
+            n0 = _launches()
             e0.record(stream)
             s.solve_async()
             e1.record(stream)
             s.wait(900)
             e1.synchronize()
+            launches += _launches() - n0
             Q, S = s.results()
             ms.append(e0.elapsed_time(e1))
             march.append(s.timing()[1])
@@ -442,9 +640,13 @@ def run_batched(args, flushbuf_mb=256):
             errs.append(rms_error(Q, S))
     t = float(np.sum(ms))
     ms_field = t / (args.steps * nsnap)
-    peak, peak_kind = peaks()
-    achieved = BYTES_PER_STEP * (steps / args.steps) / (float(np.mean(march)) / 1e3) / 1e9
-    cap, launches = s.graph_info()
+    clocks = clk.summary()
+    # the replayed graph's time brackets the whole sequence, so this
+    # per-step issue rate is a lower bound for the march itself
+    roof = issue_roofline(steps / args.steps, float(np.mean(march)), clocks)
+    roof["note"] = ("instructions per lane-step of the 128^3 network-control-variate capture (the same march "
+                    "kernel); time = the replayed graph")
+    cap, glaunches = s.graph_info()
     out = {
         "metric": METRIC, "value": ms_field, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t / args.steps, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
@@ -455,18 +657,15 @@ def run_batched(args, flushbuf_mb=256):
                    "snapshots": nsnap, "n": n, "rays_per_tau": per_tau, "rays_mean": float(rp.mean()),
                    "rays_min": int(rp.min()), "rays_max": int(rp.max()), "autotuned": cfg,
                    "autotune_cached": tune["cached"], "target_rms_error": TARGET_ERR,
-                   "rms_error_timed": float(np.mean(errs)), "graph_captures": cap, "graph_launches": launches,
+                   "rms_error_timed": float(np.mean(errs)), "graph_captures": cap, "graph_launches": glaunches,
                    "l2": "flushed before every timed step (256 MB device write)", "parallelism": "cells x1"},
         "autotune": tune["results"],
         "rays_per_s": rays_tot / (t / 1e3), "ray_steps_per_s": steps / (t / 1e3), "march_ms": float(np.mean(march)),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind},
+        "roofline": roof,
         "cpu_baseline": None,
         "e2e": None,
-        # per replay: coordinates, 3 + 2 control-variate kernels, 3 queue-order
-        # kernels (adaptive per-packet rays), march, reciprocals, finalize
-        "gpu_launches": 12 * args.steps,
-        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "clocks": clocks,
     }
     print(json.dumps(out), flush=True)
     s.close()
@@ -517,17 +716,20 @@ def run_c4(args):
     stream = torch.cuda.ExternalStream(s.stream())
     flushbuf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
     ms, march, errs, steps, rays_tot = [], [], [], 0.0, 0.0
+    launches = 0
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         for _ in range(args.steps):
             flush_l2(flushbuf)
             e0 = torch.cuda.Event(enable_timing=True)
             e1_ = torch.cuda.Event(enable_timing=True)
+            n0 = _launches()
             e0.record(stream)
             s.solve_async()
             e1_.record(stream)
             s.wait(1800)
             e1_.synchronize()
+            launches += _launches() - n0
             Q, S = s.results()
             ms.append(e0.elapsed_time(e1_))
             march.append(s.timing()[1])
@@ -543,8 +745,13 @@ def run_c4(args):
     pilot_ms = p.timing()[0]
     p.close()
     value = float(np.mean(ms))
-    peak, peak_kind = peaks()
-    achieved = 36 * (steps / args.steps) / (float(np.mean(march)) / 1e3) / 1e9
+    clocks = clk.summary()
+    roof = issue_roofline(steps / args.steps, float(np.mean(march)), clocks, bytes_per_step=36)
+    # the general-medium march has its own instruction mix: no per-step
+    # counters of it here, only its gather rate (36 B per step)
+    for k_ in ("achieved", "frac", "traffic", "hbm_gbs", "hbm_frac", "l2_bytes", "l2_gbs", "source"):
+        roof[k_] = None
+    roof["note"] = "36 B per ray-voxel step (T, x_H2O, fv, bilinear k, linear Ib); issue-bound like the gas march"
     out = {
         "metric": METRIC, "value": value, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -559,26 +766,124 @@ def run_c4(args):
                                     "pilot_solve_ms": pilot_ms, "ms_at_1pct_extrapolated": pilot_ms * rp / 32}},
         "rays_per_s": rays_tot / (np.sum(ms) / 1e3), "ray_steps_per_s": steps / (np.sum(ms) / 1e3),
         "march_ms": float(np.mean(march)),
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind,
-                     "note": "36 B per ray-voxel step (T, x_H2O, fv, bilinear k, linear Ib)"},
-        "cpu_baseline": None, "e2e": None, "gpu_launches": 7 * args.steps, "clocks": clk.summary(),
+        "roofline": roof,
+        "cpu_baseline": None, "e2e": None, "gpu_launches": launches, "clocks": clocks,
     }
     print(json.dumps(out), flush=True)
     return 0
 
 
-# DRAM bytes (read + write) of one march launch measured by an ncu capture of
-# the default command (128^3, network control variate): the tallies and L2
-# refills, not the gathers, which L1/L2 serve
-MARCH_DRAM_BYTES = {("net", 128): 189.37e6 + 252.66e6}
+# Per lane-step figures of the two-cell march at the bench configuration
+# (128^3 correlated-k channel, network control variate, 1 % budget), from
+# the committed ncu capture: warp instructions issued, L2 bytes, DRAM bytes.
+MARCH_PROFILE = os.path.join(ROOT, "profiles", "march_pair_kernel_ck128_counters.md")
+ISSUE_PEAK = 4.0  # warp instructions per SM cycle: four schedulers, one issue each
 
-# kernels per step: table coordinates, march, finalize; the control variate adds
-# layer means, surrogate table, 1-D quadrature and the two E[Y] kernels (node
-# sums, cells); per-packet ray counts (the network's) add the three kernels of
-# the longest-first queue order and the finalize's reciprocals of the counts;
-# the network adds features, MLP, coefficients and three allocation kernels
-LAUNCHES = {"plain": 3, "cv": 8, "net": 18}
+
+def march_counters():
+    """The `bench-constants:` line of the march profile, as floats, or None."""
+    try:
+        with open(MARCH_PROFILE) as fh:
+            for line in fh:
+                if line.startswith("bench-constants:"):
+                    return {k: float(v) for k, v in (kv.split("=") for kv in line.split(":", 1)[1].split())}
+    except (OSError, ValueError):
+        pass
+    return None
+
+
+def issue_roofline(lane_steps, march_ms, clocks, bytes_per_step=BYTES_PER_STEP):
+    """The march's bound: instruction issue.  achieved = warp instructions
+    per SM cycle = (instructions per lane-step from the ncu capture x the
+    lane-steps this launch counted) / (march time x median SM clock sampled
+    during the timed region x SMs); peak = 4.  Beside it the algorithmic
+    gather rate and the DRAM traffic (ncu per lane-step x lane-steps) against
+    the measured HBM copy bandwidth."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    hbm, hbm_kind = peaks()
+    c = march_counters()
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    sec = march_ms / 1e3
+    out = {"bound": "issue", "achieved": None, "peak": ISSUE_PEAK, "unit": "warp instructions per SM cycle",
+           "frac": None, "traffic": None, "peak_kind": "architectural (4 schedulers x 1 issue per cycle)",
+           "gather_bytes": bytes_per_step * lane_steps, "gather_gbs": bytes_per_step * lane_steps / sec / 1e9,
+           "lane_steps": lane_steps, "sms": sms, "sm_mhz": mhz}
+    if c and mhz:
+        inst = c["warp_inst_per_lane_step"] * lane_steps
+        out["achieved"] = inst / (sec * mhz * 1e6 * sms)
+        out["frac"] = out["achieved"] / ISSUE_PEAK
+        out["traffic"] = c["dram_bytes_per_lane_step"] * lane_steps
+        out["hbm_gbs"] = out["traffic"] / sec / 1e9
+        out["hbm_frac"] = out["hbm_gbs"] / hbm
+        out["hbm_peak_gbs"], out["hbm_peak_kind"] = hbm, hbm_kind
+        out["l2_bytes"] = c["l2_bytes_per_lane_step"] * lane_steps
+        out["l2_gbs"] = out["l2_bytes"] / sec / 1e9
+        out["source"] = os.path.relpath(MARCH_PROFILE, ROOT)
+    return out
+
+
+def fp64_validation(table, T, x, Tw, Q, S, rays_timed, threads=0):
+    """The timed field's error against the oracle's FP64 solution: the
+    packet scheme in float64 with its own layer-mean control variate and
+    exact means (oracle.fp64_cv_solution), 64 x the timed mean rays per cell
+    and group in 8 RQMC replicates, independent seed, on every 4th
+    wall-normal layer of the 8 x 8 column j, k < 8 (32 packets, 2048 cells).
+    The error is sqrt(mean (Q - Q*)^2 - mean var(Q*)) / rms(Q*), the
+    oracle's own variance removed in quadrature."""
+    import dnsmc_gb300 as D
+    from oracle import oracle as O
+    n = N_CELL
+    rays = 64 * int(rays_timed)
+    rays = -(-rays // 8) * 8
+    cfg = D.default_config(model=D.MODEL_TABLE, imax=n, jmax=n, kmax=n, Lx=2.0, Ly=2 * math.pi, Lz=math.pi,
+                           stretched_x=0, T_west=Tw, T_east=Tw, n_groups=GROUPS, seed=9001,
+                           sampler=D.SAMPLER_RQMC, local_sampling=1, nvar=8, control_variate=0)
+    m = D.Solver(cfg)  # host-only mirror: geometry, packets and sampling tables, no GPU work
+    m.set_table(table["k"], table["wvc"], table["T0"], table["dT"], dnu=table["dnu"], wq=table["wq"],
+                X0=table["X0"], dX=table["dX"])
+    m.set_region(0, n, 0, 8, 0, 8)
+    m.prepare_sampling(float(max(T.max(), Tw)), float(x.mean()))
+    m.set_rays(8)
+    t0 = time.perf_counter()
+    Qo, Vo = O.fp64_cv_solution(m, table["dnu"], table["wq"], T[None], x[None], rays=rays, nbatch=8, seed=9001,
+                                threads=threads or (os.cpu_count() or 1), layer_step=4)
+    dt = time.perf_counter() - t0
+    m.close()
+    Qo, Vo = Qo[0][..., ::4], Vo[0][..., ::4]
+    Qg = np.asarray(Q[0], np.float64)[:8, :8, ::4]
+    Sg = np.asarray(S[0], np.float64)[:8, :8, ::4]
+    qrms = math.sqrt(float((Qo ** 2).mean()))
+    d2 = float(((Qg - Qo) ** 2).mean())
+    return {"reference": "FP64 oracle: float64 packet scheme with its own layer-mean control variate and exact "
+                         f"means, {rays} RQMC rays per cell and group (64 x the timed mean), 8 replicates, "
+                         "independent seed",
+            "cells": int(Qo.size), "sample": "every 4th wall-normal layer of the 8 x 8 column j, k < 8",
+            "reference_rms_error": math.sqrt(float(Vo.mean())) / qrms,
+            "rms_error_vs_fp64": math.sqrt(max(0.0, d2 - float(Vo.mean()))) / qrms,
+            "rms_error_vs_fp64_raw": math.sqrt(d2) / qrms,
+            "rms_error_estimated": math.sqrt(float((Sg ** 2).mean())) / qrms,
+            "cpu_seconds": dt}
+
+
+def run_grey64(args):
+    """The grey 64^3 channel as the headline workload: ms per field at 1 %
+    RMS of plain MC, with the CPU reference on the same channel and tables."""
+    import torch
+    flushbuf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    n0 = _launches()
+    with ClockSampler(0) as clk:
+        c0 = run_c0(args.steps, args.warmup, flushbuf, with_cpu=not args.no_cpu)
+    g = c0["gpu_grey"]
+    out = {"metric": METRIC, "value": g["ms_at_1pct"], "unit": "ms", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": g["ms_at_1pct"], "higher_is_better": False, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": c0["workload"], "rays_per_cell": g["rays_per_cell"], "target_rms_error": TARGET_ERR,
+                      "l2": "flushed before every timed step (256 MB device write)", "parallelism": "cells x1"},
+           "rays_per_s": g["rays_per_s"], "c0": c0, "cpu_baseline": c0.get("cpu_baseline"), "e2e": None,
+           "gpu_launches": _launches() - n0, "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+    return 0
 
 
 def main():
@@ -597,9 +902,11 @@ def main():
                     help="timed estimator: network control variate (default), profile control variate, plain MC")
     ap.add_argument("--no-compare", action="store_true",
                     help="skip the profile-CV and extrapolated plain-MC comparison arms")
-    ap.add_argument("--workload", default="ck128", choices=["ck128", "batched", "particles"],
-                    help="ck128: the 128^3 correlated-k channel (default); batched: 16 snapshots of 96^3; "
-                         "particles: gas + scattering particles with grey walls, 192^3")
+    ap.add_argument("--workload", default="ck128", choices=["ck128", "grey64", "batched", "particles"],
+                    help="ck128: the 128^3 correlated-k channel (default); grey64: the grey 64^3 channel and "
+                         "the isothermal slab; batched: 16 snapshots of 96^3; particles: gas + scattering "
+                         "particles with grey walls, 192^3")
+    ap.add_argument("--no-c0", action="store_true", help="skip the grey 64^3 block of the default workload")
     ap.add_argument("--groups", type=int, default=GROUPS, help="band groups (stratification) of the solves")
     ap.add_argument("--no-validate", action="store_true",
                     help="skip the check of the timed field against an independent high-ray solution")
@@ -610,9 +917,11 @@ def main():
     REPLICATES = args.replicates
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload in ("batched", "particles"):
+    if args.workload in ("batched", "particles", "grey64"):
         import torch
         torch.cuda.set_device(0)
+        if args.workload == "grey64":
+            return run_grey64(args)
         return run_batched(args) if args.workload == "batched" else run_c4(args)
 
     world, rank, local, pg = dist_setup(args)
@@ -642,8 +951,8 @@ def main():
     rays_s = r["rays"] * world / (t_max / 1e3)
     march_avg = float(np.mean(r["march_ms"]))
     steps_per_launch = r["steps"] / args.steps
-    achieved = BYTES_PER_STEP * steps_per_launch / (march_avg / 1e3) / 1e9
-    peak, peak_kind = peaks()
+    clocks = clk.summary()
+    roof = issue_roofline(steps_per_launch, march_avg, clocks)
     # ---- end to end through the public API from host arrays ------------------
     e2e_ms, Qh, Sh = ([], r["Q"], r["S"]) if args.no_e2e else arm.e2e(T, x, args.steps)
     e2e_rank = float(np.sum(e2e_ms)) if e2e_ms else 0.0
@@ -660,18 +969,25 @@ def main():
         if pg is not None:
             pg.destroy_process_group()
         return 0
-    # ---- the timed field's actual error against an independent solution ------
+    # ---- the timed field's actual error against independent solutions --------
     validation = None
     if not args.no_validate:
+        validation = fp64_validation(table, T, x, Tw, r["Q"], r["S"], arm.rays)
+        # and against a GPU solution of the whole field at many more rays
         v = Arm("cv", table, T, x, Tw, 5000 + rank, args.threads)
         Qref, Sref = v.solve(-(-1024 // REPLICATES) * REPLICATES)
         v.close()
-        qrms = math.sqrt(float((Qref ** 2).mean()))
-        d2 = float(((r["Q"] - Qref) ** 2).mean()) - float((Sref ** 2).mean())
-        validation = {"reference": "profile control variate, 1024 rays per cell and group, independent seed",
-                      "reference_rms_error": rms_error(Qref, Sref),
-                      "rms_error_vs_reference": math.sqrt(max(0.0, d2)) / qrms,
-                      "rms_error_estimated": rms_error(r["Q"], r["S"])}
+        qrms = math.sqrt(float((np.asarray(Qref, np.float64) ** 2).mean()))
+        d2 = float(((np.asarray(r["Q"], np.float64) - Qref) ** 2).mean()) - float(
+            (np.asarray(Sref, np.float64) ** 2).mean())
+        validation["whole_field_gpu"] = {
+            "reference": "profile control variate on the GPU, 1024 rays per cell and group, independent seed",
+            "reference_rms_error": rms_error(Qref, Sref),
+            "rms_error_vs_reference": math.sqrt(max(0.0, d2)) / qrms,
+            "rms_error_estimated": rms_error(r["Q"], r["S"])}
+    c0 = None
+    if not args.no_c0 and world == 1:
+        c0 = run_c0(max(3, args.steps // 2), args.warmup, flushbuf, with_cpu=not args.no_cpu)
     compare = {}
     if not args.no_compare and not args.rays:
         if args.method != "cv":
@@ -714,20 +1030,16 @@ def main():
         "comparison": compare,
         "validation": validation,
         "rays_per_s": rays_s, "ray_steps_per_s": r["steps"] * world / (t_max / 1e3),
-        "march_ms": march_avg, "step_ms": float(np.mean(r["ms"])),
+        "march_ms": march_avg, "step_ms": float(np.mean(r["ms"])), "march_lane_steps": steps_per_launch,
         "lane_efficiency": r["steps"] / (r["packet_cells"] * r["warp_steps"]) if r["warp_steps"] else None,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": MARCH_DRAM_BYTES.get((args.method, N_CELL)), "peak_kind": peak_kind,
-                     "note": f"algorithmic gather bytes {BYTES_PER_STEP} B per ray-voxel step x lane-steps per "
-                             f"launch / march kernel time (CUDA events); the gathers are served on chip (field "
-                             f"and tables in L2, each ray's table slab in shared memory), so frac above 1 is "
-                             f"on-chip reuse; the march is bound by instruction issue; traffic = ncu DRAM "
-                             f"read+write bytes per march launch"},
+        "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_max, "unit": "ms", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "timing": "wall clock around set_fields + (network) + solve + get_results"},
-        "gpu_launches": LAUNCHES[args.method] * args.steps,
-        "clocks": clk.summary(),
+                "timing": "wall clock around set_fields + (network) + solve + get_results_float (Q and sigma "
+                          "rounded to float on the device)"},
+        "gpu_launches": int(r["launches"]),
+        "clocks": clocks,
+        "c0": c0,
     }
     print(json.dumps(out), flush=True)
     if net is not None:

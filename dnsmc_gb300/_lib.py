@@ -124,6 +124,7 @@ SIGNATURES = {
     "dnsmc_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
     "dnsmc_get_results": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
     "dnsmc_save_table": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "dnsmc_get_launch_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_longlong)]),
     "dnsmc_load_table": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "dnsmc_set_result_type": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dnsmc_get_results_float": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p]),
@@ -174,6 +175,13 @@ class DnsmcError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"dnsmc error {code}: {msg}")
         self.code = code
+
+
+def launch_count() -> int:
+    """Kernels the library has launched in this process (dnsmc_get_launch_count)."""
+    n = ctypes.c_longlong()
+    check(load().dnsmc_get_launch_count(ctypes.byref(n)))
+    return n.value
 
 
 def check(rc: int) -> None:

@@ -148,48 +148,58 @@ struct FeatParams {
     bf16 *out;                // [f * region_cells + tc][K0]
 };
 
+// The K0 bf16 features of row r (field f, cell tc of the region in tally
+// order), packed pairwise: the features kernel and the tensor-memory
+// forward both use this, so their features are the same bits.
+__device__ __forceinline__ void feature_row(const FeatParams &P, long long r, uint32_t (&out)[K0 / 2]) {
+    const int f = (int)(r / P.region_cells);
+    const long long tc = r - (long long)f * P.region_cells;
+    const int jR = (int)(tc % P.njR);
+    const long long t = tc / P.njR;
+    const int kR = (int)(t % P.nkR);
+    const int iR = (int)(t / P.nkR);
+    const int i = P.ew0 + iR, j = P.ea0 + jR, k = P.eb0 + kR;
+    const long long base = (long long)f * P.field_stride + (long long)k * P.na + j;
+    const long long plane = (long long)P.na * P.nb;
+    float feat[K0];
+#pragma unroll
+    for (int q = 0; q < K0; ++q) feat[q] = 0.0f;
+    float T, X = 0.0f;
+    if (P.mode == MODE_TX) {
+        const float2 v = P.fTX[base + i * plane];
+        T = v.x; X = v.y;
+    } else {
+        T = P.fT[base + i * plane];
+    }
+    feat[0] = __fmul_rn(__fsub_rn(T, P.Tc), P.Tis);
+    feat[1] = P.mode == MODE_TX ? __fmul_rn(__fsub_rn(X, P.Xc), P.Xis) : 0.0f;
+    const float o = __fmul_rn(0.5f, __fadd_rn(P.fw[i], P.fw[i + 1]));
+    const float eta = __fdiv_rn(__fsub_rn(o, P.fw[0]), __fsub_rn(P.fw[P.nw], P.fw[0]));
+    feat[2] = __fsub_rn(__fmul_rn(2.0f, eta), 1.0f);
+#pragma unroll
+    for (int q = 0; q < NPROF; ++q) {
+        const int l = ((2 * q + 1) * P.nw) / (2 * NPROF);
+        if (P.mode == MODE_TX) {
+            const float2 v = P.fTX[base + l * plane];
+            feat[3 + q] = __fmul_rn(__fsub_rn(v.x, P.Tc), P.Tis);
+            feat[3 + NPROF + q] = __fmul_rn(__fsub_rn(v.y, P.Xc), P.Xis);
+        } else {
+            feat[3 + q] = __fmul_rn(__fsub_rn(P.fT[base + l * plane], P.Tc), P.Tis);
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < K0 / 2; ++q) out[q] = pack_bf16(feat[2 * q], feat[2 * q + 1]);
+}
+
 __global__ void features_kernel(const FeatParams P) {
     const long long n = (long long)P.nfields * P.region_cells;
     for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n;
          r += (long long)gridDim.x * blockDim.x) {
-        const int f = (int)(r / P.region_cells);
-        const long long tc = r - (long long)f * P.region_cells;
-        const int jR = (int)(tc % P.njR);
-        const long long t = tc / P.njR;
-        const int kR = (int)(t % P.nkR);
-        const int iR = (int)(t / P.nkR);
-        const int i = P.ew0 + iR, j = P.ea0 + jR, k = P.eb0 + kR;
-        const long long base = (long long)f * P.field_stride + (long long)k * P.na + j;
-        const long long plane = (long long)P.na * P.nb;
-        float feat[K0];
-#pragma unroll
-        for (int q = 0; q < K0; ++q) feat[q] = 0.0f;
-        float T, X = 0.0f;
-        if (P.mode == MODE_TX) {
-            const float2 v = P.fTX[base + i * plane];
-            T = v.x; X = v.y;
-        } else {
-            T = P.fT[base + i * plane];
-        }
-        feat[0] = __fmul_rn(__fsub_rn(T, P.Tc), P.Tis);
-        feat[1] = P.mode == MODE_TX ? __fmul_rn(__fsub_rn(X, P.Xc), P.Xis) : 0.0f;
-        const float o = __fmul_rn(0.5f, __fadd_rn(P.fw[i], P.fw[i + 1]));
-        const float eta = __fdiv_rn(__fsub_rn(o, P.fw[0]), __fsub_rn(P.fw[P.nw], P.fw[0]));
-        feat[2] = __fsub_rn(__fmul_rn(2.0f, eta), 1.0f);
-#pragma unroll
-        for (int q = 0; q < NPROF; ++q) {
-            const int l = ((2 * q + 1) * P.nw) / (2 * NPROF);
-            if (P.mode == MODE_TX) {
-                const float2 v = P.fTX[base + l * plane];
-                feat[3 + q] = __fmul_rn(__fsub_rn(v.x, P.Tc), P.Tis);
-                feat[3 + NPROF + q] = __fmul_rn(__fsub_rn(v.y, P.Xc), P.Xis);
-            } else {
-                feat[3 + q] = __fmul_rn(__fsub_rn(P.fT[base + l * plane], P.Tc), P.Tis);
-            }
-        }
+        uint32_t packed[K0 / 2];
+        feature_row(P, r, packed);
         uint32_t *dst = reinterpret_cast<uint32_t *>(P.out + r * K0);
 #pragma unroll
-        for (int q = 0; q < K0 / 2; ++q) dst[q] = pack_bf16(feat[2 * q], feat[2 * q + 1]);
+        for (int q = 0; q < K0 / 2; ++q) dst[q] = packed[q];
     }
 }
 
@@ -523,7 +533,20 @@ __global__ void adam_kernel(float *p, const float *grad, float *m, float *v, bf1
     }
 }
 
-// bf16 copy of the weight blocks of the master array
+// bf16 copies of the weight blocks of the master array: w[0, NWEIGHT) row
+// major per matrix ([out][in], the warp-level kernels), w[NWEIGHT, 2 NWEIGHT)
+// in the tensor-core order [in/8][out][8] of the tcgen05 forward (the same
+// block offsets)
+__host__ __device__ __forceinline__ long long tc_order(long long e) {
+    long long off, rows, cols;
+    if (e < WOFF_2) { off = WOFF_1; rows = HID; cols = K0; }
+    else if (e < WOFF_3) { off = WOFF_2; rows = HID; cols = HID; }
+    else if (e < WOFF_4) { off = WOFF_3; rows = HID; cols = HID; }
+    else { off = WOFF_4; rows = NOUT; cols = HID; }
+    const long long q = e - off, n = q / cols, k = q % cols;
+    return off + (k >> 3) * rows * 8 + n * 8 + (k & 7);
+}
+
 __global__ void weights_to_bf16_kernel(const float *p, bf16 *w) {
     const long long n = NWEIGHT;
     for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
@@ -532,7 +555,9 @@ __global__ void weights_to_bf16_kernel(const float *p, bf16 *w) {
         else if (e < WOFF_3) src = OFF_W2 + (e - WOFF_2);
         else if (e < WOFF_4) src = OFF_W3 + (e - WOFF_3);
         else src = OFF_W4 + (e - WOFF_4);
-        w[e] = __float2bfloat16(p[src]);
+        const bf16 v = __float2bfloat16(p[src]);
+        w[e] = v;
+        w[NWEIGHT + tc_order(e)] = v;
     }
 }
 
@@ -592,6 +617,9 @@ __global__ void labels_kernel(const LabelParams L) {
 // Inference: network outputs -> coefficient pairs (tally layout) and per-cell
 // (v, c); per (group, packet) allocation weights; ray counts.
 // ---------------------------------------------------------------------------
+// The coefficient epilogue of dnsmc_cvnet_apply (fused into the tcgen05
+// forward): per row and band group, beta = (1, -1) + the first two outputs
+// (non-finite: (1, -1)) and (v, c) = (S_v e^o2, S_c e^o3), o clamped to 15.
 struct ApplyParams {
     long long rows;           // nfields * region_cells
     int G;
@@ -602,22 +630,9 @@ struct ApplyParams {
     long long region_cells;
 };
 
-__global__ void apply_kernel(const ApplyParams A) {
-    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < A.rows;
-         r += (long long)gridDim.x * blockDim.x) {
-        const long long f = r / A.region_cells, tc = r - f * A.region_cells;
-        for (int g = 0; g < A.G; ++g) {
-            const float *o = A.out + r * NOUT + 4 * g;
-            const long long d = (f * A.G + g) * A.region_cells + tc;
-            if (A.beta) {
-                float ba = 1.0f + o[0], bb = -1.0f + o[1];
-                if (!isfinite(ba) || !isfinite(bb)) { ba = 1.0f; bb = -1.0f; }
-                A.beta[d] = make_float2(ba, bb);
-            }
-            A.vc[d] = make_float2(A.Sv * expf(clampo(o[2])), A.Sc * expf(clampo(o[3])));
-        }
-    }
-}
+}  // namespace
+#include "mc_cvnet_tc.cuh"
+namespace {
 
 struct AllocParams {
     int nfields, G, n_packets, npa, npb, tile_a, tile_b, njR, nkR;
@@ -743,12 +758,14 @@ struct dnsmc_cvnet {
     NBuf<float> iout;
     NBuf<float2> vc;
     NBuf<float> wgt, cost, lam;
+    NBuf<unsigned int> status;                // DNSMC_STATUS_* bits of the tensor-memory forward
     std::mt19937_64 rng;
     ~dnsmc_cvnet() {
         P.release(); grad.release(); m.release(); v.release(); W.release(); dX.release(); dlab.release();
         idx.release(); H0.release(); H1.release(); H2.release(); H3.release(); dO.release(); dZ3.release();
         dZ2.release(); dZ1.release(); Z1.release(); Z2.release(); Z3.release(); out.release(); part.release();
         lpart.release(); iX.release(); iout.release(); vc.release(); wgt.release(); cost.release(); lam.release();
+        status.release();
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -776,7 +793,29 @@ int launch_forward(const FwdParams &F, cudaStream_t st) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int blocks = (int)std::max(1LL, std::min((slabs + 7) / 8, 2LL * sms));
+    dnsmc::note_launch();
     mlp_forward_kernel<<<blocks, 256, SMEM_FWD, st>>>(F);
+    CK(cudaGetLastError());
+    return DNSMC_OK;
+}
+
+// The tcgen05 forward (mc_cvnet_tc.cuh): one CTA per SM, persistent.
+int launch_forward_tc(TcParams &F, dnsmc_cvnet *n, cudaStream_t st) {
+    static int attr = 0;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(mlp_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+        attr = 1;
+    }
+    const long long tiles = (F.rows + TC_TILE - 1) / TC_TILE;
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = (int)std::max(1LL, std::min((long long)sms, (tiles + TC_WG - 1) / TC_WG));
+    F.Wtc = n->W.p + NWEIGHT;
+    F.P = n->P.p;
+    F.status = n->status.p;
+    dnsmc::note_launch();
+    mlp_tc_kernel<<<blocks, TC_THREADS, TC_SMEM, st>>>(F);
     CK(cudaGetLastError());
     return DNSMC_OK;
 }
@@ -804,12 +843,15 @@ int weight_grad(dnsmc_cvnet *n, const bf16 *dZ, int nout, const bf16 *H, int nin
     G.B = H; G.b_sk = nin; G.b_sn = 1;
     G.C = n->part.p;
     dim3 grid((nout + GBM - 1) / GBM, (nin + GBN - 1) / GBN, splits);
+    dnsmc::note_launch();
     gemm_bf16_kernel<<<grid, 128, 0, n->stream>>>(G);
     CK(cudaGetLastError());
+    dnsmc::note_launch();
     reduce_splits_kernel<<<grid1((long long)nout * nin, 256), 256, 0, n->stream>>>(n->part.p, splits,
                                                                                    (long long)nout * nin,
                                                                                    n->grad.p + offW);
     CK(cudaGetLastError());
+    dnsmc::note_launch();
     colsum_kernel<<<nout, 256, 0, n->stream>>>(dZ, rows, nout, n->grad.p + offB);
     CK(cudaGetLastError());
     return DNSMC_OK;
@@ -824,6 +866,7 @@ int input_grad(dnsmc_cvnet *n, const bf16 *dZ, int nout, long long woff, int nin
     G.B = n->W.p + woff; G.b_sk = nin; G.b_sn = 1;
     G.Z = Zprev; G.D = dZprev;
     dim3 grid((unsigned)((rows + GBM - 1) / GBM), (nin + GBN - 1) / GBN, 1);
+    dnsmc::note_launch();
     gemm_bf16_kernel<<<grid, 128, 0, n->stream>>>(G);
     CK(cudaGetLastError());
     return DNSMC_OK;
@@ -843,6 +886,7 @@ int fwd_bwd(dnsmc_cvnet *n, const bf16 *X, const float *lab, int G, const int *i
     const int lblocks = grid1(rows, 256);
     RTRY(n->lpart.ensure((size_t)lblocks * 3));
     L.part = n->lpart.p;
+    dnsmc::note_launch();
     loss_kernel<<<lblocks, 256, 0, n->stream>>>(L);
     CK(cudaGetLastError());
     RTRY(weight_grad(n, n->dO.p, NOUT, n->H3.p, HID, rows, OFF_W4, OFF_B4));
@@ -867,12 +911,28 @@ int adam_step(dnsmc_cvnet *n) {
     n->step += 1;
     const float c1 = 1.0f - powf(n->cfg.adam_beta1, (float)n->step);
     const float c2 = 1.0f - powf(n->cfg.adam_beta2, (float)n->step);
+    dnsmc::note_launch();
     adam_kernel<<<grid1(NPARAM, 256), 256, 0, n->stream>>>(n->P.p, n->grad.p, n->m.p, n->v.p, n->W.p, NPARAM,
                                                             n->cfg.lr, n->cfg.adam_beta1, n->cfg.adam_beta2,
                                                             n->cfg.adam_eps, c1, c2);
     CK(cudaGetLastError());
+    dnsmc::note_launch();
     weights_to_bf16_kernel<<<grid1(NWEIGHT, 256), 256, 0, n->stream>>>(n->P.p, n->W.p);
     CK(cudaGetLastError());
+    return DNSMC_OK;
+}
+
+int feature_params(dnsmc_cvnet *n, const SolverView &v, FeatParams *out) {
+    FeatParams &F = *out;
+    F = FeatParams{};
+    F.nw = v.imax; F.na = v.jmax; F.nb = v.kmax; F.mode = v.mode;
+    F.fT = v.fieldT; F.fTX = v.fieldTX; F.fw = v.fw; F.field_stride = v.field_stride;
+    F.ew0 = v.i0; F.ea0 = v.j0; F.eb0 = v.k0;
+    F.niR = v.i1 - v.i0; F.njR = v.j1 - v.j0; F.nkR = v.k1 - v.k0;
+    F.region_cells = v.region_cells; F.nfields = v.nfields;
+    F.Tc = n->cfg.T_center; F.Tis = 1.0f / n->cfg.T_scale;
+    F.Xc = n->cfg.x_center; F.Xis = 1.0f / n->cfg.x_scale;
+    if ((v.mode == MODE_TX && !v.fieldTX) || (v.mode != MODE_TX && !v.fieldT)) return state_fail("solver has no fields");
     return DNSMC_OK;
 }
 
@@ -887,6 +947,7 @@ int features_for(dnsmc_cvnet *n, const SolverView &v, bf16 *out, cudaStream_t st
     F.Xc = n->cfg.x_center; F.Xis = 1.0f / n->cfg.x_scale;
     F.out = out;
     if ((v.mode == MODE_TX && !v.fieldTX) || (v.mode != MODE_TX && !v.fieldT)) return state_fail("solver has no fields");
+    dnsmc::note_launch();
     features_kernel<<<grid1((long long)v.nfields * v.region_cells, 128), 128, 0, st>>>(F);
     CK(cudaGetLastError());
     return DNSMC_OK;
@@ -910,6 +971,7 @@ int init_params(dnsmc_cvnet *n) {
     CK(cudaMemcpy(n->P.p, h.data(), NPARAM * sizeof(float), cudaMemcpyHostToDevice));
     CK(cudaMemset(n->m.p, 0, NPARAM * sizeof(float)));
     CK(cudaMemset(n->v.p, 0, NPARAM * sizeof(float)));
+    dnsmc::note_launch();
     weights_to_bf16_kernel<<<grid1(NWEIGHT, 256), 256, 0, n->stream>>>(n->P.p, n->W.p);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(n->stream));
@@ -954,7 +1016,9 @@ int dnsmc_cvnet_create(const dnsmc_cvnet_config *cfg, dnsmc_cvnet **out) {
     if (!rc) rc = n->grad.ensure(NPARAM);
     if (!rc) rc = n->m.ensure(NPARAM);
     if (!rc) rc = n->v.ensure(NPARAM);
-    if (!rc) rc = n->W.ensure(NWEIGHT);
+    if (!rc) rc = n->W.ensure(2 * NWEIGHT);  // row-major and tensor-core order
+    if (!rc) rc = n->status.ensure(1);
+    if (!rc && (e = cudaMemset(n->status.p, 0, sizeof(unsigned int))) != cudaSuccess) rc = cuda_fail("cudaMemset", e);
     if (!rc) rc = init_params(n);
     if (rc) { delete n; return rc; }
     *out = n;
@@ -990,6 +1054,7 @@ int dnsmc_cvnet_set_params(dnsmc_cvnet *n, const float *params, const float *sca
         CK(cudaMemset(n->m.p, 0, NPARAM * sizeof(float)));
         CK(cudaMemset(n->v.p, 0, NPARAM * sizeof(float)));
         n->step = 0;
+        dnsmc::note_launch();
         weights_to_bf16_kernel<<<grid1(NWEIGHT, 256), 256, 0, n->stream>>>(n->P.p, n->W.p);
         CK(cudaGetLastError());
         CK(cudaStreamSynchronize(n->stream));
@@ -1092,6 +1157,7 @@ int dnsmc_cvnet_add_training_data(dnsmc_cvnet *n, dnsmc_solver *s) {
     L.region_cells = v.region_cells; L.moments = v.moments; L.varg = v.varg; L.steps = v.item_steps;
     L.rays = v.rays; L.rays_item = v.rays_item; L.rays_gstride = v.rays_gstride;
     L.lab = n->dlab.p + n->nrows * G * NLAB;
+    dnsmc::note_launch();
     labels_kernel<<<grid1(rows, 128), 128, 0, st>>>(L);
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
@@ -1169,11 +1235,14 @@ int dnsmc_cvnet_eval(dnsmc_cvnet *n, const float *features, long long rows, floa
     RTRY(n->iX.ensure((size_t)rows * K0));
     RTRY(n->iout.ensure((size_t)rows * NOUT));
     CK(cudaMemcpyAsync(n->iX.p, h.data(), h.size() * sizeof(bf16), cudaMemcpyHostToDevice, n->stream));
-    FwdParams F{};
-    F.rows = rows; F.X = n->iX.p; F.nvalid = rows; F.W = n->W.p; F.P = n->P.p; F.out = n->iout.p;
-    RTRY(launch_forward(F, n->stream));
+    TcParams F{};
+    F.rows = rows; F.X = n->iX.p; F.out = n->iout.p;
+    RTRY(launch_forward_tc(F, n, n->stream));
     CK(cudaMemcpyAsync(out, n->iout.p, (size_t)rows * NOUT * sizeof(float), cudaMemcpyDeviceToHost, n->stream));
+    unsigned int st = 0;
+    CK(cudaMemcpyAsync(&st, n->status.p, sizeof st, cudaMemcpyDeviceToHost, n->stream));
     CK(cudaStreamSynchronize(n->stream));
+    if (st) return report_error(DNSMC_ERR_TIMEOUT, "network forward: a bounded wait for the tensor cores ran out");
     return DNSMC_OK;
 }
 
@@ -1230,20 +1299,19 @@ int dnsmc_cvnet_apply(dnsmc_cvnet *n, dnsmc_solver *s, int flags, int mean_rays,
     if (flags & DNSMC_CVNET_BETA) RTRY(solver_beta_device(s, &beta, &nbeta));
     int *rays = nullptr;
     if (flags & DNSMC_CVNET_RAYS) RTRY(solver_rays_device(s, G, &rays));
-    RTRY(n->iX.ensure((size_t)rows * K0));
-    RTRY(n->iout.ensure((size_t)rows * NOUT));
     RTRY(n->vc.ensure((size_t)rows * G));
-    RTRY(features_for(n, v, n->iX.p, st));
-    FwdParams F{};
-    F.rows = rows; F.X = n->iX.p; F.nvalid = rows; F.W = n->W.p; F.P = n->P.p; F.out = n->iout.p;
+    // features, the four layers on the tensor cores and the coefficient
+    // epilogue in one kernel: neither features nor outputs go through memory
+    TcParams F{};
+    F.rows = rows;
+    F.fused_features = 1;
+    RTRY(feature_params(n, v, &F.feat));
+    F.fused_apply = 1;
+    F.apply.rows = rows; F.apply.G = G; F.apply.Sv = n->Sv; F.apply.Sc = n->Sc; F.apply.beta = beta;
+    F.apply.vc = n->vc.p; F.apply.region_cells = v.region_cells;
     // the network's weights are written on its own stream
     CK(cudaStreamSynchronize(n->stream));
-    RTRY(launch_forward(F, st));
-    ApplyParams A{};
-    A.rows = rows; A.G = G; A.out = n->iout.p; A.Sv = n->Sv; A.Sc = n->Sc; A.beta = beta; A.vc = n->vc.p;
-    A.region_cells = v.region_cells;
-    apply_kernel<<<grid1(rows, 256), 256, 0, st>>>(A);
-    CK(cudaGetLastError());
+    RTRY(launch_forward_tc(F, n, st));
     if (flags & DNSMC_CVNET_RAYS) {
         const long long items = (long long)G * v.n_packets;
         RTRY(n->wgt.ensure((size_t)items));
@@ -1253,10 +1321,13 @@ int dnsmc_cvnet_apply(dnsmc_cvnet *n, dnsmc_solver *s, int flags, int mean_rays,
         P.nfields = v.nfields; P.G = G; P.n_packets = v.n_packets; P.npa = v.npa; P.npb = v.npb;
         P.tile_a = v.tile_a; P.tile_b = v.tile_b; P.njR = v.j1 - v.j0; P.nkR = v.k1 - v.k0;
         P.region_cells = v.region_cells; P.vc = n->vc.p; P.wgt = n->wgt.p; P.cost = n->cost.p;
+        dnsmc::note_launch();
         alloc_weights_kernel<<<grid1(items * 32, 256), 256, 0, st>>>(P);
         CK(cudaGetLastError());
+        dnsmc::note_launch();
         alloc_scale_kernel<<<1, 1024, 0, st>>>(n->wgt.p, n->cost.p, items, (float)mean_rays, n->lam.p);
         CK(cudaGetLastError());
+        dnsmc::note_launch();
         alloc_rays_kernel<<<grid1(items, 256), 256, 0, st>>>(n->wgt.p, items, n->lam.p, B, min_rays, max_rays, rays);
         CK(cudaGetLastError());
     }

@@ -381,6 +381,7 @@ struct dnsmc_solver {
     cudaGraphExec_t graph_exec = nullptr;
     std::vector<unsigned char> graph_key;
     long long graph_captures = 0, graph_launches = 0;
+    long long graph_kernels = 0;             // kernel nodes of the captured graph
 };
 
 namespace {
@@ -1220,10 +1221,24 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
             if (s->graph_exec) { cudaGraphExecDestroy(s->graph_exec); s->graph_exec = nullptr; }
             cudaGraph_t g = nullptr;
             CUDA_TRY(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed));
+            const long long counted = launch_count();
             const int rc = kernels(false);
+            note_launch(counted - launch_count());  // captured, not launched: each replay counts them
             const cudaError_t ec = cudaStreamEndCapture(s->stream, &g);
             if (rc) { if (g) cudaGraphDestroy(g); return rc; }
             if (ec != cudaSuccess) return fail(DNSMC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ec));
+            // kernel nodes of the graph: the launches each replay adds
+            size_t nn = 0;
+            s->graph_kernels = 0;
+            if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
+                std::vector<cudaGraphNode_t> nodes(nn);
+                if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess)
+                    for (size_t q = 0; q < nn; ++q) {
+                        cudaGraphNodeType ty;
+                        if (cudaGraphNodeGetType(nodes[q], &ty) == cudaSuccess && ty == cudaGraphNodeTypeKernel)
+                            s->graph_kernels += 1;
+                    }
+            }
             const cudaError_t ei = cudaGraphInstantiate(&s->graph_exec, g, 0);
             cudaGraphDestroy(g);
             if (ei != cudaSuccess) { s->graph_exec = nullptr; return fail(DNSMC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei)); }
@@ -1234,6 +1249,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         CUDA_TRY(cudaGraphLaunch(s->graph_exec, s->stream));
         CUDA_TRY(cudaEventRecord(s->ev_march1, s->stream));
         s->graph_launches += 1;
+        note_launch(s->graph_kernels);
     }
     s->last = P;
     s->lastF = F;
@@ -2037,6 +2053,12 @@ int dnsmc_set_graph(dnsmc_solver *s, int enable) {
         s->graph_exec = nullptr;
         s->graph_key.clear();
     }
+    return DNSMC_OK;
+}
+
+int dnsmc_get_launch_count(long long *n) {
+    if (!n) return fail(DNSMC_ERR_ARG, "null argument");
+    *n = launch_count();
     return DNSMC_OK;
 }
 

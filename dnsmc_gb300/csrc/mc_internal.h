@@ -238,6 +238,11 @@ struct SplinePass {
 };
 int launch_spline_pass(const SplinePass &q, void *stream);
 
+// Kernels this library has launched in this process (every launch site
+// calls note_launch; a CUDA-graph replay adds the kernel nodes of its graph).
+void note_launch(long long n = 1);
+long long launch_count();
+
 // launchers (mc_kernels.cu); all stream-ordered
 int launch_march_ex(int mode, const MarchParams &p, int blocks, int threads, void *stream, bool trace, bool cv,
                     bool mom, bool gen);

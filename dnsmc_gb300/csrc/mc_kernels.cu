@@ -36,6 +36,8 @@
 // -fmad=false, so the host replay reproduces every ray bit for bit; exp and
 // sin/cos are the project's own polynomial kernels (mc_expm1 / mc_sincos) for
 // the same reason.  Tallies (sum X, sum X^2) are FP64.
+#include <atomic>
+
 #include "mc_march.cuh"
 
 namespace dnsmc {
@@ -200,6 +202,10 @@ __global__ void field_stats_pass2(const double *part, int nparts, double *out) {
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+static std::atomic<long long> g_launches{0};
+void note_launch(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+long long launch_count() { return g_launches.load(std::memory_order_relaxed); }
+
 static inline int grid_for(long long n, int threads) {
     long long b = (n + threads - 1) / threads;
     if (b > 4096) b = 4096;
@@ -745,6 +751,7 @@ __global__ void adaptive_rays_kernel(const AdaptParams A) {
 
 int launch_adaptive_rays(const AdaptParams &a, void *stream) {
     const long long threads = (long long)a.n_packets * 32;
+    dnsmc::note_launch();
     adaptive_rays_kernel<<<grid_for(threads, 256), 256, 0, (cudaStream_t)stream>>>(a);
     return (int)cudaGetLastError();
 }
@@ -801,8 +808,11 @@ int launch_item_order(const int *rays, int gstride, int n_packets, int n_groups,
     cudaStream_t st = (cudaStream_t)stream;
     cudaError_t e = cudaMemsetAsync(hist, 0, kOrderBuckets * sizeof(unsigned int), st);
     if (e != cudaSuccess) return (int)e;
+    dnsmc::note_launch();
     order_hist_kernel<<<grid_for(n_items, 256), 256, 0, st>>>(rays, gstride, n_packets, n_groups, n_items, B, hist);
+    dnsmc::note_launch();
     order_scan_kernel<<<1, 1024, 0, st>>>(hist);
+    dnsmc::note_launch();
     order_scatter_kernel<<<grid_for(n_items, 256), 256, 0, st>>>(rays, gstride, n_packets, n_groups, n_items, B,
                                                                  hist, order);
     return (int)cudaGetLastError();
@@ -810,9 +820,12 @@ int launch_item_order(const int *rays, int gstride, int n_packets, int n_groups,
 
 int launch_cv_prepare(const CvParams &c, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
+    dnsmc::note_launch();
     cv_layer_kernel<<<dim3(c.nw, c.nfields), 256, 0, st>>>(c);
     const long long n = (long long)c.nfields * c.n_samples * c.nw;
+    dnsmc::note_launch();
     cv_sur_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
+    dnsmc::note_launch();
     cv_jhat_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(c);  // one warp per (field, sample, layer)
     return (int)cudaGetLastError();
 }
@@ -822,9 +835,12 @@ int launch_cv_mean(const CvParams &c, void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
     if (c.nodes) {  // tables without particles: node sums, then the cells
         const long long blocks = (long long)c.nfields * c.n_groups * (c.ew1 - c.ew0) + c.n_groups;
+        dnsmc::note_launch();
         cv_nodes_kernel<<<(unsigned)blocks, 256, 0, st>>>(c);
+        dnsmc::note_launch();
         cv_mean_nodes_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
     } else {
+        dnsmc::note_launch();
         cv_mean_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
     }
     return (int)cudaGetLastError();
@@ -834,6 +850,7 @@ int march_occupancy(int mode, int threads) { return march_occupancy_ex(mode, thr
 
 int launch_field_pos(const float *fT, const float2 *fTX, int2 *outP, int4 *outPX, long long n, float T0,
                      float invdT, int nT, float X0, float invdX, int nX, void *stream) {
+    dnsmc::note_launch();
     field_pos_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(fT, fTX, outP, outPX, n, T0, invdT, nT,
                                                                         X0, invdX, nX);
     return (int)cudaGetLastError();
@@ -857,9 +874,11 @@ int launch_finalize(const FinalizeParams &p, void *stream) {
     if (q.rays_per_packet) {
         if (!q.rcp) return (int)cudaErrorInvalidValue;
         const long long nr = finalize_rcp_count(q);
+        dnsmc::note_launch();
         ray_reciprocals_kernel<<<grid_for(nr, 256), 256, 0, st>>>(q.rays_per_packet, nr, q.rcp);
     }
     const long long n = (long long)q.nfields * q.region_cells;
+    dnsmc::note_launch();
     finalize_kernel<<<grid_for(n, 256), 256, 0, st>>>(q);
     return (int)cudaGetLastError();
 }
@@ -921,6 +940,7 @@ __global__ void spline_pass_kernel(SplinePass q) {
 
 int launch_spline_pass(const SplinePass &q, void *stream) {
     if (q.nlines <= 0) return 0;
+    dnsmc::note_launch();
     spline_pass_kernel<<<grid_for(q.nlines, 128), 128, 0, (cudaStream_t)stream>>>(q);
     return (int)cudaGetLastError();
 }
@@ -928,6 +948,7 @@ int launch_spline_pass(const SplinePass &q, void *stream) {
 int launch_pack_T(const float *src, float *dst, int nw, int na, int nb, long long si, long long sj,
                   long long sk, long long base, void *stream) {
     const long long n = (long long)nw * na * nb;
+    dnsmc::note_launch();
     pack_T_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(src, dst, nw, na, nb, si, sj, sk, base);
     return (int)cudaGetLastError();
 }
@@ -935,6 +956,7 @@ int launch_pack_T(const float *src, float *dst, int nw, int na, int nb, long lon
 int launch_pack_TX(const float *srcT, const float *srcX, float2 *dst, int nw, int na, int nb, long long si,
                    long long sj, long long sk, long long base, void *stream) {
     const long long n = (long long)nw * na * nb;
+    dnsmc::note_launch();
     pack_TX_kernel<<<grid_for(n, 256), 256, 0, (cudaStream_t)stream>>>(srcT, srcX, dst, nw, na, nb, si, sj, sk, base);
     return (int)cudaGetLastError();
 }
@@ -942,7 +964,9 @@ int launch_pack_TX(const float *srcT, const float *srcX, float2 *dst, int nw, in
 int launch_field_stats(const float *fT, const float2 *fTX, long long n, double *partials, double *out,
                        void *stream) {
     cudaStream_t st = (cudaStream_t)stream;
+    dnsmc::note_launch();
     field_stats_pass1<<<kStatBlocks, kStatThreads, 0, st>>>(fT, fTX, n, partials);
+    dnsmc::note_launch();
     field_stats_pass2<<<1, 32, 0, st>>>(partials, kStatBlocks, out);
     return (int)cudaGetLastError();
 }

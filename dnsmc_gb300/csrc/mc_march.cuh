@@ -819,6 +819,7 @@ inline int march_prepare_smem(void (*k)(const MarchParams), size_t smem) {
 inline int march_launch_one(void (*k)(const MarchParams), int blocks, int threads, size_t smem, cudaStream_t st,
                             const MarchParams &p) {
     if (const int e = march_prepare_smem(k, smem)) return e;
+    dnsmc::note_launch();
     k<<<blocks, threads, smem, st>>>(p);
     return (int)cudaGetLastError();
 }

@@ -308,6 +308,11 @@ int  dnsmc_set_graph(dnsmc_solver *s, int enable);
 /* Number of graph captures and replays so far.                              */
 int  dnsmc_get_graph_info(const dnsmc_solver *s, long long *captures,
                           long long *launches);
+/* Kernels this library has launched in this process, all solvers and
+ * networks together (a CUDA-graph replay counts the kernel nodes of its
+ * graph).  The difference across a region of code is the number of this
+ * library's kernels that region launched.                                   */
+int  dnsmc_get_launch_count(long long *n);
 /* The solver's CUDA stream (cudaStream_t; created on first use): every solve,
  * upload and network evaluation of this solver is ordered on it, so a caller
  * can order its own work (or CUDA events) against them.                      */

@@ -570,6 +570,8 @@ typedef struct {
     float mg_da[6], mg_db[6];
     float Ly, Lz;
     int cpl;                  // cells per lane (1, 2 or 4): a packet is 32 * cpl cells (tile_a x tile_b)
+    int pw_step;              // > 1 (orc_packet_mc, orc_cv_mean): only every pw_step-th wall-normal layer
+                              // of the region, from ew0, with the rays of an unstrided run
 } OrcPacketConfig;
 
 }  // extern "C"
@@ -1265,7 +1267,8 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
     const int ta = c->tile_a, tb = nl / ta;
     const int niR = c->ew1 - c->ew0, njR = c->ea1 - c->ea0, nkR = c->eb1 - c->eb0;
     const int npa = (njR + ta - 1) / ta, npb = (nkR + tb - 1) / tb;
-    const int np = npa * npb * niR;
+    const int step = c->pw_step > 1 ? c->pw_step : 1;
+    const int np = npa * npb * ((niR + step - 1) / step);
     const int nG = c->mode == 0 ? 1 : c->n_groups;
     const long long items = (long long)c->nfields * nG * np;
     const long long rc = (long long)niR * njR * nkR;
@@ -1275,7 +1278,10 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
 #endif
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : steps)
     for (long long it = 0; it < items; ++it) {
-        const int p = (int)(it % np);
+        // packet of the region (layers strided by pw_step) and its natural
+        // index, which keys its rays and ray counts as in an unstrided run
+        const int ps = (int)(it % np);
+        const int p = ps % (npa * npb) + (ps / (npa * npb)) * step * npa * npb;
         const long long fg = it / np;
         const int G = (int)(fg % nG), f = (int)(fg / nG);
         double S[128], S2[128], st = 0;
@@ -1292,6 +1298,103 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
         }
     }
     if (steps_out) *steps_out = steps;
+    return 0;
+}
+
+// Exact means of the control variate of the packet replay (cv = 1), in FP64,
+// for every region cell and band group: E[Y_a] = sum_s C_s k_s(T_i, x_i)
+// (Ib_s(T_i) - Jhat_s(l)) and E[Y_b] = sum_s C_s k_s(T_i, x_i) Ahat_s(l)
+// (Ib_s(T_i) - Ibar_s(l)) over the group's samples s (grp_start / sid / C),
+// with Jhat_s(l) and Ahat_s(l) the direction averages of the surrogate's
+// collected intensity and own-layer absorptance: the straight flight from the
+// centre of layer l through the layer-mean medium (sur_k, sur_I), stopped
+// beyond optical depth ln(1/toll) or at the black walls (ibw), integrated over
+// mu on both hemispheres with the caller's quadrature (mu, w on [0, 1]).
+// muY: [f][G][tc][2] in tally order (with pw_step > 1 only the replay's
+// layers are written).  Table models (mode 1, 2) only.
+int orc_cv_mean(const OrcPacketConfig *c, const int *grp_start, const int *sid, const double *C, const double *mu,
+                const double *wq, int nquad, int nthreads, double *muY) {
+    if (!c || c->mode == 0 || !c->sur_k || !c->sur_I) return 1;
+    const int nw = c->nw, nsamp = c->nbands * c->nq, nG = c->n_groups;
+    const int niR = c->ew1 - c->ew0, njR = c->ea1 - c->ea0, nkR = c->eb1 - c->eb0;
+    const long long rc = (long long)niR * njR * nkR;
+    const double dtoll = (double)(float)(-std::log((double)c->toll));
+    const int step = c->pw_step > 1 ? c->pw_step : 1;
+    std::vector<double> J((size_t)c->nfields * nsamp * nw), A(J.size());
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long fs = 0; fs < (long long)c->nfields * nsamp; ++fs) {
+        const int s_ = (int)(fs % nsamp), b = s_ / c->nq;
+        const float *sk = c->sur_k + (size_t)fs * nw, *sI = c->sur_I + (size_t)fs * nw;
+        for (int l = c->ew0; l < c->ew1; l += step) {  // the region's (solved) layers
+            const double o = 0.5 * ((double)c->fw[l] + (double)c->fw[l + 1]);
+            double acc = 0, accA = 0;
+            for (int d = -1; d <= 1; d += 2) {
+                const double Iw = c->ibw[(d < 0 ? 0 : 1) * c->nbands + b];
+                for (int q = 0; q < nquad; ++q) {
+                    const double m = mu[q];
+                    double tau = 1, Jv = 0, t0 = 0, dcum = 0;
+                    int i = l;
+                    double seg = d > 0 ? ((double)c->fw[l + 1] - o) : (o - (double)c->fw[l]);
+                    for (;;) {
+                        const double opt = (double)sk[i] * seg / m;
+                        if (dcum + opt > dtoll) { Jv += tau * (double)sI[i]; break; }
+                        const double a = -std::expm1(-opt);
+                        Jv += tau * a * (double)sI[i];
+                        tau -= tau * a;
+                        dcum += opt;
+                        if (i == l) t0 = tau;
+                        i += d;
+                        if (i < 0 || i >= nw) { Jv += tau * Iw; break; }
+                        seg = (double)c->fw[i + 1] - (double)c->fw[i];
+                    }
+                    acc += wq[q] * Jv;
+                    accA += wq[q] * (1.0 - t0);
+                }
+            }
+            J[(size_t)fs * nw + l] = 0.5 * acc;
+            A[(size_t)fs * nw + l] = 0.5 * accA;
+        }
+    }
+    const double invdT = 1.0 / (double)c->dT, invdX = c->nX > 1 ? 1.0 / (double)c->dX : 1.0;
+#pragma omp parallel for schedule(static)
+    for (long long fc = 0; fc < (long long)c->nfields * rc; ++fc) {
+        const int f = (int)(fc / rc);
+        const long long tc = fc % rc;
+        const int a = (int)(tc % njR), b = (int)((tc / njR) % nkR), w = (int)(tc / ((long long)njR * nkR));
+        if (w % step) continue;  // a layer the replay skips
+        const int wi = c->ew0 + w, ai = c->ea0 + a, bi = c->eb0 + b;
+        const long long o = (long long)f * nw * c->na * c->nb + wi + (long long)nw * (ai + (long long)c->na * bi);
+        int ti = 0, xi = 0;
+        double ft = 0, fx = 0;
+        p_gpos<double>((double)c->fieldT[o], (double)c->T0, invdT, c->nT, &ti, &ft);
+        if (c->mode == 2) p_gpos<double>((double)c->fieldX[o], (double)c->X0, invdX, c->nX, &xi, &fx);
+        for (int G = 0; G < nG; ++G) {
+            double ea = 0, eb = 0;
+            for (int e = grp_start[G]; e < grp_start[G + 1]; ++e) {
+                const int s_ = sid[e], band = s_ / c->nq;
+                const float *kt = c->ktab + (size_t)s_ * c->nT * c->nX + (size_t)ti * c->nX + xi;
+                double k;
+                if (c->mode == 2) {
+                    const double k0 = (double)kt[0] + fx * ((double)kt[1] - (double)kt[0]);
+                    const double k1 = (double)kt[c->nX] + fx * ((double)kt[c->nX + 1] - (double)kt[c->nX]);
+                    k = k0 + ft * (k1 - k0);
+                } else {
+                    k = (double)kt[0] + ft * ((double)kt[1] - (double)kt[0]);
+                }
+                const float *ib = c->ibtab + (size_t)band * c->nT + ti;
+                const double Ib = (double)ib[0] + ft * ((double)ib[1] - (double)ib[0]);
+                const size_t js = ((size_t)f * nsamp + s_) * nw + wi;
+                ea += C[e] * k * (Ib - J[js]);
+                eb += C[e] * k * A[js] * (Ib - (double)c->sur_I[js]);
+            }
+            double *out = muY + 2 * (((long long)f * nG + G) * rc + tc);
+            out[0] = ea;
+            out[1] = eb;
+        }
+    }
     return 0;
 }
 

@@ -67,7 +67,7 @@ class PacketConfig(ctypes.Structure):
         ("mg_levels", ctypes.c_int), ("mg_steps", ctypes.c_int), ("mgT", _f), ("mgfw", _f),
         ("mg_off", ctypes.c_longlong * 6), ("mg_fwoff", ctypes.c_int * 6), ("mg_da", ctypes.c_float * 6),
         ("mg_db", ctypes.c_float * 6), ("Ly", ctypes.c_float), ("Lz", ctypes.c_float),
-        ("cpl", ctypes.c_int),
+        ("cpl", ctypes.c_int), ("pw_step", ctypes.c_int),
     ]
 
 
@@ -90,6 +90,9 @@ def load():
         lib.orc_packet_mc.restype = ctypes.c_int
         lib.orc_packet_trace.argtypes = [ctypes.POINTER(PacketConfig)] + [ctypes.c_int] * 5 + [_i32, _i, _u32]
         lib.orc_expm1n.argtypes = [_f, _f, ctypes.c_longlong]
+        lib.orc_cv_mean.argtypes = [ctypes.POINTER(PacketConfig), _i, _i, _d, _d, _d, ctypes.c_int, ctypes.c_int,
+                                    _d]
+        lib.orc_cv_mean.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -342,6 +345,132 @@ def cv_jhat(sur_k, sur_I, fw, toll, Iw_west, Iw_east):
                 accA += wq * (1.0 - t0)
         out[l] = 0.5 * acc, 0.5 * accA
     return out
+
+
+def layer_surrogate(tb: dict, T: np.ndarray, x: np.ndarray | None):
+    """The oracle's own layer-mean medium: per field and wall-normal layer
+    the float64 plane means of T and x_H2O, and at them k of every spectral
+    sample (bilinear in T, x) and the band intensity (linear in T), rounded
+    to float32.  Returns sur_k, sur_I of shape (nfields, nbands * nq, nw)."""
+    T = np.asarray(T, np.float64)
+    nf, nw = T.shape[0], T.shape[3]
+    Tb = T.mean(axis=(1, 2))                                   # (nf, nw)
+    Xb = np.asarray(x, np.float64).mean(axis=(1, 2)) if x is not None else np.zeros_like(Tb)
+    k = np.asarray(tb["k"], np.float64)                        # (nb, nq, nT, nX)
+    nb, nq, nT, nX = k.shape
+    p = np.clip((Tb - tb["T0"]) / tb["dT"], 0, nT - 1)
+    ti = np.minimum(p.astype(int), nT - 2)
+    ft = p - ti
+    if nX > 1:
+        px = np.clip((Xb - tb["X0"]) / tb["dX"], 0, nX - 1)
+        xi = np.minimum(px.astype(int), nX - 2)
+        fx = px - xi
+    else:
+        xi, fx = np.zeros_like(ti), np.zeros_like(Tb)
+    kk = k.reshape(nb * nq, nT, nX)
+    xj = np.minimum(xi + 1, nX - 1)
+    k00, k01 = kk[:, ti, xi], kk[:, ti, xj]
+    k10, k11 = kk[:, ti + 1, xi], kk[:, ti + 1, xj]
+    k0 = k00 + fx * (k01 - k00)
+    k1 = k10 + fx * (k11 - k10)
+    sur_k = (k0 + ft * (k1 - k0)).transpose(1, 0, 2)         # (nf, S, nw)
+    Ib = np.asarray(tb["Ib"], np.float64)                      # (nb, nT)
+    Ibl = Ib[:, ti] + ft * (Ib[:, ti + 1] - Ib[:, ti])        # (nb, nf, nw)
+    sur_I = np.repeat(Ibl, nq, axis=0).transpose(1, 0, 2)
+    return np.ascontiguousarray(sur_k, np.float32), np.ascontiguousarray(sur_I, np.float32)
+
+
+def fp64_cv_solution(mirror, dnu, wq, T: np.ndarray, x: np.ndarray | None, *, rays: int, nbatch: int = 8,
+                     seed: int = 7, threads: int = 0, layer_step: int = 1):
+    """An FP64 solution of Q over `mirror`'s region, independent of the GPU.
+
+    `mirror` is a host-only Solver carrying the table, geometry, region,
+    packet shape and host-built sampling tables (dnsmc_prepare_sampling),
+    configured without a control variate (the oracle adds its own);
+    dnu, wq: the table's band widths and g weights.
+    The estimator is the packet scheme in float64 (Packet<double>) with the
+    profile control variate built entirely here: the oracle's own layer-mean
+    medium (layer_surrogate), its exact means E[Y] (orc_cv_mean: a float64
+    quadrature over the wall-normal cosine with numpy's Gauss-Legendre
+    nodes, cv_quadrature), beta = (1, -1); `rays` RQMC rays per cell and
+    group in `nbatch` shifted replicates.  Raw tables only (C_s = 4 pi 100
+    dnu w_g, the coefficient of dnsmc_set_table without reference CDFs).
+    Returns (Q, var) of shape (nfields, nk, nj, ni) over the region, var the
+    variance of Q from the replicate means.  layer_step > 1 solves only every
+    layer_step-th wall-normal layer of the region (from its first); the other
+    layers of the returned arrays are NaN."""
+    T = np.ascontiguousarray(T, np.float32)
+    c, keep = packet_config(mirror, T, x, use_double=1)
+    tb = mirror.table()
+    sur_k, sur_I = layer_surrogate(tb, T, x)
+    keep.update(sur_k=sur_k, sur_I=sur_I)
+    c.cv, c.sur_k, c.sur_I, c.beta = 1, _fp(sur_k), _fp(sur_I), None
+    c.sampler, c.nbatch, c.rays, c.seed = 1, nbatch, rays, seed
+    c.rays_per_packet, c.rays_gstride = None, 0
+    c.pw_step = layer_step
+    nG = c.n_groups
+    i0, i1, j0, j1, k0, k1 = mirror._region
+    ni, nj, nk = i1 - i0, j1 - j0, k1 - k0
+    rc = ni * nj * nk
+    tal, _ = packet_mc(c, nG, rc, threads)
+    # C_s and the band groups of the host's sampling construction
+    nb, nq = tb["nbands"], tb["nq"]
+    dnu = np.asarray(dnu, np.float32).astype(np.float64)
+    wq = np.asarray(wq, np.float32).astype(np.float64)
+    sid, C, gs = [], [], [0]
+    for G in range(nG):
+        for b in range(G * nb // nG, (G + 1) * nb // nG):
+            for g in range(nq):
+                sid.append(b * nq + g)
+                C.append(4.0 * math.pi * 100.0 * dnu[b] * wq[g])
+        gs.append(len(sid))
+    sid = np.asarray(sid, np.int32)
+    C = np.asarray(C, np.float64)
+    gs = np.asarray(gs, np.int32)
+    mu, w = cv_quadrature()
+    muY = np.zeros((T.shape[0], nG, rc, 2), np.float64)
+    assert load().orc_cv_mean(ctypes.byref(c), gs.ctypes.data_as(_i), sid.ctypes.data_as(_i),
+                              C.ctypes.data_as(_d), mu.ctypes.data_as(_d), w.ctypes.data_as(_d), len(mu), threads,
+                              muY.ctypes.data_as(_d)) == 0
+    m = tal[..., 0] / rays                                     # (nf, G, rc): mean of X - Y_a + Y_b
+    vg = np.maximum(0.0, tal[..., 1] / nbatch - m * m) / (nbatch - 1)
+    Qg = m + muY[..., 0] - muY[..., 1]
+    shape = (T.shape[0], ni, nk, nj)                           # tally order: i, k, j
+    Q = Qg.sum(1).reshape(shape).transpose(0, 2, 3, 1)
+    V = vg.sum(1).reshape(shape).transpose(0, 2, 3, 1)
+    if layer_step > 1:
+        skip = np.ones(ni, bool)
+        skip[::layer_step] = False
+        Q[..., skip] = np.nan
+        V[..., skip] = np.nan
+    return np.ascontiguousarray(Q), np.ascontiguousarray(V)
+
+
+def ref_tables_x_slice(table: dict, xbar: float) -> dict:
+    """The reference-format tables (ref_mc, model 0) of a k(band, g, T, x)
+    table at one x_H2O: the reference has no x axis.  k(band, T, g) at xbar
+    (linear in x), band Planck intensities at the band centres, the band and
+    g CDFs of the emission k Ib dnu w_g at every table temperature, and the
+    Planck mean kP = pi sum(k Ib dnu w_g) / (sigma T^4), float32."""
+    k = np.asarray(table["k"], np.float64)
+    X = table["X0"] + table["dX"] * np.arange(k.shape[3])
+    kx = np.empty(k.shape[:3], np.float64)
+    for b in range(kx.shape[0]):
+        for g in range(kx.shape[1]):
+            kx[b, g] = [np.interp(xbar, X, k[b, g, t]) for t in range(kx.shape[2])]
+    nT = kx.shape[2]
+    Tnb = (table["T0"] + table["dT"] * np.arange(nT)).astype(np.float32)
+    C1, C2 = 3.741771790075259e-16, 0.014387741858429
+    nu = np.asarray(table["wvc"], np.float64)
+    Ib = C1 * (nu[None, :] * 100) ** 3 / (np.pi * (np.exp(C2 * nu[None, :] * 100 / Tnb[:, None]) - 1))  # [nT][nB]
+    e = kx.transpose(2, 0, 1) * Ib[:, :, None] * np.asarray(table["dnu"])[None, :, None] * 100 \
+        * np.asarray(table["wq"])[None, None, :]
+    eb = e.sum(2)
+    prob = np.cumsum(eb, 1) / eb.sum(1, keepdims=True)
+    probg = np.cumsum(e, 2) / np.maximum(e.sum(2, keepdims=True), 1e-300)
+    kP = np.pi * eb.sum(1) / (SIGMA * Tnb.astype(np.float64) ** 4)
+    return dict(Tnb=Tnb, kq=kx.transpose(0, 2, 1).astype(np.float32), wvc=np.asarray(table["wvc"], np.float32),
+                prob=prob.astype(np.float32), probg=probg.astype(np.float32), kP=kP.astype(np.float32))
 
 
 def solver_rays(solver) -> int:

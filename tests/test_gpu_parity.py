@@ -554,3 +554,19 @@ def test_results_into_caller_arrays():
     with pytest.raises(ValueError):
         s.results(out=(np.zeros(5), So))
     s.close()
+
+
+def test_launch_count_counts_every_kernel():
+    """dnsmc_get_launch_count: a grey solve launches the march and the
+    finalize kernel; a CUDA-graph replay of the same solve adds the graph's
+    two kernel nodes (the capture itself launches nothing)."""
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=16, jmax=32, kmax=8, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=0, T_west=300, T_east=300, kappa=1.0, seed=4))
+    s.set_fields(smooth_field(16, 32, 8, 400, 900, 2))
+    s.set_rays(8)
+    for graph in (False, True, True):
+        s.set_graph(graph)
+        n0 = _lib.launch_count()
+        s.solve(timeout_s=60)
+        assert _lib.launch_count() - n0 == 2, graph
+    s.close()
