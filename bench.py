@@ -601,17 +601,25 @@ def run_batched(args, flushbuf_mb=256):
     s = make(cfg["block_threads"], cfg["tile_a"], cfg["n_groups"])
     s.set_graph(True)
     s.set_fields(T, x)
+    floor = args.ray_floor
     per_tau = 400.0
     e = None
     for _ in range(4):  # rays_per_tau for 1 % RMS (the clamps make the error non-linear in it)
-        s.set_rays_adaptive(per_tau, 64, 4096)
+        s.set_rays_adaptive(per_tau, floor, 4096)
         Q, S = s.solve(timeout_s=900)
         e = rms_error(Q, S)
         if 0.9 * TARGET_ERR <= e <= 0.99 * TARGET_ERR:
             break
         per_tau *= (e / (0.97 * TARGET_ERR)) ** 2
-    s.set_rays_adaptive(per_tau, 64, 4096)
+    s.set_rays_adaptive(per_tau, floor, 4096)
     rp = s.rays_per_item()
+    # the allocation: packets per ray-count bin (powers of two from the floor)
+    edges = [floor]
+    while edges[-1] < 4096:
+        edges.append(edges[-1] * 2)
+    counts, _ = np.histogram(rp, bins=edges + [1 << 30])
+    hist = {f"{a}-{b - 1}" if b < (1 << 30) else f">={a}": int(c) for a, b, c in zip(edges, edges[1:] + [1 << 30],
+                                                                                     counts)}
     stream = torch.cuda.ExternalStream(s.stream())
     flushbuf = torch.empty(flushbuf_mb * 256 * 1024, dtype=torch.float32, device="cuda")
     for _ in range(max(3, args.warmup)):
@@ -652,10 +660,11 @@ def run_batched(args, flushbuf_mb=256):
         "ms_per_step": t / args.steps, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"batched: {nsnap} ck channel snapshots of {n}^3 (seeds 0-15) in one graph-replayed "
-                               "persistent launch, rays per packet ~ local optical thickness clamped to 64-4096, "
+                               f"persistent launch, rays per packet ~ local optical thickness clamped to {floor}-4096, "
                                "profile control variate, RQMC rays",
-                   "snapshots": nsnap, "n": n, "rays_per_tau": per_tau, "rays_mean": float(rp.mean()),
-                   "rays_min": int(rp.min()), "rays_max": int(rp.max()), "autotuned": cfg,
+                   "snapshots": nsnap, "n": n, "rays_per_tau": per_tau, "rays_floor": floor,
+                   "rays_mean": float(rp.mean()), "rays_min": int(rp.min()), "rays_max": int(rp.max()),
+                   "rays_histogram_packets": hist, "rays_at_floor": float((rp == floor).mean()), "autotuned": cfg,
                    "autotune_cached": tune["cached"], "target_rms_error": TARGET_ERR,
                    "rms_error_timed": float(np.mean(errs)), "graph_captures": cap, "graph_launches": glaunches,
                    "l2": "flushed before every timed step (256 MB device write)", "parallelism": "cells x1"},
@@ -907,6 +916,9 @@ def main():
                          "the isothermal slab; batched: 16 snapshots of 96^3; particles: gas + scattering "
                          "particles with grey walls, 192^3")
     ap.add_argument("--no-c0", action="store_true", help="skip the grey 64^3 block of the default workload")
+    ap.add_argument("--ray-floor", type=int, default=64,
+                    help="batched workload: smallest rays per packet of the optical-thickness allocation (64 as "
+                         "the configuration names; lower floors let the allocation vary)")
     ap.add_argument("--groups", type=int, default=GROUPS, help="band groups (stratification) of the solves")
     ap.add_argument("--no-validate", action="store_true",
                     help="skip the check of the timed field against an independent high-ray solution")
