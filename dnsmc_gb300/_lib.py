@@ -54,6 +54,17 @@ class TableDesc(ctypes.Structure):
     ]
 
 
+class LblDesc(ctypes.Structure):
+    """Mirror of dnsmc_lbl_desc."""
+    _fields_ = [
+        ("nT", ctypes.c_int), ("nX", ctypes.c_int), ("npts", ctypes.c_longlong),
+        ("wv0", ctypes.c_double), ("dwv", ctypes.c_double), ("kappa", ctypes.POINTER(ctypes.c_double)),
+        ("nbands", ctypes.c_int), ("first", ctypes.POINTER(ctypes.c_longlong)), ("count", ctypes.POINTER(ctypes.c_int)),
+        ("wv_left", ctypes.POINTER(ctypes.c_double)), ("wv_right", ctypes.POINTER(ctypes.c_double)),
+        ("nq", ctypes.c_int), ("gq", ctypes.POINTER(ctypes.c_double)), ("n_pwrk", ctypes.c_int),
+    ]
+
+
 class CvNetConfig(ctypes.Structure):
     """Mirror of dnsmc_cvnet_config."""
     _fields_ = [
@@ -125,6 +136,7 @@ SIGNATURES = {
     "dnsmc_get_results": (ctypes.c_int, [ctypes.c_void_p, c_double_p, c_double_p]),
     "dnsmc_save_table": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "dnsmc_get_launch_count": (ctypes.c_int, [ctypes.POINTER(ctypes.c_longlong)]),
+    "dnsmc_ck_from_lbl": (ctypes.c_int, [ctypes.POINTER(LblDesc), c_float_p, c_double_p]),
     "dnsmc_load_table": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "dnsmc_set_result_type": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "dnsmc_get_results_float": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p]),

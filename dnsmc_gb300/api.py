@@ -602,6 +602,35 @@ class CvNet:
             solver._beta_dev = True
 
 
+def ck_from_lbl(spec: dict, gq, n_pwrk: int = 10000):
+    """Correlated-k table from line-by-line spectra on the GPU
+    (dnsmc_ck_from_lbl): spec holds kappa [nT][nX][npts] (1/m, uniform grid
+    wv0 + i dwv in 1/cm) and the bands' first point, point count and edges
+    (the keys of synth.lbl_spectrum).  Returns (kq [nbands][nq][nT][nX]
+    float32, the layout of Solver.set_table's k, and kavg [nT][nX][nbands])."""
+    lib = _lib.load()
+    k = np.ascontiguousarray(spec["kappa"], np.float64)
+    nT, nX, npts = k.shape
+    gq = np.ascontiguousarray(gq, np.float64)
+    first = np.ascontiguousarray(spec["first"], np.int64)
+    count = np.ascontiguousarray(spec["count"], np.int32)
+    wl = np.ascontiguousarray(spec["wv_left"], np.float64)
+    wr = np.ascontiguousarray(spec["wv_right"], np.float64)
+    d = _lib.LblDesc()
+    d.nT, d.nX, d.npts, d.wv0, d.dwv = nT, nX, npts, float(spec["wv0"]), float(spec["dwv"])
+    dp = ctypes.POINTER(ctypes.c_double)
+    d.kappa = k.ctypes.data_as(dp)
+    d.nbands = first.size
+    d.first = first.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))
+    d.count = count.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    d.wv_left, d.wv_right = wl.ctypes.data_as(dp), wr.ctypes.data_as(dp)
+    d.nq, d.gq, d.n_pwrk = gq.size, gq.ctypes.data_as(dp), int(n_pwrk)
+    kq = np.zeros((first.size, gq.size, nT, nX), np.float32)
+    kavg = np.zeros((nT, nX, first.size))
+    check(lib.dnsmc_ck_from_lbl(ctypes.byref(d), _fp(kq), _dp(kavg)))
+    return kq, kavg
+
+
 def solver_rays_per_item(solver: "Solver"):
     """The per-(group, packet) ray table in effect, or None."""
     return solver.rays_per_item()

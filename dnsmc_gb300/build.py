@@ -66,6 +66,8 @@ def build(verbose: bool = False) -> str:
          "-o", os.path.join(bdir, "mc_noalloc.o")],
         [nvcc, *ARCH, *common, "-c", os.path.join(CSRC, "mc_cvnet.cu"),
          "-o", os.path.join(bdir, "mc_cvnet.o")],
+        [nvcc, *ARCH, *common, "-fmad=false", "-c", os.path.join(CSRC, "mc_ckgen.cu"),
+         "-o", os.path.join(bdir, "mc_ckgen.o")],
     ]
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(_run, jobs))
@@ -74,7 +76,7 @@ def build(verbose: bool = False) -> str:
     _run([nvcc, *ARCH, "-shared", "-cudart", "static", "-Xcompiler", "-fPIC",
           os.path.join(bdir, "mc_kernels.o"), os.path.join(bdir, "mc_host.o"),
           os.path.join(bdir, "mc_noalloc.o"), os.path.join(bdir, "mc_cvnet.o"), os.path.join(bdir, "mc_march_gen.o"),
-          os.path.join(bdir, "mc_march_pair.o"),
+          os.path.join(bdir, "mc_march_pair.o"), os.path.join(bdir, "mc_ckgen.o"),
           "-o", tmp])
     os.replace(tmp, out)
     if verbose:

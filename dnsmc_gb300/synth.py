@@ -147,3 +147,43 @@ def particle_table(nbands: int = 64, seed: int = 0, diameter: float = 1e-5) -> d
     f = 1.5 / diameter
     return dict(absorption=(f * qext * (1 - alb)).astype(np.float32), scattering=(f * qext * alb).astype(np.float32),
                 albedo=alb, qext=qext, g=0.6)
+
+
+def lbl_spectrum(temperatures, fractions=(0.1,), nbands: int = 6, band_width: float = 25.0,
+                 wv0: float = 1000.0, dwv: float = 0.01, lines_per_band: int = 40, seed: int = 0) -> dict:
+    """Seeded synthetic line-by-line H2O-like absorption spectra (no spectral
+    database is involved): Lorentz lines with log-normal strengths and
+    random positions, line strengths S(T) = S0 (296 / T)^1.5
+    exp(-1.4388 E'' (1/T - 1/296)) and half widths gamma = gamma0 (296 /
+    T)^0.7 (1 + 4 x) per H2O mole fraction x, absorption coefficient
+    k(nu) = 100 x sum S gamma / (pi ((nu - nu0)^2 + gamma^2)) [1/m], on a
+    uniform grid of spacing dwv [1/cm] with `nbands` contiguous bands of
+    `band_width` [1/cm].  Returns kappa [nT][nX][npts] (float64), the grid
+    (wv0, dwv) and the band point ranges and edges."""
+    rng = np.random.default_rng(seed)
+    per = int(round(band_width / dwv))
+    npts = nbands * per + 1
+    nu = wv0 + dwv * np.arange(npts)
+    nl = nbands * lines_per_band
+    pos = wv0 + rng.uniform(0, nbands * band_width, nl)
+    S0 = np.exp(rng.normal(np.log(1e-2), 2.0, nl))
+    E = rng.uniform(0.0, 3000.0, nl)
+    g0 = rng.uniform(0.02, 0.1, nl)
+    T = np.asarray(temperatures, np.float64)
+    X = np.asarray(fractions, np.float64)
+    kappa = np.zeros((T.size, X.size, npts))
+    for a, t in enumerate(T):
+        S = S0 * (296.0 / t) ** 1.5 * np.exp(-1.4388 * E * (1.0 / t - 1.0 / 296.0))
+        for b, x in enumerate(X):
+            gam = g0 * (296.0 / t) ** 0.7 * (1.0 + 4.0 * x)
+            k = np.zeros(npts)
+            for i0 in range(0, nl, 64):
+                sl = slice(i0, i0 + 64)
+                d = nu[None, :] - pos[sl, None]
+                k += (S[sl, None] * gam[sl, None] / (np.pi * (d * d + gam[sl, None] ** 2))).sum(0)
+            kappa[a, b] = 100.0 * x * k + 1e-6
+    first = np.arange(nbands, dtype=np.int64) * per
+    count = np.full(nbands, per + 1, np.int32)
+    wl = wv0 + band_width * np.arange(nbands)
+    return dict(kappa=kappa, wv0=wv0, dwv=dwv, npts=npts, first=first, count=count, wv_left=wl,
+                wv_right=wl + band_width, wvc=wl + 0.5 * band_width, T=T, X=X)

@@ -491,6 +491,40 @@ int  dnsmc_solve_grey_noalloc(const dnsmc_config *cfg, const float *xu,
                               const float *dT, double *dQ, double *dvar,
                               uint32_t *dstatus, void *stream);
 
+/* ---- correlated-k tables from line-by-line spectra -------------------------
+ * The reference's offline table generator (distr/correlatedK.cpp:145-300,
+ * correlatedKT, and the band means of distr/calc_prob.cpp:17-119) on the GPU,
+ * for every temperature, H2O mole fraction and narrow band at once: per band
+ * the k-distribution of the spectrum (n_pwrk bins uniform in k^0.1 between
+ * the band's smallest and largest k, each interval between neighbouring
+ * points at its midpoint k, weighted by its share dwv / (wv_right - wv_left)
+ * of the band), its cumulative g-function, and k at the quadrature points gq
+ * by linear interpolation in g.  The spectra are uniform in wavenumber
+ * (spacing dwv, as the reference's 0.01 1/cm); band b holds the points
+ * [first[b], first[b] + count[b]).  The output k has the layout of
+ * dnsmc_table_desc.k ([nbands][nq][nT][nX]), so it feeds dnsmc_set_table
+ * (with the band centres, widths and the quadrature weights) directly.    */
+typedef struct dnsmc_lbl_desc {
+    int nT, nX;                  /* spectra: temperatures x mole fractions       */
+    long long npts;              /* points of every spectrum                     */
+    double wv0, dwv;             /* wavenumber of point 0 and spacing [1/cm]     */
+    const double *kappa;         /* [nT][nX][npts] absorption coefficient [1/m]  */
+    int nbands;
+    const long long *first;      /* [nbands] first point of each band            */
+    const int *count;            /* [nbands] points of each band (>= 2)          */
+    const double *wv_left;       /* [nbands] band edges [1/cm]                   */
+    const double *wv_right;
+    int nq;
+    const double *gq;            /* [nq] quadrature points, ascending in (0, 1)  */
+    int n_pwrk;                  /* bins of the k-distribution, 2 .. 50000       */
+                                 /* (the reference's 10000)                     */
+} dnsmc_lbl_desc;
+/* kq: [nbands][nq][nT][nX] floats out; kavg: [nT][nX][nbands] band-mean k out
+ * (calc_prob.cpp's k_avg), or NULL.  A band whose k is constant gets that k
+ * at every g (the reference divides by a zero bin width there).  Blocking;
+ * allocates and frees its own device buffers.                                */
+int  dnsmc_ck_from_lbl(const dnsmc_lbl_desc *d, float *kq, double *kavg);
+
 /* ---- reference drop-in (code/mc_gpu.cu:440, :640) -------------------------- */
 /* Tfort: real(4) TMC(0:imax+1,0:jmax+1,0:kmax+1), i fastest, whole domain with
  * ghost layers.  *ystart: 1-based global j of this rank's slab (xstart(2)).

@@ -9,7 +9,10 @@
   code/read_tables.cpp and code/spline.cpp compiled from where they lie under
   the reference tree with oracle/ref_shim/param.h standing in for the
   reference's compile-time code/param.h (-I- keeps the reference's own param.h
-  out of the search path).  Only built when the reference tree is present
+  out of the search path);
+* oracle/_ref/libref_ckgen.so  <- the reference's distr/correlatedK.cpp (its
+  k-distribution routine correlatedKT) around oracle/ref_ckgen.cpp.
+  The reference builds are only made when the reference tree is present
   (at $DNSMC_REFERENCE, default /root/reference).
 """
 from __future__ import annotations
@@ -53,13 +56,22 @@ def _ref_cmd(kind: str) -> list[str]:
             "-o", ref_lib_path(kind)]
 
 
+def _ref_ckgen_cmd() -> list[str]:
+    # the reference's k-distribution generator (distr/correlatedK.cpp) with
+    # its compile-time sizes (distr/classes.h), around a C entry point
+    distr = os.path.join(REF_ROOT, "distr")
+    return ["g++", "-O2", "-fPIC", "-shared", "-w", "-include", "cstdio", "-include", "cstdlib", "-I", distr,
+            os.path.join(HERE, "ref_ckgen.cpp"), os.path.join(distr, "correlatedK.cpp"),
+            "-o", ref_lib_path("ckgen")]
+
+
 def build(with_ref: bool | None = None) -> None:
     jobs = [_oracle_cmd()]
     if with_ref is None:
         with_ref = os.path.isdir(REF_CODE)
     if with_ref:
         os.makedirs(REF_DIR, exist_ok=True)
-        jobs += [_ref_cmd("ck"), _ref_cmd("particle")]
+        jobs += [_ref_cmd("ck"), _ref_cmd("particle"), _ref_ckgen_cmd()]
     with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
         list(ex.map(_run, jobs))
 

@@ -1398,6 +1398,77 @@ int orc_cv_mean(const OrcPacketConfig *c, const int *grp_start, const int *sid, 
     return 0;
 }
 
+// Correlated-k distribution of line-by-line spectra (distr/correlatedK.cpp:
+// 145-300, correlatedKT, and k_avg of distr/calc_prob.cpp:17-119): per
+// (spectrum s, band b) the band's smallest and largest k, n_pwrk bins uniform
+// in k^0.1 (pwr = 0.1), the interval between points h-1 and h at its midpoint
+// k in bin MAX(0, (int)((k^0.1 - kmin^0.1) / step + 1)), the spectral
+// fraction of a bin = its interval count x dwv / band width (uniform spectra),
+// g(h) = 1 - sum of the fractions of bins h+1 .. n_pwrk-1, bin values
+// k(h) = (e(h) + e(h+1)) / 2 with e(h) = (kmin^0.1 + h step)^10 (ten-fold
+// products), k at each quadrature point by linear interpolation between the
+// first bins with g(h+1) >= g_q, and the band mean sum_h k(h) fraction(h).
+// kappa [ns][npts]; kq [nbands][nq][ns]; kavg [ns][nbands] or NULL.
+static inline double ck_edge(double p0, double step, int h) {
+    const double x = (double)h * step + p0;
+    const double x2 = x * x;
+    const double x4 = x2 * x2;
+    const double x5 = x4 * x;
+    return x5 * x5;
+}
+
+int orc_ck_from_lbl(const double *kappa, int ns, long long npts, double dwv, int nbands, const long long *first,
+                    const int *count, const double *wv_left, const double *wv_right, int nq, const double *gq,
+                    int n_pwrk, int nthreads, float *kq, double *kavg) {
+    if (!kappa || ns < 1 || nbands < 1 || nq < 1 || n_pwrk < 2) return 1;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+    for (long long it = 0; it < (long long)ns * nbands; ++it) {
+        const int b = (int)(it % nbands);
+        const long long s_ = it / nbands;
+        const double *kv = kappa + s_ * npts + first[b];
+        const int n = count[b];
+        double lo = kv[0], hi = kv[0];
+        for (int h = 1; h < n; ++h) { lo = std::min(lo, kv[h]); hi = std::max(hi, kv[h]); }
+        if (!(hi > lo)) {
+            for (int r = 0; r < nq; ++r) kq[((long long)b * nq + r) * ns + s_] = (float)lo;
+            if (kavg) kavg[s_ * nbands + b] = lo;
+            continue;
+        }
+        const double p0 = std::pow(lo, 0.1), p1 = std::pow(hi, 0.1);
+        const double step = (p1 - p0) / (double)(n_pwrk - 1);
+        std::vector<long long> cnt((size_t)n_pwrk + 2, 0);
+        for (int h = 1; h < n; ++h) {
+            const double ki = (kv[h] + kv[h - 1]) / 2.0;
+            int bin = std::max(0, (int)((std::pow(ki, 0.1) - p0) / step + 1.0));
+            bin = std::min(bin, n_pwrk);
+            cnt[(size_t)bin] += 1;
+        }
+        const double frac = dwv / (wv_right[b] - wv_left[b]);
+        // suffix counts sfx[h] = sum_{bin = h .. n_pwrk-1} cnt, sfx[n_pwrk] = 0
+        std::vector<long long> sfx((size_t)n_pwrk + 1, 0);
+        for (int h = n_pwrk - 1; h >= 1; --h) sfx[(size_t)h] = sfx[(size_t)h + 1] + cnt[(size_t)h];
+        auto g_at = [&](int h) { return 1.0 - (double)sfx[(size_t)h + 1] * frac; };
+        auto k_at = [&](int h) { return 0.5 * (ck_edge(p0, step, h) + ck_edge(p0, step, h + 1)); };
+        int t = 0;
+        for (int r = 0; r < nq; ++r) {
+            while (t < n_pwrk - 2 && !(g_at(t + 1) >= gq[r])) ++t;
+            const double g0 = g_at(t), g1 = g_at(t + 1), k0 = k_at(t), k1 = k_at(t + 1);
+            const double v = (g1 == g0) ? k1 : k0 + (k1 - k0) * (gq[r] - g0) / (g1 - g0);
+            kq[((long long)b * nq + r) * ns + s_] = (float)v;
+        }
+        if (kavg) {
+            double acc = 0.0;
+            for (int h = 1; h < n_pwrk; ++h)
+                if (cnt[(size_t)h]) acc += k_at(h) * ((double)cnt[(size_t)h] * frac);
+            kavg[s_ * nbands + b] = acc;
+        }
+    }
+    return 0;
+}
+
 int orc_packet_trace(const OrcPacketConfig *c, int f, int G, int p, int r, int max_steps, int32_t *rec, int *n,
                      uint32_t rng[4]) {
     if (!c || c->tile_a < 1 || 32 % c->tile_a || c->cpl < 0 || c->cpl > 4) return 1;

@@ -93,6 +93,10 @@ def load():
         lib.orc_cv_mean.argtypes = [ctypes.POINTER(PacketConfig), _i, _i, _d, _d, _d, ctypes.c_int, ctypes.c_int,
                                     _d]
         lib.orc_cv_mean.restype = ctypes.c_int
+        _ll = ctypes.POINTER(ctypes.c_longlong)
+        lib.orc_ck_from_lbl.argtypes = [_d, ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_int, _ll, _i,
+                                        _d, _d, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int, _f, _d]
+        lib.orc_ck_from_lbl.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -471,6 +475,63 @@ def ref_tables_x_slice(table: dict, xbar: float) -> dict:
     kP = np.pi * eb.sum(1) / (SIGMA * Tnb.astype(np.float64) ** 4)
     return dict(Tnb=Tnb, kq=kx.transpose(0, 2, 1).astype(np.float32), wvc=np.asarray(table["wvc"], np.float32),
                 prob=prob.astype(np.float32), probg=probg.astype(np.float32), kP=kP.astype(np.float32))
+
+
+def ck_from_lbl(spec: dict, gq, n_pwrk: int = 10000, threads: int = 0):
+    """The oracle's k-distribution (orc_ck_from_lbl) of a synth.lbl_spectrum
+    dict: kq [nbands][nq][nT][nX] float32 and kavg [nT][nX][nbands]."""
+    k = np.ascontiguousarray(spec["kappa"], np.float64)
+    nT, nX, npts = k.shape
+    ns = nT * nX
+    nb = len(spec["first"])
+    gq = np.ascontiguousarray(gq, np.float64)
+    first = np.ascontiguousarray(spec["first"], np.int64)
+    count = np.ascontiguousarray(spec["count"], np.int32)
+    wl = np.ascontiguousarray(spec["wv_left"], np.float64)
+    wr = np.ascontiguousarray(spec["wv_right"], np.float64)
+    kq = np.zeros((nb, gq.size, ns), np.float32)
+    kavg = np.zeros((ns, nb))
+    rc = load().orc_ck_from_lbl(k.ctypes.data_as(_d), ns, npts, float(spec["dwv"]), nb,
+                                first.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), count.ctypes.data_as(_i),
+                                wl.ctypes.data_as(_d), wr.ctypes.data_as(_d), gq.size, gq.ctypes.data_as(_d),
+                                n_pwrk, threads, kq.ctypes.data_as(_f), kavg.ctypes.data_as(_d))
+    assert rc == 0
+    return kq.reshape(nb, gq.size, nT, nX), kavg.reshape(nT, nX, nb)
+
+
+def ref_ckgen_available() -> bool:
+    return os.path.exists(_build.ref_lib_path("ckgen"))
+
+
+def ref_correlated_kt(spec: dict, workdir: str):
+    """The reference's own correlatedKT (distr/correlatedK.cpp:145-300, built
+    from the reference sources into oracle/_ref) on the spectra of the first
+    mole fraction: its compile-time sizes (nT spectra, nQuad g-points,
+    n_pwrk bins) and gq.  Returns (kq [nT][nbands][nQuad], gq, n_pwrk)."""
+    lib = ctypes.CDLL(_build.ref_lib_path("ckgen"))
+    nt, nq, npw = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    lib.ref_ck_sizes(ctypes.byref(nt), ctypes.byref(nq), ctypes.byref(npw))
+    gq = np.zeros(nq.value)
+    lib.ref_ck_gq(gq.ctypes.data_as(_d))
+    k = np.ascontiguousarray(spec["kappa"][:, 0, :], np.float64)
+    if k.shape[0] != nt.value:
+        raise ValueError(f"the reference routine takes {nt.value} temperatures")
+    npts = k.shape[1]
+    wvn = spec["wv0"] + spec["dwv"] * np.arange(npts)
+    nb = len(spec["first"])
+    first = np.ascontiguousarray(spec["first"], np.int64)
+    count = np.ascontiguousarray(spec["count"], np.int32)
+    wl = np.ascontiguousarray(spec["wv_left"], np.float64)
+    wr = np.ascontiguousarray(spec["wv_right"], np.float64)
+    kq = np.zeros((nt.value, nb, nq.value))
+    _ll = ctypes.POINTER(ctypes.c_longlong)
+    lib.ref_ck_correlatedKT.argtypes = [_d, ctypes.c_longlong, _d, ctypes.c_int, _ll, _i, _d, _d, ctypes.c_char_p,
+                                        _d]
+    rc = lib.ref_ck_correlatedKT(k.ctypes.data_as(_d), npts, wvn.ctypes.data_as(_d), nb, first.ctypes.data_as(_ll),
+                                 count.ctypes.data_as(_i), wl.ctypes.data_as(_d), wr.ctypes.data_as(_d),
+                                 os.fsencode(workdir), kq.ctypes.data_as(_d))
+    assert rc == 0, rc
+    return kq, gq, npw.value
 
 
 def solver_rays(solver) -> int:
