@@ -18,17 +18,14 @@
 // wall-normal position 2 eta - 1, and T and x_H2O at 32 points of the
 // wall-normal line through the cell (layers ((2q+1) nw) / 64), all mapped to
 // [-1, 1] by the table's T and x ranges.  Layers 67 -> 128 -> 128 -> 128 -> 64
-// with GELU (tanh form), BF16 weights and activations, FP32 accumulation
-// (mma.sync m16n8k16 bf16 tensor-core instructions).
-//
-// The forward kernel keeps the activations of a 16-row slab in registers
-// from layer to layer: the fragment layout of an m16n8k16 accumulator (row
-// g, columns 2t, 2t+1 of each n8 tile) is, pairwise packed to bf16, the A
-// fragment of the next layer's k16 step.  Weights sit in shared memory with
-// rows padded by 8 elements so the B-fragment loads are bank-conflict free.
-// Training: a loss kernel writes dL/dout; the backward pass runs bf16 GEMMs
-// (dW = dZ^T H split over the batch with a deterministic reduction, dH = dZ W
-// with the GELU derivative fused) and Adam updates FP32 master weights.
+// with GELU (tanh form), BF16 weights and activations, FP32 accumulation on
+// the fifth-generation tensor cores (tcgen05.mma, accumulators in tensor
+// memory; mc_cvnet_tc.cuh): the forward pass (inference with the features
+// and the coefficient epilogue fused in; training with its saves) and the
+// backward GEMMs.  Training: a loss kernel writes dL/dout; the backward pass
+// runs dW = dZ^T H (split over the batch with a deterministic reduction) and
+// dH = dZ W with the GELU derivative fused, and Adam updates FP32 master
+// weights.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -58,7 +55,6 @@ constexpr int K0 = 80;       // padded input width (multiple of 16)
 constexpr int HID = 128;
 constexpr int NOUT = 64;     // 16 group slots x 4 heads
 constexpr int MAXG = 16;
-constexpr int NT4 = NOUT / 8;  // n8 tiles of the output layer
 constexpr int NPROF = 32;
 constexpr int NLAB = 8;      // labels per (cell, group): Cxx Caa Cbb Cxa Cxb Cab v c
 
@@ -80,10 +76,6 @@ constexpr long long WOFF_3 = WOFF_2 + (long long)HID * HID;
 constexpr long long WOFF_4 = WOFF_3 + (long long)HID * HID;
 constexpr long long NWEIGHT = WOFF_4 + (long long)NOUT * HID;
 
-// shared-memory weight rows padded by 8 bf16
-constexpr int LD1 = K0 + 8, LDH = HID + 8;
-constexpr int SMEM_W = HID * LD1 + 2 * HID * LDH + NOUT * LDH;  // bf16 elements
-constexpr int SMEM_FWD = SMEM_W * 2 + (3 * HID + NOUT) * 4;
 
 #define CK(x)                                                                        \
     do {                                                                             \
@@ -121,15 +113,6 @@ __device__ __forceinline__ float gelu_grad(float z) {
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
     __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<uint32_t *>(&v);
-}
-
-// D = A(16x16, row) * B(16x8, col) + D, bf16 inputs, fp32 accumulation.
-__device__ __forceinline__ void mma16816(float d[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
 // ---------------------------------------------------------------------------
@@ -203,151 +186,6 @@ __global__ void features_kernel(const FeatParams P) {
     }
 }
 
-// ---------------------------------------------------------------------------
-// Fused forward: 16 rows per warp, activations in registers.
-// ---------------------------------------------------------------------------
-struct FwdParams {
-    long long rows;           // rows to evaluate
-    const bf16 *X;            // [*][K0] feature rows
-    const int *idx;           // row r reads X[idx[r]] (null: X[r])
-    long long nvalid;         // rows >= nvalid read zero features (padding)
-    const bf16 *W;            // bf16 weights
-    const float *P;           // fp32 master (biases)
-    float *out;               // [rows][NOUT]
-    // training saves (all null at inference)
-    bf16 *H0;                 // [rows][K0] gathered features
-    float *Z1, *Z2, *Z3;      // [rows][HID] pre-activations
-    bf16 *H1, *H2, *H3;       // [rows][HID] activations
-};
-
-template <int NT, int KB>
-__device__ __forceinline__ void layer_mma(float (&acc)[NT][4], const uint32_t (&a)[KB][4], const bf16 *Ws, int ld,
-                                          int g, int t) {
-#pragma unroll
-    for (int n = 0; n < NT; ++n) acc[n][0] = acc[n][1] = acc[n][2] = acc[n][3] = 0.0f;
-#pragma unroll
-    for (int kb = 0; kb < KB; ++kb) {
-#pragma unroll
-        for (int n = 0; n < NT; ++n) {
-            const bf16 *w = Ws + (n * 8 + g) * ld + kb * 16 + 2 * t;
-            const uint32_t b0 = *reinterpret_cast<const uint32_t *>(w);
-            const uint32_t b1 = *reinterpret_cast<const uint32_t *>(w + 8);
-            mma16816(acc[n], a[kb], b0, b1);
-        }
-    }
-}
-
-// bias + GELU on a 16 x 128 accumulator slab, optional saves, repack as the
-// A fragments of the next layer.
-__device__ __forceinline__ void hidden_epilogue(float (&acc)[16][4], uint32_t (&a)[8][4], const float *bias,
-                                                long long r0, long long rows, int g, int t, float *Z, bf16 *Hs) {
-#pragma unroll
-    for (int n = 0; n < 16; ++n) {
-        const int col = n * 8 + 2 * t;
-        const float b0 = bias[col], b1 = bias[col + 1];
-        const float z0 = acc[n][0] + b0, z1 = acc[n][1] + b1, z2 = acc[n][2] + b0, z3 = acc[n][3] + b1;
-        const uint32_t lo = pack_bf16(gelu(z0), gelu(z1));
-        const uint32_t hi = pack_bf16(gelu(z2), gelu(z3));
-        if (Z) {
-            const long long ra = r0 + g, rb = r0 + g + 8;
-            if (ra < rows) {
-                *reinterpret_cast<float2 *>(Z + ra * HID + col) = make_float2(z0, z1);
-                *reinterpret_cast<uint32_t *>(Hs + ra * HID + col) = lo;
-            }
-            if (rb < rows) {
-                *reinterpret_cast<float2 *>(Z + rb * HID + col) = make_float2(z2, z3);
-                *reinterpret_cast<uint32_t *>(Hs + rb * HID + col) = hi;
-            }
-        }
-        // n even -> k columns 16*(n/2) + 2t (regs 0, 1); n odd -> + 8 (regs 2, 3)
-        a[n >> 1][(n & 1) * 2 + 0] = lo;
-        a[n >> 1][(n & 1) * 2 + 1] = hi;
-    }
-}
-
-__global__ void __launch_bounds__(256) mlp_forward_kernel(const FwdParams F) {
-    extern __shared__ __align__(16) unsigned char smem[];
-    bf16 *W1s = reinterpret_cast<bf16 *>(smem);
-    bf16 *W2s = W1s + HID * LD1;
-    bf16 *W3s = W2s + HID * LDH;
-    bf16 *W4s = W3s + HID * LDH;
-    float *bs = reinterpret_cast<float *>(W4s + NOUT * LDH);
-    // stage weights (row-padded) and biases
-    for (int e = threadIdx.x; e < HID * K0; e += blockDim.x) W1s[(e / K0) * LD1 + e % K0] = F.W[WOFF_1 + e];
-    for (int e = threadIdx.x; e < HID * HID; e += blockDim.x) {
-        W2s[(e / HID) * LDH + e % HID] = F.W[WOFF_2 + e];
-        W3s[(e / HID) * LDH + e % HID] = F.W[WOFF_3 + e];
-    }
-    for (int e = threadIdx.x; e < NOUT * HID; e += blockDim.x) W4s[(e / HID) * LDH + e % HID] = F.W[WOFF_4 + e];
-    for (int e = threadIdx.x; e < HID; e += blockDim.x) {
-        bs[e] = F.P[OFF_B1 + e];
-        bs[HID + e] = F.P[OFF_B2 + e];
-        bs[2 * HID + e] = F.P[OFF_B3 + e];
-    }
-    for (int e = threadIdx.x; e < NOUT; e += blockDim.x) bs[3 * HID + e] = F.P[OFF_B4 + e];
-    __syncthreads();
-
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    const long long nslab = (F.rows + 15) / 16;
-    for (long long slab = (long long)blockIdx.x * nwarps + warp; slab < nslab; slab += (long long)gridDim.x * nwarps) {
-        const long long r0 = slab * 16;
-        // layer 1 A fragments straight from the feature rows
-        uint32_t a1[K0 / 16][4];
-        {
-            const long long ra = r0 + g, rb = r0 + g + 8;
-            const bool va = ra < F.rows && ra < F.nvalid, vb = rb < F.rows && rb < F.nvalid;
-            const long long sa = va ? (F.idx ? (long long)F.idx[ra] : ra) : 0;
-            const long long sb = vb ? (F.idx ? (long long)F.idx[rb] : rb) : 0;
-            const uint32_t *xa = reinterpret_cast<const uint32_t *>(F.X + sa * K0);
-            const uint32_t *xb = reinterpret_cast<const uint32_t *>(F.X + sb * K0);
-#pragma unroll
-            for (int kb = 0; kb < K0 / 16; ++kb) {
-                a1[kb][0] = va ? xa[kb * 8 + t] : 0u;
-                a1[kb][1] = vb ? xb[kb * 8 + t] : 0u;
-                a1[kb][2] = va ? xa[kb * 8 + 4 + t] : 0u;
-                a1[kb][3] = vb ? xb[kb * 8 + 4 + t] : 0u;
-                if (F.H0) {
-                    if (ra < F.rows) {
-                        uint32_t *h = reinterpret_cast<uint32_t *>(F.H0 + ra * K0);
-                        h[kb * 8 + t] = a1[kb][0];
-                        h[kb * 8 + 4 + t] = a1[kb][2];
-                    }
-                    if (rb < F.rows) {
-                        uint32_t *h = reinterpret_cast<uint32_t *>(F.H0 + rb * K0);
-                        h[kb * 8 + t] = a1[kb][1];
-                        h[kb * 8 + 4 + t] = a1[kb][3];
-                    }
-                }
-            }
-        }
-        float acc[16][4];
-        uint32_t a[8][4];
-        layer_mma<16, K0 / 16>(acc, a1, W1s, LD1, g, t);
-        hidden_epilogue(acc, a, bs, r0, F.rows, g, t, F.Z1, F.H1);
-        layer_mma<16, 8>(acc, a, W2s, LDH, g, t);
-        hidden_epilogue(acc, a, bs + HID, r0, F.rows, g, t, F.Z2, F.H2);
-        layer_mma<16, 8>(acc, a, W3s, LDH, g, t);
-        hidden_epilogue(acc, a, bs + 2 * HID, r0, F.rows, g, t, F.Z3, F.H3);
-        float o[NT4][4];
-        layer_mma<NT4, 8>(o, a, W4s, LDH, g, t);
-#pragma unroll
-        for (int n = 0; n < NT4; ++n) {
-            const int col = n * 8 + 2 * t;
-            const float b0 = bs[3 * HID + col], b1 = bs[3 * HID + col + 1];
-            const long long ra = r0 + g, rb = r0 + g + 8;
-            if (ra < F.rows) *reinterpret_cast<float2 *>(F.out + ra * NOUT + col) = make_float2(o[n][0] + b0, o[n][1] + b1);
-            if (rb < F.rows) *reinterpret_cast<float2 *>(F.out + rb * NOUT + col) = make_float2(o[n][2] + b0, o[n][3] + b1);
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Generic bf16 GEMM for the backward pass: C(MxN) = A(MxK) B(KxN), operands
-// with arbitrary element strides, 64x64x32 tiles, 4 warps of 32x32, split-K
-// over blockIdx.z into fp32 partials [z][M][N]; or, with Z set, the fused
-// epilogue D = bf16(C * gelu'(Z)) (single split).
-// ---------------------------------------------------------------------------
 struct GemmParams {
     int M, N, K, klen;        // klen: K range per split
     const bf16 *A;
@@ -358,73 +196,6 @@ struct GemmParams {
     const float *Z;           // [M][N] pre-activation for the fused GELU' epilogue
     bf16 *D;                  // [M][N]
 };
-
-constexpr int GBM = 64, GBN = 64, GBK = 32, GLD = GBK + 8;
-
-__global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmParams G) {
-    __shared__ __align__(16) bf16 As[GBM * GLD];
-    __shared__ __align__(16) bf16 Bs[GBN * GLD];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int g = lane >> 2, t = lane & 3;
-    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-    const int m0 = blockIdx.x * GBM, n0 = blockIdx.y * GBN;
-    const int kbeg = blockIdx.z * G.klen, kend = min(G.K, kbeg + G.klen);
-    const bf16 zero = __float2bfloat16(0.0f);
-    float acc[2][4][4];
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = acc[i][j][2] = acc[i][j][3] = 0.0f;
-    for (int k0 = kbeg; k0 < kend; k0 += GBK) {
-        for (int e = tid; e < GBM * GBK; e += 128) {
-            int m, k;
-            if (G.a_sk == 1) { m = e / GBK; k = e % GBK; } else { k = e / GBM; m = e % GBM; }
-            const int gm = m0 + m, gk = k0 + k;
-            As[m * GLD + k] = (gm < G.M && gk < kend) ? G.A[gm * G.a_sm + gk * G.a_sk] : zero;
-        }
-        for (int e = tid; e < GBN * GBK; e += 128) {
-            int n, k;
-            if (G.b_sk == 1) { n = e / GBK; k = e % GBK; } else { k = e / GBN; n = e % GBN; }
-            const int gn = n0 + n, gk = k0 + k;
-            Bs[n * GLD + k] = (gn < G.N && gk < kend) ? G.B[gk * G.b_sk + gn * G.b_sn] : zero;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < GBK; kk += 16) {
-            uint32_t af[2][4];
-#pragma unroll
-            for (int i = 0; i < 2; ++i) {
-                const bf16 *p = As + (wm + i * 16 + g) * GLD + kk + 2 * t;
-                af[i][0] = *reinterpret_cast<const uint32_t *>(p);
-                af[i][1] = *reinterpret_cast<const uint32_t *>(p + 8 * GLD);
-                af[i][2] = *reinterpret_cast<const uint32_t *>(p + 8);
-                af[i][3] = *reinterpret_cast<const uint32_t *>(p + 8 * GLD + 8);
-            }
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const bf16 *p = Bs + (wn + j * 8 + g) * GLD + kk + 2 * t;
-                const uint32_t b0 = *reinterpret_cast<const uint32_t *>(p);
-                const uint32_t b1 = *reinterpret_cast<const uint32_t *>(p + 8);
-#pragma unroll
-                for (int i = 0; i < 2; ++i) mma16816(acc[i][j], af[i], b0, b1);
-            }
-        }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int i = 0; i < 2; ++i)
-#pragma unroll
-        for (int j = 0; j < 4; ++j)
-#pragma unroll
-            for (int h = 0; h < 4; ++h) {
-                const int m = m0 + wm + i * 16 + g + (h >> 1) * 8;
-                const int n = n0 + wn + j * 8 + 2 * t + (h & 1);
-                if (m >= G.M || n >= G.N) continue;
-                const long long o = (long long)m * G.N + n;
-                if (G.D) G.D[o] = __float2bfloat16(acc[i][j][h] * gelu_grad(G.Z[o]));
-                else G.C[(long long)blockIdx.z * G.M * G.N + o] = acc[i][j][h];
-            }
-}
 
 // grad[off + e] = sum over splits of partials (fixed order)
 __global__ void reduce_splits_kernel(const float *part, int splits, long long n, float *grad) {
@@ -777,28 +548,6 @@ int set_dev(dnsmc_cvnet *n) {
     return DNSMC_OK;
 }
 
-int fwd_smem_ok() {
-    static int done = 0;
-    if (!done) {
-        CK(cudaFuncSetAttribute(mlp_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_FWD));
-        done = 1;
-    }
-    return DNSMC_OK;
-}
-
-int launch_forward(const FwdParams &F, cudaStream_t st) {
-    RTRY(fwd_smem_ok());
-    const long long slabs = (F.rows + 15) / 16;
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const int blocks = (int)std::max(1LL, std::min((slabs + 7) / 8, 2LL * sms));
-    dnsmc::note_launch();
-    mlp_forward_kernel<<<blocks, 256, SMEM_FWD, st>>>(F);
-    CK(cudaGetLastError());
-    return DNSMC_OK;
-}
-
 // The tcgen05 forward (mc_cvnet_tc.cuh): one CTA per SM, persistent.
 int launch_forward_tc(TcParams &F, dnsmc_cvnet *n, cudaStream_t st) {
     static int attr = 0;
@@ -832,20 +581,29 @@ int ensure_work(dnsmc_cvnet *n, long long rows) {
 }
 
 // dW (M=nout x N=nin) = dZ^T H over rows, split over the rows; db = colsum(dZ)
+int launch_gemm_tc(const GemmParams &G, dim3 grid, dnsmc_cvnet *n) {
+    static int attr = 0;
+    if (!attr) {
+        CK(cudaFuncSetAttribute(gemm_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, GT_SMEM));
+        attr = 1;
+    }
+    dnsmc::note_launch();
+    gemm_tc_kernel<<<grid, 128, GT_SMEM, n->stream>>>(G, n->status.p);
+    CK(cudaGetLastError());
+    return DNSMC_OK;
+}
+
 int weight_grad(dnsmc_cvnet *n, const bf16 *dZ, int nout, const bf16 *H, int nin, long long rows, long long offW,
                 long long offB) {
     const int splits = (int)std::min<long long>(64, std::max<long long>(1, rows / 256));
-    const int klen = (int)(((rows + splits - 1) / splits + GBK - 1) / GBK * GBK);
+    const int klen = (int)(((rows + splits - 1) / splits + GT_K - 1) / GT_K * GT_K);
     RTRY(n->part.ensure((size_t)splits * nout * nin));
     GemmParams G{};
     G.M = nout; G.N = nin; G.K = (int)rows; G.klen = klen;
     G.A = dZ; G.a_sm = 1; G.a_sk = nout;
     G.B = H; G.b_sk = nin; G.b_sn = 1;
     G.C = n->part.p;
-    dim3 grid((nout + GBM - 1) / GBM, (nin + GBN - 1) / GBN, splits);
-    dnsmc::note_launch();
-    gemm_bf16_kernel<<<grid, 128, 0, n->stream>>>(G);
-    CK(cudaGetLastError());
+    RTRY(launch_gemm_tc(G, dim3((nout + 127) / 128, (nin + 127) / 128, splits), n));
     dnsmc::note_launch();
     reduce_splits_kernel<<<grid1((long long)nout * nin, 256), 256, 0, n->stream>>>(n->part.p, splits,
                                                                                    (long long)nout * nin,
@@ -865,21 +623,17 @@ int input_grad(dnsmc_cvnet *n, const bf16 *dZ, int nout, long long woff, int nin
     G.A = dZ; G.a_sm = nout; G.a_sk = 1;
     G.B = n->W.p + woff; G.b_sk = nin; G.b_sn = 1;
     G.Z = Zprev; G.D = dZprev;
-    dim3 grid((unsigned)((rows + GBM - 1) / GBM), (nin + GBN - 1) / GBN, 1);
-    dnsmc::note_launch();
-    gemm_bf16_kernel<<<grid, 128, 0, n->stream>>>(G);
-    CK(cudaGetLastError());
-    return DNSMC_OK;
+    return launch_gemm_tc(G, dim3((unsigned)((rows + 127) / 128), (nin + 127) / 128, 1), n);
 }
 
 // forward + loss + backward on `rows` rows (nvalid real) of X/lab through idx
 int fwd_bwd(dnsmc_cvnet *n, const bf16 *X, const float *lab, int G, const int *idx, long long rows, long long nvalid,
             double loss[3]) {
     RTRY(ensure_work(n, rows));
-    FwdParams F{};
-    F.rows = rows; F.X = X; F.idx = idx; F.nvalid = nvalid; F.W = n->W.p; F.P = n->P.p; F.out = n->out.p;
+    TcParams F{};
+    F.rows = rows; F.X = X; F.idx = idx; F.nvalid = nvalid; F.out = n->out.p;
     F.H0 = n->H0.p; F.Z1 = n->Z1.p; F.Z2 = n->Z2.p; F.Z3 = n->Z3.p; F.H1 = n->H1.p; F.H2 = n->H2.p; F.H3 = n->H3.p;
-    RTRY(launch_forward(F, n->stream));
+    RTRY(launch_forward_tc(F, n, n->stream));
     LossParams L{};
     L.rows = rows; L.nvalid = nvalid; L.G = G; L.out = n->out.p; L.lab = lab; L.idx = idx;
     L.Sbeta = n->Sbeta; L.Sv = n->Sv; L.Sc = n->Sc; L.ridge = n->cfg.ridge; L.dout = n->dO.p;
@@ -1236,7 +990,7 @@ int dnsmc_cvnet_eval(dnsmc_cvnet *n, const float *features, long long rows, floa
     RTRY(n->iout.ensure((size_t)rows * NOUT));
     CK(cudaMemcpyAsync(n->iX.p, h.data(), h.size() * sizeof(bf16), cudaMemcpyHostToDevice, n->stream));
     TcParams F{};
-    F.rows = rows; F.X = n->iX.p; F.out = n->iout.p;
+    F.rows = rows; F.X = n->iX.p; F.nvalid = rows; F.out = n->iout.p;
     RTRY(launch_forward_tc(F, n, n->stream));
     CK(cudaMemcpyAsync(out, n->iout.p, (size_t)rows * NOUT * sizeof(float), cudaMemcpyDeviceToHost, n->stream));
     unsigned int st = 0;

@@ -1,6 +1,7 @@
-// mc_cvnet_tc.cuh -- the network's forward pass on the fifth-generation
-// tensor cores (tcgen05) with the accumulators in tensor memory.  Included by
-// mc_cvnet.cu (it uses that file's constants, GELU and feature row).
+// mc_cvnet_tc.cuh -- the network's forward pass and the backward pass's
+// GEMMs on the fifth-generation tensor cores (tcgen05) with the accumulators
+// in tensor memory.  Included by mc_cvnet.cu (it uses that file's constants,
+// GELU and feature row).  The forward pass:
 //
 // One CTA per SM, persistent over 128-row tiles; TC_WG warpgroups per CTA,
 // each with its own tile in flight so that one warpgroup's epilogue (bias,
@@ -127,7 +128,14 @@ struct TcParams {
     long long rows;
     int fused_features;       // 1: features of the solver's region (feat); 0: bf16 rows of X
     FeatParams feat;
-    const bf16 *X;            // [rows][K0]
+    const bf16 *X;            // [*][K0] feature rows
+    const int *idx;           // row r reads X[idx[r]] (null: X[r]); rows >= nvalid read zeros
+    long long nvalid;
+    // training saves (all null at inference): the layer-1 input rows, the
+    // pre-activations Z and the bf16 activations H of the hidden layers
+    bf16 *H0;                 // [rows][K0]
+    float *Z1, *Z2, *Z3;      // [rows][HID]
+    bf16 *H1, *H2, *H3;       // [rows][HID]
     const bf16 *Wtc;          // the four weight matrices in tensor-core order
     const float *P;           // FP32 master parameters (biases)
     float *out;               // [rows][NOUT] (fused_apply 0)
@@ -151,23 +159,32 @@ __device__ __forceinline__ void tc_layer(uint32_t a_addr, uint32_t b_addr, uint3
 }
 
 // Hidden-layer epilogue: the 128 accumulator columns of this thread's row,
-// bias and GELU, packed to bf16 into the A tile (this row's 16-byte chunks).
-__device__ __forceinline__ void tc_hidden(uint32_t tlane, const float *bias, unsigned char *act, int lt) {
+// bias and GELU, packed to bf16 into the A tile (this row's 16-byte chunks);
+// in training also the row's pre-activations (Zs) and activations (Hs).
+__device__ __forceinline__ void tc_hidden(uint32_t tlane, const float *bias, unsigned char *act, int lt, float *Zs,
+                                          bf16 *Hs) {
 #pragma unroll
     for (int c = 0; c < HID / 32; ++c) {
         uint32_t v[32];
         tc_ld32(tlane + c * 32, v);
         uint32_t h[16];
+        float z[32];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-            const float z0 = __uint_as_float(v[2 * q]) + bias[c * 32 + 2 * q];
-            const float z1 = __uint_as_float(v[2 * q + 1]) + bias[c * 32 + 2 * q + 1];
-            h[q] = pack_bf16(gelu(z0), gelu(z1));
-        }
+        for (int q = 0; q < 32; ++q) z[q] = __uint_as_float(v[q]) + bias[c * 32 + q];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) h[q] = pack_bf16(gelu(z[2 * q]), gelu(z[2 * q + 1]));
 #pragma unroll
         for (int m = 0; m < 4; ++m)
             *reinterpret_cast<uint4 *>(act + (c * 4 + m) * (TC_TILE * 16) + lt * 16) =
                 make_uint4(h[4 * m], h[4 * m + 1], h[4 * m + 2], h[4 * m + 3]);
+        if (Zs) {
+            float4 *zd = reinterpret_cast<float4 *>(Zs + c * 32);
+#pragma unroll
+            for (int m = 0; m < 8; ++m) zd[m] = make_float4(z[4 * m], z[4 * m + 1], z[4 * m + 2], z[4 * m + 3]);
+            uint4 *hd = reinterpret_cast<uint4 *>(Hs + c * 32);
+#pragma unroll
+            for (int m = 0; m < 4; ++m) hd[m] = make_uint4(h[4 * m], h[4 * m + 1], h[4 * m + 2], h[4 * m + 3]);
+        }
     }
 }
 
@@ -228,8 +245,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const TcParams F)
             for (int q = 0; q < K0 / 2; ++q) x[q] = 0u;
         } else if (F.fused_features) {
             feature_row(F.feat, r, x);
+        } else if (r >= F.nvalid) {
+#pragma unroll
+            for (int q = 0; q < K0 / 2; ++q) x[q] = 0u;
         } else {
-            const uint4 *src = reinterpret_cast<const uint4 *>(F.X + r * K0);
+            const long long sr = F.idx ? (long long)F.idx[r] : r;
+            const uint4 *src = reinterpret_cast<const uint4 *>(F.X + sr * K0);
 #pragma unroll
             for (int c = 0; c < K0 / 8; ++c) {
                 const uint4 u = src[c];
@@ -240,6 +261,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const TcParams F)
         for (int c = 0; c < K0 / 8; ++c)
             *reinterpret_cast<uint4 *>(act + c * (TC_TILE * 16) + lt * 16) =
                 make_uint4(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3]);
+        if (F.H0 && valid) {
+            uint4 *hd = reinterpret_cast<uint4 *>(F.H0 + r * K0);
+#pragma unroll
+            for (int c = 0; c < K0 / 8; ++c) hd[c] = make_uint4(x[4 * c], x[4 * c + 1], x[4 * c + 2], x[4 * c + 3]);
+        }
         // ---- four layers
 #pragma unroll 1
         for (int layer = 0; layer < 4; ++layer) {
@@ -257,7 +283,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const TcParams F)
             ph ^= 1u;
             tc_fence_after();
             if (layer < 3) {
-                tc_hidden(tlane, bias + layer * HID, act, lt);
+                float *Zs = layer == 0 ? F.Z1 : (layer == 1 ? F.Z2 : F.Z3);
+                bf16 *Hs = layer == 0 ? F.H1 : (layer == 1 ? F.H2 : F.H3);
+                const bool save = Zs && valid;
+                tc_hidden(tlane, bias + layer * HID, act, lt, save ? Zs + r * HID : nullptr,
+                          save ? Hs + r * HID : nullptr);
                 continue;
             }
             // ---- output layer: 64 values of this row
@@ -302,4 +332,113 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const TcParams F)
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Training GEMMs on tcgen05: C (M x N) = A (M x K) B (K x N) over the CTA's K
+// range (blockIdx.z x klen), A(m, k) = A[m a_sm + k a_sk], B(k, n) =
+// B[k b_sk + n b_sn], bf16 operands, f32 accumulator in tensor memory.  One
+// CTA (one warpgroup) per 128 x Nt tile (Nt <= 128, a multiple of 16; rows of
+// A beyond M read zeros); K in stages of 64 staged by plain loads into the
+// descriptors' K-major layout; one elected thread issues the four MMAs of a
+// stage and commits, the warpgroup waits (bounded) before the next stage.
+// Epilogue (thread t = row t): f32 partials C[split][M][N], or D = bf16(acc x
+// GELU'(Z)) (the input gradient of the previous layer).
+// ---------------------------------------------------------------------------
+constexpr int GT_K = 64;
+constexpr int GT_SMEM = 64 * 1024;  // two 16 KB operand tiles; the size keeps at most 3 CTAs (384 TMEM columns) per SM
+
+__global__ void __launch_bounds__(128) gemm_tc_kernel(const GemmParams G, unsigned int *status) {
+    extern __shared__ __align__(1024) unsigned char gsm[];
+    unsigned char *sA = gsm, *sB = gsm + 128 * GT_K * 2;
+    __shared__ uint64_t bar;
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.x * 128, n0 = blockIdx.y * 128;
+    const int nt = min(128, G.N - n0);
+    const int ntp = (nt + 15) & ~15;
+    const int kbeg = blockIdx.z * G.klen, kend = min(G.K, kbeg + G.klen);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(tc_smem(&tslot))
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tslot;
+    const uint32_t tlane = tmem + ((uint32_t)(warp * 32) << 16);
+    const uint32_t aA = tc_smem(sA), aB = tc_smem(sB);
+    const bf16 zero = __float2bfloat16(0.0f);
+    uint32_t ph = 0;
+    unsigned int err = 0;
+    for (int k0 = kbeg; k0 < kend; k0 += GT_K) {
+        // A: 128 rows x 8 chunks of 8 along K
+        for (int it = tid; it < 128 * (GT_K / 8); it += 128) {
+            const int m = it & 127, c = it >> 7;
+            const int gm = m0 + m, gk = k0 + 8 * c;
+            __align__(16) bf16 v[8];
+            if (gm < G.M && G.a_sk == 1 && gk + 8 <= kend) {
+                *reinterpret_cast<uint4 *>(v) = *reinterpret_cast<const uint4 *>(G.A + (long long)gm * G.a_sm + gk);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 8; ++e)
+                    v[e] = (gm < G.M && gk + e < kend) ? G.A[(long long)gm * G.a_sm + (long long)(gk + e) * G.a_sk] : zero;
+            }
+            *reinterpret_cast<uint4 *>(sA + c * (128 * 16) + m * 16) = *reinterpret_cast<const uint4 *>(v);
+        }
+        // B: ntp rows (n) x 8 chunks of 8 along K
+        for (int it = tid; it < ntp * (GT_K / 8); it += 128) {
+            const int n = it % ntp, c = it / ntp;
+            const int gn = n0 + n, gk = k0 + 8 * c;
+            __align__(16) bf16 v[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e)
+                v[e] = (n < nt && gk + e < kend) ? G.B[(long long)(gk + e) * G.b_sk + (long long)gn * G.b_sn] : zero;
+            *reinterpret_cast<uint4 *>(sB + c * (ntp * 16) + n * 16) = *reinterpret_cast<const uint4 *>(v);
+        }
+        tc_proxy_fence();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int k = 0; k < GT_K / 16; ++k) {
+                const uint64_t da = tc_desc(aA + k * 2 * (128 * 16), 128 * 16, 128);
+                const uint64_t db = tc_desc(aB + k * 2 * (ntp * 16), ntp * 16, 128);
+                tc_mma(tmem, da, db, tc_idesc(128, ntp), (k0 > kbeg || k > 0) ? 1u : 0u);
+            }
+            tc_commit(&bar);
+        }
+        if (!tc_wait(&bar, ph)) err |= DNSMC_STATUS_COPY_TIMEOUT;
+        ph ^= 1u;
+        tc_fence_after();
+    }
+    const int gm = m0 + tid;
+    const bool any = kend > kbeg;
+    for (int c = 0; c < (ntp + 31) / 32; ++c) {
+        uint32_t v[32];
+        tc_ld32(tlane + c * 32, v);
+        if (gm >= G.M) continue;
+#pragma unroll
+        for (int q = 0; q < 32; ++q) {
+            const int n = c * 32 + q;
+            if (n >= nt) break;
+            const float a = any ? __uint_as_float(v[q]) : 0.0f;
+            const long long o = (long long)gm * G.N + n0 + n;
+            if (G.D) G.D[o] = __float2bfloat16(a * gelu_grad(G.Z[o]));
+            else G.C[(long long)blockIdx.z * G.M * G.N + o] = a;
+        }
+    }
+    if (err && status) atomicOr(status, err);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem) : "memory");
+    }
+}
 }  // namespace
