@@ -24,6 +24,7 @@ RESULT_F64, RESULT_F32 = 0, 1
 MODEL_CK, MODEL_GREY_BANDS, MODEL_PARTICLE, MODEL_GREY, MODEL_TABLE = 0, 1, 2, 3, 4
 LAYOUT_DENSE, LAYOUT_FORTRAN = 0, 1
 SAMPLER_IID, SAMPLER_RQMC = 0, 1
+CV_BINS = 64  # DNSMC_CV_BINS: bins per hemisphere of the control variate's surrogate table
 
 
 class Config(ctypes.Structure):
@@ -150,6 +151,7 @@ SIGNATURES = {
     "dnsmc_prepare_sampling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_float, ctypes.c_float]),
     "dnsmc_set_cv_beta": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
     "dnsmc_get_cv_data": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_float_p, c_float_p, c_double_p, c_double_p]),
+    "dnsmc_get_cv_table": (ctypes.c_int, [ctypes.c_void_p, c_float_p]),
     "dnsmc_get_cv_moments": (ctypes.c_int, [ctypes.c_void_p, c_double_p]),
     "dnsmc_get_geometry": (ctypes.c_int, [ctypes.c_void_p, c_float_p, c_float_p, c_float_p]),
     "dnsmc_trace_ray": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,

@@ -418,6 +418,16 @@ class Solver:
         check(self._lib.dnsmc_get_cv_data(self._h, None, _fp(layer), _fp(sur), _dp(Jhat), _dp(muY)))
         return dict(layer=layer, sur=sur, Jhat=Jhat, muY=muY, n_samples=S)
 
+    def cv_table(self) -> np.ndarray:
+        """The tabulated surrogate of the last CV solve, (nfields, samples,
+        imax, 2, CV_BINS, 4) float32: per plane, hemisphere (west, east) and
+        bin of sqrt|mu| the (J0, dJ, A0, dA) the march interpolates."""
+        ns = ctypes.c_int()
+        check(self._lib.dnsmc_get_cv_data(self._h, ctypes.byref(ns), None, None, None, None))
+        tab = np.zeros((self._nfields, ns.value, self.cfg.imax, 2, _lib.CV_BINS, 4), np.float32)
+        check(self._lib.dnsmc_get_cv_table(self._h, _fp(tab)))
+        return tab
+
     def cv_moments(self):
         """(nfields, n_groups, nk, nj, ni, 9) per-ray moment sums of the last
         solve with cv_moments=1: X, Ya, Yb, X^2, Ya^2, Yb^2, X Ya, X Yb, Ya Yb."""

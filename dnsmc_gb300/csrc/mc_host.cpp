@@ -97,45 +97,6 @@ void gauss_half(int nq, std::vector<float> &gq, std::vector<float> &wq) {
         if (x[i] > 0) { gq.push_back((float)x[i]); wq.push_back((float)w[i]); }
 }
 
-// n-point Gauss-Legendre nodes and weights on [a, b].
-void gauss_legendre(int n, double a, double b, std::vector<double> &x, std::vector<double> &w) {
-    x.assign(n, 0.0);
-    w.assign(n, 0.0);
-    for (int i = 0; i < n; ++i) {
-        double z = cos(kPi * (i + 0.75) / (n + 0.5));
-        double pp = 1.0;
-        for (int it = 0; it < 100; ++it) {
-            double p1 = 1.0, p2 = 0.0;
-            for (int j = 1; j <= n; ++j) {
-                const double p3 = p2;
-                p2 = p1;
-                p1 = ((2.0 * j - 1.0) * z * p2 - (j - 1.0) * p3) / j;
-            }
-            pp = n * (z * p1 - p2) / (z * z - 1.0);
-            const double z1 = z;
-            z = z1 - p1 / pp;
-            if (fabs(z - z1) < 1e-15) break;
-        }
-        x[i] = 0.5 * (b - a) * (-z) + 0.5 * (b + a);
-        w[i] = (b - a) / ((1.0 - z * z) * pp * pp);
-    }
-}
-
-// Quadrature in the wall-normal cosine mu on (0, 1] for the control-variate
-// mean: 16-point Gauss-Legendre on the panels [0, 1e-3], [1e-3, 1e-2],
-// [1e-2, 0.1], [0.1, 1] (the integrand exp(-tau/mu) varies fastest near 0).
-void cv_quadrature(std::vector<double> &mu, std::vector<double> &w) {
-    const double edges[5] = {0.0, 1e-3, 1e-2, 1e-1, 1.0};
-    mu.clear();
-    w.clear();
-    for (int p = 0; p < 4; ++p) {
-        std::vector<double> x, ww;
-        gauss_legendre(16, edges[p], edges[p + 1], x, ww);
-        mu.insert(mu.end(), x.begin(), x.end());
-        w.insert(w.end(), ww.begin(), ww.end());
-    }
-}
-
 struct HostTable {
     int nbands = 0, nq = 0, nT = 0, nX = 1;
     float T0 = 0.f, dT = 1.f, X0 = 0.f, dX = 1.f;
@@ -353,6 +314,7 @@ struct dnsmc_solver {
     DevBuf<double> d_cvnodes;                // node sums of E[Y]
     DevBuf<double> d_kd, d_ibd;              // FP64 copies of the k and Ib tables (node sums)
     DevBuf<float4> d_Jf;
+    DevBuf<float4> d_surtab;                 // tabulated surrogate [f][sample][nw][2][kSurBins]
     DevBuf<float> d_cv_Cf;
     DevBuf<float2> d_beta;
     DevBuf<double> d_moments;
@@ -408,12 +370,6 @@ int ensure_device(dnsmc_solver *s) {
         sobol_directions(dirs);
         const int rc = upload_sobol_dirs(dirs);
         if (rc) return fail(DNSMC_ERR_CUDA, "Sobol' table upload: %s", cudaGetErrorString((cudaError_t)rc));
-    }
-    {
-        std::vector<double> mu, w;
-        cv_quadrature(mu, w);
-        const int rc = upload_quadrature(mu.data(), w.data(), (int)mu.size());
-        if (rc) return fail(DNSMC_ERR_CUDA, "quadrature upload: %s", cudaGetErrorString((cudaError_t)rc));
     }
     if (int rc = s->d_fw.ensure(s->fw.size())) return rc;
     CUDA_TRY(cudaMemcpy(s->d_fw.p, s->fw.data(), s->fw.size() * sizeof(float), cudaMemcpyHostToDevice));
@@ -1033,10 +989,15 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     if (cv) {
         P.n_samples = S;
         P.sur = s->d_sur.p;
+        P.surtab = s->d_surtab.p;
         P.beta = s->beta_set ? s->d_beta.p : nullptr;
     }
     const bool mom = cv && c.cv_moments;
     if (trace) {
+        // a trace reuses the surrogate of the last solve: it must cover the fields
+        const size_t nsur = (size_t)s->nfields * S * c.imax;
+        if (cv && (s->d_sur.n < nsur || s->d_surtab.n < nsur * 2 * kSurBins))
+            return fail(DNSMC_ERR_STATE, "trace with the control variate needs a prior solve of these fields");
         P.trace_f = tf; P.trace_g = tg; P.trace_p = tp; P.trace_r = tr; P.trace_max = tmax_steps;
         P.trace_rec = d_trace_rec; P.trace_n = d_trace_n; P.trace_rng = d_trace_rng;
         P.tally = nullptr;
@@ -1049,11 +1010,12 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     CvParams cp;
     memset(&cp, 0, sizeof cp);
     if (cv) {
-        // E[Y] per (field, group, cell): layer means -> surrogate table ->
-        // 1-D quadrature Jhat -> sum over the group's samples
+        // E[Y] per (field, group, cell): layer means -> layer-mean medium ->
+        // surrogate table and its means Jhat -> sum over the group's samples
         const size_t nsur = (size_t)s->nfields * S * c.imax;
         TRY(s->d_layer.ensure((size_t)s->nfields * c.imax));
         TRY(s->d_sur.ensure(nsur));
+        TRY(s->d_surtab.ensure(nsur * 2 * kSurBins));
         TRY(s->d_Jhat.ensure(nsur));
         TRY(s->d_Jf.ensure(nsur));
         TRY(s->d_muY.ensure((size_t)s->nfields * P.n_groups * P.region_cells));
@@ -1078,6 +1040,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         cp.ktab = s->d_k.p; cp.ibtab = s->d_ib.p; cp.ibw = P.ibw;
         cp.kappa = c.kappa; cp.Tw4[0] = P.Tw4[0]; cp.Tw4[1] = P.Tw4[1];
         cp.n_samples = S; cp.sur = s->d_sur.p; cp.fw = s->d_fw.p; cp.toll = c.toll; cp.dtoll = P.dtoll;
+        cp.surtab = s->d_surtab.p;
         cp.Jhat = s->d_Jhat.p;
         cp.Jf = s->d_Jf.p;
         cp.samp_Cf = s->d_cv_Cf.p;
@@ -1105,6 +1068,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         }
         s->cv_samples = S;
         P.sur = s->d_sur.p;
+        P.surtab = s->d_surtab.p;
         if (mom) {
             TRY(s->d_moments.ensure((size_t)s->nfields * P.n_groups * P.region_cells * 9));
             P.moments = s->d_moments.p;
@@ -1621,7 +1585,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_fw.release(); s->d_k.release(); s->d_ib.release(); s->d_ibw.release();
     s->d_slab.release(); s->d_posT.release(); s->d_posTX.release();
     s->d_cv_grp.release(); s->d_cv_sid.release(); s->d_cv_C.release(); s->d_layer.release();
-    s->d_sur.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_cvnodes.release(); s->d_kd.release(); s->d_ibd.release(); s->d_beta.release(); s->d_moments.release();
+    s->d_sur.release(); s->d_surtab.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_cvnodes.release(); s->d_kd.release(); s->d_ibd.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release();
     s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_rays_rcp.release(); s->d_item_steps.release(); s->d_kP.release();
     s->d_order.release(); s->d_order_hist.release();
@@ -2395,6 +2359,18 @@ int dnsmc_get_cv_moments(dnsmc_solver *s, double *moments) {
     std::vector<double> tl((size_t)(nfg * ni * nj * nk * 9));
     CUDA_TRY(cudaMemcpy(tl.data(), s->d_moments.p, tl.size() * sizeof(double), cudaMemcpyDeviceToHost));
     tally_to_dense(tl.data(), moments, nfg, ni, nj, nk, 9);
+    return DNSMC_OK;
+}
+
+static_assert(kSurBins == DNSMC_CV_BINS, "surrogate bins of the march and of the interface");
+
+int dnsmc_get_cv_table(dnsmc_solver *s, float *tab) {
+    if (!s || !tab) return fail(DNSMC_ERR_ARG, "null argument");
+    if (!s->solved || !s->cfg.control_variate) return fail(DNSMC_ERR_STATE, "no control-variate solve has been run");
+    TRY(wait_done(s, 0));
+    TRY(set_device(s));
+    const size_t n = (size_t)s->nfields * s->cv_samples * s->cfg.imax * 2 * kSurBins;
+    CUDA_TRY(cudaMemcpy(tab, s->d_surtab.p, n * sizeof(float4), cudaMemcpyDeviceToHost));
     return DNSMC_OK;
 }
 

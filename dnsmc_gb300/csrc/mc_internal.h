@@ -36,6 +36,10 @@ constexpr int kSlabWaitPolls = 1 << 16;
 // Cells per lane of the fine-grid march (mc_march_pair.cuh): a packet is
 // 32 * kLaneCells cells; the multigrid march uses 1.
 constexpr int kLaneCells = 2;
+// Bins per hemisphere of the tabulated surrogate of the control variate: the
+// surrogate is stored at the nodes u = m / kSurBins of u = sqrt(|mu|) (mu the
+// wall-normal direction cosine) and read by linear interpolation in u.
+constexpr int kSurBins = 64;
 
 struct MarchParams {
     // geometry: nw wall-normal cells (reference i), na (j) and nb (k) periodic
@@ -113,6 +117,7 @@ struct MarchParams {
     unsigned long long *counters;  // [0] rays (lane-rays), [1] lane-steps
     // control variate: Y = the same ray through the layer-mean medium
     const float2 *sur;        // [f][sample][nw] (k_bar, Ib_bar) per layer
+    const float4 *surtab;     // [f][sample][nw][2][kSurBins] surrogate per bin, see CvParams
     int n_samples;            // bands * nq (1 for the grey model)
     const float2 *beta;       // [f][group][iR][kR][jR] (beta_a, beta_b), or null: (1, -1)
     double *moments;          // [f][group][iR][kR][jR][9] per-ray moments (training solves)
@@ -300,9 +305,14 @@ struct CvParams {
     float2 *sur;              // [f][sample][nw]
     const float *fw;          // nw+1 faces
     float toll, dtoll;
-    int nquad;                // nodes per hemisphere
-    double2 *Jhat;            // [f][sample][nw] (Jhat, Ahat): direction-averaged surrogate
-                              // intensity and own-layer absorptance
+    // [f][sample][nw][h][m]: the surrogate of a ray leaving the centre of
+    // layer l into hemisphere h (0: towards the west wall, 1: east) with
+    // sqrt(|mu|) = (m + r) / kSurBins, r in [0, 1), is
+    //   J = J0 + r dJ (collected intensity), A = A0 + r dA (own-layer absorptance),
+    // stored as (J0, dJ, A0, dA): the straight walk evaluated at the bin's two nodes
+    float4 *surtab;
+    double2 *Jhat;            // [f][sample][nw] (Jhat, Ahat): exact means of J and A over the
+                              // isotropic directions (mu uniform on [-1, 1])
     float4 *Jf;               // [f][sample][nw] (Jhat hi, Jhat lo, Ahat, layer-mean Ib) for the mean
     // mean of Y per (field, group, cell) in tally layout
     int n_groups;
@@ -328,7 +338,6 @@ struct CvParams {
 long long cv_node_count(const CvParams &c);
 int launch_cv_prepare(const CvParams &c, void *stream);
 int launch_cv_mean(const CvParams &c, void *stream);
-int upload_quadrature(const double *mu, const double *w, int n);  // once per device
 int upload_sobol_dirs(const uint32_t dirs[4][32]);  // once per device
 int device_sm_count();
 

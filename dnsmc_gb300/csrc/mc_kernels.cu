@@ -258,26 +258,20 @@ int launch_march(int mode, const MarchParams &p, int blocks, int threads, void *
 
 // ---------------------------------------------------------------------------
 // Control variate preparation.  Y is the ray's contribution in the medium
-// whose temperature and x_H2O are the mean of each wall-normal plane; its
-// expectation per cell is a 1-D layered-slab integral:
-//   E[Y] = sum_s C_s k_i(s) (Ib_i(s) - Jhat_s(layer)),
-//   Jhat_s(l) = 1/2 int_{-1}^{1} J_s(mu; l) dmu,
-// J_s the intensity absorbed along a ray leaving the centre of layer l with
-// wall-normal cosine mu through the layer-mean medium (same toll cut-off,
-// same wall emission).  The march tallies X - beta*Y and finalize adds
-// beta*E[Y] back, so the estimate is unbiased for any beta.
+// whose temperature and x_H2O are the mean of each wall-normal plane, with
+// its flight through that medium replaced by a tabulated function of the
+// ray's layer, spectral sample and wall-normal cosine mu:
+//   J(mu) = the intensity the walk from the layer centre collects (same toll
+//           cut-off, same wall emission as the 3-D march),
+//   A(mu) = 1 - the transmissivity of its path out of the own layer,
+// stored at the nodes u_m = m / kSurBins of u = sqrt(|mu|) per hemisphere and
+// read by linear interpolation in u.  Whatever the table holds, its mean over
+// the isotropic directions is a finite sum over the bins, so E[Y] per cell is
+//   E[Y_a] = sum_s C_s k_i(s) (Ib_i(s) - Jhat_s(layer)),
+//   E[Y_b] = sum_s C_s k_i(s) (Ib_i(s) - Ibar_s(layer)) Ahat_s(layer),
+// exactly; the march tallies X - beta.Y and finalize adds beta.E[Y] back, so
+// the estimate is unbiased for any beta and any table.
 // ---------------------------------------------------------------------------
-__constant__ double c_quad_mu[128];
-__constant__ double c_quad_w[128];
-__constant__ int c_nquad;
-
-int upload_quadrature(const double *mu, const double *w, int n) {
-    cudaError_t e = cudaMemcpyToSymbol(c_quad_mu, mu, sizeof(double) * n);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_quad_w, w, sizeof(double) * n);
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_nquad, &n, sizeof(int));
-    return (int)e;
-}
-
 __device__ __forceinline__ float cv_k(const CvParams &c, int sid, float T, float x) {
     int ti, xi = 0;
     float ft, fx = 0.f;
@@ -359,61 +353,104 @@ __global__ void cv_sur_kernel(const CvParams c) {
     }
 }
 
-// Direction-averaged surrogate intensity Jhat per (field, sample, layer):
-// composite Gauss-Legendre in mu on each hemisphere, 1-D march through the
-// layers with the same toll cut-off and wall emission as the 3-D walk.  One
-// warp per (field, sample, layer): lane l takes the paths (hemisphere, node)
-// l, l + 32, ... of the 2 * nquad, and the FP64 weighted sums are reduced
-// across the warp (butterfly order).
-__global__ void cv_jhat_kernel(const CvParams c) {
+// The straight walk of the surrogate: from oW (the centre of layer w0) with
+// wall-normal cosine mu > 0 in direction dW (+1: east), through the layers of
+// constant (k, Ib) = surp[l], advanced layer by layer and stopped when its
+// optical depth exceeds dtoll = ln(1/toll) (the rest is absorbed in that
+// layer) or at the black wall of intensity Iw.  Returns the collected
+// intensity J and the own-layer absorptance A = 1 - (transmissivity leaving
+// layer w0; 0 if the walk stops inside it).
+__device__ __forceinline__ void cv_walk(const float *fw, int nw, float dtoll, const float2 *surp, int w0, float oW,
+                                        float mu, int dW, float Iw, float *J_out, float *A_out) {
+    const float invW = 1.0f / mu;
+    // exit face of layer l at parameter (fw[l + 1] - o)/mu going east and
+    // (fw[l] - o) * (-1/mu) going west
+    const float *fwn = fw + (dW > 0 ? 1 : 0);
+    const float sinvW = dW > 0 ? invW : -invW;
+    const int lwall = dW > 0 ? nw : -1;
+    float J = 0.0f, tauE = 1.0f, tE = 0.0f, dcum = 0.0f, tex0 = -1.0f;
+    int l = w0;
+    float2 kv = __ldg(surp + w0);
+    bool trunc;
+    for (;;) {
+        const float tn = (__ldg(fwn + l) - oW) * sinvW;
+        const float opt = kv.x * (tn - tE);
+        trunc = dcum + opt > dtoll;
+        if (trunc) break;  // truncated in layer l
+        const float as = -mc_expm1(-opt);
+        const float tas = tauE * as;
+        J = fmaf(tas, kv.y, J);
+        tauE = tauE - tas;
+        dcum = dcum + opt;
+        tE = tn;
+        tex0 = tex0 < 0.0f ? tauE : tex0;
+        l += dW;
+        if (l == lwall) break;  // reached the wall
+        kv = __ldg(surp + l);
+    }
+    *J_out = fmaf(tauE, trunc ? kv.y : Iw, J);
+    *A_out = 1.0f - (tex0 < 0.0f ? 0.0f : tex0);
+}
+
+// Surrogate table and its exact means per (field, sample, layer), one warp
+// each: the lanes walk the 2 (kSurBins + 1) nodes (mu = u_m^2, u_m = m /
+// kSurBins; the node u = 0 at mu = 2^-30, the grazing limit), the warp's
+// shared row holds them, and each lane writes kSurBins / 16 bins and their
+// FP64 contribution to the means.  With mu uniform on [0, 1] per hemisphere,
+// u has density 2u, and a bin m contributes
+//   E_h[J] += ((2m + 1) J0 + (m + 2/3) dJ) / kSurBins^2,
+// likewise for A; the warp sums in butterfly order.
+constexpr int kSurNodes = kSurBins + 1;
+__global__ void cv_table_kernel(const CvParams c) {
+    __shared__ float2 s_node[8][2 * kSurNodes];
     const long long n = (long long)c.nfields * c.n_samples * c.nw;
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const long long wpb = blockDim.x >> 5;
-    const int npath = 2 * c_nquad;
-    for (long long idx = blockIdx.x * wpb + (threadIdx.x >> 5); idx < n; idx += (long long)gridDim.x * wpb) {
+    float2 *node = s_node[wid];
+    for (long long idx = blockIdx.x * wpb + wid; idx < n; idx += (long long)gridDim.x * wpb) {
         const int w = (int)(idx % c.nw);
         const long long fs = idx / c.nw;
         const int sid = (int)(fs % c.n_samples);
         const float2 *sp = c.sur + fs * c.nw;
         const int band = c.mode == MODE_GREY ? 0 : sid / c.nq;
         const float oW = (__ldg(c.fw + w) + __ldg(c.fw + w + 1)) * 0.5f;
-        double acc = 0.0, accA = 0.0;
-        for (int path = lane; path < npath; path += 32) {
-            const int h = path >= c_nquad ? 1 : 0;
-            const int q = path - h * c_nquad;
-            const int dir = h ? 1 : -1;
+        for (int e = lane; e < 2 * kSurNodes; e += 32) {
+            const int h = e >= kSurNodes ? 1 : 0;
+            const int m = e - h * kSurNodes;
+            const float u = (float)m * (1.0f / (float)kSurBins);
+            const float mu = m ? u * u : 9.31322574615478516e-10f;  // 2^-30
             const float Iw = c.mode == MODE_GREY ? c.Tw4[h] : __ldg(c.ibw + h * c.nbands + band);
-            const float inv_mu = (float)(1.0 / c_quad_mu[q]);
-            float tau = 1.0f, J = 0.0f, t0 = 0.0f, dcum = 0.0f;
-            int l = w;
-            float seg = dir > 0 ? (__ldg(c.fw + w + 1) - oW) : (oW - __ldg(c.fw + w));
-            for (;;) {
-                const float2 kv = sp[l];
-                const float opt = kv.x * seg * inv_mu;
-                if (dcum + opt > c.dtoll) { J = fmaf(tau, kv.y, J); break; }  // truncated in layer l
-                const float a = -expm1f(-opt);
-                const float ta = tau * a;
-                J = fmaf(ta, kv.y, J);
-                tau = tau - ta;
-                dcum = dcum + opt;
-                if (l == w) t0 = tau;  // transmissivity leaving the own layer
-                l += dir;
-                if (l < 0 || l >= c.nw) { J = fmaf(tau, Iw, J); break; }
-                seg = __ldg(c.fw + l + 1) - __ldg(c.fw + l);
-            }
-            acc += c_quad_w[q] * (double)J;
-            accA += c_quad_w[q] * (1.0 - (double)t0);
+            float J, A;
+            cv_walk(c.fw, c.nw, c.dtoll, sp, w, oW, mu, h ? 1 : -1, Iw, &J, &A);
+            node[e] = make_float2(J, A);
+        }
+        __syncwarp();
+        float4 *row = c.surtab + idx * (2 * kSurBins);
+        double eJ = 0.0, eA = 0.0;
+#pragma unroll
+        for (int j = 0; j < (2 * kSurBins) / 32; ++j) {
+            const int bi = lane + 32 * j;
+            const int h = bi >= kSurBins ? 1 : 0;
+            const int m = bi - h * kSurBins;
+            const float2 v0 = node[h * kSurNodes + m], v1 = node[h * kSurNodes + m + 1];
+            const float dJ = v1.x - v0.x, dA = v1.y - v0.y;
+            row[bi] = make_float4(v0.x, dJ, v0.y, dA);
+            const double c0 = (double)(2 * m + 1), c1 = (double)m + 2.0 / 3.0;
+            eJ += c0 * (double)v0.x + c1 * (double)dJ;
+            eA += c0 * (double)v0.y + c1 * (double)dA;
         }
         for (int o = 16; o > 0; o >>= 1) {
-            acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            accA += __shfl_xor_sync(0xffffffffu, accA, o);
+            eJ += __shfl_xor_sync(0xffffffffu, eJ, o);
+            eA += __shfl_xor_sync(0xffffffffu, eA, o);
         }
         if (lane == 0) {
-            const double J = 0.5 * acc;
+            const double sc = 0.5 / ((double)kSurBins * (double)kSurBins);  // both hemispheres, weight 1/2
+            const double J = eJ * sc, A = eA * sc;
             const float Jhi = (float)J;
-            c.Jhat[idx] = make_double2(J, 0.5 * accA);
-            c.Jf[idx] = make_float4(Jhi, (float)(J - (double)Jhi), (float)(0.5 * accA), sp[w].y);
+            c.Jhat[idx] = make_double2(J, A);
+            c.Jf[idx] = make_float4(Jhi, (float)(J - (double)Jhi), (float)A, sp[w].y);
         }
+        __syncwarp();
     }
 }
 
@@ -826,7 +863,7 @@ int launch_cv_prepare(const CvParams &c, void *stream) {
     dnsmc::note_launch();
     cv_sur_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
     dnsmc::note_launch();
-    cv_jhat_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(c);  // one warp per (field, sample, layer)
+    cv_table_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(c);  // one warp per (field, sample, layer)
     return (int)cudaGetLastError();
 }
 

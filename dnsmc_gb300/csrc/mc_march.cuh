@@ -267,49 +267,17 @@ __device__ __forceinline__ void hg_scatter(float g, uint32_t uc, uint32_t um, fl
 }
 
 // Surrogate of the control variate: the ray's straight flight through the
-// layer-mean medium (k, Ib constant in each wall-normal layer, black walls),
-// advanced layer by layer and stopped when its optical depth exceeds
-// ln(1/toll).  Returns the collected intensity Jbar and the transmissivity
-// leaving the own layer.
-template <int MODE>
-__device__ __forceinline__ void surrogate_walk(const MarchParams &P, const float2 *surp, int w0, float oW, float sW,
-                                               int nbnd, float *Jbar_out, float *tex_out) {
-    const float invW = 1.0f / fabsf(sW);
-    const int dW = sW > 0.f ? 1 : -1;
-    // exit face of layer l at parameter (fw[l + 1] - o)/s going up and
-    // (fw[l] - o) * (-1/|s|) going down (the same values as (o - fw[l])/|s|)
-    const float *fwn = P.fw + (dW > 0 ? 1 : 0);
-    const float sinvW = dW > 0 ? invW : -invW;
-    const int lwall = dW > 0 ? P.nw : -1;
-    float Jbar = 0.0f, tauE = 1.0f, tE = 0.0f, dcum = 0.0f, tex0 = -1.0f;
-    int l = w0;
-    float2 kv = __ldg(surp + w0);
-    bool trunc;
-    for (;;) {
-        const float tn = (__ldg(fwn + l) - oW) * sinvW;
-        const float opt = kv.x * (tn - tE);
-        trunc = dcum + opt > P.dtoll;
-        if (trunc) break;  // truncated in layer l
-        const float as = -mc_expm1(-opt);
-        const float tas = tauE * as;
-        Jbar = fmaf(tas, kv.y, Jbar);
-        tauE = tauE - tas;
-        dcum = dcum + opt;
-        tE = tn;
-        tex0 = tex0 < 0.0f ? tauE : tex0;
-        l += dW;
-        if (l == lwall) break;  // reached the wall
-        kv = __ldg(surp + l);
-    }
-    if (trunc) {
-        Jbar = fmaf(tauE, kv.y, Jbar);
-    } else {
-        const int side = dW > 0 ? 1 : 0;
-        const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
-        Jbar = fmaf(tauE, Iw, Jbar);
-    }
-    *Jbar_out = Jbar;
-    *tex_out = tex0 < 0.0f ? 0.0f : tex0;
+// layer-mean medium, read from its table row (the ray's field, spectral
+// sample and layer; cv_table_kernel) by linear interpolation in
+// u = sqrt(|sW|) between the nodes m / kSurBins.  Returns the collected
+// intensity J and the own-layer absorptance A.  The reads are warp-uniform.
+__device__ __forceinline__ void surrogate_lookup(const float4 *row, float sW, float *J, float *A) {
+    const float x = sqrtf(fabsf(sW)) * (float)kSurBins;
+    const int m = min((int)x, kSurBins - 1);
+    const float r = x - (float)m;
+    const float4 e = __ldg(row + (sW > 0.0f ? kSurBins : 0) + m);
+    *J = fmaf(r, e.y, e.x);
+    *A = fmaf(r, e.w, e.z);
 }
 
 // ---------------------------------------------------------------------------

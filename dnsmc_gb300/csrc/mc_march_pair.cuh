@@ -354,11 +354,11 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             isteps += (unsigned long long)steps;
             // control variate: the ray's straight flight through the
             // layer-mean medium, the same for both cells (same layer)
-            float Jbar = 0.0f, tex0 = 0.0f, I0 = 0.0f;
+            float Jbar = 0.0f, Aown = 0.0f, I0 = 0.0f;
             if (CV) {
-                const float2 *surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
-                I0 = __ldg(surp + w0).y;
-                surrogate_walk<MODE>(P, surp, w0, oW, sW, nbnd, &Jbar, &tex0);
+                const long long srow = ((long long)f * P.n_samples + sid) * P.nw + w0;
+                I0 = __ldg(P.sur + srow).y;
+                surrogate_lookup(P.surtab + srow * (2 * kSurBins), sW, &Jbar, &Aown);
             }
 #pragma unroll
             for (int k = 0; k < C; ++k) {
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 if (CV) {
                     // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
                     const float Ya = wk[k] * (Ii[k] - Jbar);
-                    const float Yb = wk[k] * ((1.0f - tex0) * (Ii[k] - I0));
+                    const float Yb = wk[k] * (Aown * (Ii[k] - I0));
                     if (MOM && active[k]) {
                         const double xd = X, ya = Ya, yb = Yb;
                         mo[k][0] += xd; mo[k][1] += ya; mo[k][2] += yb;
@@ -833,11 +833,11 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
             isteps += (unsigned long long)steps;
             // control variate: the ray's straight flight through the
             // layer-mean medium, the same for both cells (same layer)
-            float Jbar = 0.0f, tex0 = 0.0f, I0 = 0.0f;
+            float Jbar = 0.0f, Aown = 0.0f, I0 = 0.0f;
             if (CV) {
-                const float2 *surp = P.sur + ((long long)f * P.n_samples + sid) * P.nw;
-                I0 = __ldg(surp + w0).y;
-                surrogate_walk<MODE>(P, surp, w0, oW, sW_e, nbnd, &Jbar, &tex0);
+                const long long srow = ((long long)f * P.n_samples + sid) * P.nw + w0;
+                I0 = __ldg(P.sur + srow).y;
+                surrogate_lookup(P.surtab + srow * (2 * kSurBins), sW_e, &Jbar, &Aown);
             }
 #pragma unroll
             for (int k = 0; k < C; ++k) {
@@ -845,7 +845,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                 if (CV) {
                     // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
                     const float Ya = wk[k] * (Ii[k] - Jbar);
-                    const float Yb = wk[k] * ((1.0f - tex0) * (Ii[k] - I0));
+                    const float Yb = wk[k] * (Aown * (Ii[k] - I0));
                     if (MOM && active[k]) {
                         const double xd = X, ya = Ya, yb = Yb;
                         mo[k][0] += xd; mo[k][1] += ya; mo[k][2] += yb;

@@ -356,12 +356,21 @@ int  dnsmc_set_cv_beta(dnsmc_solver *s, const float *beta);
  * dnsmc_cvnet_apply), same layout; DNSMC_ERR_STATE when none are set.       */
 int  dnsmc_get_cv_beta(dnsmc_solver *s, float *beta);
 /* Control-variate data of the last solve (any pointer may be NULL): layer
- * means (T_bar, x_bar) [f][imax][2], surrogate (k_bar, Ib_bar)
+ * means (T_bar, x_bar) [f][imax][2], surrogate medium (k_bar, Ib_bar)
  * [f][sample][imax][2] (sample = band*nq + g), (Jhat, Ahat) [f][sample][imax][2]
- * (direction-averaged absorbed intensity, own-plane absorptance) and
- * (E[Y_a], E[Y_b]) [f][group][cell][2] dense i fastest.                      */
+ * (the exact direction means of the tabulated surrogate's collected
+ * intensity and own-plane absorptance) and (E[Y_a], E[Y_b])
+ * [f][group][cell][2] dense i fastest.                                      */
 int  dnsmc_get_cv_data(dnsmc_solver *s, int *n_samples, float *layer, float *sur,
                        double *Jhat, double *muY);
+/* The tabulated surrogate of the last control-variate solve,
+ * [f][sample][imax][2][DNSMC_CV_BINS][4]: for a ray leaving the centre of
+ * plane i towards the west (0) or east (1) wall with sqrt(|mu|) = (m + r) /
+ * DNSMC_CV_BINS, r in [0, 1), the march reads (J0, dJ, A0, dA) of bin m and
+ * takes J = J0 + r dJ (collected intensity), A = A0 + r dA (own-plane
+ * absorptance).  Holds n_samples * imax * 2 * DNSMC_CV_BINS * 4 floats per field. */
+#define DNSMC_CV_BINS 64
+int  dnsmc_get_cv_table(dnsmc_solver *s, float *tab);
 /* Per-ray moments of the last solve with cv_moments = 1, [f][group][cell][9]
  * dense i fastest: sums of X, Y_a, Y_b, X^2, Y_a^2, Y_b^2, X Y_a, X Y_b,
  * Y_a Y_b over the cell's rays (X is the plain OERM ray contribution).       */

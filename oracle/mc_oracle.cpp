@@ -572,6 +572,8 @@ typedef struct {
     int cpl;                  // cells per lane (1, 2 or 4): a packet is 32 * cpl cells (tile_a x tile_b)
     int pw_step;              // > 1 (orc_packet_mc, orc_cv_mean): only every pw_step-th wall-normal layer
                               // of the region, from ew0, with the rays of an unstrided run
+    const float *sur_tab;     // cv = 1: the surrogate table of orc_cv_table [field][sample][nw][2][kSurBinsO][4],
+                              // read like the march does; NULL: the walk itself at the ray's cosine
 } OrcPacketConfig;
 
 }  // extern "C"
@@ -678,6 +680,49 @@ inline void p_gpos(R v, R v0, R inv, int n, int *i, R *f) {
 
 template <class R> inline R FMA(R a, R b, R c) { return std::fma(a, b, c); }
 template <> inline float FMA<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Bins per hemisphere of the control variate's surrogate table (the device's
+// kSurBins): nodes at u = m / kSurBinsO of u = sqrt(|mu|).
+constexpr int kSurBinsO = 64;
+
+template <class R> inline R expm1_r(R x);
+template <> inline float expm1_r<float>(float x) { return p_expm1(x); }
+template <> inline double expm1_r<double>(double x) { return std::expm1(x); }
+
+// The surrogate's straight walk (the device's cv_walk): from oW, the centre of
+// layer w0, with wall-normal cosine mu > 0 in direction dW through layers of
+// constant (sk[l], sI[l]), stopped beyond optical depth dtoll (the rest is
+// absorbed in that layer) or at the black wall of intensity Iw.  J: the
+// collected intensity; A: 1 - the transmissivity leaving layer w0 (0 if the
+// walk stops inside it).
+template <class R>
+inline void sur_walk(const float *fw, int nw, R dtoll, const float *sk, const float *sI, int w0, R oW, R mu, int dW,
+                     R Iw, R *J_out, R *A_out) {
+    const R invW = (R)1 / mu;
+    R J = 0, tauE = 1, tE = 0, dcum = 0, te0 = -1;
+    int l = w0;
+    R kS = (R)sk[w0], IS = (R)sI[w0];
+    bool trunc = false;
+    for (;;) {
+        const R tn = (dW > 0 ? ((R)fw[l + 1] - oW) : (oW - (R)fw[l])) * invW;
+        const R opt = kS * (tn - tE);
+        trunc = dcum + opt > dtoll;
+        if (trunc) break;
+        const R a = -expm1_r<R>(-opt);
+        const R ta = tauE * a;
+        J = FMA<R>(ta, IS, J);
+        tauE = tauE - ta;
+        dcum = dcum + opt;
+        tE = tn;
+        if (te0 < 0) te0 = tauE;
+        l += dW;
+        if (l < 0 || l >= nw) break;
+        kS = (R)sk[l];
+        IS = (R)sI[l];
+    }
+    *J_out = FMA<R>(tauE, trunc ? IS : Iw, J);
+    *A_out = (R)1 - (te0 < 0 ? (R)0 : te0);
+}
 
 inline float p_u24(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
 inline float p_u24o(uint32_t x) { return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-8f; }
@@ -878,36 +923,21 @@ struct Packet {
             const int sid = c.mode != 0 ? koff / (c.nT * c.nX) : 0;
             const int nsamp = c.mode != 0 ? c.nbands * c.nq : 1;
             const size_t sbase = ((size_t)f * nsamp + sid) * c.nw;
-            R Jbar = 0, tex0 = 0;
+            R Jbar = 0, Aown = 0;
             if (c.cv) {
-                const R dtoll = (R)(float)(-std::log((double)c.toll));
-                const R invWs = (R)1 / std::fabs(sW);
-                const int dWs = sW > 0 ? 1 : -1;
-                R tauE = 1, tE = 0, dcum = 0, te0 = -1;
-                int l = w0;
-                R kS = (R)c.sur_k[sbase + w0], IS = (R)c.sur_I[sbase + w0];
-                for (;;) {
-                    const R tn = (dWs > 0 ? ((R)c.fw[l + 1] - oW) : (oW - (R)c.fw[l])) * invWs;
-                    const R opt = kS * (tn - tE);
-                    if (dcum + opt > dtoll) { Jbar = FMA<R>(tauE, IS, Jbar); break; }
-                    const R a = -expm1n(-opt);
-                    const R ta = tauE * a;
-                    Jbar = FMA<R>(ta, IS, Jbar);
-                    tauE = tauE - ta;
-                    dcum = dcum + opt;
-                    tE = tn;
-                    if (te0 < 0) te0 = tauE;
-                    l += dWs;
-                    if (l < 0 || l >= c.nw) {
-                        const int side = l < 0 ? 0 : 1;
-                        const R Iws = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
-                        Jbar = FMA<R>(tauE, Iws, Jbar);
-                        break;
-                    }
-                    kS = (R)c.sur_k[sbase + l];
-                    IS = (R)c.sur_I[sbase + l];
+                if (c.sur_tab) {  // the march's table read: linear in sqrt(|sW|)
+                    const float x = std::sqrt(std::fabs((float)sW)) * (float)kSurBinsO;
+                    const int m = std::min((int)x, kSurBinsO - 1);
+                    const float r = x - (float)m;
+                    const float *e = c.sur_tab + (((sbase + w0) * 2 + (sW > 0 ? 1 : 0)) * kSurBinsO + m) * 4;
+                    Jbar = FMA<R>((R)r, (R)e[1], (R)e[0]);
+                    Aown = FMA<R>((R)r, (R)e[3], (R)e[2]);
+                } else {
+                    const int side = sW > 0 ? 1 : 0;
+                    const R Iws = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
+                    sur_walk<R>(c.fw, c.nw, (R)(float)(-std::log((double)c.toll)), c.sur_k + sbase,
+                                c.sur_I + sbase, w0, oW, std::fabs(sW), sW > 0 ? 1 : -1, Iws, &Jbar, &Aown);
                 }
-                tex0 = te0 < 0 ? (R)0 : te0;
             }
             // warp-uniform DDA from (pw0, fa0, fb0)
             R pw0 = oW, fa0 = (R)0.5, fb0 = (R)0.5, offA = (R)0.5, offB = (R)0.5;
@@ -1205,7 +1235,7 @@ struct Packet {
                     }
                     const R Iw0 = (R)c.sur_I[sbase + w0];
                     const R Ya = wk[l] * (Ii[l] - Jbar);
-                    const R Yb = wk[l] * (((R)1 - tex0) * (Ii[l] - Iw0));
+                    const R Yb = wk[l] * (Aown * (Ii[l] - Iw0));
                     if (c.moments) {
                         const long long tc = ((long long)(w0 - c.ew0) * nkR + (b0[l] - c.eb0)) * njR + (a0[l] - c.ea0);
                         double *mo = c.moments + 9 * (((long long)f * nG + G) * rc + tc);
@@ -1298,6 +1328,60 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
         }
     }
     if (steps_out) *steps_out = steps;
+    return 0;
+}
+
+// The control variate's surrogate table (the device's cv_table_kernel), in
+// FP32: per (field, sample, layer l) and hemisphere h (0: west, 1: east) the
+// walk of sur_walk from the centre of l at the nodes mu = (m / kSurBinsO)^2,
+// m = 0 .. kSurBinsO (m = 0 at mu = 2^-30), over the layer-mean medium
+// (sur_k, sur_I) with black walls (grey: T_wall^4, tables: ibw); each bin m
+// stored as (J0, dJ, A0, dA) = (J(m), J(m+1) - J(m), A(m), A(m+1) - A(m)).
+// tab: [f][sample][nw][2][kSurBinsO][4].  JA (or NULL): [f][sample][nw][2]
+// the exact means of the interpolant over mu uniform on [-1, 1]: with u =
+// sqrt(|mu|) of density 2u, bin m weighs ((2m+1) J0 + (m + 2/3) dJ) /
+// kSurBinsO^2 per hemisphere, the hemispheres 1/2 each.
+int orc_cv_table(const OrcPacketConfig *c, float *tab, double *JA) {
+    if (!c || !c->sur_k || !c->sur_I || !tab) return 1;
+    const int nw = c->nw, nsamp = c->mode == 0 ? 1 : c->nbands * c->nq, NB = kSurBinsO;
+    const float dtoll = (float)(-std::log((double)c->toll));
+    const float tw = c->T_west, te = c->T_east;
+    const float Tw4[2] = {tw * tw * tw * tw, te * te * te * te};
+#pragma omp parallel for schedule(dynamic, 4)
+    for (long long fs = 0; fs < (long long)c->nfields * nsamp; ++fs) {
+        const int band = c->mode == 0 ? 0 : (int)(fs % nsamp) / c->nq;
+        const float *sk = c->sur_k + (size_t)fs * nw, *sI = c->sur_I + (size_t)fs * nw;
+        for (int l = 0; l < nw; ++l) {
+            const float oW = (c->fw[l] + c->fw[l + 1]) * 0.5f;
+            float J[2][kSurBinsO + 1], A[2][kSurBinsO + 1];
+            for (int h = 0; h < 2; ++h) {
+                const float Iw = c->mode == 0 ? Tw4[h] : c->ibw[h * c->nbands + band];
+                for (int m = 0; m <= NB; ++m) {
+                    const float u = (float)m * (1.0f / (float)NB);
+                    const float mu = m ? u * u : 9.31322574615478516e-10f;
+                    sur_walk<float>(c->fw, nw, dtoll, sk, sI, l, oW, mu, h ? 1 : -1, Iw, &J[h][m], &A[h][m]);
+                }
+            }
+            float *row = tab + ((size_t)fs * nw + l) * 2 * NB * 4;
+            double eJ = 0, eA = 0;
+            for (int h = 0; h < 2; ++h)
+                for (int m = 0; m < NB; ++m) {
+                    float *e = row + (h * NB + m) * 4;
+                    e[0] = J[h][m];
+                    e[1] = J[h][m + 1] - J[h][m];
+                    e[2] = A[h][m];
+                    e[3] = A[h][m + 1] - A[h][m];
+                    const double c0 = (double)(2 * m + 1), c1 = (double)m + 2.0 / 3.0;
+                    eJ += c0 * (double)e[0] + c1 * (double)e[1];
+                    eA += c0 * (double)e[2] + c1 * (double)e[3];
+                }
+            if (JA) {
+                const double sc = 0.5 / ((double)NB * (double)NB);
+                JA[2 * ((size_t)fs * nw + l)] = eJ * sc;
+                JA[2 * ((size_t)fs * nw + l) + 1] = eA * sc;
+            }
+        }
+    }
     return 0;
 }
 

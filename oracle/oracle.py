@@ -67,7 +67,7 @@ class PacketConfig(ctypes.Structure):
         ("mg_levels", ctypes.c_int), ("mg_steps", ctypes.c_int), ("mgT", _f), ("mgfw", _f),
         ("mg_off", ctypes.c_longlong * 6), ("mg_fwoff", ctypes.c_int * 6), ("mg_da", ctypes.c_float * 6),
         ("mg_db", ctypes.c_float * 6), ("Ly", ctypes.c_float), ("Lz", ctypes.c_float),
-        ("cpl", ctypes.c_int), ("pw_step", ctypes.c_int),
+        ("cpl", ctypes.c_int), ("pw_step", ctypes.c_int), ("sur_tab", _f),
     ]
 
 
@@ -93,6 +93,8 @@ def load():
         lib.orc_cv_mean.argtypes = [ctypes.POINTER(PacketConfig), _i, _i, _d, _d, _d, ctypes.c_int, ctypes.c_int,
                                     _d]
         lib.orc_cv_mean.restype = ctypes.c_int
+        lib.orc_cv_table.argtypes = [ctypes.POINTER(PacketConfig), _f, _d]
+        lib.orc_cv_table.restype = ctypes.c_int
         _ll = ctypes.POINTER(ctypes.c_longlong)
         lib.orc_ck_from_lbl.argtypes = [_d, ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_int, _ll, _i,
                                         _d, _d, ctypes.c_int, _d, ctypes.c_int, ctypes.c_int, _f, _d]
@@ -288,6 +290,9 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
         keep.update(sk=sk, sI=sI)
         c.cv = 1
         c.sur_k, c.sur_I = _fp(sk), _fp(sI)
+        tab, _ = cv_table(c)
+        keep["sur_tab"] = tab
+        c.sur_tab = _fp(tab)
         bsrc = solver.cv_beta() if getattr(solver, "_beta_dev", False) else getattr(solver, "_beta", None)
         if bsrc is not None:
             b = np.ascontiguousarray(bsrc, np.float32)
@@ -296,6 +301,21 @@ def packet_config(solver, T: np.ndarray, x: np.ndarray | None, *, use_double: in
     if mode is not None:
         c.mode = mode
     return c, keep
+
+
+SUR_BINS = 64  # bins per hemisphere of the surrogate table (nodes uniform in sqrt|mu|)
+
+
+def cv_table(c):
+    """The control variate's surrogate table of the march (orc_cv_table) for
+    the layer-mean medium c.sur_k / c.sur_I of a PacketConfig: (table
+    [f, sample, nw, 2, SUR_BINS, 4] float32 of (J0, dJ, A0, dA) per bin,
+    means [f, sample, nw, 2] float64 of (Jhat, Ahat))."""
+    ns = 1 if c.mode == 0 else c.nbands * c.nq
+    tab = np.zeros((c.nfields, ns, c.nw, 2, SUR_BINS, 4), np.float32)
+    JA = np.zeros((c.nfields, ns, c.nw, 2), np.float64)
+    assert load().orc_cv_table(ctypes.byref(c), _fp(tab), JA.ctypes.data_as(_d)) == 0
+    return tab, JA
 
 
 def cv_quadrature():
@@ -309,44 +329,56 @@ def cv_quadrature():
     return np.concatenate(mu), np.concatenate(wt)
 
 
+def cv_walk(sur_k, sur_I, fw, toll, Iw, l, mu):
+    """The surrogate walk in float64: from the centre of layer l with
+    wall-normal cosine mu (sign: direction, > 0 towards the east wall of
+    intensity Iw[1]) through layers of constant (sur_k, sur_I), stopped once
+    its optical depth exceeds ln(1/toll) (the rest stays in that layer) or at
+    a black wall.  Returns (J, A): collected intensity and own-layer
+    absorptance 1 - t0 (t0 = 0 if it stops inside layer l)."""
+    nw = len(sur_k)
+    dtoll = -math.log(toll)
+    d = 1 if mu > 0 else -1
+    m = abs(mu)
+    o = 0.5 * (float(fw[l]) + float(fw[l + 1]))
+    tau, J, i, t0, dcum = 1.0, 0.0, l, 0.0, 0.0
+    seg = (float(fw[l + 1]) - o) if d > 0 else (o - float(fw[l]))
+    while True:
+        opt = float(sur_k[i]) * seg / m
+        if dcum + opt > dtoll:  # optical depth beyond ln(1/toll): the rest stays in layer i
+            J += tau * float(sur_I[i])
+            break
+        a = -math.expm1(-opt)
+        J += tau * a * float(sur_I[i])
+        tau -= tau * a
+        dcum += opt
+        if i == l:
+            t0 = tau
+        i += d
+        if i < 0 or i >= nw:
+            J += tau * float(Iw[1 if d > 0 else 0])
+            break
+        seg = float(fw[i + 1]) - float(fw[i])
+    return J, 1.0 - t0
+
+
 def cv_jhat(sur_k, sur_I, fw, toll, Iw_west, Iw_east):
     """For every layer l of a 1-D layered medium (k, Ib per layer; black walls
-    with intensities Iw), rays leaving the layer centre and stopped once their
-    optical depth exceeds ln(1/toll) (the surrogate walk of the march), in
-    float64:
+    with intensities Iw), the direction means of the surrogate walk (cv_walk)
+    by quadrature (cv_quadrature), in float64:
     Jhat[l] = 1/2 int_{-1}^{1} J(mu; l) dmu (absorbed intensity) and
-    Ahat[l] = 1/2 int_{-1}^{1} (1 - t0(mu; l)) dmu (own-layer absorptance).
+    Ahat[l] = 1/2 int_{-1}^{1} A(mu; l) dmu (own-layer absorptance).
     Returns an (nw, 2) array."""
     nw = len(sur_k)
     mu, wt = cv_quadrature()
-    fw = np.asarray(fw, np.float64)
-    o = 0.5 * (fw[:-1] + fw[1:])
-    dtoll = -math.log(toll)
     out = np.zeros((nw, 2))
     for l in range(nw):
         acc = accA = 0.0
-        for d, Iw in ((-1, Iw_west), (1, Iw_east)):
+        for sgn in (-1.0, 1.0):
             for m, wq in zip(mu, wt):
-                tau, J, i, t0, dcum = 1.0, 0.0, l, 0.0, 0.0
-                seg = (fw[l + 1] - o[l]) if d > 0 else (o[l] - fw[l])
-                while True:
-                    opt = float(sur_k[i]) * seg / m
-                    if dcum + opt > dtoll:  # optical depth beyond ln(1/toll): the rest stays in layer i
-                        J += tau * float(sur_I[i])
-                        break
-                    a = -math.expm1(-opt)
-                    J += tau * a * float(sur_I[i])
-                    tau -= tau * a
-                    dcum += opt
-                    if i == l:
-                        t0 = tau
-                    i += d
-                    if i < 0 or i >= nw:
-                        J += tau * Iw
-                        break
-                    seg = fw[i + 1] - fw[i]
+                J, A = cv_walk(sur_k, sur_I, fw, toll, (Iw_west, Iw_east), l, sgn * m)
                 acc += wq * J
-                accA += wq * (1.0 - t0)
+                accA += wq * A
         out[l] = 0.5 * acc, 0.5 * accA
     return out
 

@@ -1,12 +1,16 @@
 """GPU tests of the control variate (CV): Y is the same ray through the
-medium of plane-averaged T and x_H2O; the march tallies X - beta*Y and the
-exact mean beta*E[Y] (1-D layered-slab quadrature) is added back.
+medium of plane-averaged T and x_H2O, its flight read from a table of the
+straight walk per (field, spectral sample, plane) and interpolated in
+sqrt|mu|; the march tallies X - beta*Y and the exact mean beta*E[Y] of the
+tabulated Y is added back.
 
-* bit-exact tallies vs the oracle's FP32 replay, with beta = 1 and with a
-  per-cell beta array;
-* the device quadrature Jhat and E[Y] against the oracle's float64 versions;
-* isothermal slab: the surrogate is exact, so Q equals the analytic solution
-  with zero variance;
+* bit-exact tallies vs the oracle's FP32 replay (which builds its own table),
+  with beta = 1 and with a per-cell beta array;
+* the device table equals the oracle's bit for bit, its means (Jhat) the
+  oracle's, and they approach the float64 quadrature of the continuous walk;
+  E[Y] per cell matches its definition;
+* isothermal slab: the surrogate is the medium, so Q equals the analytic
+  solution with a variance left only by the interpolation;
 * unbiased: CV and plain MC agree cell by cell on the correlated-k channel;
 * the variance falls by more than 10x at equal rays.
 """
@@ -119,7 +123,7 @@ def test_cv_bitexact_table_t_only():
     s.close()
 
 
-def test_cv_quadrature_and_mean_match_oracle():
+def test_cv_table_and_mean_match_oracle():
     tb = synth.ck_table(nbands=6, nq=4, nT=20, nX=4, seed=9)
     s = D.Solver(D.default_config(model=D.MODEL_TABLE, imax=12, jmax=32, kmax=4, Lx=2.0, Ly=6.28, Lz=3.14,
                                   stretched_x=1, T_west=420, T_east=380, seed=3, n_groups=2, control_variate=1))
@@ -132,14 +136,21 @@ def test_cv_quadrature_and_mean_match_oracle():
     cv = s.cv_data()
     np.testing.assert_allclose(cv["layer"][0, :, 0], T.mean((0, 1)), rtol=1e-6)
     np.testing.assert_allclose(cv["layer"][0, :, 1], x.mean((0, 1)), rtol=1e-5)
+    # the oracle's table of the device's layer-mean medium, and its means
+    c, keep = O.packet_config(s, T[None], x[None])
+    tab_o, JA_o = O.cv_table(c)
+    np.testing.assert_array_equal(s.cv_table(), tab_o)
+    np.testing.assert_allclose(cv["Jhat"], JA_o, rtol=1e-12, atol=0)
     xu, _, _ = s.geometry()
     smp = s.sampling()
     ibw = smp["ibw"].reshape(2, -1)
     nq = 4
-    for sid in (0, 5, 17, 23):
+    for sid in (0, 5, 17, 23):  # the continuous walk's means, by quadrature: the tabulated
+        # surrogate is a close stand-in (its own means are what E[Y] uses)
         J = O.cv_jhat(cv["sur"][0, sid, :, 0], cv["sur"][0, sid, :, 1], xu, s.cfg.toll, ibw[0, sid // nq],
                       ibw[1, sid // nq])
-        np.testing.assert_allclose(cv["Jhat"][0, sid], J, rtol=2e-5, atol=1e-12)
+        np.testing.assert_allclose(cv["Jhat"][0, sid, :, 0], J[:, 0], rtol=2e-3)
+        np.testing.assert_allclose(cv["Jhat"][0, sid, :, 1], J[:, 1], rtol=5e-3, atol=1e-4)
     # E[Y] per cell from its definition: sum over the group's samples of
     # C_s k_i (Ib_i - Jhat), C_s = W_s * q(s) of the (single-bin) alias table
     from test_capi import alias_distribution
@@ -166,18 +177,29 @@ def test_cv_quadrature_and_mean_match_oracle():
     s.close()
 
 
-def test_cv_isothermal_slab_is_exact():
+def test_cv_isothermal_slab():
+    """The surrogate is the medium itself: what is left of each ray's X - Y
+    is the gap between the walk and its tabulated interpolant, so Q is the
+    analytic solution within its (tiny) standard error, and that error is
+    below 1e-3 of the plain estimate's."""
     ni, nj, nk = 32, 32, 8
-    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.2831853, Lz=3.1415927,
-                                  stretched_x=0, T_west=0.0, T_east=300.0, kappa=1.0, seed=3, control_variate=1))
-    s.set_fields(np.full((nk, nj, ni), 1000.0, np.float32))
-    s.set_rays(16)
-    Q, S = s.solve(timeout_s=60)
+    out = []
+    for cv in (1, 0):
+        s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.2831853,
+                                      Lz=3.1415927, stretched_x=0, T_west=0.0, T_east=300.0, kappa=1.0, seed=3,
+                                      control_variate=cv))
+        s.set_fields(np.full((nk, nj, ni), 1000.0, np.float32))
+        s.set_rays(16)
+        out.append(s.solve(timeout_s=60))
+        s.close()
+    (Q, S), (Qp, Sp) = out
     yc = (np.arange(ni) + 0.5) * 2.0 / ni
     exact = O.slab_divq(yc, 2.0, 1.0, 1000.0, 0.0, 300.0)
-    np.testing.assert_allclose(Q[0][0, 0], exact, rtol=2e-4)
-    assert S.max() <= 1e-5 * np.abs(Q).max()
-    s.close()
+    err = np.abs(Q[0] - exact[None, None, :])
+    # sigma from 16 rays per cell: z follows Student's t with 15 degrees of freedom
+    assert (err <= 7.0 * S[0] + 1e-6 * np.abs(exact).max()).all(), (err / S[0]).max()
+    assert math.sqrt(float(((Q[0] - exact) ** 2).mean() / (S[0] ** 2).mean())) < 1.5
+    assert S.max() < 1e-3 * Sp.max(), (S.max(), Sp.max())
 
 
 def _channel_pair(seed_plain, seed_cv, rays, n=32, sampler=D.SAMPLER_IID):
