@@ -446,21 +446,52 @@ __global__ void alloc_weights_kernel(const AllocParams A) {
     }
 }
 
-// lambda = mean_rays * sum(c) / sum(w c): one block, fixed order
-__global__ void alloc_scale_kernel(const float *wgt, const float *cost, long long n, float mean_rays, float *lam) {
-    __shared__ double r0[1024], r1[1024];
+// lambda = mean_rays * sum(c) / sum(w c), in FP64 and in a fixed order: each
+// of kScaleBlocks blocks sums its grid-strided share and writes its partial
+// sums; the last block to finish adds the partials in block order (the
+// result does not depend on which block that is) and re-arms the counter.
+constexpr int kScaleBlocks = 152, kScaleThreads = 256;
+__global__ void __launch_bounds__(kScaleThreads) alloc_scale_kernel(const float *wgt, const float *cost, long long n,
+                                                                   float mean_rays, float *lam, double2 *part,
+                                                                   unsigned int *done) {
+    __shared__ double r0[kScaleThreads], r1[kScaleThreads];
+    __shared__ bool last;
     double a = 0.0, b = 0.0;
-    for (long long e = threadIdx.x; e < n; e += blockDim.x) {
+    for (long long e = blockIdx.x * (long long)kScaleThreads + threadIdx.x; e < n;
+         e += (long long)kScaleBlocks * kScaleThreads) {
         a += (double)cost[e];
         b += (double)wgt[e] * cost[e];
     }
     r0[threadIdx.x] = a; r1[threadIdx.x] = b;
     __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    for (int w = kScaleThreads / 2; w > 0; w >>= 1) {
         if (threadIdx.x < w) { r0[threadIdx.x] += r0[threadIdx.x + w]; r1[threadIdx.x] += r1[threadIdx.x + w]; }
         __syncthreads();
     }
-    if (threadIdx.x == 0) *lam = r1[0] > 0.0 ? (float)(mean_rays * r0[0] / r1[0]) : 0.0f;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = make_double2(r0[0], r1[0]);
+        __threadfence();
+        last = atomicAdd(done, 1u) == (unsigned)(kScaleBlocks - 1);
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    a = 0.0; b = 0.0;
+    for (int i = threadIdx.x; i < kScaleBlocks; i += kScaleThreads) {
+        const double2 v = __ldcg(part + i);
+        a += v.x;
+        b += v.y;
+    }
+    r0[threadIdx.x] = a; r1[threadIdx.x] = b;
+    __syncthreads();
+    for (int w = kScaleThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) { r0[threadIdx.x] += r0[threadIdx.x + w]; r1[threadIdx.x] += r1[threadIdx.x + w]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        *lam = r1[0] > 0.0 ? (float)(mean_rays * r0[0] / r1[0]) : 0.0f;
+        *done = 0u;
+    }
 }
 
 __global__ void alloc_rays_kernel(const float *wgt, long long n, const float *lam, int B, int nmin, int nmax,
@@ -529,6 +560,8 @@ struct dnsmc_cvnet {
     NBuf<float> iout;
     NBuf<float2> vc;
     NBuf<float> wgt, cost, lam;
+    NBuf<double2> lam_part;          // alloc_scale_kernel: per-block partial sums
+    NBuf<unsigned int> lam_done;     // and its finished-block counter
     NBuf<unsigned int> status;                // DNSMC_STATUS_* bits of the tensor-memory forward
     std::mt19937_64 rng;
     ~dnsmc_cvnet() {
@@ -536,6 +569,7 @@ struct dnsmc_cvnet {
         idx.release(); H0.release(); H1.release(); H2.release(); H3.release(); dO.release(); dZ3.release();
         dZ2.release(); dZ1.release(); Z1.release(); Z2.release(); Z3.release(); out.release(); part.release();
         lpart.release(); iX.release(); iout.release(); vc.release(); wgt.release(); cost.release(); lam.release();
+        lam_part.release(); lam_done.release();
         status.release();
         if (stream) cudaStreamDestroy(stream);
     }
@@ -1071,6 +1105,9 @@ int dnsmc_cvnet_apply(dnsmc_cvnet *n, dnsmc_solver *s, int flags, int mean_rays,
         RTRY(n->wgt.ensure((size_t)items));
         RTRY(n->cost.ensure((size_t)items));
         RTRY(n->lam.ensure(1));
+        RTRY(n->lam_part.ensure(kScaleBlocks));
+        RTRY(n->lam_done.ensure(1));
+        CK(cudaMemsetAsync(n->lam_done.p, 0, sizeof(unsigned int), st));
         AllocParams P{};
         P.nfields = v.nfields; P.G = G; P.n_packets = v.n_packets; P.npa = v.npa; P.npb = v.npb;
         P.tile_a = v.tile_a; P.tile_b = v.tile_b; P.njR = v.j1 - v.j0; P.nkR = v.k1 - v.k0;
@@ -1079,7 +1116,8 @@ int dnsmc_cvnet_apply(dnsmc_cvnet *n, dnsmc_solver *s, int flags, int mean_rays,
         alloc_weights_kernel<<<grid1(items * 32, 256), 256, 0, st>>>(P);
         CK(cudaGetLastError());
         dnsmc::note_launch();
-        alloc_scale_kernel<<<1, 1024, 0, st>>>(n->wgt.p, n->cost.p, items, (float)mean_rays, n->lam.p);
+        alloc_scale_kernel<<<kScaleBlocks, kScaleThreads, 0, st>>>(n->wgt.p, n->cost.p, items, (float)mean_rays,
+                                                                    n->lam.p, n->lam_part.p, n->lam_done.p);
         CK(cudaGetLastError());
         dnsmc::note_launch();
         alloc_rays_kernel<<<grid1(items, 256), 256, 0, st>>>(n->wgt.p, items, n->lam.p, B, min_rays, max_rays, rays);

@@ -311,8 +311,7 @@ struct dnsmc_solver {
     DevBuf<double> d_cv_C;
     DevBuf<float2> d_layer, d_sur;
     DevBuf<double2> d_Jhat, d_muY;
-    DevBuf<double> d_cvnodes;                // node sums of E[Y]
-    DevBuf<double> d_kd, d_ibd;              // FP64 copies of the k and Ib tables (node sums)
+    DevBuf<double> d_cvnodes;                // node sums of E[Y] (float pairs, 8 bytes each)
     DevBuf<float4> d_Jf;
     DevBuf<float4> d_surtab;                 // tabulated surrogate [f][sample][nw][2][kSurBins]
     DevBuf<float> d_cv_Cf;
@@ -401,6 +400,10 @@ int check_config(const dnsmc_config &c) {
     if (c.control_variate != 0 && c.control_variate != 1) return fail(DNSMC_ERR_ARG, "control_variate must be 0 or 1");
     if (c.cv_moments != 0 && c.cv_moments != 1) return fail(DNSMC_ERR_ARG, "cv_moments must be 0 or 1");
     if (c.cv_moments && !c.control_variate) return fail(DNSMC_ERR_ARG, "cv_moments needs control_variate = 1");
+    // the surrogate table's sweep keeps per-plane sums of the whole wall-normal
+    // line in shared memory (44 bytes a plane)
+    if (c.control_variate && c.imax > 4096)
+        return fail(DNSMC_ERR_ARG, "the control variate supports imax <= 4096");
     if (c.block_threads && c.block_threads != 128 && c.block_threads != 256)
         return fail(DNSMC_ERR_ARG, "block_threads must be 0, 128 or 256");
     if (c.tile_a && c.tile_a != 8 && c.tile_a != 16 && c.tile_a != 32)
@@ -793,14 +796,6 @@ int upload_tables(dnsmc_solver *s) {
         const float *ib = t.Ib.data() + (size_t)(sid / t.nq) * t.nT;
         for (int ti = 0; ti < t.nT - 1; ++ti) o[klen + ti] = make_float2(ib[ti], ib[ti + 1] - ib[ti]);
     }
-    {
-        const std::vector<double> kd(t.k.begin(), t.k.end()), ibd(t.Ib.begin(), t.Ib.end());
-        TRY(s->d_kd.ensure(kd.size()));
-        TRY(s->d_ibd.ensure(ibd.size()));
-        CUDA_TRY(cudaMemcpyAsync(s->d_kd.p, kd.data(), kd.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-        CUDA_TRY(cudaMemcpyAsync(s->d_ibd.p, ibd.data(), ibd.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-        CUDA_TRY(cudaStreamSynchronize(s->stream));  // the host copies go out of scope
-    }
     TRY(s->d_slab.ensure(sl.size()));
     CUDA_TRY(cudaMemcpyAsync(s->d_slab.p, sl.data(), sl.size() * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
     s->slab_len = len;
@@ -1056,15 +1051,10 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
             cp.part = s->d_part.p;
             cp.layerV = s->d_layerV.p;
         }
-        // E[Y] from node sums for tables without particles (one thread
-        // block holds the sums of a (field, group, layer): at most 2048
-        // work units of 256 threads x 8)
-        const int units = 2 * t.nT * t.nX + (t.nT - 1) * t.nX;
-        if (mode != MODE_GREY && !have_part && units <= 2048) {
+        // E[Y] from node sums for tables without particles
+        if (mode != MODE_GREY && !have_part) {
             TRY(s->d_cvnodes.ensure((size_t)cv_node_count(cp)));
             cp.nodes = s->d_cvnodes.p;
-            cp.ktab_d = s->d_kd.p;
-            cp.ibtab_d = s->d_ibd.p;
         }
         s->cv_samples = S;
         P.sur = s->d_sur.p;
@@ -1585,7 +1575,7 @@ int dnsmc_destroy(dnsmc_solver *s) {
     s->d_fw.release(); s->d_k.release(); s->d_ib.release(); s->d_ibw.release();
     s->d_slab.release(); s->d_posT.release(); s->d_posTX.release();
     s->d_cv_grp.release(); s->d_cv_sid.release(); s->d_cv_C.release(); s->d_layer.release();
-    s->d_sur.release(); s->d_surtab.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_cvnodes.release(); s->d_kd.release(); s->d_ibd.release(); s->d_beta.release(); s->d_moments.release();
+    s->d_sur.release(); s->d_surtab.release(); s->d_Jhat.release(); s->d_Jf.release(); s->d_cv_Cf.release(); s->d_muY.release(); s->d_cvnodes.release(); s->d_beta.release(); s->d_moments.release();
     s->d_fieldT.release(); s->d_fieldTX.release(); s->d_raw.release();
     s->d_stat_part.release(); s->d_stat_out.release(); s->d_rays_pp.release(); s->d_rays_rcp.release(); s->d_item_steps.release(); s->d_kP.release();
     s->d_order.release(); s->d_order_hist.release();

@@ -330,10 +330,9 @@ struct CvParams {
     const float2 *part;       // [band] (absorption, scattering) per unit volume fraction
     float *layerV;            // [f][nw] layer-mean volume fraction
     // node sums of E[Y] (tables without particles): per (field, group,
-    // region layer) the sums over the group's samples at every table node,
-    // then per group the layer-independent ones; cv_node_count() doubles
+    // region layer) and table cell the sums over the group's samples, as
+    // float pairs (hi, lo) of 8 bytes each; cv_node_count() of them
     double *nodes;
-    const double *ktab_d, *ibtab_d;  // FP64 copies of ktab and ibtab
 };
 long long cv_node_count(const CvParams &c);
 int launch_cv_prepare(const CvParams &c, void *stream);

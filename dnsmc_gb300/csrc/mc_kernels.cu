@@ -75,57 +75,95 @@ __global__ void field_pos_kernel(const float *fT, const float2 *fTX, int2 *outP,
 // strata).  Replaces kernel_results + the host scatter (code/mc_gpu.cu:959-970,
 // :762-776); the output is dense, i fastest.
 // ---------------------------------------------------------------------------
-__global__ void finalize_kernel(const FinalizeParams F) {
-    const long long n = (long long)F.nfields * F.region_cells;
-    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const int f = (int)(idx / F.region_cells);
-        const long long c = idx - (long long)f * F.region_cells;
-        const int iR = (int)(c % F.niR);
-        const long long jk = c / F.niR;
-        const int jR = (int)(jk % F.njR);
-        const int kR = (int)(jk / F.njR);
-        const long long tc = ((long long)iR * F.nkR + kR) * F.njR + jR;
-        const int p = (iR * F.npb + kR / F.tile_b) * F.npa + jR / F.tile_a;
-        double Q = 0.0, V = 0.0;
-        for (int g = 0; g < F.n_groups; ++g) {
-            const int N = F.rays_per_packet ? F.rays_per_packet[g * F.rays_gstride + p] : F.rays;
+// One block per tile of 32 j x 32 i cells of a k row of a field: the tally
+// layout has j fastest and the outputs i fastest, so the block reads its
+// cells along j (thread x = j) and writes them along i through a
+// shared-memory transpose.  Every cell's arithmetic is in the same order as
+// a plain per-cell loop over the groups.
+constexpr int kFinTile = 32, kFinRows = 8;
+__global__ void __launch_bounds__(kFinTile * kFinRows) finalize_kernel(const FinalizeParams F) {
+    __shared__ double s_a[kFinTile][kFinTile + 1], s_b[kFinTile][kFinTile + 1];  // [i][j]
+    const int tx = threadIdx.x % kFinTile, ty = threadIdx.x / kFinTile;
+    const int ntj = (F.njR + kFinTile - 1) / kFinTile;
+    const int j0 = (blockIdx.x % ntj) * kFinTile, i0 = (blockIdx.x / ntj) * kFinTile;
+    const int kR = blockIdx.y, f = blockIdx.z;
+    constexpr int S = kFinTile / kFinRows;  // cells per thread
+    // read side: cell s of this thread is (iR = i0 + ty + kFinRows s, jR = j0 + tx)
+    const int jR = j0 + tx;
+    double Q[S], V[S];
+#pragma unroll
+    for (int s = 0; s < S; ++s) { Q[s] = 0.0; V[s] = 0.0; }
+    // write side: thread x = i, cell s at (iR = i0 + tx, jR = j0 + ty + kFinRows s)
+    const int iW = i0 + tx;
+    for (int g = 0; g < F.n_groups; ++g) {
+        double mg[S], vg[S];
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            const int iR = i0 + ty + kFinRows * s;
             double m = 0.0, v = 0.0;
-            if (!F.group_empty[g] && N > 0) {
-                // divisions by the ray counts as products with their
-                // reciprocals (FP64 division is a long sequence on this GPU)
-                const double2 r = F.rays_per_packet ? F.rcp[g * F.rays_gstride + p] : F.rcp_uniform;
+            if (iR < F.niR && jR < F.njR) {
+                const long long tc = ((long long)iR * F.nkR + kR) * F.njR + jR;
+                const int p = (iR * F.npb + kR / F.tile_b) * F.npa + jR / F.tile_a;
+                const int N = F.rays_per_packet ? F.rays_per_packet[g * F.rays_gstride + p] : F.rays;
                 const long long ti = ((long long)f * F.n_groups + g) * F.region_cells + tc;
-                const double2 t = F.tally[ti];
-                m = t.x * r.x;
-                if (F.batched) {
-                    if (F.nbatch > 1) v = fmax(0.0, t.y * F.rcp_batch.x - m * m) * F.rcp_batch.y;
-                } else if (N > 1) {
-                    v = fmax(0.0, t.y * r.x - m * m) * r.y;
+                if (!F.group_empty[g] && N > 0) {
+                    // divisions by the ray counts as products with their
+                    // reciprocals (FP64 division is a long sequence on this GPU)
+                    const double2 r = F.rays_per_packet ? F.rcp[g * F.rays_gstride + p] : F.rcp_uniform;
+                    const double2 t = F.tally[ti];
+                    m = t.x * r.x;
+                    if (F.batched) {
+                        if (F.nbatch > 1) v = fmax(0.0, t.y * F.rcp_batch.x - m * m) * F.rcp_batch.y;
+                    } else if (N > 1) {
+                        v = fmax(0.0, t.y * r.x - m * m) * r.y;
+                    }
+                }
+                if (F.muY && !F.group_empty[g]) {
+                    const float2 b = F.beta ? F.beta[ti] : make_float2(1.0f, -1.0f);
+                    const double2 mu = F.muY[ti];
+                    // Q_g = beta_a E[Y_a] + beta_b E[Y_b] + mean(X - beta_a Y_a - beta_b Y_b)
+                    m += (double)b.x * mu.x;
+                    m += (double)b.y * mu.y;
                 }
             }
-            if (F.muY && !F.group_empty[g]) {
-                const long long ti = ((long long)f * F.n_groups + g) * F.region_cells + tc;
-                const float2 b = F.beta ? F.beta[ti] : make_float2(1.0f, -1.0f);
-                const double2 mu = F.muY[ti];
-                // Q_g = beta_a E[Y_a] + beta_b E[Y_b] + mean(X - beta_a Y_a - beta_b Y_b)
-                m += (double)b.x * mu.x;
-                m += (double)b.y * mu.y;
-            }
-            Q += m;
-            V += v;
-            if (F.Qg) {
-                const long long o = ((long long)f * F.n_groups + g) * F.region_cells + c;
-                F.Qg[o] = m;
-                F.varg[o] = v;
-            }
+            Q[s] += m;
+            V[s] += v;
+            mg[s] = m;
+            vg[s] = v;
         }
-        F.Q[idx] = Q;
-        F.var[idx] = V;
-        if (F.sigma) F.sigma[idx] = sqrt(V);
-        if (F.Qf) {  // the float results the host receives (8 bytes per cell)
-            F.Qf[idx] = (float)Q;
-            F.sigf[idx] = (float)sqrt(V * F.sig_scale);
+        if (F.Qg) {  // the group's results, [f][group][cell] i fastest
+#pragma unroll
+            for (int s = 0; s < S; ++s) { s_a[ty + kFinRows * s][tx] = mg[s]; s_b[ty + kFinRows * s][tx] = vg[s]; }
+            __syncthreads();
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+                const int jW = j0 + ty + kFinRows * s;
+                if (iW < F.niR && jW < F.njR) {
+                    const long long o = ((long long)f * F.n_groups + g) * F.region_cells +
+                                        ((long long)kR * F.njR + jW) * F.niR + iW;
+                    F.Qg[o] = s_a[tx][ty + kFinRows * s];
+                    F.varg[o] = s_b[tx][ty + kFinRows * s];
+                }
+            }
+            __syncthreads();
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < S; ++s) { s_a[ty + kFinRows * s][tx] = Q[s]; s_b[ty + kFinRows * s][tx] = V[s]; }
+    __syncthreads();
+#pragma unroll
+    for (int s = 0; s < S; ++s) {
+        const int jW = j0 + ty + kFinRows * s;
+        if (iW < F.niR && jW < F.njR) {
+            const double Qc = s_a[tx][ty + kFinRows * s], Vc = s_b[tx][ty + kFinRows * s];
+            const long long idx = (long long)f * F.region_cells + ((long long)kR * F.njR + jW) * F.niR + iW;
+            F.Q[idx] = Qc;
+            F.var[idx] = Vc;
+            if (F.sigma) F.sigma[idx] = sqrt(Vc);
+            if (F.Qf) {  // the float results the host receives (8 bytes per cell)
+                F.Qf[idx] = (float)Qc;
+                F.sigf[idx] = (float)sqrt(Vc * F.sig_scale);
+            }
         }
     }
 }
@@ -353,104 +391,124 @@ __global__ void cv_sur_kernel(const CvParams c) {
     }
 }
 
-// The straight walk of the surrogate: from oW (the centre of layer w0) with
-// wall-normal cosine mu > 0 in direction dW (+1: east), through the layers of
-// constant (k, Ib) = surp[l], advanced layer by layer and stopped when its
-// optical depth exceeds dtoll = ln(1/toll) (the rest is absorbed in that
-// layer) or at the black wall of intensity Iw.  Returns the collected
-// intensity J and the own-layer absorptance A = 1 - (transmissivity leaving
-// layer w0; 0 if the walk stops inside it).
-__device__ __forceinline__ void cv_walk(const float *fw, int nw, float dtoll, const float2 *surp, int w0, float oW,
-                                        float mu, int dW, float Iw, float *J_out, float *A_out) {
-    const float invW = 1.0f / mu;
-    // exit face of layer l at parameter (fw[l + 1] - o)/mu going east and
-    // (fw[l] - o) * (-1/mu) going west
-    const float *fwn = fw + (dW > 0 ? 1 : 0);
-    const float sinvW = dW > 0 ? invW : -invW;
-    const int lwall = dW > 0 ? nw : -1;
-    float J = 0.0f, tauE = 1.0f, tE = 0.0f, dcum = 0.0f, tex0 = -1.0f;
-    int l = w0;
-    float2 kv = __ldg(surp + w0);
-    bool trunc;
-    for (;;) {
-        const float tn = (__ldg(fwn + l) - oW) * sinvW;
-        const float opt = kv.x * (tn - tE);
-        trunc = dcum + opt > dtoll;
-        if (trunc) break;  // truncated in layer l
-        const float as = -mc_expm1(-opt);
-        const float tas = tauE * as;
-        J = fmaf(tas, kv.y, J);
-        tauE = tauE - tas;
-        dcum = dcum + opt;
-        tE = tn;
-        tex0 = tex0 < 0.0f ? tauE : tex0;
-        l += dW;
-        if (l == lwall) break;  // reached the wall
-        kv = __ldg(surp + l);
-    }
-    *J_out = fmaf(tauE, trunc ? kv.y : Iw, J);
-    *A_out = 1.0f - (tex0 < 0.0f ? 0.0f : tex0);
-}
-
-// Surrogate table and its exact means per (field, sample, layer), one warp
-// each: the lanes walk the 2 (kSurBins + 1) nodes (mu = u_m^2, u_m = m /
-// kSurBins; the node u = 0 at mu = 2^-30, the grazing limit), the warp's
-// shared row holds them, and each lane writes kSurBins / 16 bins and their
-// FP64 contribution to the means.  With mu uniform on [0, 1] per hemisphere,
-// u has density 2u, and a bin m contributes
-//   E_h[J] += ((2m + 1) J0 + (m + 2/3) dJ) / kSurBins^2,
-// likewise for A; the warp sums in butterfly order.
+// Surrogate table and its exact means, one block per (field, sample).  The
+// surrogate ray leaves the centre o_l of layer l with wall-normal cosine mu
+// and flies straight through the layers of constant (k, Ib) = sur[l] to the
+// black wall (intensity Iw); what it collects is
+//   J_l = (1 - e^{-h_l}) Ib_l + e^{-h_l} F_{l+1}   (east; west alike),
+// with h_l = k_l (f_{l+1} - o_l) / mu its own half-layer depth and F_i the
+// intensity collected by a ray entering layer i from the west face,
+//   F_i = (1 - e^{-d_i}) Ib_i + e^{-d_i} F_{i+1},  F_nw = Iw,  d_i = k_i (f_{i+1} - f_i) / mu,
+// and its own-layer absorptance is A_l = 1 - e^{-h_l}.  So one sweep per
+// (node, hemisphere) from the far wall gives every layer's node: thread
+// (h, m) sweeps mu = u_m^2 (u_m = m / kSurBins; the node u = 0 at mu =
+// 2^-30, the grazing limit) across the layers, one layer per step, with
+// e^{-x} - 1 = mc_expm1(-x):
+//   J = F + e1h (F - Ib_l),  A = -e1h,  then  F <- F + e1 (F - Ib_l).
+// After each step the block writes the two layers' bins (J0, dJ, A0, dA)
+// and their contributions to the means: with mu uniform on [0, 1] per
+// hemisphere, u has density 2u, and bin m contributes
+//   E_h[J] += ((2m + 1) J0 + (m + 2/3) dJ) / kSurBins^2
+//          = (3 (2m + 1) J0 + (3m + 2) dJ) / (3 kSurBins^2),
+// likewise for A.  The integer-weighted terms are formed exactly as
+// float pairs (the product's rounding error by fma) and summed as float
+// pairs (error-free sums), each hemisphere's 64 terms by two warps in
+// butterfly order, then in FP64: about 48 bits, at FP32 rates (this GPU's
+// FP64 rate is a small fraction of that).
 constexpr int kSurNodes = kSurBins + 1;
-__global__ void cv_table_kernel(const CvParams c) {
-    __shared__ float2 s_node[8][2 * kSurNodes];
-    const long long n = (long long)c.nfields * c.n_samples * c.nw;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const long long wpb = blockDim.x >> 5;
-    float2 *node = s_node[wid];
-    for (long long idx = blockIdx.x * wpb + wid; idx < n; idx += (long long)gridDim.x * wpb) {
-        const int w = (int)(idx % c.nw);
-        const long long fs = idx / c.nw;
-        const int sid = (int)(fs % c.n_samples);
-        const float2 *sp = c.sur + fs * c.nw;
-        const int band = c.mode == MODE_GREY ? 0 : sid / c.nq;
-        const float oW = (__ldg(c.fw + w) + __ldg(c.fw + w + 1)) * 0.5f;
-        for (int e = lane; e < 2 * kSurNodes; e += 32) {
-            const int h = e >= kSurNodes ? 1 : 0;
-            const int m = e - h * kSurNodes;
-            const float u = (float)m * (1.0f / (float)kSurBins);
-            const float mu = m ? u * u : 9.31322574615478516e-10f;  // 2^-30
-            const float Iw = c.mode == MODE_GREY ? c.Tw4[h] : __ldg(c.ibw + h * c.nbands + band);
-            float J, A;
-            cv_walk(c.fw, c.nw, c.dtoll, sp, w, oW, mu, h ? 1 : -1, Iw, &J, &A);
-            node[e] = make_float2(J, A);
+
+// (hi, lo) float pairs: the sum of two pairs, renormalised; the file is
+// compiled without FMA contraction, so the error-free steps stay exact
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    float e = (a.x - (s - bb)) + (b.x - bb);
+    e = e + (a.y + b.y);
+    const float hi = s + e;
+    return make_float2(hi, e - (hi - s));
+}
+// w * v as an exact pair (w a small integer)
+__device__ __forceinline__ float2 ff_mul(float w, float v) {
+    const float p = w * v;
+    return make_float2(p, fmaf(w, v, -p));
+}
+constexpr int kTableThreads = 160;  // 2 kSurNodes sweeps; 2 kSurBins bins
+size_t cv_table_smem(int nw) { return (size_t)nw * (2 * sizeof(double2) + sizeof(float2) + sizeof(float)) + 16; }
+
+__global__ void __launch_bounds__(kTableThreads) cv_table_kernel(const CvParams c) {
+    extern __shared__ double2 s_mean[];                    // [nw][2] per-hemisphere sums (eJ, eA)
+    float2 *s_sur = reinterpret_cast<float2 *>(s_mean + 2 * c.nw);  // [nw] (k, Ib)
+    float *s_fw = reinterpret_cast<float *>(s_sur + c.nw);  // [nw + 1] faces
+    __shared__ float2 s_val[2][kSurNodes];                 // this step's nodes (J, A)
+    __shared__ double2 s_half[4];                          // this step's warp sums
+    const int t = threadIdx.x, nw = c.nw;
+    const long long fs = blockIdx.x;                       // field * n_samples + sample
+    const int sid = (int)(fs % c.n_samples);
+    const int band = c.mode == MODE_GREY ? 0 : sid / c.nq;
+    const float2 *sp = c.sur + fs * nw;
+    for (int i = t; i < nw; i += kTableThreads) s_sur[i] = sp[i];
+    for (int i = t; i <= nw; i += kTableThreads) s_fw[i] = c.fw[i];
+    // sweep thread: hemisphere h (0: towards the west wall), node m
+    const int h = t >= kSurNodes ? 1 : 0, m = t - h * kSurNodes;
+    float invmu = 0.0f, F = 0.0f;
+    if (t < 2 * kSurNodes) {
+        const float u = (float)m * (1.0f / (float)kSurBins);
+        const float mu = m ? u * u : 9.31322574615478516e-10f;  // 2^-30
+        invmu = 1.0f / mu;
+        F = c.mode == MODE_GREY ? c.Tw4[h] : __ldg(c.ibw + h * c.nbands + band);
+    }
+    __syncthreads();
+    for (int step = 0; step < nw; ++step) {
+        if (t < 2 * kSurNodes) {
+            const int l = h ? nw - 1 - step : step;
+            const float2 kv = s_sur[l];
+            const float f0 = s_fw[l], f1 = s_fw[l + 1];
+            const float o = (f0 + f1) * 0.5f;
+            const float half = h ? (f1 - o) * invmu : (o - f0) * invmu;
+            const float e1h = mc_expm1(-(kv.x * half));
+            s_val[h][m] = make_float2(fmaf(e1h, F - kv.y, F), -e1h);
+            const float e1 = mc_expm1(-(kv.x * ((f1 - f0) * invmu)));
+            F = fmaf(e1, F - kv.y, F);
         }
-        __syncwarp();
-        float4 *row = c.surtab + idx * (2 * kSurBins);
-        double eJ = 0.0, eA = 0.0;
-#pragma unroll
-        for (int j = 0; j < (2 * kSurBins) / 32; ++j) {
-            const int bi = lane + 32 * j;
-            const int h = bi >= kSurBins ? 1 : 0;
-            const int m = bi - h * kSurBins;
-            const float2 v0 = node[h * kSurNodes + m], v1 = node[h * kSurNodes + m + 1];
+        __syncthreads();
+        if (t < 2 * kSurBins) {
+            const int hb = t / kSurBins, mb = t - hb * kSurBins;
+            const int l = hb ? nw - 1 - step : step;
+            const float2 v0 = s_val[hb][mb], v1 = s_val[hb][mb + 1];
             const float dJ = v1.x - v0.x, dA = v1.y - v0.y;
-            row[bi] = make_float4(v0.x, dJ, v0.y, dA);
-            const double c0 = (double)(2 * m + 1), c1 = (double)m + 2.0 / 3.0;
-            eJ += c0 * (double)v0.x + c1 * (double)dJ;
-            eA += c0 * (double)v0.y + c1 * (double)dA;
+            c.surtab[(fs * nw + l) * (2 * kSurBins) + t] = make_float4(v0.x, dJ, v0.y, dA);
+            const float w0 = (float)(3 * (2 * mb + 1)), w1 = (float)(3 * mb + 2);
+            float2 eJ = ff_add(ff_mul(w0, v0.x), ff_mul(w1, dJ));
+            float2 eA = ff_add(ff_mul(w0, v0.y), ff_mul(w1, dA));
+            for (int o = 16; o > 0; o >>= 1) {
+                float2 pJ, pA;
+                pJ.x = __shfl_xor_sync(0xffffffffu, eJ.x, o);
+                pJ.y = __shfl_xor_sync(0xffffffffu, eJ.y, o);
+                pA.x = __shfl_xor_sync(0xffffffffu, eA.x, o);
+                pA.y = __shfl_xor_sync(0xffffffffu, eA.y, o);
+                eJ = ff_add(eJ, pJ);
+                eA = ff_add(eA, pA);
+            }
+            if ((t & 31) == 0)
+                s_half[t >> 5] = make_double2((double)eJ.x + (double)eJ.y, (double)eA.x + (double)eA.y);
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            eJ += __shfl_xor_sync(0xffffffffu, eJ, o);
-            eA += __shfl_xor_sync(0xffffffffu, eA, o);
+        __syncthreads();
+        if (t < 2) {  // the step's two layers
+            const int l = t ? nw - 1 - step : step;
+            s_mean[2 * l + t] = make_double2(s_half[2 * t].x + s_half[2 * t + 1].x,
+                                             s_half[2 * t].y + s_half[2 * t + 1].y);
         }
-        if (lane == 0) {
-            const double sc = 0.5 / ((double)kSurBins * (double)kSurBins);  // both hemispheres, weight 1/2
-            const double J = eJ * sc, A = eA * sc;
-            const float Jhi = (float)J;
-            c.Jhat[idx] = make_double2(J, A);
-            c.Jf[idx] = make_float4(Jhi, (float)(J - (double)Jhi), (float)A, sp[w].y);
-        }
-        __syncwarp();
+    }
+    __syncthreads();
+    // both hemispheres, weight 1/2; the sums carry the factor 3
+    const double sc = 0.5 / (3.0 * (double)kSurBins * (double)kSurBins);
+    for (int l = t; l < nw; l += kTableThreads) {
+        const double2 a = s_mean[2 * l], b = s_mean[2 * l + 1];
+        const double J = (a.x + b.x) * sc, A = (a.y + b.y) * sc;
+        const float Jhi = (float)J;
+        const long long idx = fs * nw + l;
+        c.Jhat[idx] = make_double2(J, A);
+        c.Jf[idx] = make_float4(Jhi, (float)(J - (double)Jhi), (float)A, s_sur[l].y);
     }
 }
 
@@ -541,134 +599,126 @@ __global__ void cv_mean_kernel(const CvParams c) {
 // ---------------------------------------------------------------------------
 // E[Y] through node sums (tables without particles).  With k_s(T, x) the
 // bilinear and Ib_s(T) the linear interpolant of the tables at the cell's
-// table coordinates (weights wt_a in T, wx_b in x),
-//   E[Y_a] = sum_s C_s k_s Ib_s - sum_s C_s Jhat_s(w) k_s,
-//   E[Y_b] = sum_s C_s Ahat_s(w) k_s Ib_s - sum_s C_s Ahat_s(w) Ibar_s(w) k_s,
-// and every sum is a fixed combination of sums over the samples taken at
-// the table nodes:
-//   GJ(w)[t][x]          = sum_s C_s Jhat_s(w) k_s[t][x]
-//   GB(w)[t][x]          = sum_s C_s Ahat_s(w) Ibar_s(w) k_s[t][x]
-//   MB(w)[t][x][a][a']   = sum_s C_s Ahat_s(w) k_s[t+a][x] Ib_s[t+a']
-//   M[t][x][a][a']       = sum_s C_s k_s[t+a][x] Ib_s[t+a']      (no layer)
-// so a cell needs 24 node sums per group instead of a pass over the group's
-// samples.  FP64 throughout (sums over the samples, and the cell's
-// combination): exact to the FP32 rounding of the march's own lookups.
+// table coordinates (weights wt_a in T, wx_b in x; sum_a' wt_a' = 1),
+//   E[Y_a] = sum_s C_s k_s (Ib_s - Jhat_s(w))
+//          = sum_{b,a,a'} wx_b wt_a wt_a' Da(w)[t][x_b][a][a'],
+//   E[Y_b] = sum_s C_s Ahat_s(w) k_s (Ib_s - Ibar_s(w))
+//          = sum_{b,a,a'} wx_b wt_a wt_a' Db(w)[t][x_b][a][a'],
+// with the node sums per (field, group, layer) and table cell (t, x)
+//   Da[t][x][a][a'] = sum_s C_s k_s[t+a][x] (Ib_s[t+a'] - Jhat_s),
+//   Db[t][x][a][a'] = sum_s C_s Ahat_s k_s[t+a][x] (Ib_s[t+a'] - Ibar_s):
+// a cell needs 16 node sums per group instead of a pass over the group's
+// samples, and the differences Ib - Jhat, where optically thick samples
+// cancel, are formed per sample before any sum.  Arithmetic in float pairs
+// (hi + lo, about 48 bits: error-free products by fma and error-free sums;
+// this file is compiled without FMA contraction), at FP32 rates -- this
+// GPU's FP64 rate is a small fraction of them.  The cell's weights are
+// formed in FP64 and its 16-term combination summed in pairs.
 // ---------------------------------------------------------------------------
 struct NodeLayout {
-    int nTX, nM, per;  // nodes, (t cell, x node, a, a') entries, doubles per (field, group, layer)
+    int nTc, per;  // table cells (t, x), pairs per (field, group, layer): Da then Db, 4 each per cell
 };
 __host__ __device__ inline NodeLayout node_layout(const CvParams &c) {
     NodeLayout L;
-    L.nTX = c.nT * c.nX;
-    L.nM = (c.nT - 1) * c.nX * 4;
-    L.per = 2 * L.nTX + L.nM;
+    L.nTc = (c.nT - 1) * c.nX;
+    L.per = L.nTc * 8;
     return L;
 }
 
 long long cv_node_count(const CvParams &c) {
     const NodeLayout L = node_layout(c);
     const long long niR = c.ew1 - c.ew0;
-    return (long long)c.nfields * c.n_groups * niR * L.per + (long long)c.n_groups * L.nM;
+    return (long long)c.nfields * c.n_groups * niR * L.per;
 }
 
-// Blocks: (field, group, region layer), then one per group for M.  Work
-// units of a block: the nodes of GJ and of GB (one sum each), and the table
-// cells (t, x) of MB or M (the four sums over a, a' together).  The tables
-// are read as FP64 copies, the per-sample weights come from shared memory,
-// so a sum costs one FP64 fma per sample (1.5 for MB / M).
-__global__ void cv_nodes_kernel(const CvParams c) {
-    __shared__ int s_band[256];
-    __shared__ int s_koff[256];
-    __shared__ double s_wJ[256], s_wB[256], s_wM[256];
+// a double as a float pair
+__device__ __forceinline__ float2 ff_of(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+// a pair times a float (the low part's product rounded)
+__device__ __forceinline__ float2 ff_mulf(float2 a, float b) {
+    const float p = a.x * b;
+    return make_float2(p, fmaf(a.x, b, -p) + a.y * b);
+}
+// a pair times a pair
+__device__ __forceinline__ float2 ff_mulff(float2 a, float2 b) {
+    const float p = a.x * b.x;
+    return make_float2(p, fmaf(a.x, b.x, -p) + (a.x * b.y + a.y * b.x));
+}
+// a float minus a pair, as a pair
+__device__ __forceinline__ float2 ff_fsub(float a, float2 b) { return ff_add(make_float2(a, 0.0f), make_float2(-b.x, -b.y)); }
+
+// Blocks: (field, group, region layer).  Work units: the table cells (t, x),
+// each with its eight sums, one per thread in rounds of blockDim.  The
+// per-sample weights and the inputs of the differences come from shared
+// memory in chunks of 256 samples.
+__global__ void __launch_bounds__(256) cv_nodes_kernel(const CvParams c) {
+    __shared__ int s_ib[256];      // band * nT
+    __shared__ int s_koff[256];    // sample * nT * nX
+    __shared__ float2 s_C[256], s_CA[256], s_J[256];  // C, C Ahat, Jhat as pairs
+    __shared__ float s_Ibar[256];
     const NodeLayout L = node_layout(c);
     const int niR = c.ew1 - c.ew0;
-    const int nTc = c.nT - 1;  // table cells along T
-    const long long nlay = (long long)c.nfields * c.n_groups * niR;
     const long long b = blockIdx.x;
-    const bool layered = b < nlay;
-    int f = 0, g, w = 0;
-    double *out;
-    if (layered) {
-        const int wR = (int)(b % niR);
-        const long long fg = b / niR;
-        g = (int)(fg % c.n_groups);
-        f = (int)(fg / c.n_groups);
-        w = c.ew0 + wR;
-        out = c.nodes + b * L.per;
-    } else {
-        g = (int)(b - nlay);
-        out = c.nodes + nlay * L.per + (long long)g * L.nM;
-    }
-    // units: [GJ nodes | GB nodes] (layered only), then (t, x) table cells
-    const int nnode = layered ? 2 * L.nTX : 0;
-    const int nunit = nnode + nTc * c.nX;
+    const int wR = (int)(b % niR);
+    const long long fg = b / niR;
+    const int g = (int)(fg % c.n_groups);
+    const int f = (int)(fg / c.n_groups);
+    const int w = c.ew0 + wR;
+    float2 *out = reinterpret_cast<float2 *>(c.nodes) + b * L.per;
     const int q0 = c.grp_start[g], q1 = c.grp_start[g + 1];
-    constexpr int kMaxUnits = 8;
-    double acc[kMaxUnits][4];
+    for (int u0 = 0; u0 < L.nTc; u0 += blockDim.x) {
+        const int u = u0 + threadIdx.x;
+        const int t = u / c.nX, x = u - t * c.nX;
+        float2 acc[8];
 #pragma unroll
-    for (int i = 0; i < kMaxUnits; ++i)
-#pragma unroll
-        for (int r = 0; r < 4; ++r) acc[i][r] = 0.0;
-    for (int qc = q0; qc < q1; qc += 256) {
-        const int nq = min(256, q1 - qc);
-        __syncthreads();
-        if ((int)threadIdx.x < nq) {
-            const int q = qc + threadIdx.x;
-            const int sid = c.samp_id[q];
-            const double C = c.samp_C[q];
-            s_band[threadIdx.x] = (sid / c.nq) * c.nT;
-            s_koff[threadIdx.x] = sid * c.nT * c.nX;
-            if (layered) {
+        for (int r = 0; r < 8; ++r) acc[r] = make_float2(0.0f, 0.0f);
+        for (int qc = q0; qc < q1; qc += 256) {
+            const int nq = min(256, q1 - qc);
+            __syncthreads();
+            if ((int)threadIdx.x < nq) {
+                const int q = qc + threadIdx.x;
+                const int sid = c.samp_id[q];
+                const double C = c.samp_C[q];
                 const long long o = ((long long)f * c.n_samples + sid) * c.nw + w;
                 const double2 jh = c.Jhat[o];
-                s_wJ[threadIdx.x] = C * jh.x;
-                s_wB[threadIdx.x] = C * jh.y * (double)c.sur[o].y;
-                s_wM[threadIdx.x] = C * jh.y;
-            } else {
-                s_wM[threadIdx.x] = C;
+                s_ib[threadIdx.x] = (sid / c.nq) * c.nT;
+                s_koff[threadIdx.x] = sid * c.nT * c.nX;
+                s_C[threadIdx.x] = ff_of(C);
+                s_CA[threadIdx.x] = ff_of(C * jh.y);
+                s_J[threadIdx.x] = ff_of(jh.x);
+                s_Ibar[threadIdx.x] = c.sur[o].y;
+            }
+            __syncthreads();
+            if (u >= L.nTc) continue;
+            for (int j = 0; j < nq; ++j) {
+                const float *kk = c.ktab + s_koff[j] + t * c.nX + x;
+                const float *ib = c.ibtab + s_ib[j] + t;
+                const float k0 = __ldg(kk), k1 = __ldg(kk + c.nX);
+                const float i0 = __ldg(ib), i1 = __ldg(ib + 1);
+                const float2 J = s_J[j];
+                const float Ibar = s_Ibar[j];
+                const float2 da0 = ff_fsub(i0, J), da1 = ff_fsub(i1, J);
+                const float2 db0 = ff_fsub(i0, make_float2(Ibar, 0.0f)), db1 = ff_fsub(i1, make_float2(Ibar, 0.0f));
+                const float2 ck0 = ff_mulf(s_C[j], k0), ck1 = ff_mulf(s_C[j], k1);
+                const float2 ca0 = ff_mulf(s_CA[j], k0), ca1 = ff_mulf(s_CA[j], k1);
+                acc[0] = ff_add(acc[0], ff_mulff(ck0, da0));
+                acc[1] = ff_add(acc[1], ff_mulff(ck0, da1));
+                acc[2] = ff_add(acc[2], ff_mulff(ck1, da0));
+                acc[3] = ff_add(acc[3], ff_mulff(ck1, da1));
+                acc[4] = ff_add(acc[4], ff_mulff(ca0, db0));
+                acc[5] = ff_add(acc[5], ff_mulff(ca0, db1));
+                acc[6] = ff_add(acc[6], ff_mulff(ca1, db0));
+                acc[7] = ff_add(acc[7], ff_mulff(ca1, db1));
             }
         }
-        __syncthreads();
+        if (u < L.nTc) {  // layout: Da [t][x][a*2 + a'], then Db alike
 #pragma unroll
-        for (int i = 0; i < kMaxUnits; ++i) {
-            const int u = threadIdx.x + i * blockDim.x;
-            if (u >= nunit) break;
-            if (u < nnode) {  // GJ or GB at node n
-                const bool gb = u >= L.nTX;
-                const int n = gb ? u - L.nTX : u;
-                const double *wv = gb ? s_wB : s_wJ;
-                double sum = acc[i][0];
-                for (int j = 0; j < nq; ++j) sum = fma(wv[j], __ldg(c.ktab_d + s_koff[j] + n), sum);
-                acc[i][0] = sum;
-            } else {  // table cell (t, x): sums over a, a' of k[t+a][x] Ib[t+a']
-                const int m = u - nnode;
-                const int t = m / c.nX, x = m - t * c.nX;
-                double s00 = acc[i][0], s01 = acc[i][1], s10 = acc[i][2], s11 = acc[i][3];
-                for (int j = 0; j < nq; ++j) {
-                    const double *kk = c.ktab_d + s_koff[j] + t * c.nX + x;
-                    const double *ib = c.ibtab_d + s_band[j] + t;
-                    const double k0 = s_wM[j] * __ldg(kk), k1 = s_wM[j] * __ldg(kk + c.nX);
-                    const double i0 = __ldg(ib), i1 = __ldg(ib + 1);
-                    s00 = fma(k0, i0, s00);
-                    s01 = fma(k0, i1, s01);
-                    s10 = fma(k1, i0, s10);
-                    s11 = fma(k1, i1, s11);
-                }
-                acc[i][0] = s00; acc[i][1] = s01; acc[i][2] = s10; acc[i][3] = s11;
+            for (int r = 0; r < 4; ++r) {
+                out[(long long)u * 4 + r] = acc[r];
+                out[(long long)L.nTc * 4 + (long long)u * 4 + r] = acc[4 + r];
             }
-        }
-    }
-    // layout: GJ [nTX], GB [nTX], then MB / M [t][x][a*2 + a']
-    double *mout = out + (layered ? 2 * L.nTX : 0);
-#pragma unroll
-    for (int i = 0; i < kMaxUnits; ++i) {
-        const int u = threadIdx.x + i * blockDim.x;
-        if (u >= nunit) break;
-        if (u < nnode) {
-            out[u] = acc[i][0];
-        } else {
-            double *o = mout + (long long)(u - nnode) * 4;
-            o[0] = acc[i][0]; o[1] = acc[i][1]; o[2] = acc[i][2]; o[3] = acc[i][3];
         }
     }
 }
@@ -679,7 +729,6 @@ __global__ void cv_mean_nodes_kernel(const CvParams c) {
     const int njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0, niR = c.ew1 - c.ew0;
     const long long n = (long long)c.nfields * c.region_cells;
     const long long plane = (long long)c.na * c.nb;
-    const double *M = c.nodes + (long long)c.nfields * c.n_groups * niR * L.per;
     for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
          idx += (long long)gridDim.x * blockDim.x) {
         const int f = (int)(idx / c.region_cells);
@@ -701,34 +750,27 @@ __global__ void cv_mean_nodes_kernel(const CvParams c) {
         const double wt[2] = {1.0 - ft, ft};
         const double wx[2] = {1.0 - fx, fx};
         const int nb = c.nX > 1 ? 2 : 1;
-        // the cell's interpolation weights, formed once for all groups:
-        // w4[bx][a][a'] = wx[bx] wt[a] wt[a'] (the product of the k and Ib
-        // interpolations) and w2[bx][a] = wx[bx] wt[a]
-        double w4[2][4], w2[2][2];
+        // the cell's interpolation weights w4[bx][a][a'] = wx[bx] wt[a] wt[a']
+        // (the product of the k and Ib interpolations), formed once for all
+        // groups
+        float2 w4[2][4];
         for (int bx = 0; bx < nb; ++bx)
-            for (int a = 0; a < 2; ++a) {
-                w2[bx][a] = wx[bx] * wt[a];
-                for (int a2 = 0; a2 < 2; ++a2) w4[bx][a * 2 + a2] = w2[bx][a] * wt[a2];
-            }
+            for (int a = 0; a < 2; ++a)
+                for (int a2 = 0; a2 < 2; ++a2) w4[bx][a * 2 + a2] = ff_of(wx[bx] * wt[a] * wt[a2]);
         for (int g = 0; g < c.n_groups; ++g) {
-            const double *lay = c.nodes + (((long long)f * c.n_groups + g) * niR + iR) * L.per;
-            const double *GJ = lay, *GB = lay + L.nTX, *MB = lay + 2 * L.nTX;
-            const double *Mg = M + (long long)g * L.nM;
-            double kI = 0.0, kJ = 0.0, kIA = 0.0, kB = 0.0;
+            const float2 *lay = reinterpret_cast<const float2 *>(c.nodes) +
+                                (((long long)f * c.n_groups + g) * niR + iR) * L.per;
+            float2 ea = make_float2(0.0f, 0.0f), eb = make_float2(0.0f, 0.0f);
             for (int bx = 0; bx < nb; ++bx) {
-                const int xn = xi + bx;
-                const double *m = Mg + ((long long)ti * c.nX + xn) * 4;
-                const double *mb = MB + ((long long)ti * c.nX + xn) * 4;
+                const long long o = ((long long)ti * c.nX + xi + bx) * 4;
+#pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    kI = fma(w4[bx][q], m[q], kI);
-                    kIA = fma(w4[bx][q], mb[q], kIA);
-                }
-                for (int a = 0; a < 2; ++a) {
-                    kJ = fma(w2[bx][a], GJ[(ti + a) * c.nX + xn], kJ);
-                    kB = fma(w2[bx][a], GB[(ti + a) * c.nX + xn], kB);
+                    ea = ff_add(ea, ff_mulff(w4[bx][q], __ldg(lay + o + q)));
+                    eb = ff_add(eb, ff_mulff(w4[bx][q], __ldg(lay + (long long)L.nTc * 4 + o + q)));
                 }
             }
-            c.muY[((long long)f * c.n_groups + g) * c.region_cells + tc] = make_double2(kI - kJ, kIA - kB);
+            c.muY[((long long)f * c.n_groups + g) * c.region_cells + tc] =
+                make_double2((double)ea.x + (double)ea.y, (double)eb.x + (double)eb.y);
         }
     }
 }
@@ -863,7 +905,13 @@ int launch_cv_prepare(const CvParams &c, void *stream) {
     dnsmc::note_launch();
     cv_sur_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
     dnsmc::note_launch();
-    cv_table_kernel<<<grid_for(n * 32, 256), 256, 0, st>>>(c);  // one warp per (field, sample, layer)
+    // one block per (field, sample)
+    const size_t smem = cv_table_smem(c.nw);
+    if (smem > 48 * 1024) {
+        const cudaError_t e = cudaFuncSetAttribute(cv_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
+    cv_table_kernel<<<(unsigned)((long long)c.nfields * c.n_samples), kTableThreads, smem, st>>>(c);
     return (int)cudaGetLastError();
 }
 
@@ -871,7 +919,7 @@ int launch_cv_mean(const CvParams &c, void *stream) {
     const long long n = (long long)c.nfields * c.region_cells;
     cudaStream_t st = (cudaStream_t)stream;
     if (c.nodes) {  // tables without particles: node sums, then the cells
-        const long long blocks = (long long)c.nfields * c.n_groups * (c.ew1 - c.ew0) + c.n_groups;
+        const long long blocks = (long long)c.nfields * c.n_groups * (c.ew1 - c.ew0);
         dnsmc::note_launch();
         cv_nodes_kernel<<<(unsigned)blocks, 256, 0, st>>>(c);
         dnsmc::note_launch();
@@ -914,9 +962,10 @@ int launch_finalize(const FinalizeParams &p, void *stream) {
         dnsmc::note_launch();
         ray_reciprocals_kernel<<<grid_for(nr, 256), 256, 0, st>>>(q.rays_per_packet, nr, q.rcp);
     }
-    const long long n = (long long)q.nfields * q.region_cells;
+    const unsigned tiles = (unsigned)(((q.njR + kFinTile - 1) / kFinTile) * ((q.niR + kFinTile - 1) / kFinTile));
+    if (tiles == 0 || q.nkR <= 0 || q.nfields <= 0) return (int)cudaGetLastError();
     dnsmc::note_launch();
-    finalize_kernel<<<grid_for(n, 256), 256, 0, st>>>(q);
+    finalize_kernel<<<dim3(tiles, (unsigned)q.nkR, (unsigned)q.nfields), kFinTile * kFinRows, 0, st>>>(q);
     return (int)cudaGetLastError();
 }
 

@@ -1332,11 +1332,17 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
 }
 
 // The control variate's surrogate table (the device's cv_table_kernel), in
-// FP32: per (field, sample, layer l) and hemisphere h (0: west, 1: east) the
-// walk of sur_walk from the centre of l at the nodes mu = (m / kSurBinsO)^2,
-// m = 0 .. kSurBinsO (m = 0 at mu = 2^-30), over the layer-mean medium
-// (sur_k, sur_I) with black walls (grey: T_wall^4, tables: ibw); each bin m
-// stored as (J0, dJ, A0, dA) = (J(m), J(m+1) - J(m), A(m), A(m+1) - A(m)).
+// FP32: per (field, sample) and hemisphere h (0: towards the west wall, 1:
+// east) and node mu = (m / kSurBinsO)^2, m = 0 .. kSurBinsO (m = 0 at mu =
+// 2^-30), one sweep from the far black wall (grey: T_wall^4, tables: ibw)
+// through the layer-mean medium (sur_k, sur_I) gives every layer's
+// straight flight from its centre:
+//   J_l = F + e1h (F - Ib_l), A_l = -e1h, then F <- F + e1 (F - Ib_l),
+// e1h = expm1(-k_l h_l / mu) over the own half layer towards the wall,
+// e1 = expm1(-k_l (f_{l+1} - f_l) / mu) over the whole layer, F starting at
+// the wall's intensity (F: the intensity collected by a ray entering the
+// layer from the side away from the wall).  Each bin m stored as (J0, dJ,
+// A0, dA) = (J(m), J(m+1) - J(m), A(m), A(m+1) - A(m)).
 // tab: [f][sample][nw][2][kSurBinsO][4].  JA (or NULL): [f][sample][nw][2]
 // the exact means of the interpolant over mu uniform on [-1, 1]: with u =
 // sqrt(|mu|) of density 2u, bin m weighs ((2m+1) J0 + (m + 2/3) dJ) /
@@ -1344,37 +1350,47 @@ int orc_packet_mc(const OrcPacketConfig *c, int nthreads, double *tally, double 
 int orc_cv_table(const OrcPacketConfig *c, float *tab, double *JA) {
     if (!c || !c->sur_k || !c->sur_I || !tab) return 1;
     const int nw = c->nw, nsamp = c->mode == 0 ? 1 : c->nbands * c->nq, NB = kSurBinsO;
-    const float dtoll = (float)(-std::log((double)c->toll));
     const float tw = c->T_west, te = c->T_east;
     const float Tw4[2] = {tw * tw * tw * tw, te * te * te * te};
 #pragma omp parallel for schedule(dynamic, 4)
     for (long long fs = 0; fs < (long long)c->nfields * nsamp; ++fs) {
         const int band = c->mode == 0 ? 0 : (int)(fs % nsamp) / c->nq;
         const float *sk = c->sur_k + (size_t)fs * nw, *sI = c->sur_I + (size_t)fs * nw;
-        for (int l = 0; l < nw; ++l) {
-            const float oW = (c->fw[l] + c->fw[l + 1]) * 0.5f;
-            float J[2][kSurBinsO + 1], A[2][kSurBinsO + 1];
-            for (int h = 0; h < 2; ++h) {
-                const float Iw = c->mode == 0 ? Tw4[h] : c->ibw[h * c->nbands + band];
-                for (int m = 0; m <= NB; ++m) {
-                    const float u = (float)m * (1.0f / (float)NB);
-                    const float mu = m ? u * u : 9.31322574615478516e-10f;
-                    sur_walk<float>(c->fw, nw, dtoll, sk, sI, l, oW, mu, h ? 1 : -1, Iw, &J[h][m], &A[h][m]);
+        std::vector<float> J((size_t)nw * 2 * (NB + 1)), A(J.size());  // [l][h][m]
+        for (int h = 0; h < 2; ++h)
+            for (int m = 0; m <= NB; ++m) {
+                const float u = (float)m * (1.0f / (float)NB);
+                const float mu = m ? u * u : 9.31322574615478516e-10f;
+                const float invmu = 1.0f / mu;
+                float F = c->mode == 0 ? Tw4[h] : c->ibw[h * c->nbands + band];
+                for (int step = 0; step < nw; ++step) {
+                    const int l = h ? nw - 1 - step : step;
+                    const float f0 = c->fw[l], f1 = c->fw[l + 1];
+                    const float o = (f0 + f1) * 0.5f;
+                    const float half = h ? (f1 - o) * invmu : (o - f0) * invmu;
+                    const float e1h = p_expm1(-(sk[l] * half));
+                    J[((size_t)l * 2 + h) * (NB + 1) + m] = fmaf(e1h, F - sI[l], F);
+                    A[((size_t)l * 2 + h) * (NB + 1) + m] = -e1h;
+                    const float e1 = p_expm1(-(sk[l] * ((f1 - f0) * invmu)));
+                    F = fmaf(e1, F - sI[l], F);
                 }
             }
+        for (int l = 0; l < nw; ++l) {
             float *row = tab + ((size_t)fs * nw + l) * 2 * NB * 4;
             double eJ = 0, eA = 0;
-            for (int h = 0; h < 2; ++h)
+            for (int h = 0; h < 2; ++h) {
+                const float *Jr = &J[((size_t)l * 2 + h) * (NB + 1)], *Ar = &A[((size_t)l * 2 + h) * (NB + 1)];
                 for (int m = 0; m < NB; ++m) {
                     float *e = row + (h * NB + m) * 4;
-                    e[0] = J[h][m];
-                    e[1] = J[h][m + 1] - J[h][m];
-                    e[2] = A[h][m];
-                    e[3] = A[h][m + 1] - A[h][m];
+                    e[0] = Jr[m];
+                    e[1] = Jr[m + 1] - Jr[m];
+                    e[2] = Ar[m];
+                    e[3] = Ar[m + 1] - Ar[m];
                     const double c0 = (double)(2 * m + 1), c1 = (double)m + 2.0 / 3.0;
                     eJ += c0 * (double)e[0] + c1 * (double)e[1];
                     eA += c0 * (double)e[2] + c1 * (double)e[3];
                 }
+            }
             if (JA) {
                 const double sc = 0.5 / ((double)NB * (double)NB);
                 JA[2 * ((size_t)fs * nw + l)] = eJ * sc;

@@ -307,8 +307,9 @@ SUR_BINS = 64  # bins per hemisphere of the surrogate table (nodes uniform in sq
 
 
 def cv_table(c):
-    """The control variate's surrogate table of the march (orc_cv_table) for
-    the layer-mean medium c.sur_k / c.sur_I of a PacketConfig: (table
+    """The control variate's surrogate table of the march (orc_cv_table: the
+    untruncated straight flight at the nodes) for the layer-mean medium
+    c.sur_k / c.sur_I of a PacketConfig: (table
     [f, sample, nw, 2, SUR_BINS, 4] float32 of (J0, dJ, A0, dA) per bin,
     means [f, sample, nw, 2] float64 of (Jhat, Ahat))."""
     ns = 1 if c.mode == 0 else c.nbands * c.nq
@@ -333,11 +334,11 @@ def cv_walk(sur_k, sur_I, fw, toll, Iw, l, mu):
     """The surrogate walk in float64: from the centre of layer l with
     wall-normal cosine mu (sign: direction, > 0 towards the east wall of
     intensity Iw[1]) through layers of constant (sur_k, sur_I), stopped once
-    its optical depth exceeds ln(1/toll) (the rest stays in that layer) or at
-    a black wall.  Returns (J, A): collected intensity and own-layer
-    absorptance 1 - t0 (t0 = 0 if it stops inside layer l)."""
+    its optical depth exceeds ln(1/toll) (the rest stays in that layer; toll
+    None: never) or at a black wall.  Returns (J, A): collected intensity and
+    own-layer absorptance 1 - t0 (t0 = 0 if it stops inside layer l)."""
     nw = len(sur_k)
-    dtoll = -math.log(toll)
+    dtoll = math.inf if toll is None else -math.log(toll)
     d = 1 if mu > 0 else -1
     m = abs(mu)
     o = 0.5 * (float(fw[l]) + float(fw[l + 1]))
@@ -364,8 +365,9 @@ def cv_walk(sur_k, sur_I, fw, toll, Iw, l, mu):
 
 def cv_jhat(sur_k, sur_I, fw, toll, Iw_west, Iw_east):
     """For every layer l of a 1-D layered medium (k, Ib per layer; black walls
-    with intensities Iw), the direction means of the surrogate walk (cv_walk)
-    by quadrature (cv_quadrature), in float64:
+    with intensities Iw), the direction means of the surrogate walk (cv_walk;
+    toll None: the untruncated straight flight) by quadrature
+    (cv_quadrature), in float64:
     Jhat[l] = 1/2 int_{-1}^{1} J(mu; l) dmu (absorbed intensity) and
     Ahat[l] = 1/2 int_{-1}^{1} A(mu; l) dmu (own-layer absorptance).
     Returns an (nw, 2) array."""

@@ -64,6 +64,17 @@ def test_bad_config_is_an_error_code(field, value):
     assert e.value.code == _lib.ERR_ARG
 
 
+def test_control_variate_grid_limit():
+    """The surrogate table's sweep keeps per-plane sums in shared memory:
+    imax up to 4096 with the control variate."""
+    c = D.default_config(control_variate=1, imax=4097)
+    with pytest.raises(D.DnsmcError) as e:
+        D.Solver(c)
+    assert e.value.code == _lib.ERR_ARG
+    assert "imax <= 4096" in str(e.value)
+    D.Solver(D.default_config(control_variate=1, imax=4096)).close()
+
+
 def test_config_from_env(monkeypatch):
     lib = _lib.load()
     monkeypatch.setenv("DNSMC_IMAX", "32")

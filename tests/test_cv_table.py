@@ -2,21 +2,24 @@
 the CPU.
 
 The march does not walk the surrogate ray through the layer-mean medium; it
-reads the walk from a table per (field, spectral sample, layer), with nodes
-uniform in u = sqrt(|mu|) on each hemisphere and linear interpolation in u.
-The estimate stays unbiased because E[Y] is the exact mean of that
-interpolant.  Checked here:
+reads the ray's straight flight from a table per (field, spectral sample,
+layer), with nodes uniform in u = sqrt(|mu|) on each hemisphere and linear
+interpolation in u.  The table is built by one sweep per node from the far
+wall (orc_cv_table; the flight is not cut off at ln(1/toll)).  The estimate
+stays unbiased because E[Y] is the exact mean of that interpolant.  Checked
+here:
 
-* the table's nodes are the walk itself (float64 restatement, cv_walk) up to
-  the FP32 rounding of the march;
+* the table's nodes are the flight itself (float64 restatement, cv_walk
+  without cut-off) up to FP32 rounding;
 * the means the oracle returns equal the exact integral of the interpolant
   over mu uniform on [-1, 1], by closed form (int sqrt(mu) dmu) and by a fine
   midpoint sum, both written here independently of the oracle's weights;
 * those means approach the continuous direction means: the analytic
   isothermal-slab result and the float64 quadrature of a layered medium;
-* the interpolant follows the walk between the nodes closely enough for the
-  control variate (the mean squared gap is a small fraction of the walk's
-  own variance over mu).
+* the interpolant follows the flight between the nodes closely enough for
+  the control variate (the mean squared gap is a small fraction of the
+  flight's own variance over mu), and the flight is within the ray cut-off
+  of the truncated walk the 3-D march performs.
 """
 from __future__ import annotations
 
@@ -71,7 +74,7 @@ def test_table_nodes_are_the_walk():
         for h, sgn in ((0, -1.0), (1, 1.0)):
             for m in (0, 1, 7, 32, 63, 64):
                 mu = (m / NB) ** 2 if m else 2.0 ** -30
-                Je, Ae = O.cv_walk(k, I, fw.astype(np.float64), c.toll, Iw, l, sgn * mu)
+                Je, Ae = O.cv_walk(k, I, fw.astype(np.float64), None, Iw, l, sgn * mu)
                 assert abs(J[l, h, m] - Je) <= 2e-5 * Je + 1e-30, (l, h, m, J[l, h, m], Je)
                 assert abs(A[l, h, m] - Ae) <= 2e-5, (l, h, m, A[l, h, m], Ae)
     # the grazing node: everything absorbed in the own layer
@@ -111,7 +114,7 @@ def test_table_means_approach_the_slab_and_the_quadrature():
     nw = 24
     fw = np.linspace(0, 2, nw + 1).astype(np.float32)
     Ib = np.float32(1000.0) ** 4
-    c, keep = config(fw, np.ones(nw, np.float32), np.full(nw, Ib, np.float32), 0.0, 300.0, toll=1e-12)
+    c, keep = config(fw, np.ones(nw, np.float32), np.full(nw, Ib, np.float32), 0.0, 300.0)
     _, JA = O.cv_table(c)
     o = 0.5 * (fw[:-1] + fw[1:]).astype(np.float64)
     ex = Ib - 0.5 * Ib * np.array([O.expn(2, t) for t in o]) \
@@ -121,7 +124,7 @@ def test_table_means_approach_the_slab_and_the_quadrature():
     fw, k, I = layered(nw=20, seed=5)
     c, keep = config(fw, k, I, 600.0, 800.0)
     _, JA = O.cv_table(c)
-    q = O.cv_jhat(k, I, fw.astype(np.float64), c.toll, np.float32(600.0) ** 4, np.float32(800.0) ** 4)
+    q = O.cv_jhat(k, I, fw.astype(np.float64), None, np.float32(600.0) ** 4, np.float32(800.0) ** 4)
     np.testing.assert_allclose(JA[0, 0, :, 0], q[:, 0], rtol=2e-4)
     np.testing.assert_allclose(JA[0, 0, :, 1], q[:, 1], rtol=2e-3, atol=1e-4)
 
@@ -136,7 +139,9 @@ def test_interpolant_follows_the_walk_between_the_nodes():
     for l in (0, 6, 12, 23):
         Je, Ae, Ji, Ai = [], [], [], []
         for mu in mus:
-            J, A = O.cv_walk(k, I, fw.astype(np.float64), c.toll, Iw, l, mu)
+            J, A = O.cv_walk(k, I, fw.astype(np.float64), None, Iw, l, mu)
+            Jt, At = O.cv_walk(k, I, fw.astype(np.float64), c.toll, Iw, l, mu)  # the march's cut-off
+            assert abs(Jt - J) <= c.toll * (I.max() + Iw[0]) and abs(At - A) <= c.toll
             x = math.sqrt(abs(mu)) * NB
             m = min(int(x), NB - 1)
             e = tab[l, 1 if mu > 0 else 0, m]

@@ -1,6 +1,6 @@
 """GPU tests of the control variate (CV): Y is the same ray through the
 medium of plane-averaged T and x_H2O, its flight read from a table of the
-straight walk per (field, spectral sample, plane) and interpolated in
+straight flight per (field, spectral sample, plane) and interpolated in
 sqrt|mu|; the march tallies X - beta*Y and the exact mean beta*E[Y] of the
 tabulated Y is added back.
 
@@ -145,9 +145,9 @@ def test_cv_table_and_mean_match_oracle():
     smp = s.sampling()
     ibw = smp["ibw"].reshape(2, -1)
     nq = 4
-    for sid in (0, 5, 17, 23):  # the continuous walk's means, by quadrature: the tabulated
+    for sid in (0, 5, 17, 23):  # the continuous flight's means, by quadrature: the tabulated
         # surrogate is a close stand-in (its own means are what E[Y] uses)
-        J = O.cv_jhat(cv["sur"][0, sid, :, 0], cv["sur"][0, sid, :, 1], xu, s.cfg.toll, ibw[0, sid // nq],
+        J = O.cv_jhat(cv["sur"][0, sid, :, 0], cv["sur"][0, sid, :, 1], xu, None, ibw[0, sid // nq],
                       ibw[1, sid // nq])
         np.testing.assert_allclose(cv["Jhat"][0, sid, :, 0], J[:, 0], rtol=2e-3)
         np.testing.assert_allclose(cv["Jhat"][0, sid, :, 1], J[:, 1], rtol=5e-3, atol=1e-4)
