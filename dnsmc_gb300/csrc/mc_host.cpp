@@ -319,6 +319,12 @@ struct dnsmc_solver {
     DevBuf<double> d_moments;
     bool beta_set = false;
     int cv_samples = 0;
+    // the spectral sampling tables on the device (entries, group bounds,
+    // wall intensities, control-variate sample lists) and what they were
+    // built from: a solve rebuilds and uploads them only when that changed
+    bool sampling_valid = false, cv_uploaded = false;
+    double sampling_key[8] = {};
+    std::vector<float2> sampling_part;
 
     // outputs
     DevBuf<double2> d_tally;
@@ -848,20 +854,35 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
     const float xm = s->have_x ? (float)(s->xsum / ((double)s->nfields * c.imax * c.jmax * c.kmax)) : 0.f;
     if (!trace) {
         CUDA_TRY(cudaEventRecord(s->ev_solve0, s->stream));
-        if (s->tab.grey_bands) { build_grey_band_tables(s->tab, Tmax); s->tables_dirty = true; }
         s->tmax_used = Tmax;
-        TRY(build_sampling(s, Tmax, xm));
-        if (c.model != DNSMC_MODEL_GREY && s->tables_dirty) TRY(upload_tables(s));
-        if (c.model != DNSMC_MODEL_GREY) {
-            TRY(s->d_entries.ensure(std::max<size_t>(1, s->entries.size())));
-            TRY(s->d_ibw.ensure(s->ibw.size()));
-            CUDA_TRY(cudaMemcpyAsync(s->d_entries.p, s->entries.data(), s->entries.size() * sizeof(SpecEntry), cudaMemcpyHostToDevice, s->stream));
-            CUDA_TRY(cudaMemcpyAsync(s->d_ibw.p, s->ibw.data(), s->ibw.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+        // the sampling tables depend on these, the tables and the particle
+        // optics only; rebuilding them is host work the device would wait for
+        const double skey[8] = {(double)Tmax, (double)xm, s->fv_mean, (double)c.n_groups, (double)c.local_sampling,
+                                (double)c.T_west, (double)c.T_east, (double)c.model};
+        const bool reuse = s->sampling_valid && !s->tables_dirty && !s->tab.grey_bands &&
+                           memcmp(skey, s->sampling_key, sizeof skey) == 0 && s->part.size() == s->sampling_part.size() &&
+                           (s->part.empty() ||
+                            memcmp(s->part.data(), s->sampling_part.data(), s->part.size() * sizeof(float2)) == 0);
+        if (!reuse) {
+            s->sampling_valid = false;
+            if (s->tab.grey_bands) { build_grey_band_tables(s->tab, Tmax); s->tables_dirty = true; }
+            TRY(build_sampling(s, Tmax, xm));
+            if (c.model != DNSMC_MODEL_GREY && s->tables_dirty) TRY(upload_tables(s));
+            if (c.model != DNSMC_MODEL_GREY) {
+                TRY(s->d_entries.ensure(std::max<size_t>(1, s->entries.size())));
+                TRY(s->d_ibw.ensure(s->ibw.size()));
+                CUDA_TRY(cudaMemcpyAsync(s->d_entries.p, s->entries.data(), s->entries.size() * sizeof(SpecEntry), cudaMemcpyHostToDevice, s->stream));
+                CUDA_TRY(cudaMemcpyAsync(s->d_ibw.p, s->ibw.data(), s->ibw.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+            }
+            TRY(s->d_group_start.ensure(s->group_start.size()));
+            TRY(s->d_group_empty.ensure(s->group_empty.size()));
+            CUDA_TRY(cudaMemcpyAsync(s->d_group_start.p, s->group_start.data(), s->group_start.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+            CUDA_TRY(cudaMemcpyAsync(s->d_group_empty.p, s->group_empty.data(), s->group_empty.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+            memcpy(s->sampling_key, skey, sizeof skey);
+            s->sampling_part = s->part;
+            s->sampling_valid = true;
+            s->cv_uploaded = false;
         }
-        TRY(s->d_group_start.ensure(s->group_start.size()));
-        TRY(s->d_group_empty.ensure(s->group_empty.size()));
-        CUDA_TRY(cudaMemcpyAsync(s->d_group_start.p, s->group_start.data(), s->group_start.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
-        CUDA_TRY(cudaMemcpyAsync(s->d_group_empty.p, s->group_empty.data(), s->group_empty.size() * sizeof(int), cudaMemcpyHostToDevice, s->stream));
     }
     const HostTable &t = s->tab;
     int ni, nj, nk, ta, tb, npa, npb, npw;
@@ -1014,7 +1035,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
         TRY(s->d_Jhat.ensure(nsur));
         TRY(s->d_Jf.ensure(nsur));
         TRY(s->d_muY.ensure((size_t)s->nfields * P.n_groups * P.region_cells));
-        if (mode != MODE_GREY) {
+        if (mode != MODE_GREY && !s->cv_uploaded) {
             TRY(s->d_cv_grp.ensure(s->cv_grp.size()));
             TRY(s->d_cv_sid.ensure(std::max<size_t>(1, s->cv_sid.size())));
             TRY(s->d_cv_C.ensure(std::max<size_t>(1, s->cv_C.size())));
@@ -1024,6 +1045,7 @@ int solve_enqueue(dnsmc_solver *s, bool trace, int tf, int tg, int tp, int tr, i
             s->cv_Cf.assign(s->cv_C.begin(), s->cv_C.end());
             TRY(s->d_cv_Cf.ensure(std::max<size_t>(1, s->cv_Cf.size())));
             CUDA_TRY(cudaMemcpyAsync(s->d_cv_Cf.p, s->cv_Cf.data(), s->cv_Cf.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+            s->cv_uploaded = true;
         }
         cp.nfields = s->nfields; cp.nw = c.imax; cp.na = c.jmax; cp.nb = c.kmax;
         cp.fieldT = (mode == MODE_TX) ? nullptr : s->d_fieldT.p;
@@ -1787,6 +1809,7 @@ int dnsmc_prepare_sampling(dnsmc_solver *s, float Tmax, float xmean) {
         return fail(DNSMC_ERR_STATE, "no tables: load or set tables first");
     if (s->tab.grey_bands) { build_grey_band_tables(s->tab, Tmax); s->tables_dirty = true; }
     s->tmax_used = Tmax;
+    s->sampling_valid = false;  // the host tables now differ from the device's: the next solve rebuilds
     return build_sampling(s, Tmax, xmean);
 }
 

@@ -570,3 +570,54 @@ def test_launch_count_counts_every_kernel():
         s.solve(timeout_s=60)
         assert _lib.launch_count() - n0 == 2, graph
     s.close()
+
+
+def test_sampling_tables_follow_fields_tables_and_particles():
+    """A solve rebuilds the spectral sampling tables only when what they are
+    built from changed (Tmax, mean x_H2O, the tables, the particle optics and
+    mean fraction): a solver that solved other fields, another table or
+    other particles first gives the same field, bit for bit, as a fresh one."""
+    tb = synth.ck_table(nbands=8, nq=4, nT=20, nX=4, seed=21)
+    tb2 = synth.ck_table(nbands=8, nq=4, nT=20, nX=4, seed=22)
+    ni, nj, nk = 12, 32, 4
+    cfg = D.default_config(model=D.MODEL_TABLE, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.28, Lz=3.14, stretched_x=0,
+                           T_west=400, T_east=450, seed=13, n_groups=2, local_sampling=1, control_variate=1)
+    T1 = smooth_field(ni, nj, nk, 450, 1500, 4)
+    T2 = smooth_field(ni, nj, nk, 500, 1700, 5)
+    x1 = np.full(T1.shape, 0.1, np.float32)
+    x2 = np.full(T1.shape, 0.14, np.float32)
+
+    def fresh(t, T, x, part=None):
+        s = D.Solver(cfg)
+        s.set_table(t["k"], t["wvc"], t["T0"], t["dT"], dnu=t["dnu"], wq=t["wq"], X0=t["X0"], dX=t["dX"])
+        s.set_fields(T, x)
+        if part is not None:
+            s.set_particles(*part)
+            s.set_particle_field(np.full(T.shape, 1e-5, np.float32))
+        s.set_rays(16)
+        out = s.solve(timeout_s=120)
+        s.close()
+        return out
+
+    s = D.Solver(cfg)
+    s.set_table(tb["k"], tb["wvc"], tb["T0"], tb["dT"], dnu=tb["dnu"], wq=tb["wq"], X0=tb["X0"], dX=tb["dX"])
+    s.set_rays(16)
+    s.set_fields(T1, x1)
+    Q1, _ = s.solve(timeout_s=120)
+    Q1b, _ = s.solve(timeout_s=120)  # the tables are reused
+    np.testing.assert_array_equal(Q1b, Q1)
+    for T, x in ((T2, x1), (T2, x2)):
+        s.set_fields(T, x)
+        Q, S = s.solve(timeout_s=120)
+        Qf, Sf = fresh(tb, T, x)
+        np.testing.assert_array_equal(Q, Qf)
+        np.testing.assert_array_equal(S, Sf)
+    s.set_table(tb2["k"], tb2["wvc"], tb2["T0"], tb2["dT"], dnu=tb2["dnu"], wq=tb2["wq"], X0=tb2["X0"], dX=tb2["dX"])
+    Q, _ = s.solve(timeout_s=120)
+    np.testing.assert_array_equal(Q, fresh(tb2, T2, x2)[0])
+    part = (np.linspace(2e3, 4e3, 8).astype(np.float32), np.linspace(1e3, 2e3, 8).astype(np.float32), 0.5)
+    s.set_particles(*part)
+    s.set_particle_field(np.full(T2.shape, 1e-5, np.float32))
+    Q, _ = s.solve(timeout_s=120)
+    np.testing.assert_array_equal(Q, fresh(tb2, T2, x2, part)[0])
+    s.close()
