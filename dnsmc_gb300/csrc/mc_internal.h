@@ -256,7 +256,7 @@ int launch_march_mg(int mode, const MarchParams &p, int blocks, int threads, voi
 int march_mg_occupancy(int mode, int threads, size_t smem);
 // dynamic shared memory of a march launch with `cells` cells per lane: each
 // warp's table slab (slab_len float2), then per thread and cell the three
-// FP64 sums of the item, then per thread the RQMC replicate's shift (uint4)
+// sums of the item (float pairs, 8 bytes), then per thread the RQMC replicate's shift (uint4)
 inline size_t march_smem(const MarchParams &p, int threads, int cells) {
     return (size_t)((threads + 31) / 32) * (size_t)p.slab_len * 8u + (size_t)threads * (24u * (size_t)cells + 16u);
 }

@@ -417,16 +417,7 @@ __global__ void cv_sur_kernel(const CvParams c) {
 // FP64 rate is a small fraction of that).
 constexpr int kSurNodes = kSurBins + 1;
 
-// (hi, lo) float pairs: the sum of two pairs, renormalised; the file is
-// compiled without FMA contraction, so the error-free steps stay exact
-__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
-    const float s = a.x + b.x;
-    const float bb = s - a.x;
-    float e = (a.x - (s - bb)) + (b.x - bb);
-    e = e + (a.y + b.y);
-    const float hi = s + e;
-    return make_float2(hi, e - (hi - s));
-}
+// (hi, lo) float pairs: ff_add (mc_march.cuh) sums two of them
 // w * v as an exact pair (w a small integer)
 __device__ __forceinline__ float2 ff_mul(float w, float v) {
     const float p = w * v;

@@ -396,23 +396,51 @@ __device__ __forceinline__ void slab_drain(const uint64_t *bar, uint32_t phase) 
     slab_bar_wait(bar, phase, kSlabWaitPolls);
 }
 
-// One ray of a cell into its FP64 sums: the sum, and the sum of squares
-// (iid) or of the squared replicate means (RQMC: *rep holds the running
-// replicate sum, m the ray's index in its replicate of M rays).
-__device__ __forceinline__ void tally_ray(const MarchParams &P, double Xd, int m, int M, double *sum, double *sq,
-                                          double *rep) {
-    *sum += Xd;
+// Float pairs (hi, lo): about 48 bits at FP32 rates (error-free sums; the
+// translation units of the marches are compiled without FMA contraction, so
+// the error terms stay exact).  This GPU's FP64 rate is a small fraction of
+// its FP32 rate, and a warp's FP64 instructions at the end of every ray
+// held the march up.
+__device__ __forceinline__ float2 ff_add(float2 a, float2 b) {
+    const float s = a.x + b.x;
+    const float bb = s - a.x;
+    float e = (a.x - (s - bb)) + (b.x - bb);
+    e = e + (a.y + b.y);
+    const float hi = s + e;
+    return make_float2(hi, e - (hi - s));
+}
+__device__ __forceinline__ float2 ff_addf(float2 a, float b) {
+    const float s = a.x + b;
+    const float bb = s - a.x;
+    float e = (a.x - (s - bb)) + (b - bb);
+    e = e + a.y;
+    const float hi = s + e;
+    return make_float2(hi, e - (hi - s));
+}
+__device__ __forceinline__ double ff_value(float2 a) { return (double)a.x + (double)a.y; }
+
+// One ray of a cell into its sums, as float pairs: the sum, and the sum of
+// squares (iid) or of the squared replicate means (RQMC: *rep holds the
+// running replicate sum, m the ray's index in its replicate of M rays; the
+// mean is the pair divided by M, its remainder exact by fma).
+__device__ __forceinline__ void tally_ray(const MarchParams &P, float X, int m, int M, float2 *sum, float2 *sq,
+                                          float2 *rep) {
+    *sum = ff_addf(*sum, X);
     if (P.sampler) {
-        const double Sb = *rep + Xd;
+        const float2 Sb = ff_addf(*rep, X);
         if (m == M - 1) {  // end of a replicate: accumulate its mean squared
-            const double mb = Sb / M;
-            *sq = fma(mb, mb, *sq);
-            *rep = 0.0;
+            const float Mf = (float)M;
+            const float q = Sb.x / Mf;
+            const float ql = (fmaf(-q, Mf, Sb.x) + Sb.y) / Mf;
+            const float p = q * q;
+            *sq = ff_add(*sq, make_float2(p, fmaf(q, q, -p) + 2.0f * (q * ql)));
+            *rep = make_float2(0.0f, 0.0f);
         } else {
             *rep = Sb;
         }
     } else {
-        *sq = fma(Xd, Xd, *sq);
+        const float p = X * X;
+        *sq = ff_add(*sq, make_float2(p, fmaf(X, X, -p)));
     }
 }
 
@@ -443,8 +471,8 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
     unsigned int flags = 0;
     const int tid = threadIdx.x;
     // dynamic shared memory (march_smem, one cell per lane): this warp's copy
-    // of the current ray's table slab (tabulated models), the item's FP64
-    // sums [3][threads] and the replicate's shift [threads]
+    // of the current ray's table slab (tabulated models), the item's sums as
+    // float pairs [3][threads] and the replicate's shift [threads]
     extern __shared__ float4 s_dyn[];
     const int nthr = blockDim.x;
     float2 *const slk = reinterpret_cast<float2 *>(s_dyn) + (threadIdx.x >> 5) * P.slab_len;
@@ -747,14 +775,17 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
             if (active) {
                 ++my_rays;
                 if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                tally_ray(P, (double)X, m, M, &s_acc[tid], &s_acc[nthr + tid], &s_acc[2 * nthr + tid]);
+                tally_ray(P, X, m, M, reinterpret_cast<float2 *>(&s_acc[tid]), reinterpret_cast<float2 *>(&s_acc[nthr + tid]),
+                          reinterpret_cast<float2 *>(&s_acc[2 * nthr + tid]));
             }
         }
         if (dead) break;  // the item's sums are incomplete; the solve fails
         my_steps += lsteps;
         if (TRACE) return;
         if (P.item_steps && lane == 0) P.item_steps[item] = isteps;
-        if (active) P.tally[cell_out] = make_double2(s_acc[tid], s_acc[nthr + tid]);
+        if (active)
+            P.tally[cell_out] = make_double2(ff_value(*reinterpret_cast<const float2 *>(&s_acc[tid])),
+                                             ff_value(*reinterpret_cast<const float2 *>(&s_acc[nthr + tid])));
     }
     if (dead) slab_drain(sbar, sphase);
     // per-warp counters and status

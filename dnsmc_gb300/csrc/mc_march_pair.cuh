@@ -50,9 +50,9 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
     unsigned long long my_rays = 0, my_steps = 0;
     unsigned int flags = 0;
     // dynamic shared memory (march_smem): this warp's copy of the current
-    // ray's table slab (tabulated models); per-cell FP64 sums of the item
-    // (ray sum, sum of squares or of squared replicate means, current
-    // replicate sum) [3][C][threads] and the replicate's shift [threads] --
+    // ray's table slab (tabulated models); per-cell sums of the item as
+    // float pairs (ray sum, sum of squares or of squared replicate means,
+    // current replicate sum) [3][C][threads] and the replicate's shift [threads] --
     // shared memory, so registers hold the march's own working set
     extern __shared__ float4 s_dyn[];
     const int nthr = blockDim.x;
@@ -381,7 +381,8 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 if (active[k]) {
                     ++my_rays;
                     if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                    tally_ray(P, (double)X, m, M, acc(0, k), acc(1, k), acc(2, k));
+                    tally_ray(P, X, m, M, reinterpret_cast<float2 *>(acc(0, k)), reinterpret_cast<float2 *>(acc(1, k)),
+                              reinterpret_cast<float2 *>(acc(2, k)));
                 }
             }
         }
@@ -393,7 +394,8 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
         for (int k = 0; k < C; ++k) {
             if (!active[k]) continue;
             const long long o = fg * P.region_cells + tcell[k];
-            P.tally[o] = make_double2(*acc(0, k), *acc(1, k));
+            P.tally[o] = make_double2(ff_value(*reinterpret_cast<const float2 *>(acc(0, k))),
+                                      ff_value(*reinterpret_cast<const float2 *>(acc(1, k))));
             if (MOM) {
                 double *out = P.moments + o * 9;
 #pragma unroll
@@ -436,9 +438,9 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
     unsigned long long my_rays = 0, my_steps = 0;
     unsigned int flags = 0;
     // dynamic shared memory (march_smem): this warp's copy of the current
-    // ray's table slab (tabulated models); per-cell FP64 sums of the item
-    // (ray sum, sum of squares or of squared replicate means, current
-    // replicate sum) [3][C][threads] and the replicate's shift [threads] --
+    // ray's table slab (tabulated models); per-cell sums of the item as
+    // float pairs (ray sum, sum of squares or of squared replicate means,
+    // current replicate sum) [3][C][threads] and the replicate's shift [threads] --
     // shared memory, so registers hold the march's own working set
     extern __shared__ float4 s_dyn[];
     const int nthr = blockDim.x;
@@ -860,7 +862,8 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                 if (active[k]) {
                     ++my_rays;
                     if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;
-                    tally_ray(P, (double)X, m, M, acc(0, k), acc(1, k), acc(2, k));
+                    tally_ray(P, X, m, M, reinterpret_cast<float2 *>(acc(0, k)), reinterpret_cast<float2 *>(acc(1, k)),
+                              reinterpret_cast<float2 *>(acc(2, k)));
                 }
             }
         }
@@ -872,7 +875,8 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
         for (int k = 0; k < C; ++k) {
             if (!active[k]) continue;
             const long long o = fg * P.region_cells + tcell[k];
-            P.tally[o] = make_double2(*acc(0, k), *acc(1, k));
+            P.tally[o] = make_double2(ff_value(*reinterpret_cast<const float2 *>(acc(0, k))),
+                                      ff_value(*reinterpret_cast<const float2 *>(acc(1, k))));
             if (MOM) {
                 double *out = P.moments + o * 9;
 #pragma unroll

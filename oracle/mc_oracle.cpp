@@ -31,6 +31,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <type_traits>
 #include <vector>
 #include <algorithm>
 #ifdef _OPENMP
@@ -685,6 +686,28 @@ template <> inline float FMA<float>(float a, float b, float c) { return fmaf(a, 
 // kSurBins): nodes at u = m / kSurBinsO of u = sqrt(|mu|).
 constexpr int kSurBinsO = 64;
 
+// Float pairs (hi, lo) for the per-ray sums of the FP32 replay, the march's
+// ff_add / ff_addf / tally_ray (this file is compiled without FMA
+// contraction, so the error-free steps stay exact).
+struct FPair { float h = 0.0f, l = 0.0f; };
+inline FPair fp_add(FPair a, FPair b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    float e = (a.h - (s - bb)) + (b.h - bb);
+    e = e + (a.l + b.l);
+    const float hi = s + e;
+    return FPair{hi, e - (hi - s)};
+}
+inline FPair fp_addf(FPair a, float b) {
+    const float s = a.h + b;
+    const float bb = s - a.h;
+    float e = (a.h - (s - bb)) + (b - bb);
+    e = e + a.l;
+    const float hi = s + e;
+    return FPair{hi, e - (hi - s)};
+}
+inline double fp_value(FPair a) { return (double)a.h + (double)a.l; }
+
 template <class R> inline R expm1_r(R x);
 template <> inline float expm1_r<float>(float x) { return p_expm1(x); }
 template <> inline double expm1_r<double>(double x) { return std::expm1(x); }
@@ -872,6 +895,9 @@ struct Packet {
         const int Mb = c.sampler == 1 ? std::max(1, N / std::max(1, c.nbatch)) : 1;
         double Sb[128];
         for (int l = 0; l < nl; ++l) Sb[l] = 0.0;
+        // the FP32 replay's sums as the march keeps them: float pairs
+        constexpr bool kPairs = std::is_same<R, float>::value;
+        FPair Sp[128], S2p[128], Sbp[128];
         for (int r = rb; r < re; ++r) {
             uint32_t x[4];
             if (c.sampler == 1) {
@@ -1247,6 +1273,27 @@ struct Packet {
                     X = X - ba * Ya;
                     X = X - bb * Yb;
                 }
+                if constexpr (kPairs) {
+                    const float Xf = (float)X;
+                    Sp[l] = fp_addf(Sp[l], Xf);
+                    if (c.sampler == 1) {
+                        const FPair Sbl = fp_addf(Sbp[l], Xf);
+                        if (r % Mb == Mb - 1) {
+                            const float Mf = (float)Mb;
+                            const float q = Sbl.h / Mf;
+                            const float ql = (fmaf(-q, Mf, Sbl.h) + Sbl.l) / Mf;
+                            const float pq = q * q;
+                            S2p[l] = fp_add(S2p[l], FPair{pq, fmaf(q, q, -pq) + 2.0f * (q * ql)});
+                            Sbp[l] = FPair{};
+                        } else {
+                            Sbp[l] = Sbl;
+                        }
+                    } else {
+                        const float pq = Xf * Xf;
+                        S2p[l] = fp_add(S2p[l], FPair{pq, fmaf(Xf, Xf, -pq)});
+                    }
+                    continue;
+                }
                 const double Xd = (double)X;
                 S[l] += Xd;
                 if (c.sampler == 1) {
@@ -1261,6 +1308,8 @@ struct Packet {
                 }
             }
         }
+        if constexpr (kPairs)
+            for (int l = 0; l < nl; ++l) { S[l] = fp_value(Sp[l]); S2[l] = fp_value(S2p[l]); }
     }
 };
 
