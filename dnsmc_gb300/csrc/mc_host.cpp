@@ -376,6 +376,8 @@ int ensure_device(dnsmc_solver *s) {
         const int rc = upload_sobol_dirs(dirs);
         if (rc) return fail(DNSMC_ERR_CUDA, "Sobol' table upload: %s", cudaGetErrorString((cudaError_t)rc));
     }
+    if (const int rc = cv_table_allow_smem())
+        return fail(DNSMC_ERR_CUDA, "table kernel shared memory: %s", cudaGetErrorString((cudaError_t)rc));
     if (int rc = s->d_fw.ensure(s->fw.size())) return rc;
     CUDA_TRY(cudaMemcpy(s->d_fw.p, s->fw.data(), s->fw.size() * sizeof(float), cudaMemcpyHostToDevice));
     return DNSMC_OK;
@@ -408,8 +410,8 @@ int check_config(const dnsmc_config &c) {
     if (c.cv_moments && !c.control_variate) return fail(DNSMC_ERR_ARG, "cv_moments needs control_variate = 1");
     // the surrogate table's sweep keeps per-plane sums of the whole wall-normal
     // line in shared memory (44 bytes a plane)
-    if (c.control_variate && c.imax > 4096)
-        return fail(DNSMC_ERR_ARG, "the control variate supports imax <= 4096");
+    if (c.control_variate && c.imax > kCvMaxPlanes)
+        return fail(DNSMC_ERR_ARG, "the control variate supports imax <= %d", kCvMaxPlanes);
     if (c.block_threads && c.block_threads != 128 && c.block_threads != 256)
         return fail(DNSMC_ERR_ARG, "block_threads must be 0, 128 or 256");
     if (c.tile_a && c.tile_a != 8 && c.tile_a != 16 && c.tile_a != 32)

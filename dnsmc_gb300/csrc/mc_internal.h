@@ -336,6 +336,8 @@ struct CvParams {
 };
 long long cv_node_count(const CvParams &c);
 int launch_cv_prepare(const CvParams &c, void *stream);
+constexpr int kCvMaxPlanes = 4096;  // wall-normal planes the control variate takes
+int cv_table_allow_smem();          // once per device, before any launch_cv_prepare
 int launch_cv_mean(const CvParams &c, void *stream);
 int upload_sobol_dirs(const uint32_t dirs[4][32]);  // once per device
 int device_sm_count();

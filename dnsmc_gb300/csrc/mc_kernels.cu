@@ -896,14 +896,18 @@ int launch_cv_prepare(const CvParams &c, void *stream) {
     dnsmc::note_launch();
     cv_sur_kernel<<<grid_for(n, 256), 256, 0, st>>>(c);
     dnsmc::note_launch();
-    // one block per (field, sample)
+    // one block per (field, sample); its shared memory beyond 48 KB was
+    // allowed once per device (cv_table_allow_smem), outside any capture
     const size_t smem = cv_table_smem(c.nw);
-    if (smem > 48 * 1024) {
-        const cudaError_t e = cudaFuncSetAttribute(cv_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return (int)e;
-    }
     cv_table_kernel<<<(unsigned)((long long)c.nfields * c.n_samples), kTableThreads, smem, st>>>(c);
     return (int)cudaGetLastError();
+}
+
+// The table kernel's dynamic shared memory for the largest grid the control
+// variate takes (imax 4096), set once per device.
+int cv_table_allow_smem() {
+    return (int)cudaFuncSetAttribute(cv_table_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)cv_table_smem(kCvMaxPlanes));
 }
 
 int launch_cv_mean(const CvParams &c, void *stream) {

@@ -274,3 +274,26 @@ def test_cv_two_term_default_beats_single_term():
         var.append(float((S ** 2).mean()))
         s.close()
     assert var[0] / var[1] > 1.2, var
+
+
+def test_cv_table_with_many_planes():
+    """1500 wall-normal planes: the table's sweep keeps 44 bytes a plane in
+    shared memory (66 KB here, past the default 48 KB), its table equals the
+    oracle's bit for bit and the march's tallies the replay's on a band of
+    planes in the middle."""
+    ni, nj, nk = 1500, 16, 8
+    s = D.Solver(D.default_config(model=D.MODEL_GREY, imax=ni, jmax=nj, kmax=nk, Lx=2.0, Ly=6.28, Lz=3.14,
+                                  stretched_x=1, T_west=300, T_east=500, kappa=3.0, seed=5, control_variate=1))
+    i = (np.arange(ni) + 0.5) / ni
+    T = np.ascontiguousarray(np.broadcast_to((400 + 800 * 4 * i * (1 - i))[None, None, :], (nk, nj, ni)),
+                             dtype=np.float32)
+    s.set_fields(T)
+    s.set_region(700, 708, 0, nj, 0, nk)
+    s.set_rays(16)
+    assert_bitexact_cv(s, T)
+    cv = s.cv_data()
+    c, keep = O.packet_config(s, T[None], None)
+    tab_o, JA_o = O.cv_table(c)
+    np.testing.assert_array_equal(s.cv_table(), tab_o)
+    np.testing.assert_allclose(cv["Jhat"], JA_o, rtol=1e-12, atol=0)
+    s.close()
