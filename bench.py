@@ -35,7 +35,9 @@ committed ncu capture (profiles/march_pair_kernel_ck128_counters.md) and
 the lane-steps and march time of this run, beside its gather rate and DRAM
 traffic.  `c0` is the grey 64^3 channel (plain MC at 1 %, the reference's
 grey-band representation beside the CPU reference on the same tables, and
-the isothermal slab against its analytic E2 solution).
+the isothermal slab against its analytic E2 solution); `c2` the batched
+workload (16 snapshots of 96^3 in one graph-replayed launch, rays from the
+local optical thickness, autotuned launch shape: ms per field at 1 %).
 
 With --gpus N (torchrun), every rank solves its own snapshots (seed = rank):
 cells are independent, no collective is needed; the whole-job value is the
@@ -579,6 +581,12 @@ class Arm:
 
 
 def run_batched(args, flushbuf_mb=256):
+    """The batched workload as the bench's JSON line (--workload batched)."""
+    print(json.dumps(batched_block(args, flushbuf_mb)), flush=True)
+    return 0
+
+
+def batched_block(args, flushbuf_mb=256):
     """16 snapshots of 96^3 (seeds 0-15) in one solve: one persistent march
     launch over all snapshots, replayed from a CUDA graph, rays per packet
     proportional to local optical thickness (64-4096), launch shape and
@@ -676,9 +684,8 @@ def run_batched(args, flushbuf_mb=256):
         "gpu_launches": launches,
         "clocks": clocks,
     }
-    print(json.dumps(out), flush=True)
     s.close()
-    return 0
+    return out
 
 
 def run_c4(args):
@@ -916,6 +923,7 @@ def main():
                          "the isothermal slab; batched: 16 snapshots of 96^3; particles: gas + scattering "
                          "particles with grey walls, 192^3")
     ap.add_argument("--no-c0", action="store_true", help="skip the grey 64^3 block of the default workload")
+    ap.add_argument("--no-c2", action="store_true", help="skip the batched 16 x 96^3 block of the default workload")
     ap.add_argument("--ray-floor", type=int, default=64,
                     help="batched workload: smallest rays per packet of the optical-thickness allocation (64 as "
                          "the configuration names; lower floors let the allocation vary)")
@@ -1000,6 +1008,13 @@ def main():
     c0 = None
     if not args.no_c0 and world == 1:
         c0 = run_c0(max(3, args.steps // 2), args.warmup, flushbuf, with_cpu=not args.no_cpu)
+    c2 = None
+    if not args.no_c2 and world == 1:
+        b = batched_block(args)
+        c2 = {k: b[k] for k in ("value", "unit", "steps", "warmup", "ms_per_step", "march_ms", "rays_per_s",
+                                "gpu_launches", "clocks")}
+        c2["config"] = {k: v for k, v in b["config"].items() if k != "l2"}
+        c2["roofline"] = {k: b["roofline"].get(k) for k in ("bound", "achieved", "peak", "frac", "unit")}
     compare = {}
     if not args.no_compare and not args.rays:
         if args.method != "cv":
@@ -1052,6 +1067,7 @@ def main():
         "gpu_launches": int(r["launches"]),
         "clocks": clocks,
         "c0": c0,
+        "c2": c2,
     }
     print(json.dumps(out), flush=True)
     if net is not None:

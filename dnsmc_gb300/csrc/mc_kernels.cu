@@ -159,10 +159,12 @@ __global__ void __launch_bounds__(kFinTile * kFinRows) finalize_kernel(const Fin
             const long long idx = (long long)f * F.region_cells + ((long long)kR * F.njR + jW) * F.niR + iW;
             F.Q[idx] = Qc;
             F.var[idx] = Vc;
-            if (F.sigma) F.sigma[idx] = sqrt(Vc);
+            const double sd = sqrt(Vc);
+            if (F.sigma) F.sigma[idx] = sd;
             if (F.Qf) {  // the float results the host receives (8 bytes per cell)
                 F.Qf[idx] = (float)Qc;
-                F.sigf[idx] = (float)sqrt(Vc * F.sig_scale);
+                // one FP64 square root per cell when no scale applies
+                F.sigf[idx] = (float)(F.sig_scale == 1.0 ? sd : sqrt(Vc * F.sig_scale));
             }
         }
     }
