@@ -358,6 +358,43 @@ def c0_budget(s, pilot=256):
     return r, e
 
 
+def dropin_e2e(T, rays, steps, warmup):
+    """The grey-band channel through the reference's own call surface: the
+    drop-in pair mc_gpu_ / get_results_ on host arrays in the Fortran
+    layout (ghost layer, code/param.h:110-111), float results; wall clock
+    of one call pair per field."""
+    import ctypes
+    import dnsmc_gb300 as D
+    from dnsmc_gb300 import _lib
+    lib = _lib.load()
+    n = C0_N
+    cfg = D.default_config(model=D.MODEL_GREY_BANDS, imax=n, jmax=n, kmax=n, Lx=2.0, Ly=2 * math.pi, Lz=math.pi,
+                           stretched_x=0, T_west=300.0, T_east=300.0, kappa=1.0, seed=104, sampler=D.SAMPLER_RQMC,
+                           nvar=REPLICATES, photmax=max(1, rays // REPLICATES), p_row=1)
+    _lib.check(lib.dnsmc_dropin_configure(ctypes.byref(cfg), None))
+    Tf = np.zeros((n + 2, n + 2, n + 2), np.float32)
+    Tf[1:-1, 1:-1, 1:-1] = T
+    res = np.zeros_like(Tf)
+    sig = np.zeros_like(Tf)
+    fp = lambda a: a.ctypes.data_as(_lib.c_float_p)
+    ystart = ctypes.c_int(1)
+    for _ in range(max(3, warmup)):
+        lib.mc_gpu_(fp(Tf), ctypes.byref(ystart))
+        lib.get_results_(fp(res), fp(sig))
+    ms = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        lib.mc_gpu_(fp(Tf), ctypes.byref(ystart))
+        lib.get_results_(fp(res), fp(sig))
+        ms.append((time.perf_counter() - t0) * 1e3)
+    lib.dnsmc_dropin_release()
+    Q, S = res[1:-1, 1:-1, 1:-1].astype(np.float64), sig[1:-1, 1:-1, 1:-1].astype(np.float64)
+    return {"ms": float(np.mean(ms)), "rays_per_cell": 2 * (rays // 2), "rms_error": rms_error(Q, S),
+            "calls": "mc_gpu_(T, ystart) + get_results_(res, var) per field, host float arrays "
+                     f"({n + 2}^3 with the ghost layer), wall clock",
+            "h2d_bytes_per_step": int(Tf.nbytes), "d2h_bytes_per_step": int(2 * n ** 3 * 4)}
+
+
 def run_c0(steps, warmup, flushbuf, with_cpu=True):
     """The grey 64^3 channel: T = 300 + 700 (1 - y^2) K + 5 % Fourier
     fluctuation, kappa = 1 per half-height, black walls at 300 K, plain MC
@@ -390,6 +427,8 @@ def run_c0(steps, warmup, flushbuf, with_cpu=True):
     out["gpu_grey_bands"] = {"rays_per_cell": rb, "ms_at_1pct": tb["ms"], "rms_error": tb["rms_error"],
                              "rays_per_s": tb["rays_per_s"],
                              "tables": "the reference's grey tables (code/grey_tables.cpp:19-109), as the CPU arm"}
+    # the same through the reference's call surface, end to end from host arrays
+    out["gpu_grey_bands"]["dropin_e2e"] = dropin_e2e(g["T"], rb, max(1, steps), warmup)
     # isothermal slab against E2
     import dnsmc_gb300 as D
     sl = D.Solver(D.default_config(model=D.MODEL_GREY, imax=C0_N, jmax=C0_N, kmax=C0_N, Lx=2.0, Ly=2 * math.pi,
