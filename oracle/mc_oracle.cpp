@@ -20,11 +20,15 @@
 //      reproducible (colliding seeds, code/mc_gpu.cu:99), so comparisons with
 //      it are statistical.
 //  (2) orc_packet_mc / orc_packet_trace: an independent restatement of the
-//      GB300 packet scheme (32 cells of one wall-normal plane share each
-//      ray's direction and spectral sample) that reproduces the device march
-//      bit for bit in FP32 (same Philox counters, same alias draw, same
-//      fmaf-based polynomial exp/sin/cos), or runs it in FP64.
-//  (3) helpers: Philox4x32-10, the reference grids, the spline.
+//      GB300 packet scheme (32, 64 or 128 cells of one wall-normal plane
+//      share each ray's direction and spectral sample) that reproduces the
+//      device march bit for bit in FP32 (same Philox counters, same alias
+//      draw, same fmaf-based polynomial exp/sin/cos, the same float-pair
+//      per-ray sums), or runs it in FP64; orc_cv_table builds the control
+//      variate's surrogate table by the device's FP32 sweeps, orc_cv_mean
+//      the FP64 solution's own exact means.
+//  (3) helpers: Philox4x32-10, the reference grids, the spline; the
+//      k-distribution of line-by-line spectra (orc_ck_from_lbl).
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
