@@ -5,7 +5,8 @@
 //
 // One CTA per SM, persistent over 128-row tiles; TC_WG warpgroups per CTA,
 // each with its own tile in flight so that one warpgroup's epilogue (bias,
-// GELU, bf16 packing) runs while the tensor core works on the other's layer.
+// GELU, bf16 packing) runs while the tensor core works on the others' layers
+// (three: 0.71 ms for the 2.1M rows of a 128^3 field, two: 0.80 ms).
 // Per tile and warpgroup:
 //
 //   features of its 128 rows (feature_row, one row per thread) or rows of a
@@ -33,8 +34,11 @@
 
 namespace {
 
-constexpr int TC_WG = 2;                 // warpgroups (tiles in flight) per CTA
+constexpr int TC_WG = 3;                 // warpgroups (tiles in flight) per CTA
 constexpr int TC_THREADS = 128 * TC_WG;
+// tensor-memory columns of the CTA: 128 per warpgroup, allocated as a power of two
+constexpr uint32_t TC_TMEM_COLS = TC_WG * 128 <= 128 ? 128 : (TC_WG * 128 <= 256 ? 256 : 512);
+static_assert(TC_WG * 128 <= 512, "tensor memory holds 512 columns");
 constexpr int TC_TILE = 128;             // rows per tile (the MMA's M)
 // shared-memory map (bytes)
 constexpr uint32_t TC_W1 = 0;                                  // [K0/8][HID][8] bf16
@@ -213,7 +217,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const TcParams F)
     for (int e = tid; e < NOUT; e += TC_THREADS) bias[3 * HID + e] = F.P[OFF_B4 + e];
     if (warp == 0) {  // the accumulators of all warpgroups: 128 columns each
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tc_smem(tslot)),
-                     "r"(128 * TC_WG)
+                     "r"(TC_TMEM_COLS)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
@@ -327,7 +331,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_tc_kernel(const TcParams F)
     __syncthreads();
     if (warp == 0) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tslot), "r"(128 * TC_WG)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(*tslot), "r"(TC_TMEM_COLS)
                      : "memory");
     }
 }
