@@ -516,7 +516,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
         const int rowW0 = w0 * plane;
         // own-cell quantities
         const VT vown = load_field<MODE>(P, fbase, rowW0 + bcl * P.na + acl);
-        float Ti4 = 0.f, invTi4 = 0.f, tpos0 = 0.f;
+        float Ti4 = 0.f, tpos0 = 0.f;
         int ti_i = 0, ki_i = 0;
         float ft_i = 0.f, fx_i = 0.f;
         if constexpr (MODE == MODE_GREY) {
@@ -524,7 +524,6 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
             if (!(Ti > 0.0f) && active) flags |= DNSMC_STATUS_BAD_FIELD;
             const float t2 = Ti * Ti;
             Ti4 = t2 * t2;
-            invTi4 = Ti4 > 0.f ? 1.0f / Ti4 : 0.f;
         } else {
             cell_coords<MODE>(vown, &ki_i, &ti_i, &ft_i, &fx_i);
             tpos0 = (float)ti_i + ft_i;  // the clamped table coordinate, exactly
@@ -563,12 +562,12 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
             float sW, sA, sB;
             ray_direction(x, &sW, &sA, &sB);
 
-            // spectral sample and ray weight (the ray's weight is wk * Ii)
-            float wk, Ii, invI;
+            // spectral sample and ray weight (the ray contributes wk D, D the
+            // net exchange in intensity units)
+            float wk, Ii;
             int nbnd = 0;
             if (MODE == MODE_GREY) {
                 Ii = Ti4;
-                invI = invTi4;
                 wk = P.Wgrey;
             } else {
                 const int j = (int)__umulhi(x.z, (uint32_t)K);
@@ -578,7 +577,6 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                 if (!load_slab(P, e.koff, slk, lane, sbar, &sphase, &flags)) { dead = true; break; }
                 const float ki = lookup_k<MODE>(slk, ki_i, ft_i, fx_i);
                 Ii = lookup_ib(sli, ti_i, ft_i);
-                invI = Ii > 0.f ? 1.0f / Ii : 0.f;
                 wk = e.W * ki;
             }
 
@@ -625,7 +623,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                     float kj, gj;
                     if constexpr (MODE == MODE_GREY) {
                         const float t2 = vcur * vcur;
-                        gj = (Ti4 - t2 * t2) * invI;
+                        gj = Ti4 - t2 * t2;
                         kj = P.kappa;
                     } else {
                         int kx, tj;
@@ -633,7 +631,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                         cell_coords<MODE>(vcur, &kx, &tj, &ftj, &fxj);
                         kj = lookup_k<MODE>(slk, kx, ftj, fxj);
                         const float Ibj = lookup_ib(sli, tj, ftj);
-                        gj = (Ii - Ibj) * invI;
+                        gj = Ii - Ibj;
                     }
                     const float alpha = -mc_expm1(-(kj * ds));
                     const float ta = tau * alpha;
@@ -653,7 +651,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                         const int side = ncw < 0 ? 0 : 1;
                         const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
                         if (tau > 0.0f) {
-                            D = fmaf(tau, (Ii - Iw) * invI, D);
+                            D = fmaf(tau, Ii - Iw, D);
                             tau = 0.0f;
                         }
                         break;
@@ -711,7 +709,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                                 float kj, gj;
                                 if constexpr (MODE == MODE_GREY) {
                                     const float t2 = Tc * Tc;
-                                    gj = (Ti4 - t2 * t2) * invI;
+                                    gj = Ti4 - t2 * t2;
                                     kj = P.kappa;
                                 } else {
                                     float pt = (Tc - P.T0) * P.invdT;
@@ -720,7 +718,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                                     float ftj;
                                     pos_split(pt, P.nT, &tj, &ftj);
                                     kj = lookup_k<MODE_T>(slk, tj, ftj, 0.0f);
-                                    gj = (Ii - lookup_ib(sli, tj, ftj)) * invI;
+                                    gj = Ii - lookup_ib(sli, tj, ftj);
                                 }
                                 float dmin = dsx;
                                 if (dmin > dsy) dmin = dsy;
@@ -744,7 +742,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
                                         const int side = ic < 0 ? 0 : 1;
                                         const float Iw = (MODE == MODE_GREY) ? P.Tw4[side]
                                                                              : __ldg(P.ibw + side * P.nbands + nbnd);
-                                        if (tau > 0.0f) D = fmaf(tau, (Ii - Iw) * invI, D);
+                                        if (tau > 0.0f) D = fmaf(tau, Ii - Iw, D);
                                         tau = 0.0f;
                                         ic = ic < 0 ? 0 : nwL - 1;
                                     }
@@ -771,7 +769,7 @@ __global__ void __launch_bounds__(256, DNSMC_MINB) march_mg_kernel(const MarchPa
             }
             if (TRACE && lane == 0) *P.trace_n = steps;
             isteps += (unsigned long long)steps;
-            const float X = (wk * Ii) * D;
+            const float X = wk * D;
             if (active) {
                 ++my_rays;
                 if (!isfinite(X)) flags |= DNSMC_STATUS_NONFINITE;

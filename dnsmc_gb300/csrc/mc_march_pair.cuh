@@ -152,9 +152,9 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             float sW, sA, sB;
             ray_direction(x, &sW, &sA, &sB);
 
-            // spectral sample, each cell's own k, Ib and weight (wk * Ii)
+            // spectral sample, each cell's own k, Ib and weight wk
             int nbnd = 0, sid = 0;
-            float wk[C], Ii[C], invI[C];
+            float wk[C], Ii[C];
             VT vcur[C];
 #pragma unroll
             for (int k = 0; k < C; ++k) vcur[k] = load_field<MODE>(P, fbase, rowW0 + bcl[k] * P.na + acl);
@@ -164,7 +164,6 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     const float Ti = vcur[k];
                     const float t2 = Ti * Ti;
                     Ii[k] = t2 * t2;
-                    invI[k] = Ii[k] > 0.f ? 1.0f / Ii[k] : 0.f;
                     wk[k] = P.Wgrey;
                 }
             } else {
@@ -181,7 +180,6 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     cell_coords<MODE>(vcur[k], &kx, &ti, &ft, &fx);
                     const float ki = lookup_k<MODE>(slk, kx, ft, fx);
                     Ii[k] = lookup_ib(sli, ti, ft);
-                    invI[k] = Ii[k] > 0.f ? 1.0f / Ii[k] : 0.f;
                     wk[k] = e.W * ki;
                 }
             }
@@ -267,7 +265,12 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                 // attenuation and collected intensity of this segment; a cell
                 // already dumped (tau 0) adds exactly nothing.  Per cell:
                 // alpha = -expm1(-k ds), ta = tau alpha, D += ta g,
-                // tau -= ta, with g = (Ii - Ib_j) / Ii.  The two cells of a
+                // tau -= ta, with g = Ii - Ib_j: D is the net exchange in
+                // intensity units and the ray's contribution wk D (the
+                // reference normalises g by Ii and multiplies the ray by Ii
+                // again; without the two the march saves a multiply per
+                // cell-step and a division per ray, and a cell whose Ii
+                // underflows keeps its absorption).  The two cells of a
                 // pair go through paired FP32 instructions with every sign
                 // moved onto an operand whose negation is exact: e =
                 // expm1(k * (t - tn)) = -alpha, nta = tau e = -ta,
@@ -280,7 +283,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                     for (int h = 0; h < 2; ++h) {
                         if constexpr (MODE == MODE_GREY) {
                             const float t2 = vcur[k + h] * vcur[k + h];
-                            ngj[h] = (t2 * t2 - Ii[k + h]) * invI[k + h];
+                            ngj[h] = t2 * t2 - Ii[k + h];
                             kj[h] = P.kappa;
                         } else {
                             int kx, tj;
@@ -288,7 +291,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                             cell_coords<MODE>(vcur[k + h], &kx, &tj, &ftj, &fxj);
                             kj[h] = lookup_k<MODE>(slk, kx, ftj, fxj);
                             const float Ibj = lookup_ib(sli, tj, ftj);
-                            ngj[h] = (Ibj - Ii[k + h]) * invI[k + h];
+                            ngj[h] = Ibj - Ii[k + h];
                         }
                     }
                     const float2 e = mc_expm1_x2(__fmul2_rn(make_float2(kj[0], kj[1]), make_float2(nds, nds)));
@@ -320,7 +323,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
                         const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
 #pragma unroll
                         for (int k = 0; k < C; ++k) {
-                            D[k] = fmaf(tau[k], (Ii[k] - Iw) * invI[k], D[k]);
+                            D[k] = fmaf(tau[k], Ii[k] - Iw, D[k]);
                             tau[k] = 0.0f;
                         }
                         break;
@@ -362,7 +365,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             }
 #pragma unroll
             for (int k = 0; k < C; ++k) {
-                float X = (wk[k] * Ii[k]) * D[k];
+                float X = wk[k] * D[k];
                 if (CV) {
                     // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
                     const float Ya = wk[k] * (Ii[k] - Jbar);
@@ -540,9 +543,9 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
             float sW_e, sA_e, sB_e;  // the emission direction
             ray_direction(x, &sW_e, &sA_e, &sB_e);
 
-            // spectral sample, each cell's own k, Ib and weight (wk * Ii)
+            // spectral sample, each cell's own k, Ib and weight wk
             int nbnd = 0, sid = 0;
-            float wk[C], Ii[C], invI[C];
+            float wk[C], Ii[C];
             VT vcur[C];
             float fvcur[C];  // the particle volume fraction of the current cells
             float pab = 0.0f, psc = 0.0f;  // particle absorption / scattering per unit volume fraction
@@ -558,7 +561,6 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                     const float Ti = vcur[k];
                     const float t2 = Ti * Ti;
                     Ii[k] = t2 * t2;
-                    invI[k] = Ii[k] > 0.f ? 1.0f / Ii[k] : 0.f;
                     wk[k] = P.W4sig * fmaf(fvcur[k], pab, P.kappa);
                 }
             } else {
@@ -577,7 +579,6 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                     float ki = lookup_k<MODE>(slk, kx, ft, fx);
                     ki = fmaf(fvcur[k], pab, ki);
                     Ii[k] = lookup_ib(sli, ti, ft);
-                    invI[k] = Ii[k] > 0.f ? 1.0f / Ii[k] : 0.f;
                     wk[k] = e.W * ki;
                 }
             }
@@ -696,7 +697,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                         lsteps += tau[k + h] > 0.0f ? 1u : 0u;
                         if constexpr (MODE == MODE_GREY) {
                             const float t2 = vcur[k + h] * vcur[k + h];
-                            ngj[h] = (t2 * t2 - Ii[k + h]) * invI[k + h];
+                            ngj[h] = t2 * t2 - Ii[k + h];
                             kj[h] = P.kappa;
                         } else {
                             int kx, tj;
@@ -704,7 +705,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
                             cell_coords<MODE>(vcur[k + h], &kx, &tj, &ftj, &fxj);
                             kj[h] = lookup_k<MODE>(slk, kx, ftj, fxj);
                             const float Ibj = lookup_ib(sli, tj, ftj);
-                            ngj[h] = (Ibj - Ii[k + h]) * invI[k + h];
+                            ngj[h] = Ibj - Ii[k + h];
                         }
                         kj[h] = fmaf(fvcur[k + h], pab, kj[h]);
                     }
@@ -737,7 +738,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
 #pragma unroll
                             for (int k = 0; k < C; ++k) {
                                 if (tau[k] > 0.0f) {
-                                    const float gw = (Ii[k] - Iw) * invI[k];
+                                    const float gw = Ii[k] - Iw;
                                     D[k] = fmaf(tau[k] * eps, gw, D[k]);
                                     tau[k] = eps >= 1.0f ? 0.0f : tau[k] * (1.0f - eps);
                                     if (tau[k] > 0.0f && tau[k] < P.toll) { D[k] = fmaf(tau[k], gw, D[k]); tau[k] = 0.0f; }
@@ -843,7 +844,7 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_gen_kernel(const M
             }
 #pragma unroll
             for (int k = 0; k < C; ++k) {
-                float X = (wk[k] * Ii[k]) * D[k];
+                float X = wk[k] * D[k];
                 if (CV) {
                     // Y_a: the ray through the layer-mean medium; Y_b: its own-layer part
                     const float Ya = wk[k] * (Ii[k] - Jbar);

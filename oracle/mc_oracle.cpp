@@ -872,17 +872,16 @@ struct Packet {
             gs = c.group_start[binoff + G];
             K = c.group_start[binoff + G + 1] - gs;
         }
-        R Ti4[128], invTi4[128], ft_i[128], fx_i[128];
+        R Ti4[128], ft_i[128], fx_i[128];
         int ti_i[128], xi_i[128];
         for (int l = 0; l < nl; ++l) {
             const long long o = cidx(f, w0, a0[l], b0[l]);
             const R Ti = (R)c.fieldT[o];
-            ti_i[l] = xi_i[l] = 0; ft_i[l] = fx_i[l] = 0; Ti4[l] = invTi4[l] = 0;
+            ti_i[l] = xi_i[l] = 0; ft_i[l] = fx_i[l] = 0; Ti4[l] = 0;
             if (c.mode == 2) p_gpos<R>((R)c.fieldX[o], (R)c.X0, invdX, c.nX, &xi_i[l], &fx_i[l]);
             if (c.mode == 0) {
                 const R t2 = Ti * Ti;
                 Ti4[l] = t2 * t2;
-                invTi4[l] = Ti4[l] > 0 ? (R)1 / Ti4[l] : (R)0;
             } else {
                 p_gpos<R>(Ti, (R)c.T0, invdT, c.nT, &ti_i[l], &ft_i[l]);
             }
@@ -931,19 +930,16 @@ struct Packet {
             // general medium: particle coefficients of the band
             R pab = 0, psc = 0;
             if (c.gen && c.part) { pab = (R)c.part[2 * nbnd]; psc = (R)c.part[2 * nbnd + 1]; }
-            R w[128], wk[128], Ii[128], invI[128], tau[128], D[128];
+            R wk[128], Ii[128], tau[128], D[128];
             for (int l = 0; l < nl; ++l) {
                 if (c.mode == 0) {
-                    Ii[l] = Ti4[l]; invI[l] = invTi4[l];
+                    Ii[l] = Ti4[l];
                     wk[l] = c.gen ? W4sig * FMA<R>(fvown[l], pab, (R)c.kappa) : Wgrey;
-                    w[l] = wk[l] * Ti4[l];
                 } else {
                     R ki = kfun(koff, ti_i[l], ft_i[l], xi_i[l], fx_i[l]);
                     if (c.gen) ki = FMA<R>(fvown[l], pab, ki);
                     Ii[l] = ibfun(nbnd, ti_i[l], ft_i[l]);
-                    invI[l] = Ii[l] > 0 ? (R)1 / Ii[l] : (R)0;
                     wk[l] = We * ki;
-                    w[l] = wk[l] * Ii[l];
                 }
                 tau[l] = act[l] ? (R)1 : (R)0;
                 D[l] = 0;
@@ -1008,7 +1004,7 @@ struct Packet {
                 if (c.mode == 0) {
                     const R Tj = (R)c.fieldT[o];
                     const R t2 = Tj * Tj;
-                    *gj = (Ti4[l] - t2 * t2) * invI[l];
+                    *gj = Ti4[l] - t2 * t2;
                     kj = (R)c.kappa;
                 } else {
                     int tj, xj = 0;
@@ -1016,7 +1012,7 @@ struct Packet {
                     if (c.mode == 2) p_gpos<R>((R)c.fieldX[o], (R)c.X0, invdX, c.nX, &xj, &fxj);
                     p_gpos<R>((R)c.fieldT[o], (R)c.T0, invdT, c.nT, &tj, &ftj);
                     kj = kfun(koff, tj, ftj, xj, fxj);
-                    *gj = (Ii[l] - ibfun(nbnd, tj, ftj)) * invI[l];
+                    *gj = Ii[l] - ibfun(nbnd, tj, ftj);
                 }
                 if (c.gen && c.fieldV) kj = FMA<R>((R)c.fieldV[o], pab, kj);
                 return kj;
@@ -1066,7 +1062,7 @@ struct Packet {
                             bool any = false;
                             for (int l = 0; l < nl; ++l) {
                                 if (tau[l] > 0) {
-                                    const R gw = (Ii[l] - Iw) * invI[l];
+                                    const R gw = Ii[l] - Iw;
                                     D[l] = FMA<R>(tau[l] * eps, gw, D[l]);
                                     tau[l] = eps >= (R)1 ? (R)0 : tau[l] * ((R)1 - eps);
                                     if (tau[l] > 0 && tau[l] < (R)c.toll) { D[l] = FMA<R>(tau[l], gw, D[l]); tau[l] = 0; }
@@ -1092,7 +1088,7 @@ struct Packet {
                         }
                         for (int l = 0; l < nl; ++l) {
                             if (!(tau[l] > 0)) continue;
-                            D[l] = FMA<R>(tau[l], (Ii[l] - Iw) * invI[l], D[l]);
+                            D[l] = FMA<R>(tau[l], Ii[l] - Iw, D[l]);
                             tau[l] = 0;
                         }
                         break;
@@ -1193,14 +1189,14 @@ struct Packet {
                                 R kj, gj;
                                 if (c.mode == 0) {
                                     const R t2 = Tc * Tc;
-                                    gj = (Ti4[l] - t2 * t2) * invI[l];
+                                    gj = Ti4[l] - t2 * t2;
                                     kj = (R)c.kappa;
                                 } else {
                                     int tj;
                                     R ftj;
                                     p_gpos<R>(Tc, (R)c.T0, invdT, c.nT, &tj, &ftj);
                                     kj = kfun(koff, tj, ftj, 0, 0);
-                                    gj = (Ii[l] - ibfun(nbnd, tj, ftj)) * invI[l];
+                                    gj = Ii[l] - ibfun(nbnd, tj, ftj);
                                 }
                                 R dmin = dsx;
                                 if (dmin > dsy) dmin = dsy;
@@ -1223,7 +1219,7 @@ struct Packet {
                                     if (ic[l] < 0 || ic[l] >= nwL) {
                                         const int side = ic[l] < 0 ? 0 : 1;
                                         const R Iw = c.mode == 0 ? Tw4[side] : (R)c.ibw[side * c.nbands + nbnd];
-                                        if (tau[l] > 0) D[l] = FMA<R>(tau[l], (Ii[l] - Iw) * invI[l], D[l]);
+                                        if (tau[l] > 0) D[l] = FMA<R>(tau[l], Ii[l] - Iw, D[l]);
                                         tau[l] = 0;
                                         ic[l] = ic[l] < 0 ? 0 : nwL - 1;
                                     }
@@ -1251,7 +1247,7 @@ struct Packet {
             if (nrec) *nrec = stepn;
             for (int l = 0; l < nl; ++l) {
                 if (!act[l]) continue;
-                R X = w[l] * D[l];
+                R X = wk[l] * D[l];
                 if (c.cv) {
                     const int nG = c.mode == 0 ? 1 : c.n_groups;
                     const int niR = c.ew1 - c.ew0, njR = c.ea1 - c.ea0, nkR = c.eb1 - c.eb0;
