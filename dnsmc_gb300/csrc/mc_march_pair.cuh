@@ -224,132 +224,148 @@ __global__ void __launch_bounds__(256, DNSMC_PAIR_MINB) march_pair_kernel(const 
             int life[C];
 #pragma unroll
             for (int k = 0; k < C; ++k) life[k] = 1 << 30;
-            // unrolled by two: the current / next field values alternate
-            // registers instead of being copied every step
-#pragma unroll 2
+            // two steps per pass, each its own copy of the body (the current /
+            // next field values alternate registers instead of being copied),
+            // the warp's exit vote after the second
             for (;;) {
-                const bool sW_ = tW <= tA && tW <= tB;
-                const bool sA_ = !sW_ && tA <= tB;
-                const int axis = sW_ ? 0 : (sA_ ? 1 : 2);
-                const float tn = sW_ ? tW : (sA_ ? tA : tB);
-                const float ds = tn - t;
-                const float nds = t - tn;  // minus the segment length (exact negation)
-                // next cell of the walk, and its field values fetched now; the
-                // axis is the same in every lane, but selects cost fewer
-                // instructions here than branches the compiler must treat as
-                // divergent
-                int ncw, nca, nrowW;
-                int nrowB[C];
-                const bool aW = axis == 0, aA = axis == 1, aB = axis == 2;
-                ncw = aW ? cw + dW : cw;
-                nrowW = aW ? rowW + dRowW : rowW;
-                {
-                    int u = ca + dA;
-                    u = u == wrapA ? resetA : u;
-                    nca = aA ? u : ca;
-                }
 #pragma unroll
-                for (int k = 0; k < C; ++k) {
-                    int u = rowB[k] + dRowB;
-                    u = u == wrapRowB ? resetRowB : u;
-                    nrowB[k] = aB ? u : rowB[k];
-                }
-                const bool wall = aW && ncw == wallW;
-                // fetched for every cell, live or not (a dumped cell's value
-                // is never used): no default copy, no per-cell predicate; at
-                // a wall the row stays inside the grid and the walk ends
-                const int lrowW = wall ? rowW : nrowW;
-                VT vnext[C];
+                for (int u = 0; u < 2; ++u) {
+                    const bool sW_ = tW <= tA && tW <= tB;
+                    const bool sA_ = !sW_ && tA <= tB;
+                    const int axis = sW_ ? 0 : (sA_ ? 1 : 2);
+                    const float tn = sW_ ? tW : (sA_ ? tA : tB);
+                    const float ds = tn - t;
+                    const float nds = t - tn;  // minus the segment length (exact negation)
+                    // next cell of the walk, and its field values fetched now; the
+                    // axis is the same in every lane, but selects cost fewer
+                    // instructions here than branches the compiler must treat as
+                    // divergent
+                    int ncw, nca, nrowW;
+                    int nrowB[C];
+                    const bool aW = axis == 0, aA = axis == 1, aB = axis == 2;
+                    ncw = aW ? cw + dW : cw;
+                    nrowW = aW ? rowW + dRowW : rowW;
+                    {
+                        int u = ca + dA;
+                        u = u == wrapA ? resetA : u;
+                        nca = aA ? u : ca;
+                    }
 #pragma unroll
-                for (int k = 0; k < C; ++k) vnext[k] = load_field<MODE>(P, fbase, lrowW + nrowB[k] + nca);
-                // attenuation and collected intensity of this segment; a cell
-                // already dumped (tau 0) adds exactly nothing.  Per cell:
-                // alpha = -expm1(-k ds), ta = tau alpha, D += ta g,
-                // tau -= ta, with g = Ii - Ib_j: D is the net exchange in
-                // intensity units and the ray's contribution wk D (the
-                // reference normalises g by Ii and multiplies the ray by Ii
-                // again; without the two the march saves a multiply per
-                // cell-step and a division per ray, and a cell whose Ii
-                // underflows keeps its absorption).  The two cells of a
-                // pair go through paired FP32 instructions with every sign
-                // moved onto an operand whose negation is exact: e =
-                // expm1(k * (t - tn)) = -alpha, nta = tau e = -ta,
-                // D += nta (-g), tau += nta -- the same roundings.
-                bool dumped[C];  // after this step: tau 0 (dumped now or before)
+                    for (int k = 0; k < C; ++k) {
+                        int u = rowB[k] + dRowB;
+                        u = u == wrapRowB ? resetRowB : u;
+                        nrowB[k] = aB ? u : rowB[k];
+                    }
+                    const bool wall = aW && ncw == wallW;
+                    // fetched for every cell, live or not (a dumped cell's value
+                    // is never used): no default copy, no per-cell predicate; at
+                    // a wall the row stays inside the grid and the walk ends
+                    const int lrowW = wall ? rowW : nrowW;
+                    VT vnext[C];
 #pragma unroll
-                for (int k = 0; k < C; k += 2) {
-                    float kj[2], ngj[2];
+                    for (int k = 0; k < C; ++k) vnext[k] = load_field<MODE>(P, fbase, lrowW + nrowB[k] + nca);
+                    // attenuation and collected intensity of this segment; a cell
+                    // already dumped (tau 0) adds exactly nothing.  Per cell:
+                    // alpha = -expm1(-k ds), ta = tau alpha, D += ta g,
+                    // tau -= ta, with g = Ii - Ib_j: D is the net exchange in
+                    // intensity units and the ray's contribution wk D (the
+                    // reference normalises g by Ii and multiplies the ray by Ii
+                    // again; without the two the march saves a multiply per
+                    // cell-step and a division per ray, and a cell whose Ii
+                    // underflows keeps its absorption).  The two cells of a
+                    // pair go through paired FP32 instructions with every sign
+                    // moved onto an operand whose negation is exact: e =
+                    // expm1(k * (t - tn)) = -alpha, nta = tau e = -ta,
+                    // D += nta (-g), tau += nta -- the same roundings.
+                    bool dumped[C];  // after this step: tau 0 (dumped now or before)
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        if constexpr (MODE == MODE_GREY) {
-                            const float t2 = vcur[k + h] * vcur[k + h];
-                            ngj[h] = t2 * t2 - Ii[k + h];
-                            kj[h] = P.kappa;
-                        } else {
-                            int kx, tj;
-                            float ftj, fxj;
-                            cell_coords<MODE>(vcur[k + h], &kx, &tj, &ftj, &fxj);
-                            kj[h] = lookup_k<MODE>(slk, kx, ftj, fxj);
-                            const float Ibj = lookup_ib(sli, tj, ftj);
-                            ngj[h] = Ibj - Ii[k + h];
+                    for (int k = 0; k < C; k += 2) {
+                        float kj[2], ngj[2];
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            if constexpr (MODE == MODE_GREY) {
+                                const float t2 = vcur[k + h] * vcur[k + h];
+                                ngj[h] = t2 * t2 - Ii[k + h];
+                                kj[h] = P.kappa;
+                            } else {
+                                int kx, tj;
+                                float ftj, fxj;
+                                cell_coords<MODE>(vcur[k + h], &kx, &tj, &ftj, &fxj);
+                                kj[h] = lookup_k<MODE>(slk, kx, ftj, fxj);
+                                const float Ibj = lookup_ib(sli, tj, ftj);
+                                ngj[h] = Ibj - Ii[k + h];
+                            }
+                        }
+                        const float2 e = mc_expm1_x2(__fmul2_rn(make_float2(kj[0], kj[1]), make_float2(nds, nds)));
+                        const float2 nta = __fmul2_rn(make_float2(tau[k], tau[k + 1]), e);
+                        const float2 d2 = __ffma2_rn(nta, make_float2(ngj[0], ngj[1]), make_float2(D[k], D[k + 1]));
+                        const float2 t2 = __fadd2_rn(make_float2(tau[k], tau[k + 1]), nta);
+                        D[k] = d2.x; D[k + 1] = d2.y;
+                        tau[k] = t2.x; tau[k + 1] = t2.y;
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            dumped[k + h] = tau[k + h] < P.toll;
+                            if (dumped[k + h]) {
+                                D[k + h] = fmaf(-tau[k + h], ngj[h], D[k + h]);
+                                tau[k + h] = 0.0f;
+                                life[k + h] = min(life[k + h], steps);
+                            }
                         }
                     }
-                    const float2 e = mc_expm1_x2(__fmul2_rn(make_float2(kj[0], kj[1]), make_float2(nds, nds)));
-                    const float2 nta = __fmul2_rn(make_float2(tau[k], tau[k + 1]), e);
-                    const float2 d2 = __ffma2_rn(nta, make_float2(ngj[0], ngj[1]), make_float2(D[k], D[k + 1]));
-                    const float2 t2 = __fadd2_rn(make_float2(tau[k], tau[k + 1]), nta);
-                    D[k] = d2.x; D[k + 1] = d2.y;
-                    tau[k] = t2.x; tau[k + 1] = t2.y;
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        dumped[k + h] = tau[k + h] < P.toll;
-                        if (dumped[k + h]) {
-                            D[k + h] = fmaf(-tau[k + h], ngj[h], D[k + h]);
-                            tau[k + h] = 0.0f;
-                            life[k + h] = min(life[k + h], steps);
-                        }
+                    if (TRACE && lane == 0 && steps < P.trace_max) {
+                        int *rec = P.trace_rec + 6 * steps;
+                        rec[0] = cw; rec[1] = dA * (int)(hA - 0.5f); rec[2] = dB * (int)(hB - 0.5f); rec[3] = axis;
+                        rec[4] = __float_as_int(ds); rec[5] = __float_as_int(tau[0]);
                     }
-                }
-                if (TRACE && lane == 0 && steps < P.trace_max) {
-                    int *rec = P.trace_rec + 6 * steps;
-                    rec[0] = cw; rec[1] = dA * (int)(hA - 0.5f); rec[2] = dB * (int)(hB - 0.5f); rec[3] = axis;
-                    rec[4] = __float_as_int(ds); rec[5] = __float_as_int(tau[0]);
-                }
-                t = tn;
-                ++steps;
-                {
-                    if (wall) {
-                        const int side = ncw < 0 ? 0 : 1;
-                        const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
+                    t = tn;
+                    ++steps;
+                    {
+                        if (wall) {
+                            const int side = ncw < 0 ? 0 : 1;
+                            const float Iw = (MODE == MODE_GREY) ? P.Tw4[side] : __ldg(P.ibw + side * P.nbands + nbnd);
 #pragma unroll
-                        for (int k = 0; k < C; ++k) {
-                            D[k] = fmaf(tau[k], Ii[k] - Iw, D[k]);
-                            tau[k] = 0.0f;
+                            for (int k = 0; k < C; ++k) {
+                                D[k] = fmaf(tau[k], Ii[k] - Iw, D[k]);
+                                tau[k] = 0.0f;
+                            }
+                            goto walk_end;
                         }
-                        break;
+                        cw = ncw;
+                        rowW = nrowW;
+                        if (aW) tW = (__ldg(fwn + cw) - oW) * sinvW;
+                        hA = aA ? hA + 1.0f : hA;
+                        tA = hA * dtA;
+                        ca = nca;
+                        hB = aB ? hB + 1.0f : hB;
+                        tB = hB * dtB;
+#pragma unroll
+                        for (int k = 0; k < C; ++k) rowB[k] = nrowB[k];
                     }
-                    cw = ncw;
-                    rowW = nrowW;
-                    if (aW) tW = (__ldg(fwn + cw) - oW) * sinvW;
-                    hA = aA ? hA + 1.0f : hA;
-                    tA = hA * dtA;
-                    ca = nca;
-                    hB = aB ? hB + 1.0f : hB;
-                    tB = hB * dtB;
 #pragma unroll
-                    for (int k = 0; k < C; ++k) rowB[k] = nrowB[k];
+                    for (int k = 0; k < C; ++k) vcur[k] = vnext[k];
+                    // a cell not dumped has tau >= toll > 0
+                    bool alive = false;
+#pragma unroll
+                    for (int k = 0; k < C; ++k) alive = alive || !dumped[k];
+                    if (steps >= P.max_steps) {
+                        if (alive) flags |= DNSMC_STATUS_STEP_CAP;
+                        goto walk_end;
+                    }
+                    if (u == 1 && !__any_sync(FULL, alive)) goto walk_end;
                 }
+            }
+        walk_end:
+            {
+                // the exit vote comes every second step, so a walk may take
+                // one step past the one that dumped the warp's last live
+                // cell; that step changes nothing (every tau is 0 and the
+                // cells stay in the grid), and the walk's length is the last
+                // dump step plus one (never dumped: 2^30, no change)
+                int last = 0;
 #pragma unroll
-                for (int k = 0; k < C; ++k) vcur[k] = vnext[k];
-                // a cell not dumped has tau >= toll > 0
-                bool alive = false;
-#pragma unroll
-                for (int k = 0; k < C; ++k) alive = alive || !dumped[k];
-                if (!__any_sync(FULL, alive)) break;
-                if (steps >= P.max_steps) {
-                    if (alive) flags |= DNSMC_STATUS_STEP_CAP;
-                    break;
-                }
+                for (int k = 0; k < C; ++k) last = max(last, life[k]);
+                last = __reduce_max_sync(FULL, last);
+                steps = min(steps, last + 1);
             }
             if (TRACE && lane == 0) *P.trace_n = steps;
 #pragma unroll
