@@ -642,8 +642,12 @@ def batched_block(args, flushbuf_mb=256):
     def make(bt, ta, ng):
         return cvtrain.ck_solver(table, n, Tw, seed=77, groups=ng, threads=bt, tile_a=ta, cv=True)
 
-    tune = autotune.autotune(make, lambda sv: sv.set_fields(T, x), f"ck {nsnap}x{n}^3 cv", nbands=64, rays=8,
-                             log=log)
+    # piloted at the ray floor: RQMC errors fall faster than 1/sqrt(rays), so
+    # a pilot far below the target's ray count misjudges it, and at the floor
+    # a decomposition whose packets would all sit there is measured as such
+    tune = autotune.autotune(make, lambda sv: sv.set_fields(T, x), f"ck {nsnap}x{n}^3 cv", nbands=64,
+                             rays=args.ray_floor, repeats=1, log=log, target_error=TARGET_ERR,
+                             floor=args.ray_floor, error_fn=rms_error)
     cfg = tune["config"]
     s = make(cfg["block_threads"], cfg["tile_a"], cfg["n_groups"])
     s.set_graph(True)

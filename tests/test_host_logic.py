@@ -123,6 +123,39 @@ class FakeSolver:
         pass
 
 
+class FakeStratSolver(FakeSolver):
+    """More band groups: time ~ groups, RMS error ~ groups^-0.6 (the
+    stratification gains a little)."""
+
+    def solve(self, timeout_s=0):
+        bt, ta, ng = self.k
+        self.ms = 100.0 * ng / 8
+        return np.ones(10), np.full(10, ng ** -0.6)
+
+
+def test_autotuner_at_target_sees_the_ray_floor(tmp_path):
+    space = {"block_threads": (256,), "tile_a": (16,), "group_bands": (4, 8)}  # 8 or 4 groups of 32 bands
+    err = lambda Q, S: float(np.sqrt((S ** 2).mean() / (Q ** 2).mean()))
+    # plain efficiency: 8 groups (variance x time ~ groups^-0.2)
+    r = autotune.autotune(lambda bt, ta, ng: FakeStratSolver(bt, ta, ng, []), lambda s: None, "fake", nbands=32,
+                          rays=8, space=space, path=str(tmp_path / "a.json"))
+    assert r["config"]["n_groups"] == 8
+    # at an error of 0.25 with a floor of 20 rays: 8 groups would need 10.5
+    # rays (raised to 20, predicted 250 ms), 4 groups 24.2 (151 ms)
+    r = autotune.autotune(lambda bt, ta, ng: FakeStratSolver(bt, ta, ng, []), lambda s: None, "fake", nbands=32,
+                          rays=8, space=space, path=str(tmp_path / "b.json"), target_error=0.25, floor=20,
+                          error_fn=err)
+    assert r["config"]["n_groups"] == 4
+    by = {x["n_groups"]: x for x in r["results"]}
+    assert by[8]["rays_at_target"] == 20.0 and abs(by[8]["ms_at_target"] - 250.0) < 1e-9
+    assert abs(by[4]["rays_at_target"] - 8 * (4 ** -0.6 / 0.25) ** 2) < 1e-9
+    # without the floor binding, the same ranking as the plain efficiency
+    r = autotune.autotune(lambda bt, ta, ng: FakeStratSolver(bt, ta, ng, []), lambda s: None, "fake", nbands=32,
+                          rays=8, space=space, path=str(tmp_path / "c.json"), target_error=0.25, floor=1,
+                          error_fn=err)
+    assert r["config"]["n_groups"] == 8
+
+
 def test_autotuner_picks_the_most_efficient_and_caches(tmp_path):
     log = []
     space = {"block_threads": (128, 256), "tile_a": (8, 16), "group_bands": (4, 8)}
